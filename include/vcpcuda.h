@@ -1,0 +1,119 @@
+/*
+ * vcpcuda.h -- C ABI of the GB300 (sm_103a) verified dense matrix product.
+ *
+ * Every function returns an int status (VCPCU_OK == 0).  No C++ exception and
+ * no CUDA/torch type crosses this boundary: pointers are plain `double*`,
+ * streams are passed as `void*` (a cudaStream_t, NULL = legacy default stream).
+ * Matrices are column-major, as in vcp::mats<T> (vcp/mats.hpp:411-417).
+ * Intervals are stored like kv::interval<double>: two doubles {inf, sup}
+ * per entry, 16 bytes, so a std::vector<kv::interval<double>> can be passed
+ * as `const double*` with no repacking.
+ *
+ * The library never touches the caller's host floating-point rounding mode:
+ * every directed rounding happens per instruction on the GPU.
+ *
+ * Two kinds of entry points:
+ *   - "host" entry points keep the reference signatures (vblas rmatmul /
+ *     udmatmul) and take host pointers; they copy to the device, run, copy
+ *     back and synchronise.  They are the drop-in replacement.
+ *   - "_dev" entry points take device pointers and leading dimensions and
+ *     are ordered on the given stream (asynchronous w.r.t. the host).
+ */
+#ifndef VCPCUDA_H
+#define VCPCUDA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define VCPCU_OK               0
+#define VCPCU_ERR_INVALID_ARG  1  /* bad shape, leading dimension, pointer or flag   */
+#define VCPCU_ERR_CUDA         2  /* a CUDA runtime/driver call failed               */
+#define VCPCU_ERR_NONFINITE    3  /* Ozaki form: an input entry is Inf or NaN        */
+#define VCPCU_ERR_RANGE        4  /* Ozaki form: exponent outside the split range    */
+#define VCPCU_ERR_TIMEOUT      5  /* a bounded device-side wait gave up              */
+#define VCPCU_ERR_UNSUPPORTED  6  /* no usable sm_103 device, or option not built    */
+#define VCPCU_ERR_ALLOC        7  /* device or pinned host allocation failed         */
+
+/* rounding_mode values, identical to vblas rmatmul (vblas/rmatmul.hpp:100-102) */
+#define VCPCU_ROUND_UP      1
+#define VCPCU_ROUND_NEAREST 0
+#define VCPCU_ROUND_DOWN   -1
+
+/* interval-product forms */
+#define VCPCU_FORM_PLAIN 0   /* FP64 CUDA cores, __fma_rd/__fma_ru, pidblas order   */
+#define VCPCU_FORM_OZAKI 1   /* error-free bf16 slices on tcgen05 tensor cores       */
+#define VCPCU_FORM_AUTO  2   /* autotuned choice of form and slice count            */
+
+/* ---- diagnostics ----------------------------------------------------------- */
+
+/* Text of the last error raised on the calling host thread ("" if none). */
+const char* vcpcu_last_error_string(void);
+
+/* Library version as an integer (major*10000 + minor*100 + patch). */
+int vcpcu_version(void);
+
+/* Number of kernels this library launched since load (all threads). */
+long long vcpcu_launch_count(void);
+
+/* ---- directed-rounding point GEMM ----------------------------------------- */
+
+/* Replaces vblas rmatmul (vblas/rmatmul.hpp:102):
+ *   void rmatmul(int m, int n, int k, const double* A, const double* B,
+ *                double* C, int rounding_mode);
+ * A is m x n, B is n x k, C is m x k (inner dimension n, the vblas naming).
+ * Every C entry is the sequential FMA chain over the inner index in
+ * ascending order, each FMA rounded in `rounding_mode` (1 up, -1 down,
+ * anything else nearest), starting from +0.0 -- the result definition of
+ * vblas (vblas/README.md, "packing layout").  m <= 0 or k <= 0: no-op;
+ * n <= 0: C is zeroed (vblas/rmatmul_avx512.hpp:482-490).  Host pointers;
+ * synchronous. */
+int vcpcu_rmatmul(int m, int n, int k, const double* A, const double* B,
+                  double* C, int rounding_mode);
+
+/* Replaces vblas udmatmul (vblas/udmatmul.hpp:758): CU = fl_up(A*B) and
+ * CD = fl_down(A*B) in one pass, same shapes and chain definition as
+ * vcpcu_rmatmul.  Host pointers; synchronous. */
+int vcpcu_udmatmul(int m, int n, int k, const double* A, const double* B,
+                   double* CU, double* CD);
+
+/* Device-pointer, stream-ordered forms of the two calls above, with
+ * leading dimensions (lda >= m, ldb >= n, ldc >= m). */
+int vcpcu_rmatmul_dev(int m, int n, int k, const double* A, int lda,
+                      const double* B, int ldb, double* C, int ldc,
+                      int rounding_mode, void* stream);
+int vcpcu_udmatmul_dev(int m, int n, int k, const double* A, int lda,
+                       const double* B, int ldb, double* CU, double* CD,
+                       int ldc, void* stream);
+
+/* ---- interval GEMM (pidblas::mulmm, vcp/pidblas.hpp:239-294) -------------- */
+
+/* C = [A] * [B] for interval matrices in kv layout ({inf,sup} pairs).
+ * BLAS naming: A is m x k (lda >= m, in interval entries), B is k x n,
+ * C is m x n.  The result encloses every exact product of point matrices
+ * taken from [A] and [B].
+ *   form == VCPCU_FORM_PLAIN: bit-identical to pidblas::mulmm over a dgemm
+ *     whose every entry is the ascending sequential FMA chain (vblas
+ *     rmatmul): lC = RD(mA*mB), uC = RU(mA*mB), T = RU((|mA|+rA)*rB) +RU
+ *     RU(rA*|mB|), uC +=RU T, lC -=RD T.  `slices` is ignored.
+ *   form == VCPCU_FORM_OZAKI: midpoint product from `slices` error-free
+ *     bf16 slices per operand (2 <= slices <= 12; 0 = default), radius and
+ *     truncation bounds rounded upward; requires finite inputs.
+ *   form == VCPCU_FORM_AUTO: the autotuner picks the form and slice count.
+ * Device pointers; stream-ordered; scratch comes from the stream-ordered
+ * allocator of the current device. */
+int vcpcu_igemm_dev(int m, int n, int k, const double* A, int lda,
+                    const double* B, int ldb, double* C, int ldc,
+                    int form, int slices, void* stream);
+
+/* Host-pointer, synchronous form of vcpcu_igemm_dev (lda = m, ldb = k,
+ * ldc = m): the drop-in for a std::vector<kv::interval<double>> product. */
+int vcpcu_igemm(int m, int n, int k, const double* A, const double* B,
+                double* C, int form, int slices);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VCPCUDA_H */

@@ -1,0 +1,182 @@
+// kv/interval.hpp -- project-written stand-in for kv::interval<T> (kv library
+// absent here).  Written to kv's public API names only, so that the unmodified
+// VCP headers (vcp/imats.hpp, vcp/pidblas.hpp) compile for the CPU reference
+// build.  Endpoints are rounded outward with <cfenv> (each operation saves and
+// restores the caller's rounding mode).  Semantics follow the published kv
+// documentation: mid() rounds to nearest (halves first on overflow), rad()
+// and midrad() round the radius up so [mid-rad, mid+rad] contains the
+// interval; comparisons are "certainly" relations.  TEST INFRASTRUCTURE ONLY.
+#ifndef INTERVAL_HPP
+#define INTERVAL_HPP
+#include <cfenv>
+#include <cmath>
+#include <algorithm>
+#include <iostream>
+#include <limits>
+#include <stdexcept>
+#include <kv/hwround.hpp>
+
+namespace kv {
+
+namespace shim {
+struct mode_guard {
+  int prev;
+  explicit mode_guard(int m) : prev(std::fegetround()) { std::fesetround(m); }
+  ~mode_guard() { std::fesetround(prev); }
+};
+template <class T> inline T add_dn(T a, T b) { mode_guard g(FE_DOWNWARD); volatile T r = a + b; return r; }
+template <class T> inline T add_up(T a, T b) { mode_guard g(FE_UPWARD); volatile T r = a + b; return r; }
+template <class T> inline T sub_dn(T a, T b) { mode_guard g(FE_DOWNWARD); volatile T r = a - b; return r; }
+template <class T> inline T sub_up(T a, T b) { mode_guard g(FE_UPWARD); volatile T r = a - b; return r; }
+template <class T> inline T mul_dn(T a, T b) { mode_guard g(FE_DOWNWARD); volatile T r = a * b; return r; }
+template <class T> inline T mul_up(T a, T b) { mode_guard g(FE_UPWARD); volatile T r = a * b; return r; }
+template <class T> inline T div_dn(T a, T b) { mode_guard g(FE_DOWNWARD); volatile T r = a / b; return r; }
+template <class T> inline T div_up(T a, T b) { mode_guard g(FE_UPWARD); volatile T r = a / b; return r; }
+template <class T> inline T sqrt_dn(T a) { mode_guard g(FE_DOWNWARD); volatile T r = std::sqrt(a); return r; }
+template <class T> inline T sqrt_up(T a) { mode_guard g(FE_UPWARD); volatile T r = std::sqrt(a); return r; }
+}  // namespace shim
+
+template <class T> class interval {
+  T inf, sup;
+
+ public:
+  typedef T base_type;
+  interval() : inf(0), sup(0) {}
+  template <class C> interval(const C& x) : inf(T(x)), sup(T(x)) {}
+  interval(const interval& x) = default;
+  interval(const T& l, const T& u) : inf(l), sup(u) {}
+  template <class C1, class C2> interval(const C1& l, const C2& u) : inf(T(l)), sup(T(u)) {}
+  interval& operator=(const interval& x) = default;
+  template <class C> interval& operator=(const C& x) { inf = sup = T(x); return *this; }
+
+  T& lower() { return inf; }
+  const T& lower() const { return inf; }
+  T& upper() { return sup; }
+  const T& upper() const { return sup; }
+
+  static interval whole() { T i = std::numeric_limits<T>::infinity(); return interval(-i, i); }
+
+  friend interval operator+(const interval& x, const interval& y) {
+    return interval(shim::add_dn(x.inf, y.inf), shim::add_up(x.sup, y.sup));
+  }
+  friend interval operator-(const interval& x, const interval& y) {
+    return interval(shim::sub_dn(x.inf, y.sup), shim::sub_up(x.sup, y.inf));
+  }
+  friend interval operator-(const interval& x) { return interval(-x.sup, -x.inf); }
+  friend interval operator*(const interval& x, const interval& y) {
+    T a[4] = {shim::mul_dn(x.inf, y.inf), shim::mul_dn(x.inf, y.sup), shim::mul_dn(x.sup, y.inf),
+              shim::mul_dn(x.sup, y.sup)};
+    T b[4] = {shim::mul_up(x.inf, y.inf), shim::mul_up(x.inf, y.sup), shim::mul_up(x.sup, y.inf),
+              shim::mul_up(x.sup, y.sup)};
+    return interval(*std::min_element(a, a + 4), *std::max_element(b, b + 4));
+  }
+  friend interval operator/(const interval& x, const interval& y) {
+    if (y.inf <= 0 && y.sup >= 0) throw std::domain_error("kvshim interval: division by 0");
+    T a[4] = {shim::div_dn(x.inf, y.inf), shim::div_dn(x.inf, y.sup), shim::div_dn(x.sup, y.inf),
+              shim::div_dn(x.sup, y.sup)};
+    T b[4] = {shim::div_up(x.inf, y.inf), shim::div_up(x.inf, y.sup), shim::div_up(x.sup, y.inf),
+              shim::div_up(x.sup, y.sup)};
+    return interval(*std::min_element(a, a + 4), *std::max_element(b, b + 4));
+  }
+  template <class C> friend interval operator+(const interval& x, const C& y) { return x + interval(y); }
+  template <class C> friend interval operator+(const C& x, const interval& y) { return interval(x) + y; }
+  template <class C> friend interval operator-(const interval& x, const C& y) { return x - interval(y); }
+  template <class C> friend interval operator-(const C& x, const interval& y) { return interval(x) - y; }
+  template <class C> friend interval operator*(const interval& x, const C& y) { return x * interval(y); }
+  template <class C> friend interval operator*(const C& x, const interval& y) { return interval(x) * y; }
+  template <class C> friend interval operator/(const interval& x, const C& y) { return x / interval(y); }
+  template <class C> friend interval operator/(const C& x, const interval& y) { return interval(x) / y; }
+  template <class C> interval& operator+=(const C& y) { *this = *this + y; return *this; }
+  template <class C> interval& operator-=(const C& y) { *this = *this - y; return *this; }
+  template <class C> interval& operator*=(const C& y) { *this = *this * y; return *this; }
+  template <class C> interval& operator/=(const C& y) { *this = *this / y; return *this; }
+
+  // "certainly" comparisons
+  friend bool operator<(const interval& x, const interval& y) { return x.sup < y.inf; }
+  friend bool operator<=(const interval& x, const interval& y) { return x.sup <= y.inf; }
+  friend bool operator>(const interval& x, const interval& y) { return x.inf > y.sup; }
+  friend bool operator>=(const interval& x, const interval& y) { return x.inf >= y.sup; }
+  friend bool operator==(const interval& x, const interval& y) { return x.inf == y.inf && x.sup == y.sup; }
+  friend bool operator!=(const interval& x, const interval& y) { return !(x == y); }
+  template <class C> friend bool operator<(const interval& x, const C& y) { return x < interval(y); }
+  template <class C> friend bool operator<(const C& x, const interval& y) { return interval(x) < y; }
+  template <class C> friend bool operator>(const interval& x, const C& y) { return x > interval(y); }
+  template <class C> friend bool operator>(const C& x, const interval& y) { return interval(x) > y; }
+  template <class C> friend bool operator<=(const interval& x, const C& y) { return x <= interval(y); }
+  template <class C> friend bool operator<=(const C& x, const interval& y) { return interval(x) <= y; }
+  template <class C> friend bool operator>=(const interval& x, const C& y) { return x >= interval(y); }
+  template <class C> friend bool operator>=(const C& x, const interval& y) { return interval(x) >= y; }
+  template <class C> friend bool operator==(const interval& x, const C& y) { return x == interval(y); }
+  template <class C> friend bool operator!=(const interval& x, const C& y) { return x != interval(y); }
+
+  friend T mid(const interval& x) {
+    shim::mode_guard g(FE_TONEAREST);
+    volatile T s = x.inf + x.sup;
+    if (std::isfinite((T)s)) return (T)s * T(0.5);
+    volatile T h = x.inf * T(0.5);
+    return h + x.sup * T(0.5);
+  }
+  friend T rad(const interval& x) {
+    T m = mid(x);
+    return std::max(shim::sub_up(m, x.inf), shim::sub_up(x.sup, m));
+  }
+  friend void midrad(const interval& x, T& m, T& r) {
+    m = mid(x);
+    r = std::max(shim::sub_up(m, x.inf), shim::sub_up(x.sup, m));
+  }
+  friend T width(const interval& x) { return shim::sub_up(x.sup, x.inf); }
+  friend T norm(const interval& x) { return std::max(std::fabs(x.inf), std::fabs(x.sup)); }
+  friend T mag(const interval& x) { return std::max(std::fabs(x.inf), std::fabs(x.sup)); }
+  friend T mig(const interval& x) {
+    if (x.inf <= 0 && x.sup >= 0) return T(0);
+    return std::min(std::fabs(x.inf), std::fabs(x.sup));
+  }
+  friend interval abs(const interval& x) {
+    if (x.inf >= 0) return x;
+    if (x.sup <= 0) return -x;
+    return interval(T(0), std::max(-x.inf, x.sup));
+  }
+  friend interval sqrt(const interval& x) {
+    return interval(shim::sqrt_dn(std::max(x.inf, T(0))), shim::sqrt_up(x.sup));
+  }
+  friend interval pow(const interval& x, int n) {
+    if (n == 0) return interval(T(1));
+    if (n < 0) return interval(T(1)) / pow(x, -n);
+    interval r = (n % 2 == 0) ? abs(x) : x;
+    interval base = r;
+    for (int i = 1; i < n; ++i) r = r * base;
+    return r;
+  }
+  friend interval pow(const interval& x, const interval& y) {
+    if (y.inf == y.sup && y.inf == std::floor(y.inf)) return pow(x, (int)y.inf);
+    throw std::domain_error("kvshim interval: non-integer power");
+  }
+  template <class C> friend interval pow(const interval& x, const C& y) { return pow(x, interval(y)); }
+  friend bool in(const T& a, const interval& x) { return x.inf <= a && a <= x.sup; }
+  friend bool zero_in(const interval& x) { return x.inf <= 0 && x.sup >= 0; }
+  friend bool subset(const interval& x, const interval& y) { return y.inf <= x.inf && x.sup <= y.sup; }
+  friend bool proper_subset(const interval& x, const interval& y) { return y.inf < x.inf && x.sup < y.sup; }
+  friend bool overlap(const interval& x, const interval& y) { return x.inf <= y.sup && y.inf <= x.sup; }
+  friend interval intersect(const interval& x, const interval& y) {
+    return interval(std::max(x.inf, y.inf), std::min(x.sup, y.sup));
+  }
+  friend interval hull(const interval& x, const interval& y) {
+    return interval(std::min(x.inf, y.inf), std::max(x.sup, y.sup));
+  }
+  friend interval max(const interval& x, const interval& y) {
+    return interval(std::max(x.inf, y.inf), std::max(x.sup, y.sup));
+  }
+  friend interval min(const interval& x, const interval& y) {
+    return interval(std::min(x.inf, y.inf), std::min(x.sup, y.sup));
+  }
+  friend std::ostream& operator<<(std::ostream& s, const interval& x) {
+    return s << "[" << x.inf << "," << x.sup << "]";
+  }
+};
+
+}  // namespace kv
+
+namespace std {
+template <class T> class numeric_limits<kv::interval<T> > : public numeric_limits<T> {};
+}
+#endif

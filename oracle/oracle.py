@@ -1,0 +1,122 @@
+"""ctypes front end of the CPU oracle (liboracle.so) and of the reference
+build (oracle/_ref/libvcpref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline legs of bench.py, as the checker or the timed CPU baseline.  The
+product (vcp_gb300, libvcpcuda.so) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .build import LIB, REF_LIB, build_oracle
+
+_i, _l, _v = C.c_int, C.c_long, C.c_void_p
+_lib = None
+_ref = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build_oracle()
+        L = C.CDLL(str(LIB))
+        L.orc_rmatmul.argtypes = [_i, _i, _i, _v, _v, _v, _i, _i]
+        L.orc_rmatmul_ld.argtypes = [_i, _i, _i, _v, _l, _v, _l, _v, _l, _i, _i]
+        L.orc_udmatmul.argtypes = [_i, _i, _i, _v, _v, _v, _v, _i]
+        L.orc_midrad.argtypes = [_l, _v, _v, _v]
+        L.orc_pidblas_mulmm.argtypes = [_i, _i, _i, _v, _v, _v, _i]
+        L.orc_exact_hull.argtypes = [_i, _i, _i, _v, _v, _l, _v, _v, _v, _v, _i]
+        L.orc_exact_dot.argtypes = [_i, _i, _i, _v, _v, _l, _v, _v, _v, _v, _i]
+        L.orc_exact_sum.argtypes = [_l, _v, _i]
+        L.orc_exact_sum.restype = C.c_double
+        _lib = L
+    return _lib
+
+
+def ref_lib() -> C.CDLL | None:
+    """The reference compiled from its own sources, or None where absent."""
+    global _ref
+    if _ref is None and Path(REF_LIB).exists():
+        R = C.CDLL(str(REF_LIB))
+        R.ref_rmatmul.argtypes = [_i, _i, _i, _v, _v, _v, _i]
+        R.ref_pidblas_mulmm.argtypes = [_i, _i, _i, _v, _v, _v]
+        R.ref_pidblas_mulmm.restype = _i
+        _ref = R
+    return _ref
+
+
+def _p(a: np.ndarray) -> int:
+    assert a.dtype == np.float64 or a.dtype == np.int32
+    assert a.flags.c_contiguous or a.flags.f_contiguous
+    return a.ctypes.data
+
+
+def rmatmul(m, n, k, A, B, rnd, threads=0) -> np.ndarray:
+    """vblas naming (A m x n, B n x k); returns C (flat, column-major)."""
+    C_ = np.zeros(max(m * k, 1), dtype=np.float64)
+    lib().orc_rmatmul(m, n, k, _p(A), _p(B), _p(C_), int(rnd), int(threads))
+    return C_
+
+
+def pidblas_mulmm(m, n, k, A, B, threads=0) -> np.ndarray:
+    """GEMM naming, kv-layout buffers; returns C's kv buffer."""
+    C_ = np.zeros(2 * m * n, dtype=np.float64)
+    st = lib().orc_pidblas_mulmm(m, n, k, _p(A), _p(B), _p(C_), int(threads))
+    assert st == 0
+    return C_
+
+
+def midrad(X: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    cnt = X.size // 2
+    m = np.empty(cnt)
+    r = np.empty(cnt)
+    lib().orc_midrad(cnt, _p(X), _p(m), _p(r))
+    return m, r
+
+
+def exact_hull(m, n, k, A, B, rows, cols, threads=0):
+    rows = np.ascontiguousarray(rows, dtype=np.int32)
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    lo = np.empty(rows.size)
+    up = np.empty(rows.size)
+    lib().orc_exact_hull(m, n, k, _p(A), _p(B), rows.size, _p(rows), _p(cols), _p(lo), _p(up),
+                         int(threads))
+    return lo, up
+
+
+def exact_dot(m, n, k, A, B, rows, cols, threads=0):
+    rows = np.ascontiguousarray(rows, dtype=np.int32)
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    dn = np.empty(rows.size)
+    up = np.empty(rows.size)
+    lib().orc_exact_dot(m, n, k, _p(A), _p(B), rows.size, _p(rows), _p(cols), _p(dn), _p(up),
+                        int(threads))
+    return dn, up
+
+
+def exact_sum(x: np.ndarray, direction: int) -> float:
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    return float(lib().orc_exact_sum(x.size, _p(x), int(direction)))
+
+
+def ref_rmatmul(m, n, k, A, B, rnd) -> np.ndarray | None:
+    R = ref_lib()
+    if R is None:
+        return None
+    C_ = np.zeros(max(m * k, 1), dtype=np.float64)
+    R.ref_rmatmul(m, n, k, _p(A), _p(B), _p(C_), int(rnd))
+    return C_
+
+
+def ref_pidblas_mulmm(m, n, k, A, B) -> np.ndarray | None:
+    R = ref_lib()
+    if R is None:
+        return None
+    C_ = np.zeros(2 * m * n, dtype=np.float64)
+    st = R.ref_pidblas_mulmm(m, n, k, _p(A), _p(B), _p(C_))
+    assert st == 0
+    return C_

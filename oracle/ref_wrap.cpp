@@ -1,0 +1,120 @@
+// ref_wrap.cpp -- recipe that compiles the reference's own CPU path into
+// oracle/_ref/libvcpref.so (see oracle/build.py).  TEST INFRASTRUCTURE ONLY.
+//
+// Included unmodified from the reference tree (-I<reference> -I<reference>/vblas):
+//   vblas/rmatmul.hpp   -- the vblas directed-rounding GEMM (backend chosen by
+//                          the compiler flags: AVX2+FMA on x86_64, NEON on Arm)
+//   vcp/pidblas.hpp     -- the pidblas interval policy (with vcp/pdblas.hpp,
+//                          vcp/imats.hpp, vcp/matrix.hpp)
+// kv (interval, hwround) is absent and comes from oracle/kvshim.  pdblas calls
+// the Fortran BLAS symbol dgemm_; this file provides dgemm_ (and ddot_,
+// dgemv_, dsyrk_) on top of the reference rmatmul with the direction taken
+// from the calling thread's current rounding mode, which is what pidblas sets
+// through kv::hwround before each call (vcp/pidblas.hpp:264-281).
+#include <cfenv>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "rmatmul.hpp"
+
+#include <kv/interval.hpp>
+#include <kv/hwround.hpp>
+#include <vcp/pidblas.hpp>
+#include <vcp/matrix.hpp>
+
+namespace {
+int current_direction() {
+  switch (std::fegetround()) {
+    case FE_UPWARD: return 1;
+    case FE_DOWNWARD: return -1;
+    default: return 0;
+  }
+}
+[[noreturn]] void unsupported(const char* what) {
+  std::fprintf(stderr, "ref_wrap: unsupported BLAS call pattern: %s\n", what);
+  std::abort();
+}
+}  // namespace
+
+extern "C" {
+
+// C = A * B for the pattern pdblas::mulmm uses (vcp/pdblas.hpp:91-110):
+// trans "N","N", alpha 1, beta 0, lda = m, ldb = k, ldc = m.
+void dgemm_(char* ta, char* tb, int* m, int* n, int* k, double* alpha, const double* A, int* lda,
+            const double* B, int* ldb, double* beta, double* C, int* ldc) {
+  if (ta[0] != 'N' || tb[0] != 'N' || *alpha != 1.0 || *beta != 0.0 || *lda != *m ||
+      *ldb != *k || *ldc != *m)
+    unsupported("dgemm_");
+  rmatmul(*m, *k, *n, A, B, C, current_direction());
+}
+
+double ddot_(int* n, const double* x, int* incx, const double* y, int* incy) {
+  if (*incx != 1 || *incy != 1) unsupported("ddot_");
+  double c = 0.0;
+  rmatmul(1, *n, 1, x, y, &c, current_direction());
+  return c;
+}
+
+void dgemv_(char* t, int* m, int* n, double* alpha, const double* A, int* lda, const double* x,
+            int* incx, double* beta, double* y, int* incy) {
+  if (t[0] != 'N' || *alpha != 1.0 || *beta != 0.0 || *lda != *m || *incx != 1 || *incy != 1)
+    unsupported("dgemv_");
+  rmatmul(*m, *n, 1, A, x, y, current_direction());
+}
+
+// Upper triangle of A^T A (vcp/pdblas.hpp:138-146: uplo "U", trans "T").
+void dsyrk_(char* uplo, char* trans, int* n, int* k, double* alpha, const double* A, int* lda,
+            double* beta, double* C, int* ldc) {
+  if (uplo[0] != 'U' || trans[0] != 'T' || *alpha != 1.0 || *beta != 0.0 || *lda != *k)
+    unsupported("dsyrk_");
+  std::vector<double> At((size_t)(*k) * (*n));
+  for (int j = 0; j < *n; ++j)
+    for (int p = 0; p < *k; ++p) At[j + (size_t)p * (*n)] = A[p + (size_t)j * (*lda)];
+  std::vector<double> full((size_t)(*n) * (*n));
+  rmatmul(*n, *k, *n, At.data(), A, full.data(), current_direction());
+  for (int j = 0; j < *n; ++j)
+    for (int i = 0; i <= j; ++i) C[i + (size_t)j * (*ldc)] = full[i + (size_t)j * (*n)];
+}
+
+// LAPACK and the remaining BLAS routines are referenced by pdblas's solver
+// members (vcp/pdblas.hpp:159-376), which are off the GEMM path: they abort.
+void dsymm_(char*, char*, int*, int*, double*, const double*, int*, const double*, int*, double*,
+            double*, int*) { unsupported("dsymm_"); }
+void dgetrf_(int*, int*, double*, int*, int*, int*) { unsupported("dgetrf_"); }
+void dgetri_(int*, double*, int*, int*, double*, int*, int*) { unsupported("dgetri_"); }
+void dsyev_(char*, char*, int*, double*, int*, double*, double*, int*, int*) { unsupported("dsyev_"); }
+void dgesv_(int*, int*, double*, int*, int*, double*, int*, int*) { unsupported("dgesv_"); }
+void dsygv_(int*, char*, char*, int*, double*, int*, double*, int*, double*, double*, int*, int*) {
+  unsupported("dsygv_");
+}
+void dpotrf_(char*, int*, double*, int*, int*) { unsupported("dpotrf_"); }
+
+// The reference vblas entry point, unchanged.
+void ref_rmatmul(int m, int n, int k, const double* A, const double* B, double* C, int rnd) {
+  rmatmul(m, n, k, A, B, C, rnd);
+}
+
+// C = A * B through vcp::matrix<kv::interval<double>, vcp::pidblas>
+// (operator* -> pidblas::mulmm, vcp/matrix.hpp:245-266).  GEMM naming:
+// A m x k, B k x n, all in kv layout.
+int ref_pidblas_mulmm(int m, int n, int k, const double* A, const double* B, double* C) {
+  try {
+    typedef kv::interval<double> I;
+    vcp::matrix<I, vcp::pidblas> a, b, c;
+    a.zeros(m, k);
+    b.zeros(k, n);
+    for (long i = 0; i < (long)m * k; ++i) a.data()[i] = I(A[2 * i], A[2 * i + 1]);
+    for (long i = 0; i < (long)k * n; ++i) b.data()[i] = I(B[2 * i], B[2 * i + 1]);
+    c = a * b;
+    for (long i = 0; i < (long)m * n; ++i) {
+      C[2 * i] = c.data()[i].lower();
+      C[2 * i + 1] = c.data()[i].upper();
+    }
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,449 @@
+/*
+ * vcp_oracle.c -- CPU oracle for the verified GEMM hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference legs of bench.py may load this code, and only as
+ * the checker or the timed CPU baseline; the GPU product never calls it.
+ *
+ * Contents (each restating the reference's own definition):
+ *   orc_rmatmul / orc_udmatmul
+ *       vblas rmatmul / udmatmul (vblas/rmatmul.hpp:102, vblas/udmatmul.hpp:758):
+ *       every C entry is the ascending sequential FMA chain over the inner
+ *       index, rounded in the requested direction, starting from +0.0
+ *       (vblas/README.md "packing layout"; micro-kernel
+ *       vblas/rmatmul_avx512.hpp:195-242 continues the chain through C).
+ *       m <= 0 or k <= 0: no-op; n <= 0: C zeroed (rmatmul_avx512.hpp:482-490).
+ *       Portable C with per-thread fesetround + fma(), OpenMP over column
+ *       blocks, the same scheme as the NEON / no-SIMD backends
+ *       (vblas/rmatmul_neon.hpp, vblas/rmatmul_nosimd.hpp).
+ *   orc_midrad
+ *       kv-style midpoint/radius used by pidblas_assist::midrad
+ *       (vcp/pidblas.hpp:43-51): m = RN((lo+up)/2) (halves first if lo+up
+ *       overflows), r = max(RU(m-lo), RU(up-m)).
+ *   orc_pidblas_mulmm
+ *       pidblas::mulmm (vcp/pidblas.hpp:239-294) with orc_rmatmul as its
+ *       dgemm_, in the reference's exact operation order.
+ *   orc_exact_hull / orc_exact_dot
+ *       exact long-accumulator dot products (a Kulisch-style fixed-point
+ *       accumulator over the whole binary64 product range) rounded down/up
+ *       to double: the containment oracle.
+ *
+ * Build: gcc -O3 -fopenmp -frounding-math -ffp-contract=off (see build.py).
+ */
+#include <fenv.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#pragma STDC FENV_ACCESS ON
+
+static int fe_mode(int rnd) {
+  if (rnd == 1) return FE_UPWARD;
+  if (rnd == -1) return FE_DOWNWARD;
+  return FE_TONEAREST;
+}
+
+/* ---------------------------------------------------------------------------
+ * Directed-rounding GEMM (vblas naming: A m x n, B n x k, C m x k).
+ * Blocking: column blocks of NR=4 C columns are distributed over threads;
+ * inside, row blocks of MR=16 and inner blocks of KC keep the A panel hot.
+ * The chain of each C entry runs over the inner index in ascending order,
+ * continuing through C between inner blocks, so blocking never changes it.
+ * ------------------------------------------------------------------------- */
+#define ORC_MR 16
+#define ORC_NR 4
+#define ORC_KC 256
+#define ORC_MC 512
+
+static void micro_chain(int mr, int nr, int kc, const double* A, long lda, const double* B,
+                        long ldb, double* C, long ldc, int first) {
+  double acc[ORC_NR][ORC_MR];
+  for (int j = 0; j < ORC_NR; ++j)
+    for (int i = 0; i < ORC_MR; ++i)
+      acc[j][i] = (first || j >= nr || i >= mr) ? 0.0 : C[i + j * ldc];
+  if (mr == ORC_MR && nr == ORC_NR) {
+    for (int p = 0; p < kc; ++p) {
+      const double* ap = A + p * lda;
+      const double b0 = B[p], b1 = B[p + ldb], b2 = B[p + 2 * ldb], b3 = B[p + 3 * ldb];
+      for (int i = 0; i < ORC_MR; ++i) acc[0][i] = fma(ap[i], b0, acc[0][i]);
+      for (int i = 0; i < ORC_MR; ++i) acc[1][i] = fma(ap[i], b1, acc[1][i]);
+      for (int i = 0; i < ORC_MR; ++i) acc[2][i] = fma(ap[i], b2, acc[2][i]);
+      for (int i = 0; i < ORC_MR; ++i) acc[3][i] = fma(ap[i], b3, acc[3][i]);
+    }
+  } else {
+    for (int p = 0; p < kc; ++p)
+      for (int j = 0; j < nr; ++j) {
+        const double b = B[p + j * ldb];
+        for (int i = 0; i < mr; ++i) acc[j][i] = fma(A[i + p * lda], b, acc[j][i]);
+      }
+  }
+  for (int j = 0; j < nr; ++j)
+    for (int i = 0; i < mr; ++i) C[i + j * ldc] = acc[j][i];
+}
+
+void orc_rmatmul_ld(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
+                    double* C, long ldc, int rnd, int nthreads) {
+  if (m <= 0 || k <= 0) return;
+  if (n <= 0) {
+    for (long j = 0; j < k; ++j)
+      for (long i = 0; i < m; ++i) C[i + j * ldc] = 0.0;
+    return;
+  }
+  const int mode = fe_mode(rnd);
+  const int ncb = (k + ORC_NR - 1) / ORC_NR;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+#endif
+  {
+    const int prev = fegetround();
+    fesetround(mode);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (int cb = 0; cb < ncb; ++cb) {
+      const int j0 = cb * ORC_NR, nr = (k - j0 < ORC_NR) ? k - j0 : ORC_NR;
+      for (int p0 = 0; p0 < n; p0 += ORC_KC) {
+        const int kc = (n - p0 < ORC_KC) ? n - p0 : ORC_KC;
+        for (int i0 = 0; i0 < m; i0 += ORC_MR) {
+          const int mr = (m - i0 < ORC_MR) ? m - i0 : ORC_MR;
+          micro_chain(mr, nr, kc, A + i0 + (long)p0 * lda, lda, B + p0 + (long)j0 * ldb, ldb,
+                      C + i0 + (long)j0 * ldc, ldc, p0 == 0);
+        }
+      }
+    }
+    fesetround(prev);
+  }
+}
+
+void orc_rmatmul(int m, int n, int k, const double* A, const double* B, double* C, int rnd,
+                 int nthreads) {
+  orc_rmatmul_ld(m, n, k, A, m, B, n > 0 ? n : 1, C, m, rnd, nthreads);
+}
+
+void orc_udmatmul(int m, int n, int k, const double* A, const double* B, double* CU, double* CD,
+                  int nthreads) {
+  orc_rmatmul(m, n, k, A, B, CU, 1, nthreads);
+  orc_rmatmul(m, n, k, A, B, CD, -1, nthreads);
+}
+
+/* ---------------------------------------------------------------------------
+ * midrad and the pidblas::mulmm restatement.
+ * ------------------------------------------------------------------------- */
+/* kv layout (pairs {inf,sup}) -> mid / rad planes, count entries.  The
+ * midpoints are formed in one round-to-nearest pass, the radii in one
+ * round-upward pass. */
+void orc_midrad(long count, const double* X, double* mid, double* rad) {
+  const int prev = fegetround();
+  fesetround(FE_TONEAREST);
+  for (long i = 0; i < count; ++i) {
+    const double lo = X[2 * i], up = X[2 * i + 1];
+    double s = lo + up;
+    mid[i] = isfinite(s) ? s * 0.5 : lo * 0.5 + up * 0.5;
+  }
+  fesetround(FE_UPWARD);
+  for (long i = 0; i < count; ++i) {
+    const double lo = X[2 * i], up = X[2 * i + 1];
+    rad[i] = fmax(mid[i] - lo, up - mid[i]);
+  }
+  fesetround(prev);
+}
+
+/* pidblas::mulmm, GEMM naming: C (m x n) = A (m x k) * B (k x n); A, B, C in
+ * kv layout, column-major with ld = rows.  Order (vcp/pidblas.hpp:256-293):
+ *   lC = RD gemm(mA, mB); uC = RU gemm(mA, mB)
+ *   mA = |mA| +RU rA; temp = RU gemm(mA, rB); mA2 = RU gemm(rA, |mB|)
+ *   temp = temp +RU mA2; uC = uC +RU temp; lC = lC -RD temp.           */
+int orc_pidblas_mulmm(int m, int n, int k, const double* A, const double* B, double* C,
+                      int nthreads) {
+  if (m <= 0 || n <= 0) return 0;
+  if (k < 0) k = 0;
+  const long na = (long)m * k, nb = (long)k * n, nc = (long)m * n;
+  double* buf = (double*)malloc(sizeof(double) * (2 * na + 2 * nb + 4 * nc + 1));
+  if (!buf) return 1;
+  double *mA = buf, *rA = mA + na, *mB = rA + na, *rB = mB + nb;
+  double *lC = rB + nb, *uC = lC + nc, *temp = uC + nc, *t2 = temp + nc;
+  const int prev = fegetround();
+  orc_midrad(na, A, mA, rA);
+  orc_midrad(nb, B, mB, rB);
+  orc_rmatmul(m, k, n, mA, mB, lC, -1, nthreads);
+  orc_rmatmul(m, k, n, mA, mB, uC, 1, nthreads);
+  fesetround(FE_UPWARD);
+  for (long i = 0; i < na; ++i) mA[i] = fabs(mA[i]) + rA[i];
+  for (long i = 0; i < nb; ++i) mB[i] = fabs(mB[i]);
+  orc_rmatmul(m, k, n, mA, rB, temp, 1, nthreads);
+  orc_rmatmul(m, k, n, rA, mB, t2, 1, nthreads);
+  fesetround(FE_UPWARD);
+  for (long i = 0; i < nc; ++i) {
+    temp[i] = temp[i] + t2[i];
+    uC[i] = uC[i] + temp[i];
+  }
+  fesetround(FE_DOWNWARD);
+  for (long i = 0; i < nc; ++i) lC[i] = lC[i] - temp[i];
+  fesetround(prev);
+  for (long i = 0; i < nc; ++i) {
+    C[2 * i] = lC[i];
+    C[2 * i + 1] = uC[i];
+  }
+  free(buf);
+  return 0;
+}
+
+/* ---------------------------------------------------------------------------
+ * Exact accumulator.  Two's complement fixed point, ACC_WORDS x 64 bits, bit
+ * 0 has weight 2^-ACC_BIAS.  Every product of two finite doubles (LSB weight
+ * >= 2^-2148, magnitude < 2^2048) and sums of up to 2^60 of them fit.
+ * ------------------------------------------------------------------------- */
+#define ACC_BIAS 2200
+#define ACC_WORDS 70
+typedef struct {
+  uint64_t w[ACC_WORDS];
+  int nonfinite; /* set if an Inf/NaN term was seen */
+} orc_acc;
+
+static void acc_zero(orc_acc* a) { memset(a, 0, sizeof(*a)); }
+
+/* Split finite x != 0 into integer mantissa and LSB exponent: x = sgn*mant*2^e. */
+static void decompose(double x, int* sgn, uint64_t* mant, int* e) {
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  *sgn = (int)(b >> 63);
+  int ex = (int)((b >> 52) & 0x7ff);
+  uint64_t f = b & ((1ULL << 52) - 1);
+  if (ex == 0) {
+    *mant = f;
+    *e = -1074;
+  } else {
+    *mant = f | (1ULL << 52);
+    *e = ex - 1075;
+  }
+}
+
+/* a += (neg ? -1 : 1) * (hi:lo) * 2^pos, pos >= 0 the bit position. */
+static void acc_add_u128(orc_acc* a, unsigned __int128 v, int pos, int neg) {
+  if (v == 0) return;
+  int w = pos >> 6, b = pos & 63;
+  uint64_t parts[3];
+  uint64_t lo = (uint64_t)v, hi = (uint64_t)(v >> 64);
+  if (b == 0) {
+    parts[0] = lo;
+    parts[1] = hi;
+    parts[2] = 0;
+  } else {
+    parts[0] = lo << b;
+    parts[1] = (hi << b) | (lo >> (64 - b));
+    parts[2] = hi >> (64 - b);
+  }
+  if (!neg) {
+    unsigned __int128 carry = 0;
+    int i = 0;
+    for (; i < 3 && w + i < ACC_WORDS; ++i) {
+      unsigned __int128 s = (unsigned __int128)a->w[w + i] + parts[i] + carry;
+      a->w[w + i] = (uint64_t)s;
+      carry = s >> 64;
+    }
+    for (int j = w + i; carry && j < ACC_WORDS; ++j) {
+      unsigned __int128 s = (unsigned __int128)a->w[j] + carry;
+      a->w[j] = (uint64_t)s;
+      carry = s >> 64;
+    }
+  } else {
+    uint64_t borrow = 0;
+    int i = 0;
+    for (; i < 3 && w + i < ACC_WORDS; ++i) {
+      uint64_t x = a->w[w + i];
+      uint64_t d = x - parts[i] - borrow;
+      borrow = (x < parts[i]) || (x - parts[i] < borrow);
+      a->w[w + i] = d;
+    }
+    for (int j = w + i; borrow && j < ACC_WORDS; ++j) {
+      uint64_t x = a->w[j];
+      a->w[j] = x - 1;
+      borrow = (x == 0);
+    }
+  }
+}
+
+/* exact product x*y as (sign, 106-bit magnitude, LSB exponent); 0 if zero */
+typedef struct {
+  int sgn;
+  unsigned __int128 mag;
+  int e;
+} xprod;
+
+static xprod exact_mul(double x, double y) {
+  xprod p = {0, 0, 0};
+  if (x == 0.0 || y == 0.0) return p;
+  int sx, sy, ex, ey;
+  uint64_t mx, my;
+  decompose(x, &sx, &mx, &ex);
+  decompose(y, &sy, &my, &ey);
+  p.sgn = sx ^ sy;
+  p.mag = (unsigned __int128)mx * my;
+  p.e = ex + ey;
+  return p;
+}
+
+static int bitlen128(unsigned __int128 v) {
+  int n = 0;
+  while (v) {
+    v >>= 1;
+    ++n;
+  }
+  return n;
+}
+
+/* compare exact products: -1, 0, 1 */
+static int xcmp(xprod a, xprod b) {
+  int za = a.mag == 0, zb = b.mag == 0;
+  if (za && zb) return 0;
+  if (za) return b.sgn ? 1 : -1;
+  if (zb) return a.sgn ? -1 : 1;
+  if (a.sgn != b.sgn) return a.sgn ? -1 : 1;
+  int la = bitlen128(a.mag), lb = bitlen128(b.mag);
+  int ta = a.e + la, tb = b.e + lb;
+  int c;
+  if (ta != tb)
+    c = ta > tb ? 1 : -1;
+  else {
+    unsigned __int128 xa = a.mag << (128 - la), xb = b.mag << (128 - lb);
+    c = xa > xb ? 1 : (xa < xb ? -1 : 0);
+  }
+  return a.sgn ? -c : c;
+}
+
+static void acc_add_xprod(orc_acc* a, xprod p) {
+  if (p.mag == 0) return;
+  acc_add_u128(a, p.mag, p.e + ACC_BIAS, p.sgn);
+}
+
+/* Round the accumulator to double: dir = -1 (down) or +1 (up). */
+static double acc_round(const orc_acc* a0, int dir) {
+  orc_acc a = *a0;
+  int neg = (int)(a.w[ACC_WORDS - 1] >> 63);
+  if (neg) { /* magnitude = two's complement negation */
+    uint64_t carry = 1;
+    for (int i = 0; i < ACC_WORDS; ++i) {
+      uint64_t x = ~a.w[i] + carry;
+      carry = (carry && x == 0) ? 1 : 0;
+      a.w[i] = x;
+    }
+  }
+  int top = -1;
+  for (int i = ACC_WORDS - 1; i >= 0 && top < 0; --i)
+    if (a.w[i]) top = i * 64 + 63 - __builtin_clzll(a.w[i]);
+  if (top < 0) return 0.0; /* exact zero: +0.0 */
+  const int min_lsb = ACC_BIAS - 1074;
+  int lsb = top - 52;
+  if (lsb < min_lsb) lsb = min_lsb;
+  uint64_t mant = 0;
+  for (int bit = top; bit >= lsb; --bit) mant = (mant << 1) | ((a.w[bit >> 6] >> (bit & 63)) & 1);
+  int sticky = 0;
+  for (int wi = 0; wi < (lsb >> 6) && !sticky; ++wi) sticky = a.w[wi] != 0;
+  if (!sticky && (lsb & 63)) sticky = (a.w[lsb >> 6] & ((1ULL << (lsb & 63)) - 1)) != 0;
+  /* magnitude rounding: away from zero if (up and positive) or (down and negative) */
+  int away = sticky && ((dir > 0 && !neg) || (dir < 0 && neg));
+  if (away) mant += 1;
+  int e = lsb - ACC_BIAS;
+  /* overflow: beyond DBL_MAX */
+  double r;
+  if (e + 64 - __builtin_clzll(mant) > 1024) {
+    int to_inf = (dir > 0 && !neg) || (dir < 0 && neg);
+    r = to_inf ? INFINITY : 1.7976931348623157e308;
+  } else {
+    r = ldexp((double)mant, e); /* exact: mant <= 2^53 */
+  }
+  return neg ? -r : r;
+}
+
+static int nonfinite2(double x, double y) { return !isfinite(x) || !isfinite(y); }
+
+/* Exact hull of sum_p [A(i,p)] * [B(p,j)] for `count` entries (rows[i], cols[i]);
+ * A (m x k), B (k x n) in kv layout with ld = rows.  Outputs RD(lower sum)
+ * and RU(upper sum).  Entries with a non-finite term get NaN. */
+void orc_exact_hull(int m, int n, int k, const double* A, const double* B, long count,
+                    const int* rows, const int* cols, double* out_lo, double* out_up,
+                    int nthreads) {
+  (void)n;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+#endif
+  for (long t = 0; t < count; ++t) {
+    const int i = rows[t], j = cols[t];
+    orc_acc lo, up;
+    acc_zero(&lo);
+    acc_zero(&up);
+    int bad = 0;
+    for (int p = 0; p < k; ++p) {
+      const double* a = A + 2 * ((long)i + (long)p * m);
+      const double* b = B + 2 * ((long)p + (long)j * k);
+      if (nonfinite2(a[0], a[1]) || nonfinite2(b[0], b[1])) {
+        bad = 1;
+        break;
+      }
+      xprod q[4] = {exact_mul(a[0], b[0]), exact_mul(a[0], b[1]), exact_mul(a[1], b[0]),
+                    exact_mul(a[1], b[1])};
+      xprod mn = q[0], mx = q[0];
+      for (int s = 1; s < 4; ++s) {
+        if (xcmp(q[s], mn) < 0) mn = q[s];
+        if (xcmp(q[s], mx) > 0) mx = q[s];
+      }
+      acc_add_xprod(&lo, mn);
+      acc_add_xprod(&up, mx);
+    }
+    if (bad) {
+      out_lo[t] = NAN;
+      out_up[t] = NAN;
+    } else {
+      out_lo[t] = acc_round(&lo, -1);
+      out_up[t] = acc_round(&up, +1);
+    }
+  }
+}
+
+/* Exact point dot products sum_p A(i,p) B(p,j) (A m x k, B k x n, plain doubles,
+ * ld = rows), rounded down and up, for `count` entries. */
+void orc_exact_dot(int m, int n, int k, const double* A, const double* B, long count,
+                   const int* rows, const int* cols, double* out_dn, double* out_up,
+                   int nthreads) {
+  (void)n;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+#endif
+  for (long t = 0; t < count; ++t) {
+    const int i = rows[t], j = cols[t];
+    orc_acc s;
+    acc_zero(&s);
+    int bad = 0;
+    for (int p = 0; p < k; ++p) {
+      double a = A[(long)i + (long)p * m], b = B[(long)p + (long)j * k];
+      if (nonfinite2(a, b)) {
+        bad = 1;
+        break;
+      }
+      acc_add_xprod(&s, exact_mul(a, b));
+    }
+    out_dn[t] = bad ? NAN : acc_round(&s, -1);
+    out_up[t] = bad ? NAN : acc_round(&s, +1);
+  }
+}
+
+/* Exact sum of a list of doubles, rounded in direction dir (self-test hook). */
+double orc_exact_sum(long count, const double* x, int dir) {
+  orc_acc s;
+  acc_zero(&s);
+  for (long i = 0; i < count; ++i) {
+    if (x[i] == 0.0) continue;
+    int sg, e;
+    uint64_t mt;
+    decompose(x[i], &sg, &mt, &e);
+    acc_add_u128(&s, (unsigned __int128)mt, e + ACC_BIAS, sg);
+  }
+  return acc_round(&s, dir);
+}

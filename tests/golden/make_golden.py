@@ -1,0 +1,62 @@
+"""Generate the golden vectors in tests/golden/ from the reference itself.
+
+The reference ships no golden vectors (its tests are print-only mains), so
+this script runs the reference's own code -- vblas rmatmul and
+vcp::matrix<kv::interval<double>, vcp::pidblas> compiled from the reference
+tree by oracle/build.py (kv from the project's kvshim) -- on small seeded
+inputs and stores inputs and outputs as golden.npz.  It needs the reference
+sources, so it runs only where they are mounted; the .npz travels with the
+repository.
+
+Run:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle import oracle as O  # noqa: E402
+from oracle.build import build_reference  # noqa: E402
+from vcp_gb300 import workloads as W  # noqa: E402
+
+OUT = Path(__file__).resolve().parent / "golden.npz"
+
+
+def main() -> None:
+    if build_reference() is None:
+        raise SystemExit("reference sources not mounted; cannot regenerate golden vectors")
+    rng = np.random.default_rng(20261203)
+    data: dict[str, np.ndarray] = {}
+    # vblas rmatmul, vblas naming (A m x n, B n x k), three modes, ragged shapes
+    cases = [(1, 1, 1), (7, 5, 3), (16, 64, 4), (33, 17, 29), (64, 64, 64), (3, 200, 2)]
+    for idx, (m, n, k) in enumerate(cases):
+        phi = [0, 8, 32][idx % 3]
+        A = W.ephi(rng, m * n, phi)
+        B = W.ephi(rng, n * k, phi)
+        data[f"rm{idx}_shape"] = np.array([m, n, k])
+        data[f"rm{idx}_A"] = A
+        data[f"rm{idx}_B"] = B
+        for rnd, tag in ((1, "up"), (-1, "dn"), (0, "rn")):
+            data[f"rm{idx}_{tag}"] = O.ref_rmatmul(m, n, k, A, B, rnd)
+    # pidblas::mulmm through vcp::matrix, GEMM naming (A m x k, B k x n)
+    icases = [(5, 4, 6), (32, 32, 32), (17, 40, 64), (64, 9, 3)]
+    for idx, (m, n, k) in enumerate(icases):
+        A = W.interval_ephi(rng, m, k, phi=4, rad_ratio=2.0 ** -40)
+        B = W.interval_ephi(rng, k, n, phi=4, rad_ratio=2.0 ** -20)
+        data[f"iv{idx}_shape"] = np.array([m, n, k])
+        data[f"iv{idx}_A"] = A
+        data[f"iv{idx}_B"] = B
+        data[f"iv{idx}_C"] = O.ref_pidblas_mulmm(m, n, k, A, B)
+    data["n_rm"] = np.array([len(cases)])
+    data["n_iv"] = np.array([len(icases)])
+    np.savez_compressed(OUT, **data)
+    print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
+
+
+if __name__ == "__main__":
+    main()

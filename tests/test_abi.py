@@ -1,0 +1,43 @@
+"""CPU tests of the C ABI boundary: the library loads (no GPU calls) and
+exports every function include/vcpcuda.h declares, and the ctypes table of
+the Python host side matches the header."""
+import re
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"\b(vcpcu_\w+)\s*\(", text))
+    return names
+
+
+def test_header_declares_core_entry_points():
+    names = declared_functions()
+    for n in ("vcpcu_rmatmul", "vcpcu_udmatmul", "vcpcu_igemm", "vcpcu_igemm_dev",
+              "vcpcu_last_error_string"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(cuda_lib):
+    missing = [n for n in sorted(declared_functions()) if not hasattr(cuda_lib, n)]
+    assert not missing, missing
+
+
+def test_ctypes_table_matches_header():
+    from vcp_gb300._lib import SIGNATURES
+    assert set(SIGNATURES) == declared_functions()
+
+
+def test_error_mapping():
+    import pytest
+    from vcp_gb300 import errors
+    with pytest.raises(errors.DimensionError):
+        errors.raise_for_status(1, "x")
+    with pytest.raises(errors.NonFiniteError):
+        errors.raise_for_status(3, "x")
+    assert issubclass(errors.CudaError, errors.StateError)
+    errors.raise_for_status(0, "fine")

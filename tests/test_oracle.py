@@ -1,0 +1,146 @@
+"""CPU tests: the oracle pinned against the reference.
+
+* golden vectors produced by the reference's own code (tests/golden/golden.npz,
+  made by tests/golden/make_golden.py from vblas rmatmul and
+  vcp::matrix<interval, pidblas>);
+* where the reference sources are mounted, live bit-for-bit comparison with
+  the reference compiled from its tree (oracle/_ref);
+* the known-answer rounding tests of vblas/Check_rmatmul_rounding.cpp:51-116
+  and vblas/Check_udmatmul_rounding.cpp:40-102 (every entry must differ
+  between the upward and downward products);
+* self-tests of the exact accumulator against Python's exact rationals.
+"""
+from fractions import Fraction
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from vcp_gb300 import workloads as W
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "golden.npz"
+
+
+def bits(x):
+    return np.asarray(x, dtype=np.float64).view(np.int64)
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(GOLDEN)
+
+
+def test_oracle_rmatmul_matches_golden(oracle, golden):
+    for idx in range(int(golden["n_rm"][0])):
+        m, n, k = map(int, golden[f"rm{idx}_shape"])
+        A, B = golden[f"rm{idx}_A"], golden[f"rm{idx}_B"]
+        for rnd, tag in ((1, "up"), (-1, "dn"), (0, "rn")):
+            got = oracle.rmatmul(m, n, k, A, B, rnd)
+            assert np.array_equal(bits(got), bits(golden[f"rm{idx}_{tag}"])), (idx, tag)
+
+
+def test_oracle_pidblas_matches_golden(oracle, golden):
+    for idx in range(int(golden["n_iv"][0])):
+        m, n, k = map(int, golden[f"iv{idx}_shape"])
+        got = oracle.pidblas_mulmm(m, n, k, golden[f"iv{idx}_A"], golden[f"iv{idx}_B"])
+        assert np.array_equal(bits(got), bits(golden[f"iv{idx}_C"])), idx
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1), (31, 257, 17), (100, 513, 12), (16, 1000, 5)])
+def test_oracle_rmatmul_matches_reference_build(oracle, shape):
+    if oracle.ref_lib() is None:
+        from oracle.build import build_reference
+        if build_reference() is None:
+            pytest.skip("reference sources not mounted")
+    m, n, k = shape
+    rng = np.random.default_rng(sum(shape))
+    A, B = W.ephi(rng, m * n, 32), W.ephi(rng, n * k, 32)
+    for rnd in (1, -1, 0):
+        assert np.array_equal(bits(oracle.rmatmul(m, n, k, A, B, rnd)),
+                              bits(oracle.ref_rmatmul(m, n, k, A, B, rnd)))
+
+
+def test_oracle_pidblas_matches_reference_build(oracle):
+    if oracle.ref_lib() is None:
+        from oracle.build import build_reference
+        if build_reference() is None:
+            pytest.skip("reference sources not mounted")
+    rng = np.random.default_rng(5)
+    for m, n, k in [(48, 40, 100), (1, 30, 20), (30, 1, 20), (25, 25, 1)]:
+        A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
+        B = W.interval_ephi(rng, k, n, 4, 2.0 ** -10)
+        assert np.array_equal(bits(oracle.pidblas_mulmm(m, n, k, A, B)),
+                              bits(oracle.ref_pidblas_mulmm(m, n, k, A, B)))
+
+
+def kat_patterns(n):
+    """The two patterns of vblas/Check_rmatmul_rounding.cpp (column-major A, B)."""
+    pats = []
+    for i in (0, n // 2, n - 1):  # 1/3 rank-1 pattern (:55-79), a few i
+        A = np.zeros((n, n)); B = np.zeros((n, n))
+        A[:, i] = 1.0 / 3.0; B[i, :] = 1.0 / 3.0
+        pats.append((A.ravel(order="F"), B.ravel(order="F")))
+    for i in (2, n // 2, n - 1):  # 1 + 2^-54 pattern (:83-114)
+        A = np.zeros((n, n)); B = np.zeros((n, n))
+        A[:, 1] = 1.0; B[1, :] = 1.0
+        A[:, i] = 2.0 ** -27; B[i, :] = 2.0 ** -27
+        pats.append((A.ravel(order="F"), B.ravel(order="F")))
+    return pats
+
+
+def test_oracle_rounding_kat(oracle):
+    n = 90
+    for A, B in kat_patterns(n):
+        cu = oracle.rmatmul(n, n, n, A, B, 1)
+        cd = oracle.rmatmul(n, n, n, A, B, -1)
+        assert np.all(cu > cd)
+
+
+def test_exact_sum_matches_fractions(oracle):
+    rng = np.random.default_rng(3)
+    for trial in range(20):
+        x = rng.standard_normal(200) * np.exp2(rng.integers(-300, 300, 200))
+        if trial % 4 == 0:
+            x[:5] = [5e-324, -5e-324, 1e308, -1e308, 2.0 ** -1074 * 3]
+        F = sum(Fraction(float(v)) for v in x)
+        lo, hi = oracle.exact_sum(x, -1), oracle.exact_sum(x, 1)
+        assert Fraction(lo) <= F <= Fraction(hi)
+        assert hi == lo if Fraction(lo) == F else np.nextafter(lo, np.inf) == hi
+
+
+def test_exact_dot_and_hull(oracle):
+    rng = np.random.default_rng(4)
+    m, n, k = 6, 5, 40
+    A = W.ephi(rng, m * k, 30)
+    B = W.ephi(rng, k * n, 30)
+    rows = np.repeat(np.arange(m), n)
+    cols = np.tile(np.arange(n), m)
+    dn, up = oracle.exact_dot(m, n, k, A, B, rows, cols)
+    for t, (i, j) in enumerate(zip(rows, cols)):
+        F = sum(Fraction(float(A[i + p * m])) * Fraction(float(B[p + j * k])) for p in range(k))
+        assert Fraction(dn[t]) <= F <= Fraction(up[t])
+    # interval hull: endpoints straddling zero exercise every min/max case
+    Ai = W.interval_ephi(rng, m, k, 3, 0.7)
+    Bi = W.interval_ephi(rng, k, n, 3, 1.3)
+    lo, hi = oracle.exact_hull(m, n, k, Ai, Bi, rows, cols)
+    for t, (i, j) in enumerate(zip(rows, cols)):
+        L = Fraction(0); U = Fraction(0)
+        for p in range(k):
+            a = [Fraction(float(Ai[2 * (i + p * m) + s])) for s in (0, 1)]
+            b = [Fraction(float(Bi[2 * (p + j * k) + s])) for s in (0, 1)]
+            prods = [x * y for x in a for y in b]
+            L += min(prods); U += max(prods)
+        assert Fraction(lo[t]) <= L and U <= Fraction(hi[t])
+        assert Fraction(float(np.nextafter(lo[t], np.inf))) > L  # tight: RD of the exact sum
+        assert Fraction(float(np.nextafter(hi[t], -np.inf))) < U
+
+
+def test_midrad_encloses(oracle):
+    rng = np.random.default_rng(6)
+    X = W.interval_ephi(rng, 50, 50, 40, 0.3)
+    X[:4] = [-1e308, 1.7e308, 1.7e308, 1.79e308]  # lo + up overflow path
+    m, r = oracle.midrad(X)
+    for t in range(X.size // 2):
+        lo, up = Fraction(float(X[2 * t])), Fraction(float(X[2 * t + 1]))
+        assert Fraction(float(m[t])) - Fraction(float(r[t])) <= lo
+        assert up <= Fraction(float(m[t])) + Fraction(float(r[t]))

@@ -1,0 +1,63 @@
+"""ctypes binding of libvcpcuda.so (the C ABI declared in include/vcpcuda.h).
+
+There is no fallback: if the shared library is missing or cannot be loaded,
+every entry point raises.  Build it with ``vcp_gb300.build.build()``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+from .errors import raise_for_status
+
+LIB_PATH = Path(__file__).resolve().parent / "libvcpcuda.so"
+
+_lock = threading.Lock()
+_lib: C.CDLL | None = None
+
+_i, _d, _v, _ll = C.c_int, C.POINTER(C.c_double), C.c_void_p, C.c_longlong
+
+# name -> (restype, argtypes); must match include/vcpcuda.h
+SIGNATURES: dict[str, tuple] = {
+    "vcpcu_last_error_string": (C.c_char_p, []),
+    "vcpcu_version": (_i, []),
+    "vcpcu_launch_count": (_ll, []),
+    "vcpcu_rmatmul": (_i, [_i, _i, _i, _v, _v, _v, _i]),
+    "vcpcu_udmatmul": (_i, [_i, _i, _i, _v, _v, _v, _v]),
+    "vcpcu_rmatmul_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _i, _v]),
+    "vcpcu_udmatmul_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _v, _i, _v]),
+    "vcpcu_igemm_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _i, _i, _v]),
+    "vcpcu_igemm": (_i, [_i, _i, _i, _v, _v, _v, _i, _i]),
+}
+
+
+def load() -> C.CDLL:
+    """Load libvcpcuda.so once; raise if it is absent."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise RuntimeError(
+                    f"{LIB_PATH} is not built; run vcp_gb300.build.build() "
+                    "(no CPU fallback exists)")
+            lib = C.CDLL(str(LIB_PATH))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+        return _lib
+
+
+def call(name: str, *args) -> None:
+    """Call an int-returning entry point and raise on a non-zero status."""
+    lib = load()
+    st = getattr(lib, name)(*args)
+    if st != 0:
+        msg = lib.vcpcu_last_error_string().decode(errors="replace")
+        raise_for_status(st, f"{name}: {msg}")
+
+
+def launch_count() -> int:
+    return int(load().vcpcu_launch_count())

@@ -1,0 +1,184 @@
+// capi.cu -- the exported C ABI (include/vcpcuda.h): argument checks,
+// host<->device staging for the host-pointer entry points, dispatch.
+#include "common.cuh"
+#include "plain_gemm.cuh"
+#include "ozaki.cuh"
+
+#include <cstring>
+
+using namespace vcpcu;
+
+namespace {
+
+// One non-blocking stream per (host thread, device) for the host-pointer
+// entry points, so they do not serialise with unrelated work.
+cudaStream_t host_stream() {
+  thread_local cudaStream_t streams[64] = {nullptr};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return nullptr;
+  if (!streams[dev]) cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking);
+  return streams[dev];
+}
+
+int point_kind(int rounding_mode) {
+  if (rounding_mode == 1) return PK_UP;
+  if (rounding_mode == -1) return PK_DOWN;
+  return PK_NEAREST;
+}
+
+// vblas naming -> GEMM naming: rmatmul(m, n, k): A m x n, B n x k, C m x k.
+int rmatmul_dev_impl(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                     double* C0, double* C1, int ldc, int kind, cudaStream_t s) {
+  clear_error();
+  if (m <= 0 || k <= 0) return VCPCU_OK;
+  if (!C0 || (kind == PK_UPDOWN && !C1)) {
+    set_error("rmatmul: null output pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (ldc < m) {
+    set_error("rmatmul: ldc (%d) < m (%d)", ldc, m);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (n > 0) {
+    if (!A || !B) {
+      set_error("rmatmul: null input pointer");
+      return VCPCU_ERR_INVALID_ARG;
+    }
+    if (lda < m || ldb < n) {
+      set_error("rmatmul: lda (%d) < m (%d) or ldb (%d) < n (%d)", lda, m, ldb, n);
+      return VCPCU_ERR_INVALID_ARG;
+    }
+  }
+  int st = check_device();
+  if (st) return st;
+  return launch_point_gemm(m, k, n > 0 ? n : 0, A, lda, B, ldb, C0, C1, ldc, kind, s);
+}
+
+int rmatmul_host_impl(int m, int n, int k, const double* A, const double* B, double* C0,
+                      double* C1, int kind) {
+  clear_error();
+  if (m <= 0 || k <= 0) return VCPCU_OK;
+  if (!C0 || (kind == PK_UPDOWN && !C1) || (n > 0 && (!A || !B))) {
+    set_error("rmatmul: null pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  int st = check_device();
+  if (st) return st;
+  cudaStream_t s = host_stream();
+  const size_t na = n > 0 ? (size_t)m * n : 0, nb = n > 0 ? (size_t)n * k : 0,
+               nc = (size_t)m * k;
+  const size_t nouts = (kind == PK_UPDOWN) ? 2 : 1;
+  Scratch buf;
+  st = buf.alloc(sizeof(double) * (na + nb + nouts * nc), s);
+  if (st) return st;
+  double* dA = (double*)buf.ptr;
+  double* dB = dA + na;
+  double* dC0 = dB + nb;
+  double* dC1 = (kind == PK_UPDOWN) ? dC0 + nc : nullptr;
+  if (na) VCPCU_CUDA_TRY(cudaMemcpyAsync(dA, A, na * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (nb) VCPCU_CUDA_TRY(cudaMemcpyAsync(dB, B, nb * sizeof(double), cudaMemcpyHostToDevice, s));
+  st = launch_point_gemm(m, k, n > 0 ? n : 0, dA, m, dB, n > 0 ? n : 1, dC0, dC1, m, kind, s);
+  if (st) return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(C0, dC0, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (dC1) VCPCU_CUDA_TRY(cudaMemcpyAsync(C1, dC1, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  return VCPCU_OK;
+}
+
+int igemm_check(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                const double* C, int ldc, int form, int slices) {
+  if (form != VCPCU_FORM_PLAIN && form != VCPCU_FORM_OZAKI && form != VCPCU_FORM_AUTO) {
+    set_error("igemm: unknown form %d", form);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (form == VCPCU_FORM_OZAKI && slices != 0 && (slices < 2 || slices > OZ_MAX_SLICES)) {
+    set_error("igemm: slices must be 0 or in [2, %d], got %d", OZ_MAX_SLICES, slices);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (m <= 0 || n <= 0) return VCPCU_OK;
+  if (!C || (k > 0 && (!A || !B))) {
+    set_error("igemm: null pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (ldc < m || (k > 0 && (lda < m || ldb < k))) {
+    set_error("igemm: leading dimension too small (lda %d, ldb %d, ldc %d for m %d, k %d)", lda,
+              ldb, ldc, m, k);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  return VCPCU_OK;
+}
+
+int igemm_dispatch(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
+                   double* C, long ldc, int form, int slices, cudaStream_t s) {
+  if (k < 0) k = 0;
+  if (form == VCPCU_FORM_PLAIN) {
+    Scratch ws;
+    int st = ws.alloc(interval_gemm_plain_ws_bytes(m, n, k), s);
+    if (st) return st;
+    return launch_interval_gemm_plain(m, n, k, A, lda, B, ldb, C, ldc, (double*)ws.ptr, s);
+  }
+  return ozaki_igemm(m, n, k, A, lda, B, ldb, C, ldc, form, slices, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int vcpcu_rmatmul(int m, int n, int k, const double* A, const double* B, double* C,
+                  int rounding_mode) {
+  return rmatmul_host_impl(m, n, k, A, B, C, nullptr, point_kind(rounding_mode));
+}
+
+int vcpcu_udmatmul(int m, int n, int k, const double* A, const double* B, double* CU,
+                   double* CD) {
+  return rmatmul_host_impl(m, n, k, A, B, CU, CD, PK_UPDOWN);
+}
+
+int vcpcu_rmatmul_dev(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                      double* C, int ldc, int rounding_mode, void* stream) {
+  return rmatmul_dev_impl(m, n, k, A, lda, B, ldb, C, nullptr, ldc, point_kind(rounding_mode),
+                          (cudaStream_t)stream);
+}
+
+int vcpcu_udmatmul_dev(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                       double* CU, double* CD, int ldc, void* stream) {
+  return rmatmul_dev_impl(m, n, k, A, lda, B, ldb, CU, CD, ldc, PK_UPDOWN, (cudaStream_t)stream);
+}
+
+int vcpcu_igemm_dev(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                    double* C, int ldc, int form, int slices, void* stream) {
+  clear_error();
+  int st = igemm_check(m, n, k, A, lda, B, ldb, C, ldc, form, slices);
+  if (st || m <= 0 || n <= 0) return st;
+  st = check_device();
+  if (st) return st;
+  return igemm_dispatch(m, n, k, A, lda, B, ldb, C, ldc, form, slices, (cudaStream_t)stream);
+}
+
+int vcpcu_igemm(int m, int n, int k, const double* A, const double* B, double* C, int form,
+                int slices) {
+  clear_error();
+  int st = igemm_check(m, n, k, A, m, B, k > 0 ? k : 1, C, m, form, slices);
+  if (st || m <= 0 || n <= 0) return st;
+  st = check_device();
+  if (st) return st;
+  if (k < 0) k = 0;
+  cudaStream_t s = host_stream();
+  const size_t na = 2 * (size_t)m * k, nb = 2 * (size_t)k * n, nc = 2 * (size_t)m * n;
+  Scratch buf;
+  st = buf.alloc(sizeof(double) * (na + nb + nc), s);
+  if (st) return st;
+  double* dA = (double*)buf.ptr;
+  double* dB = dA + na;
+  double* dC = dB + nb;
+  if (na) VCPCU_CUDA_TRY(cudaMemcpyAsync(dA, A, na * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (nb) VCPCU_CUDA_TRY(cudaMemcpyAsync(dB, B, nb * sizeof(double), cudaMemcpyHostToDevice, s));
+  st = igemm_dispatch(m, n, k, dA, m, dB, k > 0 ? k : 1, dC, m, form, slices, s);
+  if (st) return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(C, dC, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  return VCPCU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,365 @@
+// plain_gemm.cu -- FP64 CUDA-core GEMMs with per-instruction directed
+// rounding: the "plain form" of the verified product.
+//
+// Result definition (vblas/README.md, "packing layout"; the AVX-512 micro
+// kernel vblas/rmatmul_avx512.hpp:195-242 keeps the C tile in registers and
+// continues the chain across k blocks): entry C(i,j) is the sequential chain
+//     c = +0.0;  for p = 0..K-1:  c = fma_dir(A(i,p), B(p,j), c)
+// in ascending p.  Every thread here owns whole C entries and runs exactly
+// that chain, so the kernels are bit-identical to vblas rmatmul/udmatmul for
+// any tiling.  K tails are padded with +0.0 * +0.0 = +0.0 products, which
+// leave every chain value unchanged in all three rounding modes (a -0.0
+// accumulator can only arise under round-down, where -0.0 + +0.0 = -0.0).
+//
+// The interval kernel follows pidblas::mulmm (vcp/pidblas.hpp:239-294): its
+// four dgemm_ calls become four chains per entry in one pass over A and B:
+//     lo = chain_rd(mA*mB)          (:264-266)
+//     up = chain_ru(mA*mB)          (:269-271)
+//     t1 = chain_ru((|mA|+rA)*rB)   (:273-279; |mA|+rA rounded up)
+//     t2 = chain_ru(rA*|mB|)        (:281)
+//     T  = t1 +ru t2 ; up = up +ru T ; lo = lo -rd T   (:283-286)
+// with mA, rA, mB, rB from kv-style midrad (pidblas.hpp:43-51).
+#include "common.cuh"
+#include "plain_gemm.cuh"
+
+namespace vcpcu {
+
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+
+// Kinds of chains a kernel runs per C entry.
+enum Kind { K_RN = 0, K_RU = 1, K_RD = 2, K_UD = 3 };
+
+template <int KIND>
+__device__ __forceinline__ double fma_k(double a, double b, double c) {
+  if (KIND == K_RU) return __fma_ru(a, b, c);
+  if (KIND == K_RD) return __fma_rd(a, b, c);
+  return __fma_rn(a, b, c);
+}
+
+// One-direction (KIND RN/RU/RD) or up+down (K_UD) point GEMM.
+// GEMM naming: C(M x N) = A(M x K) * B(K x N), column-major.
+template <int KIND>
+__global__ void __launch_bounds__(NT)
+point_gemm_kernel(int M, int N, int K, const double* __restrict__ A, long lda,
+                  const double* __restrict__ B, long ldb, double* __restrict__ C0,
+                  double* __restrict__ C1, long ldc) {
+  constexpr int NCH = (KIND == K_UD) ? 2 : 1;
+  __shared__ double As[2][BK][BM];
+  __shared__ double Bs[2][BK][BN];
+
+  const int tid = threadIdx.x;
+  const int tr = tid / 16, tc = tid % 16;
+  const int row0 = blockIdx.x * BM, col0 = blockIdx.y * BN;
+
+  // loader coordinates
+  const int a_i = tid % BM, a_k = tid / BM;        // A: 4 rows of k per pass
+  const int b_k = tid % BK, b_j = tid / BK;        // B: 16 columns per pass
+
+  double acc[NCH][4][4];
+#pragma unroll
+  for (int c = 0; c < NCH; ++c)
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[c][i][j] = 0.0;
+
+  double ra[4], rb[4];
+  auto load_tile = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int gi = row0 + a_i, gk = k0 + a_k + 4 * q;
+      ra[q] = (gi < M && gk < K) ? A[gi + gk * lda] : 0.0;
+      int hk = k0 + b_k, hj = col0 + b_j + 16 * q;
+      rb[q] = (hk < K && hj < N) ? B[hk + hj * ldb] : 0.0;
+    }
+  };
+  auto store_tile = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      As[buf][a_k + 4 * q][a_i] = ra[q];
+      Bs[buf][b_k][b_j + 16 * q] = rb[q];
+    }
+  };
+
+  const int nk = (K + BK - 1) / BK;
+  load_tile(0);
+  store_tile(0);
+  __syncthreads();
+  for (int t = 0; t < nk; ++t) {
+    const int buf = t & 1;
+    if (t + 1 < nk) load_tile((t + 1) * BK);
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[buf][kk][tr + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[buf][kk][tc + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (KIND == K_UD) {
+            acc[0][i][j] = __fma_ru(a[i], b[j], acc[0][i][j]);
+            acc[NCH - 1][i][j] = __fma_rd(a[i], b[j], acc[NCH - 1][i][j]);
+          } else {
+            acc[0][i][j] = fma_k<KIND>(a[i], b[j], acc[0][i][j]);
+          }
+        }
+    }
+    if (t + 1 < nk) {
+      store_tile(buf ^ 1);
+    }
+    __syncthreads();
+  }
+
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int gi = row0 + tr + 16 * i, gj = col0 + tc + 16 * j;
+      if (gi < M && gj < N) {
+        C0[gi + gj * ldc] = acc[0][i][j];
+        if (KIND == K_UD) C1[gi + gj * ldc] = acc[NCH - 1][i][j];
+      }
+    }
+}
+
+// C = 0 for the n <= 0 (empty inner dimension) case of vblas rmatmul.
+__global__ void zero_kernel(int M, int N, double* C, long ldc) {
+  long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  long total = (long)M * N;
+  for (; idx < total; idx += (long)gridDim.x * blockDim.x) {
+    long i = idx % M, j = idx / M;
+    C[i + j * ldc] = 0.0;
+  }
+}
+
+}  // namespace
+
+// kv-style midpoint/radius of [lo, up]: m = fl((lo + up) / 2) to nearest
+// (halves taken separately when lo + up overflows), r = max(m - lo, up - m)
+// rounded up, so that [m - r, m + r] contains [lo, up].  Explicit _rn
+// intrinsics keep the compiler from contracting into an FMA.
+__device__ __forceinline__ void midrad_dev(double lo, double up, double& m, double& r) {
+  double s = __dadd_rn(lo, up);
+  if (isfinite(s))
+    m = __dmul_rn(s, 0.5);
+  else
+    m = __dadd_rn(__dmul_rn(lo, 0.5), __dmul_rn(up, 0.5));
+  r = fmax(__dsub_ru(m, lo), __dsub_ru(up, m));
+}
+
+// Left factor: interval A (m x k, ld in intervals) -> planes mA, pA = |mA| +ru rA, rA
+// (ld = M).  Right factor: interval B -> planes mB, rB (ld = K).
+__global__ void interval_prep_left(int M, int K, const double* __restrict__ A, long lda,
+                                   double* __restrict__ mA, double* __restrict__ pA,
+                                   double* __restrict__ rA) {
+  long total = (long)M * K;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    long i = idx % M, p = idx / M;
+    const double* e = A + 2 * (i + p * lda);
+    double m, r;
+    midrad_dev(e[0], e[1], m, r);
+    mA[idx] = m;
+    rA[idx] = r;
+    pA[idx] = __dadd_ru(fabs(m), r);
+  }
+}
+
+__global__ void interval_prep_right(int K, int N, const double* __restrict__ B, long ldb,
+                                    double* __restrict__ mB, double* __restrict__ rB) {
+  long total = (long)K * N;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    long p = idx % K, j = idx / K;
+    const double* e = B + 2 * (p + j * ldb);
+    double m, r;
+    midrad_dev(e[0], e[1], m, r);
+    mB[idx] = m;
+    rB[idx] = r;
+  }
+}
+
+namespace {
+
+// Fused mid-rad interval GEMM over prepped planes (ld = M for A planes,
+// ld = K for B planes).  Writes C as {inf, sup} pairs (ld in intervals).
+// Five operand planes are staged per k step, so the k tile is BKI = 8 deep
+// (double-buffered: 40 KB of shared memory).
+constexpr int BKI = 8;
+__global__ void __launch_bounds__(NT)
+interval_gemm_kernel(int M, int N, int K, const double* __restrict__ mA,
+                     const double* __restrict__ pA, const double* __restrict__ rA,
+                     const double* __restrict__ mB, const double* __restrict__ rB,
+                     double* __restrict__ C, long ldc) {
+  __shared__ double Am[2][BKI][BM], Ap[2][BKI][BM], Ar[2][BKI][BM];
+  __shared__ double Bm[2][BKI][BN], Br[2][BKI][BN];
+
+  const int tid = threadIdx.x;
+  const int tr = tid / 16, tc = tid % 16;
+  const int row0 = blockIdx.x * BM, col0 = blockIdx.y * BN;
+  const int a_i = tid % BM, a_k = tid / BM;    // 4 k rows per pass, 2 passes
+  const int b_k = tid % BKI, b_j = tid / BKI;  // 32 columns per pass, 2 passes
+  constexpr int QA = BKI / (NT / BM), QB = BN / (NT / BKI);
+
+  double lo[4][4], up[4][4], t1[4][4], t2[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) lo[i][j] = up[i][j] = t1[i][j] = t2[i][j] = 0.0;
+
+  double ram[QA], rap[QA], rar[QA], rbm[QB], rbr[QB];
+  auto load_tile = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < QA; ++q) {
+      int gi = row0 + a_i, gk = k0 + a_k + (NT / BM) * q;
+      bool ok = gi < M && gk < K;
+      long o = gi + (long)gk * M;
+      ram[q] = ok ? mA[o] : 0.0;
+      rap[q] = ok ? pA[o] : 0.0;
+      rar[q] = ok ? rA[o] : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < QB; ++q) {
+      int hk = k0 + b_k, hj = col0 + b_j + (NT / BKI) * q;
+      bool okb = hk < K && hj < N;
+      long ob = hk + (long)hj * K;
+      rbm[q] = okb ? mB[ob] : 0.0;
+      rbr[q] = okb ? rB[ob] : 0.0;
+    }
+  };
+  auto store_tile = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < QA; ++q) {
+      Am[buf][a_k + (NT / BM) * q][a_i] = ram[q];
+      Ap[buf][a_k + (NT / BM) * q][a_i] = rap[q];
+      Ar[buf][a_k + (NT / BM) * q][a_i] = rar[q];
+    }
+#pragma unroll
+    for (int q = 0; q < QB; ++q) {
+      Bm[buf][b_k][b_j + (NT / BKI) * q] = rbm[q];
+      Br[buf][b_k][b_j + (NT / BKI) * q] = rbr[q];
+    }
+  };
+
+  const int nk = (K + BKI - 1) / BKI;
+  load_tile(0);
+  store_tile(0);
+  __syncthreads();
+  for (int t = 0; t < nk; ++t) {
+    const int buf = t & 1;
+    if (t + 1 < nk) load_tile((t + 1) * BKI);
+#pragma unroll 2
+    for (int kk = 0; kk < BKI; ++kk) {
+      double am[4], ap[4], ar[4], bm[4], br[4], bma[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        am[i] = Am[buf][kk][tr + 16 * i];
+        ap[i] = Ap[buf][kk][tr + 16 * i];
+        ar[i] = Ar[buf][kk][tr + 16 * i];
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        bm[j] = Bm[buf][kk][tc + 16 * j];
+        br[j] = Br[buf][kk][tc + 16 * j];
+        bma[j] = fabs(bm[j]);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          lo[i][j] = __fma_rd(am[i], bm[j], lo[i][j]);
+          up[i][j] = __fma_ru(am[i], bm[j], up[i][j]);
+          t1[i][j] = __fma_ru(ap[i], br[j], t1[i][j]);
+          t2[i][j] = __fma_ru(ar[i], bma[j], t2[i][j]);
+        }
+    }
+    if (t + 1 < nk) store_tile(buf ^ 1);
+    __syncthreads();
+  }
+
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int gi = row0 + tr + 16 * i, gj = col0 + tc + 16 * j;
+      if (gi < M && gj < N) {
+        double T = __dadd_ru(t1[i][j], t2[i][j]);
+        double u = __dadd_ru(up[i][j], T);
+        double l = __dsub_rd(lo[i][j], T);
+        double* e = C + 2 * (gi + (long)gj * ldc);
+        e[0] = l;
+        e[1] = u;
+      }
+    }
+}
+
+inline int grid_1d(long total) {
+  long b = (total + 255) / 256;
+  if (b > 152 * 32) b = 152 * 32;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+}  // namespace
+
+int launch_point_gemm(int M, int N, int K, const double* A, long lda, const double* B,
+                      long ldb, double* C0, double* C1, long ldc, int kind,
+                      cudaStream_t s) {
+  if (M <= 0 || N <= 0) return VCPCU_OK;
+  if (K <= 0) {
+    zero_kernel<<<grid_1d((long)M * N), 256, 0, s>>>(M, N, C0, ldc);
+    VCPCU_LAUNCH_CHECK("zero_kernel");
+    if (C1) {
+      zero_kernel<<<grid_1d((long)M * N), 256, 0, s>>>(M, N, C1, ldc);
+      VCPCU_LAUNCH_CHECK("zero_kernel");
+    }
+    return VCPCU_OK;
+  }
+  dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
+  switch (kind) {
+    case PK_UP:
+      point_gemm_kernel<K_RU><<<grid, NT, 0, s>>>(M, N, K, A, lda, B, ldb, C0, nullptr, ldc);
+      break;
+    case PK_DOWN:
+      point_gemm_kernel<K_RD><<<grid, NT, 0, s>>>(M, N, K, A, lda, B, ldb, C0, nullptr, ldc);
+      break;
+    case PK_UPDOWN:
+      point_gemm_kernel<K_UD><<<grid, NT, 0, s>>>(M, N, K, A, lda, B, ldb, C0, C1, ldc);
+      break;
+    default:
+      point_gemm_kernel<K_RN><<<grid, NT, 0, s>>>(M, N, K, A, lda, B, ldb, C0, nullptr, ldc);
+      break;
+  }
+  VCPCU_LAUNCH_CHECK("point_gemm_kernel");
+  return VCPCU_OK;
+}
+
+int launch_interval_gemm_plain(int M, int N, int K, const double* A, long lda,
+                               const double* B, long ldb, double* C, long ldc,
+                               double* ws, cudaStream_t s) {
+  // ws holds 3*M*K + 2*K*N doubles.
+  double* mA = ws;
+  double* pA = mA + (size_t)M * K;
+  double* rA = pA + (size_t)M * K;
+  double* mB = rA + (size_t)M * K;
+  double* rB = mB + (size_t)K * N;
+  interval_prep_left<<<grid_1d((long)M * K), 256, 0, s>>>(M, K, A, lda, mA, pA, rA);
+  VCPCU_LAUNCH_CHECK("interval_prep_left");
+  interval_prep_right<<<grid_1d((long)K * N), 256, 0, s>>>(K, N, B, ldb, mB, rB);
+  VCPCU_LAUNCH_CHECK("interval_prep_right");
+  dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
+  interval_gemm_kernel<<<grid, NT, 0, s>>>(M, N, K, mA, pA, rA, mB, rB, C, ldc);
+  VCPCU_LAUNCH_CHECK("interval_gemm_kernel");
+  return VCPCU_OK;
+}
+
+size_t interval_gemm_plain_ws_bytes(int M, int N, int K) {
+  return sizeof(double) * (3 * (size_t)M * K + 2 * (size_t)K * N);
+}
+
+}  // namespace vcpcu

@@ -1,0 +1,23 @@
+// plain_gemm.cuh -- launchers of the FP64 directed-rounding kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+
+namespace vcpcu {
+
+enum PointKind { PK_NEAREST = 0, PK_UP = 1, PK_DOWN = 2, PK_UPDOWN = 3 };
+
+// C0 (and C1 for PK_UPDOWN, rounded down) = A * B, GEMM naming
+// C(M x N) = A(M x K) B(K x N); K <= 0 zeroes the outputs.
+int launch_point_gemm(int M, int N, int K, const double* A, long lda, const double* B,
+                      long ldb, double* C0, double* C1, long ldc, int kind,
+                      cudaStream_t s);
+
+// Plain-form interval GEMM over kv-layout intervals; ws must hold
+// interval_gemm_plain_ws_bytes(M, N, K) bytes.
+int launch_interval_gemm_plain(int M, int N, int K, const double* A, long lda,
+                               const double* B, long ldb, double* C, long ldc,
+                               double* ws, cudaStream_t s);
+size_t interval_gemm_plain_ws_bytes(int M, int N, int K);
+
+}  // namespace vcpcu
