@@ -57,6 +57,14 @@ int vcpcu_version(void);
 /* Number of kernels this library launched since load (all threads). */
 long long vcpcu_launch_count(void);
 
+/* Synchronise `stream` and report (then clear) the sticky device status of
+ * earlier stream-ordered Ozaki-form calls on the current device:
+ * VCPCU_ERR_NONFINITE if one saw an Inf/NaN input (its output is NaN),
+ * VCPCU_ERR_TIMEOUT if a bounded device-side wait gave up (its output is
+ * invalid), else VCPCU_OK.  The host-pointer entry points check this
+ * themselves. */
+int vcpcu_status(void* stream);
+
 /* ---- directed-rounding point GEMM ----------------------------------------- */
 
 /* Replaces vblas rmatmul (vblas/rmatmul.hpp:102):

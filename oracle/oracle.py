@@ -33,6 +33,8 @@ def lib() -> C.CDLL:
         L.orc_exact_dot.argtypes = [_i, _i, _i, _v, _v, _l, _v, _v, _v, _v, _i]
         L.orc_exact_sum.argtypes = [_l, _v, _i]
         L.orc_exact_sum.restype = C.c_double
+        L.orc_ozaki_igemm.argtypes = [_i, _i, _i, _v, _v, _v, _i, _i]
+        L.orc_ozaki_igemm.restype = _i
         _lib = L
     return _lib
 
@@ -96,6 +98,15 @@ def exact_dot(m, n, k, A, B, rows, cols, threads=0):
     lib().orc_exact_dot(m, n, k, _p(A), _p(B), rows.size, _p(rows), _p(cols), _p(dn), _p(up),
                         int(threads))
     return dn, up
+
+
+def ozaki_igemm(m, n, k, A, B, s=8, sr=2):
+    """Host model of the Ozaki-form interval product (kv buffers, GEMM
+    naming).  Returns (C kv buffer, status) -- status 3 on non-finite input."""
+    C_ = np.zeros(2 * m * n, dtype=np.float64)
+    st = lib().orc_ozaki_igemm(m, n, k, _p(A) if k > 0 else None, _p(B) if k > 0 else None,
+                               _p(C_), int(s), int(sr))
+    return C_, st
 
 
 def exact_sum(x: np.ndarray, direction: int) -> float:

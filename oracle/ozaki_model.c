@@ -1,3 +1,454 @@
-/* ozaki_model.c -- host model of the Ozaki-scheme slicing (filled in with the
- * tensor-core form).  TEST INFRASTRUCTURE ONLY. */
-int orc_ozaki_model_version(void) { return 0; }
+/*
+ * ozaki_model.c -- host model of the Ozaki-form interval product.
+ *
+ * TEST INFRASTRUCTURE ONLY (see vcp_oracle.c).  The GPU form must be
+ * bit-identical to this model, which restates, in plain C and integer
+ * arithmetic, the same slicing, summation order and directed-rounding
+ * reassembly:
+ *
+ *  - operands: kv-style midrad of every interval entry (as pidblas_assist::
+ *    midrad, vcp/pidblas.hpp:43-51), P = |mA| +ru rA, S = |mB|;
+ *  - exponents: E with max |x| <= 2^(E-1) per row (left) / column (right);
+ *    the reference's per-row/column sigma = 2^(e+s) split of
+ *    pddblas_assist::split_row/split_col (vcp/pddblas.hpp:82-154);
+ *  - digits: N = x 2^(8s-E) rounded (nearest-even; upward for the radius
+ *    factors) and written as s balanced base-256 digits in [-128, 128];
+ *  - products: pairs (p, q) with p + q <= s + 1 (midpoint; all pairs for
+ *    the radius factors) in ascending t = p + q, each split into chunks of
+ *    1024 inner indices; chunk sums are folded into the int64 value
+ *    W = sum C_t 2^(8 (t_ref - t)) every 64 chunks and at the end of each
+ *    t (right shifts floor) -- the accumulation order of the reference's
+ *    ozaki_acc (vcp/pddblas.hpp:160-193: t ascending, p ascending);
+ *  - reassembly: [RD(W u) - e, RU((W + R) u) + e] with u = 2^(E + F - 8 t_ref),
+ *    e = RU(trunc + T), trunc = 2^(E-8s) RU(RU(0.515625 delta) 2^(F-8) +
+ *    RU(beta/2)), T = RU(RU((W'+R') u') + RU((W''+R'') u'')).
+ */
+#include <fenv.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define OZ_ZERO_EXP (-30000)
+#define OZ_CHUNK 1024
+#define OZ_FOLD 64
+#define OZ_MAXS 12
+
+static uint64_t dbits(double x) {
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  return b;
+}
+static double bitsd(uint64_t b) {
+  double x;
+  memcpy(&x, &b, 8);
+  return x;
+}
+
+static int oz_exponent(double amax) {
+  uint64_t b = dbits(amax);
+  int be = (int)((b >> 52) & 0x7ff);
+  uint64_t mant = b & ((1ULL << 52) - 1);
+  if (be == 0 && mant == 0) return OZ_ZERO_EXP;
+  if (be == 0) {
+    int bl = 0;
+    while (mant) {
+      mant >>= 1;
+      ++bl;
+    }
+    return bl - 1073;
+  }
+  return be - 1021;
+}
+
+static __int128 oz_scaled_int(double x, int E, int s, int up) {
+  uint64_t b = dbits(x);
+  int neg = (int)(b >> 63), be = (int)((b >> 52) & 0x7ff);
+  uint64_t mant = b & ((1ULL << 52) - 1);
+  if (be == 0 && mant == 0) return 0;
+  int ex;
+  if (be == 0)
+    ex = -1074;
+  else {
+    mant |= 1ULL << 52;
+    ex = be - 1075;
+  }
+  int sh = ex + 8 * s - E;
+  unsigned __int128 N;
+  if (sh >= 0) {
+    N = (unsigned __int128)mant << sh;
+  } else {
+    int r = -sh;
+    uint64_t q;
+    int rem_nz, above, at;
+    if (r >= 64) {
+      q = 0;
+      rem_nz = mant != 0;
+      above = 0;
+      at = 0;
+    } else {
+      q = mant >> r;
+      uint64_t rem = mant & ((1ULL << r) - 1), half = 1ULL << (r - 1);
+      rem_nz = rem != 0;
+      above = rem > half;
+      at = rem == half;
+    }
+    if (up) {
+      if (!neg && rem_nz) q += 1;
+    } else if (above || (at && (q & 1))) {
+      q += 1;
+    }
+    N = q;
+  }
+  return neg ? -(__int128)N : (__int128)N;
+}
+
+static void oz_digits(__int128 N, int s, int* d) {
+  for (int p = s - 1; p >= 1; --p) {
+    int lo = (int)((uint64_t)(N + 128) & 255ULL) - 128;
+    d[p] = lo;
+    N = (N - lo) >> 8;
+  }
+  d[0] = (int)N;
+}
+
+static void midrad_rp(double lo, double up, double* m, double* r, double* pabs) {
+  /* caller holds FE_TONEAREST */
+  double s = lo + up;
+  double mm = isfinite(s) ? s * 0.5 : lo * 0.5 + up * 0.5;
+  fesetround(FE_UPWARD);
+  double d1 = mm - lo, d2 = up - mm;
+  double rr = fmax(d1, d2);
+  *pabs = fabs(mm) + rr;
+  fesetround(FE_TONEAREST);
+  *m = mm;
+  *r = rr;
+}
+
+static double mul_dir(double x, double y, int up) {
+  fesetround(up ? FE_UPWARD : FE_DOWNWARD);
+  double z = x * y;
+  fesetround(FE_TONEAREST);
+  return z;
+}
+
+static double scale_dir(double x, int e, int up) {
+  while (e > 1023) {
+    x = mul_dir(x, 0x1p1023, up);
+    e -= 1023;
+  }
+  while (e < -1022) {
+    x = mul_dir(x, 0x1p-1022, up);
+    e += 1022;
+  }
+  return mul_dir(x, bitsd((uint64_t)(e + 1023) << 52), up);
+}
+
+static double pow2_ru(int e) {
+  if (e >= -1022) return scale_dir(1.0, e, 1);
+  if (e >= -1074) return bitsd(1ULL << (e + 1074));
+  return bitsd(1ULL);
+}
+
+static double ll2d(long long v, int up) {
+  fesetround(up ? FE_UPWARD : FE_DOWNWARD);
+  double z = (double)v;
+  fesetround(FE_TONEAREST);
+  return z;
+}
+
+typedef struct {
+  int npairs, ngroups;
+  int pa[80], pb[80];
+  int gstart[27], gt[26];
+} pairlist;
+
+static void build_pairs(int sa, int sb, int triangular, pairlist* pl) {
+  memset(pl, 0, sizeof(*pl));
+  int tmax = triangular ? (sa > sb ? sa : sb) + 1 : sa + sb;
+  int n = 0, g = 0;
+  for (int t = 2; t <= tmax; ++t) {
+    int start = n;
+    for (int p = 1; p < t; ++p) {
+      int q = t - p;
+      if (p > sa || q > sb) continue;
+      pl->pa[n] = p - 1;
+      pl->pb[n] = q - 1;
+      ++n;
+    }
+    if (n > start) {
+      pl->gstart[g] = start;
+      pl->gt[g] = t;
+      ++g;
+    }
+  }
+  pl->gstart[g] = n;
+  pl->npairs = n;
+  pl->ngroups = g;
+}
+
+static void choose_scaling(const pairlist* pl, int nchunks, int* t_ref, int* R) {
+  int best = 2, tmax = pl->gt[pl->ngroups - 1];
+  for (int tr = 2; tr <= tmax; ++tr) {
+    double bound = 0.0;
+    for (int g = 0; g < pl->ngroups; ++g) {
+      double np = (double)(pl->gstart[g + 1] - pl->gstart[g]);
+      bound += np * nchunks * 16777216.0 * ldexp(1.0, 8 * (tr - pl->gt[g])) + 64.0;
+    }
+    if (bound < ldexp(1.0, 62)) best = tr;
+  }
+  int r = 0;
+  for (int g = 0; g < pl->ngroups; ++g) {
+    if (pl->gt[g] <= best) continue;
+    int total = (pl->gstart[g + 1] - pl->gstart[g]) * nchunks;
+    r += (total + OZ_FOLD - 1) / OZ_FOLD;
+  }
+  *t_ref = best;
+  *R = r;
+}
+
+static long long shift_t(long long c, int sh) { return sh >= 0 ? (c << sh) : (c >> (-sh)); }
+
+/* W of one element from K-major digit rows da[p][k], db[q][k] (stride Kp). */
+static long long element_W(const int8_t* da, const int8_t* db, long plane_a, long plane_b,
+                           int Kp, const pairlist* pl, int t_ref) {
+  const int nchunks = (Kp + OZ_CHUNK - 1) / OZ_CHUNK;
+  long long W = 0;
+  int have = 0;
+  for (int g = 0; g < pl->ngroups; ++g) {
+    int sh = 8 * (t_ref - pl->gt[g]);
+    long long C = 0;
+    int cnt = 0;
+    int total = (pl->gstart[g + 1] - pl->gstart[g]) * nchunks, idx = 0;
+    for (int pi = pl->gstart[g]; pi < pl->gstart[g + 1]; ++pi) {
+      const int8_t* a = da + pl->pa[pi] * plane_a;
+      const int8_t* b = db + pl->pb[pi] * plane_b;
+      for (int ch = 0; ch < nchunks; ++ch, ++idx) {
+        int k0 = ch * OZ_CHUNK, k1 = k0 + OZ_CHUNK < Kp ? k0 + OZ_CHUNK : Kp;
+        int s32 = 0;
+        for (int k = k0; k < k1; ++k) s32 += (int)a[k] * (int)b[k];
+        C += s32;
+        ++cnt;
+        if (cnt == OZ_FOLD || idx == total - 1) {
+          long long v = shift_t(C, sh);
+          W = have ? W + v : v;
+          have = 1;
+          C = 0;
+          cnt = 0;
+        }
+      }
+    }
+  }
+  return W;
+}
+
+/*
+ * The whole Ozaki-form product: C (m x n, kv layout, ld m) = [A] (m x k) *
+ * [B] (k x n), s midpoint slices, sr radius slices.  Digits are int8 except
+ * +128, stored as int8 -128 with a flag... (digits in [-128,128] do not fit
+ * int8): they are kept as int16 internally.  Returns 0, 3 on non-finite input.
+ */
+int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, double* Cout, int s,
+                    int sr) {
+  const int prev = fegetround();
+  fesetround(FE_TONEAREST);
+  const int Kp = k <= 0 ? 64 : (k + 63) / 64 * 64;
+  const int nchunks = (Kp + OZ_CHUNK - 1) / OZ_CHUNK;
+  int nonfinite = 0;
+  /* --- left factor ---------------------------------------------------- */
+  double* mA = calloc((size_t)m * (k > 0 ? k : 1), sizeof(double));
+  double* rA = calloc((size_t)m * (k > 0 ? k : 1), sizeof(double));
+  double* pA = calloc((size_t)m * (k > 0 ? k : 1), sizeof(double));
+  for (long t = 0; t < (long)m * k; ++t) {
+    double lo = A[2 * t], up = A[2 * t + 1];
+    if (!isfinite(lo) || !isfinite(up)) {
+      nonfinite = 1;
+      continue;
+    }
+    midrad_rp(lo, up, &mA[t], &rA[t], &pA[t]);
+  }
+  int* Em = malloc(sizeof(int) * m);
+  int* Ep = malloc(sizeof(int) * m);
+  int* Er = malloc(sizeof(int) * m);
+  long long* delta = calloc(m, sizeof(long long));
+  /* digits stored as int16 in [-128, 128]: planes [p][i][Kp] */
+  int16_t* dAm = calloc((size_t)s * m * Kp, sizeof(int16_t));
+  int16_t* dAp = calloc((size_t)sr * m * Kp, sizeof(int16_t));
+  int16_t* dAr = calloc((size_t)sr * m * Kp, sizeof(int16_t));
+  for (int i = 0; i < m; ++i) {
+    double am = 0, ap = 0, ar = 0;
+    for (int p = 0; p < k; ++p) {
+      long t = i + (long)p * m;
+      am = fmax(am, fabs(mA[t]));
+      ap = fmax(ap, pA[t]);
+      ar = fmax(ar, rA[t]);
+    }
+    Em[i] = oz_exponent(am);
+    Ep[i] = oz_exponent(ap);
+    Er[i] = oz_exponent(ar);
+    int d[OZ_MAXS];
+    for (int p = 0; p < k; ++p) {
+      long t = i + (long)p * m;
+      if (Em[i] != OZ_ZERO_EXP && mA[t] != 0.0) {
+        oz_digits(oz_scaled_int(mA[t], Em[i], s, 0), s, d);
+        for (int q = 0; q < s; ++q) {
+          dAm[((size_t)q * m + i) * Kp + p] = (int16_t)d[q];
+          delta[i] += abs(d[q]);
+        }
+      }
+      if (Ep[i] != OZ_ZERO_EXP && pA[t] != 0.0) {
+        oz_digits(oz_scaled_int(pA[t], Ep[i], sr, 1), sr, d);
+        for (int q = 0; q < sr; ++q) dAp[((size_t)q * m + i) * Kp + p] = (int16_t)d[q];
+      }
+      if (Er[i] != OZ_ZERO_EXP && rA[t] != 0.0) {
+        oz_digits(oz_scaled_int(rA[t], Er[i], sr, 1), sr, d);
+        for (int q = 0; q < sr; ++q) dAr[((size_t)q * m + i) * Kp + p] = (int16_t)d[q];
+      }
+    }
+  }
+  /* --- right factor --------------------------------------------------- */
+  int* Fm = malloc(sizeof(int) * n);
+  int* Fr = malloc(sizeof(int) * n);
+  double* beta = malloc(sizeof(double) * n);
+  int16_t* dBm = calloc((size_t)s * n * Kp, sizeof(int16_t));
+  int16_t* dBr = calloc((size_t)sr * n * Kp, sizeof(int16_t));
+  int16_t* dBs = calloc((size_t)sr * n * Kp, sizeof(int16_t));
+  double* mcol = malloc(sizeof(double) * (k > 0 ? k : 1));
+  double* rcol = malloc(sizeof(double) * (k > 0 ? k : 1));
+  for (int j = 0; j < n; ++j) {
+    double am = 0, ar = 0;
+    double part[256];
+    for (int t = 0; t < 256; ++t) part[t] = 0.0;
+    for (int p = 0; p < k; ++p) {
+      long t = p + (long)j * k;
+      double lo = B[2 * t], up = B[2 * t + 1], pp;
+      if (!isfinite(lo) || !isfinite(up)) {
+        nonfinite = 1;
+        mcol[p] = rcol[p] = 0.0;
+        continue;
+      }
+      midrad_rp(lo, up, &mcol[p], &rcol[p], &pp);
+      am = fmax(am, fabs(mcol[p]));
+      ar = fmax(ar, rcol[p]);
+      fesetround(FE_UPWARD);
+      part[p % 256] = part[p % 256] + fabs(mcol[p]);
+      fesetround(FE_TONEAREST);
+    }
+    fesetround(FE_UPWARD);
+    for (int w = 128; w > 0; w >>= 1)
+      for (int t = 0; t < w; ++t) part[t] = part[t] + part[t + w];
+    fesetround(FE_TONEAREST);
+    beta[j] = part[0];
+    Fm[j] = oz_exponent(am);
+    Fr[j] = oz_exponent(ar);
+    int d[OZ_MAXS];
+    for (int p = 0; p < k; ++p) {
+      if (Fm[j] != OZ_ZERO_EXP && mcol[p] != 0.0) {
+        oz_digits(oz_scaled_int(mcol[p], Fm[j], s, 0), s, d);
+        for (int q = 0; q < s; ++q) dBm[((size_t)q * n + j) * Kp + p] = (int16_t)d[q];
+        oz_digits(oz_scaled_int(fabs(mcol[p]), Fm[j], sr, 1), sr, d);
+        for (int q = 0; q < sr; ++q) dBs[((size_t)q * n + j) * Kp + p] = (int16_t)d[q];
+      }
+      if (Fr[j] != OZ_ZERO_EXP && rcol[p] != 0.0) {
+        oz_digits(oz_scaled_int(rcol[p], Fr[j], sr, 1), sr, d);
+        for (int q = 0; q < sr; ++q) dBr[((size_t)q * n + j) * Kp + p] = (int16_t)d[q];
+      }
+    }
+  }
+  /* int8 copies ([-128,128] -> the element loop multiplies int16) */
+  pairlist pm, pr;
+  build_pairs(s, s, 1, &pm);
+  build_pairs(sr, sr, 0, &pr);
+  int tm, Rm, trr, Rr;
+  choose_scaling(&pm, nchunks, &tm, &Rm);
+  choose_scaling(&pr, nchunks, &trr, &Rr);
+  int status = nonfinite ? 3 : 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+  for (int j = 0; j < n; ++j) {
+    fesetround(FE_TONEAREST);
+    for (int i = 0; i < m; ++i) {
+      /* element W with int16 digits */
+      long long W[3];
+      const pairlist* pls[3] = {&pr, &pr, &pm};
+      const int trefs[3] = {trr, trr, tm};
+      const int16_t* as[3] = {dAp, dAr, dAm};
+      const int16_t* bs[3] = {dBr, dBs, dBm};
+      for (int w = 0; w < 3; ++w) {
+        const pairlist* pl = pls[w];
+        long long acc = 0;
+        int have = 0;
+        for (int g = 0; g < pl->ngroups; ++g) {
+          int sh = 8 * (trefs[w] - pl->gt[g]);
+          long long C = 0;
+          int cnt = 0, total = (pl->gstart[g + 1] - pl->gstart[g]) * nchunks, idx = 0;
+          for (int pi = pl->gstart[g]; pi < pl->gstart[g + 1]; ++pi) {
+            const int16_t* a = as[w] + ((size_t)pl->pa[pi] * m + i) * Kp;
+            const int16_t* b = bs[w] + ((size_t)pl->pb[pi] * n + j) * Kp;
+            for (int ch = 0; ch < nchunks; ++ch, ++idx) {
+              int k0 = ch * OZ_CHUNK, k1 = k0 + OZ_CHUNK < Kp ? k0 + OZ_CHUNK : Kp;
+              int s32 = 0;
+              for (int kk = k0; kk < k1; ++kk) s32 += (int)a[kk] * (int)b[kk];
+              C += s32;
+              ++cnt;
+              if (cnt == OZ_FOLD || idx == total - 1) {
+                long long v = shift_t(C, sh);
+                acc = have ? acc + v : v;
+                have = 1;
+                C = 0;
+                cnt = 0;
+              }
+            }
+          }
+        }
+        W[w] = acc;
+      }
+      /* radius bound */
+      double T = 0.0;
+      {
+        int z1 = Ep[i] == OZ_ZERO_EXP || Fr[j] == OZ_ZERO_EXP;
+        double b1 = z1 ? 0.0 : scale_dir(ll2d(W[0] + Rr, 1), Ep[i] + Fr[j] - 8 * trr, 1);
+        int z2 = Er[i] == OZ_ZERO_EXP || Fm[j] == OZ_ZERO_EXP;
+        double b2 = z2 ? 0.0 : scale_dir(ll2d(W[1] + Rr, 1), Er[i] + Fm[j] - 8 * trr, 1);
+        fesetround(FE_UPWARD);
+        T = b1 + b2;
+        fesetround(FE_TONEAREST);
+      }
+      double mlo = 0.0, mup = 0.0, tr = 0.0;
+      int z = Em[i] == OZ_ZERO_EXP || Fm[j] == OZ_ZERO_EXP;
+      if (!z) {
+        int ex = Em[i] + Fm[j] - 8 * tm;
+        mlo = scale_dir(ll2d(W[2], 0), ex, 0);
+        mup = scale_dir(ll2d(W[2] + Rm, 1), ex, 1);
+        double dlt = mul_dir((double)delta[i], 0.515625, 1);
+        double bh = mul_dir(beta[j], 0.5, 1);
+        double f2 = pow2_ru(Fm[j] - 8);
+        fesetround(FE_UPWARD);
+        double x = fma(dlt, f2, bh);
+        fesetround(FE_TONEAREST);
+        tr = scale_dir(x, Em[i] - 8 * s, 1);
+      }
+      fesetround(FE_UPWARD);
+      double err = tr + T;
+      double up = mup + err;
+      fesetround(FE_DOWNWARD);
+      double lo = mlo - err;
+      fesetround(FE_TONEAREST);
+      if (nonfinite) lo = up = NAN;
+      Cout[2 * ((size_t)i + (size_t)j * m)] = lo;
+      Cout[2 * ((size_t)i + (size_t)j * m) + 1] = up;
+    }
+  }
+  (void)element_W;
+  free(mA); free(rA); free(pA); free(Em); free(Ep); free(Er); free(delta);
+  free(dAm); free(dAp); free(dAr); free(Fm); free(Fr); free(beta);
+  free(dBm); free(dBr); free(dBs); free(mcol); free(rcol);
+  fesetround(prev);
+  return status;
+}
+
+int orc_ozaki_model_version(void) { return 1; }

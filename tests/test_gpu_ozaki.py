@@ -1,0 +1,144 @@
+"""GPU parity of the Ozaki (tensor-core) form of the interval product.
+
+* bit-identical to the host model oracle/ozaki_model.c (same slicing,
+  summation order and directed reassembly) on ragged shapes, several slice
+  counts, inner dimensions spanning several 1024-element chunks, and the
+  extreme digit patterns (every digit +-128, so chunk sums reach 2^24);
+* zero containment failures against the exact interval hull (long
+  accumulator) on every checked entry;
+* enclosure no wider than the plain FP64 form at the benchmark distribution;
+* non-finite inputs give NaN results and VCPCU_ERR_NONFINITE.
+"""
+import numpy as np
+import pytest
+
+from vcp_gb300 import pidcuda
+from vcp_gb300 import workloads as W
+from vcp_gb300.errors import NonFiniteError
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(x):
+    return np.asarray(x, dtype=np.float64).view(np.int64)
+
+
+def check_contains(oracle, m, n, k, A, B, C, rows=None, cols=None):
+    if rows is None:
+        rows = np.repeat(np.arange(m), n)
+        cols = np.tile(np.arange(n), m)
+    lo, up = oracle.exact_hull(m, n, k, A, B, rows, cols)
+    idx = 2 * (rows + cols * m)
+    assert np.all(C[idx] <= lo), "lower end above the exact hull"
+    assert np.all(C[idx + 1] >= up), "upper end below the exact hull"
+
+
+CASES = [(1, 1, 1, 8), (5, 7, 3, 8), (128, 256, 64, 8), (129, 257, 65, 6), (200, 100, 1500, 8),
+         (64, 300, 2048, 4), (33, 40, 999, 12), (256, 256, 256, 2)]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_ozaki_bitexact_model_and_encloses(cuda_lib, oracle, case):
+    m, n, k, s = case
+    rng = np.random.default_rng(m * 7 + n * 3 + k + s)
+    A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
+    B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
+    C = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=s)
+    ref, st = oracle.ozaki_igemm(m, n, k, A, B, s, 2)
+    assert st == 0
+    assert np.array_equal(bits(C), bits(ref)), "GPU differs from the host model"
+    check_contains(oracle, m, n, k, A, B, C)
+
+
+def test_ozaki_extreme_digits(cuda_lib, oracle):
+    """All midpoints equal in magnitude: every top digit is +-128 and every
+    1024-chunk of digit products sums to +-2^24, the exactness limit."""
+    m, n, k = 130, 260, 3000
+    A = np.empty(2 * m * k); B = np.empty(2 * k * n)
+    A[0::2] = A[1::2] = 1.0
+    B[0::2] = B[1::2] = 1.0
+    C = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=8)
+    ref, _ = oracle.ozaki_igemm(m, n, k, A, B, 8, 2)
+    assert np.array_equal(bits(C), bits(ref))
+    assert np.all(C[0::2] <= k) and np.all(C[1::2] >= k)
+    # alternating signs by column of A: cancellation to exactly zero
+    rng = np.random.default_rng(2)
+    sg = np.where(rng.random(m * k) < 0.5, -1.0, 1.0)
+    A[0::2] = A[1::2] = sg
+    C = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=8)
+    ref, _ = oracle.ozaki_igemm(m, n, k, A, B, 8, 2)
+    assert np.array_equal(bits(C), bits(ref))
+    check_contains(oracle, m, n, k, A, B, C, rows=np.arange(0, m, 7).repeat(4),
+                   cols=np.tile(np.array([0, 1, 100, 259]), len(range(0, m, 7))))
+
+
+def test_ozaki_wide_and_straddling(cuda_lib, oracle):
+    rng = np.random.default_rng(3)
+    m, n, k = 90, 70, 500
+    A = W.interval_ephi(rng, m, k, 20, 0.9)
+    B = W.interval_ephi(rng, k, n, 20, 1.7)
+    C = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=5)
+    ref, _ = oracle.ozaki_igemm(m, n, k, A, B, 5, 2)
+    assert np.array_equal(bits(C), bits(ref))
+    check_contains(oracle, m, n, k, A, B, C)
+
+
+def test_ozaki_zero_rows_and_columns(cuda_lib, oracle):
+    rng = np.random.default_rng(4)
+    m, n, k = 40, 50, 300
+    A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
+    B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
+    A.reshape(k, m, 2)[:, 3, :] = 0.0     # row 3 of A is [0, 0]
+    B.reshape(n, k, 2)[7, :, :] = 0.0     # column 7 of B is [0, 0]
+    C = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=8)
+    ref, _ = oracle.ozaki_igemm(m, n, k, A, B, 8, 2)
+    assert np.array_equal(bits(C), bits(ref))
+    check_contains(oracle, m, n, k, A, B, C)
+
+
+def test_ozaki_not_wider_than_plain(cuda_lib):
+    """At the benchmark distribution (mid E(4), rad 2^-40 |mid|) and k = 2048
+    the default 8 slices give enclosures no wider than the plain form."""
+    rng = np.random.default_rng(5)
+    m = n = 256
+    k = 2048
+    A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
+    B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
+    Co = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=8)
+    Cp = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_PLAIN)
+    wo = Co[1::2] - Co[0::2]
+    wp = Cp[1::2] - Cp[0::2]
+    assert np.all(wo <= wp), float(np.max(wo / wp))
+
+
+def test_ozaki_nonfinite(cuda_lib):
+    rng = np.random.default_rng(6)
+    m, n, k = 20, 20, 30
+    A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
+    B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
+    A[10] = np.inf
+    C = np.zeros(2 * m * n)
+    with pytest.raises(NonFiniteError):
+        pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, out=C)
+    assert np.all(np.isnan(C))
+    # the sticky status is cleared: the next call is clean
+    A[10] = 1.0
+    pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI)
+
+
+def test_ozaki_dev_stream(cuda_lib, oracle):
+    import torch
+    rng = np.random.default_rng(7)
+    m, n, k = 150, 140, 700
+    A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
+    B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
+    ldc = 160
+    dA = torch.from_numpy(A).cuda(); dB = torch.from_numpy(B).cuda()
+    dC = torch.zeros(2 * ldc * n, dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    pidcuda.mulmm_dev(m, n, k, dA, m, dB, k, dC, ldc, pidcuda.FORM_OZAKI, 7, stream=s)
+    from vcp_gb300 import _lib
+    _lib.call("vcpcu_status", s.cuda_stream)
+    C = dC.cpu().numpy().reshape(n, ldc, 2)[:, :m, :].ravel()
+    ref, _ = oracle.ozaki_igemm(m, n, k, A, B, 7, 2)
+    assert np.array_equal(bits(C), bits(ref))

@@ -23,6 +23,7 @@ SIGNATURES: dict[str, tuple] = {
     "vcpcu_last_error_string": (C.c_char_p, []),
     "vcpcu_version": (_i, []),
     "vcpcu_launch_count": (_ll, []),
+    "vcpcu_status": (_i, [_v]),
     "vcpcu_rmatmul": (_i, [_i, _i, _i, _v, _v, _v, _i]),
     "vcpcu_udmatmul": (_i, [_i, _i, _i, _v, _v, _v, _v]),
     "vcpcu_rmatmul_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _i, _v]),

@@ -121,9 +121,40 @@ int igemm_dispatch(int m, int n, int k, const double* A, long lda, const double*
   return ozaki_igemm(m, n, k, A, lda, B, ldb, C, ldc, form, slices, s);
 }
 
+int take_status() {
+  int status = 0;
+  int st = oz_take_status(host_stream(), &status);
+  if (st) return st;
+  if (status & 2) {
+    set_error("igemm (Ozaki form): a bounded device-side wait timed out; result invalid");
+    return VCPCU_ERR_TIMEOUT;
+  }
+  if (status & 1) {
+    set_error("igemm (Ozaki form): non-finite input entry; the result is NaN");
+    return VCPCU_ERR_NONFINITE;
+  }
+  return VCPCU_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int vcpcu_status(void* stream) {
+  clear_error();
+  int status = 0;
+  int st = oz_take_status((cudaStream_t)stream, &status);
+  if (st) return st;
+  if (status & 2) {
+    set_error("a bounded device-side wait timed out in an earlier call");
+    return VCPCU_ERR_TIMEOUT;
+  }
+  if (status & 1) {
+    set_error("an earlier Ozaki-form call saw a non-finite input (its result is NaN)");
+    return VCPCU_ERR_NONFINITE;
+  }
+  return VCPCU_OK;
+}
 
 int vcpcu_rmatmul(int m, int n, int k, const double* A, const double* B, double* C,
                   int rounding_mode) {
@@ -178,6 +209,7 @@ int vcpcu_igemm(int m, int n, int k, const double* A, const double* B, double* C
   if (st) return st;
   VCPCU_CUDA_TRY(cudaMemcpyAsync(C, dC, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
   VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  if (form != VCPCU_FORM_PLAIN) return take_status();
   return VCPCU_OK;
 }
 

@@ -1,11 +1,185 @@
-// ozaki.cu -- placeholder until the tensor-core form lands.
+// ozaki.cu -- orchestration of the Ozaki-form interval product:
+//   plan (slice counts, pair lists, fixed-point scaling), scratch layout,
+//   operand preparation, the three slice-GEMM launches
+//     1. T  = RU(P^ * rB^)        P = |mA| +ru rA, both factors rounded up
+//     2. T += RU(rA^ * |mB|^)
+//     3. C  = [RD(mA mB) - e, RU(mA mB) + e], e = RU(truncation + T)
+// which together enclose pidblas's midpoint-radius product
+// (vcp/pidblas.hpp:239-294): mA*mB from the truncated slice expansion plus
+// its rigorous truncation bound, and the radius term
+// (|mA| + rA) * rB + rA * |mB| bounded from above.
 #include "common.cuh"
 #include "ozaki.cuh"
+#include "ozaki_common.cuh"
+
+#include <cmath>
+#include <cstring>
 
 namespace vcpcu {
-int ozaki_igemm(int, int, int, const double*, long, const double*, long, double*, long, int,
-                int, cudaStream_t) {
-  set_error("igemm: the Ozaki form is not built yet");
-  return VCPCU_ERR_UNSUPPORTED;
+
+namespace {
+
+void build_pairs(int sa, int sb, bool triangular, OzPairList* pl) {
+  memset(pl, 0, sizeof(*pl));
+  const int tmax = triangular ? (sa > sb ? sa : sb) + 1 : sa + sb;
+  int n = 0, g = 0;
+  for (int t = 2; t <= tmax; ++t) {
+    const int start = n;
+    for (int p = 1; p < t; ++p) {
+      const int q = t - p;
+      if (p > sa || q > sb) continue;
+      pl->pa[n] = (int8_t)(p - 1);
+      pl->pb[n] = (int8_t)(q - 1);
+      ++n;
+    }
+    if (n > start) {
+      pl->gstart[g] = (int16_t)start;
+      pl->gt[g] = (int8_t)t;
+      ++g;
+    }
+  }
+  pl->gstart[g] = (int16_t)n;
+  pl->npairs = n;
+  pl->ngroups = g;
 }
+
+// Largest t_ref keeping |W| < 2^62, and the number of floored folds.
+void choose_scaling(const OzPairList& pl, int nchunks, int* t_ref, int* R) {
+  int best = 2;
+  const int tmax = pl.gt[pl.ngroups - 1];
+  for (int tr = 2; tr <= tmax; ++tr) {
+    double bound = 0.0;
+    for (int g = 0; g < pl.ngroups; ++g) {
+      const double np = (double)(pl.gstart[g + 1] - pl.gstart[g]);
+      bound += np * nchunks * 16777216.0 * std::ldexp(1.0, 8 * (tr - pl.gt[g])) + 64.0;
+    }
+    if (bound < std::ldexp(1.0, 62)) best = tr;
+  }
+  int r = 0;
+  for (int g = 0; g < pl.ngroups; ++g) {
+    if (pl.gt[g] <= best) continue;
+    const int total = (pl.gstart[g + 1] - pl.gstart[g]) * nchunks;
+    r += (total + OZ_FOLD_CHUNKS - 1) / OZ_FOLD_CHUNKS;
+  }
+  *t_ref = best;
+  *R = r;
+}
+
+size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Sticky per-device status of the Ozaki form: bit 0 non-finite input, bit 1
+// a bounded device wait timed out.  Merged after every product, read and
+// cleared by oz_take_status.
+__device__ int g_oz_status;
+
+__global__ void oz_status_merge(const int* flag) {
+  int v = (flag[0] ? 1 : 0) | (flag[1] ? 2 : 0);
+  if (v) atomicOr(&g_oz_status, v);
+}
+
+}  // namespace
+
+int oz_take_status(cudaStream_t s, int* status) {
+  int zero = 0;
+  VCPCU_CUDA_TRY(cudaMemcpyFromSymbolAsync(status, g_oz_status, sizeof(int), 0,
+                                           cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  VCPCU_CUDA_TRY(cudaMemcpyToSymbolAsync(g_oz_status, &zero, sizeof(int), 0,
+                                         cudaMemcpyHostToDevice, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  return VCPCU_OK;
+}
+
+int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan) {
+  memset(plan, 0, sizeof(*plan));
+  OzProblem& pb = plan->pb;
+  pb.M = M;
+  pb.N = N;
+  pb.K = K;
+  pb.Mp = (M + OZ_BM - 1) / OZ_BM * OZ_BM;
+  pb.Np = (N + OZ_BN - 1) / OZ_BN * OZ_BN;
+  pb.Kp = K <= 0 ? OZ_BK : (K + OZ_BK - 1) / OZ_BK * OZ_BK;
+  pb.s = s;
+  pb.sr = sr;
+  build_pairs(s, s, true, &plan->mid);
+  build_pairs(sr, sr, false, &plan->rad);
+  const int nchunks = (pb.Kp + OZ_CHUNK - 1) / OZ_CHUNK;
+  choose_scaling(plan->mid, nchunks, &plan->t_ref_mid, &plan->R_mid);
+  choose_scaling(plan->rad, nchunks, &plan->t_ref_rad, &plan->R_rad);
+  return VCPCU_OK;
+}
+
+size_t oz_workspace_bytes(const OzProblem& pb) {
+  const size_t np = (size_t)(pb.s + 2 * pb.sr);
+  size_t b = 0;
+  b += al256(np * pb.Mp * pb.Kp * 2);
+  b += al256(np * pb.Np * pb.Kp * 2);
+  b += al256(sizeof(unsigned long long) * 3 * pb.Mp);
+  b += al256(sizeof(int) * 3 * pb.Mp);
+  b += al256(sizeof(unsigned long long) * pb.Mp);
+  b += al256(sizeof(int) * 2 * pb.Np);
+  b += al256(sizeof(double) * pb.Np);
+  b += al256(sizeof(double) * (size_t)pb.Mp * pb.Np);
+  b += al256(sizeof(long long) * (size_t)pb.Mp * pb.Np);
+  b += al256(sizeof(int) * 4);
+  return b;
+}
+
+int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws) {
+  uint8_t* p = (uint8_t*)base;
+  const size_t mk = (size_t)pb.Mp * pb.Kp, nk = (size_t)pb.Np * pb.Kp;
+  const size_t np = (size_t)(pb.s + 2 * pb.sr);
+  uint16_t* a = (uint16_t*)p;
+  ws->a_mid = a;
+  ws->a_p = a + pb.s * mk;
+  ws->a_r = ws->a_p + pb.sr * mk;
+  p += al256(np * mk * 2);
+  uint16_t* b = (uint16_t*)p;
+  ws->b_mid = b;
+  ws->b_r = b + pb.s * nk;
+  ws->b_s = ws->b_r + pb.sr * nk;
+  p += al256(np * nk * 2);
+  ws->rowmax = (unsigned long long*)p;
+  p += al256(sizeof(unsigned long long) * 3 * pb.Mp);
+  ws->E3 = (int*)p;
+  p += al256(sizeof(int) * 3 * pb.Mp);
+  ws->delta = (unsigned long long*)p;
+  p += al256(sizeof(unsigned long long) * pb.Mp);
+  ws->F2 = (int*)p;
+  p += al256(sizeof(int) * 2 * pb.Np);
+  ws->beta = (double*)p;
+  p += al256(sizeof(double) * pb.Np);
+  ws->T = (double*)p;
+  p += al256(sizeof(double) * (size_t)pb.Mp * pb.Np);
+  ws->W = (long long*)p;
+  p += al256(sizeof(long long) * (size_t)pb.Mp * pb.Np);
+  ws->flag = (int*)p;
+  return VCPCU_OK;
+}
+
+int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
+                double* C, long ldc, int form, int slices, cudaStream_t s) {
+  (void)form;
+  const int nslices = slices > 0 ? slices : 8;
+  const int sr = 2;
+  if (k > (1 << 20)) {
+    set_error("igemm (Ozaki form): inner dimension %d above the supported 2^20", k);
+    return VCPCU_ERR_UNSUPPORTED;
+  }
+  OzPlan plan;
+  oz_make_plan(m, n, k, nslices, sr, &plan);
+  Scratch buf;
+  int st = buf.alloc(oz_workspace_bytes(plan.pb), s);
+  if (st) return st;
+  OzWorkspace ws;
+  oz_carve_workspace(plan.pb, buf.ptr, &ws);
+  if ((st = oz_prepare(plan.pb, A, lda, B, ldb, ws, s))) return st;
+  if ((st = oz_run_gemm(plan, OZ_RAD_SET, ws, nullptr, 0, s))) return st;
+  if ((st = oz_run_gemm(plan, OZ_RAD_ADD, ws, nullptr, 0, s))) return st;
+  if ((st = oz_run_gemm(plan, OZ_MID, ws, C, ldc, s))) return st;
+  oz_status_merge<<<1, 1, 0, s>>>(ws.flag);
+  VCPCU_LAUNCH_CHECK("oz_status_merge");
+  return VCPCU_OK;
+}
+
 }  // namespace vcpcu

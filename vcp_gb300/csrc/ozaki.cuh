@@ -1,10 +1,91 @@
 // ozaki.cuh -- Ozaki-scheme interval GEMM on tcgen05 tensor cores.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cstdint>
 
 namespace vcpcu {
 
 constexpr int OZ_MAX_SLICES = 12;
+constexpr int OZ_MAX_RSLICES = 4;
+constexpr int OZ_MAX_PAIRS = 80;
+constexpr int OZ_MAX_GROUPS = 26;
+
+// Tile geometry of the slice GEMM.
+constexpr int OZ_BM = 128, OZ_BN = 256, OZ_BK = 64, OZ_STAGES = 4;
+
+struct OzProblem {
+  int M, N, K;     // logical sizes: C (M x N) = A (M x K) * B (K x N)
+  int Mp, Np, Kp;  // padded: Mp % 128 == 0, Np % 256 == 0, Kp % 64 == 0
+  int s, sr;       // digit slices of the midpoints / of the radius factors
+};
+
+// Device scratch of one Ozaki-form product (pointers into one allocation).
+struct OzWorkspace {
+  uint16_t *a_mid, *a_p, *a_r;        // left digit planes  [s|sr][Mp][Kp] (bf16)
+  uint16_t *b_mid, *b_r, *b_s;        // right digit planes [s|sr][Np][Kp] (bf16)
+  unsigned long long* rowmax;         // [Mp][3] maxima of |mA|, P, rA (double bits)
+  int* E3;                            // [Mp][3] exponents Em, Ep, Er
+  unsigned long long* delta;          // [Mp] sum of |midpoint digits| per row
+  int* F2;                            // [Np][2] exponents Fm, Fr
+  double* beta;                       // [Np] sum_k |mB(k,j)| rounded up
+  double* T;                          // [N][Mp] upper bound of the radius product
+  long long* W;                       // [Np][Mp] int64 fold buffer
+  int* flag;                          // [0] non-finite input, [1] device wait timeout
+};
+
+// Ordered list of slice pairs grouped by t = p + q (1-based slice numbers).
+struct OzPairList {
+  int npairs, ngroups;
+  int8_t pa[OZ_MAX_PAIRS], pb[OZ_MAX_PAIRS];   // 0-based plane indices
+  int16_t gstart[OZ_MAX_GROUPS + 1];           // group g = pairs [gstart[g], gstart[g+1])
+  int8_t gt[OZ_MAX_GROUPS];                    // t of group g
+};
+
+enum OzMode { OZ_RAD_SET = 0, OZ_RAD_ADD = 1, OZ_MID = 2 };
+
+struct alignas(64) OzGemmArgs {
+  CUtensorMap tmA;  // left digit planes, dims {Kp, Mp, planes}
+  CUtensorMap tmB;  // right digit planes, dims {Kp, Np, planes}
+  int M, N, Mp, Np, Kp;
+  int tiles_m, tiles_n;
+  int t_ref, R;     // W unit 2^(E_i + F_j - 8 t_ref); R = floor-shifted folds
+  int mode;
+  int s;            // midpoint slices (OZ_MID truncation bound)
+  const int* Erow;  // row exponent of the left operand:  Erow[erow_stride * i]
+  int erow_stride;
+  const int* Fcol;  // column exponent of the right operand: Fcol[fcol_stride * j]
+  int fcol_stride;
+  const unsigned long long* delta;
+  const double* beta;
+  long long* W;
+  double* T;
+  double* C;        // interval output (kv layout), OZ_MID
+  long ldc;
+  int* flag;
+  long long timeout_cycles;
+  OzPairList pl;
+};
+
+// Plan of one product (host side): slice counts, the pair lists and the
+// W scaling, shared with the host model.
+struct OzPlan {
+  OzProblem pb;
+  OzPairList mid, rad;
+  int t_ref_mid, R_mid, t_ref_rad, R_rad;
+};
+
+int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan);
+int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, long ldb,
+               OzWorkspace& ws, cudaStream_t st);
+int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, long ldc,
+                cudaStream_t st);
+size_t oz_workspace_bytes(const OzProblem& pb);
+int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws);
+
+// Read and clear the sticky status (bit 0 non-finite input, bit 1 timeout);
+// synchronises the stream.
+int oz_take_status(cudaStream_t s, int* status);
 
 int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
                 double* C, long ldc, int form, int slices, cudaStream_t s);

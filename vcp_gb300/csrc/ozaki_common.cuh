@@ -1,0 +1,130 @@
+// ozaki_common.cuh -- integer slicing shared by the split kernels and the
+// slice-GEMM epilogue (host- and device-callable, bit-for-bit the same as the
+// host model in oracle/ozaki_model.c).
+//
+// Slicing (the Ozaki scheme, error-free splitting; cf. the reference's
+// pddblas_assist::split_row / split_col, vcp/pddblas.hpp:82-154, which
+// slices with sigma = 2^(e+s) per row/column): every row i of a left factor
+// (column j of a right factor) gets an exponent E with max |x| <= 2^(E-1).
+// x * 2^(8s-E) is rounded to an integer N (to nearest-even for two-sided
+// products, upward for the non-negative radius factors) and N is written
+// as s balanced base-256 digits d_1..d_s, each in [-128, 128], so that
+//     x = 2^E * (sum_p d_p 2^(-8p)) + remainder.
+// Every digit is an integer of at most 8 significant bits, hence exact in
+// bf16, every digit product is at most 2^14, and a sum of up to 1024 such
+// products is an integer of magnitude <= 2^24, exact in the fp32 tensor-core
+// accumulator.
+#pragma once
+#include <cstdint>
+#include <cstring>
+
+#ifdef __CUDACC__
+#define OZ_HD __host__ __device__ __forceinline__
+#else
+#define OZ_HD inline
+#endif
+
+namespace vcpcu {
+
+constexpr int OZ_ZERO_EXP = -30000;   // exponent sentinel of an all-zero row/column
+constexpr int OZ_CHUNK = 1024;        // k elements per exact fp32 accumulation chunk
+constexpr int OZ_FOLD_CHUNKS = 64;    // chunks per int32 fold (64 * 2^24 = 2^30)
+
+OZ_HD uint64_t oz_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  return b;
+#endif
+}
+
+// E such that |x| <= 2^(E-1) for the largest magnitude `amax` (>= 0, finite);
+// OZ_ZERO_EXP for amax == 0.
+OZ_HD int oz_exponent(double amax) {
+  uint64_t b = oz_bits(amax);
+  int be = (int)((b >> 52) & 0x7ff);
+  uint64_t mant = b & ((1ULL << 52) - 1);
+  if (be == 0 && mant == 0) return OZ_ZERO_EXP;
+  if (be == 0) {  // subnormal: amax < 2^(bitlen(mant) - 1074)
+    int bl = 0;
+    while (mant) {
+      mant >>= 1;
+      ++bl;
+    }
+    return bl - 1074 + 1;
+  }
+  return be - 1021;  // amax < 2^(be-1022)
+}
+
+// N = x * 2^(8s - E) rounded to an integer: to nearest-even (up == 0) or
+// toward +inf (up == 1; used for x >= 0).  Requires |x| <= 2^(E-1), so
+// |N| <= 2^(8s-1) (s <= 12 keeps N within 96 bits).
+OZ_HD __int128 oz_scaled_int(double x, int E, int s, int up) {
+  uint64_t b = oz_bits(x);
+  const int neg = (int)(b >> 63);
+  const int be = (int)((b >> 52) & 0x7ff);
+  uint64_t mant = b & ((1ULL << 52) - 1);
+  if (be == 0 && mant == 0) return 0;
+  int ex;
+  if (be == 0) {
+    ex = -1074;
+  } else {
+    mant |= 1ULL << 52;
+    ex = be - 1075;
+  }
+  const int sh = ex + 8 * s - E;
+  unsigned __int128 N;
+  if (sh >= 0) {
+    N = (unsigned __int128)mant << sh;
+  } else {
+    const int r = -sh;
+    uint64_t q;
+    bool rem_nz, above_half, at_half;
+    if (r >= 64) {
+      q = 0;
+      rem_nz = mant != 0;
+      above_half = false;
+      at_half = false;
+    } else {
+      q = mant >> r;
+      const uint64_t rem = mant & ((1ULL << r) - 1);
+      const uint64_t half = 1ULL << (r - 1);
+      rem_nz = rem != 0;
+      above_half = rem > half;
+      at_half = rem == half;
+    }
+    if (up) {
+      // ceil of the magnitude for x >= 0; for x < 0 (not used) truncate
+      if (!neg && rem_nz) q += 1;
+    } else {
+      if (above_half || (at_half && (q & 1))) q += 1;
+    }
+    N = q;
+  }
+  return neg ? -(__int128)N : (__int128)N;
+}
+
+// Balanced base-256 digits of N, most significant first: d[0] = d_1.
+OZ_HD void oz_digits(__int128 N, int s, int* d) {
+  for (int p = s - 1; p >= 1; --p) {
+    const int lo = (int)((uint64_t)(N + 128) & 255ULL) - 128;
+    d[p] = lo;
+    N = (N - lo) >> 8;
+  }
+  d[0] = (int)N;
+}
+
+// bf16 bit pattern of an integer |v| <= 256 (exact).
+OZ_HD uint16_t oz_bf16_of_int(int v) {
+  if (v == 0) return 0;
+  uint16_t sign = v < 0 ? 0x8000 : 0;
+  unsigned a = (unsigned)(v < 0 ? -v : v);
+  int e = 0;  // a = 1.f * 2^e, e <= 8
+  while ((a >> (e + 1)) != 0) ++e;
+  unsigned frac = (e <= 7 ? (a << (7 - e)) : (a >> (e - 7))) & 0x7f;  // 7 explicit bits
+  return (uint16_t)(sign | ((unsigned)(e + 127) << 7) | frac);
+}
+
+}  // namespace vcpcu

@@ -1,0 +1,420 @@
+// ozaki_gemm.cu -- the slice GEMM of the Ozaki form on tcgen05 tensor cores.
+//
+// For one output tile (128 x 256) the kernel runs an ordered list of digit
+// plane pairs (A_p, B_q), grouped by t = p + q.  Each pair is a bf16 GEMM
+// over the whole (padded) inner dimension, split into chunks of 1024: every
+// chunk accumulates in fp32 in tensor memory, where it is an exact integer
+// (|digit products| <= 2^14, 1024 of them <= 2^24).  Epilogue warps drain
+// each finished chunk (double-buffered TMEM accumulators, so draining
+// overlaps the next chunk's MMAs) into int32 registers, and fold the
+// group's integer sum C_t into an int64 fixed-point value
+//     W = sum_t C_t * 2^(8 (t_ref - t))      (unit 2^(E_i + F_j - 8 t_ref))
+// kept in global memory (one read-modify-write per fold).  Shifts to the
+// right floor, so the exact truncated product lies in [W, W + R] units
+// where R counts the floored folds.  The last fold is merged into the
+// final epilogue:
+//   OZ_RAD_SET / OZ_RAD_ADD  T(i,j) (+)= RU((W + R) * unit)  (radius factors
+//                            were rounded up, so this bounds them from above)
+//   OZ_MID                   [lo, up] = [RD(W unit) - e, RU((W+R) unit) + e],
+//                            e = RU(truncation bound + T(i,j)).
+//
+// Warp roles (320 threads, one CTA per SM, persistent over tiles):
+//   warp 0      TMA producer (4-stage ring of 48 KB A+B k-blocks)
+//   warp 1      TMEM owner + MMA issuer (one thread)
+//   warps 2..9  epilogue: warp w reads TMEM lanes 32*(w%4).. and columns
+//               128*((w-2)/4).. of each accumulator.
+// Every mbarrier wait is bounded; a timeout sets flag[1] and the CTA winds
+// down (waits for its copies and MMAs, frees TMEM, returns).
+#include "common.cuh"
+#include "ozaki.cuh"
+#include "ozaki_common.cuh"
+#include "tc_ptx.cuh"
+
+namespace vcpcu {
+
+namespace {
+
+constexpr int NTHREADS = 320;
+constexpr int A_STAGE = OZ_BM * OZ_BK * 2;  // 16 KB
+constexpr int B_STAGE = OZ_BN * OZ_BK * 2;  // 32 KB
+constexpr int STAGE_BYTES = A_STAGE + B_STAGE;
+constexpr uint32_t IDESC = ptx::idesc_bf16_f32(OZ_BM, OZ_BN);
+constexpr int TMEM_COLS = 512;  // two 128 x 256 fp32 accumulators
+
+struct Smem {
+  uint64_t full[OZ_STAGES], empty[OZ_STAGES];
+  uint64_t tfull[2], tempty[2];
+  uint64_t mma_done;
+  uint32_t tmem_base;
+  int abort;
+};
+
+__device__ __forceinline__ void raise_timeout(Smem* sm, int* flag, int where) {
+  atomicOr(&flag[1], 1 << where);
+  *(volatile int*)&sm->abort = 1;
+}
+
+__device__ __forceinline__ double scale_dir(double x, int e, bool up) {
+  while (e > 1023) {
+    x = up ? __dmul_ru(x, 0x1p1023) : __dmul_rd(x, 0x1p1023);
+    e -= 1023;
+  }
+  while (e < -1022) {
+    x = up ? __dmul_ru(x, 0x1p-1022) : __dmul_rd(x, 0x1p-1022);
+    e += 1022;
+  }
+  const double p = __longlong_as_double((long long)(e + 1023) << 52);
+  return up ? __dmul_ru(x, p) : __dmul_rd(x, p);
+}
+
+// Smallest double >= 2^e (e may be below the subnormal range).
+__device__ __forceinline__ double pow2_ru(int e) {
+  if (e >= -1022) return scale_dir(1.0, e, true);
+  if (e >= -1074) return __longlong_as_double(1LL << (e + 1074));
+  return __longlong_as_double(1LL);
+}
+
+__device__ __forceinline__ long long shift_t(int c, int sh) {
+  const long long v = (long long)c;
+  return sh >= 0 ? (v << sh) : (v >> (-sh));
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
+  extern __shared__ uint8_t dsmem_raw[];
+  __shared__ Smem sm;
+  uint8_t* dsmem = (uint8_t*)(((uintptr_t)dsmem_raw + 1023) & ~(uintptr_t)1023);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = args.tiles_m * args.tiles_n;
+  const int nchunks = (args.Kp + OZ_CHUNK - 1) / OZ_CHUNK;
+  const int kblocks = args.Kp / OZ_BK;
+  const long long lim = args.timeout_cycles;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < OZ_STAGES; ++i) {
+      ptx::mbar_init(&sm.full[i], 1);
+      ptx::mbar_init(&sm.empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      ptx::mbar_init(&sm.tfull[i], 1);
+      ptx::mbar_init(&sm.tempty[i], 8);
+    }
+    ptx::mbar_init(&sm.mma_done, 1);
+    sm.abort = 0;
+    ptx::fence_mbar_init();
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(&sm.tmem_base, TMEM_COLS);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = sm.tmem_base;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      ptx::prefetch_tmap(&args.tmA);
+      ptx::prefetch_tmap(&args.tmB);
+      int stage = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      uint32_t used = 0, lastpar = 0;  // per-stage bit masks
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int tm = tile % args.tiles_m, tn = tile / args.tiles_m;
+        for (int pi = 0; pi < args.pl.npairs && ok; ++pi) {
+          const int pa = args.pl.pa[pi], pb = args.pl.pb[pi];
+          for (int kb = 0; kb < kblocks; ++kb) {
+            if (*(volatile int*)&sm.abort || !ptx::mbar_wait(&sm.empty[stage], phase ^ 1, lim)) {
+              if (!*(volatile int*)&sm.abort) raise_timeout(&sm, args.flag, 0);
+              ok = false;
+              break;
+            }
+            uint8_t* sA = dsmem + stage * STAGE_BYTES;
+            uint8_t* sB = sA + A_STAGE;
+            ptx::mbar_expect_tx(&sm.full[stage], STAGE_BYTES);
+            ptx::tma_load_3d(sA, &args.tmA, &sm.full[stage], kb * OZ_BK, tm * OZ_BM, pa);
+            ptx::tma_load_3d(sB, &args.tmB, &sm.full[stage], kb * OZ_BK, tn * OZ_BN, pb);
+            used |= 1u << stage;
+            lastpar = (lastpar & ~(1u << stage)) | (phase << stage);
+            if (++stage == OZ_STAGES) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+        }
+      }
+      // every issued copy has landed before the CTA may exit (immediate in
+      // the normal case: the MMA thread consumed them all)
+      for (int i = 0; i < OZ_STAGES; ++i)
+        if (used & (1u << i)) ptx::mbar_wait(&sm.full[i], (lastpar >> i) & 1u, lim);
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      uint32_t acc = 0;  // global chunk counter
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        for (int pi = 0; pi < args.pl.npairs && ok; ++pi) {
+          for (int ch = 0; ch < nchunks && ok; ++ch, ++acc) {
+            const int buf = acc & 1;
+            const uint32_t par = (acc >> 1) & 1;
+            if (*(volatile int*)&sm.abort || !ptx::mbar_wait(&sm.tempty[buf], par ^ 1, lim)) {
+              if (!*(volatile int*)&sm.abort) raise_timeout(&sm, args.flag, 1);
+              ok = false;
+              break;
+            }
+            ptx::tc_fence_after();
+            const uint32_t dt = tmem + buf * OZ_BN;
+            const int kb0 = ch * (OZ_CHUNK / OZ_BK);
+            const int kb1 = min(kblocks, kb0 + OZ_CHUNK / OZ_BK);
+            for (int kb = kb0; kb < kb1; ++kb) {
+              if (*(volatile int*)&sm.abort || !ptx::mbar_wait(&sm.full[stage], phase, lim)) {
+                if (!*(volatile int*)&sm.abort) raise_timeout(&sm, args.flag, 2);
+                ok = false;
+                break;
+              }
+              ptx::tc_fence_after();
+              const uint32_t sA = ptx::smem_u32(dsmem + stage * STAGE_BYTES);
+              const uint32_t sB = sA + A_STAGE;
+#pragma unroll
+              for (int kk = 0; kk < OZ_BK / 16; ++kk) {
+                const uint64_t ad = ptx::sw128_kmajor_desc(sA + kk * 32);
+                const uint64_t bd = ptx::sw128_kmajor_desc(sB + kk * 32);
+                ptx::mma_bf16(dt, ad, bd, IDESC, (kb > kb0 || kk > 0) ? 1u : 0u);
+              }
+              ptx::mma_commit(&sm.empty[stage]);
+              if (++stage == OZ_STAGES) {
+                stage = 0;
+                phase ^= 1;
+              }
+            }
+            if (!ok) break;
+            ptx::mma_commit(&sm.tfull[buf]);
+          }
+        }
+      }
+      // all MMAs of this thread done before TMEM is released
+      ptx::mma_commit(&sm.mma_done);
+      ptx::mbar_wait(&sm.mma_done, 0, lim);
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int ew = warp - 2;
+    const int quarter = warp & 3;
+    const int half = ew >> 2;
+    const int row_in_tile = quarter * 32 + lane;
+    const uint32_t lane_addr = (uint32_t)(quarter * 32) << 16;
+    uint32_t acc = 0;
+    bool ok = true;
+    bool nonfinite = args.flag[0] != 0;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      const int tm = tile % args.tiles_m, tn = tile / args.tiles_m;
+      const int gi = tm * OZ_BM + row_in_tile;
+      const int gj0 = tn * OZ_BN + half * 128;
+      bool have_w = false;
+      for (int g = 0; g < args.pl.ngroups && ok; ++g) {
+        const int t = args.pl.gt[g];
+        const int sh = 8 * (args.t_ref - t);
+        const int npg = args.pl.gstart[g + 1] - args.pl.gstart[g];
+        const int total = npg * nchunks;
+        int c[128];
+#pragma unroll
+        for (int e = 0; e < 128; ++e) c[e] = 0;
+        int cnt = 0;
+        for (int idx = 0; idx < total; ++idx, ++acc) {
+          const int buf = acc & 1;
+          const uint32_t par = (acc >> 1) & 1;
+          if (*(volatile int*)&sm.abort || !ptx::mbar_wait(&sm.tfull[buf], par, lim)) {
+            if (!*(volatile int*)&sm.abort) raise_timeout(&sm, args.flag, 3);
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+#pragma unroll
+          for (int c4 = 0; c4 < 4; ++c4) {
+            uint32_t r[32];
+            ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c4 * 32, r);
+            ptx::tmem_ld_wait();
+#pragma unroll
+            for (int e = 0; e < 32; ++e) c[c4 * 32 + e] += __float2int_rn(__uint_as_float(r[e]));
+          }
+          ptx::tc_fence_before();
+          __syncwarp();
+          if (lane == 0) ptx::mbar_arrive(&sm.tempty[buf]);
+          ++cnt;
+          const bool last_of_group = idx == total - 1;
+          if (cnt == OZ_FOLD_CHUNKS || last_of_group) {
+            // fold into W (global, column-major, ld = Mp); the first fold of
+            // a tile stores, later folds add
+#pragma unroll
+            for (int e = 0; e < 128; ++e) {
+              long long* wp = args.W + (size_t)(gj0 + e) * args.Mp + gi;
+              const long long v = shift_t(c[e], sh);
+              *wp = have_w ? *wp + v : v;
+              c[e] = 0;
+            }
+            have_w = true;
+            cnt = 0;
+          }
+        }
+      }
+      if (!ok) break;
+      // ------------------------------------------------------ final epilogue
+      const int Ei = (gi < args.M) ? args.Erow[(size_t)args.erow_stride * gi] : OZ_ZERO_EXP;
+      double dlt = 0.0;
+      if (args.mode == OZ_MID && gi < args.M) dlt = __dmul_ru((double)args.delta[gi], 0.515625);
+      if (gi < args.M) {
+        for (int e = 0; e < 128; ++e) {
+          const int gj = gj0 + e;
+          if (gj >= args.N) break;
+          const long long v = args.W[(size_t)gj * args.Mp + gi];
+          const int Fj = args.Fcol[(size_t)args.fcol_stride * gj];
+          const bool zero = (Ei == OZ_ZERO_EXP) || (Fj == OZ_ZERO_EXP);
+          const int ex = Ei + Fj - 8 * args.t_ref;
+          double* Tp = args.T + (size_t)gj * args.Mp + gi;
+          if (args.mode == OZ_RAD_SET || args.mode == OZ_RAD_ADD) {
+            const double b = zero ? 0.0 : scale_dir(__ll2double_ru(v + args.R), ex, true);
+            *Tp = (args.mode == OZ_RAD_SET) ? b : __dadd_ru(*Tp, b);
+          } else {
+            double mlo = 0.0, mup = 0.0, tr = 0.0;
+            if (!zero) {
+              mlo = scale_dir(__ll2double_rd(v), ex, false);
+              mup = scale_dir(__ll2double_ru(v + args.R), ex, true);
+              const double bh = __dmul_ru(args.beta[gj], 0.5);
+              const double x = __fma_ru(dlt, pow2_ru(Fj - 8), bh);
+              tr = scale_dir(x, Ei - 8 * args.s, true);
+            }
+            const double err = __dadd_ru(tr, *Tp);
+            double lo = __dsub_rd(mlo, err), up = __dadd_ru(mup, err);
+            if (nonfinite) lo = up = __longlong_as_double(0x7ff8000000000000LL);
+            double* cp = args.C + 2 * ((size_t)gi + (size_t)gj * args.ldc);
+            cp[0] = lo;
+            cp[1] = up;
+          }
+        }
+      }
+    }
+  }
+
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+// ------------------------------------------------------------- host side
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+int make_tmap(CUtensorMap* m, const void* base, int Kp, int rows, int planes, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) {
+    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return VCPCU_ERR_CUDA;
+  }
+  cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)planes};
+  cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)Kp * rows * 2};
+  cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return VCPCU_ERR_CUDA;
+  }
+  return VCPCU_OK;
+}
+
+int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 148;
+  }
+  return n;
+}
+
+}  // namespace
+
+size_t oz_dyn_smem() { return (size_t)OZ_STAGES * STAGE_BYTES + 1024; }
+
+int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, long ldc,
+                cudaStream_t st) {
+  const OzProblem& pb = plan.pb;
+  static bool attr_set = false;
+  if (!attr_set) {
+    VCPCU_CUDA_TRY(cudaFuncSetAttribute(oz_slice_gemm_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)oz_dyn_smem()));
+    attr_set = true;
+  }
+  OzGemmArgs a;
+  memset(&a, 0, sizeof(a));
+  int st_;
+  const bool mid = mode == OZ_MID;
+  const uint16_t* ap;
+  const uint16_t* bp;
+  int apl, bpl;
+  if (mid) {
+    ap = ws.a_mid; bp = ws.b_mid; apl = pb.s; bpl = pb.s;
+    a.Erow = ws.E3 + 0; a.Fcol = ws.F2 + 0;
+    a.pl = plan.mid; a.t_ref = plan.t_ref_mid; a.R = plan.R_mid;
+  } else if (mode == OZ_RAD_SET) {  // (|mA| + rA) * rB
+    ap = ws.a_p; bp = ws.b_r; apl = pb.sr; bpl = pb.sr;
+    a.Erow = ws.E3 + 1; a.Fcol = ws.F2 + 1;
+    a.pl = plan.rad; a.t_ref = plan.t_ref_rad; a.R = plan.R_rad;
+  } else {  // rA * |mB|
+    ap = ws.a_r; bp = ws.b_s; apl = pb.sr; bpl = pb.sr;
+    a.Erow = ws.E3 + 2; a.Fcol = ws.F2 + 0;
+    a.pl = plan.rad; a.t_ref = plan.t_ref_rad; a.R = plan.R_rad;
+  }
+  if ((st_ = make_tmap(&a.tmA, ap, pb.Kp, pb.Mp, apl, OZ_BM))) return st_;
+  if ((st_ = make_tmap(&a.tmB, bp, pb.Kp, pb.Np, bpl, OZ_BN))) return st_;
+  a.M = pb.M; a.N = pb.N; a.Mp = pb.Mp; a.Np = pb.Np; a.Kp = pb.Kp;
+  a.tiles_m = pb.Mp / OZ_BM;
+  a.tiles_n = pb.Np / OZ_BN;
+  a.mode = mode;
+  a.s = pb.s;
+  a.erow_stride = 3;
+  a.fcol_stride = 2;
+  a.delta = ws.delta;
+  a.beta = ws.beta;
+  a.W = ws.W;
+  a.T = ws.T;
+  a.C = C;
+  a.ldc = ldc;
+  a.flag = ws.flag;
+  a.timeout_cycles = 4000000000LL;  // about 2 s at 2 GHz
+  const int ntiles = a.tiles_m * a.tiles_n;
+  const int grid = ntiles < num_sms() ? ntiles : num_sms();
+  oz_slice_gemm_kernel<<<grid, NTHREADS, oz_dyn_smem(), st>>>(a);
+  VCPCU_LAUNCH_CHECK("oz_slice_gemm_kernel");
+  return VCPCU_OK;
+}
+
+}  // namespace vcpcu
