@@ -65,6 +65,17 @@ long long vcpcu_launch_count(void);
  * themselves. */
 int vcpcu_status(void* stream);
 
+/* Per-phase timing of Ozaki-form calls: while enabled, every call records
+ * CUDA events on its own stream around its phases (0 operand preparation,
+ * 1 and 2 the two radius slice GEMMs, 3 the midpoint slice GEMM and
+ * reassembly).  vcpcu_profile_read waits for the recorded events, writes
+ * the summed milliseconds of the first `nphases` phases to ms[], the summed
+ * algorithmic tensor-core flops (2 m n k per slice pair) to *tensor_flops,
+ * and clears the record.  No counterpart in the reference (it has only
+ * vcp::time tic/toc, vcp/vcp_timer.hpp:39-62). */
+int vcpcu_profile(int enable);
+int vcpcu_profile_read(double* ms, int nphases, long long* tensor_flops);
+
 /* ---- directed-rounding point GEMM ----------------------------------------- */
 
 /* Replaces vblas rmatmul (vblas/rmatmul.hpp:102):

@@ -24,16 +24,27 @@ struct mode_guard {
   explicit mode_guard(int m) : prev(std::fegetround()) { std::fesetround(m); }
   ~mode_guard() { std::fesetround(prev); }
 };
-template <class T> inline T add_dn(T a, T b) { mode_guard g(FE_DOWNWARD); volatile T r = a + b; return r; }
-template <class T> inline T add_up(T a, T b) { mode_guard g(FE_UPWARD); volatile T r = a + b; return r; }
-template <class T> inline T sub_dn(T a, T b) { mode_guard g(FE_DOWNWARD); volatile T r = a - b; return r; }
-template <class T> inline T sub_up(T a, T b) { mode_guard g(FE_UPWARD); volatile T r = a - b; return r; }
-template <class T> inline T mul_dn(T a, T b) { mode_guard g(FE_DOWNWARD); volatile T r = a * b; return r; }
-template <class T> inline T mul_up(T a, T b) { mode_guard g(FE_UPWARD); volatile T r = a * b; return r; }
-template <class T> inline T div_dn(T a, T b) { mode_guard g(FE_DOWNWARD); volatile T r = a / b; return r; }
-template <class T> inline T div_up(T a, T b) { mode_guard g(FE_UPWARD); volatile T r = a / b; return r; }
-template <class T> inline T sqrt_dn(T a) { mode_guard g(FE_DOWNWARD); volatile T r = std::sqrt(a); return r; }
-template <class T> inline T sqrt_up(T a) { mode_guard g(FE_UPWARD); volatile T r = std::sqrt(a); return r; }
+// Operands are read through volatile copies after the mode switch and the
+// result is stored to a volatile before it is restored, so the arithmetic
+// cannot move across the fesetround calls.
+#define KVSHIM_DIR(name, mode, expr)                 \
+  template <class T> inline T name(T a, T b) {       \
+    volatile T x = a, y = b;                         \
+    mode_guard g(mode);                              \
+    volatile T r = expr;                             \
+    return r;                                        \
+  }
+KVSHIM_DIR(add_dn, FE_DOWNWARD, x + y)
+KVSHIM_DIR(add_up, FE_UPWARD, x + y)
+KVSHIM_DIR(sub_dn, FE_DOWNWARD, x - y)
+KVSHIM_DIR(sub_up, FE_UPWARD, x - y)
+KVSHIM_DIR(mul_dn, FE_DOWNWARD, x * y)
+KVSHIM_DIR(mul_up, FE_UPWARD, x * y)
+KVSHIM_DIR(div_dn, FE_DOWNWARD, x / y)
+KVSHIM_DIR(div_up, FE_UPWARD, x / y)
+#undef KVSHIM_DIR
+template <class T> inline T sqrt_dn(T a) { volatile T x = a; mode_guard g(FE_DOWNWARD); volatile T r = std::sqrt((T)x); return r; }
+template <class T> inline T sqrt_up(T a) { volatile T x = a; mode_guard g(FE_UPWARD); volatile T r = std::sqrt((T)x); return r; }
 }  // namespace shim
 
 template <class T> class interval {
@@ -110,11 +121,11 @@ template <class T> class interval {
   template <class C> friend bool operator!=(const interval& x, const C& y) { return x != interval(y); }
 
   friend T mid(const interval& x) {
+    volatile T a = x.inf, b = x.sup;
     shim::mode_guard g(FE_TONEAREST);
-    volatile T s = x.inf + x.sup;
-    if (std::isfinite((T)s)) return (T)s * T(0.5);
-    volatile T h = x.inf * T(0.5);
-    return h + x.sup * T(0.5);
+    volatile T s = a + b;
+    volatile T r = std::isfinite((T)s) ? (T)s * T(0.5) : (T)a * T(0.5) + (T)b * T(0.5);
+    return r;
   }
   friend T rad(const interval& x) {
     T m = mid(x);

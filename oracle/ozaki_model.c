@@ -115,24 +115,54 @@ static void oz_digits(__int128 N, int s, int* d) {
   d[0] = (int)N;
 }
 
-static void midrad_rp(double lo, double up, double* m, double* r, double* pabs) {
-  /* caller holds FE_TONEAREST */
-  double s = lo + up;
-  double mm = isfinite(s) ? s * 0.5 : lo * 0.5 + up * 0.5;
-  fesetround(FE_UPWARD);
-  double d1 = mm - lo, d2 = up - mm;
-  double rr = fmax(d1, d2);
-  *pabs = fabs(mm) + rr;
+/* Directed operations.  The operands are read through volatile copies
+ * after the mode switch and the result is stored to a volatile before the
+ * mode is restored, so the compiler cannot move the arithmetic across the
+ * fesetround calls (which -frounding-math alone does not guarantee). */
+static double add_dir(double a, double b, int mode) {
+  volatile double x = a, y = b;
+  fesetround(mode);
+  volatile double r = x + y;
   fesetround(FE_TONEAREST);
-  *m = mm;
-  *r = rr;
+  return r;
+}
+static double sub_dir(double a, double b, int mode) {
+  volatile double x = a, y = b;
+  fesetround(mode);
+  volatile double r = x - y;
+  fesetround(FE_TONEAREST);
+  return r;
+}
+static double mul_dir(double a, double b, int up) {
+  volatile double x = a, y = b;
+  fesetround(up ? FE_UPWARD : FE_DOWNWARD);
+  volatile double r = x * y;
+  fesetround(FE_TONEAREST);
+  return r;
+}
+static double fma_ru(double a, double b, double c) {
+  volatile double x = a, y = b, z = c;
+  fesetround(FE_UPWARD);
+  volatile double r = fma(x, y, z);
+  fesetround(FE_TONEAREST);
+  return r;
+}
+static double ll2d(long long v, int up) {
+  volatile long long x = v;
+  fesetround(up ? FE_UPWARD : FE_DOWNWARD);
+  volatile double r = (double)x;
+  fesetround(FE_TONEAREST);
+  return r;
 }
 
-static double mul_dir(double x, double y, int up) {
-  fesetround(up ? FE_UPWARD : FE_DOWNWARD);
-  double z = x * y;
-  fesetround(FE_TONEAREST);
-  return z;
+/* midrad as in the plain form; the caller runs in round-to-nearest */
+static void midrad_rp(double lo, double up, double* m, double* r, double* pabs) {
+  double s = lo + up;
+  double mm = isfinite(s) ? s * 0.5 : lo * 0.5 + up * 0.5;
+  double rr = fmax(sub_dir(mm, lo, FE_UPWARD), sub_dir(up, mm, FE_UPWARD));
+  *pabs = add_dir(fabs(mm), rr, FE_UPWARD);
+  *m = mm;
+  *r = rr;
 }
 
 static double scale_dir(double x, int e, int up) {
@@ -151,13 +181,6 @@ static double pow2_ru(int e) {
   if (e >= -1022) return scale_dir(1.0, e, 1);
   if (e >= -1074) return bitsd(1ULL << (e + 1074));
   return bitsd(1ULL);
-}
-
-static double ll2d(long long v, int up) {
-  fesetround(up ? FE_UPWARD : FE_DOWNWARD);
-  double z = (double)v;
-  fesetround(FE_TONEAREST);
-  return z;
 }
 
 typedef struct {
@@ -212,44 +235,10 @@ static void choose_scaling(const pairlist* pl, int nchunks, int* t_ref, int* R) 
 
 static long long shift_t(long long c, int sh) { return sh >= 0 ? (c << sh) : (c >> (-sh)); }
 
-/* W of one element from K-major digit rows da[p][k], db[q][k] (stride Kp). */
-static long long element_W(const int8_t* da, const int8_t* db, long plane_a, long plane_b,
-                           int Kp, const pairlist* pl, int t_ref) {
-  const int nchunks = (Kp + OZ_CHUNK - 1) / OZ_CHUNK;
-  long long W = 0;
-  int have = 0;
-  for (int g = 0; g < pl->ngroups; ++g) {
-    int sh = 8 * (t_ref - pl->gt[g]);
-    long long C = 0;
-    int cnt = 0;
-    int total = (pl->gstart[g + 1] - pl->gstart[g]) * nchunks, idx = 0;
-    for (int pi = pl->gstart[g]; pi < pl->gstart[g + 1]; ++pi) {
-      const int8_t* a = da + pl->pa[pi] * plane_a;
-      const int8_t* b = db + pl->pb[pi] * plane_b;
-      for (int ch = 0; ch < nchunks; ++ch, ++idx) {
-        int k0 = ch * OZ_CHUNK, k1 = k0 + OZ_CHUNK < Kp ? k0 + OZ_CHUNK : Kp;
-        int s32 = 0;
-        for (int k = k0; k < k1; ++k) s32 += (int)a[k] * (int)b[k];
-        C += s32;
-        ++cnt;
-        if (cnt == OZ_FOLD || idx == total - 1) {
-          long long v = shift_t(C, sh);
-          W = have ? W + v : v;
-          have = 1;
-          C = 0;
-          cnt = 0;
-        }
-      }
-    }
-  }
-  return W;
-}
-
 /*
  * The whole Ozaki-form product: C (m x n, kv layout, ld m) = [A] (m x k) *
- * [B] (k x n), s midpoint slices, sr radius slices.  Digits are int8 except
- * +128, stored as int8 -128 with a flag... (digits in [-128,128] do not fit
- * int8): they are kept as int16 internally.  Returns 0, 3 on non-finite input.
+ * [B] (k x n), s midpoint slices, sr radius slices.  Digits (in [-128, 128])
+ * are kept as int16.  Returns 0, or 3 on non-finite input (result NaN).
  */
 int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, double* Cout, int s,
                     int sr) {
@@ -333,14 +322,10 @@ int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, doubl
       midrad_rp(lo, up, &mcol[p], &rcol[p], &pp);
       am = fmax(am, fabs(mcol[p]));
       ar = fmax(ar, rcol[p]);
-      fesetround(FE_UPWARD);
-      part[p % 256] = part[p % 256] + fabs(mcol[p]);
-      fesetround(FE_TONEAREST);
+      part[p % 256] = add_dir(part[p % 256], fabs(mcol[p]), FE_UPWARD);
     }
-    fesetround(FE_UPWARD);
     for (int w = 128; w > 0; w >>= 1)
-      for (int t = 0; t < w; ++t) part[t] = part[t] + part[t + w];
-    fesetround(FE_TONEAREST);
+      for (int t = 0; t < w; ++t) part[t] = add_dir(part[t], part[t + w], FE_UPWARD);
     beta[j] = part[0];
     Fm[j] = oz_exponent(am);
     Fr[j] = oz_exponent(ar);
@@ -358,7 +343,6 @@ int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, doubl
       }
     }
   }
-  /* int8 copies ([-128,128] -> the element loop multiplies int16) */
   pairlist pm, pr;
   build_pairs(s, s, 1, &pm);
   build_pairs(sr, sr, 0, &pr);
@@ -414,9 +398,7 @@ int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, doubl
         double b1 = z1 ? 0.0 : scale_dir(ll2d(W[0] + Rr, 1), Ep[i] + Fr[j] - 8 * trr, 1);
         int z2 = Er[i] == OZ_ZERO_EXP || Fm[j] == OZ_ZERO_EXP;
         double b2 = z2 ? 0.0 : scale_dir(ll2d(W[1] + Rr, 1), Er[i] + Fm[j] - 8 * trr, 1);
-        fesetround(FE_UPWARD);
-        T = b1 + b2;
-        fesetround(FE_TONEAREST);
+        T = add_dir(b1, b2, FE_UPWARD);
       }
       double mlo = 0.0, mup = 0.0, tr = 0.0;
       int z = Em[i] == OZ_ZERO_EXP || Fm[j] == OZ_ZERO_EXP;
@@ -427,23 +409,17 @@ int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, doubl
         double dlt = mul_dir((double)delta[i], 0.515625, 1);
         double bh = mul_dir(beta[j], 0.5, 1);
         double f2 = pow2_ru(Fm[j] - 8);
-        fesetround(FE_UPWARD);
-        double x = fma(dlt, f2, bh);
-        fesetround(FE_TONEAREST);
+        double x = fma_ru(dlt, f2, bh);
         tr = scale_dir(x, Em[i] - 8 * s, 1);
       }
-      fesetround(FE_UPWARD);
-      double err = tr + T;
-      double up = mup + err;
-      fesetround(FE_DOWNWARD);
-      double lo = mlo - err;
-      fesetround(FE_TONEAREST);
+      double err = add_dir(tr, T, FE_UPWARD);
+      double up = add_dir(mup, err, FE_UPWARD);
+      double lo = sub_dir(mlo, err, FE_DOWNWARD);
       if (nonfinite) lo = up = NAN;
       Cout[2 * ((size_t)i + (size_t)j * m)] = lo;
       Cout[2 * ((size_t)i + (size_t)j * m) + 1] = up;
     }
   }
-  (void)element_W;
   free(mA); free(rA); free(pA); free(Em); free(Ep); free(Er); free(delta);
   free(dAm); free(dAp); free(dAr); free(Fm); free(Fr); free(beta);
   free(dBm); free(dBr); free(dBs); free(mcol); free(rcol);

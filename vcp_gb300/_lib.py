@@ -24,6 +24,8 @@ SIGNATURES: dict[str, tuple] = {
     "vcpcu_version": (_i, []),
     "vcpcu_launch_count": (_ll, []),
     "vcpcu_status": (_i, [_v]),
+    "vcpcu_profile": (_i, [_i]),
+    "vcpcu_profile_read": (_i, [_v, _i, _v]),
     "vcpcu_rmatmul": (_i, [_i, _i, _i, _v, _v, _v, _i]),
     "vcpcu_udmatmul": (_i, [_i, _i, _i, _v, _v, _v, _v]),
     "vcpcu_rmatmul_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _i, _v]),
@@ -58,6 +60,18 @@ def call(name: str, *args) -> None:
     if st != 0:
         msg = lib.vcpcu_last_error_string().decode(errors="replace")
         raise_for_status(st, f"{name}: {msg}")
+
+
+def profile(enable: bool) -> None:
+    call("vcpcu_profile", 1 if enable else 0)
+
+
+def profile_read() -> tuple[list[float], int]:
+    """(ms per phase [prep, radius 1, radius 2, midpoint], tensor flops)."""
+    ms = (C.c_double * 4)()
+    fl = C.c_longlong(0)
+    call("vcpcu_profile_read", C.cast(ms, C.c_void_p), 4, C.cast(C.pointer(fl), C.c_void_p))
+    return list(ms), int(fl.value)
 
 
 def launch_count() -> int:

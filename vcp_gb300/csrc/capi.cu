@@ -156,6 +156,12 @@ int vcpcu_status(void* stream) {
   return VCPCU_OK;
 }
 
+int vcpcu_profile(int enable) { return oz_profile_enable(enable); }
+
+int vcpcu_profile_read(double* ms, int nphases, long long* tensor_flops) {
+  return oz_profile_read(ms, nphases, tensor_flops);
+}
+
 int vcpcu_rmatmul(int m, int n, int k, const double* A, const double* B, double* C,
                   int rounding_mode) {
   return rmatmul_host_impl(m, n, k, A, B, C, nullptr, point_kind(rounding_mode));

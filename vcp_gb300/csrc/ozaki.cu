@@ -14,6 +14,9 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <utility>
+#include <vector>
 
 namespace vcpcu {
 
@@ -77,7 +80,60 @@ __global__ void oz_status_merge(const int* flag) {
   if (v) atomicOr(&g_oz_status, v);
 }
 
+// Optional per-phase timing (CUDA events recorded on the call's stream).
+struct OzProfile {
+  bool on = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[4];  // prep, rad1, rad2, mid
+  long long flops = 0;
+};
+OzProfile g_prof;
+std::mutex g_prof_mu;
+
+struct PhaseTimer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  int phase;
+  cudaStream_t s;
+  PhaseTimer(int ph, cudaStream_t st) : phase(ph), s(st) {
+    if (!g_prof.on) return;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+  }
+  ~PhaseTimer() {
+    if (!a) return;
+    cudaEventRecord(b, s);
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof.ev[phase].emplace_back(a, b);
+  }
+};
+
 }  // namespace
+
+int oz_profile_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof.on = on != 0;
+  return VCPCU_OK;
+}
+
+int oz_profile_read(double* ms, int nphases, long long* flops) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  for (int ph = 0; ph < 4; ++ph) {
+    double tot = 0.0;
+    for (auto& e : g_prof.ev[ph]) {
+      cudaEventSynchronize(e.second);
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e.first, e.second);
+      tot += t;
+      cudaEventDestroy(e.first);
+      cudaEventDestroy(e.second);
+    }
+    g_prof.ev[ph].clear();
+    if (ph < nphases && ms) ms[ph] = tot;
+  }
+  if (flops) *flops = g_prof.flops;
+  g_prof.flops = 0;
+  return VCPCU_OK;
+}
 
 int oz_take_status(cudaStream_t s, int* status) {
   int zero = 0;
@@ -173,10 +229,27 @@ int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B,
   if (st) return st;
   OzWorkspace ws;
   oz_carve_workspace(plan.pb, buf.ptr, &ws);
-  if ((st = oz_prepare(plan.pb, A, lda, B, ldb, ws, s))) return st;
-  if ((st = oz_run_gemm(plan, OZ_RAD_SET, ws, nullptr, 0, s))) return st;
-  if ((st = oz_run_gemm(plan, OZ_RAD_ADD, ws, nullptr, 0, s))) return st;
-  if ((st = oz_run_gemm(plan, OZ_MID, ws, C, ldc, s))) return st;
+  {
+    PhaseTimer t(0, s);
+    if ((st = oz_prepare(plan.pb, A, lda, B, ldb, ws, s))) return st;
+  }
+  {
+    PhaseTimer t(1, s);
+    if ((st = oz_run_gemm(plan, OZ_RAD_SET, ws, nullptr, 0, s))) return st;
+  }
+  {
+    PhaseTimer t(2, s);
+    if ((st = oz_run_gemm(plan, OZ_RAD_ADD, ws, nullptr, 0, s))) return st;
+  }
+  {
+    PhaseTimer t(3, s);
+    if ((st = oz_run_gemm(plan, OZ_MID, ws, C, ldc, s))) return st;
+  }
+  if (g_prof.on) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof.flops += 2LL * m * n * (long long)(k > 0 ? k : 0) *
+                    (plan.mid.npairs + 2LL * plan.rad.npairs);
+  }
   oz_status_merge<<<1, 1, 0, s>>>(ws.flag);
   VCPCU_LAUNCH_CHECK("oz_status_merge");
   return VCPCU_OK;

@@ -87,6 +87,10 @@ int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws);
 // synchronises the stream.
 int oz_take_status(cudaStream_t s, int* status);
 
+// Per-phase timing of the Ozaki form (prep, radius 1, radius 2, midpoint).
+int oz_profile_enable(int on);
+int oz_profile_read(double* ms, int nphases, long long* flops);
+
 int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
                 double* C, long ldc, int form, int slices, cudaStream_t s);
 
