@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-rows", type=int, default=0, help="row sample of the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only-headline", action="store_true",
+                    help="time the headline form only (profiling runs): no plain form, "
+                         "width, containment, e2e or CPU legs")
     return ap.parse_args()
 
 
@@ -270,6 +273,12 @@ def run_ours(args, ws, rank, local):
         tc_flops = int(tc_flops * frac)
     ms_max = max_over_ranks(ms, ws, dev)
     value = ws * 2.0 * n ** 3 / (ms_max * 1e-3) / 1e12
+    if args.only_headline:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": ws * 2.0 * n ** 3 / (ms_max * 1e-3) / 1e12,
+                              "unit": UNIT, "ms_per_step": ms_max, "form": form_name, "n": n,
+                              "only_headline": True}), flush=True)
+        return
     C_head = dC.cpu().numpy().copy()
 
     # plain FP64 form on the same inputs (also the width reference)

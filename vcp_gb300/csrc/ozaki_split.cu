@@ -257,7 +257,7 @@ int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, 
   const int M = pb.M, N = pb.N, K = pb.K;
   VCPCU_CUDA_TRY(cudaMemsetAsync(ws.rowmax, 0, sizeof(unsigned long long) * 3 * (size_t)pb.Mp, st));
   VCPCU_CUDA_TRY(cudaMemsetAsync(ws.delta, 0, sizeof(unsigned long long) * (size_t)pb.Mp, st));
-  VCPCU_CUDA_TRY(cudaMemsetAsync(ws.flag, 0, sizeof(int), st));
+  VCPCU_CUDA_TRY(cudaMemsetAsync(ws.flag, 0, 4 * sizeof(int), st));  // every status word
   if (M > 0 && K > 0) {
     const int cpb = 256;
     dim3 g1((M + 31) / 32, (K + cpb - 1) / cpb);
