@@ -131,6 +131,36 @@ int vcpcu_igemm_dev(int m, int n, int k, const double* A, int lda,
 int vcpcu_igemm(int m, int n, int k, const double* A, const double* B,
                 double* C, int form, int slices);
 
+/* ---- interval GEMM without device allocation ------------------------------ */
+
+/* Size of the static device scratch used by vcpcu_igemm_noalloc_dev. */
+#define VCPCU_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* The Ozaki-form interval product (same kernels and same results as
+ * vcpcu_igemm_dev with form VCPCU_FORM_OZAKI and the same `slices`) for
+ * callers that must not allocate device memory: code running inside a
+ * stream capture that forbids memory nodes, a real-time loop that must not
+ * reach cudaMalloc (it can synchronise the device), a process whose device
+ * memory belongs to another allocator, or an FFI caller that promises no
+ * allocation after start-up.  No counterpart in the reference (the
+ * reference is CPU code and allocates with std::vector).
+ *
+ * Scratch is one static 32 MiB (VCPCU_NOALLOC_SCRATCH_BYTES) device array
+ * that every device loading this library holds until the process exits;
+ * problems whose scratch would exceed it (about m = n = k = 700 with 8
+ * slices) are rejected with VCPCU_ERR_INVALID_ARG.  No cudaMalloc, cudaFree
+ * or allocating library routine is called.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  All
+ * calls share the array: calls whose GPU work overlaps (different streams,
+ * or unordered host threads) race and give wrong results -- order them on
+ * one stream.  Device pointers; stream-ordered; returns before the GPU
+ * finishes.  Non-finite inputs, or a bounded device wait that gave up,
+ * make every output entry NaN. */
+int vcpcu_igemm_noalloc_dev(int m, int n, int k, const double* A, int lda,
+                            const double* B, int ldb, double* C, int ldc,
+                            int slices, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

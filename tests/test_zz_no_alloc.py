@@ -1,0 +1,63 @@
+"""GPU test of vcpcu_igemm_noalloc_dev, the interval product for callers that
+cannot allocate device memory (stream captures that forbid memory nodes,
+real-time loops that must not reach cudaMalloc, processes whose device
+memory belongs to another allocator, FFI callers that promise no
+allocation after start-up).
+
+It is called through the C ABI and compared with vcpcu_igemm_dev (Ozaki
+form, same slice count): the two run the same kernels, so the results must
+be bit-identical -- the tolerance of every Ozaki parity test here.  Two calls
+in a row with different shapes and data check that the shared static scratch
+carries no state from one call into the next.  A problem larger than the
+32 MiB static scratch must be rejected.
+
+This file sorts last so that a run stopping at the first failure has run
+every other test first; it also passes alone in a fresh process.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from vcp_gb300 import workloads as W
+from vcp_gb300.errors import DimensionError
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(x):
+    return np.asarray(x, dtype=np.float64).view(np.int64)
+
+
+def run_both(cuda_lib, m, n, k, slices, seed):
+    import torch
+    from vcp_gb300 import _lib, pidcuda
+    rng = np.random.default_rng(seed)
+    A = torch.from_numpy(W.interval_ephi(rng, m, k, 4, 2.0 ** -40)).cuda()
+    B = torch.from_numpy(W.interval_ephi(rng, k, n, 4, 2.0 ** -40)).cuda()
+    C_ref = torch.full((2 * m * n,), -7.0, dtype=torch.float64, device="cuda")
+    C_new = torch.full((2 * m * n,), 3.0, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    pidcuda.mulmm_dev(m, n, k, A, m, B, k, C_ref, m, pidcuda.FORM_OZAKI, slices)
+    _lib.call("vcpcu_igemm_noalloc_dev", m, n, k, A.data_ptr(), m, B.data_ptr(), k,
+              C_new.data_ptr(), m, slices, s)
+    torch.cuda.synchronize()
+    _lib.call("vcpcu_status", s)
+    return C_ref.cpu().numpy(), C_new.cpu().numpy()
+
+
+def test_noalloc_matches_allocating_entry_point_twice(cuda_lib):
+    ref1, new1 = run_both(cuda_lib, 300, 260, 700, 8, seed=1)
+    assert np.array_equal(bits(new1), bits(ref1))
+    # second call: a different (smaller) problem over the same static scratch
+    ref2, new2 = run_both(cuda_lib, 129, 70, 1100, 6, seed=2)
+    assert np.array_equal(bits(new2), bits(ref2))
+    assert np.all(new2[0::2] <= new2[1::2])
+
+
+def test_noalloc_rejects_problems_beyond_the_static_scratch(cuda_lib):
+    from vcp_gb300 import _lib
+    with pytest.raises(DimensionError, match="static scratch"):
+        # checked before any pointer is touched
+        _lib.call("vcpcu_igemm_noalloc_dev", 4096, 4096, 4096, 16, 4096, 16, 4096, 16, 4096,
+                  8, None)

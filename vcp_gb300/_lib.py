@@ -32,6 +32,7 @@ SIGNATURES: dict[str, tuple] = {
     "vcpcu_udmatmul_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _v, _i, _v]),
     "vcpcu_igemm_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _i, _i, _v]),
     "vcpcu_igemm": (_i, [_i, _i, _i, _v, _v, _v, _i, _i]),
+    "vcpcu_igemm_noalloc_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _i, _v]),
 }
 
 

@@ -1,0 +1,123 @@
+// noalloc.cu -- the Ozaki-form interval product for callers that cannot
+// allocate device memory.
+//
+// Who needs it: code that runs where cudaMalloc / cudaMallocAsync are not
+// allowed or not safe -- a host thread inside a CUDA stream capture of a
+// framework that forbids memory nodes, a real-time loop that must not hit
+// the allocator (cudaMalloc can synchronise the device), a process whose
+// device memory is already owned by another allocator (a framework's
+// caching pool), or an FFI caller whose contract is "no allocation after
+// initialisation".  This entry point runs the same kernels as
+// vcpcu_igemm_dev with form VCPCU_FORM_OZAKI, but takes its scratch from one
+// file-scope static device array instead of the stream-ordered allocator.
+//
+// The array (VCPCU_NOALLOC_SCRATCH_BYTES, 32 MiB) exists on every device
+// that loads this library, for the life of the process.  Every call shares
+// it and it keeps the previous call's contents; each call re-initialises
+// every word that must start at zero (the row maxima, digit sums and status
+// words are cleared on the call's stream, the digit planes, fold buffer and
+// radius bounds are fully overwritten).  Calls whose GPU work overlaps -- on
+// two streams, or from two host threads without ordering -- race on the
+// array and give wrong results: order them on one stream.
+#include "common.cuh"
+#include "ozaki.cuh"
+
+#include <mutex>
+
+namespace vcpcu {
+
+namespace {
+
+// The scratch of every no-allocation call on a device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[VCPCU_NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch per device (host code cannot use the
+// symbol itself: on the host it names a stand-in, not device memory).
+void* g_scratch_ptr[64] = {nullptr};
+std::mutex g_scratch_mu;
+
+int scratch_for_current_device(void** out) {
+  int dev = 0;
+  VCPCU_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("igemm_noalloc: device ordinal %d out of range", dev);
+    return VCPCU_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      set_error("igemm_noalloc: cudaGetSymbolAddress of the static scratch failed: %s",
+                cudaGetErrorString(e));
+      return VCPCU_ERR_CUDA;
+    }
+    g_scratch_ptr[dev] = p;
+  }
+  *out = g_scratch_ptr[dev];
+  return VCPCU_OK;
+}
+
+// After the three slice GEMMs: a timed-out device wait leaves the output
+// unfinished, so every entry becomes NaN (non-finite inputs are already NaN).
+__global__ void noalloc_poison_on_timeout(const int* flag, int m, int n, double* C, long ldc) {
+  if (flag[1] == 0) return;
+  const double nan = __longlong_as_double(0x7ff8000000000000LL);
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < (long)m * n;
+       idx += (long)gridDim.x * blockDim.x) {
+    long i = idx % m, j = idx / m;
+    C[2 * (i + j * ldc)] = nan;
+    C[2 * (i + j * ldc) + 1] = nan;
+  }
+}
+
+}  // namespace
+
+}  // namespace vcpcu
+
+using namespace vcpcu;
+
+extern "C" int vcpcu_igemm_noalloc_dev(int m, int n, int k, const double* A, int lda,
+                                       const double* B, int ldb, double* C, int ldc,
+                                       int slices, void* stream) {
+  clear_error();
+  if (slices != 0 && (slices < 2 || slices > OZ_MAX_SLICES)) {
+    set_error("igemm_noalloc: slices must be 0 or in [2, %d], got %d", OZ_MAX_SLICES, slices);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (m <= 0 || n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (!C || (k > 0 && (!A || !B))) {
+    set_error("igemm_noalloc: null pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (ldc < m || (k > 0 && (lda < m || ldb < k))) {
+    set_error("igemm_noalloc: leading dimension too small (lda %d, ldb %d, ldc %d)", lda, ldb,
+              ldc);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  OzPlan plan;
+  oz_make_plan(m, n, k, slices > 0 ? slices : 8, 2, &plan);
+  const size_t need = oz_workspace_bytes(plan.pb);
+  if (need > (size_t)VCPCU_NOALLOC_SCRATCH_BYTES) {
+    set_error("igemm_noalloc: %d x %d x %d with %d slices needs %zu bytes of scratch, more than "
+              "the %u-byte static scratch; use vcpcu_igemm_dev",
+              m, n, k, plan.pb.s, need, (unsigned)VCPCU_NOALLOC_SCRATCH_BYTES);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  int st = check_device();
+  if (st) return st;
+  void* base = nullptr;
+  if ((st = scratch_for_current_device(&base))) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  OzWorkspace ws;
+  oz_carve_workspace(plan.pb, base, &ws);
+  if ((st = oz_prepare(plan.pb, A, lda, B, ldb, ws, s))) return st;
+  if ((st = oz_run_gemm(plan, OZ_RAD_SET, ws, nullptr, 0, s))) return st;
+  if ((st = oz_run_gemm(plan, OZ_RAD_ADD, ws, nullptr, 0, s))) return st;
+  if ((st = oz_run_gemm(plan, OZ_MID, ws, C, ldc, s))) return st;
+  noalloc_poison_on_timeout<<<64, 256, 0, s>>>(ws.flag, m, n, C, ldc);
+  VCPCU_LAUNCH_CHECK("noalloc_poison_on_timeout");
+  return VCPCU_OK;
+}
