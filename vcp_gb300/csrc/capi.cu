@@ -106,6 +106,12 @@ int igemm_check(int m, int n, int k, const double* A, int lda, const double* B, 
               ldb, ldc, m, k);
     return VCPCU_ERR_INVALID_ARG;
   }
+  if (form != VCPCU_FORM_PLAIN && k > 0 &&
+      (((uintptr_t)A | (uintptr_t)B) & 15) != 0) {
+    set_error("igemm: the Ozaki form reads intervals as 16-byte pairs; A and B must be "
+              "16-byte aligned");
+    return VCPCU_ERR_INVALID_ARG;
+  }
   return VCPCU_OK;
 }
 

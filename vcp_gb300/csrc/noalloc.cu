@@ -97,6 +97,10 @@ extern "C" int vcpcu_igemm_noalloc_dev(int m, int n, int k, const double* A, int
               ldc);
     return VCPCU_ERR_INVALID_ARG;
   }
+  if (k > 0 && (((uintptr_t)A | (uintptr_t)B) & 15) != 0) {
+    set_error("igemm_noalloc: A and B must be 16-byte aligned (intervals are read as pairs)");
+    return VCPCU_ERR_INVALID_ARG;
+  }
   OzPlan plan;
   oz_make_plan(m, n, k, slices > 0 ? slices : 8, 2, &plan);
   const size_t need = oz_workspace_bytes(plan.pb);

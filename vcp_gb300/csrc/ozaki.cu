@@ -178,6 +178,8 @@ size_t oz_workspace_bytes(const OzProblem& pb) {
   b += al256(sizeof(double) * (size_t)pb.Mp * pb.Np);
   b += al256(sizeof(long long) * (size_t)pb.Mp * pb.Np);
   b += al256(sizeof(int) * 4);
+  b += 2 * al256(sizeof(double) * (size_t)pb.M * (pb.K > 0 ? pb.K : 1));
+  b += 2 * al256(sizeof(double) * (size_t)pb.Np * pb.Kp);
   return b;
 }
 
@@ -210,6 +212,15 @@ int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws) {
   ws->W = (long long*)p;
   p += al256(sizeof(long long) * (size_t)pb.Mp * pb.Np);
   ws->flag = (int*)p;
+  p += al256(sizeof(int) * 4);
+  const size_t mk1 = sizeof(double) * (size_t)pb.M * (pb.K > 0 ? pb.K : 1);
+  ws->midA = (double*)p;
+  p += al256(mk1);
+  ws->radA = (double*)p;
+  p += al256(mk1);
+  ws->midB = (double*)p;
+  p += al256(sizeof(double) * (size_t)pb.Np * pb.Kp);
+  ws->radB = (double*)p;
   return VCPCU_OK;
 }
 

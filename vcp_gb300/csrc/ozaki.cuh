@@ -29,6 +29,8 @@ struct OzWorkspace {
   unsigned long long* delta;          // [Mp] sum of |midpoint digits| per row
   int* F2;                            // [Np][2] exponents Fm, Fr
   double* beta;                       // [Np] sum_k |mB(k,j)| rounded up
+  double *midA, *radA;                // [K][M] midpoints / radii of A (column-major)
+  double *midB, *radB;                // [Np][Kp] midpoints / radii of B (k contiguous)
   double* T;                          // [N][Mp] upper bound of the radius product
   long long* W;                       // [Np][Mp] int64 fold buffer
   int* flag;                          // [0] non-finite input, [1] device wait timeout

@@ -34,12 +34,50 @@ __device__ __forceinline__ unsigned long long dbits(double x) {
   return (unsigned long long)__double_as_longlong(x);
 }
 
+// bf16 bit pattern of an integer digit |d| <= 256 (exact: the float has at
+// most 9 significant bits, so its low 16 bits are zero).
+__device__ __forceinline__ uint32_t bf16_bits(int d) {
+  return __float_as_uint(__int2float_rn(d)) >> 16;
+}
+
+template <int S>
+__device__ __forceinline__ void digits_of(double x, int E, int up, int (&d)[S]) {
+  if (E == OZ_ZERO_EXP || x == 0.0) {
+#pragma unroll
+    for (int q = 0; q < S; ++q) d[q] = 0;
+    return;
+  }
+  const __int128 N = oz_scaled_int(x, E, S, up);
+  if (S <= 7) {
+    long long n = (long long)N;
+#pragma unroll
+    for (int p = S - 1; p >= 1; --p) {
+      const int lo = (int)((unsigned long long)(n + 128) & 255ULL) - 128;
+      d[p] = lo;
+      n = (n - lo) >> 8;
+    }
+    d[0] = (int)n;
+  } else {
+    __int128 n = N;
+#pragma unroll
+    for (int p = S - 1; p >= 1; --p) {
+      const int lo = (int)((unsigned long long)(n + 128) & 255ULL) - 128;
+      d[p] = lo;
+      n = (n - lo) >> 8;
+    }
+    d[0] = (int)n;
+  }
+}
+
 // ---------------------------------------------------------------- left factor
-// Row maxima of |mA|, P and rA as double bit patterns (non-negative doubles
-// order like their bit patterns).  Block: 32 rows x 8 column phases.
-__global__ void oz_rowmax_left(int M, int K, const double* __restrict__ A, long lda,
-                               int cols_per_block, unsigned long long* __restrict__ mx,
-                               int* __restrict__ flag) {
+// Pass 1: kv midrad of every entry, stored as the planes mA, rA (column-major,
+// ld = M), and the row maxima of |mA|, P = |mA| +ru rA and rA as double bit
+// patterns (non-negative doubles order like their bit patterns).
+// Block: 32 rows x 8 column phases over a column range.
+__global__ void __launch_bounds__(256)
+oz_rowmax_left(int M, int K, const double* __restrict__ A, long lda, int cols_per_block,
+               double* __restrict__ mA, double* __restrict__ rA,
+               unsigned long long* __restrict__ mx, int* __restrict__ flag) {
   __shared__ unsigned long long red[3][32];
   const int lane = threadIdx.x & 31, ph = threadIdx.x >> 5;
   const int i = blockIdx.x * 32 + lane;
@@ -51,18 +89,19 @@ __global__ void oz_rowmax_left(int M, int K, const double* __restrict__ A, long 
     const int c0 = blockIdx.y * cols_per_block;
     const int c1 = min(K, c0 + cols_per_block);
     for (int c = c0 + ph; c < c1; c += 8) {
-      const double* e = A + 2 * (i + (long)c * lda);
-      double lo = e[0], up = e[1];
-      if (!isfinite(lo) || !isfinite(up)) {
+      const double2 e = *reinterpret_cast<const double2*>(A + 2 * (i + (long)c * lda));
+      double m = 0.0, r = 0.0;
+      if (isfinite(e.x) && isfinite(e.y)) {
+        oz_midrad(e.x, e.y, m, r);
+        const double p = __dadd_ru(fabs(m), r);
+        am = max(am, dbits(fabs(m)));
+        ap = max(ap, dbits(p));
+        ar = max(ar, dbits(r));
+      } else {
         bad = true;
-        continue;
       }
-      double m, r;
-      oz_midrad(lo, up, m, r);
-      double p = __dadd_ru(fabs(m), r);
-      am = max(am, dbits(fabs(m)));
-      ap = max(ap, dbits(p));
-      ar = max(ar, dbits(r));
+      mA[i + (long)c * M] = m;
+      rA[i + (long)c * M] = r;
     }
   }
   if (bad) atomicOr(flag, 1);
@@ -82,19 +121,22 @@ __global__ void oz_exponents(int R, const unsigned long long* __restrict__ mx, i
                              int* __restrict__ E) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= R) return;
-  for (int t = 0; t < nper; ++t) E[nper * i + t] = oz_exponent(__longlong_as_double((long long)mx[nper * i + t]));
+  for (int t = 0; t < nper; ++t)
+    E[nper * i + t] = oz_exponent(__longlong_as_double((long long)mx[nper * i + t]));
 }
 
-// Digit planes of the left factor.  Block: 32 rows x 64 k, 256 threads;
-// digits are staged in shared memory and written K-contiguous (transpose).
-constexpr int LT_R = 32, LT_K = 64;
+// Pass 2: digit planes of the left factor from the stored mA, rA.  Block:
+// 32 rows x 64 k, 256 threads; digits are staged in shared memory and
+// written K-contiguous (a transpose), 16 bytes per store.
+constexpr int LT_R = 32, LT_K = 64, LT_KS = LT_K + 2;  // padded row: no bank conflicts
+template <int S, int SR>
 __global__ void __launch_bounds__(256)
-oz_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long lda, int s,
-              int sr, const int* __restrict__ E3, uint16_t* __restrict__ planes_m,
-              uint16_t* __restrict__ planes_p, uint16_t* __restrict__ planes_r,
-              unsigned long long* __restrict__ delta) {
-  extern __shared__ int16_t sd[];  // digits [plane][LT_R][LT_K], values in [-128, 128]
-  const int np = s + 2 * sr;
+oz_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
+              const double* __restrict__ rA, const int* __restrict__ E3,
+              uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_p,
+              uint16_t* __restrict__ planes_r, unsigned long long* __restrict__ delta) {
+  extern __shared__ int16_t sd[];  // digits [plane][LT_R][LT_KS], values in [-128, 128]
+  constexpr int s = S, sr = SR, np = S + 2 * SR;
   const int tid = threadIdx.x;
   const int r = tid % LT_R, kph = tid / LT_R;  // 8 k phases
   const int i = blockIdx.y * LT_R + r;
@@ -106,41 +148,27 @@ oz_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long l
     Er = E3[3 * i + 2];
   }
   unsigned dsum = 0;
-  int d[OZ_MAX_SLICES];
+  int d[S], dr[SR];
   for (int kk = kph; kk < LT_K; kk += 8) {
     const int k = k0 + kk;
     double m = 0.0, rr = 0.0, p = 0.0;
     if (i < M && k < K) {
-      const double* e = A + 2 * (i + (long)k * lda);
-      double lo = e[0], up = e[1];
-      if (isfinite(lo) && isfinite(up)) {
-        oz_midrad(lo, up, m, rr);
-        p = __dadd_ru(fabs(m), rr);
-      }
+      m = mA[i + (long)k * M];
+      rr = rA[i + (long)k * M];
+      p = __dadd_ru(fabs(m), rr);
     }
-    // midpoint digits (two-sided)
-    if (Em != OZ_ZERO_EXP && m != 0.0) {
-      oz_digits(oz_scaled_int(m, Em, s, 0), s, d);
-    } else {
-      for (int q = 0; q < s; ++q) d[q] = 0;
-    }
+    digits_of<S>(m, Em, 0, d);
+#pragma unroll
     for (int q = 0; q < s; ++q) {
-      sd[(q * LT_R + r) * LT_K + kk] = (int16_t)d[q];
+      sd[(q * LT_R + r) * LT_KS + kk] = (int16_t)d[q];
       dsum += (unsigned)abs(d[q]);
     }
-    // radius factors (upward digits)
-    if (Ep != OZ_ZERO_EXP && p != 0.0) {
-      oz_digits(oz_scaled_int(p, Ep, sr, 1), sr, d);
-    } else {
-      for (int q = 0; q < sr; ++q) d[q] = 0;
-    }
-    for (int q = 0; q < sr; ++q) sd[((s + q) * LT_R + r) * LT_K + kk] = (int16_t)d[q];
-    if (Er != OZ_ZERO_EXP && rr != 0.0) {
-      oz_digits(oz_scaled_int(rr, Er, sr, 1), sr, d);
-    } else {
-      for (int q = 0; q < sr; ++q) d[q] = 0;
-    }
-    for (int q = 0; q < sr; ++q) sd[((s + sr + q) * LT_R + r) * LT_K + kk] = (int16_t)d[q];
+    digits_of<SR>(p, Ep, 1, dr);
+#pragma unroll
+    for (int q = 0; q < sr; ++q) sd[((s + q) * LT_R + r) * LT_KS + kk] = (int16_t)dr[q];
+    digits_of<SR>(rr, Er, 1, dr);
+#pragma unroll
+    for (int q = 0; q < sr; ++q) sd[((s + sr + q) * LT_R + r) * LT_KS + kk] = (int16_t)dr[q];
   }
   // per-row digit magnitude sum (midpoint slices)
   __shared__ unsigned rsum[LT_R];
@@ -166,23 +194,27 @@ oz_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long l
       base = planes_r;
       pl = q - s - sr;
     }
+    const int16_t* src = sd + (q * LT_R + wr) * LT_KS + wk;
     uint4 v;
-    uint16_t h[8];
-#pragma unroll
-    for (int t = 0; t < 8; ++t) h[t] = oz_bf16_of_int(sd[(q * LT_R + wr) * LT_K + wk + t]);
-    v.x = h[0] | ((uint32_t)h[1] << 16);
-    v.y = h[2] | ((uint32_t)h[3] << 16);
-    v.z = h[4] | ((uint32_t)h[5] << 16);
-    v.w = h[6] | ((uint32_t)h[7] << 16);
+    v.x = bf16_bits(src[0]) | (bf16_bits(src[1]) << 16);
+    v.y = bf16_bits(src[2]) | (bf16_bits(src[3]) << 16);
+    v.z = bf16_bits(src[4]) | (bf16_bits(src[5]) << 16);
+    v.w = bf16_bits(src[6]) | (bf16_bits(src[7]) << 16);
     if (gi < Mp) *reinterpret_cast<uint4*>(base + ((size_t)pl * Mp + gi) * Kp + k0 + wk) = v;
   }
 }
 
 // --------------------------------------------------------------- right factor
-// One block per column j < Np: maxima, beta_j, exponents and digit planes.
+// One block per column j < Np.  Pass 1 (thread t takes k = t, t+256, ...):
+// midrad into the planes mB, rB (k contiguous), the column maxima and
+// beta_j = RU sum |mB| (per-thread chains, then a pairwise tree).  Pass 2
+// (thread t takes 8 consecutive k): digits from the stored planes, 16-byte
+// stores.
+template <int S, int SR>
 __global__ void __launch_bounds__(256)
-oz_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb, int s,
-               int sr, uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_r,
+oz_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb,
+               double* __restrict__ mBp, double* __restrict__ rBp,
+               uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_r,
                uint16_t* __restrict__ planes_s, int* __restrict__ F2,
                double* __restrict__ beta, int* __restrict__ flag) {
   const int j = blockIdx.x;
@@ -194,19 +226,22 @@ oz_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
   unsigned long long am = 0, ar = 0;
   double bsum = 0.0;
   bool bad = false;
+  double* mcol = mBp + (size_t)j * Kp;
+  double* rcol = rBp + (size_t)j * Kp;
   if (j < N) {
     for (int k = tid; k < K; k += 256) {
-      const double* e = B + 2 * (k + (long)j * ldb);
-      double lo = e[0], up = e[1];
-      if (!isfinite(lo) || !isfinite(up)) {
+      const double2 e = *reinterpret_cast<const double2*>(B + 2 * (k + (long)j * ldb));
+      double m = 0.0, r = 0.0;
+      if (isfinite(e.x) && isfinite(e.y)) {
+        oz_midrad(e.x, e.y, m, r);
+        am = max(am, dbits(fabs(m)));
+        ar = max(ar, dbits(r));
+        bsum = __dadd_ru(bsum, fabs(m));
+      } else {
         bad = true;
-        continue;
       }
-      double m, r;
-      oz_midrad(lo, up, m, r);
-      am = max(am, dbits(fabs(m)));
-      ar = max(ar, dbits(r));
-      bsum = __dadd_ru(bsum, fabs(m));
+      mcol[k] = m;
+      rcol[k] = r;
     }
   }
   if (bad) atomicOr(flag, 1);
@@ -225,33 +260,71 @@ oz_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
     F2[2 * j + 1] = Fr;
     beta[j] = ssum[0];
   }
-  int d[OZ_MAX_SLICES];
-  for (int k = tid; k < Kp; k += 256) {
-    double m = 0.0, r = 0.0;
-    if (j < N && k < K) {
-      const double* e = B + 2 * (k + (long)j * ldb);
-      double lo = e[0], up = e[1];
-      if (isfinite(lo) && isfinite(up)) oz_midrad(lo, up, m, r);
+  // pass 2: the planes written above by this block are visible after the
+  // barriers of the reduction
+  constexpr int s = S, sr = SR;
+  int d[S], dr[SR];
+  uint32_t hm[S][4], hr[SR][4], hs[SR][4];
+  for (int k0 = tid * 8; k0 < Kp; k0 += 256 * 8) {
+#pragma unroll
+    for (int h = 0; h < 8; ++h) {
+      const int k = k0 + h;
+      double m = 0.0, r = 0.0;
+      if (j < N && k < K) {
+        m = mcol[k];
+        r = rcol[k];
+      }
+      digits_of<S>(m, Fm, 0, d);
+#pragma unroll
+      for (int q = 0; q < s; ++q) {
+        const uint32_t b = bf16_bits(d[q]);
+        if (h & 1) hm[q][h >> 1] |= b << 16; else hm[q][h >> 1] = b;
+      }
+      digits_of<SR>(r, Fr, 1, dr);
+#pragma unroll
+      for (int q = 0; q < sr; ++q) {
+        const uint32_t b = bf16_bits(dr[q]);
+        if (h & 1) hr[q][h >> 1] |= b << 16; else hr[q][h >> 1] = b;
+      }
+      digits_of<SR>(fabs(m), Fm, 1, dr);
+#pragma unroll
+      for (int q = 0; q < sr; ++q) {
+        const uint32_t b = bf16_bits(dr[q]);
+        if (h & 1) hs[q][h >> 1] |= b << 16; else hs[q][h >> 1] = b;
+      }
     }
-    if (Fm != OZ_ZERO_EXP && m != 0.0)
-      oz_digits(oz_scaled_int(m, Fm, s, 0), s, d);
-    else
-      for (int q = 0; q < s; ++q) d[q] = 0;
-    for (int q = 0; q < s; ++q) planes_m[((size_t)q * Np + j) * Kp + k] = oz_bf16_of_int(d[q]);
-    if (Fr != OZ_ZERO_EXP && r != 0.0)
-      oz_digits(oz_scaled_int(r, Fr, sr, 1), sr, d);
-    else
-      for (int q = 0; q < sr; ++q) d[q] = 0;
-    for (int q = 0; q < sr; ++q) planes_r[((size_t)q * Np + j) * Kp + k] = oz_bf16_of_int(d[q]);
-    if (Fm != OZ_ZERO_EXP && m != 0.0)
-      oz_digits(oz_scaled_int(fabs(m), Fm, sr, 1), sr, d);
-    else
-      for (int q = 0; q < sr; ++q) d[q] = 0;
-    for (int q = 0; q < sr; ++q) planes_s[((size_t)q * Np + j) * Kp + k] = oz_bf16_of_int(d[q]);
+#pragma unroll
+    for (int q = 0; q < s; ++q)
+      *reinterpret_cast<uint4*>(planes_m + ((size_t)q * Np + j) * Kp + k0) =
+          make_uint4(hm[q][0], hm[q][1], hm[q][2], hm[q][3]);
+#pragma unroll
+    for (int q = 0; q < sr; ++q) {
+      *reinterpret_cast<uint4*>(planes_r + ((size_t)q * Np + j) * Kp + k0) =
+          make_uint4(hr[q][0], hr[q][1], hr[q][2], hr[q][3]);
+      *reinterpret_cast<uint4*>(planes_s + ((size_t)q * Np + j) * Kp + k0) =
+          make_uint4(hs[q][0], hs[q][1], hs[q][2], hs[q][3]);
+    }
   }
 }
 
 // ------------------------------------------------------------------ launchers
+template <int S, int SR>
+int launch_splits(const OzProblem& pb, const double* B, long ldb, OzWorkspace& ws,
+                  cudaStream_t st) {
+  dim3 g2(pb.Kp / LT_K, pb.Mp / LT_R);
+  const size_t shm = sizeof(int16_t) * (size_t)(S + 2 * SR) * LT_R * LT_KS;
+  VCPCU_CUDA_TRY(cudaFuncSetAttribute(oz_split_left<S, SR>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+  oz_split_left<S, SR><<<g2, 256, shm, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, ws.E3,
+                                             ws.a_mid, ws.a_p, ws.a_r, ws.delta);
+  VCPCU_LAUNCH_CHECK("oz_split_left");
+  oz_split_right<S, SR><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, ws.midB,
+                                               ws.radB, ws.b_mid, ws.b_r, ws.b_s, ws.F2,
+                                               ws.beta, ws.flag);
+  VCPCU_LAUNCH_CHECK("oz_split_right");
+  return VCPCU_OK;
+}
+
 int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, long ldb,
                OzWorkspace& ws, cudaStream_t st) {
   const int M = pb.M, N = pb.N, K = pb.K;
@@ -261,23 +334,30 @@ int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, 
   if (M > 0 && K > 0) {
     const int cpb = 256;
     dim3 g1((M + 31) / 32, (K + cpb - 1) / cpb);
-    oz_rowmax_left<<<g1, 256, 0, st>>>(M, K, A, lda, cpb, ws.rowmax, ws.flag);
+    oz_rowmax_left<<<g1, 256, 0, st>>>(M, K, A, lda, cpb, ws.midA, ws.radA, ws.rowmax, ws.flag);
     VCPCU_LAUNCH_CHECK("oz_rowmax_left");
   }
   oz_exponents<<<(pb.Mp + 255) / 256, 256, 0, st>>>(pb.Mp, ws.rowmax, 3, ws.E3);
   VCPCU_LAUNCH_CHECK("oz_exponents");
-  {
-    dim3 g2(pb.Kp / LT_K, pb.Mp / LT_R);
-    const size_t shm = sizeof(int16_t) * (size_t)(pb.s + 2 * pb.sr) * LT_R * LT_K;
-    VCPCU_CUDA_TRY(cudaFuncSetAttribute(oz_split_left, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)shm));
-    oz_split_left<<<g2, 256, shm, st>>>(M, K, pb.Mp, pb.Kp, A, lda, pb.s, pb.sr, ws.E3,
-                                        ws.a_mid, ws.a_p, ws.a_r, ws.delta);
-    VCPCU_LAUNCH_CHECK("oz_split_left");
+  if (pb.sr != 2) {
+    set_error("Ozaki form: radius slice count %d is not built (2 is)", pb.sr);
+    return VCPCU_ERR_UNSUPPORTED;
   }
-  oz_split_right<<<pb.Np, 256, 0, st>>>(K, N, pb.Kp, pb.Np, B, ldb, pb.s, pb.sr, ws.b_mid,
-                                        ws.b_r, ws.b_s, ws.F2, ws.beta, ws.flag);
-  VCPCU_LAUNCH_CHECK("oz_split_right");
+  int st_ = VCPCU_OK;
+  switch (pb.s) {
+#define OZ_SPLIT_CASE(S)                                                          \
+  case S:                                                                         \
+    st_ = launch_splits<S, 2>(pb, B, ldb, ws, st);                                \
+    break;
+    OZ_SPLIT_CASE(2) OZ_SPLIT_CASE(3) OZ_SPLIT_CASE(4) OZ_SPLIT_CASE(5) OZ_SPLIT_CASE(6)
+    OZ_SPLIT_CASE(7) OZ_SPLIT_CASE(8) OZ_SPLIT_CASE(9) OZ_SPLIT_CASE(10) OZ_SPLIT_CASE(11)
+    OZ_SPLIT_CASE(12)
+#undef OZ_SPLIT_CASE
+    default:
+      set_error("Ozaki form: slice count %d outside [2, 12]", pb.s);
+      return VCPCU_ERR_INVALID_ARG;
+  }
+  if (st_) return st_;
   return VCPCU_OK;
 }
 
