@@ -74,6 +74,19 @@ __device__ __forceinline__ double pow2_ru(int e) {
   return __longlong_as_double(1LL);
 }
 
+// Tile order: groups of OZ_RASTER row blocks, column blocks outer inside a
+// group, so the CTAs resident at one time share a few A row panels and
+// B column panels (both stay in L2 across the CTAs of one group).
+constexpr int OZ_RASTER = 16;
+__device__ __forceinline__ void tile_coords(int tile, int tiles_m, int tiles_n, int& tm, int& tn) {
+  const int per_group = OZ_RASTER * tiles_n;
+  const int g = tile / per_group;
+  const int rows = min(OZ_RASTER, tiles_m - g * OZ_RASTER);
+  const int idx = tile - g * per_group;
+  tn = idx / rows;
+  tm = g * OZ_RASTER + idx % rows;
+}
+
 __device__ __forceinline__ long long shift_t(int c, int sh) {
   const long long v = (long long)c;
   return sh >= 0 ? (v << sh) : (v >> (-sh));
@@ -123,7 +136,8 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
       bool ok = true;
       uint32_t used = 0, lastpar = 0;  // per-stage bit masks
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int tm = tile % args.tiles_m, tn = tile / args.tiles_m;
+        int tm, tn;
+        tile_coords(tile, args.tiles_m, args.tiles_n, tm, tn);
         for (int pi = 0; pi < args.pl.npairs && ok; ++pi) {
           const int pa = args.pl.pa[pi], pb = args.pl.pb[pi];
           for (int kb = 0; kb < kblocks; ++kb) {
@@ -213,7 +227,8 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
     bool ok = true;
     bool nonfinite = args.flag[0] != 0;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-      const int tm = tile % args.tiles_m, tn = tile / args.tiles_m;
+      int tm, tn;
+        tile_coords(tile, args.tiles_m, args.tiles_n, tm, tn);
       const int gi = tm * OZ_BM + row_in_tile;
       const int gj0 = tn * OZ_BN + half * 128;
       bool have_w = false;
