@@ -45,6 +45,7 @@ extern "C" {
 #define VCPCU_FORM_PLAIN 0   /* FP64 CUDA cores, __fma_rd/__fma_ru, pidblas order   */
 #define VCPCU_FORM_OZAKI 1   /* error-free bf16 slices on tcgen05 tensor cores       */
 #define VCPCU_FORM_AUTO  2   /* autotuned choice of form and slice count            */
+#define VCPCU_FORM_OZAKI_SLICES 3 /* tensor cores, midpoint by triangular slice pairs */
 
 /* ---- diagnostics ----------------------------------------------------------- */
 
@@ -116,9 +117,17 @@ int vcpcu_udmatmul_dev(int m, int n, int k, const double* A, int lda,
  *     whose every entry is the ascending sequential FMA chain (vblas
  *     rmatmul): lC = RD(mA*mB), uC = RU(mA*mB), T = RU((|mA|+rA)*rB) +RU
  *     RU(rA*|mB|), uC +=RU T, lC -=RD T.  `slices` is ignored.
- *   form == VCPCU_FORM_OZAKI: midpoint product from `slices` error-free
- *     bf16 slices per operand (2 <= slices <= 12; 0 = default), radius and
- *     truncation bounds rounded upward; requires finite inputs.
+ *   form == VCPCU_FORM_OZAKI: tensor-core form.  The midpoints are scaled
+ *     per row / column to w = 7 * slices bit integers (2 <= slices <= 12;
+ *     0 = default 8, w = 56); their product is exact, from residues modulo
+ *     up to 16 moduli <= 256 (one bf16 GEMM each, Chinese remaindering);
+ *     the rounding of the midpoints to w bits, the radius term (upward bf16
+ *     digit slices) and the final roundings are bounded upward.  Requires
+ *     finite inputs (NaN results and VCPCU_ERR_NONFINITE otherwise) and
+ *     16-byte aligned A and B.
+ *   form == VCPCU_FORM_OZAKI_SLICES: as OZAKI, but the midpoint product is
+ *     the triangular sum of `slices` balanced 8-bit digit slices per operand
+ *     (the classic Ozaki splitting) with a rigorous truncation bound.
  *   form == VCPCU_FORM_AUTO: the autotuner picks the form and slice count.
  * Device pointers; stream-ordered; scratch comes from the stream-ordered
  * allocator of the current device. */
@@ -147,8 +156,8 @@ int vcpcu_igemm(int m, int n, int k, const double* A, const double* B,
  *
  * Scratch is one static 32 MiB (VCPCU_NOALLOC_SCRATCH_BYTES) device array
  * that every device loading this library holds until the process exits;
- * problems whose scratch would exceed it (about m = n = k = 700 with 8
- * slices) are rejected with VCPCU_ERR_INVALID_ARG.  No cudaMalloc, cudaFree
+ * problems whose scratch would exceed it (about m = n = k = 400 at the
+ * default precision) are rejected with VCPCU_ERR_INVALID_ARG.  No cudaMalloc, cudaFree
  * or allocating library routine is called.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that
  * device current; make that first call before any stream capture.  All

@@ -35,6 +35,8 @@ def lib() -> C.CDLL:
         L.orc_exact_sum.restype = C.c_double
         L.orc_ozaki_igemm.argtypes = [_i, _i, _i, _v, _v, _v, _i, _i]
         L.orc_ozaki_igemm.restype = _i
+        L.orc_ozaki2_igemm.argtypes = [_i, _i, _i, _v, _v, _v, _i, _i]
+        L.orc_ozaki2_igemm.restype = _i
         _lib = L
     return _lib
 
@@ -100,12 +102,14 @@ def exact_dot(m, n, k, A, B, rows, cols, threads=0):
     return dn, up
 
 
-def ozaki_igemm(m, n, k, A, B, s=8, sr=2):
+def ozaki_igemm(m, n, k, A, B, s=8, sr=2, crt=True):
     """Host model of the Ozaki-form interval product (kv buffers, GEMM
-    naming).  Returns (C kv buffer, status) -- status 3 on non-finite input."""
+    naming): crt=True the CRT form (GPU form OZAKI), crt=False the slice form
+    (GPU form OZAKI_SLICES).  Returns (C kv buffer, status) -- status 3 on
+    non-finite input."""
     C_ = np.zeros(2 * m * n, dtype=np.float64)
-    st = lib().orc_ozaki_igemm(m, n, k, _p(A) if k > 0 else None, _p(B) if k > 0 else None,
-                               _p(C_), int(s), int(sr))
+    fn = lib().orc_ozaki2_igemm if crt else lib().orc_ozaki_igemm
+    st = fn(m, n, k, _p(A) if k > 0 else None, _p(B) if k > 0 else None, _p(C_), int(s), int(sr))
     return C_, st
 
 

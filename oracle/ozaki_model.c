@@ -64,7 +64,7 @@ static int oz_exponent(double amax) {
   return be - 1021;
 }
 
-static __int128 oz_scaled_int(double x, int E, int s, int up) {
+static __int128 oz_scaled_int_bits(double x, int E, int bits, int up) {
   uint64_t b = dbits(x);
   int neg = (int)(b >> 63), be = (int)((b >> 52) & 0x7ff);
   uint64_t mant = b & ((1ULL << 52) - 1);
@@ -76,7 +76,7 @@ static __int128 oz_scaled_int(double x, int E, int s, int up) {
     mant |= 1ULL << 52;
     ex = be - 1075;
   }
-  int sh = ex + 8 * s - E;
+  int sh = ex + bits - E;
   unsigned __int128 N;
   if (sh >= 0) {
     N = (unsigned __int128)mant << sh;
@@ -104,6 +104,10 @@ static __int128 oz_scaled_int(double x, int E, int s, int up) {
     N = q;
   }
   return neg ? -(__int128)N : (__int128)N;
+}
+
+static __int128 oz_scaled_int(double x, int E, int s, int up) {
+  return oz_scaled_int_bits(x, E, 8 * s, up);
 }
 
 static void oz_digits(__int128 N, int s, int* d) {
@@ -235,13 +239,67 @@ static void choose_scaling(const pairlist* pl, int nchunks, int* t_ref, int* R) 
 
 static long long shift_t(long long c, int sh) { return sh >= 0 ? (c << sh) : (c >> (-sh)); }
 
+/* CRT form: integer bits w per operand for precision parameter s (w = 7 s,
+ * lowered while 16 moduli cannot hold K 2^(2w-1)); the moduli are those of
+ * the GPU form (pairwise coprime, <= 256). */
+static const int OZ_MOD[16] = {256, 255, 253, 251, 247, 241, 239, 233,
+                               229, 227, 223, 217, 211, 199, 197, 193};
+static int crt_bits(int K, int s) {
+  int w = 7 * s;
+  const int Keff = K > 1 ? K : 1;
+  for (;;) {
+    double need = (2.0 * w - 1.0) + log2((double)Keff) + 0.01, bits = 0.0;
+    int L = 0;
+    while (L < 16 && bits <= need) bits += log2((double)OZ_MOD[L++]);
+    if (bits > need) return w;
+    --w;
+  }
+}
+
+/* RD and RU of (-1)^neg * mag * 2^e for an unsigned 128-bit mag, the same
+ * two steps as the GPU: the top 64 bits with a sticky bit, converted in the
+ * direction, then scaled in the direction. */
+static void big_to_dir(unsigned __int128 mag, int neg, int e, double* lo, double* up) {
+  if (mag == 0) {
+    *lo = *up = 0.0;
+    return;
+  }
+  int bl = 0;
+  for (unsigned __int128 t = mag; t; t >>= 1) ++bl;
+  unsigned long long t;
+  int sh = 0;
+  if (bl <= 64) {
+    t = (unsigned long long)mag;
+  } else {
+    sh = bl - 64;
+    t = (unsigned long long)(mag >> sh);
+    if (mag & ((((unsigned __int128)1) << sh) - 1)) t |= 1ULL;
+  }
+  volatile unsigned long long vt = t;
+  fesetround(FE_DOWNWARD);
+  volatile double a_dn = (double)vt;
+  fesetround(FE_UPWARD);
+  volatile double a_up = (double)vt;
+  fesetround(FE_TONEAREST);
+  if (!neg) {
+    *lo = scale_dir(a_dn, e + sh, 0);
+    *up = scale_dir(a_up, e + sh, 1);
+  } else {
+    *lo = -scale_dir(a_up, e + sh, 1);
+    *up = -scale_dir(a_dn, e + sh, 0);
+  }
+}
+
 /*
  * The whole Ozaki-form product: C (m x n, kv layout, ld m) = [A] (m x k) *
- * [B] (k x n), s midpoint slices, sr radius slices.  Digits (in [-128, 128])
- * are kept as int16.  Returns 0, or 3 on non-finite input (result NaN).
+ * [B] (k x n), precision s, sr radius slices.  crt == 0: the midpoint is the
+ * triangular sum of s digit slices; crt != 0: the midpoint is the exact
+ * product of w-bit integers (what the GPU recovers from its residues).
+ * Digits (in [-128, 128]) are kept as int16.  Returns 0, or 3 on non-finite
+ * input (result NaN).
  */
-int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, double* Cout, int s,
-                    int sr) {
+static int ozaki_model(int m, int n, int k, const double* A, const double* B, double* Cout,
+                       int s, int sr, int crt) {
   const int prev = fegetround();
   fesetround(FE_TONEAREST);
   const int Kp = k <= 0 ? 64 : (k + 63) / 64 * 64;
@@ -281,7 +339,7 @@ int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, doubl
     int d[OZ_MAXS];
     for (int p = 0; p < k; ++p) {
       long t = i + (long)p * m;
-      if (Em[i] != OZ_ZERO_EXP && mA[t] != 0.0) {
+      if (!crt && Em[i] != OZ_ZERO_EXP && mA[t] != 0.0) {
         oz_digits(oz_scaled_int(mA[t], Em[i], s, 0), s, d);
         for (int q = 0; q < s; ++q) {
           dAm[((size_t)q * m + i) * Kp + p] = (int16_t)d[q];
@@ -297,6 +355,27 @@ int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, doubl
         for (int q = 0; q < sr; ++q) dAr[((size_t)q * m + i) * Kp + p] = (int16_t)d[q];
       }
     }
+  }
+  const int wbits = crt ? crt_bits(k, s) : 0;
+  long long* Ai = NULL;      /* A' (m x k, row-major per row i) */
+  unsigned long long* Ahi = NULL, *Alo = NULL;
+  long long* Bi = NULL;      /* B' (column j contiguous) */
+  if (crt) {
+    const int kk1 = k > 0 ? k : 1;
+    Ai = calloc((size_t)m * kk1, sizeof(long long));
+    Ahi = calloc(m, sizeof(unsigned long long));
+    Alo = calloc(m, sizeof(unsigned long long));
+    Bi = calloc((size_t)n * kk1, sizeof(long long));
+    for (int i = 0; i < m; ++i)
+      for (int p = 0; p < k; ++p) {
+        const double x = mA[i + (long)p * m];
+        long long a = (Em[i] == OZ_ZERO_EXP || x == 0.0)
+                          ? 0 : (long long)oz_scaled_int_bits(x, Em[i], wbits, 0);
+        Ai[(size_t)i * kk1 + p] = a;
+        unsigned long long ua = (unsigned long long)(a < 0 ? -a : a);
+        Ahi[i] += ua >> 32;
+        Alo[i] += ua & 0xffffffffULL;
+      }
   }
   /* --- right factor --------------------------------------------------- */
   int* Fm = malloc(sizeof(int) * n);
@@ -332,8 +411,12 @@ int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, doubl
     int d[OZ_MAXS];
     for (int p = 0; p < k; ++p) {
       if (Fm[j] != OZ_ZERO_EXP && mcol[p] != 0.0) {
-        oz_digits(oz_scaled_int(mcol[p], Fm[j], s, 0), s, d);
-        for (int q = 0; q < s; ++q) dBm[((size_t)q * n + j) * Kp + p] = (int16_t)d[q];
+        if (!crt) {
+          oz_digits(oz_scaled_int(mcol[p], Fm[j], s, 0), s, d);
+          for (int q = 0; q < s; ++q) dBm[((size_t)q * n + j) * Kp + p] = (int16_t)d[q];
+        } else {
+          Bi[(size_t)j * (k > 0 ? k : 1) + p] = (long long)oz_scaled_int_bits(mcol[p], Fm[j], wbits, 0);
+        }
         oz_digits(oz_scaled_int(fabs(mcol[p]), Fm[j], sr, 1), sr, d);
         for (int q = 0; q < sr; ++q) dBs[((size_t)q * n + j) * Kp + p] = (int16_t)d[q];
       }
@@ -402,7 +485,19 @@ int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, doubl
       }
       double mlo = 0.0, mup = 0.0, tr = 0.0;
       int z = Em[i] == OZ_ZERO_EXP || Fm[j] == OZ_ZERO_EXP;
-      if (!z) {
+      if (!z && crt) {
+        const int kk1 = k > 0 ? k : 1;
+        __int128 X = 0;
+        for (int p = 0; p < k; ++p)
+          X += (__int128)Ai[(size_t)i * kk1 + p] * (__int128)Bi[(size_t)j * kk1 + p];
+        int neg = X < 0;
+        unsigned __int128 mag = (unsigned __int128)(neg ? -X : X);
+        big_to_dir(mag, neg, Em[i] + Fm[j] - 2 * wbits, &mlo, &mup);
+        double sA = fma_ru((double)Ahi[i], 0x1p32, (double)Alo[i]);
+        double t1 = scale_dir(beta[j], Em[i] - wbits - 1, 1);
+        double t2 = scale_dir(sA, Em[i] + Fm[j] - 2 * wbits - 1, 1);
+        tr = add_dir(t1, t2, FE_UPWARD);
+      } else if (!z) {
         int ex = Em[i] + Fm[j] - 8 * tm;
         mlo = scale_dir(ll2d(W[2], 0), ex, 0);
         mup = scale_dir(ll2d(W[2] + Rm, 1), ex, 1);
@@ -423,8 +518,21 @@ int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, doubl
   free(mA); free(rA); free(pA); free(Em); free(Ep); free(Er); free(delta);
   free(dAm); free(dAp); free(dAr); free(Fm); free(Fr); free(beta);
   free(dBm); free(dBr); free(dBs); free(mcol); free(rcol);
+  free(Ai); free(Ahi); free(Alo); free(Bi);
   fesetround(prev);
   return status;
+}
+
+/* Slice form (GPU form VCPCU_FORM_OZAKI_SLICES). */
+int orc_ozaki_igemm(int m, int n, int k, const double* A, const double* B, double* Cout, int s,
+                    int sr) {
+  return ozaki_model(m, n, k, A, B, Cout, s, sr, 0);
+}
+
+/* CRT form (GPU form VCPCU_FORM_OZAKI). */
+int orc_ozaki2_igemm(int m, int n, int k, const double* A, const double* B, double* Cout, int s,
+                     int sr) {
+  return ozaki_model(m, n, k, A, B, Cout, s, sr, 1);
 }
 
 int orc_ozaki_model_version(void) { return 1; }

@@ -1,9 +1,13 @@
-"""GPU parity of the Ozaki (tensor-core) form of the interval product.
+"""GPU parity of the Ozaki (tensor-core) forms of the interval product.
 
-* bit-identical to the host model oracle/ozaki_model.c (same slicing,
-  summation order and directed reassembly) on ragged shapes, several slice
-  counts, inner dimensions spanning several 1024-element chunks, and the
-  extreme digit patterns (every digit +-128, so chunk sums reach 2^24);
+* FORM_OZAKI (CRT form) is bit-identical to the host model
+  oracle/ozaki_model.c, which computes the exact product of the w-bit
+  integer operands directly in 128-bit integers -- so equality also proves
+  the residue GEMMs and the Chinese remaindering exact; FORM_OZAKI_SLICES
+  (triangular digit slices) is bit-identical to the slice host model (same
+  slicing, summation order, folds and directed reassembly).  Cases: ragged
+  shapes, several precisions, inner dimensions spanning several
+  1024-element chunks, and extreme digit patterns (chunk sums of +-2^24);
 * zero containment failures against the exact interval hull (long
   accumulator) on every checked entry;
 * enclosure no wider than the plain FP64 form at the benchmark distribution;
@@ -38,13 +42,15 @@ CASES = [(1, 1, 1, 8), (5, 7, 3, 8), (128, 256, 64, 8), (129, 257, 65, 6), (200,
 
 
 @pytest.mark.parametrize("case", CASES)
-def test_ozaki_bitexact_model_and_encloses(cuda_lib, oracle, case):
+@pytest.mark.parametrize("crt", [True, False], ids=["crt", "slices"])
+def test_ozaki_bitexact_model_and_encloses(cuda_lib, oracle, case, crt):
     m, n, k, s = case
     rng = np.random.default_rng(m * 7 + n * 3 + k + s)
     A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
     B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
-    C = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=s)
-    ref, st = oracle.ozaki_igemm(m, n, k, A, B, s, 2)
+    form = pidcuda.FORM_OZAKI if crt else pidcuda.FORM_OZAKI_SLICES
+    C = pidcuda.mulmm(A, B, m, n, k, form=form, slices=s)
+    ref, st = oracle.ozaki_igemm(m, n, k, A, B, s, 2, crt=crt)
     assert st == 0
     assert np.array_equal(bits(C), bits(ref)), "GPU differs from the host model"
     check_contains(oracle, m, n, k, A, B, C)
@@ -57,17 +63,19 @@ def test_ozaki_extreme_digits(cuda_lib, oracle):
     A = np.empty(2 * m * k); B = np.empty(2 * k * n)
     A[0::2] = A[1::2] = 1.0
     B[0::2] = B[1::2] = 1.0
-    C = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=8)
-    ref, _ = oracle.ozaki_igemm(m, n, k, A, B, 8, 2)
-    assert np.array_equal(bits(C), bits(ref))
-    assert np.all(C[0::2] <= k) and np.all(C[1::2] >= k)
+    for form, crt in ((pidcuda.FORM_OZAKI, True), (pidcuda.FORM_OZAKI_SLICES, False)):
+        C = pidcuda.mulmm(A, B, m, n, k, form=form, slices=8)
+        ref, _ = oracle.ozaki_igemm(m, n, k, A, B, 8, 2, crt=crt)
+        assert np.array_equal(bits(C), bits(ref))
+        assert np.all(C[0::2] <= k) and np.all(C[1::2] >= k)
     # alternating signs by column of A: cancellation to exactly zero
     rng = np.random.default_rng(2)
     sg = np.where(rng.random(m * k) < 0.5, -1.0, 1.0)
     A[0::2] = A[1::2] = sg
-    C = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=8)
-    ref, _ = oracle.ozaki_igemm(m, n, k, A, B, 8, 2)
-    assert np.array_equal(bits(C), bits(ref))
+    for form, crt in ((pidcuda.FORM_OZAKI, True), (pidcuda.FORM_OZAKI_SLICES, False)):
+        C = pidcuda.mulmm(A, B, m, n, k, form=form, slices=8)
+        ref, _ = oracle.ozaki_igemm(m, n, k, A, B, 8, 2, crt=crt)
+        assert np.array_equal(bits(C), bits(ref))
     check_contains(oracle, m, n, k, A, B, C, rows=np.arange(0, m, 7).repeat(4),
                    cols=np.tile(np.array([0, 1, 100, 259]), len(range(0, m, 7))))
 

@@ -88,11 +88,13 @@ int rmatmul_host_impl(int m, int n, int k, const double* A, const double* B, dou
 
 int igemm_check(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
                 const double* C, int ldc, int form, int slices) {
-  if (form != VCPCU_FORM_PLAIN && form != VCPCU_FORM_OZAKI && form != VCPCU_FORM_AUTO) {
+  if (form != VCPCU_FORM_PLAIN && form != VCPCU_FORM_OZAKI && form != VCPCU_FORM_AUTO &&
+      form != VCPCU_FORM_OZAKI_SLICES) {
     set_error("igemm: unknown form %d", form);
     return VCPCU_ERR_INVALID_ARG;
   }
-  if (form == VCPCU_FORM_OZAKI && slices != 0 && (slices < 2 || slices > OZ_MAX_SLICES)) {
+  if ((form == VCPCU_FORM_OZAKI || form == VCPCU_FORM_OZAKI_SLICES) && slices != 0 &&
+      (slices < 2 || slices > OZ_MAX_SLICES)) {
     set_error("igemm: slices must be 0 or in [2, %d], got %d", OZ_MAX_SLICES, slices);
     return VCPCU_ERR_INVALID_ARG;
   }

@@ -14,9 +14,9 @@
 // The array (VCPCU_NOALLOC_SCRATCH_BYTES, 32 MiB) exists on every device
 // that loads this library, for the life of the process.  Every call shares
 // it and it keeps the previous call's contents; each call re-initialises
-// every word that must start at zero (the row maxima, digit sums and status
-// words are cleared on the call's stream, the digit planes, fold buffer and
-// radius bounds are fully overwritten).  Calls whose GPU work overlaps -- on
+// every word that must start at zero (the row maxima, digit and integer sums
+// and status words are cleared on the call's stream; the digit and residue
+// planes, fold buffer and radius bounds are fully overwritten).  Calls whose GPU work overlaps -- on
 // two streams, or from two host threads without ordering -- race on the
 // array and give wrong results: order them on one stream.
 #include "common.cuh"
@@ -102,7 +102,7 @@ extern "C" int vcpcu_igemm_noalloc_dev(int m, int n, int k, const double* A, int
     return VCPCU_ERR_INVALID_ARG;
   }
   OzPlan plan;
-  oz_make_plan(m, n, k, slices > 0 ? slices : 8, 2, &plan);
+  oz_make_plan(m, n, k, slices > 0 ? slices : 8, 2, &plan, /*crt=*/1);
   const size_t need = oz_workspace_bytes(plan.pb);
   if (need > (size_t)VCPCU_NOALLOC_SCRATCH_BYTES) {
     set_error("igemm_noalloc: %d x %d x %d with %d slices needs %zu bytes of scratch, more than "
@@ -117,10 +117,7 @@ extern "C" int vcpcu_igemm_noalloc_dev(int m, int n, int k, const double* A, int
   cudaStream_t s = (cudaStream_t)stream;
   OzWorkspace ws;
   oz_carve_workspace(plan.pb, base, &ws);
-  if ((st = oz_prepare(plan.pb, A, lda, B, ldb, ws, s))) return st;
-  if ((st = oz_run_gemm(plan, OZ_RAD_SET, ws, nullptr, 0, s))) return st;
-  if ((st = oz_run_gemm(plan, OZ_RAD_ADD, ws, nullptr, 0, s))) return st;
-  if ((st = oz_run_gemm(plan, OZ_MID, ws, C, ldc, s))) return st;
+  if ((st = oz_run_product(plan, ws, A, lda, B, ldb, C, ldc, s))) return st;
   noalloc_poison_on_timeout<<<64, 256, 0, s>>>(ws.flag, m, n, C, ldc);
   VCPCU_LAUNCH_CHECK("noalloc_poison_on_timeout");
   return VCPCU_OK;

@@ -146,7 +146,37 @@ int oz_take_status(cudaStream_t s, int* status) {
   return VCPCU_OK;
 }
 
-int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan) {
+// CRT form: number of moduli L and basis Q_l for w-bit operands and inner
+// dimension K: the product A'B' satisfies |A'B'| <= K 2^(2w-2), and it is
+// recovered from its residues iff prod m_l > 2 K 2^(2w-2) = K 2^(2w-1).
+// Returns 0, or -1 if 16 moduli do not suffice.
+int crt_setup(int K, int w, OzPlan* plan) {
+  const double need = (2.0 * w - 1.0) + std::log2((double)(K > 1 ? K : 1)) + 0.01;
+  double bits = 0.0;
+  int L = 0;
+  while (L < OZ_MAX_MODULI && bits <= need) bits += std::log2((double)OZ_MODULI[L++]);
+  if (bits <= need) return -1;
+  unsigned __int128 Mv = 1;
+  for (int l = 0; l < L; ++l) Mv *= (unsigned __int128)OZ_MODULI[l];
+  for (int l = 0; l < L; ++l) {
+    const int m = OZ_MODULI[l];
+    const unsigned __int128 Ml = Mv / (unsigned __int128)m;
+    const int r = (int)(Ml % (unsigned __int128)m);
+    int inv = 0;
+    for (int x = 1; x < m; ++x)
+      if ((r * x) % m == 1) {
+        inv = x;
+        break;
+      }
+    const unsigned __int128 Q = Ml * (unsigned __int128)inv;  // < M
+    for (int t = 0; t < 4; ++t) plan->Q[l][t] = (uint32_t)(Q >> (32 * t));
+  }
+  for (int t = 0; t < 4; ++t) plan->Mlimb[t] = (uint32_t)(Mv >> (32 * t));
+  plan->pb.L = L;
+  return 0;
+}
+
+int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan, int crt) {
   memset(plan, 0, sizeof(*plan));
   OzProblem& pb = plan->pb;
   pb.M = M;
@@ -159,6 +189,24 @@ int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan) {
   pb.sr = sr;
   build_pairs(s, s, true, &plan->mid);
   build_pairs(sr, sr, false, &plan->rad);
+  pb.mplanes = s;
+  if (crt) {
+    pb.crt = 1;
+    pb.w = 7 * s;
+    const int Keff = pb.K > 1 ? pb.K : 1;
+    while (crt_setup(Keff, pb.w, plan) != 0) --pb.w;  // very long K: fewer bits per operand
+    pb.mplanes = pb.L;
+    OzPairList& pl = plan->crt;
+    memset(&pl, 0, sizeof(pl));
+    for (int l = 0; l < pb.L; ++l) {
+      pl.pa[l] = (int8_t)l;
+      pl.pb[l] = (int8_t)l;
+      pl.gstart[l] = (int16_t)l;
+      pl.gt[l] = (int8_t)l;
+    }
+    pl.gstart[pb.L] = (int16_t)pb.L;
+    pl.npairs = pl.ngroups = pb.L;
+  }
   const int nchunks = (pb.Kp + OZ_CHUNK - 1) / OZ_CHUNK;
   choose_scaling(plan->mid, nchunks, &plan->t_ref_mid, &plan->R_mid);
   choose_scaling(plan->rad, nchunks, &plan->t_ref_rad, &plan->R_rad);
@@ -166,7 +214,7 @@ int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan) {
 }
 
 size_t oz_workspace_bytes(const OzProblem& pb) {
-  const size_t np = (size_t)(pb.s + 2 * pb.sr);
+  const size_t np = (size_t)(pb.mplanes + 2 * pb.sr);
   size_t b = 0;
   b += al256(np * pb.Mp * pb.Kp * 2);
   b += al256(np * pb.Np * pb.Kp * 2);
@@ -180,21 +228,23 @@ size_t oz_workspace_bytes(const OzProblem& pb) {
   b += al256(sizeof(int) * 4);
   b += 2 * al256(sizeof(double) * (size_t)pb.M * (pb.K > 0 ? pb.K : 1));
   b += 2 * al256(sizeof(double) * (size_t)pb.Np * pb.Kp);
+  b += al256(sizeof(unsigned long long) * 2 * pb.Mp);
+  if (pb.crt) b += al256((size_t)pb.L * pb.Np * pb.Mp);
   return b;
 }
 
 int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws) {
   uint8_t* p = (uint8_t*)base;
   const size_t mk = (size_t)pb.Mp * pb.Kp, nk = (size_t)pb.Np * pb.Kp;
-  const size_t np = (size_t)(pb.s + 2 * pb.sr);
+  const size_t np = (size_t)(pb.mplanes + 2 * pb.sr);
   uint16_t* a = (uint16_t*)p;
   ws->a_mid = a;
-  ws->a_p = a + pb.s * mk;
+  ws->a_p = a + pb.mplanes * mk;
   ws->a_r = ws->a_p + pb.sr * mk;
   p += al256(np * mk * 2);
   uint16_t* b = (uint16_t*)p;
   ws->b_mid = b;
-  ws->b_r = b + pb.s * nk;
+  ws->b_r = b + pb.mplanes * nk;
   ws->b_s = ws->b_r + pb.sr * nk;
   p += al256(np * nk * 2);
   ws->rowmax = (unsigned long long*)p;
@@ -221,25 +271,16 @@ int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws) {
   ws->midB = (double*)p;
   p += al256(sizeof(double) * (size_t)pb.Np * pb.Kp);
   ws->radB = (double*)p;
+  p += al256(sizeof(double) * (size_t)pb.Np * pb.Kp);
+  ws->asum = (unsigned long long*)p;
+  p += al256(sizeof(unsigned long long) * 2 * pb.Mp);
+  ws->res = pb.crt ? (uint8_t*)p : nullptr;
   return VCPCU_OK;
 }
 
-int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
-                double* C, long ldc, int form, int slices, cudaStream_t s) {
-  (void)form;
-  const int nslices = slices > 0 ? slices : 8;
-  const int sr = 2;
-  if (k > (1 << 20)) {
-    set_error("igemm (Ozaki form): inner dimension %d above the supported 2^20", k);
-    return VCPCU_ERR_UNSUPPORTED;
-  }
-  OzPlan plan;
-  oz_make_plan(m, n, k, nslices, sr, &plan);
-  Scratch buf;
-  int st = buf.alloc(oz_workspace_bytes(plan.pb), s);
-  if (st) return st;
-  OzWorkspace ws;
-  oz_carve_workspace(plan.pb, buf.ptr, &ws);
+int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long lda,
+                   const double* B, long ldb, double* C, long ldc, cudaStream_t s) {
+  int st;
   {
     PhaseTimer t(0, s);
     if ((st = oz_prepare(plan.pb, A, lda, B, ldb, ws, s))) return st;
@@ -254,12 +295,36 @@ int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B,
   }
   {
     PhaseTimer t(3, s);
-    if ((st = oz_run_gemm(plan, OZ_MID, ws, C, ldc, s))) return st;
+    if (plan.pb.crt) {
+      if ((st = oz_run_gemm(plan, OZ_CRT, ws, nullptr, 0, s))) return st;
+      if ((st = oz_crt_assemble(plan, ws, C, ldc, s))) return st;
+    } else {
+      if ((st = oz_run_gemm(plan, OZ_MID, ws, C, ldc, s))) return st;
+    }
   }
+  return VCPCU_OK;
+}
+
+int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
+                double* C, long ldc, int form, int slices, cudaStream_t s) {
+  const int nslices = slices > 0 ? slices : 8;
+  const int sr = 2;
+  if (k > (1 << 20)) {
+    set_error("igemm (Ozaki form): inner dimension %d above the supported 2^20", k);
+    return VCPCU_ERR_UNSUPPORTED;
+  }
+  OzPlan plan;
+  oz_make_plan(m, n, k, nslices, sr, &plan, form == VCPCU_FORM_OZAKI_SLICES ? 0 : 1);
+  Scratch buf;
+  int st = buf.alloc(oz_workspace_bytes(plan.pb), s);
+  if (st) return st;
+  OzWorkspace ws;
+  oz_carve_workspace(plan.pb, buf.ptr, &ws);
+  if ((st = oz_run_product(plan, ws, A, lda, B, ldb, C, ldc, s))) return st;
   if (g_prof.on) {
     std::lock_guard<std::mutex> lk(g_prof_mu);
     g_prof.flops += 2LL * m * n * (long long)(k > 0 ? k : 0) *
-                    (plan.mid.npairs + 2LL * plan.rad.npairs);
+                    ((plan.pb.crt ? plan.pb.L : plan.mid.npairs) + 2LL * plan.rad.npairs);
   }
   oz_status_merge<<<1, 1, 0, s>>>(ws.flag);
   VCPCU_LAUNCH_CHECK("oz_status_merge");

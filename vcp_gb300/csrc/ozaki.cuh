@@ -18,6 +18,9 @@ struct OzProblem {
   int M, N, K;     // logical sizes: C (M x N) = A (M x K) * B (K x N)
   int Mp, Np, Kp;  // padded: Mp % 128 == 0, Np % 256 == 0, Kp % 64 == 0
   int s, sr;       // digit slices of the midpoints / of the radius factors
+  int crt;         // 1: midpoint by the CRT form (w-bit integers, L moduli)
+  int w, L;        // CRT form: integer bits per operand, number of moduli
+  int mplanes;     // midpoint planes per operand: s (slice form) or L (CRT form)
 };
 
 // Device scratch of one Ozaki-form product (pointers into one allocation).
@@ -29,6 +32,8 @@ struct OzWorkspace {
   unsigned long long* delta;          // [Mp] sum of |midpoint digits| per row
   int* F2;                            // [Np][2] exponents Fm, Fr
   double* beta;                       // [Np] sum_k |mB(k,j)| rounded up
+  unsigned long long* asum;           // [Mp][2] CRT form: sum_k |A'(i,k)| as (bits >= 32, bits < 32)
+  uint8_t* res;                       // [L][Np][Mp] CRT form: residues of A'B' mod m_l
   double *midA, *radA;                // [K][M] midpoints / radii of A (column-major)
   double *midB, *radB;                // [Np][Kp] midpoints / radii of B (k contiguous)
   double* T;                          // [N][Mp] upper bound of the radius product
@@ -44,7 +49,7 @@ struct OzPairList {
   int8_t gt[OZ_MAX_GROUPS];                    // t of group g
 };
 
-enum OzMode { OZ_RAD_SET = 0, OZ_RAD_ADD = 1, OZ_MID = 2 };
+enum OzMode { OZ_RAD_SET = 0, OZ_RAD_ADD = 1, OZ_MID = 2, OZ_CRT = 3 };
 
 struct alignas(64) OzGemmArgs {
   CUtensorMap tmA;  // left digit planes, dims {Kp, Mp, planes}
@@ -66,6 +71,8 @@ struct alignas(64) OzGemmArgs {
   long ldc;
   int* flag;
   long long timeout_cycles;
+  uint8_t* res;                 // OZ_CRT: residue planes [L][Np][Mp]
+  int moduli[16];               // OZ_CRT: modulus of group g
   OzPairList pl;
 };
 
@@ -73,11 +80,16 @@ struct alignas(64) OzGemmArgs {
 // W scaling, shared with the host model.
 struct OzPlan {
   OzProblem pb;
-  OzPairList mid, rad;
+  OzPairList mid, rad, crt;
   int t_ref_mid, R_mid, t_ref_rad, R_rad;
+  uint32_t Q[16][4];   // CRT basis: Q_l = (M/m_l) * ((M/m_l)^-1 mod m_l), 32-bit limbs
+  uint32_t Mlimb[4];   // M = prod m_l
 };
 
-int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan);
+// crt != 0 selects the CRT form of the midpoint with w = 7 * s integer bits.
+int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan, int crt = 0);
+int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long ldc,
+                    cudaStream_t st);
 int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, long ldb,
                OzWorkspace& ws, cudaStream_t st);
 int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, long ldc,
@@ -92,6 +104,11 @@ int oz_take_status(cudaStream_t s, int* status);
 // Per-phase timing of the Ozaki form (prep, radius 1, radius 2, midpoint).
 int oz_profile_enable(int on);
 int oz_profile_read(double* ms, int nphases, long long* flops);
+
+// Operand preparation, the three slice-GEMM phases and the reassembly of
+// one planned product (shared by every entry point of the Ozaki form).
+int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long lda,
+                   const double* B, long ldb, double* C, long ldc, cudaStream_t s);
 
 int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
                 double* C, long ldc, int form, int slices, cudaStream_t s);

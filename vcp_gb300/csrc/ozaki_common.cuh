@@ -58,10 +58,10 @@ OZ_HD int oz_exponent(double amax) {
   return be - 1021;  // amax < 2^(be-1022)
 }
 
-// N = x * 2^(8s - E) rounded to an integer: to nearest-even (up == 0) or
+// N = x * 2^(bits - E) rounded to an integer: to nearest-even (up == 0) or
 // toward +inf (up == 1; used for x >= 0).  Requires |x| <= 2^(E-1), so
-// |N| <= 2^(8s-1) (s <= 12 keeps N within 96 bits).
-OZ_HD __int128 oz_scaled_int(double x, int E, int s, int up) {
+// |N| <= 2^(bits-1) (bits <= 96 keeps N within an int128).
+OZ_HD __int128 oz_scaled_int_bits(double x, int E, int bits, int up) {
   uint64_t b = oz_bits(x);
   const int neg = (int)(b >> 63);
   const int be = (int)((b >> 52) & 0x7ff);
@@ -74,7 +74,7 @@ OZ_HD __int128 oz_scaled_int(double x, int E, int s, int up) {
     mant |= 1ULL << 52;
     ex = be - 1075;
   }
-  const int sh = ex + 8 * s - E;
+  const int sh = ex + bits - E;
   unsigned __int128 N;
   if (sh >= 0) {
     N = (unsigned __int128)mant << sh;
@@ -104,6 +104,27 @@ OZ_HD __int128 oz_scaled_int(double x, int E, int s, int up) {
     N = q;
   }
   return neg ? -(__int128)N : (__int128)N;
+}
+
+// Digit form: x * 2^(8s - E) (s base-256 digits).
+OZ_HD __int128 oz_scaled_int(double x, int E, int s, int up) {
+  return oz_scaled_int_bits(x, E, 8 * s, up);
+}
+
+// Moduli of the CRT (Ozaki-II) form: pairwise coprime, at most 256, so a
+// residue taken in the symmetric range fits in [-128, 127] (exact in bf16).
+constexpr int OZ_MAX_MODULI = 16;
+constexpr int OZ_MODULI[OZ_MAX_MODULI] = {256, 255, 253, 251, 247, 241, 239, 233,
+                                          229, 227, 223, 217, 211, 199, 197, 193};
+
+// Symmetric residue of (neg ? -a : a) modulo m (2 <= m <= 256), in
+// [-floor(m/2), ceil(m/2) - 1].
+OZ_HD int oz_sym_residue(unsigned long long a, int neg, int m) {
+  unsigned long long r = a % (unsigned long long)m;
+  if (neg && r) r = (unsigned long long)m - r;
+  int rs = (int)r;
+  if (2 * rs >= m) rs -= m;
+  return rs;
 }
 
 // Balanced base-256 digits of N, most significant first: d[0] = d_1.

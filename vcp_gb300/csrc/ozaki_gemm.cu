@@ -263,7 +263,30 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
           if (lane == 0) ptx::mbar_arrive(&sm.tempty[buf]);
           ++cnt;
           const bool last_of_group = idx == total - 1;
-          if (cnt == OZ_FOLD_CHUNKS || last_of_group) {
+          if ((cnt == OZ_FOLD_CHUNKS || last_of_group) && args.mode == OZ_CRT) {
+            // CRT form: group g is modulus m_g; keep (A'B') mod m_g as a byte
+            // in res[g][col][row], adding to an earlier fold of the group
+            const uint32_t m = (uint32_t)args.moduli[g];
+            const uint32_t mg = 0xFFFFFFFFu / m;
+            uint8_t* rp = args.res + (size_t)g * args.Np * args.Mp + (size_t)gj0 * args.Mp + gi;
+            const bool first = cnt == idx + 1;  // no earlier fold in this group
+#pragma unroll
+            for (int e = 0; e < 128; ++e) {
+              const int v = c[e];
+              const uint32_t a = (uint32_t)(v < 0 ? -v : v);
+              uint32_t r = a - __umulhi(a, mg) * m;
+              if (r >= m) r -= m;
+              if (r >= m) r -= m;
+              if (v < 0 && r) r = m - r;
+              if (!first) {
+                r += rp[(size_t)e * args.Mp];
+                if (r >= m) r -= m;
+              }
+              rp[(size_t)e * args.Mp] = (uint8_t)r;
+              c[e] = 0;
+            }
+            cnt = 0;
+          } else if (cnt == OZ_FOLD_CHUNKS || last_of_group) {
             // fold into W (global, column-major, ld = Mp); the first fold of
             // a tile stores, later folds add
 #pragma unroll
@@ -279,6 +302,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
         }
       }
       if (!ok) break;
+      if (args.mode == OZ_CRT) continue;  // reassembled by oz_crt_assemble
       // ------------------------------------------------------ final epilogue
       const int Ei = (gi < args.M) ? args.Erow[(size_t)args.erow_stride * gi] : OZ_ZERO_EXP;
       double dlt = 0.0;
@@ -396,17 +420,23 @@ int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, 
   const uint16_t* bp;
   int apl, bpl;
   if (mid) {
-    ap = ws.a_mid; bp = ws.b_mid; apl = pb.s; bpl = pb.s;
+    ap = ws.a_mid; bp = ws.b_mid; apl = pb.mplanes; bpl = pb.mplanes;
     a.Erow = ws.E3 + 0; a.Fcol = ws.F2 + 0;
     a.pl = plan.mid; a.t_ref = plan.t_ref_mid; a.R = plan.R_mid;
   } else if (mode == OZ_RAD_SET) {  // (|mA| + rA) * rB
     ap = ws.a_p; bp = ws.b_r; apl = pb.sr; bpl = pb.sr;
     a.Erow = ws.E3 + 1; a.Fcol = ws.F2 + 1;
     a.pl = plan.rad; a.t_ref = plan.t_ref_rad; a.R = plan.R_rad;
-  } else {  // rA * |mB|
+  } else if (mode == OZ_RAD_ADD) {  // rA * |mB|
     ap = ws.a_r; bp = ws.b_s; apl = pb.sr; bpl = pb.sr;
     a.Erow = ws.E3 + 2; a.Fcol = ws.F2 + 0;
     a.pl = plan.rad; a.t_ref = plan.t_ref_rad; a.R = plan.R_rad;
+  } else {  // OZ_CRT: residue products, one modulus per group
+    ap = ws.a_mid; bp = ws.b_mid; apl = pb.L; bpl = pb.L;
+    a.Erow = ws.E3 + 0; a.Fcol = ws.F2 + 0;
+    a.pl = plan.crt; a.t_ref = 0; a.R = 0;
+    a.res = ws.res;
+    for (int l = 0; l < pb.L; ++l) a.moduli[l] = OZ_MODULI[l];
   }
   if ((st_ = make_tmap(&a.tmA, ap, pb.Kp, pb.Mp, apl, OZ_BM))) return st_;
   if ((st_ = make_tmap(&a.tmB, bp, pb.Kp, pb.Np, bpl, OZ_BN))) return st_;

@@ -307,6 +307,197 @@ oz_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
   }
 }
 
+// ------------------------------------------------------ CRT form (residues)
+// Barrett reduction constants of the moduli (x < 2^32): q = umulhi(x, magic)
+// is at most two below floor(x / m).
+__constant__ uint32_t c_mod[OZ_MAX_MODULI] = {256, 255, 253, 251, 247, 241, 239, 233,
+                                              229, 227, 223, 217, 211, 199, 197, 193};
+#define OZ_MAGIC(m) (0xFFFFFFFFu / (m))
+__constant__ uint32_t c_magic[OZ_MAX_MODULI] = {
+    OZ_MAGIC(256), OZ_MAGIC(255), OZ_MAGIC(253), OZ_MAGIC(251), OZ_MAGIC(247), OZ_MAGIC(241),
+    OZ_MAGIC(239), OZ_MAGIC(233), OZ_MAGIC(229), OZ_MAGIC(227), OZ_MAGIC(223), OZ_MAGIC(217),
+    OZ_MAGIC(211), OZ_MAGIC(199), OZ_MAGIC(197), OZ_MAGIC(193)};
+#define OZ_P32(m) ((uint32_t)(4294967296ULL % (m)))
+__constant__ uint32_t c_pow32[OZ_MAX_MODULI] = {
+    OZ_P32(256), OZ_P32(255), OZ_P32(253), OZ_P32(251), OZ_P32(247), OZ_P32(241),
+    OZ_P32(239), OZ_P32(233), OZ_P32(229), OZ_P32(227), OZ_P32(223), OZ_P32(217),
+    OZ_P32(211), OZ_P32(199), OZ_P32(197), OZ_P32(193)};
+
+__device__ __forceinline__ uint32_t umod32(uint32_t x, uint32_t m, uint32_t magic) {
+  uint32_t r = x - __umulhi(x, magic) * m;
+  if (r >= m) r -= m;
+  if (r >= m) r -= m;
+  return r;
+}
+
+// Symmetric residue of (neg ? -a : a) mod m_l, a < 2^63; equals oz_sym_residue.
+__device__ __forceinline__ int dev_sym_residue(unsigned long long a, int neg, int l) {
+  const uint32_t m = c_mod[l], mg = c_magic[l];
+  const uint32_t rh = umod32((uint32_t)(a >> 32), m, mg);
+  const uint32_t rl = umod32((uint32_t)a, m, mg);
+  uint32_t r = umod32(rh * c_pow32[l] + rl, m, mg);
+  if (neg && r) r = m - r;
+  int rs = (int)r;
+  if (2 * rs >= (int)m) rs -= (int)m;
+  return rs;
+}
+
+// w-bit integer of x (|x| <= 2^(E-1)): round to nearest even, |result| <= 2^(w-1).
+__device__ __forceinline__ long long crt_int(double x, int E, int w) {
+  if (E == OZ_ZERO_EXP || x == 0.0) return 0;
+  return (long long)oz_scaled_int_bits(x, E, w, 0);
+}
+
+// Left factor, CRT form: residues of A' (L planes) + radius digits, and
+// sum_k |A'(i,k)| split as (|A'| >> 32, |A'| & 0xffffffff) sums.
+template <int SR>
+__global__ void __launch_bounds__(256)
+oz_split_left_crt(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
+                  const double* __restrict__ rA, int L, int w, const int* __restrict__ E3,
+                  uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_p,
+                  uint16_t* __restrict__ planes_r, unsigned long long* __restrict__ asum) {
+  extern __shared__ int16_t sd[];  // [plane][LT_R][LT_KS]
+  const int np = L + 2 * SR;
+  const int tid = threadIdx.x;
+  const int r = tid % LT_R, kph = tid / LT_R;
+  const int i = blockIdx.y * LT_R + r;
+  const int k0 = blockIdx.x * LT_K;
+  int Em = OZ_ZERO_EXP, Ep = OZ_ZERO_EXP, Er = OZ_ZERO_EXP;
+  if (i < M) {
+    Em = E3[3 * i + 0];
+    Ep = E3[3 * i + 1];
+    Er = E3[3 * i + 2];
+  }
+  unsigned long long shi = 0, slo = 0;
+  int dr[SR];
+  for (int kk = kph; kk < LT_K; kk += 8) {
+    const int k = k0 + kk;
+    double m = 0.0, rr = 0.0, p = 0.0;
+    if (i < M && k < K) {
+      m = mA[i + (long)k * M];
+      rr = rA[i + (long)k * M];
+      p = __dadd_ru(fabs(m), rr);
+    }
+    const long long a = crt_int(m, Em, w);
+    const unsigned long long ua = (unsigned long long)(a < 0 ? -a : a);
+    shi += ua >> 32;
+    slo += ua & 0xffffffffULL;
+    for (int l = 0; l < L; ++l)
+      sd[(l * LT_R + r) * LT_KS + kk] = (int16_t)dev_sym_residue(ua, a < 0, l);
+    digits_of<SR>(p, Ep, 1, dr);
+#pragma unroll
+    for (int q = 0; q < SR; ++q) sd[((L + q) * LT_R + r) * LT_KS + kk] = (int16_t)dr[q];
+    digits_of<SR>(rr, Er, 1, dr);
+#pragma unroll
+    for (int q = 0; q < SR; ++q) sd[((L + SR + q) * LT_R + r) * LT_KS + kk] = (int16_t)dr[q];
+  }
+  __shared__ unsigned long long rs[2][LT_R];
+  if (tid < LT_R) rs[0][tid] = rs[1][tid] = 0;
+  __syncthreads();
+  atomicAdd(&rs[0][r], shi);
+  atomicAdd(&rs[1][r], slo);
+  __syncthreads();
+  if (tid < LT_R && blockIdx.y * LT_R + tid < M) {
+    atomicAdd(&asum[2 * (blockIdx.y * LT_R + tid) + 0], rs[0][tid]);
+    atomicAdd(&asum[2 * (blockIdx.y * LT_R + tid) + 1], rs[1][tid]);
+  }
+  const int wr = tid / 8, wk = (tid % 8) * 8;
+  const int gi = blockIdx.y * LT_R + wr;
+  for (int q = 0; q < np; ++q) {
+    uint16_t* base;
+    int pl;
+    if (q < L) {
+      base = planes_m;
+      pl = q;
+    } else if (q < L + SR) {
+      base = planes_p;
+      pl = q - L;
+    } else {
+      base = planes_r;
+      pl = q - L - SR;
+    }
+    const int16_t* src = sd + (q * LT_R + wr) * LT_KS + wk;
+    uint4 v;
+    v.x = bf16_bits(src[0]) | (bf16_bits(src[1]) << 16);
+    v.y = bf16_bits(src[2]) | (bf16_bits(src[3]) << 16);
+    v.z = bf16_bits(src[4]) | (bf16_bits(src[5]) << 16);
+    v.w = bf16_bits(src[6]) | (bf16_bits(src[7]) << 16);
+    if (gi < Mp) *reinterpret_cast<uint4*>(base + ((size_t)pl * Mp + gi) * Kp + k0 + wk) = v;
+  }
+}
+
+// Right factor, CRT form: as oz_split_right, with the residues of B' in
+// place of the midpoint digits (one element per thread in pass 2).
+template <int SR>
+__global__ void __launch_bounds__(256)
+oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb,
+                   int L, int w, double* __restrict__ mBp, double* __restrict__ rBp,
+                   uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_r,
+                   uint16_t* __restrict__ planes_s, int* __restrict__ F2,
+                   double* __restrict__ beta, int* __restrict__ flag) {
+  const int j = blockIdx.x;
+  const int tid = threadIdx.x;
+  __shared__ unsigned long long smax[2];
+  __shared__ double ssum[256];
+  if (tid == 0) smax[0] = smax[1] = 0;
+  __syncthreads();
+  unsigned long long am = 0, ar = 0;
+  double bsum = 0.0;
+  bool bad = false;
+  double* mcol = mBp + (size_t)j * Kp;
+  double* rcol = rBp + (size_t)j * Kp;
+  if (j < N) {
+    for (int k = tid; k < K; k += 256) {
+      const double2 e = *reinterpret_cast<const double2*>(B + 2 * (k + (long)j * ldb));
+      double m = 0.0, r = 0.0;
+      if (isfinite(e.x) && isfinite(e.y)) {
+        oz_midrad(e.x, e.y, m, r);
+        am = max(am, dbits(fabs(m)));
+        ar = max(ar, dbits(r));
+        bsum = __dadd_ru(bsum, fabs(m));
+      } else {
+        bad = true;
+      }
+      mcol[k] = m;
+      rcol[k] = r;
+    }
+  }
+  if (bad) atomicOr(flag, 1);
+  atomicMax(&smax[0], am);
+  atomicMax(&smax[1], ar);
+  ssum[tid] = bsum;
+  __syncthreads();
+  for (int wv = 128; wv > 0; wv >>= 1) {
+    if (tid < wv) ssum[tid] = __dadd_ru(ssum[tid], ssum[tid + wv]);
+    __syncthreads();
+  }
+  const int Fm = oz_exponent(__longlong_as_double((long long)smax[0]));
+  const int Fr = oz_exponent(__longlong_as_double((long long)smax[1]));
+  if (tid == 0 && j < N) {
+    F2[2 * j + 0] = Fm;
+    F2[2 * j + 1] = Fr;
+    beta[j] = ssum[0];
+  }
+  int dr[SR];
+  for (int k = tid; k < Kp; k += 256) {
+    double m = 0.0, r = 0.0;
+    if (j < N && k < K) {
+      m = mcol[k];
+      r = rcol[k];
+    }
+    const long long b = crt_int(m, Fm, w);
+    const unsigned long long ub = (unsigned long long)(b < 0 ? -b : b);
+    for (int l = 0; l < L; ++l)
+      planes_m[((size_t)l * Np + j) * Kp + k] = (uint16_t)bf16_bits(dev_sym_residue(ub, b < 0, l));
+    digits_of<SR>(r, Fr, 1, dr);
+#pragma unroll
+    for (int q = 0; q < SR; ++q) planes_r[((size_t)q * Np + j) * Kp + k] = (uint16_t)bf16_bits(dr[q]);
+    digits_of<SR>(fabs(m), Fm, 1, dr);
+#pragma unroll
+    for (int q = 0; q < SR; ++q) planes_s[((size_t)q * Np + j) * Kp + k] = (uint16_t)bf16_bits(dr[q]);
+  }
+}
+
 // ------------------------------------------------------------------ launchers
 template <int S, int SR>
 int launch_splits(const OzProblem& pb, const double* B, long ldb, OzWorkspace& ws,
@@ -344,6 +535,21 @@ int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, 
     return VCPCU_ERR_UNSUPPORTED;
   }
   int st_ = VCPCU_OK;
+  if (pb.crt) {
+    VCPCU_CUDA_TRY(cudaMemsetAsync(ws.asum, 0, sizeof(unsigned long long) * 2 * (size_t)pb.Mp, st));
+    dim3 g2(pb.Kp / LT_K, pb.Mp / LT_R);
+    const size_t shm = sizeof(int16_t) * (size_t)(pb.L + 4) * LT_R * LT_KS;
+    VCPCU_CUDA_TRY(cudaFuncSetAttribute(oz_split_left_crt<2>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    oz_split_left_crt<2><<<g2, 256, shm, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, pb.L,
+                                               pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r, ws.asum);
+    VCPCU_LAUNCH_CHECK("oz_split_left_crt");
+    oz_split_right_crt<2><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L, pb.w,
+                                                 ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,
+                                                 ws.F2, ws.beta, ws.flag);
+    VCPCU_LAUNCH_CHECK("oz_split_right_crt");
+    return VCPCU_OK;
+  }
   switch (pb.s) {
 #define OZ_SPLIT_CASE(S)                                                          \
   case S:                                                                         \

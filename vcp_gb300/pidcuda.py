@@ -22,6 +22,7 @@ from .vblas import _dev_ptr, _host_ptr, _stream_ptr
 FORM_PLAIN = 0
 FORM_OZAKI = 1
 FORM_AUTO = 2
+FORM_OZAKI_SLICES = 3
 
 
 def to_kv(lo: np.ndarray, up: np.ndarray) -> np.ndarray:
