@@ -140,6 +140,50 @@ int vcpcu_igemm_dev(int m, int n, int k, const double* A, int lda,
 int vcpcu_igemm(int m, int n, int k, const double* A, const double* B,
                 double* C, int form, int slices);
 
+/* ---- interval x point, [A]^T[A], verified A^T A, ||R[A] - I|| ------------ */
+
+/* Mixed interval / point products, GEMM naming (L m x k, R k x n, C m x n):
+ *   interval_side == 0: C = [L] * R, L interval, R point -- replaces
+ *     pidblas::mul_im_m (vcp/pidblas.hpp:90-140);
+ *   interval_side == 1: C = L * [R], L point, R interval -- replaces
+ *     pidblas::mul_m_im (vcp/pidblas.hpp:142-196).
+ * Point matrices are plain doubles, intervals kv pairs.  The plain form is
+ * bit-identical to pidblas over a sequential-chain dgemm (lC = RD(mid*P),
+ * uC = RU(mid*P), temp = RU(rad*|P|), uC +=RU temp, lC -=RD temp); the
+ * Ozaki forms enclose the same product. */
+int vcpcu_igemm_point_dev(int interval_side, int m, int n, int k,
+                          const double* L, int ldl, const double* R, int ldr,
+                          double* C, int ldc, int form, int slices, void* stream);
+int vcpcu_igemm_point(int interval_side, int m, int n, int k, const double* L,
+                      const double* R, double* C, int form, int slices);
+
+/* C (n x n) = [A]^T [A] for an interval A (k x n) -- replaces
+ * pidblas::mulltmm (vcp/pidblas.hpp:296-358; matrix::ltransmul,
+ * vcp/matrix.hpp:405-415).  Plain form: bit-identical to pidblas over
+ * sequential-chain dsyrk/dgemm (upper triangle computed, mirrored). */
+int vcpcu_isyrk_dev(int n, int k, const double* A, int lda, double* C, int ldc,
+                    int form, int slices, void* stream);
+int vcpcu_isyrk(int n, int k, const double* A, double* C, int form, int slices);
+
+/* C (n x n, intervals) = [RD(A^T A), RU(A^T A)] for a point A (k x n), each
+ * entry the sequential chain -- replaces pidblas::vmulmm
+ * (vcp/pidblas.hpp:198-236). */
+int vcpcu_vsyrk_dev(int n, int k, const double* A, int lda, double* C, int ldc,
+                    void* stream);
+int vcpcu_vsyrk(int n, int k, const double* A, double* C);
+
+/* Upper bound of ||R [A] - I||_inf for a point R and an interval A (n x n):
+ * the check of imats::linearsolve (vcp/imats.hpp:316-336; mats::norminf,
+ * vcp/mats.hpp:1583-1597): RA by vcpcu_igemm_point (side 1) in `form`,
+ * the diagonal shifted by -1 outward, per row the upward sum of |.| in
+ * ascending column order, then the largest row sum.  The _dev form writes
+ * the bound to device memory (*bound), the host form to host memory. */
+int vcpcu_norm_I_minus_RA_dev(int n, const double* R, int ldr, const double* A,
+                              int lda, double* bound, int form, int slices,
+                              void* stream);
+int vcpcu_norm_I_minus_RA(int n, const double* R, const double* A, double* bound,
+                          int form, int slices);
+
 /* ---- interval GEMM without device allocation ------------------------------ */
 
 /* Size of the static device scratch used by vcpcu_igemm_noalloc_dev. */

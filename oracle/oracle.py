@@ -37,6 +37,14 @@ def lib() -> C.CDLL:
         L.orc_ozaki_igemm.restype = _i
         L.orc_ozaki2_igemm.argtypes = [_i, _i, _i, _v, _v, _v, _i, _i]
         L.orc_ozaki2_igemm.restype = _i
+        L.orc_pidblas_mul_point.argtypes = [_i, _i, _i, _i, _v, _v, _v, _i]
+        L.orc_pidblas_mul_point.restype = _i
+        L.orc_pidblas_mulltmm.argtypes = [_i, _i, _v, _v, _i]
+        L.orc_pidblas_mulltmm.restype = _i
+        L.orc_pidblas_vmulmm.argtypes = [_i, _i, _v, _v, _i]
+        L.orc_pidblas_vmulmm.restype = _i
+        L.orc_norm_I_minus_RA.argtypes = [_i, _v, _v, _i]
+        L.orc_norm_I_minus_RA.restype = C.c_double
         _lib = L
     return _lib
 
@@ -49,6 +57,14 @@ def ref_lib() -> C.CDLL | None:
         R.ref_rmatmul.argtypes = [_i, _i, _i, _v, _v, _v, _i]
         R.ref_pidblas_mulmm.argtypes = [_i, _i, _i, _v, _v, _v]
         R.ref_pidblas_mulmm.restype = _i
+        R.ref_pidblas_mul_point.argtypes = [_i, _i, _i, _i, _v, _v, _v]
+        R.ref_pidblas_mul_point.restype = _i
+        R.ref_pidblas_mulltmm.argtypes = [_i, _i, _v, _v]
+        R.ref_pidblas_mulltmm.restype = _i
+        R.ref_pidblas_vmulmm.argtypes = [_i, _i, _v, _v]
+        R.ref_pidblas_vmulmm.restype = _i
+        R.ref_norm_I_minus_RA.argtypes = [_i, _v, _v, _v]
+        R.ref_norm_I_minus_RA.restype = _i
         _ref = R
     return _ref
 
@@ -111,6 +127,37 @@ def ozaki_igemm(m, n, k, A, B, s=8, sr=2, crt=True):
     fn = lib().orc_ozaki2_igemm if crt else lib().orc_ozaki_igemm
     st = fn(m, n, k, _p(A) if k > 0 else None, _p(B) if k > 0 else None, _p(C_), int(s), int(sr))
     return C_, st
+
+
+def pidblas_mul_point(side, m, n, k, L, R, threads=0):
+    """pidblas::mul_im_m (side 0: [L] R) / mul_m_im (side 1: L [R]); kv C."""
+    C_ = np.zeros(2 * m * n)
+    assert lib().orc_pidblas_mul_point(side, m, n, k, _p(L), _p(R), _p(C_), threads) == 0
+    return C_
+
+
+def pidblas_mulltmm(n, k, A, threads=0):
+    C_ = np.zeros(2 * n * n)
+    assert lib().orc_pidblas_mulltmm(n, k, _p(A), _p(C_), threads) == 0
+    return C_
+
+
+def pidblas_vmulmm(n, k, A, threads=0):
+    C_ = np.zeros(2 * n * n)
+    assert lib().orc_pidblas_vmulmm(n, k, _p(A), _p(C_), threads) == 0
+    return C_
+
+
+def norm_I_minus_RA(n, R, A, threads=0) -> float:
+    return float(lib().orc_norm_I_minus_RA(n, _p(R), _p(A), threads))
+
+
+def ref_call(name, *args):
+    """Call a reference-build wrapper; None where the reference is absent."""
+    R = ref_lib()
+    if R is None:
+        return None
+    return getattr(R, name)(*args)
 
 
 def exact_sum(x: np.ndarray, direction: int) -> float:

@@ -118,3 +118,102 @@ int ref_pidblas_mulmm(int m, int n, int k, const double* A, const double* B, dou
 }
 
 }  // extern "C"
+
+namespace {
+// Exposes pidblas's protected interval x point hooks (vcp/pidblas.hpp:90-236).
+struct pidblas_open : vcp::pidblas {
+  using vcp::pidblas::mul_im_m;
+  using vcp::pidblas::mul_m_im;
+  using vcp::pidblas::vmulmm;
+};
+typedef kv::interval<double> I;
+void fill_iv(vcp::mats<I>& X, int r, int c, const double* kvp) {
+  X.zeros(r, c);
+  for (long t = 0; t < (long)r * c; ++t) X.v[t] = I(kvp[2 * t], kvp[2 * t + 1]);
+}
+void fill_pt(vcp::pdblas& X, int r, int c, const double* p) {
+  X.zeros(r, c);
+  for (long t = 0; t < (long)r * c; ++t) X.v[t] = p[t];
+}
+void out_iv(const vcp::mats<I>& X, double* kvp) {
+  for (long t = 0; t < (long)X.n; ++t) {
+    kvp[2 * t] = X.v[t].lower();
+    kvp[2 * t + 1] = X.v[t].upper();
+  }
+}
+}  // namespace
+
+extern "C" {
+
+// pidblas::mul_im_m (side 0: [L] R) / mul_m_im (side 1: L [R]), GEMM naming.
+int ref_pidblas_mul_point(int side, int m, int n, int k, const double* L, const double* R,
+                          double* C) {
+  try {
+    pidblas_open iv;
+    vcp::pdblas pt;
+    vcp::imats<double, vcp::pdblas> c;
+    if (side == 0) {
+      fill_iv(iv, m, k, L);
+      fill_pt(pt, k, n, R);
+      iv.mul_im_m(pt, c);
+    } else {
+      fill_iv(iv, k, n, R);
+      fill_pt(pt, m, k, L);
+      iv.mul_m_im(pt, c);
+    }
+    out_iv(c, C);
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// pidblas::mulltmm: C (n x n) = [A]^T [A], A k x n.
+int ref_pidblas_mulltmm(int n, int k, const double* A, double* C) {
+  try {
+    pidblas_open a;
+    fill_iv(a, k, n, A);
+    vcp::mats<I> c;
+    a.mulltmm(c);
+    out_iv(c, C);
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// pidblas::vmulmm: [A^T A] of a point A (k x n).
+int ref_pidblas_vmulmm(int n, int k, const double* A, double* C) {
+  try {
+    vcp::pdblas a;
+    fill_pt(a, k, n, A);
+    pidblas_open c;
+    c.vmulmm(a);
+    out_iv(c, C);
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// The bound of imats::linearsolve (vcp/imats.hpp:316-336): b = R [A] by
+// pidblas::mul_m_im, b(i,i) -= 1, mats::norminf, upper end.
+int ref_norm_I_minus_RA(int n, const double* R, const double* A, double* bound) {
+  try {
+    pidblas_open a;
+    fill_iv(a, n, n, A);
+    vcp::pdblas r;
+    fill_pt(r, n, n, R);
+    vcp::imats<double, vcp::pdblas> b;
+    a.mul_m_im(r, b);
+    for (int i = 0; i < n; ++i) b.v[i + n * i] -= 1.0;
+    vcp::mats<I> g;
+    b.norminf(g);
+    *bound = g.v[0].upper();
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+}  // extern "C"

@@ -447,3 +447,150 @@ double orc_exact_sum(long count, const double* x, int dir) {
   }
   return acc_round(&s, dir);
 }
+
+/* ---------------------------------------------------------------------------
+ * The other pidblas products, restated in the reference's operation order
+ * over orc_rmatmul (the sequential-chain dgemm / dsyrk).
+ * ------------------------------------------------------------------------- */
+static void transpose_d(int rows, int cols, const double* X, double* Xt) {
+  for (long j = 0; j < cols; ++j)
+    for (long i = 0; i < rows; ++i) Xt[j + i * cols] = X[i + j * rows];
+}
+
+/* pidblas::mul_im_m (vcp/pidblas.hpp:90-140): C = [A] B, A m x k interval,
+ * B k x n point.  pidblas::mul_m_im (:142-196): C = B [A], B m x k point,
+ * A k x n interval.  side 0 / 1 selects which. */
+int orc_pidblas_mul_point(int side, int m, int n, int k, const double* L, const double* R,
+                          double* C, int nthreads) {
+  if (m <= 0 || n <= 0) return 0;
+  if (k < 0) k = 0;
+  const long nl = (long)m * k, nr = (long)k * n, nc = (long)m * n;
+  const long ni = side == 0 ? nl : nr;  /* interval factor entries */
+  const long np = side == 0 ? nr : nl;  /* point factor entries */
+  double* buf = (double*)malloc(sizeof(double) * (2 * ni + np + 3 * nc + 1));
+  if (!buf) return 1;
+  double *mid = buf, *rad = mid + ni, *absP = rad + ni;
+  double *lC = absP + np, *uC = lC + nc, *temp = uC + nc;
+  const int prev = fegetround();
+  orc_midrad(ni, side == 0 ? L : R, mid, rad);
+  const double* P = side == 0 ? R : L;  /* the point factor */
+  for (long t = 0; t < np; ++t) absP[t] = fabs(P[t]);
+  if (side == 0) {
+    orc_rmatmul(m, k, n, mid, P, lC, -1, nthreads);
+    orc_rmatmul(m, k, n, mid, P, uC, 1, nthreads);
+    orc_rmatmul(m, k, n, rad, absP, temp, 1, nthreads);
+  } else {
+    orc_rmatmul(m, k, n, P, mid, lC, -1, nthreads);
+    orc_rmatmul(m, k, n, P, mid, uC, 1, nthreads);
+    orc_rmatmul(m, k, n, absP, rad, temp, 1, nthreads);
+  }
+  fesetround(FE_UPWARD);
+  for (long i = 0; i < nc; ++i) uC[i] = uC[i] + temp[i];
+  fesetround(FE_DOWNWARD);
+  for (long i = 0; i < nc; ++i) lC[i] = lC[i] - temp[i];
+  fesetround(prev);
+  for (long i = 0; i < nc; ++i) {
+    C[2 * i] = lC[i];
+    C[2 * i + 1] = uC[i];
+  }
+  free(buf);
+  return 0;
+}
+
+/* pidblas::mulltmm (vcp/pidblas.hpp:296-358): C (n x n) = [A]^T [A], A k x n. */
+int orc_pidblas_mulltmm(int n, int k, const double* A, double* C, int nthreads) {
+  if (n <= 0) return 0;
+  if (k < 0) k = 0;
+  const long na = (long)k * n, nc = (long)n * n;
+  double* buf = (double*)malloc(sizeof(double) * (5 * (na + 1) + 4 * nc));
+  if (!buf) return 1;
+  double *mA = buf, *rA = mA + na + 1, *mAt = rA + na + 1, *aAt = mAt + na + 1, *rAt = aAt + na + 1;
+  double *lC = rAt + na + 1, *uC = lC + nc, *temp = uC + nc, *rr = temp + nc;
+  const int prev = fegetround();
+  orc_midrad(na, A, mA, rA);
+  transpose_d(k, n, mA, mAt);
+  transpose_d(k, n, rA, rAt);
+  for (long t = 0; t < na; ++t) aAt[t] = fabs(mAt[t]);
+  orc_rmatmul(n, k, n, mAt, mA, lC, -1, nthreads);   /* dsyrk under RD */
+  orc_rmatmul(n, k, n, mAt, mA, uC, 1, nthreads);    /* dsyrk under RU */
+  orc_rmatmul(n, k, n, aAt, rA, temp, 1, nthreads);  /* temp = |mA|^T rA */
+  orc_rmatmul(n, k, n, rAt, rA, rr, 1, nthreads);    /* rA^T rA */
+  fesetround(FE_UPWARD);
+  for (int i = 0; i < n; ++i)
+    for (int j = i; j < n; ++j) {
+      const double t = temp[j + (long)n * i] + rr[i + (long)n * j];
+      temp[i + (long)n * j] = temp[i + (long)n * j] + t;
+    }
+  for (int i = 0; i < n; ++i)
+    for (int j = i + 1; j < n; ++j) temp[j + (long)n * i] = temp[i + (long)n * j];
+  for (long i = 0; i < nc; ++i) uC[i] = uC[i] + temp[i];
+  fesetround(FE_DOWNWARD);
+  for (long i = 0; i < nc; ++i) lC[i] = lC[i] - temp[i];
+  fesetround(prev);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      const long s = (i <= j) ? i + (long)n * j : j + (long)n * i;  /* upper triangle */
+      C[2 * (i + (long)n * j)] = lC[s];
+      C[2 * (i + (long)n * j) + 1] = uC[s];
+    }
+  free(buf);
+  return 0;
+}
+
+/* pidblas::vmulmm (vcp/pidblas.hpp:198-236): [RD(A^T A), RU(A^T A)], A k x n point. */
+int orc_pidblas_vmulmm(int n, int k, const double* A, double* C, int nthreads) {
+  if (n <= 0) return 0;
+  if (k < 0) k = 0;
+  const long na = (long)k * n, nc = (long)n * n;
+  double* buf = (double*)malloc(sizeof(double) * (na + 1 + 2 * nc));
+  if (!buf) return 1;
+  double *At = buf, *lo = At + na + 1, *up = lo + nc;
+  transpose_d(k, n, A, At);
+  orc_rmatmul(n, k, n, At, A, lo, -1, nthreads);
+  orc_rmatmul(n, k, n, At, A, up, 1, nthreads);
+  for (long i = 0; i < nc; ++i) {
+    C[2 * i] = lo[i];
+    C[2 * i + 1] = up[i];
+  }
+  free(buf);
+  return 0;
+}
+
+/* The bound ||R [A] - I||_inf of imats::linearsolve (vcp/imats.hpp:316-336,
+ * mats::norminf vcp/mats.hpp:1583-1597). */
+double orc_norm_I_minus_RA(int n, const double* R, const double* A, int nthreads) {
+  double* b = (double*)malloc(sizeof(double) * 2 * (size_t)n * n);
+  if (!b) return NAN;
+  orc_pidblas_mul_point(1, n, n, n, R, A, b, nthreads);
+  const int prev = fegetround();
+  double g = -INFINITY;
+  for (int i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < n; ++j) {
+      double lo = b[2 * (i + (long)n * j)], up = b[2 * (i + (long)n * j) + 1];
+      if (i == j) {
+        volatile double vl = lo, vu = up;
+        fesetround(FE_DOWNWARD);
+        volatile double l2 = vl - 1.0;
+        fesetround(FE_UPWARD);
+        volatile double u2 = vu - 1.0;
+        fesetround(FE_TONEAREST);
+        lo = l2;
+        up = u2;
+      }
+      const double mg = fmax(fabs(lo), fabs(up));
+      volatile double vs = s, vm = mg;
+      fesetround(FE_UPWARD);
+      volatile double ns = (j == 0) ? vm : vs + vm;
+      fesetround(FE_TONEAREST);
+      s = ns;
+    }
+    if (isnan(s))
+      g = NAN;
+    else if (!isnan(g) && s > g)
+      g = s;
+  }
+  fesetround(prev);
+  free(b);
+  return g;
+}

@@ -52,6 +52,38 @@ def main() -> None:
         data[f"iv{idx}_A"] = A
         data[f"iv{idx}_B"] = B
         data[f"iv{idx}_C"] = O.ref_pidblas_mulmm(m, n, k, A, B)
+    # pidblas::mul_im_m / mul_m_im, mulltmm, vmulmm and the linearsolve bound
+    import ctypes
+    pcases = [(0, 9, 7, 11), (1, 9, 7, 11), (0, 33, 20, 64), (1, 20, 33, 64)]
+    for idx, (side, m, n, k) in enumerate(pcases):
+        L = W.interval_ephi(rng, m, k, 4, 2.0 ** -30) if side == 0 else W.ephi(rng, m * k, 4)
+        R = W.ephi(rng, k * n, 4) if side == 0 else W.interval_ephi(rng, k, n, 4, 2.0 ** -30)
+        C = np.zeros(2 * m * n)
+        assert O.ref_call("ref_pidblas_mul_point", side, m, n, k, O._p(L), O._p(R), O._p(C)) == 0
+        data[f"mp{idx}_shape"] = np.array([side, m, n, k])
+        data[f"mp{idx}_L"], data[f"mp{idx}_R"], data[f"mp{idx}_C"] = L, R, C
+    for idx, (n, k) in enumerate([(6, 9), (40, 33)]):
+        A = W.interval_ephi(rng, k, n, 4, 2.0 ** -20)
+        C = np.zeros(2 * n * n)
+        assert O.ref_call("ref_pidblas_mulltmm", n, k, O._p(A), O._p(C)) == 0
+        P = W.ephi(rng, k * n, 8)
+        V = np.zeros(2 * n * n)
+        assert O.ref_call("ref_pidblas_vmulmm", n, k, O._p(P), O._p(V)) == 0
+        data[f"sy{idx}_shape"] = np.array([n, k])
+        data[f"sy{idx}_A"], data[f"sy{idx}_C"] = A, C
+        data[f"sy{idx}_P"], data[f"sy{idx}_V"] = P, V
+    for idx, nn in enumerate([12, 48]):
+        Am = np.eye(nn) + 0.05 * rng.standard_normal((nn, nn))
+        Ai = W._kv(Am.ravel(order="F"), np.abs(Am.ravel(order="F")) * 1e-9)
+        Rinv = np.linalg.inv(Am).ravel(order="F")
+        g = ctypes.c_double(0.0)
+        assert O.ref_call("ref_norm_I_minus_RA", nn, O._p(Rinv), O._p(Ai), ctypes.addressof(g)) == 0
+        data[f"nm{idx}_n"] = np.array([nn])
+        data[f"nm{idx}_R"], data[f"nm{idx}_A"] = Rinv, Ai
+        data[f"nm{idx}_bound"] = np.array([g.value])
+    data["n_mp"] = np.array([len(pcases)])
+    data["n_sy"] = np.array([2])
+    data["n_nm"] = np.array([2])
     data["n_rm"] = np.array([len(cases)])
     data["n_iv"] = np.array([len(icases)])
     np.savez_compressed(OUT, **data)

@@ -144,3 +144,51 @@ def test_midrad_encloses(oracle):
         lo, up = Fraction(float(X[2 * t])), Fraction(float(X[2 * t + 1]))
         assert Fraction(float(m[t])) - Fraction(float(r[t])) <= lo
         assert up <= Fraction(float(m[t])) + Fraction(float(r[t]))
+
+
+def test_oracle_other_products_match_golden(oracle, golden):
+    """pidblas::mul_im_m / mul_m_im / mulltmm / vmulmm and the imats::linearsolve
+    bound, against vectors the reference produced."""
+    for idx in range(int(golden["n_mp"][0])):
+        side, m, n, k = map(int, golden[f"mp{idx}_shape"])
+        got = oracle.pidblas_mul_point(side, m, n, k, golden[f"mp{idx}_L"], golden[f"mp{idx}_R"])
+        assert np.array_equal(bits(got), bits(golden[f"mp{idx}_C"])), idx
+    for idx in range(int(golden["n_sy"][0])):
+        n, k = map(int, golden[f"sy{idx}_shape"])
+        assert np.array_equal(bits(oracle.pidblas_mulltmm(n, k, golden[f"sy{idx}_A"])),
+                              bits(golden[f"sy{idx}_C"])), idx
+        assert np.array_equal(bits(oracle.pidblas_vmulmm(n, k, golden[f"sy{idx}_P"])),
+                              bits(golden[f"sy{idx}_V"])), idx
+    for idx in range(int(golden["n_nm"][0])):
+        n = int(golden[f"nm{idx}_n"][0])
+        g = oracle.norm_I_minus_RA(n, golden[f"nm{idx}_R"], golden[f"nm{idx}_A"])
+        assert g == float(golden[f"nm{idx}_bound"][0])
+
+
+def test_oracle_other_products_match_reference_build(oracle):
+    import ctypes
+    if oracle.ref_lib() is None:
+        from oracle.build import build_reference
+        if build_reference() is None:
+            pytest.skip("reference sources not mounted")
+    rng = np.random.default_rng(8)
+    for side, m, n, k in [(0, 40, 17, 90), (1, 17, 40, 90), (0, 1, 5, 7), (1, 5, 1, 7)]:
+        L = W.interval_ephi(rng, m, k, 6, 0.01) if side == 0 else W.ephi(rng, m * k, 6)
+        R = W.ephi(rng, k * n, 6) if side == 0 else W.interval_ephi(rng, k, n, 6, 0.01)
+        ref = np.zeros(2 * m * n)
+        assert oracle.ref_call("ref_pidblas_mul_point", side, m, n, k, oracle._p(L), oracle._p(R),
+                               oracle._p(ref)) == 0
+        assert np.array_equal(bits(oracle.pidblas_mul_point(side, m, n, k, L, R)), bits(ref))
+    n, k = 30, 70
+    A = W.interval_ephi(rng, k, n, 5, 0.001)
+    ref = np.zeros(2 * n * n)
+    assert oracle.ref_call("ref_pidblas_mulltmm", n, k, oracle._p(A), oracle._p(ref)) == 0
+    assert np.array_equal(bits(oracle.pidblas_mulltmm(n, k, A)), bits(ref))
+    nn = 25
+    Am = np.eye(nn) + 0.1 * rng.standard_normal((nn, nn))
+    Ai = W._kv(Am.ravel(order="F"), np.abs(Am.ravel(order="F")) * 1e-6)
+    Rinv = np.linalg.inv(Am).ravel(order="F")
+    g = ctypes.c_double(0.0)
+    assert oracle.ref_call("ref_norm_I_minus_RA", nn, oracle._p(Rinv), oracle._p(Ai),
+                           ctypes.addressof(g)) == 0
+    assert oracle.norm_I_minus_RA(nn, Rinv, Ai) == g.value

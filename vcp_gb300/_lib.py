@@ -32,6 +32,14 @@ SIGNATURES: dict[str, tuple] = {
     "vcpcu_udmatmul_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _v, _i, _v]),
     "vcpcu_igemm_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _i, _i, _v]),
     "vcpcu_igemm": (_i, [_i, _i, _i, _v, _v, _v, _i, _i]),
+    "vcpcu_igemm_point_dev": (_i, [_i, _i, _i, _i, _v, _i, _v, _i, _v, _i, _i, _i, _v]),
+    "vcpcu_igemm_point": (_i, [_i, _i, _i, _i, _v, _v, _v, _i, _i]),
+    "vcpcu_isyrk_dev": (_i, [_i, _i, _v, _i, _v, _i, _i, _i, _v]),
+    "vcpcu_isyrk": (_i, [_i, _i, _v, _v, _i, _i]),
+    "vcpcu_vsyrk_dev": (_i, [_i, _i, _v, _i, _v, _i, _v]),
+    "vcpcu_vsyrk": (_i, [_i, _i, _v, _v]),
+    "vcpcu_norm_I_minus_RA_dev": (_i, [_i, _v, _i, _v, _i, _v, _i, _i, _v]),
+    "vcpcu_norm_I_minus_RA": (_i, [_i, _v, _v, _v, _i, _i]),
     "vcpcu_igemm_noalloc_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _i, _v]),
 }
 

@@ -3,6 +3,7 @@
 #include "common.cuh"
 #include "plain_gemm.cuh"
 #include "ozaki.cuh"
+#include "variants.cuh"
 
 #include <cstring>
 
@@ -117,8 +118,10 @@ int igemm_check(int m, int n, int k, const double* A, int lda, const double* B, 
   return VCPCU_OK;
 }
 
-int igemm_dispatch(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
-                   double* C, long ldc, int form, int slices, cudaStream_t s) {
+}  // namespace
+
+int vcpcu::igemm_any(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
+                     double* C, long ldc, int form, int slices, cudaStream_t s) {
   if (k < 0) k = 0;
   if (form == VCPCU_FORM_PLAIN) {
     Scratch ws;
@@ -127,6 +130,34 @@ int igemm_dispatch(int m, int n, int k, const double* A, long lda, const double*
     return launch_interval_gemm_plain(m, n, k, A, lda, B, ldb, C, ldc, (double*)ws.ptr, s);
   }
   return ozaki_igemm(m, n, k, A, lda, B, ldb, C, ldc, form, slices, s);
+}
+
+namespace {
+
+int igemm_dispatch(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
+                   double* C, long ldc, int form, int slices, cudaStream_t s) {
+  return igemm_any(m, n, k, A, lda, B, ldb, C, ldc, form, slices, s);
+}
+
+int form_check(int form, int slices) {
+  if (form != VCPCU_FORM_PLAIN && form != VCPCU_FORM_OZAKI && form != VCPCU_FORM_AUTO &&
+      form != VCPCU_FORM_OZAKI_SLICES) {
+    set_error("unknown form %d", form);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (form != VCPCU_FORM_PLAIN && slices != 0 && (slices < 2 || slices > OZ_MAX_SLICES)) {
+    set_error("slices must be 0 or in [2, %d], got %d", OZ_MAX_SLICES, slices);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  return VCPCU_OK;
+}
+
+bool misaligned16(const void* p) { return ((uintptr_t)p & 15) != 0; }
+
+// Copies `n` doubles host -> device into dst (skips n == 0).
+int h2d(double* dst, const double* src, size_t n, cudaStream_t s) {
+  if (n) VCPCU_CUDA_TRY(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  return VCPCU_OK;
 }
 
 int take_status() {
@@ -225,6 +256,182 @@ int vcpcu_igemm(int m, int n, int k, const double* A, const double* B, double* C
   VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
   if (form != VCPCU_FORM_PLAIN) return take_status();
   return VCPCU_OK;
+}
+
+int vcpcu_igemm_point_dev(int interval_side, int m, int n, int k, const double* L, int ldl,
+                          const double* R, int ldr, double* C, int ldc, int form, int slices,
+                          void* stream) {
+  clear_error();
+  int st = form_check(form, slices);
+  if (st) return st;
+  if (interval_side != 0 && interval_side != 1) {
+    set_error("igemm_point: interval_side must be 0 ([L]*R) or 1 (L*[R])");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (m <= 0 || n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (!C || (k > 0 && (!L || !R)) || ldc < m || (k > 0 && (ldl < m || ldr < k))) {
+    set_error("igemm_point: null pointer or leading dimension too small");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (form != VCPCU_FORM_PLAIN && k > 0 && misaligned16(interval_side == 0 ? L : R)) {
+    set_error("igemm_point: the interval factor must be 16-byte aligned for the Ozaki form");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  return igemm_point_dispatch(interval_side, m, n, k, L, ldl, R, ldr, C, ldc, form, slices,
+                              (cudaStream_t)stream);
+}
+
+int vcpcu_igemm_point(int interval_side, int m, int n, int k, const double* L, const double* R,
+                      double* C, int form, int slices) {
+  clear_error();
+  int st = form_check(form, slices);
+  if (st) return st;
+  if (interval_side != 0 && interval_side != 1) {
+    set_error("igemm_point: interval_side must be 0 ([L]*R) or 1 (L*[R])");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (m <= 0 || n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (!C || (k > 0 && (!L || !R))) {
+    set_error("igemm_point: null pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  cudaStream_t s = host_stream();
+  const size_t wl = interval_side == 0 ? 2 : 1, wr = interval_side == 0 ? 1 : 2;
+  const size_t nl = wl * (size_t)m * k, nr = wr * (size_t)k * n, nc = 2 * (size_t)m * n;
+  Scratch buf;
+  if ((st = buf.alloc(sizeof(double) * (nl + nr + nc), s))) return st;
+  // the interval factor first, so that it is 16-byte aligned
+  double* base = (double*)buf.ptr;
+  double* dL = interval_side == 0 ? base : base + nr;
+  double* dR = interval_side == 0 ? base + nl : base;
+  double* dC = base + nl + nr;
+  if ((st = h2d(dL, L, nl, s)) || (st = h2d(dR, R, nr, s))) return st;
+  st = igemm_point_dispatch(interval_side, m, n, k, dL, m, dR, k > 0 ? k : 1, dC, m, form, slices,
+                            s);
+  if (st) return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(C, dC, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  return form != VCPCU_FORM_PLAIN ? take_status() : VCPCU_OK;
+}
+
+int vcpcu_isyrk_dev(int n, int k, const double* A, int lda, double* C, int ldc, int form,
+                    int slices, void* stream) {
+  clear_error();
+  int st = form_check(form, slices);
+  if (st) return st;
+  if (n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (!C || (k > 0 && !A) || ldc < n || (k > 0 && lda < k)) {
+    set_error("isyrk: null pointer or leading dimension too small");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  return isyrk_dispatch(n, k, A, lda, C, ldc, form, slices, (cudaStream_t)stream);
+}
+
+int vcpcu_isyrk(int n, int k, const double* A, double* C, int form, int slices) {
+  clear_error();
+  int st = form_check(form, slices);
+  if (st) return st;
+  if (n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (!C || (k > 0 && !A)) {
+    set_error("isyrk: null pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  cudaStream_t s = host_stream();
+  const size_t na = 2 * (size_t)k * n, nc = 2 * (size_t)n * n;
+  Scratch buf;
+  if ((st = buf.alloc(sizeof(double) * (na + nc), s))) return st;
+  double* dA = (double*)buf.ptr;
+  double* dC = dA + na;
+  if ((st = h2d(dA, A, na, s))) return st;
+  if ((st = isyrk_dispatch(n, k, dA, k > 0 ? k : 1, dC, n, form, slices, s))) return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(C, dC, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  return form != VCPCU_FORM_PLAIN ? take_status() : VCPCU_OK;
+}
+
+int vcpcu_vsyrk_dev(int n, int k, const double* A, int lda, double* C, int ldc, void* stream) {
+  clear_error();
+  if (n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (!C || (k > 0 && !A) || ldc < n || (k > 0 && lda < k)) {
+    set_error("vsyrk: null pointer or leading dimension too small");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  int st = check_device();
+  if (st) return st;
+  return vsyrk_dispatch(n, k, A, lda, C, ldc, (cudaStream_t)stream);
+}
+
+int vcpcu_vsyrk(int n, int k, const double* A, double* C) {
+  clear_error();
+  if (n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (!C || (k > 0 && !A)) {
+    set_error("vsyrk: null pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  int st = check_device();
+  if (st) return st;
+  cudaStream_t s = host_stream();
+  const size_t na = (size_t)k * n, nc = 2 * (size_t)n * n;
+  Scratch buf;
+  if ((st = buf.alloc(sizeof(double) * (na + nc), s))) return st;
+  double* dA = (double*)buf.ptr;
+  double* dC = dA + na;
+  if ((st = h2d(dA, A, na, s))) return st;
+  if ((st = vsyrk_dispatch(n, k, dA, k > 0 ? k : 1, dC, n, s))) return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(C, dC, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  return VCPCU_OK;
+}
+
+int vcpcu_norm_I_minus_RA_dev(int n, const double* R, int ldr, const double* A, int lda,
+                              double* bound, int form, int slices, void* stream) {
+  clear_error();
+  int st = form_check(form, slices);
+  if (st) return st;
+  if (n <= 0 || !R || !A || !bound || ldr < n || lda < n) {
+    set_error("norm_I_minus_RA: n must be positive, pointers non-null, ld >= n");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (form != VCPCU_FORM_PLAIN && misaligned16(A)) {
+    set_error("norm_I_minus_RA: A must be 16-byte aligned for the Ozaki form");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  return norm_dispatch(n, R, ldr, A, lda, bound, form, slices, (cudaStream_t)stream);
+}
+
+int vcpcu_norm_I_minus_RA(int n, const double* R, const double* A, double* bound, int form,
+                          int slices) {
+  clear_error();
+  int st = form_check(form, slices);
+  if (st) return st;
+  if (n <= 0 || !R || !A || !bound) {
+    set_error("norm_I_minus_RA: n must be positive and pointers non-null");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  cudaStream_t s = host_stream();
+  const size_t nr = (size_t)n * n, na = 2 * (size_t)n * n;
+  Scratch buf;
+  if ((st = buf.alloc(sizeof(double) * (nr + na + 1), s))) return st;
+  double* dA = (double*)buf.ptr;  // interval factor first: 16-byte aligned
+  double* dR = dA + na;
+  double* dB = dR + nr;
+  if ((st = h2d(dR, R, nr, s)) || (st = h2d(dA, A, na, s))) return st;
+  if ((st = norm_dispatch(n, dR, n, dA, n, dB, form, slices, s))) return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(bound, dB, sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  return form != VCPCU_FORM_PLAIN ? take_status() : VCPCU_OK;
 }
 
 }  // extern "C"

@@ -154,9 +154,10 @@ __device__ __forceinline__ void midrad_dev(double lo, double up, double& m, doub
 
 // Left factor: interval A (m x k, ld in intervals) -> planes mA, pA = |mA| +ru rA, rA
 // (ld = M).  Right factor: interval B -> planes mB, rB (ld = K).
+// With plus_rad == 0 the middle plane is |mA| itself (the Aᵀ[A] kernel).
 __global__ void interval_prep_left(int M, int K, const double* __restrict__ A, long lda,
                                    double* __restrict__ mA, double* __restrict__ pA,
-                                   double* __restrict__ rA) {
+                                   double* __restrict__ rA, int plus_rad = 1) {
   long total = (long)M * K;
   for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (long)gridDim.x * blockDim.x) {
@@ -166,7 +167,7 @@ __global__ void interval_prep_left(int M, int K, const double* __restrict__ A, l
     midrad_dev(e[0], e[1], m, r);
     mA[idx] = m;
     rA[idx] = r;
-    pA[idx] = __dadd_ru(fabs(m), r);
+    pA[idx] = plus_rad ? __dadd_ru(fabs(m), r) : fabs(m);
   }
 }
 
@@ -298,6 +299,121 @@ interval_gemm_kernel(int M, int N, int K, const double* __restrict__ mA,
     }
 }
 
+// [A]ᵀ[A] with pidblas::mulltmm semantics (vcp/pidblas.hpp:296-358) over
+// prepped planes: X = Aᵀ (n x k: mX, aX = |mX|, rX), Y = A (k x n: mY, rY).
+// Five chains per entry (i, j):
+//   lo = RD Σ mX mY, up = RU Σ mX mY          (dsyrk under RD / RU)
+//   t1 = RU Σ aX rY   = (|mA|ᵀ rA)(i,j)       (the dgemm temp)
+//   t2 = RU Σ rX |mY| = (|mA|ᵀ rA)(j,i)
+//   t3 = RU Σ rX rY   = (rAᵀ rA)(i,j)          (dsyrk of rA)
+// temp = t1 +ru (t2 +ru t3) for i <= j; C(i,j) = C(j,i) =
+// [lo -rd temp, up +ru temp] taken from the upper triangle.
+__global__ void __launch_bounds__(NT)
+syrk_interval_kernel(int N, int K, const double* __restrict__ mX, const double* __restrict__ aX,
+                     const double* __restrict__ rX, const double* __restrict__ mY,
+                     const double* __restrict__ rY, double* __restrict__ C, long ldc) {
+  __shared__ double Xm[2][BKI][BM], Xa[2][BKI][BM], Xr[2][BKI][BM];
+  __shared__ double Ym[2][BKI][BN], Yr[2][BKI][BN];
+  const int row0 = blockIdx.x * BM, col0 = blockIdx.y * BN;
+  if (col0 + BN <= row0) return;  // tile entirely below the diagonal
+  const int tid = threadIdx.x;
+  const int tr = tid / 16, tc = tid % 16;
+  const int a_i = tid % BM, a_k = tid / BM;
+  const int b_k = tid % BKI, b_j = tid / BKI;
+  constexpr int QA = BKI / (NT / BM), QB = BN / (NT / BKI);
+  double lo[4][4], up[4][4], t1[4][4], t2[4][4], t3[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) lo[i][j] = up[i][j] = t1[i][j] = t2[i][j] = t3[i][j] = 0.0;
+  double ram[QA], raa[QA], rar[QA], rbm[QB], rbr[QB];
+  auto load_tile = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < QA; ++q) {
+      int gi = row0 + a_i, gk = k0 + a_k + (NT / BM) * q;
+      bool ok = gi < N && gk < K;
+      long o = gi + (long)gk * N;
+      ram[q] = ok ? mX[o] : 0.0;
+      raa[q] = ok ? aX[o] : 0.0;
+      rar[q] = ok ? rX[o] : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < QB; ++q) {
+      int hk = k0 + b_k, hj = col0 + b_j + (NT / BKI) * q;
+      bool okb = hk < K && hj < N;
+      long ob = hk + (long)hj * K;
+      rbm[q] = okb ? mY[ob] : 0.0;
+      rbr[q] = okb ? rY[ob] : 0.0;
+    }
+  };
+  auto store_tile = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < QA; ++q) {
+      Xm[buf][a_k + (NT / BM) * q][a_i] = ram[q];
+      Xa[buf][a_k + (NT / BM) * q][a_i] = raa[q];
+      Xr[buf][a_k + (NT / BM) * q][a_i] = rar[q];
+    }
+#pragma unroll
+    for (int q = 0; q < QB; ++q) {
+      Ym[buf][b_k][b_j + (NT / BKI) * q] = rbm[q];
+      Yr[buf][b_k][b_j + (NT / BKI) * q] = rbr[q];
+    }
+  };
+  const int nk = (K + BKI - 1) / BKI;
+  load_tile(0);
+  store_tile(0);
+  __syncthreads();
+  for (int t = 0; t < nk; ++t) {
+    const int buf = t & 1;
+    if (t + 1 < nk) load_tile((t + 1) * BKI);
+#pragma unroll 2
+    for (int kk = 0; kk < BKI; ++kk) {
+      double xm[4], xa[4], xr[4], ym[4], yr[4], ya[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        xm[i] = Xm[buf][kk][tr + 16 * i];
+        xa[i] = Xa[buf][kk][tr + 16 * i];
+        xr[i] = Xr[buf][kk][tr + 16 * i];
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        ym[j] = Ym[buf][kk][tc + 16 * j];
+        yr[j] = Yr[buf][kk][tc + 16 * j];
+        ya[j] = fabs(ym[j]);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          lo[i][j] = __fma_rd(xm[i], ym[j], lo[i][j]);
+          up[i][j] = __fma_ru(xm[i], ym[j], up[i][j]);
+          t1[i][j] = __fma_ru(xa[i], yr[j], t1[i][j]);
+          t2[i][j] = __fma_ru(xr[i], ya[j], t2[i][j]);
+          t3[i][j] = __fma_ru(xr[i], yr[j], t3[i][j]);
+        }
+    }
+    if (t + 1 < nk) store_tile(buf ^ 1);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int gi = row0 + tr + 16 * i, gj = col0 + tc + 16 * j;
+      if (gi < N && gj < N && gi <= gj) {
+        const double temp = __dadd_ru(t1[i][j], __dadd_ru(t2[i][j], t3[i][j]));
+        const double u = __dadd_ru(up[i][j], temp);
+        const double l = __dsub_rd(lo[i][j], temp);
+        double* e = C + 2 * (gi + (long)gj * ldc);
+        e[0] = l;
+        e[1] = u;
+        double* f = C + 2 * (gj + (long)gi * ldc);
+        f[0] = l;
+        f[1] = u;
+      }
+    }
+}
+
 inline int grid_1d(long total) {
   long b = (total + 255) / 256;
   if (b > 152 * 32) b = 152 * 32;
@@ -357,6 +473,44 @@ int launch_interval_gemm_plain(int M, int N, int K, const double* A, long lda,
   VCPCU_LAUNCH_CHECK("interval_gemm_kernel");
   return VCPCU_OK;
 }
+
+// (A k x n interval, lda) -> Aᵀ (n x k, ld = n) interval.
+__global__ void transpose_interval(int K, int N, const double* __restrict__ A, long lda,
+                                   double* __restrict__ At) {
+  long total = (long)K * N;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    long j = idx % N, p = idx / N;  // At(j, p) = A(p, j), writes coalesced
+    const double* e = A + 2 * (p + j * lda);
+    At[2 * idx] = e[0];
+    At[2 * idx + 1] = e[1];
+  }
+}
+
+int launch_isyrk_plain(int N, int K, const double* A, long lda, double* C, long ldc, double* ws,
+                       cudaStream_t s) {
+  // ws: At (2 N K) + mX, aX, rX (3 N K) + mY, rY (2 K N)
+  double* At = ws;
+  double* mX = At + 2 * (size_t)N * K;
+  double* aX = mX + (size_t)N * K;
+  double* rX = aX + (size_t)N * K;
+  double* mY = rX + (size_t)N * K;
+  double* rY = mY + (size_t)N * K;
+  if (K > 0) {
+    transpose_interval<<<grid_1d((long)N * K), 256, 0, s>>>(K, N, A, lda, At);
+    VCPCU_LAUNCH_CHECK("transpose_interval");
+    interval_prep_left<<<grid_1d((long)N * K), 256, 0, s>>>(N, K, At, N, mX, aX, rX, 0);
+    VCPCU_LAUNCH_CHECK("interval_prep_left");
+    interval_prep_right<<<grid_1d((long)K * N), 256, 0, s>>>(K, N, A, lda, mY, rY);
+    VCPCU_LAUNCH_CHECK("interval_prep_right");
+  }
+  dim3 grid((N + BM - 1) / BM, (N + BN - 1) / BN);
+  syrk_interval_kernel<<<grid, NT, 0, s>>>(N, K, mX, aX, rX, mY, rY, C, ldc);
+  VCPCU_LAUNCH_CHECK("syrk_interval_kernel");
+  return VCPCU_OK;
+}
+
+size_t isyrk_plain_ws_bytes(int N, int K) { return sizeof(double) * 7 * (size_t)N * K; }
 
 size_t interval_gemm_plain_ws_bytes(int M, int N, int K) {
   return sizeof(double) * (3 * (size_t)M * K + 2 * (size_t)K * N);

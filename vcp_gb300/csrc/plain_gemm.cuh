@@ -20,4 +20,10 @@ int launch_interval_gemm_plain(int M, int N, int K, const double* A, long lda,
                                double* ws, cudaStream_t s);
 size_t interval_gemm_plain_ws_bytes(int M, int N, int K);
 
+// C = [A]ᵀ[A] (A K x N interval) with pidblas::mulltmm semantics, full
+// symmetric output; ws holds isyrk_plain_ws_bytes(N, K).
+int launch_isyrk_plain(int N, int K, const double* A, long lda, double* C, long ldc, double* ws,
+                       cudaStream_t s);
+size_t isyrk_plain_ws_bytes(int N, int K);
+
 }  // namespace vcpcu

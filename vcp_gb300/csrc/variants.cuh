@@ -1,0 +1,22 @@
+// variants.cuh -- interval x point, [A]^T[A], verified A^T A, ||R[A] - I||.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace vcpcu {
+
+// Interval product of either form on device pointers (defined in capi.cu).
+int igemm_any(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
+              double* C, long ldc, int form, int slices, cudaStream_t s);
+
+// interval_side 0: C = [L] * R (R point, pidblas::mul_im_m);
+// interval_side 1: C = L * [R] (L point, pidblas::mul_m_im).
+int igemm_point_dispatch(int interval_side, int m, int n, int k, const double* L, long ldl,
+                         const double* R, long ldr, double* C, long ldc, int form, int slices,
+                         cudaStream_t s);
+int isyrk_dispatch(int n, int k, const double* A, long lda, double* C, long ldc, int form,
+                   int slices, cudaStream_t s);
+int vsyrk_dispatch(int n, int k, const double* A, long lda, double* C, long ldc, cudaStream_t s);
+int norm_dispatch(int n, const double* R, long ldr, const double* A, long lda, double* bound,
+                  int form, int slices, cudaStream_t s);
+
+}  // namespace vcpcu

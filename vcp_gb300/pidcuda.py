@@ -61,3 +61,50 @@ def mulmm_dev(m, n, k, A, lda, B, ldb, C, ldc, form=FORM_PLAIN, slices=0, stream
     """Device-pointer interval product on a CUDA stream (torch tensors)."""
     _lib.call("vcpcu_igemm_dev", m, n, k, _dev_ptr(A, "A"), lda, _dev_ptr(B, "B"), ldb,
               _dev_ptr(C, "C"), ldc, int(form), int(slices), _stream_ptr(stream))
+
+
+# ---- interval x point, [A]^T[A], verified A^T A, ||R[A] - I|| ------------------
+
+def mul_point(interval_side: int, L: np.ndarray, R: np.ndarray, m: int, n: int, k: int,
+              form: int = FORM_PLAIN, slices: int = 0) -> np.ndarray:
+    """interval_side 0: [L] * R (pidblas::mul_im_m); 1: L * [R] (pidblas::mul_m_im).
+    The interval factor is a kv buffer, the point factor a float64 buffer."""
+    out = np.empty(2 * m * n, dtype=np.float64)
+    if m <= 0 or n <= 0:
+        return out
+    wl, wr = (2, 1) if interval_side == 0 else (1, 2)
+    pl = _host_ptr(L, wl * m * k, "L") if k > 0 else None
+    pr = _host_ptr(R, wr * k * n, "R") if k > 0 else None
+    _lib.call("vcpcu_igemm_point", int(interval_side), m, n, k, pl, pr, out.ctypes.data,
+              int(form), int(slices))
+    return out
+
+
+def isyrk(A: np.ndarray, n: int, k: int, form: int = FORM_PLAIN, slices: int = 0) -> np.ndarray:
+    """[A]^T [A] for an interval A (k x n): pidblas::mulltmm."""
+    out = np.empty(2 * n * n, dtype=np.float64)
+    if n <= 0:
+        return out
+    pa = _host_ptr(A, 2 * k * n, "A") if k > 0 else None
+    _lib.call("vcpcu_isyrk", n, k, pa, out.ctypes.data, int(form), int(slices))
+    return out
+
+
+def vsyrk(A: np.ndarray, n: int, k: int) -> np.ndarray:
+    """Verified A^T A of a point A (k x n): pidblas::vmulmm."""
+    out = np.empty(2 * n * n, dtype=np.float64)
+    if n <= 0:
+        return out
+    pa = _host_ptr(A, k * n, "A") if k > 0 else None
+    _lib.call("vcpcu_vsyrk", n, k, pa, out.ctypes.data)
+    return out
+
+
+def norm_I_minus_RA(R: np.ndarray, A: np.ndarray, n: int, form: int = FORM_PLAIN,
+                    slices: int = 0) -> float:
+    """Upper bound of ||R [A] - I||_inf (the check of imats::linearsolve)."""
+    import ctypes
+    out = ctypes.c_double(0.0)
+    _lib.call("vcpcu_norm_I_minus_RA", n, _host_ptr(R, n * n, "R"), _host_ptr(A, 2 * n * n, "A"),
+              ctypes.addressof(out), int(form), int(slices))
+    return out.value
