@@ -1,0 +1,149 @@
+// vcp_cuda/pidcuda.hpp -- vcp::pidcuda, the GPU drop-in for vcp::pidblas.
+//
+// Use exactly like pidblas (vcp/pidblas.hpp:87):
+//     vcp::matrix< kv::interval<double>, vcp::pidcuda > A, B, C;
+//     C = A * B;                  // pidcuda::mulmm        (pidblas.hpp:239)
+//     C = ltransmul(A);           // pidcuda::mulltmm      (pidblas.hpp:296)
+//     x = lss(A, b);              // imats::linearsolve -> mul_im_m / mul_m_im
+// The class derives from vcp::imats<double, vcp::pdblas> as pidblas does, so
+// every imats algorithm (linearsolve, eigsym, eigsymge) routes its interval
+// products through the hooks below to libvcpcuda (include/vcpcuda.h).
+//
+// Form and precision are process-wide settings:
+//     vcp::pidcuda_settings::form()   = VCPCU_FORM_OZAKI;   // default
+//     vcp::pidcuda_settings::slices() = 0;                  // default precision
+// VCPCU_FORM_PLAIN reproduces pidblas bit for bit over a sequential-chain
+// BLAS; the Ozaki forms enclose the same products on the tensor cores.
+// Non-zero statuses become vcp::dimension_error (bad shapes) or
+// vcp::state_error (everything else), as pidblas reports its failures
+// (vcp/error.hpp).  Scalar ('S') operands keep the host shortcuts of pidblas.
+#ifndef VCP_CUDA_PIDCUDA_HPP
+#define VCP_CUDA_PIDCUDA_HPP
+
+#include <kv/interval.hpp>
+#include <vcp/error.hpp>
+#include <vcp/imats.hpp>
+#include <vcp/pdblas.hpp>
+
+#include "../vcpcuda.h"
+
+namespace vcp {
+
+struct pidcuda_settings {
+  static int& form() {
+    static int f = VCPCU_FORM_OZAKI;
+    return f;
+  }
+  static int& slices() {
+    static int s = 0;
+    return s;
+  }
+};
+
+namespace pidcuda_detail {
+static_assert(sizeof(kv::interval<double>) == 2 * sizeof(double),
+              "kv::interval<double> must be two packed doubles {inf, sup}");
+inline const double* cd(const std::vector<kv::interval<double> >& v) {
+  return reinterpret_cast<const double*>(v.data());
+}
+inline double* md(std::vector<kv::interval<double> >& v) {
+  return reinterpret_cast<double*>(v.data());
+}
+inline void check(int st, const char* what) {
+  if (st == VCPCU_OK) return;
+  if (st == VCPCU_ERR_INVALID_ARG)
+    vcp::throw_error<vcp::dimension_error>(what, ": ", vcpcu_last_error_string());
+  vcp::throw_error<vcp::state_error>(what, ": ", vcpcu_last_error_string());
+}
+}  // namespace pidcuda_detail
+
+class pidcuda : public vcp::imats<double, vcp::pdblas> {
+  typedef vcp::imats<double, vcp::pdblas> base;
+
+ protected:
+  // C = [A] * B, B point (pidblas::mul_im_m)
+  void mul_im_m(const vcp::pdblas& B, base& c) const override {
+    if (this->type == 'S' || B.type == 'S') {
+      base::mul_im_m(B, c);
+      return;
+    }
+    if (this->column != B.row)
+      vcp::throw_error<vcp::dimension_error>("pidcuda::mul_im_m: (", this->row, ", ",
+                                             this->column, ") * (", B.row, ", ", B.column, ")");
+    c.zeros(this->row, B.column);
+    pidcuda_detail::check(
+        vcpcu_igemm_point(0, this->row, B.column, this->column, pidcuda_detail::cd(this->v),
+                          B.v.data(), pidcuda_detail::md(c.v), pidcuda_settings::form(),
+                          pidcuda_settings::slices()),
+        "pidcuda::mul_im_m");
+  }
+  // C = B * [A], B point (pidblas::mul_m_im)
+  void mul_m_im(const vcp::pdblas& B, base& c) const override {
+    if (this->type == 'S' || B.type == 'S') {
+      base::mul_m_im(B, c);
+      return;
+    }
+    if (B.column != this->row)
+      vcp::throw_error<vcp::dimension_error>("pidcuda::mul_m_im: (", B.row, ", ", B.column,
+                                             ") * (", this->row, ", ", this->column, ")");
+    c.zeros(B.row, this->column);
+    pidcuda_detail::check(
+        vcpcu_igemm_point(1, B.row, this->column, B.column, B.v.data(),
+                          pidcuda_detail::cd(this->v), pidcuda_detail::md(c.v),
+                          pidcuda_settings::form(), pidcuda_settings::slices()),
+        "pidcuda::mul_m_im");
+  }
+  // this = verified C^T C of a point C (pidblas::vmulmm)
+  void vmulmm(const vcp::pdblas& C) override {
+    if (C.type == 'S') {
+      base::vmulmm(C);
+      return;
+    }
+    this->zeros(C.column, C.column);
+    pidcuda_detail::check(
+        vcpcu_vsyrk(C.column, C.row, C.v.data(), pidcuda_detail::md(this->v)), "pidcuda::vmulmm");
+  }
+
+ public:
+  // C = [A] * [B] (pidblas::mulmm)
+  void mulmm(const vcp::mats<kv::interval<double> >& B,
+             vcp::mats<kv::interval<double> >& c) const override {
+    if (this->type == 'S' || B.type == 'S') {
+      // scalar times matrix: elementwise interval products on the host
+      if (this->type == 'S') {
+        c = B;
+        for (int i = 0; i < B.n; i++) c.v[i] *= this->v[0];
+      } else {
+        c = *this;
+        for (int i = 0; i < this->n; i++) c.v[i] *= B.v[0];
+      }
+      return;
+    }
+    if (this->column != B.row)
+      vcp::throw_error<vcp::dimension_error>("pidcuda::mulmm: (", this->row, ", ", this->column,
+                                             ") * (", B.row, ", ", B.column, ")");
+    c.zeros(this->row, B.column);
+    pidcuda_detail::check(
+        vcpcu_igemm(this->row, B.column, this->column, pidcuda_detail::cd(this->v),
+                    pidcuda_detail::cd(B.v), pidcuda_detail::md(c.v), pidcuda_settings::form(),
+                    pidcuda_settings::slices()),
+        "pidcuda::mulmm");
+  }
+  // C = [A]^T [A] (pidblas::mulltmm)
+  void mulltmm(vcp::mats<kv::interval<double> >& c) const override {
+    if (this->type == 'S') {
+      c.zeros(1, 1);
+      c.v[0] = this->v[0] * this->v[0];
+      return;
+    }
+    c.zeros(this->column, this->column);
+    pidcuda_detail::check(
+        vcpcu_isyrk(this->column, this->row, pidcuda_detail::cd(this->v), pidcuda_detail::md(c.v),
+                    pidcuda_settings::form(), pidcuda_settings::slices()),
+        "pidcuda::mulltmm");
+  }
+};
+
+}  // namespace vcp
+
+#endif  // VCP_CUDA_PIDCUDA_HPP
