@@ -184,6 +184,28 @@ int vcpcu_norm_I_minus_RA_dev(int n, const double* R, int ldr, const double* A,
 int vcpcu_norm_I_minus_RA(int n, const double* R, const double* A, double* bound,
                           int form, int slices);
 
+/* ---- double-double GEMM (pddblas::mulmm, vcp/pddblas.hpp:318-376) --------- */
+
+/* C = A * B for kv::dd matrices (pairs {a1, a2} of doubles, column-major;
+ * A m x k, B k x n, C m x n) -- replaces pddblas::mulmm and, with A^T as
+ * the left factor, pddblas::mulltmm (:379-409).  Each dd entry is scaled
+ * per row (A) / column (B) to a w-bit integer, w = 8 * slices (7 <= slices
+ * <= 14; 0 = default 13, w = 104; lowered for very long k); the integer
+ * product is exact (residues modulo up to 32 moduli <= 256 on the bf16
+ * tensor cores, Chinese remaindering in 256-bit arithmetic) and is rounded
+ * to the dd C = c.a1 + c.a2 (round to nearest, then the exact remainder to
+ * nearest).  If Cerr != NULL it receives a rigorous upper bound of
+ * |A B - C| per entry (ld lde): the truncation of the operands to w bits,
+ * k 2^(E_i + F_j - w) (1 + 2^-40), plus the conversion error; +Inf marks
+ * entries whose scaling leaves the normal double range.  Non-finite inputs
+ * make every output NaN (VCPCU_ERR_NONFINITE from the host form, or
+ * vcpcu_status).  A and B must be 16-byte aligned. */
+int vcpcu_ddgemm_dev(int m, int n, int k, const double* A, int lda,
+                     const double* B, int ldb, double* C, int ldc, double* Cerr,
+                     int lde, int slices, void* stream);
+int vcpcu_ddgemm(int m, int n, int k, const double* A, const double* B,
+                 double* C, double* Cerr, int slices);
+
 /* ---- interval GEMM without device allocation ------------------------------ */
 
 /* Size of the static device scratch used by vcpcu_igemm_noalloc_dev. */

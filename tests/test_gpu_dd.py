@@ -1,0 +1,64 @@
+"""GPU parity of the dd GEMM (pddblas::mulmm semantics, vcpcu_ddgemm):
+bit-identical to the exact-integer host model (tests/dd_model.py), and the
+returned bound holds against the exact product (Python rationals)."""
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from vcp_gb300 import pddcuda
+from vcp_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def dd_matrix(rng, rows, cols, phi):
+    hi = W.ephi(rng, rows * cols, phi)
+    lo = hi * 2.0 ** -53 * rng.uniform(-1, 1, rows * cols)
+    out = np.empty(2 * rows * cols)
+    out[0::2], out[1::2] = hi, lo
+    return out
+
+
+@pytest.mark.parametrize("case", [(1, 1, 1, 13), (5, 7, 9, 13), (40, 33, 300, 13),
+                                  (17, 20, 1100, 10), (30, 9, 64, 7)])
+def test_ddgemm_bitexact_and_bound(cuda_lib, case):
+    from tests.dd_model import ddgemm
+    m, n, k, s = case
+    rng = np.random.default_rng(m + 10 * n + k)
+    A = dd_matrix(rng, m, k, 16)
+    B = dd_matrix(rng, k, n, 16)
+    C, E = pddcuda.mulmm(A, B, m, n, k, slices=s)
+    Cm, Em = ddgemm(m, n, k, list(A), list(B), slices=s)
+    assert np.array_equal(C.view(np.int64), np.array(Cm).view(np.int64))
+    assert np.array_equal(E.view(np.int64), np.array(Em).view(np.int64))
+    for t in range(0, m * n, max(1, (m * n) // 50)):
+        i, j = t % m, t // m
+        exact = sum((Fraction(A[2 * (i + p * m)]) + Fraction(A[2 * (i + p * m) + 1])) *
+                    (Fraction(B[2 * (p + j * k)]) + Fraction(B[2 * (p + j * k) + 1]))
+                    for p in range(k))
+        assert abs(exact - Fraction(C[2 * t]) - Fraction(C[2 * t + 1])) <= Fraction(E[t])
+
+
+def test_ddgemm_accuracy_vs_exact(cuda_lib, oracle):
+    """Relative error of the dd midpoint against the exact product (long
+    accumulator over the four double products of each dd pair)."""
+    rng = np.random.default_rng(5)
+    m = n = 64
+    k = 1024
+    A = dd_matrix(rng, m, k, 0)
+    B = dd_matrix(rng, k, n, 0)
+    C, E = pddcuda.mulmm(A, B, m, n, k)
+    # expand dd pairs: A2 (m x 2k) = [hi | lo], B2 (2k x n) = [hi ; lo] twice
+    Ahi, Alo = A[0::2].reshape(k, m).T, A[1::2].reshape(k, m).T
+    Bhi, Blo = B[0::2].reshape(n, k).T, B[1::2].reshape(n, k).T
+    A4 = np.hstack([Ahi, Ahi, Alo, Alo]).ravel(order="F")
+    B4 = np.vstack([Bhi, Blo, Bhi, Blo]).ravel(order="F")
+    rows = np.repeat(np.arange(m), n)
+    cols = np.tile(np.arange(n), m)
+    dn, up = oracle.exact_dot(m, n, 4 * k, A4, B4, rows, cols)
+    idx = rows + cols * m
+    c = C[0::2][idx] + C[1::2][idx]
+    # the exact value lies in [dn, up] (adjacent doubles); the dd is far more accurate
+    assert np.all(np.abs(C[0::2][idx] - dn) <= np.abs(dn) * 2.0 ** -50)
+    assert np.all(E[idx] <= np.maximum(np.abs(dn), 1.0) * 2.0 ** -80)

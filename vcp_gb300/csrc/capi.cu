@@ -434,4 +434,60 @@ int vcpcu_norm_I_minus_RA(int n, const double* R, const double* A, double* bound
   return form != VCPCU_FORM_PLAIN ? take_status() : VCPCU_OK;
 }
 
+int vcpcu_ddgemm_dev(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                     double* C, int ldc, double* Cerr, int lde, int slices, void* stream) {
+  clear_error();
+  if (slices != 0 && (slices < 7 || slices > 14)) {
+    set_error("ddgemm: slices must be 0 or in [7, 14], got %d", slices);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (m <= 0 || n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (!C || (k > 0 && (!A || !B)) || ldc < m || (k > 0 && (lda < m || ldb < k)) ||
+      (Cerr && lde < m)) {
+    set_error("ddgemm: null pointer or leading dimension too small");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (k > 0 && (misaligned16(A) || misaligned16(B))) {
+    set_error("ddgemm: A and B must be 16-byte aligned (dd entries are read as pairs)");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  int st = check_device();
+  if (st) return st;
+  return ozaki_ddgemm(m, n, k, A, lda, B, ldb, C, ldc, Cerr, lde, slices, (cudaStream_t)stream);
+}
+
+int vcpcu_ddgemm(int m, int n, int k, const double* A, const double* B, double* C, double* Cerr,
+                 int slices) {
+  clear_error();
+  if (slices != 0 && (slices < 7 || slices > 14)) {
+    set_error("ddgemm: slices must be 0 or in [7, 14], got %d", slices);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (m <= 0 || n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (!C || (k > 0 && (!A || !B))) {
+    set_error("ddgemm: null pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  int st = check_device();
+  if (st) return st;
+  cudaStream_t s = host_stream();
+  const size_t na = 2 * (size_t)m * k, nb = 2 * (size_t)k * n, nc = 2 * (size_t)m * n,
+               ne = Cerr ? (size_t)m * n : 0;
+  Scratch buf;
+  if ((st = buf.alloc(sizeof(double) * (na + nb + nc + ne), s))) return st;
+  double* dA = (double*)buf.ptr;
+  double* dB = dA + na;
+  double* dC = dB + nb;
+  double* dE = Cerr ? dC + nc : nullptr;
+  if ((st = h2d(dA, A, na, s)) || (st = h2d(dB, B, nb, s))) return st;
+  if ((st = ozaki_ddgemm(m, n, k, dA, m, dB, k > 0 ? k : 1, dC, m, dE, m, slices, s))) return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(C, dC, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (Cerr)
+    VCPCU_CUDA_TRY(cudaMemcpyAsync(Cerr, dE, ne * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  return take_status();
+}
+
 }  // extern "C"

@@ -135,6 +135,11 @@ int oz_profile_read(double* ms, int nphases, long long* flops) {
   return VCPCU_OK;
 }
 
+void oz_merge_status(const int* flag, cudaStream_t s) {
+  oz_status_merge<<<1, 1, 0, s>>>(flag);
+  count_launch();
+}
+
 int oz_take_status(cudaStream_t s, int* status) {
   int zero = 0;
   VCPCU_CUDA_TRY(cudaMemcpyFromSymbolAsync(status, g_oz_status, sizeof(int), 0,
@@ -154,7 +159,7 @@ int crt_setup(int K, int w, OzPlan* plan) {
   const double need = (2.0 * w - 1.0) + std::log2((double)(K > 1 ? K : 1)) + 0.01;
   double bits = 0.0;
   int L = 0;
-  while (L < OZ_MAX_MODULI && bits <= need) bits += std::log2((double)OZ_MODULI[L++]);
+  while (L < OZ_MAX_MODULI_128 && bits <= need) bits += std::log2((double)OZ_MODULI[L++]);
   if (bits <= need) return -1;
   unsigned __int128 Mv = 1;
   for (int l = 0; l < L; ++l) Mv *= (unsigned __int128)OZ_MODULI[l];

@@ -9,7 +9,7 @@ namespace vcpcu {
 constexpr int OZ_MAX_SLICES = 12;
 constexpr int OZ_MAX_RSLICES = 4;
 constexpr int OZ_MAX_PAIRS = 80;
-constexpr int OZ_MAX_GROUPS = 26;
+constexpr int OZ_MAX_GROUPS = 32;
 
 // Tile geometry of the slice GEMM.
 constexpr int OZ_BM = 128, OZ_BN = 256, OZ_BK = 64, OZ_STAGES = 4;
@@ -72,7 +72,7 @@ struct alignas(64) OzGemmArgs {
   int* flag;
   long long timeout_cycles;
   uint8_t* res;                 // OZ_CRT: residue planes [L][Np][Mp]
-  int moduli[16];               // OZ_CRT: modulus of group g
+  int moduli[32];               // OZ_CRT: modulus of group g
   OzPairList pl;
 };
 
@@ -100,6 +100,16 @@ int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws);
 // Read and clear the sticky status (bit 0 non-finite input, bit 1 timeout);
 // synchronises the stream.
 int oz_take_status(cudaStream_t s, int* status);
+// Merge a product's status words into the sticky device status.
+void oz_merge_status(const int* flag, cudaStream_t s);
+
+// dd GEMM (pddblas semantics) by the CRT form: C, Cerr as documented in
+// include/vcpcuda.h.  static_scratch != nullptr: use that device buffer of
+// static_bytes instead of allocating.
+int ozaki_ddgemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
+                 double* C, long ldc, double* Cerr, long lde, int slices, cudaStream_t s,
+                 void* static_scratch = nullptr, size_t static_bytes = 0);
+int dd_plan_bits(int k, int slices, int* w, int* L);
 
 // Per-phase timing of the Ozaki form (prep, radius 1, radius 2, midpoint).
 int oz_profile_enable(int on);

@@ -113,9 +113,13 @@ OZ_HD __int128 oz_scaled_int(double x, int E, int s, int up) {
 
 // Moduli of the CRT (Ozaki-II) form: pairwise coprime, at most 256, so a
 // residue taken in the symmetric range fits in [-128, 127] (exact in bf16).
-constexpr int OZ_MAX_MODULI = 16;
+constexpr int OZ_MAX_MODULI = 32;
 constexpr int OZ_MODULI[OZ_MAX_MODULI] = {256, 255, 253, 251, 247, 241, 239, 233,
-                                          229, 227, 223, 217, 211, 199, 197, 193};
+                                          229, 227, 223, 217, 211, 199, 197, 193,
+                                          191, 181, 179, 173, 167, 163, 157, 151,
+                                          149, 139, 137, 131, 127, 113, 109, 107};
+// The interval (double) CRT form uses the first 16 (product < 2^128).
+constexpr int OZ_MAX_MODULI_128 = 16;
 
 // Symmetric residue of (neg ? -a : a) modulo m (2 <= m <= 256), in
 // [-floor(m/2), ceil(m/2) - 1].

@@ -310,18 +310,16 @@ oz_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
 // ------------------------------------------------------ CRT form (residues)
 // Barrett reduction constants of the moduli (x < 2^32): q = umulhi(x, magic)
 // is at most two below floor(x / m).
-__constant__ uint32_t c_mod[OZ_MAX_MODULI] = {256, 255, 253, 251, 247, 241, 239, 233,
-                                              229, 227, 223, 217, 211, 199, 197, 193};
+#define OZ_MOD_LIST(F)                                                                   \
+  F(256), F(255), F(253), F(251), F(247), F(241), F(239), F(233), F(229), F(227), F(223),     \
+      F(217), F(211), F(199), F(197), F(193), F(191), F(181), F(179), F(173), F(167), F(163), \
+      F(157), F(151), F(149), F(139), F(137), F(131), F(127), F(113), F(109), F(107)
+#define OZ_ID(m) (m)
 #define OZ_MAGIC(m) (0xFFFFFFFFu / (m))
-__constant__ uint32_t c_magic[OZ_MAX_MODULI] = {
-    OZ_MAGIC(256), OZ_MAGIC(255), OZ_MAGIC(253), OZ_MAGIC(251), OZ_MAGIC(247), OZ_MAGIC(241),
-    OZ_MAGIC(239), OZ_MAGIC(233), OZ_MAGIC(229), OZ_MAGIC(227), OZ_MAGIC(223), OZ_MAGIC(217),
-    OZ_MAGIC(211), OZ_MAGIC(199), OZ_MAGIC(197), OZ_MAGIC(193)};
 #define OZ_P32(m) ((uint32_t)(4294967296ULL % (m)))
-__constant__ uint32_t c_pow32[OZ_MAX_MODULI] = {
-    OZ_P32(256), OZ_P32(255), OZ_P32(253), OZ_P32(251), OZ_P32(247), OZ_P32(241),
-    OZ_P32(239), OZ_P32(233), OZ_P32(229), OZ_P32(227), OZ_P32(223), OZ_P32(217),
-    OZ_P32(211), OZ_P32(199), OZ_P32(197), OZ_P32(193)};
+__constant__ uint32_t c_mod[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_ID)};
+__constant__ uint32_t c_magic[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_MAGIC)};
+__constant__ uint32_t c_pow32[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_P32)};
 
 __device__ __forceinline__ uint32_t umod32(uint32_t x, uint32_t m, uint32_t magic) {
   uint32_t r = x - __umulhi(x, magic) * m;
@@ -564,6 +562,176 @@ int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, 
       return VCPCU_ERR_INVALID_ARG;
   }
   if (st_) return st_;
+  return VCPCU_OK;
+}
+
+
+// ------------------------------------------------------------ dd (pddcuda)
+// Symmetric residue of (neg ? -a : a) mod m_l for a < 2^128 (Horner over
+// 32-bit limbs).
+__device__ __forceinline__ int dev_sym_residue128(unsigned __int128 a, int neg, int l) {
+  const uint32_t m = c_mod[l], mg = c_magic[l], p = c_pow32[l];
+  uint32_t r = 0;
+#pragma unroll
+  for (int t = 3; t >= 0; --t) {
+    const uint32_t limb = (uint32_t)(a >> (32 * t));
+    r = umod32(r * p + umod32(limb, m, mg), m, mg);
+  }
+  if (neg && r) r = m - r;
+  int rs = (int)r;
+  if (2 * rs >= (int)m) rs -= (int)m;
+  return rs;
+}
+
+// w-bit integer of a dd value hi + lo against exponent E: the two words are
+// scaled and rounded to integers separately (|error| <= 1 unit).
+__device__ __forceinline__ __int128 dd_int(double hi, double lo, int E, int w) {
+  if (E == OZ_ZERO_EXP) return 0;
+  __int128 a = 0;
+  if (hi != 0.0) a += oz_scaled_int_bits(hi, E, w, 0);
+  if (lo != 0.0) a += oz_scaled_int_bits(lo, E, w, 0);
+  return a;
+}
+
+// Row maxima of |hi| of a dd matrix (kv pairs {a1, a2}, column-major).
+__global__ void __launch_bounds__(256)
+dd_rowmax(int M, int K, const double* __restrict__ A, long lda, int cols_per_block,
+          unsigned long long* __restrict__ mx, int* __restrict__ flag) {
+  __shared__ unsigned long long red[32];
+  const int lane = threadIdx.x & 31, ph = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
+  if (threadIdx.x < 32) red[lane] = 0;
+  __syncthreads();
+  unsigned long long am = 0;
+  bool bad = false;
+  if (i < M) {
+    const int c0 = blockIdx.y * cols_per_block, c1 = min(K, c0 + cols_per_block);
+    for (int c = c0 + ph; c < c1; c += 8) {
+      const double2 e = *reinterpret_cast<const double2*>(A + 2 * (i + (long)c * lda));
+      if (isfinite(e.x) && isfinite(e.y))
+        am = max(am, dbits(fabs(e.x)));
+      else
+        bad = true;
+    }
+  }
+  if (bad) atomicOr(flag, 1);
+  atomicMax(&red[lane], am);
+  __syncthreads();
+  if (threadIdx.x < 32 && i < M) atomicMax(&mx[i], red[lane]);
+}
+
+// Exponents of the dd form: one bit of headroom over max |hi| so that
+// |hi + lo| <= 2^(E-1).
+__global__ void dd_exponents(int R, const unsigned long long* __restrict__ mx,
+                             int* __restrict__ E) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= R) return;
+  const int e = oz_exponent(__longlong_as_double((long long)mx[i]));
+  E[i] = e == OZ_ZERO_EXP ? e : e + 1;
+}
+
+// Left dd factor -> residue planes [L][Mp][Kp] (transposed through smem).
+__global__ void __launch_bounds__(256)
+dd_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long lda, int L, int w,
+              const int* __restrict__ E, uint16_t* __restrict__ planes) {
+  extern __shared__ int16_t sd[];  // [L][LT_R][LT_KS]
+  const int tid = threadIdx.x;
+  const int r = tid % LT_R, kph = tid / LT_R;
+  const int i = blockIdx.y * LT_R + r;
+  const int k0 = blockIdx.x * LT_K;
+  const int Ei = i < M ? E[i] : OZ_ZERO_EXP;
+  for (int kk = kph; kk < LT_K; kk += 8) {
+    const int k = k0 + kk;
+    double hi = 0.0, lo = 0.0;
+    if (i < M && k < K) {
+      const double2 e = *reinterpret_cast<const double2*>(A + 2 * (i + (long)k * lda));
+      if (isfinite(e.x) && isfinite(e.y)) {
+        hi = e.x;
+        lo = e.y;
+      }
+    }
+    const __int128 a = dd_int(hi, lo, Ei, w);
+    const unsigned __int128 ua = (unsigned __int128)(a < 0 ? -a : a);
+    for (int l = 0; l < L; ++l)
+      sd[(l * LT_R + r) * LT_KS + kk] = (int16_t)dev_sym_residue128(ua, a < 0, l);
+  }
+  __syncthreads();
+  const int wr = tid / 8, wk = (tid % 8) * 8;
+  const int gi = blockIdx.y * LT_R + wr;
+  for (int q = 0; q < L; ++q) {
+    const int16_t* src = sd + (q * LT_R + wr) * LT_KS + wk;
+    uint4 v;
+    v.x = bf16_bits(src[0]) | (bf16_bits(src[1]) << 16);
+    v.y = bf16_bits(src[2]) | (bf16_bits(src[3]) << 16);
+    v.z = bf16_bits(src[4]) | (bf16_bits(src[5]) << 16);
+    v.w = bf16_bits(src[6]) | (bf16_bits(src[7]) << 16);
+    if (gi < Mp) *reinterpret_cast<uint4*>(planes + ((size_t)q * Mp + gi) * Kp + k0 + wk) = v;
+  }
+}
+
+// Right dd factor: one block per column; exponent, then residue planes
+// [L][Np][Kp].
+__global__ void __launch_bounds__(256)
+dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb, int L, int w,
+               int* __restrict__ F, uint16_t* __restrict__ planes, int* __restrict__ flag) {
+  const int j = blockIdx.x, tid = threadIdx.x;
+  __shared__ unsigned long long smax;
+  if (tid == 0) smax = 0;
+  __syncthreads();
+  unsigned long long am = 0;
+  bool bad = false;
+  if (j < N) {
+    for (int k = tid; k < K; k += 256) {
+      const double2 e = *reinterpret_cast<const double2*>(B + 2 * (k + (long)j * ldb));
+      if (isfinite(e.x) && isfinite(e.y))
+        am = max(am, dbits(fabs(e.x)));
+      else
+        bad = true;
+    }
+  }
+  if (bad) atomicOr(flag, 1);
+  atomicMax(&smax, am);
+  __syncthreads();
+  int Fj = oz_exponent(__longlong_as_double((long long)smax));
+  if (Fj != OZ_ZERO_EXP) Fj += 1;
+  if (tid == 0 && j < N) F[j] = Fj;
+  for (int k = tid; k < Kp; k += 256) {
+    double hi = 0.0, lo = 0.0;
+    if (j < N && k < K) {
+      const double2 e = *reinterpret_cast<const double2*>(B + 2 * (k + (long)j * ldb));
+      if (isfinite(e.x) && isfinite(e.y)) {
+        hi = e.x;
+        lo = e.y;
+      }
+    }
+    const __int128 b = dd_int(hi, lo, Fj, w);
+    const unsigned __int128 ub = (unsigned __int128)(b < 0 ? -b : b);
+    for (int l = 0; l < L; ++l)
+      planes[((size_t)l * Np + j) * Kp + k] = (uint16_t)bf16_bits(dev_sym_residue128(ub, b < 0, l));
+  }
+}
+
+int dd_prepare(int M, int N, int K, int Mp, int Np, int Kp, int L, int w, const double* A,
+               long lda, const double* B, long ldb, unsigned long long* rowmax, int* E, int* F,
+               uint16_t* planesA, uint16_t* planesB, int* flag, cudaStream_t st) {
+  VCPCU_CUDA_TRY(cudaMemsetAsync(rowmax, 0, sizeof(unsigned long long) * (size_t)Mp, st));
+  VCPCU_CUDA_TRY(cudaMemsetAsync(flag, 0, 4 * sizeof(int), st));
+  if (M > 0 && K > 0) {
+    const int cpb = 256;
+    dim3 g1((M + 31) / 32, (K + cpb - 1) / cpb);
+    dd_rowmax<<<g1, 256, 0, st>>>(M, K, A, lda, cpb, rowmax, flag);
+    VCPCU_LAUNCH_CHECK("dd_rowmax");
+  }
+  dd_exponents<<<(Mp + 255) / 256, 256, 0, st>>>(Mp, rowmax, E);
+  VCPCU_LAUNCH_CHECK("dd_exponents");
+  dim3 g2(Kp / LT_K, Mp / LT_R);
+  const size_t shm = sizeof(int16_t) * (size_t)L * LT_R * LT_KS;
+  VCPCU_CUDA_TRY(
+      cudaFuncSetAttribute(dd_split_left, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+  dd_split_left<<<g2, 256, shm, st>>>(M, K, Mp, Kp, A, lda, L, w, E, planesA);
+  VCPCU_LAUNCH_CHECK("dd_split_left");
+  dd_split_right<<<Np, 256, 0, st>>>(K, N, Kp, Np, B, ldb, L, w, F, planesB, flag);
+  VCPCU_LAUNCH_CHECK("dd_split_right");
   return VCPCU_OK;
 }
 
