@@ -184,6 +184,44 @@ int vcpcu_norm_I_minus_RA_dev(int n, const double* R, int ldr, const double* A,
 int vcpcu_norm_I_minus_RA(int n, const double* R, const double* A, double* bound,
                           int form, int slices);
 
+/* ---- batches of uneven interval GEMMs -------------------------------------- */
+
+/* One problem of a batch: C (m x n) = [A] (m x k) * [B] (k x n), kv-layout
+ * interval matrices, device pointers, column-major with leading dimensions. */
+typedef struct {
+  int m, n, k;
+  int lda, ldb, ldc;
+  const double* A;
+  const double* B;
+  double* C;
+} vcpcu_problem;
+
+/* Runs `count` independent interval products (the many small, uneven
+ * products that Newton / verification steps and the Legendre basis
+ * generator of the reference emit; no single reference entry point: each
+ * would be a pidblas::mulmm call).  Form PLAIN: one persistent grouped
+ * launch over all problems' 64 x 64 tiles (work counter, no waits),
+ * bit-identical per problem to vcpcu_igemm_dev PLAIN.  Ozaki forms: the
+ * problems in sequence on the stream.  The table is read from host memory
+ * during the call; stream-ordered. */
+int vcpcu_igemm_batched_dev(int count, const vcpcu_problem* problems, int form,
+                            int slices, void* stream);
+
+/* The same batch captured once into an instantiated CUDA graph (the problem
+ * table is copied; its device pointers must stay valid), replayed with one
+ * launch per call, with device clock stamps per problem: after a replay,
+ * vcpcu_batch_graph_latencies synchronises `stream` and writes, per
+ * problem, its start relative to the batch's first start and its latency
+ * (first tile start to last tile end for PLAIN, call start to end for the
+ * Ozaki forms), in microseconds (either pointer may be NULL). */
+typedef struct vcpcu_batch_graph_s* vcpcu_batch_graph;
+int vcpcu_batch_graph_create(int count, const vcpcu_problem* problems, int form,
+                             int slices, void* stream, vcpcu_batch_graph* out);
+int vcpcu_batch_graph_launch(vcpcu_batch_graph g, void* stream);
+int vcpcu_batch_graph_latencies(vcpcu_batch_graph g, void* stream,
+                                double* start_us, double* latency_us);
+int vcpcu_batch_graph_destroy(vcpcu_batch_graph g);
+
 /* ---- double-double GEMM (pddblas::mulmm, vcp/pddblas.hpp:318-376) --------- */
 
 /* C = A * B for kv::dd matrices (pairs {a1, a2} of doubles, column-major;
