@@ -184,6 +184,21 @@ int vcpcu_norm_I_minus_RA_dev(int n, const double* R, int ldr, const double* A,
 int vcpcu_norm_I_minus_RA(int n, const double* R, const double* A, double* bound,
                           int form, int slices);
 
+/* ---- autotuner ------------------------------------------------------------- */
+
+/* VCPCU_FORM_AUTO runs, per product, the form with the smaller predicted
+ * time: plain 8mnk/fp64_rate + t_launch against Ozaki (L + 8) 2 Mp Np Kp /
+ * tc_rate + 16 (mk + kn) / prep_bw + 12 t_launch (L moduli, tile-padded
+ * sizes).  vcpcu_autotune measures the constants on the current device
+ * (one plain and two Ozaki products on synthetic data), keeps them for the
+ * process, stores them in the file named by the environment variable
+ * VCPCU_AUTOTUNE_CACHE (read back at the first AUTO decision of a later
+ * process), and writes {fp64_rate, tc_rate, prep_bw, t_launch} to
+ * constants[4] if non-NULL.  No counterpart in the reference.
+ * vcpcu_autotune_choice returns the form AUTO would use for m x n x k. */
+int vcpcu_autotune(void* stream, double* constants);
+int vcpcu_autotune_choice(int m, int n, int k);
+
 /* ---- batches of uneven interval GEMMs -------------------------------------- */
 
 /* One problem of a batch: C (m x n) = [A] (m x k) * [B] (k x n), kv-layout

@@ -41,3 +41,16 @@ def test_error_mapping():
         errors.raise_for_status(3, "x")
     assert issubclass(errors.CudaError, errors.StateError)
     errors.raise_for_status(0, "fine")
+
+
+def test_autotune_choice_host_model(cuda_lib):
+    """The AUTO choice is a host-side cost model: tiny products stay on the
+    FP64 plain kernel, large ones go to the tensor-core form.  No GPU call."""
+    choose = cuda_lib.vcpcu_autotune_choice
+    assert choose(8, 8, 8) == 0
+    assert choose(32, 1, 32) == 0
+    assert choose(4096, 4096, 4096) == 1
+    assert choose(8192, 8192, 8192) == 1
+    # monotone along the diagonal: once Ozaki wins it keeps winning
+    picks = [choose(n, n, n) for n in (16, 64, 128, 256, 512, 1024, 2048)]
+    assert picks == sorted(picks)

@@ -250,6 +250,7 @@ struct BatchGraph {
   int count = 0, form = 0, slices = 0;
   std::vector<BatchProblem> probs;
   std::vector<int> tiles;
+  std::vector<char> ozaki;  // AUTO: problem runs in the tensor-core form
   void* state = nullptr;  // device: BatchDev arrays
   BatchDev d{};
   cudaGraph_t graph = nullptr;
@@ -276,7 +277,39 @@ int batch_launch_ozaki(const BatchGraph& g, cudaStream_t s) {
 
 int batch_record(BatchGraph& g, cudaStream_t s) {
   if (g.form == VCPCU_FORM_PLAIN) return batch_launch_plain(g.d, s);
-  return batch_launch_ozaki(g, s);
+  if (g.form != VCPCU_FORM_AUTO) return batch_launch_ozaki(g, s);
+  // AUTO: the problems the cost model gives to the plain form run in the
+  // grouped launch (the others have zero tiles there), the rest in sequence
+  int st = batch_launch_plain(g.d, s);
+  if (st) return st;
+  for (int i = 0; i < g.count; ++i) {
+    const BatchProblem& q = g.probs[i];
+    if (q.m <= 0 || q.n <= 0 || !g.ozaki[i]) continue;
+    stamp<<<1, 1, 0, s>>>(g.d.t_first + i);
+    VCPCU_LAUNCH_CHECK("stamp");
+    if ((st = igemm_any(q.m, q.n, q.k > 0 ? q.k : 0, q.A, q.lda, q.B, q.ldb, q.C, q.ldc,
+                        VCPCU_FORM_OZAKI, g.slices, s)))
+      return st;
+    stamp<<<1, 1, 0, s>>>(g.d.t_last + i);
+    VCPCU_LAUNCH_CHECK("stamp");
+  }
+  return VCPCU_OK;
+}
+
+// AUTO: mark the problems the autotuner sends to the tensor-core form and
+// hide them from the grouped plain launch (zero tiles).
+void batch_split_auto(BatchGraph& g, std::vector<BatchProblem>& plain_view) {
+  g.ozaki.assign(g.count, 0);
+  plain_view = g.probs;
+  if (g.form != VCPCU_FORM_AUTO) return;
+  for (int i = 0; i < g.count; ++i) {
+    const BatchProblem& q = g.probs[i];
+    if (q.m > 0 && q.n > 0 && autotune_choose(q.m, q.n, q.k > 0 ? q.k : 0) != VCPCU_FORM_PLAIN &&
+        ((((uintptr_t)q.A) | ((uintptr_t)q.B)) & 15) == 0) {
+      g.ozaki[i] = 1;
+      plain_view[i].m = 0;
+    }
+  }
 }
 
 }  // namespace
@@ -291,7 +324,7 @@ int vcpcu_igemm_batched_dev(int count, const vcpcu_problem* problems, int form, 
   clear_error();
   if (count <= 0) return VCPCU_OK;
   if (!problems || (form != VCPCU_FORM_PLAIN && form != VCPCU_FORM_OZAKI &&
-                    form != VCPCU_FORM_OZAKI_SLICES)) {
+                    form != VCPCU_FORM_OZAKI_SLICES && form != VCPCU_FORM_AUTO)) {
     set_error("igemm_batched: null problem table or unsupported form %d", form);
     return VCPCU_ERR_INVALID_ARG;
   }
@@ -308,9 +341,11 @@ int vcpcu_igemm_batched_dev(int count, const vcpcu_problem* problems, int form, 
       set_error("igemm_batched: leading dimension too small in a problem");
       return VCPCU_ERR_INVALID_ARG;
     }
+  std::vector<BatchProblem> plain_view;
+  batch_split_auto(g, plain_view);
   Scratch mem;
   if ((st = mem.alloc(batch_state_bytes(count), s))) return st;
-  if ((st = batch_upload(count, g.probs.data(), mem.ptr, &g.d, s, &g.tiles))) return st;
+  if ((st = batch_upload(count, plain_view.data(), mem.ptr, &g.d, s, &g.tiles))) return st;
   return batch_record(g, s);
 }
 
@@ -318,7 +353,8 @@ int vcpcu_batch_graph_create(int count, const vcpcu_problem* problems, int form,
                              void* stream, vcpcu_batch_graph* out) {
   clear_error();
   if (!out || count <= 0 || !problems ||
-      (form != VCPCU_FORM_PLAIN && form != VCPCU_FORM_OZAKI && form != VCPCU_FORM_OZAKI_SLICES)) {
+      (form != VCPCU_FORM_PLAIN && form != VCPCU_FORM_OZAKI && form != VCPCU_FORM_OZAKI_SLICES &&
+       form != VCPCU_FORM_AUTO)) {
     set_error("batch_graph_create: bad arguments");
     return VCPCU_ERR_INVALID_ARG;
   }
@@ -330,12 +366,14 @@ int vcpcu_batch_graph_create(int count, const vcpcu_problem* problems, int form,
   g->form = form;
   g->slices = slices;
   g->probs.assign((const BatchProblem*)problems, (const BatchProblem*)problems + count);
+  std::vector<BatchProblem> plain_view;
+  batch_split_auto(*g, plain_view);
   cudaError_t e = cudaMalloc(&g->state, batch_state_bytes(count));
   if (e != cudaSuccess) {
     delete g;
     return cuda_fail(e, "cudaMalloc(batch state)");
   }
-  if ((st = batch_upload(count, g->probs.data(), g->state, &g->d, s, &g->tiles))) {
+  if ((st = batch_upload(count, plain_view.data(), g->state, &g->d, s, &g->tiles))) {
     cudaFree(g->state);
     delete g;
     return st;

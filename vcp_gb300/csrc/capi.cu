@@ -123,6 +123,11 @@ int igemm_check(int m, int n, int k, const double* A, int lda, const double* B, 
 int vcpcu::igemm_any(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
                      double* C, long ldc, int form, int slices, cudaStream_t s) {
   if (k < 0) k = 0;
+  if (form == VCPCU_FORM_AUTO) {
+    form = autotune_choose(m, n, k);
+    if (form != VCPCU_FORM_PLAIN && k > 0 && ((((uintptr_t)A) | ((uintptr_t)B)) & 15) != 0)
+      form = VCPCU_FORM_PLAIN;  // the tensor-core form reads 16-byte pairs
+  }
   if (form == VCPCU_FORM_PLAIN) {
     Scratch ws;
     int st = ws.alloc(interval_gemm_plain_ws_bytes(m, n, k), s);

@@ -4,6 +4,10 @@
 
 namespace vcpcu {
 
+// VCPCU_FORM_PLAIN or VCPCU_FORM_OZAKI, whichever the cost model of the
+// autotuner predicts faster (autotune.cu).
+int autotune_choose(int m, int n, int k);
+
 // Interval product of either form on device pointers (defined in capi.cu).
 int igemm_any(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
               double* C, long ldc, int form, int slices, cudaStream_t s);

@@ -108,3 +108,19 @@ def norm_I_minus_RA(R: np.ndarray, A: np.ndarray, n: int, form: int = FORM_PLAIN
     _lib.call("vcpcu_norm_I_minus_RA", n, _host_ptr(R, n * n, "R"), _host_ptr(A, 2 * n * n, "A"),
               ctypes.addressof(out), int(form), int(slices))
     return out.value
+
+
+# ---- AUTO form -------------------------------------------------------------------
+
+def autotune(stream=None) -> dict:
+    """Measure the cost-model constants of FORM_AUTO on the current GPU (one
+    plain and two Ozaki products) and keep them for the process; stored in
+    the file named by VCPCU_AUTOTUNE_CACHE when that variable is set."""
+    c = np.zeros(4, dtype=np.float64)
+    _lib.call("vcpcu_autotune", _stream_ptr(stream), c.ctypes.data)
+    return dict(fp64_rate=c[0], tc_rate=c[1], prep_bw=c[2], t_launch=c[3])
+
+
+def autotune_choice(m: int, n: int, k: int) -> int:
+    """The form (FORM_PLAIN or FORM_OZAKI) that FORM_AUTO uses for m x n x k."""
+    return int(_lib.load().vcpcu_autotune_choice(int(m), int(n), int(k)))
