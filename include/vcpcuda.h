@@ -107,6 +107,22 @@ int vcpcu_udmatmul_dev(int m, int n, int k, const double* A, int lda,
                        const double* B, int ldb, double* CU, double* CD,
                        int ldc, void* stream);
 
+/* Tensor-core enclosure of a point product in the shape of vblas udmatmul
+ * (vblas/udmatmul.hpp:758): CD <= A*B <= CU entrywise, rigorous, but not
+ * the FMA-chain bits of vcpcu_udmatmul.  A is m x n, B is n x k, C is
+ * m x k (vblas naming).  The product is the Ozaki form of vcpcu_igemm_dev
+ * on zero-radius operands with the radius products skipped: residues of
+ * w = 7 * slices bit scaled integers (0 = default 8), Chinese remaindering,
+ * truncation bound.  m <= 0 or k <= 0: no-op; n <= 0: CU = CD = 0.
+ * Requires finite inputs (VCPCU_ERR_NONFINITE).  The _dev form is
+ * stream-ordered (status through vcpcu_status); the host form is
+ * synchronous. */
+int vcpcu_udmatmul_ozaki_dev(int m, int n, int k, const double* A, int lda,
+                             const double* B, int ldb, double* CU, double* CD,
+                             int ldc, int slices, void* stream);
+int vcpcu_udmatmul_ozaki(int m, int n, int k, const double* A, const double* B,
+                         double* CU, double* CD, int slices);
+
 /* ---- interval GEMM (pidblas::mulmm, vcp/pidblas.hpp:239-294) -------------- */
 
 /* C = [A] * [B] for interval matrices in kv layout ({inf,sup} pairs).

@@ -44,6 +44,10 @@ def test_mul_point_plain_bitexact_and_ozaki_encloses(cuda_lib, oracle, side, sha
     for form in (pidcuda.FORM_OZAKI, pidcuda.FORM_OZAKI_SLICES):
         Co = pidcuda.mul_point(side, L, R, m, n, k, form=form)
         assert np.all(Co[idx] <= lo) and np.all(Co[idx + 1] >= up)
+        # the GPU skips the radius product with the zero factor; the host
+        # model runs both on the degenerate operands: same bits
+        Cm, _ = oracle.ozaki_igemm(m, n, k, Li, Ri, crt=form == pidcuda.FORM_OZAKI)
+        assert np.array_equal(bits(Co), bits(Cm)), form
 
 
 def test_other_products_golden(cuda_lib):

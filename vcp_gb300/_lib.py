@@ -42,6 +42,8 @@ SIGNATURES: dict[str, tuple] = {
     "vcpcu_norm_I_minus_RA": (_i, [_i, _v, _v, _v, _i, _i]),
     "vcpcu_ddgemm_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _v, _i, _i, _v]),
     "vcpcu_ddgemm": (_i, [_i, _i, _i, _v, _v, _v, _v, _i]),
+    "vcpcu_udmatmul_ozaki_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _v, _i, _i, _v]),
+    "vcpcu_udmatmul_ozaki": (_i, [_i, _i, _i, _v, _v, _v, _v, _i]),
     "vcpcu_autotune": (_i, [_v, _v]),
     "vcpcu_autotune_choice": (_i, [_i, _i, _i]),
     "vcpcu_igemm_batched_dev": (_i, [_i, _v, _i, _i, _v]),

@@ -121,7 +121,7 @@ int igemm_check(int m, int n, int k, const double* A, int lda, const double* B, 
 }  // namespace
 
 int vcpcu::igemm_any(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
-                     double* C, long ldc, int form, int slices, cudaStream_t s) {
+                     double* C, long ldc, int form, int slices, cudaStream_t s, int point_mask) {
   if (k < 0) k = 0;
   if (form == VCPCU_FORM_AUTO) {
     form = autotune_choose(m, n, k);
@@ -134,7 +134,7 @@ int vcpcu::igemm_any(int m, int n, int k, const double* A, long lda, const doubl
     if (st) return st;
     return launch_interval_gemm_plain(m, n, k, A, lda, B, ldb, C, ldc, (double*)ws.ptr, s);
   }
-  return ozaki_igemm(m, n, k, A, lda, B, ldb, C, ldc, form, slices, s);
+  return ozaki_igemm(m, n, k, A, lda, B, ldb, C, ldc, form, slices, s, point_mask);
 }
 
 namespace {
@@ -225,6 +225,62 @@ int vcpcu_rmatmul_dev(int m, int n, int k, const double* A, int lda, const doubl
 int vcpcu_udmatmul_dev(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
                        double* CU, double* CD, int ldc, void* stream) {
   return rmatmul_dev_impl(m, n, k, A, lda, B, ldb, CU, CD, ldc, PK_UPDOWN, (cudaStream_t)stream);
+}
+
+namespace {
+int udoz_check(int m, int n, int k, const void* A, const void* B, const void* CU, const void* CD,
+               int slices) {
+  if (slices != 0 && (slices < 2 || slices > OZ_MAX_SLICES)) {
+    set_error("udmatmul_ozaki: slices must be 0 or in [2, %d], got %d", OZ_MAX_SLICES, slices);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (m <= 0 || k <= 0) return VCPCU_OK;
+  if (!CU || !CD || (n > 0 && (!A || !B))) {
+    set_error("udmatmul_ozaki: null pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  return VCPCU_OK;
+}
+}  // namespace
+
+int vcpcu_udmatmul_ozaki_dev(int m, int n, int k, const double* A, int lda, const double* B,
+                             int ldb, double* CU, double* CD, int ldc, int slices, void* stream) {
+  clear_error();
+  int st = udoz_check(m, n, k, A, B, CU, CD, slices);
+  if (st || m <= 0 || k <= 0) return st;
+  if (n < 0) n = 0;
+  if (ldc < m || (n > 0 && (lda < m || ldb < n))) {
+    set_error("udmatmul_ozaki: leading dimension too small (lda %d, ldb %d, ldc %d)", lda, ldb,
+              ldc);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  return udmatmul_ozaki_dispatch(m, n, k, A, lda, B, ldb, CU, CD, ldc, slices,
+                                 (cudaStream_t)stream);
+}
+
+int vcpcu_udmatmul_ozaki(int m, int n, int k, const double* A, const double* B, double* CU,
+                         double* CD, int slices) {
+  clear_error();
+  int st = udoz_check(m, n, k, A, B, CU, CD, slices);
+  if (st || m <= 0 || k <= 0) return st;
+  if (n < 0) n = 0;
+  if ((st = check_device())) return st;
+  cudaStream_t s = host_stream();
+  const size_t na = (size_t)m * n, nb = (size_t)n * k, nc = (size_t)m * k;
+  Scratch buf;
+  if ((st = buf.alloc(sizeof(double) * (na + nb + 2 * nc), s))) return st;
+  double* dA = (double*)buf.ptr;
+  double* dB = dA + na;
+  double* dU = dB + nb;
+  double* dD = dU + nc;
+  if ((st = h2d(dA, A, na, s)) || (st = h2d(dB, B, nb, s))) return st;
+  st = udmatmul_ozaki_dispatch(m, n, k, dA, m, dB, n > 0 ? n : 1, dU, dD, m, slices, s);
+  if (st) return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(CU, dU, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(CD, dD, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  return take_status();
 }
 
 int vcpcu_igemm_dev(int m, int n, int k, const double* A, int lda, const double* B, int ldb,

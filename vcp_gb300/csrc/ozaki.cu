@@ -290,14 +290,20 @@ int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long ld
     PhaseTimer t(0, s);
     if ((st = oz_prepare(plan.pb, A, lda, B, ldb, ws, s))) return st;
   }
-  {
+  // T = (|mA| + rA) * rB + rA * |mB|; a product with a zero factor gives
+  // exactly 0 (its exponent is the zero sentinel), so skipping it leaves
+  // every bit of T unchanged
+  const bool rad1 = !(plan.point_mask & 2), rad2 = !(plan.point_mask & 1);
+  if (rad1) {
     PhaseTimer t(1, s);
     if ((st = oz_run_gemm(plan, OZ_RAD_SET, ws, nullptr, 0, s))) return st;
   }
-  {
+  if (rad2) {
     PhaseTimer t(2, s);
-    if ((st = oz_run_gemm(plan, OZ_RAD_ADD, ws, nullptr, 0, s))) return st;
+    if ((st = oz_run_gemm(plan, rad1 ? OZ_RAD_ADD : OZ_RAD_SET, ws, nullptr, 0, s))) return st;
   }
+  if (!rad1 && !rad2)
+    VCPCU_CUDA_TRY(cudaMemsetAsync(ws.T, 0, sizeof(double) * (size_t)plan.pb.Mp * plan.pb.Np, s));
   {
     PhaseTimer t(3, s);
     if (plan.pb.crt) {
@@ -311,7 +317,7 @@ int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long ld
 }
 
 int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
-                double* C, long ldc, int form, int slices, cudaStream_t s) {
+                double* C, long ldc, int form, int slices, cudaStream_t s, int point_mask) {
   const int nslices = slices > 0 ? slices : 8;
   const int sr = 2;
   if (k > (1 << 20)) {
@@ -320,6 +326,7 @@ int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B,
   }
   OzPlan plan;
   oz_make_plan(m, n, k, nslices, sr, &plan, form == VCPCU_FORM_OZAKI_SLICES ? 0 : 1);
+  plan.point_mask = point_mask & 3;
   Scratch buf;
   int st = buf.alloc(oz_workspace_bytes(plan.pb), s);
   if (st) return st;
@@ -329,7 +336,8 @@ int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B,
   if (g_prof.on) {
     std::lock_guard<std::mutex> lk(g_prof_mu);
     g_prof.flops += 2LL * m * n * (long long)(k > 0 ? k : 0) *
-                    ((plan.pb.crt ? plan.pb.L : plan.mid.npairs) + 2LL * plan.rad.npairs);
+                    ((plan.pb.crt ? plan.pb.L : plan.mid.npairs) +
+                     (long long)(!(point_mask & 2) + !(point_mask & 1)) * plan.rad.npairs);
   }
   oz_status_merge<<<1, 1, 0, s>>>(ws.flag);
   VCPCU_LAUNCH_CHECK("oz_status_merge");

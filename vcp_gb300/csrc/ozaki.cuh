@@ -84,6 +84,9 @@ struct OzPlan {
   int t_ref_mid, R_mid, t_ref_rad, R_rad;
   uint32_t Q[16][4];   // CRT basis: Q_l = (M/m_l) * ((M/m_l)^-1 mod m_l), 32-bit limbs
   uint32_t Mlimb[4];   // M = prod m_l
+  // bit 0: A is a point matrix (rA = 0), bit 1: B is (rB = 0).  The radius
+  // product with a zero factor is skipped; it would add exactly 0 to T.
+  int point_mask = 0;
 };
 
 // crt != 0 selects the CRT form of the midpoint with w = 7 * s integer bits.
@@ -120,7 +123,8 @@ int oz_profile_read(double* ms, int nphases, long long* flops);
 int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long lda,
                    const double* B, long ldb, double* C, long ldc, cudaStream_t s);
 
+// point_mask as OzPlan::point_mask (the caller guarantees the zero radii).
 int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
-                double* C, long ldc, int form, int slices, cudaStream_t s);
+                double* C, long ldc, int form, int slices, cudaStream_t s, int point_mask = 0);
 
 }  // namespace vcpcu

@@ -148,8 +148,51 @@ int igemm_point_dispatch(int interval_side, int m, int n, int k, const double* L
     VCPCU_LAUNCH_CHECK("expand_point");
   }
   if (interval_side == 0)
-    return igemm_any(m, n, k, L, ldl, P, prow > 0 ? prow : 1, C, ldc, form, slices, s);
-  return igemm_any(m, n, k, P, prow > 0 ? prow : 1, R, ldr, C, ldc, form, slices, s);
+    return igemm_any(m, n, k, L, ldl, P, prow > 0 ? prow : 1, C, ldc, form, slices, s, 2);
+  return igemm_any(m, n, k, P, prow > 0 ? prow : 1, R, ldr, C, ldc, form, slices, s, 1);
+}
+
+namespace {
+// kv interval result (ld = rows) -> upper ends CU and lower ends CD (ldc)
+__global__ void split_kv(int rows, int cols, const double* __restrict__ C, double* __restrict__ CU,
+                         double* __restrict__ CD, long ldc) {
+  long total = (long)rows * cols;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    long i = idx % rows, j = idx / rows;
+    const double2 c = reinterpret_cast<const double2*>(C)[idx];
+    CD[i + j * ldc] = c.x;
+    CU[i + j * ldc] = c.y;
+  }
+}
+}  // namespace
+
+int udmatmul_ozaki_dispatch(int m, int n, int k, const double* A, long lda, const double* B,
+                            long ldb, double* CU, double* CD, long ldc, int slices,
+                            cudaStream_t s) {
+  // vblas naming: A m x n, B n x k, C m x k; as a BLAS product M = m, N = k, K = n
+  if (n <= 0) {  // empty inner dimension: the exact product is 0
+    VCPCU_CUDA_TRY(cudaMemset2DAsync(CU, sizeof(double) * ldc, 0, sizeof(double) * m, k, s));
+    VCPCU_CUDA_TRY(cudaMemset2DAsync(CD, sizeof(double) * ldc, 0, sizeof(double) * m, k, s));
+    return VCPCU_OK;
+  }
+  const size_t na = 2 * (size_t)m * (n > 0 ? n : 1), nb = 2 * (size_t)(n > 0 ? n : 1) * k,
+               nc = 2 * (size_t)m * k;
+  Scratch buf;
+  int st = buf.alloc(sizeof(double) * (na + nb + nc), s);
+  if (st) return st;
+  double* PA = (double*)buf.ptr;
+  double* PB = PA + na;
+  double* PC = PB + nb;
+  expand_point<<<grid1((long)m * n), 256, 0, s>>>(m, n, A, lda, PA);
+  VCPCU_LAUNCH_CHECK("expand_point");
+  expand_point<<<grid1((long)n * k), 256, 0, s>>>(n, k, B, ldb, PB);
+  VCPCU_LAUNCH_CHECK("expand_point");
+  if ((st = igemm_any(m, k, n, PA, m, PB, n, PC, m, VCPCU_FORM_OZAKI, slices, s, 3)))
+    return st;
+  split_kv<<<grid1((long)m * k), 256, 0, s>>>(m, k, PC, CU, CD, ldc);
+  VCPCU_LAUNCH_CHECK("split_kv");
+  return VCPCU_OK;
 }
 
 int isyrk_dispatch(int n, int k, const double* A, long lda, double* C, long ldc, int form,

@@ -9,14 +9,20 @@ namespace vcpcu {
 int autotune_choose(int m, int n, int k);
 
 // Interval product of either form on device pointers (defined in capi.cu).
+// point_mask bit 0 / bit 1: A / B has zero radii (the tensor-core form then
+// skips the radius product that vanishes; the result is the same).
 int igemm_any(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
-              double* C, long ldc, int form, int slices, cudaStream_t s);
+              double* C, long ldc, int form, int slices, cudaStream_t s, int point_mask = 0);
 
 // interval_side 0: C = [L] * R (R point, pidblas::mul_im_m);
 // interval_side 1: C = L * [R] (L point, pidblas::mul_m_im).
 int igemm_point_dispatch(int interval_side, int m, int n, int k, const double* L, long ldl,
                          const double* R, long ldr, double* C, long ldc, int form, int slices,
                          cudaStream_t s);
+// CD <= A B <= CU by the tensor-core form (vblas naming: A m x n, B n x k).
+int udmatmul_ozaki_dispatch(int m, int n, int k, const double* A, long lda, const double* B,
+                            long ldb, double* CU, double* CD, long ldc, int slices,
+                            cudaStream_t s);
 int isyrk_dispatch(int n, int k, const double* A, long lda, double* C, long ldc, int form,
                    int slices, cudaStream_t s);
 int vsyrk_dispatch(int n, int k, const double* A, long lda, double* C, long ldc, cudaStream_t s);

@@ -75,3 +75,20 @@ def rmatmul_dev(m, n, k, A, lda, B, ldb, C, ldc, rounding_mode, stream=None) -> 
 def udmatmul_dev(m, n, k, A, lda, B, ldb, CU, CD, ldc, stream=None) -> None:
     _lib.call("vcpcu_udmatmul_dev", m, n, k, _dev_ptr(A, "A"), lda, _dev_ptr(B, "B"), ldb,
               _dev_ptr(CU, "CU"), _dev_ptr(CD, "CD"), ldc, _stream_ptr(stream))
+
+
+def udmatmul_ozaki(m: int, n: int, k: int, A: np.ndarray, B: np.ndarray, CU: np.ndarray,
+                   CD: np.ndarray, slices: int = 0) -> None:
+    """CD <= A B <= CU on the tensor cores (Ozaki form; not the FMA-chain bits)."""
+    if m <= 0 or k <= 0:
+        return
+    pa = _host_ptr(A, m * n, "A") if n > 0 else None
+    pb = _host_ptr(B, n * k, "B") if n > 0 else None
+    pu = _host_ptr(CU, m * k, "CU", writable=True)
+    pd = _host_ptr(CD, m * k, "CD", writable=True)
+    _lib.call("vcpcu_udmatmul_ozaki", m, n, k, pa, pb, pu, pd, int(slices))
+
+
+def udmatmul_ozaki_dev(m, n, k, A, lda, B, ldb, CU, CD, ldc, slices=0, stream=None) -> None:
+    _lib.call("vcpcu_udmatmul_ozaki_dev", m, n, k, _dev_ptr(A, "A"), lda, _dev_ptr(B, "B"), ldb,
+              _dev_ptr(CU, "CU"), _dev_ptr(CD, "CD"), ldc, int(slices), _stream_ptr(stream))
