@@ -16,6 +16,18 @@ Our arm (default) prints one JSON line with
   roofline       the dominant kernel against the measured peak;
   cpu_baseline   the CPU restatement of pidblas::mulmm (oracle port of the
                  reference path) on the host cores, bounded row sample.
+  also           short runs of the other benchmark workloads in the same
+                 process (``--workload`` runs one of them at full size):
+                 batch  4096 uneven interval GEMMs, m, n, k log-uniform in
+                        [32, 1024], mid U[-1, 1], rad 1e-12 |mid|: throughput
+                        and p50 / p99 per-problem latency from device stamps,
+                        plain vs Ozaki vs AUTO, each a captured CUDA graph;
+                 dd     dd GEMM (pddblas semantics), hi E(phi), lo = hi 2^-53 u:
+                        TFLOP/s, relative error against the exact product and
+                        the tightness of the returned bound;
+                 point  up/down point GEMM (udmatmul shape), entries E(phi):
+                        plain RU/RD FMA chains vs the Ozaki enclosure at
+                        slice counts s, width ratio and containment.
 --impl reference times that CPU path alone as the reference arm.
 
 Inputs are 1 GiB per operand (larger than the 129 MB L2), so no L2 flush is
@@ -54,6 +66,14 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-rows", type=int, default=0, help="row sample of the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="interval",
+                    choices=["interval", "batch", "dd", "point"],
+                    help="interval: the headline line (default); the others print their own "
+                         "line at the full sizes of that workload")
+    ap.add_argument("--sizes", default="", help="point / dd: comma-separated n (or m:n:k)")
+    ap.add_argument("--phis", default="", help="point / dd: comma-separated phi")
+    ap.add_argument("--slice-list", default="", help="point: comma-separated slice counts")
+    ap.add_argument("--no-also", action="store_true", help="skip the short other workloads")
     ap.add_argument("--only-headline", action="store_true",
                     help="time the headline form only (profiling runs): no plain form, "
                          "width, containment, e2e or CPU legs")
@@ -339,6 +359,12 @@ def run_ours(args, ws, rank, local):
                "sample": f"{rows_s} x {n} x {n} row panel ({dt:.1f} s), oracle restatement of "
                          "pidblas::mulmm over the vblas sequential-chain dgemm"}
 
+    also = None
+    if rank == 0 and not args.no_also:
+        del dA, dB, dC
+        torch.cuda.empty_cache()
+        also = bench_also(dev, stream)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -359,6 +385,7 @@ def run_ours(args, ws, rank, local):
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
+            "also": also,
         }
         print(json.dumps(line), flush=True)
 
@@ -401,11 +428,273 @@ def ozaki_roofline(phases, tc_flops, steps, pk, pk_kind):
                                   "radius2": phases[2] / steps, "midpoint": phases[3] / steps}}
 
 
+# ---------------------------------------------------------------- other workloads
+BATCH_WORKLOAD = ("batched interval GEMMs: 4096 problems, m,n,k log-uniform [32,1024], "
+                  "mid U[-1,1], rad 1e-12|mid|")
+
+
+def dev_intervals(count, gen, dev, rad_ratio=1e-12):
+    """kv buffer of `count` intervals, mid U[-1, 1], rad rad_ratio |mid|."""
+    import torch
+    out = torch.empty(2 * count, dtype=torch.float64, device=dev)
+    v = out.view(-1, 2)
+    step = 1 << 26
+    for a in range(0, count, step):
+        b = min(count, a + step)
+        mid = torch.rand(b - a, generator=gen, dtype=torch.float64, device=dev) * 2.0 - 1.0
+        rad = mid.abs() * rad_ratio
+        v[a:b, 0] = mid - rad
+        v[a:b, 1] = mid + rad
+    return out
+
+
+def dev_ephi(count, phi, gen, dev):
+    """E(phi) entries on the device: mantissa U[1, 2), random sign, exponent U{-phi..phi}."""
+    import torch
+    mant = 1.0 + torch.rand(count, generator=gen, dtype=torch.float64, device=dev)
+    sign = torch.randint(0, 2, (count,), generator=gen, device=dev) * 2 - 1
+    ex = torch.randint(-phi, phi + 1, (count,), generator=gen, device=dev)
+    return torch.ldexp(mant * sign, ex.to(torch.float64))
+
+
+def dev_dd(count, phi, gen, dev):
+    """dd buffer: hi from E(phi), lo = hi 2^-53 u, u U[-1, 1]."""
+    import torch
+    hi = dev_ephi(count, phi, gen, dev)
+    u = torch.rand(count, generator=gen, dtype=torch.float64, device=dev) * 2.0 - 1.0
+    out = torch.empty(2 * count, dtype=torch.float64, device=dev)
+    out.view(-1, 2)[:, 0] = hi
+    out.view(-1, 2)[:, 1] = hi * 2.0 ** -53 * u
+    return out
+
+
+def time_stream(fn, stream, steps, warmup=1):
+    import torch
+    torch.cuda.synchronize()  # inputs are made on torch's stream, the work runs on `stream`
+    for _ in range(warmup):
+        fn()
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    stream.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def bench_batch(dev, stream, steps=1, count=4096, seed=4096, forms=("plain", "ozaki", "auto"),
+                check=True):
+    """Batched uneven interval GEMMs through captured CUDA graphs."""
+    import torch
+    from vcp_gb300 import batch, pidcuda
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    dims = np.exp(rng.uniform(np.log(32), np.log(1024), (count, 3))).round().astype(np.int64)
+    m, n, k = dims[:, 0], dims[:, 1], dims[:, 2]
+    na, nb, nc = m * k, k * n, m * n
+    oa = np.concatenate([[0], np.cumsum(na)])
+    ob = np.concatenate([[0], np.cumsum(nb)])
+    oc = np.concatenate([[0], np.cumsum(nc)])
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    pa = dev_intervals(int(oa[-1]), gen, dev)
+    pb = dev_intervals(int(ob[-1]), gen, dev)
+    pc = torch.empty(2 * int(oc[-1]), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()  # the pools are written on torch's stream
+    probs = [(int(m[i]), int(n[i]), int(k[i]), pa[2 * oa[i]:2 * oa[i + 1]], int(m[i]),
+              pb[2 * ob[i]:2 * ob[i + 1]], int(k[i]), pc[2 * oc[i]:2 * oc[i + 1]], int(m[i]))
+             for i in range(count)]
+    flops = float(np.sum(2.0 * m * n * k))
+    out = {"workload": BATCH_WORKLOAD, "problems": count, "gflop_per_batch": flops / 1e9,
+           "seed": seed}
+    codes = {"plain": pidcuda.FORM_PLAIN, "ozaki": pidcuda.FORM_OZAKI, "auto": pidcuda.FORM_AUTO}
+    sample = rng.choice(count, 6, replace=False)
+    widths = {}
+    for name in forms:
+        t0 = time.perf_counter()
+        g = batch.BatchGraph(probs, codes[name], 0, stream)
+        t_create = time.perf_counter() - t0
+        ms = time_stream(lambda: g.launch(stream), stream, steps)
+        _, lat = g.latencies(stream)
+        rec = {"tflops": flops / (ms * 1e-3) / 1e12, "ms_per_batch": ms,
+               "p50_us": float(np.percentile(lat, 50)), "p99_us": float(np.percentile(lat, 99)),
+               "graph_create_s": t_create}
+        if name == "auto":
+            rec["problems_on_tensor_cores"] = int(sum(
+                pidcuda.autotune_choice(int(m[i]), int(n[i]), int(k[i])) != pidcuda.FORM_PLAIN
+                for i in range(count)))
+        if check:
+            fails, ws = 0, []
+            for i in sample:
+                Ah = probs[i][3].cpu().numpy()
+                Bh = probs[i][5].cpu().numpy()
+                Ch = probs[i][7].cpu().numpy()
+                mi, ni, ki = int(m[i]), int(n[i]), int(k[i])
+                r = np.random.default_rng(i).integers(0, mi, 64)
+                c = np.random.default_rng(i + 1).integers(0, ni, 64)
+                lo, up = O.exact_hull(mi, ni, ki, Ah, Bh, r, c)
+                idx = 2 * (r + c * mi)
+                fails += int(np.sum(Ch[idx] > lo) + np.sum(Ch[idx + 1] < up))
+                ws.append(Ch[1::2] - Ch[0::2])
+            rec["containment_failures"] = fails
+            rec["containment_sample"] = int(64 * len(sample))
+            widths[name] = np.concatenate(ws)
+        g.close()
+        out[name] = rec
+    if "plain" in widths and "ozaki" in widths:
+        out["width_ozaki_vs_plain_median"] = float(np.median(widths["ozaki"] / widths["plain"]))
+    del pa, pb, pc
+    return out
+
+
+def bench_dd(dev, stream, n, phi, steps=2, seed=77, sample=256):
+    import torch
+    from vcp_gb300 import pddcuda
+    from oracle import oracle as O
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed + n + phi)
+    A = dev_dd(n * n, phi, gen, dev)
+    B = dev_dd(n * n, phi, gen, dev)
+    C = torch.empty(2 * n * n, dtype=torch.float64, device=dev)
+    E = torch.empty(n * n, dtype=torch.float64, device=dev)
+    ms = time_stream(lambda: pddcuda.mulmm_dev(n, n, n, A, n, B, n, C, n, E, n, 0, stream),
+                     stream, steps)
+    Ah, Bh, Ch, Eh = (t.cpu().numpy() for t in (A, B, C, E))
+    rs = np.random.default_rng(seed)
+    r = rs.integers(0, n, sample)
+    c = rs.integers(0, n, sample)
+    err, ab = O.dd_residual(n, n, n, Ah, Bh, Ch, r, c)
+    bnd = Eh[r + c * n]
+    rel = err / np.where(ab > 0, ab, 1.0)
+    nz = err > 0
+    return {"n": n, "phi": phi, "tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12, "ms": ms,
+            "rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel)),
+            "bound_failures": int(np.sum(err > bnd)),
+            "bound_over_err_median": float(np.median(bnd[nz] / err[nz])) if nz.any() else None,
+            "bound_rel_median": float(np.median(bnd / np.where(ab > 0, ab, 1.0))),
+            "sample": sample, "slices": "default (13, w = 104)"}
+
+
+def bench_point(dev, stream, m, n, k, phi, slice_list, steps=2, plain=True, seed=11,
+                sample=256):
+    """udmatmul shape (vblas naming: A m x n, B n x k)."""
+    import torch
+    from vcp_gb300 import vblas
+    from oracle import oracle as O
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed + m + n + k + phi)
+    A = dev_ephi(m * n, phi, gen, dev)
+    B = dev_ephi(n * k, phi, gen, dev)
+    CU = torch.empty(m * k, dtype=torch.float64, device=dev)
+    CD = torch.empty_like(CU)
+    fl = 2.0 * m * n * k
+    rs = np.random.default_rng(seed)
+    r = rs.integers(0, m, sample)
+    c = rs.integers(0, k, sample)
+    Ah, Bh = A.cpu().numpy(), B.cpu().numpy()
+    dn, up = O.exact_dot(m, k, n, Ah, Bh, r, c)
+    idx = r + c * m
+    out = {"m": m, "n": n, "k": k, "phi": phi}
+    wp = None
+    if plain:
+        ms = time_stream(lambda: vblas.udmatmul_dev(m, n, k, A, m, B, n, CU, CD, m, stream),
+                         stream, steps)
+        u, d = CU.cpu().numpy(), CD.cpu().numpy()
+        wp = u - d
+        out["plain"] = {"tflops": fl / (ms * 1e-3) / 1e12, "ms": ms,
+                        "containment_failures": int(np.sum(d[idx] > dn) + np.sum(u[idx] < up))}
+    for s_ in slice_list:
+        ms = time_stream(lambda: vblas.udmatmul_ozaki_dev(m, n, k, A, m, B, n, CU, CD, m, s_,
+                                                          stream), stream, steps)
+        u, d = CU.cpu().numpy(), CD.cpu().numpy()
+        rec = {"tflops": fl / (ms * 1e-3) / 1e12, "ms": ms,
+               "containment_failures": int(np.sum(d[idx] > dn) + np.sum(u[idx] < up))}
+        if wp is not None:
+            ok = wp > 0
+            rec["width_vs_plain_median"] = float(np.median((u - d)[ok] / wp[ok]))
+        out[f"ozaki_s{s_}"] = rec
+    return out
+
+
+def parse_list(text, default, conv=int):
+    return [conv(x) for x in text.split(",") if x] if text else default
+
+
+def run_workload(args, dev, stream):
+    """--workload batch | dd | point: one JSON line at that workload's sizes."""
+    import torch
+    from vcp_gb300 import pidcuda
+    t0 = time.perf_counter()
+    with ClockSampler(dev.index or 0) as clk:
+        if args.workload == "batch":
+            pidcuda.autotune(stream)
+            res = bench_batch(dev, stream, steps=args.steps)
+            metric, unit = "batched interval GEMM TFLOP/s (4096 uneven problems)", "TFLOP/s"
+            value = res["ozaki"]["tflops"]
+        elif args.workload == "dd":
+            res = {"cases": [bench_dd(dev, stream, n, phi, steps=args.steps)
+                             for n in parse_list(args.sizes, [2048, 8192])
+                             for phi in parse_list(args.phis, [0, 16])]}
+            metric, unit = "dd GEMM TFLOP/s (pddblas semantics)", "TFLOP/s"
+            value = max(c["tflops"] for c in res["cases"])
+        else:
+            shapes = []
+            for tok in (args.sizes.split(",") if args.sizes else
+                        ["1024", "4096", "8192", "16384", "16384:16384:256"]):
+                dims = [int(x) for x in tok.split(":")]
+                shapes.append(tuple(dims) if len(dims) == 3 else (dims[0],) * 3)
+            cases = []
+            for (m_, n_, k_) in shapes:
+                for phi in parse_list(args.phis, [0, 8, 32]):
+                    cases.append(bench_point(dev, stream, m_, n_, k_, phi,
+                                             parse_list(args.slice_list, [4, 5, 6, 7, 8, 9]),
+                                             steps=args.steps))
+                    torch.cuda.empty_cache()
+            res = {"cases": cases}
+            metric, unit = "up/down point GEMM TFLOP/s: Ozaki enclosure vs FP64 RU/RD", "TFLOP/s"
+            value = None
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "workload": args.workload, "data": "synthetic (seeded)", "results": res,
+            "wall_s": time.perf_counter() - t0, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def bench_also(dev, stream):
+    """Short runs of the other workloads for the headline line."""
+    from vcp_gb300 import pidcuda
+    out = {}
+    for key, fn in (("autotune", lambda: pidcuda.autotune(stream)),
+                    ("batch", lambda: bench_batch(dev, stream, steps=1)),
+                    ("dd", lambda: [bench_dd(dev, stream, 2048, phi, steps=2) for phi in (0, 16)]),
+                    ("point", lambda: bench_point(dev, stream, 4096, 4096, 4096, 0, [6, 8],
+                                                  steps=2))):
+        t0 = time.perf_counter()
+        try:
+            out[key] = fn()
+        except Exception as e:  # reported, the headline line still prints
+            out[key] = {"error": f"{type(e).__name__}: {e}"}
+        if isinstance(out[key], dict):
+            out[key]["wall_s"] = time.perf_counter() - t0
+    return out
+
+
 def main():
     args = parse()
     ws, rank, local = dist_init(args)
     if args.impl == "reference":
         run_reference(args, ws, rank)
+    elif args.workload != "interval":
+        import torch
+        from vcp_gb300.build import build
+        if rank == 0:
+            build()
+        barrier(ws)
+        torch.cuda.set_device(local)
+        dev = torch.device("cuda", local)
+        if rank == 0:
+            run_workload(args, dev, torch.cuda.Stream(device=dev))
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

@@ -32,6 +32,7 @@ def lib() -> C.CDLL:
         L.orc_exact_hull.argtypes = [_i, _i, _i, _v, _v, _l, _v, _v, _v, _v, _i]
         L.orc_exact_dot.argtypes = [_i, _i, _i, _v, _v, _l, _v, _v, _v, _v, _i]
         L.orc_exact_sum.argtypes = [_l, _v, _i]
+        L.orc_dd_residual.argtypes = [_i, _i, _i, _v, _v, _v, _l, _v, _v, _v, _v, _i]
         L.orc_exact_sum.restype = C.c_double
         L.orc_ozaki_igemm.argtypes = [_i, _i, _i, _v, _v, _v, _i, _i]
         L.orc_ozaki_igemm.restype = _i
@@ -116,6 +117,18 @@ def exact_dot(m, n, k, A, B, rows, cols, threads=0):
     lib().orc_exact_dot(m, n, k, _p(A), _p(B), rows.size, _p(rows), _p(cols), _p(dn), _p(up),
                         int(threads))
     return dn, up
+
+
+def dd_residual(m, n, k, A, B, C, rows, cols, threads=0):
+    """(RU|exact - C|, RD|exact|) per sampled entry of a dd product C ~ A B
+    (dd pairs, ld = rows): the error of a dd GEMM against the exact value."""
+    rows = np.ascontiguousarray(rows, dtype=np.int32)
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    err = np.empty(rows.size)
+    ab = np.empty(rows.size)
+    lib().orc_dd_residual(m, n, k, _p(A), _p(B), _p(C), rows.size, _p(rows), _p(cols), _p(err),
+                          _p(ab), int(threads))
+    return err, ab
 
 
 def ozaki_igemm(m, n, k, A, B, s=8, sr=2, crt=True):

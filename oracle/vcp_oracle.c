@@ -434,6 +434,49 @@ void orc_exact_dot(int m, int n, int k, const double* A, const double* B, long c
   }
 }
 
+static void acc_add_double(orc_acc* a, double x, int negate) {
+  if (x == 0.0) return;
+  int sg, e;
+  uint64_t mt;
+  decompose(x, &sg, &mt, &e);
+  acc_add_u128(a, (unsigned __int128)mt, e + ACC_BIAS, sg ^ negate);
+}
+
+/* Error of a dd GEMM result against the exact product (pddblas::mulmm,
+ * vcp/pddblas.hpp:318-376, computes C ~ A*B in dd).  A (m x k), B (k x n),
+ * C (m x n) are dd matrices as {hi, lo} pairs, ld = rows.  For each sampled
+ * entry: S = sum_p (A1 + A2)(B1 + B2) exactly (four double products per
+ * term), out_err = RU(|S - (C1 + C2)|) and out_abs = RD(|S|). */
+void orc_dd_residual(int m, int n, int k, const double* A, const double* B, const double* C,
+                     long count, const int* rows, const int* cols, double* out_err,
+                     double* out_abs, int nthreads) {
+  (void)n;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+#endif
+  for (long t = 0; t < count; ++t) {
+    const int i = rows[t], j = cols[t];
+    orc_acc s;
+    acc_zero(&s);
+    for (int p = 0; p < k; ++p) {
+      const double* a = A + 2 * ((long)i + (long)p * m);
+      const double* b = B + 2 * ((long)p + (long)j * k);
+      acc_add_xprod(&s, exact_mul(a[0], b[0]));
+      acc_add_xprod(&s, exact_mul(a[0], b[1]));
+      acc_add_xprod(&s, exact_mul(a[1], b[0]));
+      acc_add_xprod(&s, exact_mul(a[1], b[1]));
+    }
+    const double sd = acc_round(&s, -1), su = acc_round(&s, +1);
+    out_abs[t] = (sd > 0.0) ? sd : (su < 0.0 ? -su : 0.0);
+    const double* c = C + 2 * ((long)i + (long)j * m);
+    acc_add_double(&s, c[0], 1);
+    acc_add_double(&s, c[1], 1);
+    const double du = acc_round(&s, +1), dd = acc_round(&s, -1);
+    out_err[t] = fabs(du) > fabs(dd) ? fabs(du) : fabs(dd);
+  }
+}
+
 /* Exact sum of a list of doubles, rounded in direction dir (self-test hook). */
 double orc_exact_sum(long count, const double* x, int dir) {
   orc_acc s;

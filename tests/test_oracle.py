@@ -192,3 +192,21 @@ def test_oracle_other_products_match_reference_build(oracle):
     assert oracle.ref_call("ref_norm_I_minus_RA", nn, oracle._p(Rinv), oracle._p(Ai),
                            ctypes.addressof(g)) == 0
     assert oracle.norm_I_minus_RA(nn, Rinv, Ai) == g.value
+
+
+def test_dd_residual_known_answers(oracle):
+    """orc_dd_residual: exact |S - C| for a dd product with a known value."""
+    import numpy as np
+    A = np.array([1.0, 2.0 ** -60])          # 1 + 2^-60
+    B = np.array([3.0, 0.0])
+    rows = np.array([0])
+    cols = np.array([0])
+    err, ab = oracle.dd_residual(1, 1, 1, A, B, np.array([3.0, 3 * 2.0 ** -60]), rows, cols)
+    assert err[0] == 0.0 and ab[0] == 3.0
+    err, _ = oracle.dd_residual(1, 1, 1, A, B, np.array([3.0, 0.0]), rows, cols)
+    assert err[0] == 3 * 2.0 ** -60
+    # two terms whose hi parts cancel: S = 2^-70 exactly
+    A2 = np.array([1.0, 0.0, 1.0, 2.0 ** -70])
+    B2 = np.array([1.0, 0.0, -1.0, 0.0])
+    err, ab = oracle.dd_residual(1, 1, 2, A2, B2, np.array([0.0, 0.0]), rows, cols)
+    assert ab[0] == 2.0 ** -70 and err[0] == 2.0 ** -70

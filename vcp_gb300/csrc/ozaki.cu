@@ -300,7 +300,7 @@ int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long ld
   }
   if (rad2) {
     PhaseTimer t(2, s);
-    if ((st = oz_run_gemm(plan, rad1 ? OZ_RAD_ADD : OZ_RAD_SET, ws, nullptr, 0, s))) return st;
+    if ((st = oz_run_gemm(plan, OZ_RAD_ADD, ws, nullptr, 0, s, rad1 ? 0 : 1))) return st;
   }
   if (!rad1 && !rad2)
     VCPCU_CUDA_TRY(cudaMemsetAsync(ws.T, 0, sizeof(double) * (size_t)plan.pb.Mp * plan.pb.Np, s));

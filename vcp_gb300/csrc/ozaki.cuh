@@ -49,6 +49,8 @@ struct OzPairList {
   int8_t gt[OZ_MAX_GROUPS];                    // t of group g
 };
 
+// OZ_RAD_SET: radius product 1, (|mA| + rA) * rB; OZ_RAD_ADD: radius
+// product 2, rA * |mB|.  Each writes T or adds to it (OzGemmArgs::t_set).
 enum OzMode { OZ_RAD_SET = 0, OZ_RAD_ADD = 1, OZ_MID = 2, OZ_CRT = 3 };
 
 struct alignas(64) OzGemmArgs {
@@ -58,6 +60,7 @@ struct alignas(64) OzGemmArgs {
   int tiles_m, tiles_n;
   int t_ref, R;     // W unit 2^(E_i + F_j - 8 t_ref); R = floor-shifted folds
   int mode;
+  int t_set;        // radius modes: 1 T = product, 0 T +=RU product
   int s;            // midpoint slices (OZ_MID truncation bound)
   const int* Erow;  // row exponent of the left operand:  Erow[erow_stride * i]
   int erow_stride;
@@ -95,8 +98,10 @@ int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long l
                     cudaStream_t st);
 int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, long ldb,
                OzWorkspace& ws, cudaStream_t st);
+// t_set < 0: the radius product of OZ_RAD_SET writes T, that of OZ_RAD_ADD
+// adds to it; 0 / 1 force add / write.
 int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, long ldc,
-                cudaStream_t st);
+                cudaStream_t st, int t_set = -1);
 size_t oz_workspace_bytes(const OzProblem& pb);
 int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws);
 

@@ -21,7 +21,7 @@ namespace {
 struct CrtConst {
   uint32_t Q[16][4];
   uint32_t M[4];
-  double Md;
+  float invMf;  // 2^64 / M rounded to float: the quotient estimate of the reduction
 };
 
 __device__ __forceinline__ double scale_dir2(double x, int e, bool up) {
@@ -35,6 +35,38 @@ __device__ __forceinline__ double scale_dir2(double x, int e, bool up) {
   }
   const double p = __longlong_as_double((long long)(e + 1023) << 52);
   return up ? __dmul_ru(x, p) : __dmul_rd(x, p);
+}
+
+// x * 2^e rounded up (up) or down: the exponent field is moved on the
+// integer pipe when x and the result are normal (then the product is exact
+// and equals scale_dir2's); otherwise scale_dir2.
+__device__ __forceinline__ double scale_pow2(double x, int e, bool up) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int be = (int)((b >> 52) & 0x7ff);
+  if (be != 0 && be != 0x7ff && be + e >= 1 && be + e <= 2046)
+    return __longlong_as_double((long long)(b + ((unsigned long long)(long long)e << 52)));
+  if (x == 0.0) return x;
+  return scale_dir2(x, e, up);
+}
+
+// RD and RU of t * 2^e for t > 0 (64 bits) built on the integer pipe: the
+// top 53 bits of t are the truncated significand, any lower bit set makes
+// RU one unit larger (a carry into the exponent field is the correct
+// rounding).  Equal to scale_dir2(__ull2double_rd/ru(t), e) -- which runs
+// when the result leaves the normal range.
+__device__ __forceinline__ void u64_to_dir(unsigned long long t, int e, double& dn, double& upv) {
+  const int lz = __clzll(t);
+  const unsigned long long tn = t << lz;
+  const int be = 1023 + 63 - lz + e;
+  if (be >= 1 && be <= 2046) {
+    const unsigned long long d =
+        ((unsigned long long)be << 52) + ((tn >> 11) & ((1ULL << 52) - 1));
+    dn = __longlong_as_double((long long)d);
+    upv = __longlong_as_double((long long)(d + ((tn & 0x7ffULL) ? 1ULL : 0ULL)));
+    return;
+  }
+  dn = scale_dir2(__ull2double_rd(t), e, false);
+  upv = scale_dir2(__ull2double_ru(t), e, true);
 }
 
 // r (5 limbs of 32 bits, little endian) >= m (4 limbs)?
@@ -93,17 +125,88 @@ __device__ __forceinline__ void big_to_dir(const uint32_t* mag, int neg, int e, 
     if (bq) sticky |= (mag[wq] & ((1u << bq) - 1u)) != 0;
   }
   if (sticky) t |= 1ULL;
-  const double a_dn = __ull2double_rd(t), a_up = __ull2double_ru(t);
-  const int ex = e + sh;
+  double a_dn, a_up;
+  u64_to_dir(t, e + sh, a_dn, a_up);
   if (!neg) {
-    lo = scale_dir2(a_dn, ex, false);
-    up = scale_dir2(a_up, ex, true);
+    lo = a_dn;
+    up = a_up;
   } else {
-    lo = -scale_dir2(a_up, ex, true);
-    up = -scale_dir2(a_dn, ex, false);
+    lo = -a_up;
+    up = -a_dn;
   }
 }
 
+// Exact X = (A'B')(i, j) from its residues (see the file comment); returns
+// the magnitude in mag[4] and the sign.
+// c[l] = 0 and Q_l = 0 for l >= L.
+__device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const CrtConst& cc,
+                                         uint32_t (&mag)[4]) {
+  unsigned long long s[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int l = 0; l < 16; ++l) {
+#pragma unroll
+    for (int t = 0; t < 4; ++t) s[t] += (unsigned long long)c[l] * cc.Q[l][t];
+  }
+  uint32_t r[5];
+  unsigned long long carry = 0;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const unsigned long long v = s[t] + carry;
+    r[t] = (uint32_t)v;
+    carry = v >> 32;
+  }
+  r[4] = (uint32_t)carry;
+  // q = floor(S / M) < 2^12 estimated in fp32 (relative error < 2^-20, so
+  // off by at most one), then corrected exactly
+  const float Sf = __uint2float_rn(r[4]) * 0x1p64f + __uint2float_rn(r[3]) * 0x1p32f +
+                   __uint2float_rn(r[2]) + __uint2float_rn(r[1]) * 0x1p-32f +
+                   __uint2float_rn(r[0]) * 0x1p-64f;
+  const unsigned int q = (unsigned int)(Sf * cc.invMf);
+  if (q) {
+    unsigned long long qm[5];
+    unsigned long long c2 = 0;
+    for (int t = 0; t < 4; ++t) {
+      const unsigned long long v = (unsigned long long)q * cc.M[t] + c2;
+      qm[t] = (uint32_t)v;
+      c2 = v >> 32;
+    }
+    qm[4] = c2;
+    unsigned long long borrow = 0;
+    for (int t = 0; t < 5; ++t) {
+      const unsigned long long d = (unsigned long long)r[t] - qm[t] - borrow;
+      r[t] = (uint32_t)d;
+      borrow = (d >> 63) & 1ULL;
+    }
+    for (int it = 0; it < 4 && borrow; ++it) {  // q was too large
+      add_M(r, cc.M);
+      borrow = (r[4] >> 31) & 1u;  // still negative (two's complement in 5 limbs)
+    }
+  }
+  for (int it = 0; it < 4 && ge_M(r, cc.M); ++it) sub_M(r, cc.M);
+  // centre: X = r if 2r < M, else r - M (magnitude M - r)
+  uint32_t twice[5];
+  unsigned long long cy = 0;
+  for (int t = 0; t < 5; ++t) {
+    const unsigned long long v = ((unsigned long long)r[t] << 1) + cy;
+    twice[t] = (uint32_t)v;
+    cy = v >> 32;
+  }
+  if (ge_M(twice, cc.M)) {
+    unsigned long long b = 0;
+    for (int t = 0; t < 4; ++t) {
+      const unsigned long long d = (unsigned long long)cc.M[t] - r[t] - b;
+      mag[t] = (uint32_t)d;
+      b = (d >> 63) & 1ULL;
+    }
+    return 1;
+  }
+  for (int t = 0; t < 4; ++t) mag[t] = r[t];
+  return 0;
+}
+
+// One thread per 4 consecutive rows of one column: the residue planes are
+// read 4 bytes at a time, T 32 bytes, C written as 4 consecutive pairs.  Only the final
+// error sum and the two outward roundings use the FP64 pipe.
 __global__ void __launch_bounds__(256)
 oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __restrict__ res,
                        size_t plane, const int* __restrict__ E3, const int* __restrict__ F2,
@@ -112,88 +215,58 @@ oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __rest
                        double* __restrict__ C, long ldc, const int* __restrict__ flag,
                        const __grid_constant__ CrtConst cc) {
   const bool nonfinite = flag[0] != 0 || flag[1] != 0;
-  const long total = (long)M * N;
+  const int Mq = (M + 3) >> 2;
+  const long total = (long)Mq * N;
   for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(idx % M), j = (int)(idx / M);
-    const size_t e = (size_t)j * Mp + i;
-    const int Ei = E3[3 * i], Fj = F2[2 * j];
-    double lo = 0.0, up = 0.0, tr = 0.0;
-    if (Ei != OZ_ZERO_EXP && Fj != OZ_ZERO_EXP) {
-      unsigned long long s[4] = {0, 0, 0, 0};
-      for (int l = 0; l < L; ++l) {
-        const unsigned long long c = res[(size_t)l * plane + e];
+    const int i0 = 4 * (int)(idx % Mq), j = (int)(idx / Mq);
+    const size_t e0 = (size_t)j * Mp + i0;
+    const int Fj = F2[2 * j];
+    const double bj = beta[j];
+    uint32_t pk[16];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) s[t] += c * cc.Q[l][t];
-      }
-      uint32_t r[5];
-      unsigned long long carry = 0;
+    for (int l = 0; l < 16; ++l)
+      pk[l] = l < L ? *reinterpret_cast<const uint32_t*>(res + (size_t)l * plane + e0) : 0u;
+    const double4 Tv = *reinterpret_cast<const double4*>(T + e0);
+    const double Ta[4] = {Tv.x, Tv.y, Tv.z, Tv.w};
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const unsigned long long v = s[t] + carry;
-        r[t] = (uint32_t)v;
-        carry = v >> 32;
-      }
-      r[4] = (uint32_t)carry;
-      // q = floor(S / M) estimated from the top limbs, then corrected
-      const double Sd = (double)r[4] * 0x1p128 + (double)r[3] * 0x1p96 + (double)r[2] * 0x1p64 +
-                        (double)r[1] * 0x1p32 + (double)r[0];
-      unsigned int q = (unsigned int)(Sd / cc.Md);
-      if (q) {
-        // r -= q * M
-        unsigned long long qm[5];
-        unsigned long long c2 = 0;
-        for (int t = 0; t < 4; ++t) {
-          const unsigned long long v = (unsigned long long)q * cc.M[t] + c2;
-          qm[t] = (uint32_t)v;
-          c2 = v >> 32;
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u;
+      if (i >= M) break;
+      const int Ei = E3[3 * i];
+      double lo = 0.0, up = 0.0, tr = 0.0;
+      if (Ei != OZ_ZERO_EXP && Fj != OZ_ZERO_EXP) {
+        uint32_t c[16], mag[4];
+#pragma unroll
+        for (int l = 0; l < 16; ++l) c[l] = (pk[l] >> (8 * u)) & 0xffu;
+        const int neg = crt_value(c, cc, mag);
+        big_to_dir(mag, neg, Ei + Fj - 2 * w, lo, up);
+        // truncation bound: sA = RU(asum_hi 2^32 + asum_lo) (exact below 2^96)
+        const unsigned long long ah = asum[2 * i + 0], al = asum[2 * i + 1];
+        const unsigned __int128 sx = ((unsigned __int128)ah << 32) + al;
+        double sA = 0.0, sAdn;
+        if (sx) {
+          const unsigned long long hi64 = (unsigned long long)(sx >> 64);
+          if (hi64 == 0) {
+            u64_to_dir((unsigned long long)sx, 0, sAdn, sA);
+          } else {
+            const int sh = 64 - __clzll(hi64);
+            unsigned long long t = (unsigned long long)(sx >> sh);
+            if ((unsigned long long)sx & ((1ULL << sh) - 1)) t |= 1ULL;
+            u64_to_dir(t, sh, sAdn, sA);
+          }
         }
-        qm[4] = c2;
-        unsigned long long borrow = 0;
-        for (int t = 0; t < 5; ++t) {
-          const unsigned long long d = (unsigned long long)r[t] - qm[t] - borrow;
-          r[t] = (uint32_t)d;
-          borrow = (d >> 63) & 1ULL;
-        }
-        for (int it = 0; it < 4 && borrow; ++it) {  // q was too large
-          add_M(r, cc.M);
-          borrow = (r[4] >> 31) & 1u;  // still negative (two's complement in 5 limbs)
-        }
+        const double t1 = scale_pow2(bj, Ei - w - 1, true);
+        const double t2 = scale_pow2(sA, Ei + Fj - 2 * w - 1, true);
+        tr = __dadd_ru(t1, t2);
       }
-      for (int it = 0; it < 4 && ge_M(r, cc.M); ++it) sub_M(r, cc.M);
-      // centre: X = r if 2r < M, else r - M (magnitude M - r)
-      uint32_t twice[5];
-      unsigned long long cy = 0;
-      for (int t = 0; t < 5; ++t) {
-        const unsigned long long v = ((unsigned long long)r[t] << 1) + cy;
-        twice[t] = (uint32_t)v;
-        cy = v >> 32;
-      }
-      int neg = 0;
-      uint32_t mag[4];
-      if (ge_M(twice, cc.M)) {
-        neg = 1;
-        unsigned long long b = 0;
-        for (int t = 0; t < 4; ++t) {
-          const unsigned long long d = (unsigned long long)cc.M[t] - r[t] - b;
-          mag[t] = (uint32_t)d;
-          b = (d >> 63) & 1ULL;
-        }
-      } else {
-        for (int t = 0; t < 4; ++t) mag[t] = r[t];
-      }
-      big_to_dir(mag, neg, Ei + Fj - 2 * w, lo, up);
-      // truncation bound
-      const double sA = __fma_ru((double)asum[2 * i + 0], 0x1p32, (double)asum[2 * i + 1]);
-      const double t1 = scale_dir2(beta[j], Ei - w - 1, true);
-      const double t2 = scale_dir2(sA, Ei + Fj - 2 * w - 1, true);
-      tr = __dadd_ru(t1, t2);
+      const double err = __dadd_ru(tr, Ta[u]);
+      double clo = __dsub_rd(lo, err), cup = __dadd_ru(up, err);
+      if (nonfinite) clo = cup = __longlong_as_double(0x7ff8000000000000LL);
+      double* cp = C + 2 * ((size_t)i + (size_t)j * ldc);  // C may be only 8-byte aligned
+      cp[0] = clo;
+      cp[1] = cup;
     }
-    const double err = __dadd_ru(tr, T[e]);
-    double clo = __dsub_rd(lo, err), cup = __dadd_ru(up, err);
-    if (nonfinite) clo = cup = __longlong_as_double(0x7ff8000000000000LL);
-    C[2 * ((size_t)i + (size_t)j * ldc)] = clo;
-    C[2 * ((size_t)i + (size_t)j * ldc) + 1] = cup;
   }
 }
 
@@ -207,9 +280,10 @@ int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long l
   for (int l = 0; l < pb.L; ++l)
     for (int t = 0; t < 4; ++t) cc.Q[l][t] = plan.Q[l][t];
   for (int t = 0; t < 4; ++t) cc.M[t] = plan.Mlimb[t];
-  cc.Md = (double)cc.M[3] * 0x1p96 + (double)cc.M[2] * 0x1p64 + (double)cc.M[1] * 0x1p32 +
-          (double)cc.M[0];
-  const long total = (long)pb.M * pb.N;
+  const double Md = (double)cc.M[3] * 0x1p96 + (double)cc.M[2] * 0x1p64 +
+                    (double)cc.M[1] * 0x1p32 + (double)cc.M[0];
+  cc.invMf = (float)(0x1p64 / Md);
+  const long total = (long)((pb.M + 3) / 4) * pb.N;
   long blocks = (total + 255) / 256;
   if (blocks > 152L * 64) blocks = 152L * 64;
   if (blocks < 1) blocks = 1;

@@ -318,7 +318,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
           double* Tp = args.T + (size_t)gj * args.Mp + gi;
           if (args.mode == OZ_RAD_SET || args.mode == OZ_RAD_ADD) {
             const double b = zero ? 0.0 : scale_dir(__ll2double_ru(v + args.R), ex, true);
-            *Tp = (args.mode == OZ_RAD_SET) ? b : __dadd_ru(*Tp, b);
+            *Tp = args.t_set ? b : __dadd_ru(*Tp, b);
           } else {
             double mlo = 0.0, mup = 0.0, tr = 0.0;
             if (!zero) {
@@ -403,7 +403,7 @@ int num_sms() {
 size_t oz_dyn_smem() { return (size_t)OZ_STAGES * STAGE_BYTES + 1024; }
 
 int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, long ldc,
-                cudaStream_t st) {
+                cudaStream_t st, int t_set) {
   const OzProblem& pb = plan.pb;
   static bool attr_set = false;
   if (!attr_set) {
@@ -444,6 +444,7 @@ int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, 
   a.tiles_m = pb.Mp / OZ_BM;
   a.tiles_n = pb.Np / OZ_BN;
   a.mode = mode;
+  a.t_set = t_set >= 0 ? t_set : (mode == OZ_RAD_SET ? 1 : 0);
   a.s = pb.s;
   a.erow_stride = 3;
   a.fcol_stride = 2;

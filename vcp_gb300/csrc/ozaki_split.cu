@@ -348,79 +348,87 @@ __device__ __forceinline__ long long crt_int(double x, int E, int w) {
 
 // Left factor, CRT form: residues of A' (L planes) + radius digits, and
 // sum_k |A'(i,k)| split as (|A'| >> 32, |A'| & 0xffffffff) sums.
+// Block: 32 rows x 64 k; lane = row, warp q takes k0 + 8q .. k0 + 8q + 7, so
+// the loads of mA / rA are coalesced across the warp and each lane writes 8
+// bf16 (16 bytes) per plane -- no shared-memory transpose, full occupancy.
 template <int SR>
 __global__ void __launch_bounds__(256)
 oz_split_left_crt(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
                   const double* __restrict__ rA, int L, int w, const int* __restrict__ E3,
                   uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_p,
                   uint16_t* __restrict__ planes_r, unsigned long long* __restrict__ asum) {
-  extern __shared__ int16_t sd[];  // [plane][LT_R][LT_KS]
-  const int np = L + 2 * SR;
-  const int tid = threadIdx.x;
-  const int r = tid % LT_R, kph = tid / LT_R;
-  const int i = blockIdx.y * LT_R + r;
-  const int k0 = blockIdx.x * LT_K;
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  const int i = blockIdx.y * 32 + lane;
+  const int k0 = blockIdx.x * 64 + wq * 8;
   int Em = OZ_ZERO_EXP, Ep = OZ_ZERO_EXP, Er = OZ_ZERO_EXP;
   if (i < M) {
     Em = E3[3 * i + 0];
     Ep = E3[3 * i + 1];
     Er = E3[3 * i + 2];
   }
+  unsigned long long ua[8];
+  unsigned negm = 0;
+  double pv[8], rv[8];
   unsigned long long shi = 0, slo = 0;
-  int dr[SR];
-  for (int kk = kph; kk < LT_K; kk += 8) {
-    const int k = k0 + kk;
-    double m = 0.0, rr = 0.0, p = 0.0;
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    const int k = k0 + t;
+    double m = 0.0, r = 0.0, p = 0.0;
     if (i < M && k < K) {
       m = mA[i + (long)k * M];
-      rr = rA[i + (long)k * M];
-      p = __dadd_ru(fabs(m), rr);
+      r = rA[i + (long)k * M];
+      p = __dadd_ru(fabs(m), r);
     }
     const long long a = crt_int(m, Em, w);
-    const unsigned long long ua = (unsigned long long)(a < 0 ? -a : a);
-    shi += ua >> 32;
-    slo += ua & 0xffffffffULL;
-    for (int l = 0; l < L; ++l)
-      sd[(l * LT_R + r) * LT_KS + kk] = (int16_t)dev_sym_residue(ua, a < 0, l);
-    digits_of<SR>(p, Ep, 1, dr);
-#pragma unroll
-    for (int q = 0; q < SR; ++q) sd[((L + q) * LT_R + r) * LT_KS + kk] = (int16_t)dr[q];
-    digits_of<SR>(rr, Er, 1, dr);
-#pragma unroll
-    for (int q = 0; q < SR; ++q) sd[((L + SR + q) * LT_R + r) * LT_KS + kk] = (int16_t)dr[q];
+    ua[t] = (unsigned long long)(a < 0 ? -a : a);
+    if (a < 0) negm |= 1u << t;
+    pv[t] = p;
+    rv[t] = r;
+    shi += ua[t] >> 32;
+    slo += ua[t] & 0xffffffffULL;
   }
-  __shared__ unsigned long long rs[2][LT_R];
-  if (tid < LT_R) rs[0][tid] = rs[1][tid] = 0;
+  __shared__ unsigned long long red[2][32];
+  if (threadIdx.x < 32) red[0][lane] = red[1][lane] = 0;
   __syncthreads();
-  atomicAdd(&rs[0][r], shi);
-  atomicAdd(&rs[1][r], slo);
+  atomicAdd(&red[0][lane], shi);
+  atomicAdd(&red[1][lane], slo);
   __syncthreads();
-  if (tid < LT_R && blockIdx.y * LT_R + tid < M) {
-    atomicAdd(&asum[2 * (blockIdx.y * LT_R + tid) + 0], rs[0][tid]);
-    atomicAdd(&asum[2 * (blockIdx.y * LT_R + tid) + 1], rs[1][tid]);
+  if (threadIdx.x < 32 && i < M) {
+    atomicAdd(&asum[2 * i + 0], red[0][lane]);
+    atomicAdd(&asum[2 * i + 1], red[1][lane]);
   }
-  const int wr = tid / 8, wk = (tid % 8) * 8;
-  const int gi = blockIdx.y * LT_R + wr;
-  for (int q = 0; q < np; ++q) {
-    uint16_t* base;
-    int pl;
-    if (q < L) {
-      base = planes_m;
-      pl = q;
-    } else if (q < L + SR) {
-      base = planes_p;
-      pl = q - L;
-    } else {
-      base = planes_r;
-      pl = q - L - SR;
+  const size_t rowoff = (size_t)i * Kp + k0;
+  const size_t pstride = (size_t)Mp * Kp;
+  for (int l = 0; l < L; ++l) {
+    uint32_t h[4];
+#pragma unroll
+    for (int t = 0; t < 8; t += 2) {
+      const int r0 = dev_sym_residue(ua[t], (negm >> t) & 1u, l);
+      const int r1 = dev_sym_residue(ua[t + 1], (negm >> (t + 1)) & 1u, l);
+      h[t / 2] = bf16_bits(r0) | (bf16_bits(r1) << 16);
     }
-    const int16_t* src = sd + (q * LT_R + wr) * LT_KS + wk;
-    uint4 v;
-    v.x = bf16_bits(src[0]) | (bf16_bits(src[1]) << 16);
-    v.y = bf16_bits(src[2]) | (bf16_bits(src[3]) << 16);
-    v.z = bf16_bits(src[4]) | (bf16_bits(src[5]) << 16);
-    v.w = bf16_bits(src[6]) | (bf16_bits(src[7]) << 16);
-    if (gi < Mp) *reinterpret_cast<uint4*>(base + ((size_t)pl * Mp + gi) * Kp + k0 + wk) = v;
+    *reinterpret_cast<uint4*>(planes_m + l * pstride + rowoff) = make_uint4(h[0], h[1], h[2], h[3]);
+  }
+  uint32_t hp[SR][4], hr[SR][4];
+#pragma unroll
+  for (int t = 0; t < 8; t += 2) {
+    int d0[SR], d1[SR], e0[SR], e1[SR];
+    digits_of<SR>(pv[t], Ep, 1, d0);
+    digits_of<SR>(pv[t + 1], Ep, 1, d1);
+    digits_of<SR>(rv[t], Er, 1, e0);
+    digits_of<SR>(rv[t + 1], Er, 1, e1);
+#pragma unroll
+    for (int q = 0; q < SR; ++q) {
+      hp[q][t / 2] = bf16_bits(d0[q]) | (bf16_bits(d1[q]) << 16);
+      hr[q][t / 2] = bf16_bits(e0[q]) | (bf16_bits(e1[q]) << 16);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < SR; ++q) {
+    *reinterpret_cast<uint4*>(planes_p + q * pstride + rowoff) =
+        make_uint4(hp[q][0], hp[q][1], hp[q][2], hp[q][3]);
+    *reinterpret_cast<uint4*>(planes_r + q * pstride + rowoff) =
+        make_uint4(hr[q][0], hr[q][1], hr[q][2], hr[q][3]);
   }
 }
 
@@ -535,12 +543,9 @@ int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, 
   int st_ = VCPCU_OK;
   if (pb.crt) {
     VCPCU_CUDA_TRY(cudaMemsetAsync(ws.asum, 0, sizeof(unsigned long long) * 2 * (size_t)pb.Mp, st));
-    dim3 g2(pb.Kp / LT_K, pb.Mp / LT_R);
-    const size_t shm = sizeof(int16_t) * (size_t)(pb.L + 4) * LT_R * LT_KS;
-    VCPCU_CUDA_TRY(cudaFuncSetAttribute(oz_split_left_crt<2>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-    oz_split_left_crt<2><<<g2, 256, shm, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, pb.L,
-                                               pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r, ws.asum);
+    dim3 g2(pb.Kp / 64, pb.Mp / 32);
+    oz_split_left_crt<2><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, pb.L,
+                                             pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r, ws.asum);
     VCPCU_LAUNCH_CHECK("oz_split_left_crt");
     oz_split_right_crt<2><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L, pb.w,
                                                  ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,
@@ -630,18 +635,21 @@ __global__ void dd_exponents(int R, const unsigned long long* __restrict__ mx,
   E[i] = e == OZ_ZERO_EXP ? e : e + 1;
 }
 
-// Left dd factor -> residue planes [L][Mp][Kp] (transposed through smem).
+// Left dd factor -> residue planes [L][Mp][Kp].  Block: 32 rows x 64 k;
+// lane = row, warp q takes k0 + 8q .. k0 + 8q + 7 (coalesced loads across
+// the warp, 16-byte stores per plane, no shared memory).
 __global__ void __launch_bounds__(256)
 dd_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long lda, int L, int w,
               const int* __restrict__ E, uint16_t* __restrict__ planes) {
-  extern __shared__ int16_t sd[];  // [L][LT_R][LT_KS]
-  const int tid = threadIdx.x;
-  const int r = tid % LT_R, kph = tid / LT_R;
-  const int i = blockIdx.y * LT_R + r;
-  const int k0 = blockIdx.x * LT_K;
+  const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+  const int i = blockIdx.y * 32 + lane;
+  const int k0 = blockIdx.x * 64 + wq * 8;
   const int Ei = i < M ? E[i] : OZ_ZERO_EXP;
-  for (int kk = kph; kk < LT_K; kk += 8) {
-    const int k = k0 + kk;
+  unsigned __int128 ua[8];
+  unsigned negm = 0;
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    const int k = k0 + t;
     double hi = 0.0, lo = 0.0;
     if (i < M && k < K) {
       const double2 e = *reinterpret_cast<const double2*>(A + 2 * (i + (long)k * lda));
@@ -651,21 +659,20 @@ dd_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long l
       }
     }
     const __int128 a = dd_int(hi, lo, Ei, w);
-    const unsigned __int128 ua = (unsigned __int128)(a < 0 ? -a : a);
-    for (int l = 0; l < L; ++l)
-      sd[(l * LT_R + r) * LT_KS + kk] = (int16_t)dev_sym_residue128(ua, a < 0, l);
+    ua[t] = (unsigned __int128)(a < 0 ? -a : a);
+    if (a < 0) negm |= 1u << t;
   }
-  __syncthreads();
-  const int wr = tid / 8, wk = (tid % 8) * 8;
-  const int gi = blockIdx.y * LT_R + wr;
-  for (int q = 0; q < L; ++q) {
-    const int16_t* src = sd + (q * LT_R + wr) * LT_KS + wk;
-    uint4 v;
-    v.x = bf16_bits(src[0]) | (bf16_bits(src[1]) << 16);
-    v.y = bf16_bits(src[2]) | (bf16_bits(src[3]) << 16);
-    v.z = bf16_bits(src[4]) | (bf16_bits(src[5]) << 16);
-    v.w = bf16_bits(src[6]) | (bf16_bits(src[7]) << 16);
-    if (gi < Mp) *reinterpret_cast<uint4*>(planes + ((size_t)q * Mp + gi) * Kp + k0 + wk) = v;
+  const size_t rowoff = (size_t)i * Kp + k0;
+  const size_t pstride = (size_t)Mp * Kp;
+  for (int l = 0; l < L; ++l) {
+    uint32_t h[4];
+#pragma unroll
+    for (int t = 0; t < 8; t += 2) {
+      const int r0 = dev_sym_residue128(ua[t], (negm >> t) & 1u, l);
+      const int r1 = dev_sym_residue128(ua[t + 1], (negm >> (t + 1)) & 1u, l);
+      h[t / 2] = bf16_bits(r0) | (bf16_bits(r1) << 16);
+    }
+    *reinterpret_cast<uint4*>(planes + l * pstride + rowoff) = make_uint4(h[0], h[1], h[2], h[3]);
   }
 }
 
@@ -724,11 +731,8 @@ int dd_prepare(int M, int N, int K, int Mp, int Np, int Kp, int L, int w, const 
   }
   dd_exponents<<<(Mp + 255) / 256, 256, 0, st>>>(Mp, rowmax, E);
   VCPCU_LAUNCH_CHECK("dd_exponents");
-  dim3 g2(Kp / LT_K, Mp / LT_R);
-  const size_t shm = sizeof(int16_t) * (size_t)L * LT_R * LT_KS;
-  VCPCU_CUDA_TRY(
-      cudaFuncSetAttribute(dd_split_left, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-  dd_split_left<<<g2, 256, shm, st>>>(M, K, Mp, Kp, A, lda, L, w, E, planesA);
+  dim3 g2(Kp / 64, Mp / 32);
+  dd_split_left<<<g2, 256, 0, st>>>(M, K, Mp, Kp, A, lda, L, w, E, planesA);
   VCPCU_LAUNCH_CHECK("dd_split_left");
   dd_split_right<<<Np, 256, 0, st>>>(K, N, Kp, Np, B, ldb, L, w, F, planesB, flag);
   VCPCU_LAUNCH_CHECK("dd_split_right");
