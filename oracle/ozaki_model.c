@@ -246,6 +246,7 @@ static const int OZ_MOD[16] = {256, 255, 253, 251, 247, 241, 239, 233,
                                229, 227, 223, 217, 211, 199, 197, 193};
 static int crt_bits(int K, int s) {
   int w = 7 * s;
+  if (w > 62) w = 62; /* |A'|, |B'| <= 2^61 stay 64-bit integers */
   const int Keff = K > 1 ? K : 1;
   for (;;) {
     double need = (2.0 * w - 1.0) + log2((double)Keff) + 0.01, bits = 0.0;
@@ -409,13 +410,18 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
     Fm[j] = oz_exponent(am);
     Fr[j] = oz_exponent(ar);
     int d[OZ_MAXS];
+    uint64_t bhi = 0, blo = 0;
     for (int p = 0; p < k; ++p) {
       if (Fm[j] != OZ_ZERO_EXP && mcol[p] != 0.0) {
         if (!crt) {
           oz_digits(oz_scaled_int(mcol[p], Fm[j], s, 0), s, d);
           for (int q = 0; q < s; ++q) dBm[((size_t)q * n + j) * Kp + p] = (int16_t)d[q];
         } else {
-          Bi[(size_t)j * (k > 0 ? k : 1) + p] = (long long)oz_scaled_int_bits(mcol[p], Fm[j], wbits, 0);
+          const long long bi = (long long)oz_scaled_int_bits(mcol[p], Fm[j], wbits, 0);
+          Bi[(size_t)j * (k > 0 ? k : 1) + p] = bi;
+          const uint64_t ub = (uint64_t)(bi < 0 ? -bi : bi);
+          bhi += ub >> 32;
+          blo += ub & 0xffffffffULL;
         }
         oz_digits(oz_scaled_int(fabs(mcol[p]), Fm[j], sr, 1), sr, d);
         for (int q = 0; q < sr; ++q) dBs[((size_t)q * n + j) * Kp + p] = (int16_t)d[q];
@@ -425,6 +431,13 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
         for (int q = 0; q < sr; ++q) dBr[((size_t)q * n + j) * Kp + p] = (int16_t)d[q];
       }
     }
+    /* CRT form: beta_j = RU((sum_k |B'| + ceil(K/2)) 2^(F - w)) >= sum_k |mB|,
+       since |mB| 2^(w - F) <= |B'| + 1/2 */
+    if (crt)
+      beta[j] = Fm[j] == OZ_ZERO_EXP
+                    ? 0.0
+                    : scale_dir(fma_ru((double)bhi, 0x1p32, (double)(blo + (uint64_t)(k + 1) / 2)),
+                                Fm[j] - wbits, 1);
   }
   pairlist pm, pr;
   build_pairs(s, s, 1, &pm);

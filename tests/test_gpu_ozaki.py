@@ -150,3 +150,59 @@ def test_ozaki_dev_stream(cuda_lib, oracle):
     C = dC.cpu().numpy().reshape(n, ldc, 2)[:, :m, :].ravel()
     ref, _ = oracle.ozaki_igemm(m, n, k, A, B, 7, 2)
     assert np.array_equal(bits(C), bits(ref))
+
+
+def mixed_intervals(rng, rows, cols):
+    """Entries that take every branch of the operand preparation: narrow
+    intervals of either sign (the integer-pipe midrad), adjacent doubles
+    (rounding ties of the midpoint), intervals straddling zero, wide ones,
+    degenerate ones, subnormal and near-overflow endpoints, signed zeros."""
+    n = rows * cols
+    kind = rng.integers(0, 9, n)
+    mid = W.ephi(rng, n, 6)
+    lo = mid - np.abs(mid) * 2.0 ** -40
+    up = mid + np.abs(mid) * 2.0 ** -40
+    adj = kind == 1
+    lo[adj] = mid[adj]
+    up[adj] = np.nextafter(mid[adj], np.inf)
+    st = kind == 2
+    lo[st] = -np.abs(mid[st]) * 0.3
+    up[st] = np.abs(mid[st])
+    wide = kind == 3
+    lo[wide] = np.abs(mid[wide]) * 0.1
+    up[wide] = np.abs(mid[wide]) * 7.0
+    deg = kind == 4
+    lo[deg] = up[deg] = mid[deg]
+    sub = kind == 5
+    lo[sub] = 3e-310
+    up[sub] = 5e-310
+    big = kind == 6
+    lo[big] = np.abs(mid[big]) * 1e290
+    up[big] = np.nextafter(lo[big], np.inf)
+    zer = kind == 7
+    lo[zer] = -0.0
+    up[zer] = 0.0
+    ulps = kind == 8
+    lo[ulps] = mid[ulps]
+    up[ulps] = mid[ulps] + np.abs(mid[ulps]) * 2.0 ** -50
+    out = np.empty(2 * n)
+    out[0::2], out[1::2] = np.minimum(lo, up), np.maximum(lo, up)
+    return out
+
+
+@pytest.mark.parametrize("crt", [True, False], ids=["crt", "slices"])
+def test_ozaki_midrad_paths(cuda_lib, oracle, crt):
+    """Bit-identical to the host model (FP64 midrad) on entries that take the
+    integer-pipe midrad and every fall-back to the FP64 instructions."""
+    rng = np.random.default_rng(17)
+    m, n, k = 70, 60, 400
+    A = mixed_intervals(rng, m, k)
+    B = mixed_intervals(rng, k, n)
+    B[0::2] *= 1e-300   # keep the products of the near-overflow rows finite
+    B[1::2] *= 1e-300
+    form = pidcuda.FORM_OZAKI if crt else pidcuda.FORM_OZAKI_SLICES
+    C = pidcuda.mulmm(A, B, m, n, k, form=form, slices=8)
+    ref, st = oracle.ozaki_igemm(m, n, k, A, B, 8, 2, crt=crt)
+    assert st == 0
+    assert np.array_equal(bits(C), bits(ref))
+    check_contains(oracle, m, n, k, A, B, C)

@@ -197,7 +197,7 @@ int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan, int crt) {
   pb.mplanes = s;
   if (crt) {
     pb.crt = 1;
-    pb.w = 7 * s;
+    pb.w = 7 * s < 62 ? 7 * s : 62;  // |A'|, |B'| <= 2^61 stay 64-bit integers
     const int Keff = pb.K > 1 ? pb.K : 1;
     while (crt_setup(Keff, pb.w, plan) != 0) --pb.w;  // very long K: fewer bits per operand
     pb.mplanes = pb.L;

@@ -106,6 +106,51 @@ OZ_HD __int128 oz_scaled_int_bits(double x, int E, int bits, int up) {
   return neg ? -(__int128)N : (__int128)N;
 }
 
+// The same for bits <= 62 in 64-bit arithmetic (|N| <= 2^(bits-1)).
+OZ_HD long long oz_scaled_int64(double x, int E, int bits, int up) {
+  uint64_t b = oz_bits(x);
+  const int neg = (int)(b >> 63);
+  const int be = (int)((b >> 52) & 0x7ff);
+  uint64_t mant = b & ((1ULL << 52) - 1);
+  if (be == 0 && mant == 0) return 0;
+  int ex;
+  if (be == 0) {
+    ex = -1074;
+  } else {
+    mant |= 1ULL << 52;
+    ex = be - 1075;
+  }
+  const int sh = ex + bits - E;
+  uint64_t N;
+  if (sh >= 0) {
+    N = mant << sh;
+  } else {
+    const int r = -sh;
+    uint64_t q;
+    bool rem_nz, above_half, at_half;
+    if (r >= 64) {
+      q = 0;
+      rem_nz = mant != 0;
+      above_half = false;
+      at_half = false;
+    } else {
+      q = mant >> r;
+      const uint64_t rem = mant & ((1ULL << r) - 1);
+      const uint64_t half = 1ULL << (r - 1);
+      rem_nz = rem != 0;
+      above_half = rem > half;
+      at_half = rem == half;
+    }
+    if (up) {
+      if (!neg && rem_nz) q += 1;
+    } else {
+      if (above_half || (at_half && (q & 1))) q += 1;
+    }
+    N = q;
+  }
+  return neg ? -(long long)N : (long long)N;
+}
+
 // Digit form: x * 2^(8s - E) (s base-256 digits).
 OZ_HD __int128 oz_scaled_int(double x, int E, int s, int up) {
   return oz_scaled_int_bits(x, E, 8 * s, up);

@@ -18,17 +18,9 @@
 #include "common.cuh"
 #include "ozaki.cuh"
 #include "ozaki_common.cuh"
+#include "swfp.cuh"
 
 namespace vcpcu {
-
-__device__ __forceinline__ void oz_midrad(double lo, double up, double& m, double& r) {
-  double s = __dadd_rn(lo, up);
-  if (isfinite(s))
-    m = __dmul_rn(s, 0.5);
-  else
-    m = __dadd_rn(__dmul_rn(lo, 0.5), __dmul_rn(up, 0.5));
-  r = fmax(__dsub_ru(m, lo), __dsub_ru(up, m));
-}
 
 __device__ __forceinline__ unsigned long long dbits(double x) {
   return (unsigned long long)__double_as_longlong(x);
@@ -47,9 +39,8 @@ __device__ __forceinline__ void digits_of(double x, int E, int up, int (&d)[S]) 
     for (int q = 0; q < S; ++q) d[q] = 0;
     return;
   }
-  const __int128 N = oz_scaled_int(x, E, S, up);
   if (S <= 7) {
-    long long n = (long long)N;
+    long long n = oz_scaled_int64(x, E, 8 * S, up);
 #pragma unroll
     for (int p = S - 1; p >= 1; --p) {
       const int lo = (int)((unsigned long long)(n + 128) & 255ULL) - 128;
@@ -58,7 +49,7 @@ __device__ __forceinline__ void digits_of(double x, int E, int up, int (&d)[S]) 
     }
     d[0] = (int)n;
   } else {
-    __int128 n = N;
+    __int128 n = oz_scaled_int(x, E, S, up);
 #pragma unroll
     for (int p = S - 1; p >= 1; --p) {
       const int lo = (int)((unsigned long long)(n + 128) & 255ULL) - 128;
@@ -90,10 +81,9 @@ oz_rowmax_left(int M, int K, const double* __restrict__ A, long lda, int cols_pe
     const int c1 = min(K, c0 + cols_per_block);
     for (int c = c0 + ph; c < c1; c += 8) {
       const double2 e = *reinterpret_cast<const double2*>(A + 2 * (i + (long)c * lda));
-      double m = 0.0, r = 0.0;
-      if (isfinite(e.x) && isfinite(e.y)) {
-        oz_midrad(e.x, e.y, m, r);
-        const double p = __dadd_ru(fabs(m), r);
+      double m = 0.0, r = 0.0, p;
+      if (sw_finite(e.x) && sw_finite(e.y)) {
+        sw_midrad(e.x, e.y, m, r, p);
         am = max(am, dbits(fabs(m)));
         ap = max(ap, dbits(p));
         ar = max(ar, dbits(r));
@@ -155,7 +145,7 @@ oz_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
     if (i < M && k < K) {
       m = mA[i + (long)k * M];
       rr = rA[i + (long)k * M];
-      p = __dadd_ru(fabs(m), rr);
+      p = sw_add_ru_pos(fabs(m), rr);
     }
     digits_of<S>(m, Em, 0, d);
 #pragma unroll
@@ -231,9 +221,9 @@ oz_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
   if (j < N) {
     for (int k = tid; k < K; k += 256) {
       const double2 e = *reinterpret_cast<const double2*>(B + 2 * (k + (long)j * ldb));
-      double m = 0.0, r = 0.0;
-      if (isfinite(e.x) && isfinite(e.y)) {
-        oz_midrad(e.x, e.y, m, r);
+      double m = 0.0, r = 0.0, p;
+      if (sw_finite(e.x) && sw_finite(e.y)) {
+        sw_midrad(e.x, e.y, m, r, p);
         am = max(am, dbits(fabs(m)));
         ar = max(ar, dbits(r));
         bsum = __dadd_ru(bsum, fabs(m));
@@ -340,10 +330,90 @@ __device__ __forceinline__ int dev_sym_residue(unsigned long long a, int neg, in
   return rs;
 }
 
+// Residues on the FP32 pipe (the integer multiply pipe is half as wide).
+// |a| is cut into 12-bit limbs h_t, exact as floats; x = sum_t h_t c_lt with
+// c_lt = 2^(12t) mod m_l < 256 stays below 10 2^20 < 2^24, an exact float;
+// x mod m_l follows from a rounded quotient (off by at most one) and one
+// exact FMA.  The symmetric residue is that of dev_sym_residue, returned as
+// its bf16 bit pattern (|r| <= 128 has at most 8 significant bits).
+constexpr float oz_limb_c(unsigned long long m, int t) {
+  unsigned long long c = 1 % m;
+  for (int i = 0; i < t; ++i) c = (c << 12) % m;
+  return (float)c;
+}
+#define OZ_LIMB_ROW(m)                                                                 \
+  {oz_limb_c(m, 0), oz_limb_c(m, 1), oz_limb_c(m, 2), oz_limb_c(m, 3), oz_limb_c(m, 4), \
+   oz_limb_c(m, 5), oz_limb_c(m, 6), oz_limb_c(m, 7), oz_limb_c(m, 8), oz_limb_c(m, 9)}
+#define OZ_MODF(m) ((float)(m))
+#define OZ_INVF(m) (1.0f / (float)(m))
+__constant__ float c_limbf[OZ_MAX_MODULI][10] = {OZ_MOD_LIST(OZ_LIMB_ROW)};
+__constant__ float c_modf[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_MODF)};
+__constant__ float c_invf[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_INVF)};
+
+// Signed 12-bit limbs of (neg ? -a : a) as exact floats:
+// h_t = sg (2^23 + v_t) - sg 2^23 with sg = -1 or 1.
+template <int NL>
+__device__ __forceinline__ void limbs12(unsigned long long a, bool neg, float (&h)[NL]) {
+  static_assert(NL <= 6, "64-bit magnitudes have at most 6 limbs");
+  const float sg = neg ? -1.0f : 1.0f;
+#pragma unroll
+  for (int t = 0; t < NL; ++t) {
+    const unsigned v = (unsigned)((a >> (12 * t)) & 0xfffULL);
+    h[t] = __fmaf_rn(sg, __uint_as_float(0x4B000000u | v), -8388608.0f * sg);
+  }
+}
+template <int NL>
+__device__ __forceinline__ void limbs12(unsigned __int128 a, bool neg, float (&h)[NL]) {
+  const float sg = neg ? -1.0f : 1.0f;
+#pragma unroll
+  for (int t = 0; t < NL; ++t) {
+    const unsigned v = (unsigned)((a >> (12 * t)) & 0xfffULL);
+    h[t] = __fmaf_rn(sg, __uint_as_float(0x4B000000u | v), -8388608.0f * sg);
+  }
+}
+
+// round to the nearest integer, |v| < 2^22
+__device__ __forceinline__ float rint_small(float v) {
+  return __fsub_rn(__fadd_rn(v, 12582912.0f), 12582912.0f);
+}
+
+// Residue r = x mod m_l with |r| <= m_l / 2 <= 128 of the integer given by
+// its signed limbs: two rounded-quotient steps, all on the FP32 pipe (the
+// first leaves |r0| < m/2 + 2, the second lands in [-m/2, m/2]).
+template <int NL>
+__device__ __forceinline__ float res_sym(const float (&h)[NL], int l) {
+  const float m = c_modf[l], inv = c_invf[l];
+  float x = h[0];
+#pragma unroll
+  for (int t = 1; t < NL; ++t) x = __fmaf_rn(h[t], c_limbf[l][t], x);
+  const float r0 = __fmaf_rn(-rint_small(__fmul_rn(x, inv)), m, x);
+  return __fmaf_rn(-rint_small(__fmul_rn(r0, inv)), m, r0);
+}
+
+// bf16 patterns of two small integers (exact: at most 8 significant bits) in
+// one word, the first in the low half.
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  return __byte_perm(__float_as_uint(a), __float_as_uint(b), 0x7632);
+}
+
+// x * 2^e rounded up (up) or down, in steps that stay in the double range.
+__device__ __forceinline__ double dev_scale_dir(double x, int e, bool up) {
+  while (e > 1023) {
+    x = up ? __dmul_ru(x, 0x1p1023) : __dmul_rd(x, 0x1p1023);
+    e -= 1023;
+  }
+  while (e < -1022) {
+    x = up ? __dmul_ru(x, 0x1p-1022) : __dmul_rd(x, 0x1p-1022);
+    e += 1022;
+  }
+  const double p = __longlong_as_double((long long)(e + 1023) << 52);
+  return up ? __dmul_ru(x, p) : __dmul_rd(x, p);
+}
+
 // w-bit integer of x (|x| <= 2^(E-1)): round to nearest even, |result| <= 2^(w-1).
 __device__ __forceinline__ long long crt_int(double x, int E, int w) {
   if (E == OZ_ZERO_EXP || x == 0.0) return 0;
-  return (long long)oz_scaled_int_bits(x, E, w, 0);
+  return oz_scaled_int64(x, E, w, 0);
 }
 
 // Left factor, CRT form: residues of A' (L planes) + radius digits, and
@@ -351,8 +421,8 @@ __device__ __forceinline__ long long crt_int(double x, int E, int w) {
 // Block: 32 rows x 64 k; lane = row, warp q takes k0 + 8q .. k0 + 8q + 7, so
 // the loads of mA / rA are coalesced across the warp and each lane writes 8
 // bf16 (16 bytes) per plane -- no shared-memory transpose, full occupancy.
-template <int SR>
-__global__ void __launch_bounds__(256)
+template <int SR, int NL>
+__global__ void __launch_bounds__(256, 4)
 oz_split_left_crt(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
                   const double* __restrict__ rA, int L, int w, const int* __restrict__ E3,
                   uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_p,
@@ -366,26 +436,50 @@ oz_split_left_crt(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
     Ep = E3[3 * i + 1];
     Er = E3[3 * i + 2];
   }
-  unsigned long long ua[8];
-  unsigned negm = 0;
-  double pv[8], rv[8];
+  const size_t rowoff = (size_t)i * Kp + k0;
+  const size_t pstride = (size_t)Mp * Kp;
+  long long a[8];
   unsigned long long shi = 0, slo = 0;
+  {
+    // radius digit planes first, so that the doubles die before the residues
+    uint32_t hp[SR][4], hr[SR][4];
+#pragma unroll
+    for (int t = 0; t < 8; t += 2) {
+      int d0[SR], d1[SR], e0[SR], e1[SR];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int k = k0 + t + u;
+        double m = 0.0, r = 0.0, p = 0.0;
+        if (i < M && k < K) {
+          m = mA[i + (long)k * M];
+          r = rA[i + (long)k * M];
+          p = sw_add_ru_pos(fabs(m), r);
+        }
+        a[t + u] = crt_int(m, Em, w);
+        digits_of<SR>(p, Ep, 1, u ? d1 : d0);
+        digits_of<SR>(r, Er, 1, u ? e1 : e0);
+      }
+#pragma unroll
+      for (int q = 0; q < SR; ++q) {
+        hp[q][t / 2] = bf16_bits(d0[q]) | (bf16_bits(d1[q]) << 16);
+        hr[q][t / 2] = bf16_bits(e0[q]) | (bf16_bits(e1[q]) << 16);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < SR; ++q) {
+      *reinterpret_cast<uint4*>(planes_p + q * pstride + rowoff) =
+          make_uint4(hp[q][0], hp[q][1], hp[q][2], hp[q][3]);
+      *reinterpret_cast<uint4*>(planes_r + q * pstride + rowoff) =
+          make_uint4(hr[q][0], hr[q][1], hr[q][2], hr[q][3]);
+    }
+  }
+  float hl[8][NL];
 #pragma unroll
   for (int t = 0; t < 8; ++t) {
-    const int k = k0 + t;
-    double m = 0.0, r = 0.0, p = 0.0;
-    if (i < M && k < K) {
-      m = mA[i + (long)k * M];
-      r = rA[i + (long)k * M];
-      p = __dadd_ru(fabs(m), r);
-    }
-    const long long a = crt_int(m, Em, w);
-    ua[t] = (unsigned long long)(a < 0 ? -a : a);
-    if (a < 0) negm |= 1u << t;
-    pv[t] = p;
-    rv[t] = r;
-    shi += ua[t] >> 32;
-    slo += ua[t] & 0xffffffffULL;
+    const unsigned long long ua = (unsigned long long)(a[t] < 0 ? -a[t] : a[t]);
+    shi += ua >> 32;
+    slo += ua & 0xffffffffULL;
+    limbs12<NL>(ua, a[t] < 0, hl[t]);
   }
   __shared__ unsigned long long red[2][32];
   if (threadIdx.x < 32) red[0][lane] = red[1][lane] = 0;
@@ -397,45 +491,24 @@ oz_split_left_crt(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
     atomicAdd(&asum[2 * i + 0], red[0][lane]);
     atomicAdd(&asum[2 * i + 1], red[1][lane]);
   }
-  const size_t rowoff = (size_t)i * Kp + k0;
-  const size_t pstride = (size_t)Mp * Kp;
-  for (int l = 0; l < L; ++l) {
+#pragma unroll
+  for (int l = 0; l < OZ_MAX_MODULI_128; ++l) {
+    if (l >= L) break;
     uint32_t h[4];
 #pragma unroll
-    for (int t = 0; t < 8; t += 2) {
-      const int r0 = dev_sym_residue(ua[t], (negm >> t) & 1u, l);
-      const int r1 = dev_sym_residue(ua[t + 1], (negm >> (t + 1)) & 1u, l);
-      h[t / 2] = bf16_bits(r0) | (bf16_bits(r1) << 16);
-    }
+    for (int t = 0; t < 8; t += 2) h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
     *reinterpret_cast<uint4*>(planes_m + l * pstride + rowoff) = make_uint4(h[0], h[1], h[2], h[3]);
-  }
-  uint32_t hp[SR][4], hr[SR][4];
-#pragma unroll
-  for (int t = 0; t < 8; t += 2) {
-    int d0[SR], d1[SR], e0[SR], e1[SR];
-    digits_of<SR>(pv[t], Ep, 1, d0);
-    digits_of<SR>(pv[t + 1], Ep, 1, d1);
-    digits_of<SR>(rv[t], Er, 1, e0);
-    digits_of<SR>(rv[t + 1], Er, 1, e1);
-#pragma unroll
-    for (int q = 0; q < SR; ++q) {
-      hp[q][t / 2] = bf16_bits(d0[q]) | (bf16_bits(d1[q]) << 16);
-      hr[q][t / 2] = bf16_bits(e0[q]) | (bf16_bits(e1[q]) << 16);
-    }
-  }
-#pragma unroll
-  for (int q = 0; q < SR; ++q) {
-    *reinterpret_cast<uint4*>(planes_p + q * pstride + rowoff) =
-        make_uint4(hp[q][0], hp[q][1], hp[q][2], hp[q][3]);
-    *reinterpret_cast<uint4*>(planes_r + q * pstride + rowoff) =
-        make_uint4(hr[q][0], hr[q][1], hr[q][2], hr[q][3]);
   }
 }
 
-// Right factor, CRT form: as oz_split_right, with the residues of B' in
-// place of the midpoint digits (one element per thread in pass 2).
-template <int SR>
-__global__ void __launch_bounds__(256)
+// Right factor, CRT form.  One block per column j < Np.  Pass 1 (thread t
+// takes k = t, t+256, ...): midrad into mB, rB (k contiguous) and the column
+// maxima.  Pass 2: B' = round(mB 2^(w - Fm)), its residues, the radius
+// digits, and sum_k |B'| (as >> 32 / & 0xffffffff parts); then
+// beta_j = RU((sum_k |B'| + ceil(K/2)) 2^(Fm - w)) >= sum_k |mB|.  No FP64
+// instruction on the common path (midrad on the integer pipe).
+template <int SR, int NL>
+__global__ void __launch_bounds__(256, 3)
 oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb,
                    int L, int w, double* __restrict__ mBp, double* __restrict__ rBp,
                    uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_r,
@@ -444,23 +517,21 @@ oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, l
   const int j = blockIdx.x;
   const int tid = threadIdx.x;
   __shared__ unsigned long long smax[2];
-  __shared__ double ssum[256];
-  if (tid == 0) smax[0] = smax[1] = 0;
+  __shared__ unsigned long long bs[2];
+  if (tid == 0) smax[0] = smax[1] = bs[0] = bs[1] = 0;
   __syncthreads();
   unsigned long long am = 0, ar = 0;
-  double bsum = 0.0;
   bool bad = false;
   double* mcol = mBp + (size_t)j * Kp;
   double* rcol = rBp + (size_t)j * Kp;
   if (j < N) {
     for (int k = tid; k < K; k += 256) {
       const double2 e = *reinterpret_cast<const double2*>(B + 2 * (k + (long)j * ldb));
-      double m = 0.0, r = 0.0;
-      if (isfinite(e.x) && isfinite(e.y)) {
-        oz_midrad(e.x, e.y, m, r);
+      double m = 0.0, r = 0.0, p;
+      if (sw_finite(e.x) && sw_finite(e.y)) {
+        sw_midrad(e.x, e.y, m, r, p);
         am = max(am, dbits(fabs(m)));
         ar = max(ar, dbits(r));
-        bsum = __dadd_ru(bsum, fabs(m));
       } else {
         bad = true;
       }
@@ -471,36 +542,73 @@ oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, l
   if (bad) atomicOr(flag, 1);
   atomicMax(&smax[0], am);
   atomicMax(&smax[1], ar);
-  ssum[tid] = bsum;
   __syncthreads();
-  for (int wv = 128; wv > 0; wv >>= 1) {
-    if (tid < wv) ssum[tid] = __dadd_ru(ssum[tid], ssum[tid + wv]);
-    __syncthreads();
-  }
   const int Fm = oz_exponent(__longlong_as_double((long long)smax[0]));
   const int Fr = oz_exponent(__longlong_as_double((long long)smax[1]));
   if (tid == 0 && j < N) {
     F2[2 * j + 0] = Fm;
     F2[2 * j + 1] = Fr;
-    beta[j] = ssum[0];
   }
-  int dr[SR];
-  for (int k = tid; k < Kp; k += 256) {
-    double m = 0.0, r = 0.0;
-    if (j < N && k < K) {
-      m = mcol[k];
-      r = rcol[k];
+  // pass 2: thread t takes the 8 consecutive k of 8 (t + 256 it) .. + 7
+  unsigned long long shi = 0, slo = 0;
+  const size_t pstride = (size_t)Np * Kp;
+  for (int k0 = 8 * tid; k0 < Kp; k0 += 8 * 256) {
+    const size_t off = (size_t)j * Kp + k0;
+    float hl[8][NL];
+    uint32_t hr[SR][4], hs[SR][4];
+#pragma unroll
+    for (int t = 0; t < 8; t += 2) {
+      int d0[SR], d1[SR], e0[SR], e1[SR];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int k = k0 + t + u;
+        double m = 0.0, r = 0.0;
+        if (j < N && k < K) {
+          m = mcol[k];
+          r = rcol[k];
+        }
+        const long long b = crt_int(m, Fm, w);
+        const unsigned long long ub = (unsigned long long)(b < 0 ? -b : b);
+        shi += ub >> 32;
+        slo += ub & 0xffffffffULL;
+        limbs12<NL>(ub, b < 0, hl[t + u]);
+        digits_of<SR>(r, Fr, 1, u ? d1 : d0);
+        digits_of<SR>(fabs(m), Fm, 1, u ? e1 : e0);
+      }
+#pragma unroll
+      for (int q = 0; q < SR; ++q) {
+        hr[q][t / 2] = bf16_bits(d0[q]) | (bf16_bits(d1[q]) << 16);
+        hs[q][t / 2] = bf16_bits(e0[q]) | (bf16_bits(e1[q]) << 16);
+      }
     }
-    const long long b = crt_int(m, Fm, w);
-    const unsigned long long ub = (unsigned long long)(b < 0 ? -b : b);
-    for (int l = 0; l < L; ++l)
-      planes_m[((size_t)l * Np + j) * Kp + k] = (uint16_t)bf16_bits(dev_sym_residue(ub, b < 0, l));
-    digits_of<SR>(r, Fr, 1, dr);
 #pragma unroll
-    for (int q = 0; q < SR; ++q) planes_r[((size_t)q * Np + j) * Kp + k] = (uint16_t)bf16_bits(dr[q]);
-    digits_of<SR>(fabs(m), Fm, 1, dr);
+    for (int q = 0; q < SR; ++q) {
+      *reinterpret_cast<uint4*>(planes_r + q * pstride + off) =
+          make_uint4(hr[q][0], hr[q][1], hr[q][2], hr[q][3]);
+      *reinterpret_cast<uint4*>(planes_s + q * pstride + off) =
+          make_uint4(hs[q][0], hs[q][1], hs[q][2], hs[q][3]);
+    }
 #pragma unroll
-    for (int q = 0; q < SR; ++q) planes_s[((size_t)q * Np + j) * Kp + k] = (uint16_t)bf16_bits(dr[q]);
+    for (int l = 0; l < OZ_MAX_MODULI_128; ++l) {
+      if (l >= L) break;
+      uint32_t h[4];
+#pragma unroll
+      for (int t = 0; t < 8; t += 2)
+        h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
+      *reinterpret_cast<uint4*>(planes_m + l * pstride + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    }
+  }
+  atomicAdd(&bs[0], shi);
+  atomicAdd(&bs[1], slo);
+  __syncthreads();
+  if (tid == 0 && j < N) {
+    double bj = 0.0;
+    if (Fm != OZ_ZERO_EXP) {
+      const double v = __fma_ru((double)bs[0], 0x1p32,
+                                (double)(bs[1] + (unsigned long long)(K + 1) / 2));
+      bj = dev_scale_dir(v, Fm - w, true);
+    }
+    beta[j] = bj;
   }
 }
 
@@ -543,13 +651,25 @@ int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, 
   int st_ = VCPCU_OK;
   if (pb.crt) {
     VCPCU_CUDA_TRY(cudaMemsetAsync(ws.asum, 0, sizeof(unsigned long long) * 2 * (size_t)pb.Mp, st));
+    // |A'|, |B'| < 2^(w-1): five 12-bit limbs up to w = 61, six up to 73
     dim3 g2(pb.Kp / 64, pb.Mp / 32);
-    oz_split_left_crt<2><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, pb.L,
-                                             pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r, ws.asum);
-    VCPCU_LAUNCH_CHECK("oz_split_left_crt");
-    oz_split_right_crt<2><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L, pb.w,
-                                                 ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,
-                                                 ws.F2, ws.beta, ws.flag);
+    if (pb.w <= 61) {
+      oz_split_left_crt<2, 5><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA,
+                                                  pb.L, pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r,
+                                                  ws.asum);
+      VCPCU_LAUNCH_CHECK("oz_split_left_crt");
+      oz_split_right_crt<2, 5><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L,
+                                                      pb.w, ws.midB, ws.radB, ws.b_mid, ws.b_r,
+                                                      ws.b_s, ws.F2, ws.beta, ws.flag);
+    } else {
+      oz_split_left_crt<2, 6><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA,
+                                                  pb.L, pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r,
+                                                  ws.asum);
+      VCPCU_LAUNCH_CHECK("oz_split_left_crt");
+      oz_split_right_crt<2, 6><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L,
+                                                      pb.w, ws.midB, ws.radB, ws.b_mid, ws.b_r,
+                                                      ws.b_s, ws.F2, ws.beta, ws.flag);
+    }
     VCPCU_LAUNCH_CHECK("oz_split_right_crt");
     return VCPCU_OK;
   }
@@ -664,14 +784,16 @@ dd_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long l
   }
   const size_t rowoff = (size_t)i * Kp + k0;
   const size_t pstride = (size_t)Mp * Kp;
-  for (int l = 0; l < L; ++l) {
+  float hl[8][10];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) limbs12<10>(ua[t], (negm >> t) & 1u, hl[t]);
+#pragma unroll
+  for (int l = 0; l < OZ_MAX_MODULI; ++l) {
+    if (l >= L) break;
     uint32_t h[4];
 #pragma unroll
-    for (int t = 0; t < 8; t += 2) {
-      const int r0 = dev_sym_residue128(ua[t], (negm >> t) & 1u, l);
-      const int r1 = dev_sym_residue128(ua[t + 1], (negm >> (t + 1)) & 1u, l);
-      h[t / 2] = bf16_bits(r0) | (bf16_bits(r1) << 16);
-    }
+    for (int t = 0; t < 8; t += 2)
+      h[t / 2] = pack_bf16x2(res_sym<10>(hl[t], l), res_sym<10>(hl[t + 1], l));
     *reinterpret_cast<uint4*>(planes + l * pstride + rowoff) = make_uint4(h[0], h[1], h[2], h[3]);
   }
 }
@@ -713,8 +835,13 @@ dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
     }
     const __int128 b = dd_int(hi, lo, Fj, w);
     const unsigned __int128 ub = (unsigned __int128)(b < 0 ? -b : b);
-    for (int l = 0; l < L; ++l)
-      planes[((size_t)l * Np + j) * Kp + k] = (uint16_t)bf16_bits(dev_sym_residue128(ub, b < 0, l));
+    float hb[10];
+    limbs12<10>(ub, b < 0, hb);
+#pragma unroll
+    for (int l = 0; l < OZ_MAX_MODULI; ++l) {
+      if (l >= L) break;
+      planes[((size_t)l * Np + j) * Kp + k] = (uint16_t)(__float_as_uint(res_sym<10>(hb, l)) >> 16);
+    }
   }
 }
 
