@@ -215,8 +215,44 @@ int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan, int crt) {
   const int nchunks = (pb.Kp + OZ_CHUNK - 1) / OZ_CHUNK;
   choose_scaling(plan->mid, nchunks, &plan->t_ref_mid, &plan->R_mid);
   choose_scaling(plan->rad, nchunks, &plan->t_ref_rad, &plan->R_rad);
+  // the folds of a radius product, in the order the epilogue makes them
+  int f = 0;
+  const OzPairList& rl = plan->rad;
+  for (int g = 0; g < rl.ngroups; ++g) {
+    const int total = (rl.gstart[g + 1] - rl.gstart[g]) * nchunks;
+    for (int c = 0; c < total; c += OZ_FOLD_CHUNKS)
+      if (f < OZ_MAX_RAD_SLOTS) plan->rad_sh[f++] = (int8_t)(8 * (plan->t_ref_rad - rl.gt[g]));
+  }
+  plan->rad_slots = f;
   return VCPCU_OK;
 }
+
+OzRadConst oz_rad_const(const OzPlan& plan) {
+  OzRadConst rc;
+  memset(&rc, 0, sizeof(rc));
+  rc.nslot = plan.rad_slots;
+  rc.run1 = !(plan.point_mask & 2);
+  rc.run2 = !(plan.point_mask & 1);
+  rc.t_ref = plan.t_ref_rad;
+  rc.R = plan.R_rad;
+  for (int f = 0; f < plan.rad_slots; ++f) rc.sh[f] = plan.rad_sh[f];
+  return rc;
+}
+
+namespace {
+// folds per radius product of a problem (the count oz_make_plan derives)
+int rad_slot_count(const OzProblem& pb) {
+  OzPairList rl;
+  build_pairs(pb.sr, pb.sr, false, &rl);
+  const int nchunks = (pb.Kp + OZ_CHUNK - 1) / OZ_CHUNK;
+  int f = 0;
+  for (int g = 0; g < rl.ngroups; ++g) {
+    const int total = (rl.gstart[g + 1] - rl.gstart[g]) * nchunks;
+    f += (total + OZ_FOLD_CHUNKS - 1) / OZ_FOLD_CHUNKS;
+  }
+  return f;
+}
+}  // namespace
 
 size_t oz_workspace_bytes(const OzProblem& pb) {
   const size_t np = (size_t)(pb.mplanes + 2 * pb.sr);
@@ -228,8 +264,11 @@ size_t oz_workspace_bytes(const OzProblem& pb) {
   b += al256(sizeof(unsigned long long) * pb.Mp);
   b += al256(sizeof(int) * 2 * pb.Np);
   b += al256(sizeof(double) * pb.Np);
-  b += al256(sizeof(double) * (size_t)pb.Mp * pb.Np);
-  b += al256(sizeof(long long) * (size_t)pb.Mp * pb.Np);
+  if (!pb.crt) {  // T and the midpoint fold buffer: slice form only
+    b += al256(sizeof(double) * (size_t)pb.Mp * pb.Np);
+    b += al256(sizeof(long long) * (size_t)pb.Mp * pb.Np);
+  }
+  b += al256(sizeof(int32_t) * 2 * (size_t)rad_slot_count(pb) * pb.Mp * pb.Np);
   b += al256(sizeof(int) * 4);
   b += 2 * al256(sizeof(double) * (size_t)pb.M * (pb.K > 0 ? pb.K : 1));
   b += 2 * al256(sizeof(double) * (size_t)pb.Np * pb.Kp);
@@ -262,10 +301,16 @@ int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws) {
   p += al256(sizeof(int) * 2 * pb.Np);
   ws->beta = (double*)p;
   p += al256(sizeof(double) * pb.Np);
-  ws->T = (double*)p;
-  p += al256(sizeof(double) * (size_t)pb.Mp * pb.Np);
-  ws->W = (long long*)p;
-  p += al256(sizeof(long long) * (size_t)pb.Mp * pb.Np);
+  ws->T = nullptr;
+  ws->W = nullptr;
+  if (!pb.crt) {
+    ws->T = (double*)p;
+    p += al256(sizeof(double) * (size_t)pb.Mp * pb.Np);
+    ws->W = (long long*)p;
+    p += al256(sizeof(long long) * (size_t)pb.Mp * pb.Np);
+  }
+  ws->P = (int32_t*)p;
+  p += al256(sizeof(int32_t) * 2 * (size_t)rad_slot_count(pb) * pb.Mp * pb.Np);
   ws->flag = (int*)p;
   p += al256(sizeof(int) * 4);
   const size_t mk1 = sizeof(double) * (size_t)pb.M * (pb.K > 0 ? pb.K : 1);
@@ -290,20 +335,19 @@ int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long ld
     PhaseTimer t(0, s);
     if ((st = oz_prepare(plan.pb, A, lda, B, ldb, ws, s))) return st;
   }
-  // T = (|mA| + rA) * rB + rA * |mB|; a product with a zero factor gives
-  // exactly 0 (its exponent is the zero sentinel), so skipping it leaves
-  // every bit of T unchanged
-  const bool rad1 = !(plan.point_mask & 2), rad2 = !(plan.point_mask & 1);
-  if (rad1) {
+  // T = (|mA| + rA) * rB + rA * |mB|: each product leaves its folds in its
+  // half of ws.P.  A product with a zero factor would give exactly 0 (its
+  // exponent is the zero sentinel), so it is skipped; the reassembly (CRT
+  // form) or oz_radius_T (slice form) combines what ran.
+  if (!(plan.point_mask & 2)) {
     PhaseTimer t(1, s);
     if ((st = oz_run_gemm(plan, OZ_RAD_SET, ws, nullptr, 0, s))) return st;
   }
-  if (rad2) {
+  if (!(plan.point_mask & 1)) {
     PhaseTimer t(2, s);
-    if ((st = oz_run_gemm(plan, OZ_RAD_ADD, ws, nullptr, 0, s, rad1 ? 0 : 1))) return st;
+    if ((st = oz_run_gemm(plan, OZ_RAD_ADD, ws, nullptr, 0, s))) return st;
   }
-  if (!rad1 && !rad2)
-    VCPCU_CUDA_TRY(cudaMemsetAsync(ws.T, 0, sizeof(double) * (size_t)plan.pb.Mp * plan.pb.Np, s));
+  if (!plan.pb.crt && (st = oz_radius_T(plan, ws, s))) return st;
   {
     PhaseTimer t(3, s);
     if (plan.pb.crt) {

@@ -36,8 +36,9 @@ struct OzWorkspace {
   uint8_t* res;                       // [L][Np][Mp] CRT form: residues of A'B' mod m_l
   double *midA, *radA;                // [K][M] midpoints / radii of A (column-major)
   double *midB, *radB;                // [Np][Kp] midpoints / radii of B (k contiguous)
-  double* T;                          // [N][Mp] upper bound of the radius product
-  long long* W;                       // [Np][Mp] int64 fold buffer
+  double* T;                          // [N][Mp] upper bound of the radius product (slice form)
+  long long* W;                       // [Np][Mp] int64 fold buffer (slice form)
+  int32_t* P;                         // [2 slots][Np][Mp] folds of the two radius products
   int* flag;                          // [0] non-finite input, [1] device wait timeout
 };
 
@@ -51,6 +52,8 @@ struct OzPairList {
 
 // OZ_RAD_SET: radius product 1, (|mA| + rA) * rB; OZ_RAD_ADD: radius
 // product 2, rA * |mB|.  Each writes T or adds to it (OzGemmArgs::t_set).
+constexpr int OZ_MAX_RAD_SLOTS = 64;  // K <= 2^20: at most 64 folds of 64 chunks per product
+
 enum OzMode { OZ_RAD_SET = 0, OZ_RAD_ADD = 1, OZ_MID = 2, OZ_CRT = 3 };
 
 struct alignas(64) OzGemmArgs {
@@ -76,6 +79,8 @@ struct alignas(64) OzGemmArgs {
   long long timeout_cycles;
   uint8_t* res;                 // OZ_CRT: residue planes [L][Np][Mp]
   int moduli[32];               // OZ_CRT: modulus of group g
+  int32_t* P;                   // radius modes: fold f of a tile -> slot slot0 + f
+  int slot0;
   OzPairList pl;
 };
 
@@ -90,7 +95,24 @@ struct OzPlan {
   // bit 0: A is a point matrix (rA = 0), bit 1: B is (rB = 0).  The radius
   // product with a zero factor is skipped; it would add exactly 0 to T.
   int point_mask = 0;
+  // Folds of one radius product: each is an int32 partial sum of one group,
+  // scaled by 2^rad_sh[f] into W (exact: t_ref_rad is the largest t).
+  int rad_slots;
+  int8_t rad_sh[OZ_MAX_RAD_SLOTS];
 };
+
+// The radius bound T(i, j) from the folds of the two radius products (the
+// same values the radius epilogue would write): passed by value to kernels.
+struct OzRadConst {
+  int nslot;                    // folds per product (slots [0, n) and [n, 2n))
+  int run1, run2;               // which products ran (zero-radius operands skip)
+  int t_ref, R;
+  int8_t sh[OZ_MAX_RAD_SLOTS];
+};
+OzRadConst oz_rad_const(const OzPlan& plan);
+// Slice form: T from the folds into ws.T (the CRT form's reassembly
+// computes it in place).
+int oz_radius_T(const OzPlan& plan, const OzWorkspace& ws, cudaStream_t st);
 
 // crt != 0 selects the CRT form of the midpoint with w = 7 * s integer bits.
 int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan, int crt = 0);

@@ -13,6 +13,7 @@
 #include "common.cuh"
 #include "ozaki.cuh"
 #include "ozaki_common.cuh"
+#include "swfp.cuh"
 
 namespace vcpcu {
 
@@ -204,6 +205,75 @@ __device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const CrtConst
   return 0;
 }
 
+// W of both radius products for 4 consecutive rows (e0 = j Mp + i0): the
+// sums of their folds, exact in int64 (every shift is >= 0).
+__device__ __forceinline__ void rad_folds(const int32_t* __restrict__ P, size_t plane,
+                                          size_t e0, const OzRadConst& rc, long long (&W1)[4],
+                                          long long (&W2)[4]) {
+#pragma unroll
+  for (int u = 0; u < 4; ++u) W1[u] = W2[u] = 0;
+  for (int f = 0; f < rc.nslot; ++f) {
+    const long long m = 1LL << rc.sh[f];
+    if (rc.run1) {
+      const int4 v = *reinterpret_cast<const int4*>(P + (size_t)f * plane + e0);
+      W1[0] += v.x * m;
+      W1[1] += v.y * m;
+      W1[2] += v.z * m;
+      W1[3] += v.w * m;
+    }
+    if (rc.run2) {
+      const int4 v = *reinterpret_cast<const int4*>(P + (size_t)(rc.nslot + f) * plane + e0);
+      W2[0] += v.x * m;
+      W2[1] += v.y * m;
+      W2[2] += v.z * m;
+      W2[3] += v.w * m;
+    }
+  }
+}
+
+// RU((W + R) 2^ex), 0 for a zero row or column: what the radius epilogue of
+// one product writes.
+__device__ __forceinline__ double rad_term(long long W, bool zero, int ex, int R) {
+  double b = 0.0;
+  if (!zero && !sw_i64_scale_ru(W + R, ex, &b)) b = scale_dir2(__ll2double_ru(W + R), ex, true);
+  return b;
+}
+
+// T = RU(RU((|mA| + rA) rB) + RU(rA |mB|)) at (i, j), the products that ran.
+__device__ __forceinline__ double rad_T(long long W1, long long W2, int Ep, int Er, int Fm,
+                                        int Fr, const OzRadConst& rc) {
+  const double b1 = rc.run1 ? rad_term(W1, Ep == OZ_ZERO_EXP || Fr == OZ_ZERO_EXP,
+                                       Ep + Fr - 8 * rc.t_ref, rc.R)
+                            : 0.0;
+  if (!rc.run2) return b1;
+  const double b2 =
+      rad_term(W2, Er == OZ_ZERO_EXP || Fm == OZ_ZERO_EXP, Er + Fm - 8 * rc.t_ref, rc.R);
+  return rc.run1 ? sw_add_ru_pos(b1, b2) : b2;
+}
+
+// Slice form: T (ld Mp) from the folds, before the midpoint product.
+__global__ void __launch_bounds__(256)
+oz_radius_T_kernel(int M, int N, int Mp, size_t plane, const int32_t* __restrict__ P,
+                   const int* __restrict__ E3, const int* __restrict__ F2,
+                   double* __restrict__ T, const __grid_constant__ OzRadConst rc) {
+  const int Mq = (M + 3) >> 2;
+  const long total = (long)Mq * N;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    const int i0 = 4 * (int)(idx % Mq), j = (int)(idx / Mq);
+    const size_t e0 = (size_t)j * Mp + i0;
+    long long W1[4], W2[4];
+    rad_folds(P, plane, e0, rc, W1, W2);
+    const int Fm = F2[2 * j], Fr = F2[2 * j + 1];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u;
+      if (i >= M) break;
+      T[e0 + u] = rad_T(W1[u], W2[u], E3[3 * i + 1], E3[3 * i + 2], Fm, Fr, rc);
+    }
+  }
+}
+
 // One thread per 4 consecutive rows of one column: the residue planes are
 // read 4 bytes at a time, T 32 bytes, C written as 4 consecutive pairs.  Only the final
 // error sum and the two outward roundings use the FP64 pipe.
@@ -211,9 +281,9 @@ __global__ void __launch_bounds__(256)
 oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __restrict__ res,
                        size_t plane, const int* __restrict__ E3, const int* __restrict__ F2,
                        const unsigned long long* __restrict__ asum,
-                       const double* __restrict__ beta, const double* __restrict__ T,
+                       const double* __restrict__ beta, const int32_t* __restrict__ P,
                        double* __restrict__ C, long ldc, const int* __restrict__ flag,
-                       const __grid_constant__ CrtConst cc) {
+                       const __grid_constant__ CrtConst cc, const __grid_constant__ OzRadConst rc) {
   const bool nonfinite = flag[0] != 0 || flag[1] != 0;
   const int Mq = (M + 3) >> 2;
   const long total = (long)Mq * N;
@@ -221,14 +291,14 @@ oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __rest
        idx += (long)gridDim.x * blockDim.x) {
     const int i0 = 4 * (int)(idx % Mq), j = (int)(idx / Mq);
     const size_t e0 = (size_t)j * Mp + i0;
-    const int Fj = F2[2 * j];
+    const int Fj = F2[2 * j], Frj = F2[2 * j + 1];
     const double bj = beta[j];
     uint32_t pk[16];
 #pragma unroll
     for (int l = 0; l < 16; ++l)
       pk[l] = l < L ? *reinterpret_cast<const uint32_t*>(res + (size_t)l * plane + e0) : 0u;
-    const double4 Tv = *reinterpret_cast<const double4*>(T + e0);
-    const double Ta[4] = {Tv.x, Tv.y, Tv.z, Tv.w};
+    long long W1[4], W2[4];
+    rad_folds(P, plane, e0, rc, W1, W2);
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int i = i0 + u;
@@ -260,7 +330,8 @@ oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __rest
         const double t2 = scale_pow2(sA, Ei + Fj - 2 * w - 1, true);
         tr = __dadd_ru(t1, t2);
       }
-      const double err = __dadd_ru(tr, Ta[u]);
+      const double Tu = rad_T(W1[u], W2[u], E3[3 * i + 1], E3[3 * i + 2], Fj, Frj, rc);
+      const double err = __dadd_ru(tr, Tu);
       double clo = __dsub_rd(lo, err), cup = __dadd_ru(up, err);
       if (nonfinite) clo = cup = __longlong_as_double(0x7ff8000000000000LL);
       double* cp = C + 2 * ((size_t)i + (size_t)j * ldc);  // C may be only 8-byte aligned
@@ -289,8 +360,20 @@ int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long l
   if (blocks < 1) blocks = 1;
   oz_crt_assemble_kernel<<<(int)blocks, 256, 0, st>>>(
       pb.M, pb.N, pb.Mp, pb.L, pb.w, ws.res, (size_t)pb.Np * pb.Mp, ws.E3, ws.F2, ws.asum,
-      ws.beta, ws.T, C, ldc, ws.flag, cc);
+      ws.beta, ws.P, C, ldc, ws.flag, cc, oz_rad_const(plan));
   VCPCU_LAUNCH_CHECK("oz_crt_assemble_kernel");
+  return VCPCU_OK;
+}
+
+int oz_radius_T(const OzPlan& plan, const OzWorkspace& ws, cudaStream_t st) {
+  const OzProblem& pb = plan.pb;
+  const long total = (long)((pb.M + 3) / 4) * pb.N;
+  long blocks = (total + 255) / 256;
+  if (blocks > 152L * 64) blocks = 152L * 64;
+  if (blocks < 1) blocks = 1;
+  oz_radius_T_kernel<<<(int)blocks, 256, 0, st>>>(pb.M, pb.N, pb.Mp, (size_t)pb.Np * pb.Mp, ws.P,
+                                                  ws.E3, ws.F2, ws.T, oz_rad_const(plan));
+  VCPCU_LAUNCH_CHECK("oz_radius_T_kernel");
   return VCPCU_OK;
 }
 

@@ -28,6 +28,7 @@
 #include "common.cuh"
 #include "ozaki.cuh"
 #include "ozaki_common.cuh"
+#include "swfp.cuh"
 #include "tc_ptx.cuh"
 
 namespace vcpcu {
@@ -232,6 +233,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
       const int gi = tm * OZ_BM + row_in_tile;
       const int gj0 = tn * OZ_BN + half * 128;
       bool have_w = false;
+      int fold = 0;  // radius modes: folds of this tile so far (slot index)
       for (int g = 0; g < args.pl.ngroups && ok; ++g) {
         const int t = args.pl.gt[g];
         const int sh = 8 * (args.t_ref - t);
@@ -286,6 +288,17 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
               c[e] = 0;
             }
             cnt = 0;
+          } else if ((cnt == OZ_FOLD_CHUNKS || last_of_group) && args.mode != OZ_MID) {
+            // radius modes: the fold is stored, never read back here -- the
+            // reassembly combines the slots (no load stalls the drain)
+            int32_t* pp = args.P + ((size_t)(args.slot0 + fold) * args.Np + gj0) * args.Mp + gi;
+#pragma unroll
+            for (int e = 0; e < 128; ++e) {
+              pp[(size_t)e * args.Mp] = c[e];
+              c[e] = 0;
+            }
+            ++fold;
+            cnt = 0;
           } else if (cnt == OZ_FOLD_CHUNKS || last_of_group) {
             // fold into W (global, column-major, ld = Mp); the first fold of
             // a tile stores, later folds add
@@ -302,7 +315,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
         }
       }
       if (!ok) break;
-      if (args.mode == OZ_CRT) continue;  // reassembled by oz_crt_assemble
+      if (args.mode != OZ_MID) continue;  // CRT residues / radius folds: combined later
       // ------------------------------------------------------ final epilogue
       const int Ei = (gi < args.M) ? args.Erow[(size_t)args.erow_stride * gi] : OZ_ZERO_EXP;
       double dlt = 0.0;
@@ -316,10 +329,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
           const bool zero = (Ei == OZ_ZERO_EXP) || (Fj == OZ_ZERO_EXP);
           const int ex = Ei + Fj - 8 * args.t_ref;
           double* Tp = args.T + (size_t)gj * args.Mp + gi;
-          if (args.mode == OZ_RAD_SET || args.mode == OZ_RAD_ADD) {
-            const double b = zero ? 0.0 : scale_dir(__ll2double_ru(v + args.R), ex, true);
-            *Tp = args.t_set ? b : __dadd_ru(*Tp, b);
-          } else {
+          {
             double mlo = 0.0, mup = 0.0, tr = 0.0;
             if (!zero) {
               mlo = scale_dir(__ll2double_rd(v), ex, false);
@@ -452,6 +462,8 @@ int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, 
   a.beta = ws.beta;
   a.W = ws.W;
   a.T = ws.T;
+  a.P = ws.P;
+  a.slot0 = mode == OZ_RAD_ADD ? plan.rad_slots : 0;
   a.C = C;
   a.ldc = ldc;
   a.flag = ws.flag;

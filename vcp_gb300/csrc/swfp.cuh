@@ -166,4 +166,22 @@ __device__ __forceinline__ double sw_add_ru_pos(double a, double b) {
   return sw_double(((unsigned long long)B << 52) | (M & (H - 1)));
 }
 
+// RU(v * 2^ex) for an int64 v >= 0 built on the integer pipe (equal to
+// RU-scaling of __ll2double_ru(v)); false when the result is not normal or
+// v < 0.
+__device__ __forceinline__ bool sw_i64_scale_ru(long long v, int ex, double* out) {
+  if (v <= 0) {
+    *out = 0.0;
+    return v == 0;
+  }
+  const unsigned long long t = (unsigned long long)v;
+  const int lz = __clzll(t);
+  const unsigned long long tn = t << lz;
+  const int be = 1023 + 63 - lz + ex;
+  if (be < 1 || be > 2046) return false;
+  *out = sw_double(((unsigned long long)be << 52) + ((tn >> 11) & ((1ULL << 52) - 1)) +
+                   ((tn & 0x7ffULL) ? 1ULL : 0ULL));
+  return true;
+}
+
 }  // namespace vcpcu
