@@ -275,8 +275,9 @@ oz_radius_T_kernel(int M, int N, int Mp, size_t plane, const int32_t* __restrict
 }
 
 // One thread per 4 consecutive rows of one column: the residue planes are
-// read 4 bytes at a time, T 32 bytes, C written as 4 consecutive pairs.  Only the final
-// error sum and the two outward roundings use the FP64 pipe.
+// read 4 bytes at a time, the radius folds 16 bytes, C written as 4
+// consecutive pairs.  Only the final error sum and the two outward roundings
+// use the FP64 pipe on the common path.
 __global__ void __launch_bounds__(256)
 oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __restrict__ res,
                        size_t plane, const int* __restrict__ E3, const int* __restrict__ F2,

@@ -88,6 +88,25 @@ __device__ __forceinline__ void tile_coords(int tile, int tiles_m, int tiles_n, 
   tm = g * OZ_RASTER + idx % rows;
 }
 
+// Work items.  MID (slice form): one item per tile, all groups (the groups
+// accumulate into one W).  CRT and radius modes: one item per (group, tile),
+// group-major -- every group writes its own residue plane or fold slots, so
+// items are independent, and the CTAs in flight share one group's planes
+// (compact L2 working set; the tail is one group of one tile).
+__device__ __forceinline__ void item_coords(const OzGemmArgs& a, int item, int ntiles, int& tm,
+                                            int& tn, int& g0, int& g1) {
+  int tile = item;
+  if (a.mode == OZ_MID) {
+    g0 = 0;
+    g1 = a.pl.ngroups;
+  } else {
+    g0 = item / ntiles;
+    g1 = g0 + 1;
+    tile = item - g0 * ntiles;
+  }
+  tile_coords(tile, a.tiles_m, a.tiles_n, tm, tn);
+}
+
 __device__ __forceinline__ long long shift_t(int c, int sh) {
   const long long v = (long long)c;
   return sh >= 0 ? (v << sh) : (v >> (-sh));
@@ -101,6 +120,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = args.tiles_m * args.tiles_n;
+  const int nitems = args.mode == OZ_MID ? ntiles : ntiles * args.pl.ngroups;
   const int nchunks = (args.Kp + OZ_CHUNK - 1) / OZ_CHUNK;
   const int kblocks = args.Kp / OZ_BK;
   const long long lim = args.timeout_cycles;
@@ -136,10 +156,10 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
       uint32_t phase = 0;
       bool ok = true;
       uint32_t used = 0, lastpar = 0;  // per-stage bit masks
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        int tm, tn;
-        tile_coords(tile, args.tiles_m, args.tiles_n, tm, tn);
-        for (int pi = 0; pi < args.pl.npairs && ok; ++pi) {
+      for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+        int tm, tn, g0, g1;
+        item_coords(args, item, ntiles, tm, tn, g0, g1);
+        for (int pi = args.pl.gstart[g0]; pi < args.pl.gstart[g1] && ok; ++pi) {
           const int pa = args.pl.pa[pi], pb = args.pl.pb[pi];
           for (int kb = 0; kb < kblocks; ++kb) {
             if (*(volatile int*)&sm.abort || !ptx::mbar_wait(&sm.empty[stage], phase ^ 1, lim)) {
@@ -173,8 +193,10 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
       uint32_t phase = 0;
       uint32_t acc = 0;  // global chunk counter
       bool ok = true;
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        for (int pi = 0; pi < args.pl.npairs && ok; ++pi) {
+      for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+        int tm, tn, g0, g1;
+        item_coords(args, item, ntiles, tm, tn, g0, g1);
+        for (int pi = args.pl.gstart[g0]; pi < args.pl.gstart[g1] && ok; ++pi) {
           for (int ch = 0; ch < nchunks && ok; ++ch, ++acc) {
             const int buf = acc & 1;
             const uint32_t par = (acc >> 1) & 1;
@@ -227,14 +249,18 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
     uint32_t acc = 0;
     bool ok = true;
     bool nonfinite = args.flag[0] != 0;
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-      int tm, tn;
-        tile_coords(tile, args.tiles_m, args.tiles_n, tm, tn);
+    for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
+      int tm, tn, g0, g1;
+      item_coords(args, item, ntiles, tm, tn, g0, g1);
       const int gi = tm * OZ_BM + row_in_tile;
       const int gj0 = tn * OZ_BN + half * 128;
       bool have_w = false;
-      int fold = 0;  // radius modes: folds of this tile so far (slot index)
-      for (int g = 0; g < args.pl.ngroups && ok; ++g) {
+      // radius modes: slot of the next fold = folds of the earlier groups
+      int fold = 0;
+      for (int g = 0; g < g0; ++g)
+        fold += ((args.pl.gstart[g + 1] - args.pl.gstart[g]) * nchunks + OZ_FOLD_CHUNKS - 1) /
+                OZ_FOLD_CHUNKS;
+      for (int g = g0; g < g1 && ok; ++g) {
         const int t = args.pl.gt[g];
         const int sh = 8 * (args.t_ref - t);
         const int npg = args.pl.gstart[g + 1] - args.pl.gstart[g];
@@ -469,7 +495,8 @@ int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, 
   a.flag = ws.flag;
   a.timeout_cycles = 4000000000LL;  // about 2 s at 2 GHz
   const int ntiles = a.tiles_m * a.tiles_n;
-  const int grid = ntiles < num_sms() ? ntiles : num_sms();
+  const int nitems = mode == OZ_MID ? ntiles : ntiles * a.pl.ngroups;
+  const int grid = nitems < num_sms() ? nitems : num_sms();
   oz_slice_gemm_kernel<<<grid, NTHREADS, oz_dyn_smem(), st>>>(a);
   VCPCU_LAUNCH_CHECK("oz_slice_gemm_kernel");
   return VCPCU_OK;
