@@ -5,6 +5,7 @@
 //     C = A * B;                  // pidcuda::mulmm        (pidblas.hpp:239)
 //     C = ltransmul(A);           // pidcuda::mulltmm      (pidblas.hpp:296)
 //     x = lss(A, b);              // imats::linearsolve -> mul_im_m / mul_m_im
+//     vcp::matrix< kv::interval<double>, vcp::pidcuda_fma > F;  // pidblas_fma drop-in
 // The class derives from vcp::imats<double, vcp::pdblas> as pidblas does, so
 // every imats algorithm (linearsolve, eigsym, eigsymge) routes its interval
 // products through the hooks below to libvcpcuda (include/vcpcuda.h).
@@ -141,6 +142,29 @@ class pidcuda : public vcp::imats<double, vcp::pdblas> {
         vcpcu_isyrk(this->column, this->row, pidcuda_detail::cd(this->v), pidcuda_detail::md(c.v),
                     pidcuda_settings::form(), pidcuda_settings::slices()),
         "pidcuda::mulltmm");
+  }
+};
+
+// vcp::pidcuda_fma -- the GPU drop-in for vcp::pidblas_fma
+// (vcp/pidblas_fma.hpp:43-80): pidcuda with the interval product replaced by
+// the inf-sup ifma chain (vcpcu_igemm_fma), bit-identical to pidblas_fma's
+// loop; the other hooks stay those of pidcuda.
+class pidcuda_fma : public pidcuda {
+ public:
+  void mulmm(const vcp::mats<kv::interval<double> >& B,
+             vcp::mats<kv::interval<double> >& c) const override {
+    if (this->type == 'S' || B.type == 'S') {
+      pidcuda::mulmm(B, c);
+      return;
+    }
+    if (this->column != B.row)
+      vcp::throw_error<vcp::dimension_error>("pidcuda_fma::mulmm: (", this->row, ", ",
+                                             this->column, ") * (", B.row, ", ", B.column, ")");
+    c.zeros(this->row, B.column);
+    pidcuda_detail::check(vcpcu_igemm_fma(this->row, B.column, this->column,
+                                          pidcuda_detail::cd(this->v), pidcuda_detail::cd(B.v),
+                                          pidcuda_detail::md(c.v)),
+                          "pidcuda_fma::mulmm");
   }
 };
 

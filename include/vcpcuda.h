@@ -200,6 +200,27 @@ int vcpcu_norm_I_minus_RA_dev(int n, const double* R, int ldr, const double* A,
 int vcpcu_norm_I_minus_RA(int n, const double* R, const double* A, double* bound,
                           int form, int slices);
 
+/* ---- inf-sup interval FMA (vcp/ifma.hpp, vcp/pidblas_fma.hpp) ------------- */
+
+/* Replaces vcp::ifma (vcp/ifma.hpp:48-139), elementwise over kv pairs:
+ *   R[i] = ifma(A[i], B[i], C[i]) encloses {x y + z : x in A[i], y in B[i],
+ *   z in C[i]}, with the sign-case selection and directed fused
+ *   multiply-adds of the reference's portable branch (bit-identical).
+ * R may alias C.  Finite inputs.  A, B 16-byte aligned (_dev form). */
+int vcpcu_ifma_dev(long count, const double* A, const double* B, const double* C,
+                   double* R, void* stream);
+int vcpcu_ifma(long count, const double* A, const double* B, const double* C,
+               double* R);
+
+/* Replaces vcp::pidblas_fma::mulmm (vcp/pidblas_fma.hpp:46-80):
+ * C = [A] [B] (kv layout, A m x k, B k x n, C m x n) with every entry the
+ * ifma chain over the inner index in ascending order from [0, 0] --
+ * bit-identical to the reference loop; FP64 pipe (2 to 4 directed FMAs per
+ * inner step).  A, B 16-byte aligned (_dev form). */
+int vcpcu_igemm_fma_dev(int m, int n, int k, const double* A, int lda,
+                        const double* B, int ldb, double* C, int ldc, void* stream);
+int vcpcu_igemm_fma(int m, int n, int k, const double* A, const double* B, double* C);
+
 /* ---- autotuner ------------------------------------------------------------- */
 
 /* VCPCU_FORM_AUTO runs, per product, the form with the smaller predicted

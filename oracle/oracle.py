@@ -32,6 +32,8 @@ def lib() -> C.CDLL:
         L.orc_exact_hull.argtypes = [_i, _i, _i, _v, _v, _l, _v, _v, _v, _v, _i]
         L.orc_exact_dot.argtypes = [_i, _i, _i, _v, _v, _l, _v, _v, _v, _v, _i]
         L.orc_exact_sum.argtypes = [_l, _v, _i]
+        L.orc_ifma.argtypes = [_l, _v, _v, _v, _v]
+        L.orc_pidblas_fma_mulmm.argtypes = [_i, _i, _i, _v, _v, _v, _i]
         L.orc_dd_residual.argtypes = [_i, _i, _i, _v, _v, _v, _l, _v, _v, _v, _v, _i]
         L.orc_exact_sum.restype = C.c_double
         L.orc_ozaki_igemm.argtypes = [_i, _i, _i, _v, _v, _v, _i, _i]
@@ -65,6 +67,9 @@ def ref_lib() -> C.CDLL | None:
         R.ref_pidblas_vmulmm.argtypes = [_i, _i, _v, _v]
         R.ref_pidblas_vmulmm.restype = _i
         R.ref_norm_I_minus_RA.argtypes = [_i, _v, _v, _v]
+        R.ref_ifma.argtypes = [_l, _v, _v, _v, _v]
+        R.ref_pidblas_fma_mulmm.argtypes = [_i, _i, _i, _v, _v, _v]
+        R.ref_pidblas_fma_mulmm.restype = _i
         R.ref_norm_I_minus_RA.restype = _i
         _ref = R
     return _ref
@@ -163,6 +168,21 @@ def pidblas_vmulmm(n, k, A, threads=0):
 
 def norm_I_minus_RA(n, R, A, threads=0) -> float:
     return float(lib().orc_norm_I_minus_RA(n, _p(R), _p(A), threads))
+
+
+def ifma(A, B, C_) -> np.ndarray:
+    """vcp::ifma elementwise over kv buffers (restatement)."""
+    n = A.size // 2
+    R = np.empty(2 * n)
+    lib().orc_ifma(n, _p(A), _p(B), _p(C_), _p(R))
+    return R
+
+
+def pidblas_fma_mulmm(m, n, k, A, B, threads=0) -> np.ndarray:
+    """vcp::pidblas_fma::mulmm (restatement), kv buffers, GEMM naming."""
+    C_ = np.empty(2 * m * n)
+    lib().orc_pidblas_fma_mulmm(m, n, k, _p(A), _p(B), _p(C_), int(threads))
+    return C_
 
 
 def ref_call(name, *args):

@@ -21,6 +21,8 @@
 #include <kv/interval.hpp>
 #include <kv/hwround.hpp>
 #include <vcp/pidblas.hpp>
+#include <vcp/pidblas_fma.hpp>
+#include <vcp/ifma.hpp>
 #include <vcp/matrix.hpp>
 
 namespace {
@@ -210,6 +212,37 @@ int ref_norm_I_minus_RA(int n, const double* R, const double* A, double* bound) 
     vcp::mats<I> g;
     b.norminf(g);
     *bound = g.v[0].upper();
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// vcp::ifma (vcp/ifma.hpp, the portable branch: VCP_USE_AVX512 undefined),
+// elementwise over kv pairs.
+void ref_ifma(long count, const double* A, const double* B, const double* C, double* R) {
+  for (long i = 0; i < count; ++i) {
+    double ru, rd;
+    vcp::ifma(A[2 * i + 1], A[2 * i], B[2 * i + 1], B[2 * i], C[2 * i + 1], C[2 * i], ru, rd);
+    R[2 * i] = rd;
+    R[2 * i + 1] = ru;
+  }
+}
+
+// C = A * B through vcp::matrix<kv::interval<double>, vcp::pidblas_fma>
+// (pidblas_fma::mulmm, vcp/pidblas_fma.hpp:46-80).  GEMM naming, kv layout.
+int ref_pidblas_fma_mulmm(int m, int n, int k, const double* A, const double* B, double* C) {
+  try {
+    vcp::matrix<I, vcp::pidblas_fma> a, b, c;
+    a.zeros(m, k);
+    b.zeros(k, n);
+    for (long i = 0; i < (long)m * k; ++i) a.data()[i] = I(A[2 * i], A[2 * i + 1]);
+    for (long i = 0; i < (long)k * n; ++i) b.data()[i] = I(B[2 * i], B[2 * i + 1]);
+    c = a * b;
+    for (long i = 0; i < (long)m * n; ++i) {
+      C[2 * i] = c.data()[i].lower();
+      C[2 * i + 1] = c.data()[i].upper();
+    }
     return 0;
   } catch (...) {
     return 1;

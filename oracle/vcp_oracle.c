@@ -637,3 +637,99 @@ double orc_norm_I_minus_RA(int n, const double* R, const double* A, int nthreads
   free(b);
   return g;
 }
+
+/* ---------------------------------------------------------------------------
+ * vcp::ifma (vcp/ifma.hpp:48-139, the portable branch) and the product of
+ * vcp::pidblas_fma::mulmm (vcp/pidblas_fma.hpp:46-80) built on it.
+ * ------------------------------------------------------------------------- */
+static double fma_dir(double a, double b, double c, int mode) {
+  volatile double x = a, y = b, z = c;
+  fesetround(mode);
+  volatile double r = fma(x, y, z);
+  fesetround(FE_TONEAREST);
+  return r;
+}
+
+/* [rd, ru] = [ad, au] * [bd, bu] + [cd, cu]: the reference's sign cases. */
+static void ifma_c(double au, double ad, double bu, double bd, double cu, double cd,
+                   double* ru, double* rd) {
+  double u = 0.0, d = 0.0, t;
+  if (ad >= 0) {
+    if (bd >= 0) {
+      u = fma_dir(au, bu, cu, FE_UPWARD);
+      d = fma_dir(ad, bd, cd, FE_DOWNWARD);
+    } else if (bd <= 0 && bu >= 0) {
+      u = fma_dir(au, bu, cu, FE_UPWARD);
+      d = fma_dir(au, bd, cd, FE_DOWNWARD);
+    } else if (bu <= 0) {
+      u = fma_dir(ad, bu, cu, FE_UPWARD);
+      d = fma_dir(au, bd, cd, FE_DOWNWARD);
+    }
+  } else if (ad <= 0 && au >= 0) {
+    if (bd >= 0) {
+      u = fma_dir(au, bu, cu, FE_UPWARD);
+      d = fma_dir(ad, bu, cd, FE_DOWNWARD);
+    } else if (bd <= 0 && bu >= 0) {
+      t = fma_dir(au, bu, cu, FE_UPWARD);
+      u = fma_dir(ad, bd, cu, FE_UPWARD);
+      if (u < t) u = t;
+      t = fma_dir(au, bd, cd, FE_DOWNWARD);
+      d = fma_dir(ad, bu, cd, FE_DOWNWARD);
+      if (d > t) d = t;
+    } else if (bu <= 0) {
+      u = fma_dir(ad, bd, cu, FE_UPWARD);
+      d = fma_dir(au, bd, cd, FE_DOWNWARD);
+    }
+  } else if (au <= 0) {
+    if (bd >= 0) {
+      u = fma_dir(au, bd, cu, FE_UPWARD);
+      d = fma_dir(ad, bu, cd, FE_DOWNWARD);
+    } else if (bd <= 0 && bu >= 0) {
+      u = fma_dir(ad, bd, cu, FE_UPWARD);
+      d = fma_dir(ad, bu, cd, FE_DOWNWARD);
+    } else if (bu <= 0) {
+      u = fma_dir(ad, bd, cu, FE_UPWARD);
+      d = fma_dir(au, bu, cd, FE_DOWNWARD);
+    }
+  }
+  *ru = u;
+  *rd = d;
+}
+
+void orc_ifma(long count, const double* A, const double* B, const double* C, double* R) {
+  for (long i = 0; i < count; ++i) {
+    double ru, rd;
+    ifma_c(A[2 * i + 1], A[2 * i], B[2 * i + 1], B[2 * i], C[2 * i + 1], C[2 * i], &ru, &rd);
+    R[2 * i] = rd;
+    R[2 * i + 1] = ru;
+  }
+}
+
+/* C (m x n) = fold of ifma over p = 0..k-1 from [0, 0] (the loop order of
+ * pidblas_fma::mulmm: column of C, inner index, row). */
+int orc_pidblas_fma_mulmm(int m, int n, int k, const double* A, const double* B, double* C,
+                          int nthreads) {
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+  for (int j = 0; j < n; ++j) {
+    for (int i = 0; i < m; ++i) {
+      C[2 * ((long)i + (long)j * m)] = 0.0;
+      C[2 * ((long)i + (long)j * m) + 1] = 0.0;
+    }
+    for (int p = 0; p < k; ++p) {
+      for (int i = 0; i < m; ++i) {
+        const double* a = A + 2 * ((long)i + (long)p * m);
+        const double* b = B + 2 * ((long)p + (long)j * k);
+        double* c = C + 2 * ((long)i + (long)j * m);
+        double ru, rd;
+        ifma_c(a[1], a[0], b[1], b[0], c[1], c[0], &ru, &rd);
+        c[0] = rd;
+        c[1] = ru;
+      }
+    }
+  }
+  (void)nthreads;
+  return 0;
+}

@@ -27,6 +27,25 @@ from vcp_gb300 import workloads as W  # noqa: E402
 OUT = Path(__file__).resolve().parent / "golden.npz"
 
 
+def mixed_intervals(rng, n: int) -> np.ndarray:
+    """kv buffer of n intervals of every sign case of vcp::ifma: positive,
+    negative, straddling zero, [0, 0] and [0, x]."""
+    a = rng.standard_normal(n)
+    b = rng.standard_normal(n)
+    lo, up = np.minimum(a, b), np.maximum(a, b)
+    kind = rng.integers(0, 4, n)
+    pos, neg, zer = kind == 1, kind == 2, kind == 3
+    lo[pos] = np.abs(lo[pos])
+    up[pos] = lo[pos] + np.abs(up[pos])
+    up[neg] = -np.abs(up[neg])
+    lo[neg] = up[neg] - np.abs(lo[neg])
+    lo[zer] = 0.0
+    up[zer] = np.where(rng.random(int(zer.sum())) < 0.5, 0.0, np.abs(up[zer]))
+    out = np.empty(2 * n)
+    out[0::2], out[1::2] = lo, up
+    return out
+
+
 def main() -> None:
     if build_reference() is None:
         raise SystemExit("reference sources not mounted; cannot regenerate golden vectors")
@@ -81,6 +100,23 @@ def main() -> None:
         data[f"nm{idx}_n"] = np.array([nn])
         data[f"nm{idx}_R"], data[f"nm{idx}_A"] = Rinv, Ai
         data[f"nm{idx}_bound"] = np.array([g.value])
+    # vcp::ifma elementwise and vcp::pidblas_fma::mulmm (own seed, so the
+    # vectors above stay as they were)
+    rng2 = np.random.default_rng(20261204)
+    n_if = 4096
+    A, B, Cc = (mixed_intervals(rng2, n_if) for _ in range(3))
+    R = np.empty(2 * n_if)
+    O.ref_lib().ref_ifma(n_if, O._p(A), O._p(B), O._p(Cc), O._p(R))
+    data["if_A"], data["if_B"], data["if_C"], data["if_R"] = A, B, Cc, R
+    fcases = [(5, 4, 6), (33, 17, 40), (64, 64, 20)]
+    for idx, (m, n, k) in enumerate(fcases):
+        A = mixed_intervals(rng2, m * k)
+        B = mixed_intervals(rng2, k * n)
+        C_ = np.empty(2 * m * n)
+        assert O.ref_lib().ref_pidblas_fma_mulmm(m, n, k, O._p(A), O._p(B), O._p(C_)) == 0
+        data[f"fm{idx}_shape"] = np.array([m, n, k])
+        data[f"fm{idx}_A"], data[f"fm{idx}_B"], data[f"fm{idx}_C"] = A, B, C_
+    data["n_fm"] = np.array([len(fcases)])
     data["n_mp"] = np.array([len(pcases)])
     data["n_sy"] = np.array([2])
     data["n_nm"] = np.array([2])

@@ -210,3 +210,40 @@ def test_dd_residual_known_answers(oracle):
     B2 = np.array([1.0, 0.0, -1.0, 0.0])
     err, ab = oracle.dd_residual(1, 1, 2, A2, B2, np.array([0.0, 0.0]), rows, cols)
     assert ab[0] == 2.0 ** -70 and err[0] == 2.0 ** -70
+
+
+def test_ifma_oracle_golden(oracle):
+    """The C restatement of vcp::ifma and pidblas_fma::mulmm reproduces the
+    reference's outputs (golden vectors made by the reference build)."""
+    import numpy as np
+    from pathlib import Path
+    g = np.load(Path(__file__).resolve().parent / "golden" / "golden.npz")
+    R = oracle.ifma(g["if_A"], g["if_B"], g["if_C"])
+    assert np.array_equal(R.view(np.int64), g["if_R"].view(np.int64))
+    for idx in range(int(g["n_fm"][0])):
+        m, n, k = map(int, g[f"fm{idx}_shape"])
+        C = oracle.pidblas_fma_mulmm(m, n, k, g[f"fm{idx}_A"], g[f"fm{idx}_B"])
+        assert np.array_equal(C.view(np.int64), g[f"fm{idx}_C"].view(np.int64)), idx
+
+
+def test_ifma_oracle_vs_reference_build(oracle):
+    """Fresh random cases against the reference compiled here (skipped where
+    the reference sources are not mounted)."""
+    import numpy as np
+    import pytest
+    R = oracle.ref_lib()
+    if R is None:
+        pytest.skip("reference build unavailable")
+    from tests.golden.make_golden import mixed_intervals
+    rng = np.random.default_rng(99)
+    n = 10000
+    A, B, C = (mixed_intervals(rng, n) for _ in range(3))
+    out = np.empty(2 * n)
+    R.ref_ifma(n, oracle._p(A), oracle._p(B), oracle._p(C), oracle._p(out))
+    assert np.array_equal(oracle.ifma(A, B, C).view(np.int64), out.view(np.int64))
+    m, nn, k = 23, 19, 77
+    A, B = mixed_intervals(rng, m * k), mixed_intervals(rng, k * nn)
+    ref = np.empty(2 * m * nn)
+    assert R.ref_pidblas_fma_mulmm(m, nn, k, oracle._p(A), oracle._p(B), oracle._p(ref)) == 0
+    assert np.array_equal(oracle.pidblas_fma_mulmm(m, nn, k, A, B).view(np.int64),
+                          ref.view(np.int64))

@@ -46,6 +46,7 @@ void dpotrf_(char*, int*, double*, int*, int*) { std::abort(); }
 
 typedef kv::interval<double> I;
 typedef vcp::matrix<I, vcp::pidcuda> M;
+typedef vcp::matrix<I, vcp::pidcuda_fma> MF;
 
 int main(int argc, char**) {
   M A, B, C;
@@ -68,6 +69,16 @@ int main(int argc, char**) {
     std::printf("STATE_ERROR mulltmm: %s\n", e.what());
     ++errors;
   }
+  try {
+    MF F, G, H;
+    F.zeros(4, 3);
+    G.zeros(3, 5);
+    H = F * G;                            // pidcuda_fma::mulmm -> vcpcu_igemm_fma
+    std::printf("NO_ERROR mulmm_fma\n");
+  } catch (vcp::state_error& e) {
+    std::printf("STATE_ERROR mulmm_fma: %s\n", e.what());
+    ++errors;
+  }
   if (argc > 99) {  // never run: instantiates imats::linearsolve over the pidcuda hooks
     M S;
     S.zeros(3, 3);
@@ -83,7 +94,7 @@ int main(int argc, char**) {
     std::printf("RUNTIME_ERROR rmatmul: %s\n", e.what());
     ++errors;
   }
-  return errors == 3 ? 0 : 1;
+  return errors == 4 ? 0 : 1;
 }
 '''
 
@@ -109,4 +120,91 @@ def test_policy_headers_compile_link_and_map_errors(tmp_path, cuda_lib):
     run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert run.returncode == 0, run.stdout + run.stderr
     assert "STATE_ERROR mulmm" in run.stdout and "STATE_ERROR mulltmm" in run.stdout
+    assert "STATE_ERROR mulmm_fma" in run.stdout
     assert "RUNTIME_ERROR rmatmul" in run.stdout
+
+
+PROGRAM_DD = r'''
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <kv/dd.hpp>
+#include <vcp/matrix.hpp>
+#include <vcp_cuda/pddcuda.hpp>
+
+extern "C" {
+void dgemm_(char*, char*, int*, int*, int*, double*, const double*, int*, const double*, int*,
+            double*, double*, int*) { std::abort(); }
+double ddot_(int*, const double*, int*, const double*, int*) { std::abort(); }
+void dgemv_(char*, int*, int*, double*, const double*, int*, const double*, int*, double*,
+            double*, int*) { std::abort(); }
+void dsyrk_(char*, char*, int*, int*, double*, const double*, int*, double*, double*, int*) {
+  std::abort();
+}
+void dsymm_(char*, char*, int*, int*, double*, const double*, int*, const double*, int*,
+            double*, double*, int*) { std::abort(); }
+void dgetrf_(int*, int*, double*, int*, int*, int*) { std::abort(); }
+void dgetrs_(char*, int*, int*, double*, int*, int*, double*, int*, int*) { std::abort(); }
+void dgetri_(int*, double*, int*, int*, double*, int*, int*) { std::abort(); }
+void dsyev_(char*, char*, int*, double*, int*, double*, double*, int*, int*) { std::abort(); }
+void dgesv_(int*, int*, double*, int*, int*, double*, int*, int*) { std::abort(); }
+void dsygv_(int*, char*, char*, int*, double*, int*, double*, int*, double*, double*, int*,
+            int*) { std::abort(); }
+void dpotrf_(char*, int*, double*, int*, int*) { std::abort(); }
+}
+
+typedef vcp::matrix<kv::dd, vcp::pddcuda> M;
+
+int main() {
+  M A, B, C;
+  A.zeros(4, 3);
+  B.zeros(3, 5);
+  for (int i = 0; i < 12; ++i) A.data()[i] = kv::dd(i - 1.0, std::ldexp(1.0, -60));
+  for (int i = 0; i < 15; ++i) B.data()[i] = kv::dd(2.0 * i);
+  int errors = 0;
+  try {
+    C = A * B;                            // pddcuda::mulmm -> vcpcu_ddgemm
+    std::printf("NO_ERROR mulmm\n");
+  } catch (vcp::state_error& e) {
+    std::printf("STATE_ERROR mulmm: %s\n", e.what());
+    ++errors;
+  }
+  try {
+    C = ltransmul(A);                     // pddcuda::mulltmm -> vcpcu_ddgemm
+    std::printf("NO_ERROR mulltmm\n");
+  } catch (vcp::state_error& e) {
+    std::printf("STATE_ERROR mulltmm: %s\n", e.what());
+    ++errors;
+  }
+  M s, t;                                 // the scalar shortcut of pddblas stays on the host
+  s.zeros(1, 1);
+  s.data()[0] = kv::dd(3.0);
+  t = s * A;
+  if (t.data()[5].a1 != 12.0) ++errors;
+  std::fflush(stdout);
+  return errors == 2 ? 0 : 1;
+}
+'''
+
+
+def test_pddcuda_header_compile_link_and_map_errors(tmp_path, cuda_lib):
+    if not (REF / "vcp" / "pddblas.hpp").exists():
+        pytest.skip("reference headers not mounted")
+    src = tmp_path / "use_pddcuda.cpp"
+    src.write_text(PROGRAM_DD)
+    exe = tmp_path / "use_pddcuda"
+    cmd = ["g++", "-std=c++11", "-O1", f"-I{ROOT / 'oracle' / 'kvshim'}", f"-I{REF}",
+           f"-I{ROOT / 'include'}", str(src), "-o", str(exe), f"-L{ROOT / 'vcp_gb300'}",
+           "-lvcpcuda", f"-Wl,-rpath,{ROOT / 'vcp_gb300'}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("compiled; the no-device error path is checked on CPU-only hosts")
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stdout + run.stderr
+    assert "STATE_ERROR mulmm" in run.stdout and "STATE_ERROR mulltmm" in run.stdout

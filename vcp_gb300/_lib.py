@@ -44,6 +44,10 @@ SIGNATURES: dict[str, tuple] = {
     "vcpcu_ddgemm": (_i, [_i, _i, _i, _v, _v, _v, _v, _i]),
     "vcpcu_udmatmul_ozaki_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _v, _i, _i, _v]),
     "vcpcu_udmatmul_ozaki": (_i, [_i, _i, _i, _v, _v, _v, _v, _i]),
+    "vcpcu_ifma_dev": (_i, [C.c_long, _v, _v, _v, _v, _v]),
+    "vcpcu_ifma": (_i, [C.c_long, _v, _v, _v, _v]),
+    "vcpcu_igemm_fma_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _v]),
+    "vcpcu_igemm_fma": (_i, [_i, _i, _i, _v, _v, _v]),
     "vcpcu_autotune": (_i, [_v, _v]),
     "vcpcu_autotune_choice": (_i, [_i, _i, _i]),
     "vcpcu_igemm_batched_dev": (_i, [_i, _v, _i, _i, _v]),

@@ -227,6 +227,89 @@ int vcpcu_udmatmul_dev(int m, int n, int k, const double* A, int lda, const doub
   return rmatmul_dev_impl(m, n, k, A, lda, B, ldb, CU, CD, ldc, PK_UPDOWN, (cudaStream_t)stream);
 }
 
+int vcpcu_ifma_dev(long count, const double* A, const double* B, const double* C, double* R,
+                   void* stream) {
+  clear_error();
+  if (count <= 0) return VCPCU_OK;
+  if (!A || !B || !C || !R) {
+    set_error("ifma: null pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (misaligned16(A) || misaligned16(B)) {
+    set_error("ifma: A and B must be 16-byte aligned");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  int st = check_device();
+  if (st) return st;
+  return launch_ifma(count, A, B, C, R, (cudaStream_t)stream);
+}
+
+int vcpcu_ifma(long count, const double* A, const double* B, const double* C, double* R) {
+  clear_error();
+  if (count <= 0) return VCPCU_OK;
+  if (!A || !B || !C || !R) {
+    set_error("ifma: null pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  int st = check_device();
+  if (st) return st;
+  cudaStream_t s = host_stream();
+  const size_t n2 = 2 * (size_t)count;
+  Scratch buf;
+  if ((st = buf.alloc(sizeof(double) * 4 * n2, s))) return st;
+  double* dA = (double*)buf.ptr;
+  double* dB = dA + n2;
+  double* dC = dB + n2;
+  double* dR = dC + n2;
+  if ((st = h2d(dA, A, n2, s)) || (st = h2d(dB, B, n2, s)) || (st = h2d(dC, C, n2, s))) return st;
+  if ((st = launch_ifma(count, dA, dB, dC, dR, s))) return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(R, dR, n2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  return VCPCU_OK;
+}
+
+int vcpcu_igemm_fma_dev(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                        double* C, int ldc, void* stream) {
+  clear_error();
+  if (m <= 0 || n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (!C || (k > 0 && (!A || !B)) || ldc < m || (k > 0 && (lda < m || ldb < k))) {
+    set_error("igemm_fma: null pointer or leading dimension too small");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (k > 0 && (misaligned16(A) || misaligned16(B))) {
+    set_error("igemm_fma: A and B must be 16-byte aligned");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  int st = check_device();
+  if (st) return st;
+  return launch_igemm_fma(m, n, k, A, lda, B, ldb, C, ldc, (cudaStream_t)stream);
+}
+
+int vcpcu_igemm_fma(int m, int n, int k, const double* A, const double* B, double* C) {
+  clear_error();
+  if (m <= 0 || n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (!C || (k > 0 && (!A || !B))) {
+    set_error("igemm_fma: null pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  int st = check_device();
+  if (st) return st;
+  cudaStream_t s = host_stream();
+  const size_t na = 2 * (size_t)m * k, nb = 2 * (size_t)k * n, nc = 2 * (size_t)m * n;
+  Scratch buf;
+  if ((st = buf.alloc(sizeof(double) * (na + nb + nc), s))) return st;
+  double* dA = (double*)buf.ptr;
+  double* dB = dA + na;
+  double* dC = dB + nb;
+  if ((st = h2d(dA, A, na, s)) || (st = h2d(dB, B, nb, s))) return st;
+  if ((st = launch_igemm_fma(m, n, k, dA, m, dB, k > 0 ? k : 1, dC, m, s))) return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(C, dC, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  return VCPCU_OK;
+}
+
 namespace {
 int udoz_check(int m, int n, int k, const void* A, const void* B, const void* CU, const void* CD,
                int slices) {

@@ -29,4 +29,10 @@ int vsyrk_dispatch(int n, int k, const double* A, long lda, double* C, long ldc,
 int norm_dispatch(int n, const double* R, long ldr, const double* A, long lda, double* bound,
                   int form, int slices, cudaStream_t s);
 
+// ifma.cu: elementwise inf-sup interval FMA and the ifma-chain product.
+int launch_ifma(long count, const double* A, const double* B, const double* C, double* R,
+                cudaStream_t s);
+int launch_igemm_fma(int M, int N, int K, const double* A, long lda, const double* B, long ldb,
+                     double* C, long ldc, cudaStream_t s);
+
 }  // namespace vcpcu

@@ -124,3 +124,34 @@ def autotune(stream=None) -> dict:
 def autotune_choice(m: int, n: int, k: int) -> int:
     """The form (FORM_PLAIN or FORM_OZAKI) that FORM_AUTO uses for m x n x k."""
     return int(_lib.load().vcpcu_autotune_choice(int(m), int(n), int(k)))
+
+
+# ---- inf-sup interval FMA (vcp::ifma) and its product (vcp::pidblas_fma) ------------
+
+def ifma(A: np.ndarray, B: np.ndarray, C: np.ndarray) -> np.ndarray:
+    """Elementwise vcp::ifma over kv buffers: R = [A] [B] + [C] (inf-sup form,
+    directed fused multiply-adds; vcp/ifma.hpp:48-139)."""
+    n = np.asarray(A).size // 2
+    R = np.empty(2 * n, dtype=np.float64)
+    if n == 0:
+        return R
+    _lib.call("vcpcu_ifma", n, _host_ptr(A, 2 * n, "A"), _host_ptr(B, 2 * n, "B"),
+              _host_ptr(C, 2 * n, "C"), _host_ptr(R, 2 * n, "R", writable=True))
+    return R
+
+
+def mulmm_fma(A: np.ndarray, B: np.ndarray, m: int, n: int, k: int) -> np.ndarray:
+    """C = [A] [B] as vcp::pidblas_fma::mulmm (an ifma chain per entry, ascending
+    inner index; vcp/pidblas_fma.hpp:46-80).  Returns the kv buffer of C."""
+    out = np.empty(2 * m * n, dtype=np.float64)
+    if m <= 0 or n <= 0:
+        return out
+    pa = _host_ptr(A, 2 * m * k, "A") if k > 0 else None
+    pb = _host_ptr(B, 2 * k * n, "B") if k > 0 else None
+    _lib.call("vcpcu_igemm_fma", m, n, k, pa, pb, _host_ptr(out, 2 * m * n, "C", writable=True))
+    return out
+
+
+def mulmm_fma_dev(m, n, k, A, lda, B, ldb, C, ldc, stream=None) -> None:
+    _lib.call("vcpcu_igemm_fma_dev", m, n, k, _dev_ptr(A, "A"), lda, _dev_ptr(B, "B"), ldb,
+              _dev_ptr(C, "C"), ldc, _stream_ptr(stream))
