@@ -40,6 +40,21 @@ OZ_HD uint64_t oz_bits(double x) {
 #endif
 }
 
+// x == +-0 tested on the bit pattern (an FP64 comparison would issue on the
+// narrow FP64 pipe of GB300).
+OZ_HD bool oz_zero(double x) { return (oz_bits(x) << 1) == 0; }
+// |x| by clearing the sign bit (integer pipe).
+OZ_HD double oz_abs(double x) {
+  const uint64_t b = oz_bits(x) & 0x7fffffffffffffffULL;
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double r;
+  memcpy(&r, &b, 8);
+  return r;
+#endif
+}
+
 // E such that |x| <= 2^(E-1) for the largest magnitude `amax` (>= 0, finite);
 // OZ_ZERO_EXP for amax == 0.
 OZ_HD int oz_exponent(double amax) {

@@ -46,7 +46,7 @@ __device__ __forceinline__ double scale_pow2(double x, int e, bool up) {
   const int be = (int)((b >> 52) & 0x7ff);
   if (be != 0 && be != 0x7ff && be + e >= 1 && be + e <= 2046)
     return __longlong_as_double((long long)(b + ((unsigned long long)(long long)e << 52)));
-  if (x == 0.0) return x;
+  if (oz_zero(x)) return x;
   return scale_dir2(x, e, up);
 }
 

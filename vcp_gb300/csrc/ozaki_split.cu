@@ -34,7 +34,7 @@ __device__ __forceinline__ uint32_t bf16_bits(int d) {
 
 template <int S>
 __device__ __forceinline__ void digits_of(double x, int E, int up, int (&d)[S]) {
-  if (E == OZ_ZERO_EXP || x == 0.0) {
+  if (E == OZ_ZERO_EXP || oz_zero(x)) {
 #pragma unroll
     for (int q = 0; q < S; ++q) d[q] = 0;
     return;
@@ -84,7 +84,7 @@ oz_rowmax_left(int M, int K, const double* __restrict__ A, long lda, int cols_pe
       double m = 0.0, r = 0.0, p;
       if (sw_finite(e.x) && sw_finite(e.y)) {
         sw_midrad(e.x, e.y, m, r, p);
-        am = max(am, dbits(fabs(m)));
+        am = max(am, dbits(oz_abs(m)));
         ap = max(ap, dbits(p));
         ar = max(ar, dbits(r));
       } else {
@@ -145,7 +145,7 @@ oz_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
     if (i < M && k < K) {
       m = mA[i + (long)k * M];
       rr = rA[i + (long)k * M];
-      p = sw_add_ru_pos(fabs(m), rr);
+      p = sw_add_ru_pos(oz_abs(m), rr);
     }
     digits_of<S>(m, Em, 0, d);
 #pragma unroll
@@ -224,7 +224,7 @@ oz_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
       double m = 0.0, r = 0.0, p;
       if (sw_finite(e.x) && sw_finite(e.y)) {
         sw_midrad(e.x, e.y, m, r, p);
-        am = max(am, dbits(fabs(m)));
+        am = max(am, dbits(oz_abs(m)));
         ar = max(ar, dbits(r));
         bsum = __dadd_ru(bsum, fabs(m));
       } else {
@@ -276,7 +276,7 @@ oz_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
         const uint32_t b = bf16_bits(dr[q]);
         if (h & 1) hr[q][h >> 1] |= b << 16; else hr[q][h >> 1] = b;
       }
-      digits_of<SR>(fabs(m), Fm, 1, dr);
+      digits_of<SR>(oz_abs(m), Fm, 1, dr);
 #pragma unroll
       for (int q = 0; q < sr; ++q) {
         const uint32_t b = bf16_bits(dr[q]);
@@ -412,7 +412,7 @@ __device__ __forceinline__ double dev_scale_dir(double x, int e, bool up) {
 
 // w-bit integer of x (|x| <= 2^(E-1)): round to nearest even, |result| <= 2^(w-1).
 __device__ __forceinline__ long long crt_int(double x, int E, int w) {
-  if (E == OZ_ZERO_EXP || x == 0.0) return 0;
+  if (E == OZ_ZERO_EXP || oz_zero(x)) return 0;
   return oz_scaled_int64(x, E, w, 0);
 }
 
@@ -453,7 +453,7 @@ oz_split_left_crt(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
         if (i < M && k < K) {
           m = mA[i + (long)k * M];
           r = rA[i + (long)k * M];
-          p = sw_add_ru_pos(fabs(m), r);
+          p = sw_add_ru_pos(oz_abs(m), r);
         }
         a[t + u] = crt_int(m, Em, w);
         digits_of<SR>(p, Ep, 1, u ? d1 : d0);
@@ -530,7 +530,7 @@ oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, l
       double m = 0.0, r = 0.0, p;
       if (sw_finite(e.x) && sw_finite(e.y)) {
         sw_midrad(e.x, e.y, m, r, p);
-        am = max(am, dbits(fabs(m)));
+        am = max(am, dbits(oz_abs(m)));
         ar = max(ar, dbits(r));
       } else {
         bad = true;
@@ -573,7 +573,7 @@ oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, l
         slo += ub & 0xffffffffULL;
         limbs12<NL>(ub, b < 0, hl[t + u]);
         digits_of<SR>(r, Fr, 1, u ? d1 : d0);
-        digits_of<SR>(fabs(m), Fm, 1, u ? e1 : e0);
+        digits_of<SR>(oz_abs(m), Fm, 1, u ? e1 : e0);
       }
 #pragma unroll
       for (int q = 0; q < SR; ++q) {
@@ -713,8 +713,8 @@ __device__ __forceinline__ int dev_sym_residue128(unsigned __int128 a, int neg, 
 __device__ __forceinline__ __int128 dd_int(double hi, double lo, int E, int w) {
   if (E == OZ_ZERO_EXP) return 0;
   __int128 a = 0;
-  if (hi != 0.0) a += oz_scaled_int_bits(hi, E, w, 0);
-  if (lo != 0.0) a += oz_scaled_int_bits(lo, E, w, 0);
+  if (!oz_zero(hi)) a += oz_scaled_int_bits(hi, E, w, 0);
+  if (!oz_zero(lo)) a += oz_scaled_int_bits(lo, E, w, 0);
   return a;
 }
 
@@ -734,7 +734,7 @@ dd_rowmax(int M, int K, const double* __restrict__ A, long lda, int cols_per_blo
     for (int c = c0 + ph; c < c1; c += 8) {
       const double2 e = *reinterpret_cast<const double2*>(A + 2 * (i + (long)c * lda));
       if (isfinite(e.x) && isfinite(e.y))
-        am = max(am, dbits(fabs(e.x)));
+        am = max(am, dbits(oz_abs(e.x)));
       else
         bad = true;
     }
@@ -813,7 +813,7 @@ dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
     for (int k = tid; k < K; k += 256) {
       const double2 e = *reinterpret_cast<const double2*>(B + 2 * (k + (long)j * ldb));
       if (isfinite(e.x) && isfinite(e.y))
-        am = max(am, dbits(fabs(e.x)));
+        am = max(am, dbits(oz_abs(e.x)));
       else
         bad = true;
     }
