@@ -283,9 +283,9 @@ def run_ours(args, ws, rank, local):
         _lib.profile_read()  # discard anything recorded before the timed region
     with ClockSampler(local) as clk:
         ms, launches = timed(form, args.steps, args.warmup)
-    phases, tc_flops = ([0.0] * 4, 0)
+    phases, tc_flops = ([0.0] * 5, 0)
     if form == pidcuda.FORM_OZAKI:
-        phases, tc_flops = _lib.profile_read()
+        phases, tc_flops = _lib.profile_read(5)
         _lib.profile(False)
         # the warm-up calls were recorded too: keep the timed steps' share
         frac = args.steps / (args.steps + args.warmup)
@@ -348,7 +348,8 @@ def run_ours(args, ws, rank, local):
                 "traffic": None, "peak_kind": fp64_kind,
                 "algorithmic": "8 n^3 FP64 flops per launch (4 directed FMA chains)"}
     else:
-        roof = ozaki_roofline(phases, tc_flops, args.steps, pk, pk_kind)
+        roof = ozaki_roofline(phases, tc_flops, args.steps, pk, pk_kind, n,
+                              args.slices in (0, 8))
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -413,19 +414,29 @@ def measure_fp64_peak(dev):
         return 1.25, "nominal"
 
 
-def ozaki_roofline(phases, tc_flops, steps, pk, pk_kind):
+# DRAM bytes (read + write) of the three oz_slice_gemm_kernel launches of one
+# n = 8192 product at the default precision, from a one-pass ncu capture of
+# dram__bytes_read.sum and dram__bytes_write.sum on a GB300 (radius 1:
+# 5.29 + 0.83 GB, radius 2: 5.27 + 0.83 GB, midpoint residues: 15.19 + 1.31 GB).
+GEMM_TRAFFIC_N8192 = 28.73e9
+
+
+def ozaki_roofline(phases, tc_flops, steps, pk, pk_kind, n=8192, default_form=True):
     """Dominant kernel oz_slice_gemm_kernel (three launches per call): the
-    algorithmic bf16 tensor flops (2 m n k per slice pair) over their summed
-    CUDA-event time on the launching stream."""
+    algorithmic bf16 tensor flops (2 m n k per slice pair or modulus) over
+    their summed CUDA-event time on the launching stream."""
     gemm_ms = sum(phases[1:4])
     achieved = tc_flops / (gemm_ms * 1e-3) / 1e12 if gemm_ms > 0 else None
     peak = pk.get("bf16_tflops", 1900.0)
     return {"bound": "tensor", "kernel": "oz_slice_gemm_kernel", "achieved": achieved,
             "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
-            "traffic": None, "peak_kind": f"{pk_kind} bf16 dense (burst)",
-            "algorithmic": "2*m*n*k per bf16 slice-pair product",
+            "traffic": GEMM_TRAFFIC_N8192 if (n == 8192 and default_form) else None,
+            "traffic_unit": "bytes per call (3 launches)",
+            "peak_kind": f"{pk_kind} bf16 dense (burst); sustained {pk.get('bf16_tflops_sustained')}",
+            "algorithmic": "2*m*n*k per bf16 product: L residue GEMMs + 2 x 4 radius digit pairs",
             "phase_ms_per_call": {"prep": phases[0] / steps, "radius1": phases[1] / steps,
-                                  "radius2": phases[2] / steps, "midpoint": phases[3] / steps}}
+                                  "radius2": phases[2] / steps, "midpoint": phases[3] / steps,
+                                  "reassembly": phases[4] / steps}}
 
 
 # ---------------------------------------------------------------- other workloads

@@ -68,8 +68,8 @@ int vcpcu_status(void* stream);
 
 /* Per-phase timing of Ozaki-form calls: while enabled, every call records
  * CUDA events on its own stream around its phases (0 operand preparation,
- * 1 and 2 the two radius slice GEMMs, 3 the midpoint slice GEMM and
- * reassembly).  vcpcu_profile_read waits for the recorded events, writes
+ * 1 and 2 the two radius slice GEMMs, 3 the midpoint slice GEMM, 4 the
+ * reassembly of the CRT form).  vcpcu_profile_read waits for the recorded events, writes
  * the summed milliseconds of the first `nphases` phases to ms[], the summed
  * algorithmic tensor-core flops (2 m n k per slice pair) to *tensor_flops,
  * and clears the record.  No counterpart in the reference (it has only

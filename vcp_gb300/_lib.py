@@ -90,11 +90,13 @@ def profile(enable: bool) -> None:
     call("vcpcu_profile", 1 if enable else 0)
 
 
-def profile_read() -> tuple[list[float], int]:
-    """(ms per phase [prep, radius 1, radius 2, midpoint], tensor flops)."""
-    ms = (C.c_double * 4)()
+def profile_read(nphases: int = 5) -> tuple[list[float], int]:
+    """(ms per phase [prep, radius 1, radius 2, midpoint GEMM, reassembly],
+    tensor flops)."""
+    ms = (C.c_double * nphases)()
     fl = C.c_longlong(0)
-    call("vcpcu_profile_read", C.cast(ms, C.c_void_p), 4, C.cast(C.pointer(fl), C.c_void_p))
+    call("vcpcu_profile_read", C.cast(ms, C.c_void_p), nphases,
+         C.cast(C.pointer(fl), C.c_void_p))
     return list(ms), int(fl.value)
 
 

@@ -83,7 +83,7 @@ __global__ void oz_status_merge(const int* flag) {
 // Optional per-phase timing (CUDA events recorded on the call's stream).
 struct OzProfile {
   bool on = false;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[4];  // prep, rad1, rad2, mid
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[5];  // prep, rad1, rad2, mid, reassembly
   long long flops = 0;
 };
 OzProfile g_prof;
@@ -117,7 +117,7 @@ int oz_profile_enable(int on) {
 
 int oz_profile_read(double* ms, int nphases, long long* flops) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
-  for (int ph = 0; ph < 4; ++ph) {
+  for (int ph = 0; ph < 5; ++ph) {
     double tot = 0.0;
     for (auto& e : g_prof.ev[ph]) {
       cudaEventSynchronize(e.second);
@@ -350,12 +350,13 @@ int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long ld
   if (!plan.pb.crt && (st = oz_radius_T(plan, ws, s))) return st;
   {
     PhaseTimer t(3, s);
-    if (plan.pb.crt) {
-      if ((st = oz_run_gemm(plan, OZ_CRT, ws, nullptr, 0, s))) return st;
-      if ((st = oz_crt_assemble(plan, ws, C, ldc, s))) return st;
-    } else {
-      if ((st = oz_run_gemm(plan, OZ_MID, ws, C, ldc, s))) return st;
-    }
+    if ((st = oz_run_gemm(plan, plan.pb.crt ? OZ_CRT : OZ_MID, ws, plan.pb.crt ? nullptr : C,
+                          ldc, s)))
+      return st;
+  }
+  if (plan.pb.crt) {
+    PhaseTimer t(4, s);
+    if ((st = oz_crt_assemble(plan, ws, C, ldc, s))) return st;
   }
   return VCPCU_OK;
 }
