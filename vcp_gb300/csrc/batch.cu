@@ -257,43 +257,87 @@ struct BatchGraph {
   cudaGraphExec_t exec = nullptr;
 };
 
-// Ozaki form: the problems one after another, each bracketed by device
-// clock stamps (t_first / t_last of the problem).
-int batch_launch_ozaki(const BatchGraph& g, cudaStream_t s) {
+// Tensor-core forms: every selected problem is one product (preparation,
+// slice GEMMs, reassembly) bracketed by device clock stamps (t_first /
+// t_last).  The products are spread round-robin over OZ_BATCH_STREAMS
+// streams forked from `s` and joined back into it, so the small products of
+// a batch overlap on the GPU (inside a capture the branches become parallel
+// graph branches).
+constexpr int OZ_BATCH_STREAMS = 16;
+
+// Forked branches of one batch: created by fork(), joined back into the
+// parent stream by join().
+struct Branches {
+  cudaStream_t side[OZ_BATCH_STREAMS];
+  cudaEvent_t join_ev[OZ_BATCH_STREAMS];
+  int made = 0;
+
+  int fork(cudaStream_t s, int want) {
+    cudaEvent_t f;
+    VCPCU_CUDA_TRY(cudaEventCreateWithFlags(&f, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(f, s);
+    for (; e == cudaSuccess && made < want; ++made) {
+      e = cudaStreamCreateWithFlags(&side[made], cudaStreamNonBlocking);
+      if (e != cudaSuccess) break;
+      e = cudaEventCreateWithFlags(&join_ev[made], cudaEventDisableTiming);
+      if (e != cudaSuccess) {
+        cudaStreamDestroy(side[made]);
+        break;
+      }
+      e = cudaStreamWaitEvent(side[made], f, 0);
+    }
+    cudaEventDestroy(f);
+    return e == cudaSuccess ? VCPCU_OK : cuda_fail(e, "batch: fork streams");
+  }
+  // every branch rejoins s (also after an error: a capture must end joined)
+  void join(cudaStream_t s) {
+    for (int b = 0; b < made; ++b) {
+      cudaEventRecord(join_ev[b], side[b]);
+      cudaStreamWaitEvent(s, join_ev[b], 0);
+      cudaEventDestroy(join_ev[b]);
+      cudaStreamDestroy(side[b]);
+    }
+    made = 0;
+  }
+};
+
+// The selected problems round-robin over the branches, each bracketed by
+// its stamps.
+int batch_issue_ozaki(const BatchGraph& g, Branches& br, bool auto_only) {
+  int r = 0;
   for (int i = 0; i < g.count; ++i) {
     const BatchProblem& q = g.probs[i];
-    stamp<<<1, 1, 0, s>>>(g.d.t_first + i);
-    VCPCU_LAUNCH_CHECK("stamp");
-    if (q.m > 0 && q.n > 0) {
-      int st = igemm_any(q.m, q.n, q.k > 0 ? q.k : 0, q.A, q.lda, q.B, q.ldb, q.C, q.ldc, g.form,
-                         g.slices, s);
+    const bool run = q.m > 0 && q.n > 0 && (!auto_only || g.ozaki[i]);
+    if (auto_only && !run) continue;
+    cudaStream_t t = br.side[r++ % br.made];
+    stamp<<<1, 1, 0, t>>>(g.d.t_first + i);
+    if (run) {
+      const int st = igemm_any(q.m, q.n, q.k > 0 ? q.k : 0, q.A, q.lda, q.B, q.ldb, q.C, q.ldc,
+                               auto_only ? VCPCU_FORM_OZAKI : g.form, g.slices, t);
       if (st) return st;
     }
-    stamp<<<1, 1, 0, s>>>(g.d.t_last + i);
-    VCPCU_LAUNCH_CHECK("stamp");
+    stamp<<<1, 1, 0, t>>>(g.d.t_last + i);
   }
+  VCPCU_LAUNCH_CHECK("stamp");
   return VCPCU_OK;
 }
 
 int batch_record(BatchGraph& g, cudaStream_t s) {
   if (g.form == VCPCU_FORM_PLAIN) return batch_launch_plain(g.d, s);
-  if (g.form != VCPCU_FORM_AUTO) return batch_launch_ozaki(g, s);
+  const bool auto_only = g.form == VCPCU_FORM_AUTO;
+  int nsel = 0;
+  for (int i = 0; i < g.count; ++i) nsel += auto_only ? g.ozaki[i] != 0 : 1;
+  Branches br;
+  int st = VCPCU_OK;
+  if (nsel > 0)
+    st = br.fork(s, nsel < OZ_BATCH_STREAMS ? nsel : OZ_BATCH_STREAMS);
   // AUTO: the problems the cost model gives to the plain form run in the
-  // grouped launch (the others have zero tiles there), the rest in sequence
-  int st = batch_launch_plain(g.d, s);
-  if (st) return st;
-  for (int i = 0; i < g.count; ++i) {
-    const BatchProblem& q = g.probs[i];
-    if (q.m <= 0 || q.n <= 0 || !g.ozaki[i]) continue;
-    stamp<<<1, 1, 0, s>>>(g.d.t_first + i);
-    VCPCU_LAUNCH_CHECK("stamp");
-    if ((st = igemm_any(q.m, q.n, q.k > 0 ? q.k : 0, q.A, q.lda, q.B, q.ldb, q.C, q.ldc,
-                        VCPCU_FORM_OZAKI, g.slices, s)))
-      return st;
-    stamp<<<1, 1, 0, s>>>(g.d.t_last + i);
-    VCPCU_LAUNCH_CHECK("stamp");
-  }
-  return VCPCU_OK;
+  // grouped launch on s (the others have zero tiles there), concurrently
+  // with the tensor-core products on the branches
+  if (!st && auto_only) st = batch_launch_plain(g.d, s);
+  if (!st && nsel > 0) st = batch_issue_ozaki(g, br, auto_only);
+  br.join(s);
+  return st;
 }
 
 // AUTO: mark the problems the autotuner sends to the tensor-core form and
