@@ -495,6 +495,31 @@ def time_stream(fn, stream, steps, warmup=1):
     return e0.elapsed_time(e1) / steps
 
 
+def time_profiled(fn, stream, steps, pk):
+    """time_stream plus the library's phase timing: (ms per call, roofline of
+    the slice GEMMs against the measured bf16 burst peak)."""
+    from vcp_gb300 import _lib
+    fn()
+    stream.synchronize()
+    _lib.profile(True)
+    _lib.profile_read()
+    ms = time_stream(fn, stream, steps, warmup=0)
+    phases, flops = _lib.profile_read()
+    _lib.profile(False)
+    gemm_ms = sum(phases[1:4])
+    peak = pk.get("bf16_tflops", 1900.0)
+    ach = flops / (gemm_ms * 1e-3) / 1e12 if gemm_ms > 0 else None
+    return ms, {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                "frac": ach / peak if ach else None,
+                "phase_ms_per_call": [p / steps for p in phases]}
+
+
+def cpu_rate(fn, flops):
+    t0 = time.perf_counter()
+    fn()
+    return flops / (time.perf_counter() - t0) / 1e12
+
+
 def bench_batch(dev, stream, steps=1, count=4096, seed=4096, forms=("plain", "ozaki", "auto"),
                 check=True):
     """Batched uneven interval GEMMs through captured CUDA graphs."""
@@ -556,6 +581,16 @@ def bench_batch(dev, stream, steps=1, count=4096, seed=4096, forms=("plain", "oz
         out[name] = rec
     if "plain" in widths and "ozaki" in widths:
         out["width_ozaki_vs_plain_median"] = float(np.median(widths["ozaki"] / widths["plain"]))
+    # CPU: the oracle restatement of pidblas::mulmm on the first 64 problems
+    sel = list(range(min(64, count)))
+    hs = [(int(m[i]), int(n[i]), int(k[i]), probs[i][3].cpu().numpy(), probs[i][5].cpu().numpy())
+          for i in sel]
+    fl_s = float(sum(2.0 * a * b * c for (a, b, c, _, _) in hs))
+    out["cpu_baseline"] = {
+        "value": cpu_rate(lambda: [O.pidblas_mulmm(a, b, c, Ah_, Bh_, cpu_count())
+                                   for (a, b, c, Ah_, Bh_) in hs], fl_s),
+        "unit": "TFLOP/s", "cores": cpu_count(), "kind": "port",
+        "sample": f"the first {len(sel)} problems, oracle restatement of pidblas::mulmm"}
     del pa, pb, pc
     return out
 
@@ -570,8 +605,8 @@ def bench_dd(dev, stream, n, phi, steps=2, seed=77, sample=256):
     B = dev_dd(n * n, phi, gen, dev)
     C = torch.empty(2 * n * n, dtype=torch.float64, device=dev)
     E = torch.empty(n * n, dtype=torch.float64, device=dev)
-    ms = time_stream(lambda: pddcuda.mulmm_dev(n, n, n, A, n, B, n, C, n, E, n, 0, stream),
-                     stream, steps)
+    ms, roof = time_profiled(lambda: pddcuda.mulmm_dev(n, n, n, A, n, B, n, C, n, E, n, 0, stream),
+                             stream, steps, peaks()[0])
     Ah, Bh, Ch, Eh = (t.cpu().numpy() for t in (A, B, C, E))
     rs = np.random.default_rng(seed)
     r = rs.integers(0, n, sample)
@@ -585,7 +620,7 @@ def bench_dd(dev, stream, n, phi, steps=2, seed=77, sample=256):
             "bound_failures": int(np.sum(err > bnd)),
             "bound_over_err_median": float(np.median(bnd[nz] / err[nz])) if nz.any() else None,
             "bound_rel_median": float(np.median(bnd / np.where(ab > 0, ab, 1.0))),
-            "sample": sample, "slices": "default (13, w = 104)"}
+            "sample": sample, "slices": "default (13, w = 104)", "roofline": roof}
 
 
 def bench_point(dev, stream, m, n, k, phi, slice_list, steps=2, plain=True, seed=11,
@@ -615,12 +650,22 @@ def bench_point(dev, stream, m, n, k, phi, slice_list, steps=2, plain=True, seed
         u, d = CU.cpu().numpy(), CD.cpu().numpy()
         wp = u - d
         out["plain"] = {"tflops": fl / (ms * 1e-3) / 1e12, "ms": ms,
-                        "containment_failures": int(np.sum(d[idx] > dn) + np.sum(u[idx] < up))}
+                        "containment_failures": int(np.sum(d[idx] > dn) + np.sum(u[idx] < up)),
+                        "fp64_tflops": 2 * fl / (ms * 1e-3) / 1e12}
+        # CPU: the oracle restatement of vblas rmatmul (one direction) on a row panel
+        rows = max(1, min(m, int(2e10 / (2.0 * n * k))))
+        Ap = Ah.reshape(n, m)[:, :rows].copy().reshape(-1)
+        out["cpu_baseline"] = {
+            "value": cpu_rate(lambda: O.rmatmul(rows, n, k, Ap, Bh, 1, cpu_count()),
+                              2.0 * rows * n * k),
+            "unit": "TFLOP/s (one direction)", "cores": cpu_count(), "kind": "port",
+            "sample": f"{rows} x {n} x {k} row panel, oracle restatement of vblas rmatmul"}
     for s_ in slice_list:
-        ms = time_stream(lambda: vblas.udmatmul_ozaki_dev(m, n, k, A, m, B, n, CU, CD, m, s_,
-                                                          stream), stream, steps)
+        ms, roof = time_profiled(lambda: vblas.udmatmul_ozaki_dev(m, n, k, A, m, B, n, CU, CD, m,
+                                                                  s_, stream),
+                                 stream, steps, peaks()[0])
         u, d = CU.cpu().numpy(), CD.cpu().numpy()
-        rec = {"tflops": fl / (ms * 1e-3) / 1e12, "ms": ms,
+        rec = {"tflops": fl / (ms * 1e-3) / 1e12, "ms": ms, "roofline": roof,
                "containment_failures": int(np.sum(d[idx] > dn) + np.sum(u[idx] < up))}
         if wp is not None:
             ok = wp > 0

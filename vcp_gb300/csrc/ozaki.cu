@@ -89,25 +89,27 @@ struct OzProfile {
 OzProfile g_prof;
 std::mutex g_prof_mu;
 
-struct PhaseTimer {
-  cudaEvent_t a = nullptr, b = nullptr;
-  int phase;
-  cudaStream_t s;
-  PhaseTimer(int ph, cudaStream_t st) : phase(ph), s(st) {
-    if (!g_prof.on) return;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
-    cudaEventRecord(a, s);
-  }
-  ~PhaseTimer() {
-    if (!a) return;
-    cudaEventRecord(b, s);
-    std::lock_guard<std::mutex> lk(g_prof_mu);
-    g_prof.ev[phase].emplace_back(a, b);
-  }
-};
-
 }  // namespace
+
+PhaseTimer::PhaseTimer(int ph, cudaStream_t st) : phase(ph), s(st) {
+  if (!g_prof.on) return;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, s);
+}
+
+PhaseTimer::~PhaseTimer() {
+  if (!a) return;
+  cudaEventRecord(b, s);
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof.ev[phase].emplace_back(a, b);
+}
+
+void oz_profile_add_flops(long long f) {
+  if (!g_prof.on) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof.flops += f;
+}
 
 int oz_profile_enable(int on) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
@@ -378,12 +380,9 @@ int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B,
   OzWorkspace ws;
   oz_carve_workspace(plan.pb, buf.ptr, &ws);
   if ((st = oz_run_product(plan, ws, A, lda, B, ldb, C, ldc, s))) return st;
-  if (g_prof.on) {
-    std::lock_guard<std::mutex> lk(g_prof_mu);
-    g_prof.flops += 2LL * m * n * (long long)(k > 0 ? k : 0) *
-                    ((plan.pb.crt ? plan.pb.L : plan.mid.npairs) +
-                     (long long)(!(point_mask & 2) + !(point_mask & 1)) * plan.rad.npairs);
-  }
+  oz_profile_add_flops(2LL * m * n * (long long)(k > 0 ? k : 0) *
+                       ((plan.pb.crt ? plan.pb.L : plan.mid.npairs) +
+                        (long long)(!(point_mask & 2) + !(point_mask & 1)) * plan.rad.npairs));
   oz_status_merge<<<1, 1, 0, s>>>(ws.flag);
   VCPCU_LAUNCH_CHECK("oz_status_merge");
   return VCPCU_OK;

@@ -141,9 +141,19 @@ int ozaki_ddgemm(int m, int n, int k, const double* A, long lda, const double* B
                  void* static_scratch = nullptr, size_t static_bytes = 0);
 int dd_plan_bits(int k, int slices, int* w, int* L);
 
-// Per-phase timing of the Ozaki form (prep, radius 1, radius 2, midpoint).
+// Per-phase timing of the Ozaki form (0 prep, 1 radius 1, 2 radius 2,
+// 3 midpoint / residue GEMMs, 4 reassembly): CUDA events on the call's
+// stream while profiling is enabled.
 int oz_profile_enable(int on);
 int oz_profile_read(double* ms, int nphases, long long* flops);
+struct PhaseTimer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  int phase;
+  cudaStream_t s;
+  PhaseTimer(int ph, cudaStream_t st);
+  ~PhaseTimer();
+};
+void oz_profile_add_flops(long long f);
 
 // Operand preparation, the three slice-GEMM phases and the reassembly of
 // one planned product (shared by every entry point of the Ozaki form).

@@ -373,17 +373,28 @@ int ozaki_ddgemm(int m, int n, int k, const double* A, long lda, const double* B
   ws.flag = (int*)(base + bA + bB + bR + bM + bE + bF);
   ws.E3 = E;
   ws.F2 = F;
-  int st = dd_prepare(m, n, k, pb.Mp, pb.Np, pb.Kp, L, w, A, lda, B, ldb, rowmax, E, F, ws.a_mid,
-                      ws.b_mid, ws.flag, s);
-  if (st) return st;
-  if ((st = oz_run_gemm(plan, OZ_CRT, ws, nullptr, 0, s))) return st;
+  int st;
+  {
+    PhaseTimer t(0, s);
+    st = dd_prepare(m, n, k, pb.Mp, pb.Np, pb.Kp, L, w, A, lda, B, ldb, rowmax, E, F, ws.a_mid,
+                    ws.b_mid, ws.flag, s);
+    if (st) return st;
+  }
+  {
+    PhaseTimer t(3, s);
+    if ((st = oz_run_gemm(plan, OZ_CRT, ws, nullptr, 0, s))) return st;
+  }
+  oz_profile_add_flops(2LL * m * n * (long long)(k > 0 ? k : 0) * L);
   long blocks = ((long)m * n + 255) / 256;
   if (blocks > 152L * 64) blocks = 152L * 64;
   if (blocks < 1) blocks = 1;
-  dd_crt_assemble_kernel<<<(int)blocks, 256, 0, s>>>(m, n, k, pb.Mp, L, w, ws.res,
-                                                     (size_t)pb.Np * pb.Mp, E, F, C, ldc, Cerr,
-                                                     lde, ws.flag, cc);
-  VCPCU_LAUNCH_CHECK("dd_crt_assemble_kernel");
+  {
+    PhaseTimer t(4, s);
+    dd_crt_assemble_kernel<<<(int)blocks, 256, 0, s>>>(m, n, k, pb.Mp, L, w, ws.res,
+                                                       (size_t)pb.Np * pb.Mp, E, F, C, ldc, Cerr,
+                                                       lde, ws.flag, cc);
+    VCPCU_LAUNCH_CHECK("dd_crt_assemble_kernel");
+  }
   oz_merge_status(ws.flag, s);
   return VCPCU_OK;
 }
