@@ -54,3 +54,30 @@ def test_batch_graph_replay_and_latencies(cuda_lib, form):
         assert torch.equal(p[7].view(torch.int64), f.view(torch.int64))
     assert np.all(lat > 0) and np.all(start >= 0)
     g.close()
+
+
+def test_grouped_tensor_core_batch_edges(cuda_lib):
+    """The grouped tensor-core path (buckets of equal padded K, stacked
+    operand planes) on problems spanning several tiles and chunks, with empty
+    and k = 0 problems mixed in: every product bit-identical to its single
+    call."""
+    import torch
+    rng = np.random.default_rng(77)
+    shapes = [(1100, 300, 2100), (130, 600, 1030), (5, 7, 0), (0, 9, 12), (64, 1, 64),
+              (257, 513, 64), (40, 40, 40), (129, 257, 1025), (3, 900, 7)]
+    probs = []
+    for (m, n, k) in shapes:
+        A = torch.from_numpy(W.interval_uniform(rng, max(m, 1), max(k, 1), 1e-12)).cuda()
+        B = torch.from_numpy(W.interval_uniform(rng, max(k, 1), max(n, 1), 1e-12)).cuda()
+        C = torch.full((2 * max(m, 1) * max(n, 1),), float("nan"), dtype=torch.float64,
+                       device="cuda")
+        probs.append((m, n, k, A, max(m, 1), B, max(k, 1), C, max(m, 1)))
+    batch.run(probs, pidcuda.FORM_OZAKI)
+    torch.cuda.synchronize()
+    for (m, n, k, A, lda, B, ldb, C, ldc) in probs:
+        if m == 0 or n == 0:
+            continue
+        ref = torch.empty_like(C)
+        pidcuda.mulmm_dev(m, n, k, A, lda, B, ldb, ref, ldc, pidcuda.FORM_OZAKI)
+        torch.cuda.synchronize()
+        assert torch.equal(C.view(torch.int64), ref.view(torch.int64)), (m, n, k)

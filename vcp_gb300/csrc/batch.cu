@@ -221,12 +221,20 @@ int batch_upload(int count, const BatchProblem* host_probs, void* mem, BatchDev*
 
 // One grouped launch of the plain form (reset of the counter and the
 // timestamps included), stream-ordered and capturable.
-int batch_launch_plain(const BatchDev& d, cudaStream_t s) {
-  VCPCU_CUDA_TRY(cudaMemsetAsync(d.counter, 0, sizeof(int), s));
+int batch_reset_stamps(const BatchDev& d, cudaStream_t s) {
   fill_u64<<<(d.count + 255) / 256, 256, 0, s>>>(d.t_first, d.count, ~0ULL);
   VCPCU_LAUNCH_CHECK("fill_u64");
   fill_u64<<<(d.count + 255) / 256, 256, 0, s>>>(d.t_last, d.count, 0ULL);
   VCPCU_LAUNCH_CHECK("fill_u64");
+  return VCPCU_OK;
+}
+
+int batch_launch_plain(const BatchDev& d, cudaStream_t s, bool reset = true) {
+  VCPCU_CUDA_TRY(cudaMemsetAsync(d.counter, 0, sizeof(int), s));
+  if (reset) {
+    int st = batch_reset_stamps(d, s);
+    if (st) return st;
+  }
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -248,6 +256,7 @@ __global__ void stamp(unsigned long long* p) { *p = gtimer(); }
 
 struct BatchGraph {
   int count = 0, form = 0, slices = 0;
+  OzGroupPlan* group = nullptr;  // CRT / AUTO: the grouped tensor-core products
   std::vector<BatchProblem> probs;
   std::vector<int> tiles;
   std::vector<char> ozaki;  // AUTO: problem runs in the tensor-core form
@@ -324,20 +333,47 @@ int batch_issue_ozaki(const BatchGraph& g, Branches& br, bool auto_only) {
 
 int batch_record(BatchGraph& g, cudaStream_t s) {
   if (g.form == VCPCU_FORM_PLAIN) return batch_launch_plain(g.d, s);
-  const bool auto_only = g.form == VCPCU_FORM_AUTO;
-  int nsel = 0;
-  for (int i = 0; i < g.count; ++i) nsel += auto_only ? g.ozaki[i] != 0 : 1;
+  if (g.form == VCPCU_FORM_OZAKI_SLICES) {  // product by product on forked streams
+    Branches br;
+    int st = br.fork(s, g.count < OZ_BATCH_STREAMS ? g.count : OZ_BATCH_STREAMS);
+    if (!st) st = batch_issue_ozaki(g, br, false);
+    br.join(s);
+    return st;
+  }
+  // CRT form and AUTO: the tensor-core problems as grouped products on s;
+  // AUTO's plain problems in the grouped plain launch on a forked branch
+  const bool is_auto = g.form == VCPCU_FORM_AUTO;
+  int st = batch_reset_stamps(g.d, s);
+  if (st) return st;
   Branches br;
-  int st = VCPCU_OK;
-  if (nsel > 0)
-    st = br.fork(s, nsel < OZ_BATCH_STREAMS ? nsel : OZ_BATCH_STREAMS);
-  // AUTO: the problems the cost model gives to the plain form run in the
-  // grouped launch on s (the others have zero tiles there), concurrently
-  // with the tensor-core products on the branches
-  if (!st && auto_only) st = batch_launch_plain(g.d, s);
-  if (!st && nsel > 0) st = batch_issue_ozaki(g, br, auto_only);
+  if (is_auto) {
+    if ((st = br.fork(s, 1))) {
+      br.join(s);
+      return st;
+    }
+    st = batch_launch_plain(g.d, br.side[0], false);
+  }
+  // tensor-core problems outside the groups (k == 0) one by one
+  for (int i = 0; i < g.count && !st; ++i) {
+    const BatchProblem& q = g.probs[i];
+    if (q.m <= 0 || q.n <= 0 || q.k > 0 || (is_auto && !g.ozaki[i])) continue;
+    stamp<<<1, 1, 0, s>>>(g.d.t_first + i);
+    st = igemm_any(q.m, q.n, 0, q.A, q.lda, q.B, q.ldb, q.C, q.ldc, VCPCU_FORM_OZAKI, g.slices,
+                   s);
+    stamp<<<1, 1, 0, s>>>(g.d.t_last + i);
+  }
+  if (!st && g.group) st = oz_group_record(g.group, g.d.t_first, g.d.t_last, s);
   br.join(s);
   return st;
+}
+
+// The grouped tensor-core plan of a CRT / AUTO batch (null otherwise).
+int batch_group_plan(BatchGraph& g, int persistent, cudaStream_t s) {
+  if (g.form != VCPCU_FORM_OZAKI && g.form != VCPCU_FORM_AUTO) return VCPCU_OK;
+  std::vector<char> sel;
+  if (g.form == VCPCU_FORM_AUTO) sel = g.ozaki;
+  return oz_group_plan(g.count, reinterpret_cast<const BatchProblemView*>(g.probs.data()),
+                       sel.empty() ? nullptr : sel.data(), g.slices, persistent, s, &g.group);
 }
 
 // AUTO: mark the problems the autotuner sends to the tensor-core form and
@@ -390,7 +426,10 @@ int vcpcu_igemm_batched_dev(int count, const vcpcu_problem* problems, int form, 
   Scratch mem;
   if ((st = mem.alloc(batch_state_bytes(count), s))) return st;
   if ((st = batch_upload(count, plain_view.data(), mem.ptr, &g.d, s, &g.tiles))) return st;
-  return batch_record(g, s);
+  if ((st = batch_group_plan(g, 0, s))) return st;
+  st = batch_record(g, s);
+  oz_group_free(g.group, s);
+  return st;
 }
 
 int vcpcu_batch_graph_create(int count, const vcpcu_problem* problems, int form, int slices,
@@ -417,7 +456,9 @@ int vcpcu_batch_graph_create(int count, const vcpcu_problem* problems, int form,
     delete g;
     return cuda_fail(e, "cudaMalloc(batch state)");
   }
-  if ((st = batch_upload(count, plain_view.data(), g->state, &g->d, s, &g->tiles))) {
+  if ((st = batch_upload(count, plain_view.data(), g->state, &g->d, s, &g->tiles)) ||
+      (st = batch_group_plan(*g, 1, s))) {
+    oz_group_free(g->group, s);
     cudaFree(g->state);
     delete g;
     return st;
@@ -447,6 +488,7 @@ int vcpcu_batch_graph_create(int count, const vcpcu_problem* problems, int form,
   if (st) {
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
+    oz_group_free(g->group, s);
     cudaFree(g->state);
     delete g;
     return st;
@@ -500,6 +542,7 @@ int vcpcu_batch_graph_destroy(vcpcu_batch_graph h) {
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
   if (g->state) cudaFree(g->state);
+  oz_group_free(g->group, nullptr);
   delete g;
   return VCPCU_OK;
 }

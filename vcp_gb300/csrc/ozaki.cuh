@@ -81,6 +81,12 @@ struct alignas(64) OzGemmArgs {
   int moduli[32];               // OZ_CRT: modulus of group g
   int32_t* P;                   // radius modes: fold f of a tile -> slot slot0 + f
   int slot0;
+  // grouped products: items of problem p are [gitem[p], gitem[p+1]); its
+  // tiles read rows gp[p].rowoff.. / gp[p].coloff.. of the stacked planes and
+  // write res + gp[p].res_off / P + gp[p].P_off (null gp: one product)
+  const struct OzGProb* gp;
+  const int* gitem;
+  int gnprob, gnitems;
   OzPairList pl;
 };
 
@@ -132,6 +138,8 @@ int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws);
 int oz_take_status(cudaStream_t s, int* status);
 // Merge a product's status words into the sticky device status.
 void oz_merge_status(const int* flag, cudaStream_t s);
+// ... of n products (status words 4 ints apart).
+void oz_merge_status_n(const int* flag, int n, cudaStream_t s);
 
 // dd GEMM (pddblas semantics) by the CRT form: C, Cerr as documented in
 // include/vcpcuda.h.  static_scratch != nullptr: use that device buffer of
@@ -159,6 +167,82 @@ void oz_profile_add_flops(long long f);
 // one planned product (shared by every entry point of the Ozaki form).
 int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long lda,
                    const double* B, long ldb, double* C, long ldc, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Grouped CRT-form products (a batch of uneven interval products in a few
+// launches).  Problems with the same padded inner dimension Kp form a
+// bucket; the bucket's operand planes are stacked: the rows of problem p
+// occupy rows [rowoff, rowoff + Mp) of the A planes ([plane][Mtot][Kp]) and
+// [coloff, coloff + Np) of the B planes ([plane][Ntot][Kp]); its residue
+// bytes and radius folds live at res_off / P_off of the bucket's arrays,
+// laid out as in a single product.  Every kernel of the CRT form has a
+// grouped twin that finds its problem by a binary search over a prefix
+// array of blocks or work items.
+struct OzGProb {
+  int m, n, k;
+  const double* A;
+  long lda;
+  const double* B;
+  long ldb;
+  double* C;
+  long ldc;
+  int Mp, Np, L, w;
+  int rowoff, coloff;          // stacked rows of the bucket's A / B planes
+  int tiles_m, tiles_n;
+  long long res_off, P_off;    // element offsets into the bucket's res / P
+  int orig;                    // index in the caller's problem table
+  uint32_t Q[16][4];           // CRT basis of this problem's L moduli
+  uint32_t Mlimb[4];
+  float invMf;                 // 2^64 / M rounded to float
+};
+
+// Device view of one bucket (all pointers device memory).
+struct OzGBucket {
+  int nprob, Kp, Lmax, Mtot, Ntot;
+  const OzGProb* probs;
+  const int* blk_rowmax;   // [nprob + 1] prefix of rowmax blocks
+  const int* blk_split;    // [nprob + 1] prefix of split_left blocks
+  const int* item_rad;     // [nprob + 1] prefix of radius work items (groups x tiles)
+  const int* item_crt;     // [nprob + 1] prefix of residue work items (L x tiles)
+  const int* blk_asm;      // [nprob + 1] prefix of reassembly blocks
+  const int* col_prob;     // [Ntot] problem of each stacked B column
+  uint16_t* planesA;       // [Lmax + 4][Mtot][Kp]: residues, |mA|+rA digits, rA digits
+  uint16_t* planesB;       // [Lmax + 4][Ntot][Kp]: residues, rB digits, |mB| digits
+  unsigned long long* rowmax;  // [Mtot][3]
+  int* E3;                 // [Mtot][3]
+  int* F2;                 // [Ntot][2]
+  double* beta;            // [Ntot]
+  unsigned long long* asum;  // [Mtot][2]
+  uint8_t* res;
+  int32_t* P;
+  int* flag;               // [nprob][4]: non-finite input, wait timeout
+  unsigned long long* t_first;  // per caller problem (may be null)
+  unsigned long long* t_last;
+};
+
+// Kernels of the grouped form (ozaki_split.cu, ozaki_gemm.cu, ozaki_crt.cu).
+int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, cudaStream_t st);
+int oz_grun_gemm(const OzGBucket& b, const OzPlan& shape, int mode, int nitems,
+                 cudaStream_t st);
+int oz_gassemble(const OzGBucket& b, const OzRadConst& rc, int nblk, cudaStream_t st);
+// The grouped CRT-form product of a batch (batch.cu's tensor-core path).
+// oz_group_plan builds the buckets and uploads their tables (outside any
+// stream capture); oz_group_record launches the kernels of every bucket on
+// one stream (capturable); oz_group_free releases the plan.  With
+// persistent != 0 the device memory comes from cudaMalloc (kept for graph
+// replays), else from the stream-ordered allocator of `s`.
+struct BatchProblemView {
+  int m, n, k, lda, ldb, ldc;
+  const double* A;
+  const double* B;
+  double* C;
+};
+struct OzGroupPlan;
+int oz_group_plan(int count, const BatchProblemView* problems, const char* select, int slices,
+                  int persistent, cudaStream_t s, OzGroupPlan** out);
+int oz_group_record(OzGroupPlan* g, unsigned long long* t_first, unsigned long long* t_last,
+                    cudaStream_t s);
+void oz_group_free(OzGroupPlan* g, cudaStream_t s);
 
 // point_mask as OzPlan::point_mask (the caller guarantees the zero radii).
 int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,

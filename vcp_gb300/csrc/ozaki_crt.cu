@@ -140,13 +140,14 @@ __device__ __forceinline__ void big_to_dir(const uint32_t* mag, int neg, int e, 
 // Exact X = (A'B')(i, j) from its residues (see the file comment); returns
 // the magnitude in mag[4] and the sign.
 // c[l] = 0 and Q_l = 0 for l >= L.
-__device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const CrtConst& cc,
+__device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const uint32_t (&Q)[16][4],
+                                         const uint32_t (&Mm)[4], float invMf,
                                          uint32_t (&mag)[4]) {
   unsigned long long s[4] = {0, 0, 0, 0};
 #pragma unroll
   for (int l = 0; l < 16; ++l) {
 #pragma unroll
-    for (int t = 0; t < 4; ++t) s[t] += (unsigned long long)c[l] * cc.Q[l][t];
+    for (int t = 0; t < 4; ++t) s[t] += (unsigned long long)c[l] * Q[l][t];
   }
   uint32_t r[5];
   unsigned long long carry = 0;
@@ -162,12 +163,12 @@ __device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const CrtConst
   const float Sf = __uint2float_rn(r[4]) * 0x1p64f + __uint2float_rn(r[3]) * 0x1p32f +
                    __uint2float_rn(r[2]) + __uint2float_rn(r[1]) * 0x1p-32f +
                    __uint2float_rn(r[0]) * 0x1p-64f;
-  const unsigned int q = (unsigned int)(Sf * cc.invMf);
+  const unsigned int q = (unsigned int)(Sf * invMf);
   if (q) {
     unsigned long long qm[5];
     unsigned long long c2 = 0;
     for (int t = 0; t < 4; ++t) {
-      const unsigned long long v = (unsigned long long)q * cc.M[t] + c2;
+      const unsigned long long v = (unsigned long long)q * Mm[t] + c2;
       qm[t] = (uint32_t)v;
       c2 = v >> 32;
     }
@@ -179,11 +180,11 @@ __device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const CrtConst
       borrow = (d >> 63) & 1ULL;
     }
     for (int it = 0; it < 4 && borrow; ++it) {  // q was too large
-      add_M(r, cc.M);
+      add_M(r, Mm);
       borrow = (r[4] >> 31) & 1u;  // still negative (two's complement in 5 limbs)
     }
   }
-  for (int it = 0; it < 4 && ge_M(r, cc.M); ++it) sub_M(r, cc.M);
+  for (int it = 0; it < 4 && ge_M(r, Mm); ++it) sub_M(r, Mm);
   // centre: X = r if 2r < M, else r - M (magnitude M - r)
   uint32_t twice[5];
   unsigned long long cy = 0;
@@ -192,10 +193,10 @@ __device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const CrtConst
     twice[t] = (uint32_t)v;
     cy = v >> 32;
   }
-  if (ge_M(twice, cc.M)) {
+  if (ge_M(twice, Mm)) {
     unsigned long long b = 0;
     for (int t = 0; t < 4; ++t) {
-      const unsigned long long d = (unsigned long long)cc.M[t] - r[t] - b;
+      const unsigned long long d = (unsigned long long)Mm[t] - r[t] - b;
       mag[t] = (uint32_t)d;
       b = (d >> 63) & 1ULL;
     }
@@ -277,7 +278,64 @@ oz_radius_T_kernel(int M, int N, int Mp, size_t plane, const int32_t* __restrict
 // One thread per 4 consecutive rows of one column: the residue planes are
 // read 4 bytes at a time, the radius folds 16 bytes, C written as 4
 // consecutive pairs.  Only the final error sum and the two outward roundings
-// use the FP64 pipe on the common path.
+// use the FP64 pipe on the common path.  E3, F2, asum, beta, res and P point
+// at row / column 0 of this product; plane = Np Mp of its layout.
+__device__ __forceinline__ void assemble_quad(
+    int i0, int j, int M, int Mp, int L, int w, const uint8_t* __restrict__ res, size_t plane,
+    const int* __restrict__ E3, const int* __restrict__ F2,
+    const unsigned long long* __restrict__ asum, const double* __restrict__ beta,
+    const int32_t* __restrict__ P, double* __restrict__ C, long ldc, bool nonfinite,
+    const uint32_t (&Q)[16][4], const uint32_t (&Mm)[4], float invMf, const OzRadConst& rc) {
+  const size_t e0 = (size_t)j * Mp + i0;
+  const int Fj = F2[2 * j], Frj = F2[2 * j + 1];
+  const double bj = beta[j];
+  uint32_t pk[16];
+#pragma unroll
+  for (int l = 0; l < 16; ++l)
+    pk[l] = l < L ? *reinterpret_cast<const uint32_t*>(res + (size_t)l * plane + e0) : 0u;
+  long long W1[4], W2[4];
+  rad_folds(P, plane, e0, rc, W1, W2);
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int i = i0 + u;
+    if (i >= M) break;
+    const int Ei = E3[3 * i];
+    double lo = 0.0, up = 0.0, tr = 0.0;
+    if (Ei != OZ_ZERO_EXP && Fj != OZ_ZERO_EXP) {
+      uint32_t c[16], mag[4];
+#pragma unroll
+      for (int l = 0; l < 16; ++l) c[l] = (pk[l] >> (8 * u)) & 0xffu;
+      const int neg = crt_value(c, Q, Mm, invMf, mag);
+      big_to_dir(mag, neg, Ei + Fj - 2 * w, lo, up);
+      // truncation bound: sA = RU(asum_hi 2^32 + asum_lo) (exact below 2^96)
+      const unsigned long long ah = asum[2 * i + 0], al = asum[2 * i + 1];
+      const unsigned __int128 sx = ((unsigned __int128)ah << 32) + al;
+      double sA = 0.0, sAdn;
+      if (sx) {
+        const unsigned long long hi64 = (unsigned long long)(sx >> 64);
+        if (hi64 == 0) {
+          u64_to_dir((unsigned long long)sx, 0, sAdn, sA);
+        } else {
+          const int sh = 64 - __clzll(hi64);
+          unsigned long long t = (unsigned long long)(sx >> sh);
+          if ((unsigned long long)sx & ((1ULL << sh) - 1)) t |= 1ULL;
+          u64_to_dir(t, sh, sAdn, sA);
+        }
+      }
+      const double t1 = scale_pow2(bj, Ei - w - 1, true);
+      const double t2 = scale_pow2(sA, Ei + Fj - 2 * w - 1, true);
+      tr = __dadd_ru(t1, t2);
+    }
+    const double Tu = rad_T(W1[u], W2[u], E3[3 * i + 1], E3[3 * i + 2], Fj, Frj, rc);
+    const double err = __dadd_ru(tr, Tu);
+    double clo = __dsub_rd(lo, err), cup = __dadd_ru(up, err);
+    if (nonfinite) clo = cup = __longlong_as_double(0x7ff8000000000000LL);
+    double* cp = C + 2 * ((size_t)i + (size_t)j * ldc);  // C may be only 8-byte aligned
+    cp[0] = clo;
+    cp[1] = cup;
+  }
+}
+
 __global__ void __launch_bounds__(256)
 oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __restrict__ res,
                        size_t plane, const int* __restrict__ E3, const int* __restrict__ F2,
@@ -289,55 +347,44 @@ oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __rest
   const int Mq = (M + 3) >> 2;
   const long total = (long)Mq * N;
   for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long)gridDim.x * blockDim.x) {
-    const int i0 = 4 * (int)(idx % Mq), j = (int)(idx / Mq);
-    const size_t e0 = (size_t)j * Mp + i0;
-    const int Fj = F2[2 * j], Frj = F2[2 * j + 1];
-    const double bj = beta[j];
-    uint32_t pk[16];
-#pragma unroll
-    for (int l = 0; l < 16; ++l)
-      pk[l] = l < L ? *reinterpret_cast<const uint32_t*>(res + (size_t)l * plane + e0) : 0u;
-    long long W1[4], W2[4];
-    rad_folds(P, plane, e0, rc, W1, W2);
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int i = i0 + u;
-      if (i >= M) break;
-      const int Ei = E3[3 * i];
-      double lo = 0.0, up = 0.0, tr = 0.0;
-      if (Ei != OZ_ZERO_EXP && Fj != OZ_ZERO_EXP) {
-        uint32_t c[16], mag[4];
-#pragma unroll
-        for (int l = 0; l < 16; ++l) c[l] = (pk[l] >> (8 * u)) & 0xffu;
-        const int neg = crt_value(c, cc, mag);
-        big_to_dir(mag, neg, Ei + Fj - 2 * w, lo, up);
-        // truncation bound: sA = RU(asum_hi 2^32 + asum_lo) (exact below 2^96)
-        const unsigned long long ah = asum[2 * i + 0], al = asum[2 * i + 1];
-        const unsigned __int128 sx = ((unsigned __int128)ah << 32) + al;
-        double sA = 0.0, sAdn;
-        if (sx) {
-          const unsigned long long hi64 = (unsigned long long)(sx >> 64);
-          if (hi64 == 0) {
-            u64_to_dir((unsigned long long)sx, 0, sAdn, sA);
-          } else {
-            const int sh = 64 - __clzll(hi64);
-            unsigned long long t = (unsigned long long)(sx >> sh);
-            if ((unsigned long long)sx & ((1ULL << sh) - 1)) t |= 1ULL;
-            u64_to_dir(t, sh, sAdn, sA);
-          }
-        }
-        const double t1 = scale_pow2(bj, Ei - w - 1, true);
-        const double t2 = scale_pow2(sA, Ei + Fj - 2 * w - 1, true);
-        tr = __dadd_ru(t1, t2);
-      }
-      const double Tu = rad_T(W1[u], W2[u], E3[3 * i + 1], E3[3 * i + 2], Fj, Frj, rc);
-      const double err = __dadd_ru(tr, Tu);
-      double clo = __dsub_rd(lo, err), cup = __dadd_ru(up, err);
-      if (nonfinite) clo = cup = __longlong_as_double(0x7ff8000000000000LL);
-      double* cp = C + 2 * ((size_t)i + (size_t)j * ldc);  // C may be only 8-byte aligned
-      cp[0] = clo;
-      cp[1] = cup;
+       idx += (long)gridDim.x * blockDim.x)
+    assemble_quad(4 * (int)(idx % Mq), (int)(idx / Mq), M, Mp, L, w, res, plane, E3, F2, asum,
+                  beta, P, C, ldc, nonfinite, cc.Q, cc.M, cc.invMf, rc);
+}
+
+__device__ __forceinline__ int gfind(const int* __restrict__ prefix, int nprob, int x) {
+  int lo = 0, hi = nprob - 1;  // largest p with prefix[p] <= x
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= x)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// Grouped reassembly: each block works on one problem (blk_asm prefix);
+// every block stamps the problem's end.  A device-wait timeout of the slice
+// GEMM (flag[1] of problem 0) poisons every output of the bucket.
+__global__ void __launch_bounds__(256)
+oz_crt_assemble_g(const __grid_constant__ OzGBucket b, const __grid_constant__ OzRadConst rc) {
+  const int p = gfind(b.blk_asm, b.nprob, blockIdx.x);
+  const OzGProb& q = b.probs[p];
+  const int Mq = (q.m + 3) >> 2;
+  const long idx = (long)(blockIdx.x - b.blk_asm[p]) * blockDim.x + threadIdx.x;
+  const bool nonfinite = b.flag[4 * p] != 0 || b.flag[1] != 0;
+  if (idx < (long)Mq * q.n)
+    assemble_quad(4 * (int)(idx % Mq), (int)(idx / Mq), q.m, q.Mp, q.L, q.w, b.res + q.res_off,
+                  (size_t)q.Np * q.Mp, b.E3 + 3 * (size_t)q.rowoff, b.F2 + 2 * (size_t)q.coloff,
+                  b.asum + 2 * (size_t)q.rowoff, b.beta + q.coloff, b.P + q.P_off, q.C, q.ldc,
+                  nonfinite, q.Q, q.Mlimb, q.invMf, rc);
+  if (b.t_last) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long t;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+      atomicMax(&b.t_last[q.orig], t);
     }
   }
 }
@@ -363,6 +410,13 @@ int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long l
       pb.M, pb.N, pb.Mp, pb.L, pb.w, ws.res, (size_t)pb.Np * pb.Mp, ws.E3, ws.F2, ws.asum,
       ws.beta, ws.P, C, ldc, ws.flag, cc, oz_rad_const(plan));
   VCPCU_LAUNCH_CHECK("oz_crt_assemble_kernel");
+  return VCPCU_OK;
+}
+
+int oz_gassemble(const OzGBucket& b, const OzRadConst& rc, int nblk, cudaStream_t st) {
+  if (nblk <= 0) return VCPCU_OK;
+  oz_crt_assemble_g<<<nblk, 256, 0, st>>>(b, rc);
+  VCPCU_LAUNCH_CHECK("oz_crt_assemble_g");
   return VCPCU_OK;
 }
 

@@ -92,19 +92,63 @@ __device__ __forceinline__ void tile_coords(int tile, int tiles_m, int tiles_n, 
 // accumulate into one W).  CRT and radius modes: one item per (group, tile),
 // group-major -- every group writes its own residue plane or fold slots, so
 // items are independent, and the CTAs in flight share one group's planes
-// (compact L2 working set; the tail is one group of one tile).
-__device__ __forceinline__ void item_coords(const OzGemmArgs& a, int item, int ntiles, int& tm,
-                                            int& tn, int& g0, int& g1) {
+// (compact L2 working set; the tail is one group of one tile).  Grouped
+// products: the items of problem p follow one another, group-major within p.
+struct ItemInfo {
+  int arow, bcol;   // TMA row of the A tile / of the B tile in the planes
+  int tm, tn, g0, g1;
+  int Mp, Np;       // output layout of this item's problem
+  uint8_t* res;
+  int32_t* P;
+};
+
+__device__ __forceinline__ int gfind_item(const int* __restrict__ prefix, int nprob, int x) {
+  int lo = 0, hi = nprob - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= x)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ ItemInfo item_info(const OzGemmArgs& a, int item, int ntiles) {
+  ItemInfo f;
+  if (a.gp) {
+    const int p = gfind_item(a.gitem, a.gnprob, item);
+    const OzGProb& q = a.gp[p];
+    const int nt = q.tiles_m * q.tiles_n;
+    const int local = item - a.gitem[p];
+    f.g0 = local / nt;
+    f.g1 = f.g0 + 1;
+    tile_coords(local - f.g0 * nt, q.tiles_m, q.tiles_n, f.tm, f.tn);
+    f.arow = q.rowoff + f.tm * OZ_BM;
+    f.bcol = q.coloff + f.tn * OZ_BN;
+    f.Mp = q.Mp;
+    f.Np = q.Np;
+    f.res = a.res ? a.res + q.res_off : nullptr;
+    f.P = a.P ? a.P + q.P_off : nullptr;
+    return f;
+  }
   int tile = item;
   if (a.mode == OZ_MID) {
-    g0 = 0;
-    g1 = a.pl.ngroups;
+    f.g0 = 0;
+    f.g1 = a.pl.ngroups;
   } else {
-    g0 = item / ntiles;
-    g1 = g0 + 1;
-    tile = item - g0 * ntiles;
+    f.g0 = item / ntiles;
+    f.g1 = f.g0 + 1;
+    tile = item - f.g0 * ntiles;
   }
-  tile_coords(tile, a.tiles_m, a.tiles_n, tm, tn);
+  tile_coords(tile, a.tiles_m, a.tiles_n, f.tm, f.tn);
+  f.arow = f.tm * OZ_BM;
+  f.bcol = f.tn * OZ_BN;
+  f.Mp = a.Mp;
+  f.Np = a.Np;
+  f.res = a.res;
+  f.P = a.P;
+  return f;
 }
 
 __device__ __forceinline__ long long shift_t(int c, int sh) {
@@ -120,7 +164,8 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = args.tiles_m * args.tiles_n;
-  const int nitems = args.mode == OZ_MID ? ntiles : ntiles * args.pl.ngroups;
+  const int nitems = args.gp ? args.gnitems
+                             : (args.mode == OZ_MID ? ntiles : ntiles * args.pl.ngroups);
   const int nchunks = (args.Kp + OZ_CHUNK - 1) / OZ_CHUNK;
   const int kblocks = args.Kp / OZ_BK;
   const long long lim = args.timeout_cycles;
@@ -157,9 +202,8 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
       bool ok = true;
       uint32_t used = 0, lastpar = 0;  // per-stage bit masks
       for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
-        int tm, tn, g0, g1;
-        item_coords(args, item, ntiles, tm, tn, g0, g1);
-        for (int pi = args.pl.gstart[g0]; pi < args.pl.gstart[g1] && ok; ++pi) {
+        const ItemInfo f = item_info(args, item, ntiles);
+        for (int pi = args.pl.gstart[f.g0]; pi < args.pl.gstart[f.g1] && ok; ++pi) {
           const int pa = args.pl.pa[pi], pb = args.pl.pb[pi];
           for (int kb = 0; kb < kblocks; ++kb) {
             if (*(volatile int*)&sm.abort || !ptx::mbar_wait(&sm.empty[stage], phase ^ 1, lim)) {
@@ -170,8 +214,8 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
             uint8_t* sA = dsmem + stage * STAGE_BYTES;
             uint8_t* sB = sA + A_STAGE;
             ptx::mbar_expect_tx(&sm.full[stage], STAGE_BYTES);
-            ptx::tma_load_3d(sA, &args.tmA, &sm.full[stage], kb * OZ_BK, tm * OZ_BM, pa);
-            ptx::tma_load_3d(sB, &args.tmB, &sm.full[stage], kb * OZ_BK, tn * OZ_BN, pb);
+            ptx::tma_load_3d(sA, &args.tmA, &sm.full[stage], kb * OZ_BK, f.arow, pa);
+            ptx::tma_load_3d(sB, &args.tmB, &sm.full[stage], kb * OZ_BK, f.bcol, pb);
             used |= 1u << stage;
             lastpar = (lastpar & ~(1u << stage)) | (phase << stage);
             if (++stage == OZ_STAGES) {
@@ -194,9 +238,8 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
       uint32_t acc = 0;  // global chunk counter
       bool ok = true;
       for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
-        int tm, tn, g0, g1;
-        item_coords(args, item, ntiles, tm, tn, g0, g1);
-        for (int pi = args.pl.gstart[g0]; pi < args.pl.gstart[g1] && ok; ++pi) {
+        const ItemInfo f = item_info(args, item, ntiles);
+        for (int pi = args.pl.gstart[f.g0]; pi < args.pl.gstart[f.g1] && ok; ++pi) {
           for (int ch = 0; ch < nchunks && ok; ++ch, ++acc) {
             const int buf = acc & 1;
             const uint32_t par = (acc >> 1) & 1;
@@ -250,10 +293,10 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
     bool ok = true;
     bool nonfinite = args.flag[0] != 0;
     for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
-      int tm, tn, g0, g1;
-      item_coords(args, item, ntiles, tm, tn, g0, g1);
-      const int gi = tm * OZ_BM + row_in_tile;
-      const int gj0 = tn * OZ_BN + half * 128;
+      const ItemInfo f = item_info(args, item, ntiles);
+      const int g0 = f.g0, g1 = f.g1;
+      const int gi = f.tm * OZ_BM + row_in_tile;
+      const int gj0 = f.tn * OZ_BN + half * 128;
       bool have_w = false;
       // radius modes: slot of the next fold = folds of the earlier groups
       int fold = 0;
@@ -296,7 +339,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
             // in res[g][col][row], adding to an earlier fold of the group
             const uint32_t m = (uint32_t)args.moduli[g];
             const uint32_t mg = 0xFFFFFFFFu / m;
-            uint8_t* rp = args.res + (size_t)g * args.Np * args.Mp + (size_t)gj0 * args.Mp + gi;
+            uint8_t* rp = f.res + (size_t)g * f.Np * f.Mp + (size_t)gj0 * f.Mp + gi;
             const bool first = cnt == idx + 1;  // no earlier fold in this group
 #pragma unroll
             for (int e = 0; e < 128; ++e) {
@@ -307,20 +350,20 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
               if (r >= m) r -= m;
               if (v < 0 && r) r = m - r;
               if (!first) {
-                r += rp[(size_t)e * args.Mp];
+                r += rp[(size_t)e * f.Mp];
                 if (r >= m) r -= m;
               }
-              rp[(size_t)e * args.Mp] = (uint8_t)r;
+              rp[(size_t)e * f.Mp] = (uint8_t)r;
               c[e] = 0;
             }
             cnt = 0;
           } else if ((cnt == OZ_FOLD_CHUNKS || last_of_group) && args.mode != OZ_MID) {
             // radius modes: the fold is stored, never read back here -- the
             // reassembly combines the slots (no load stalls the drain)
-            int32_t* pp = args.P + ((size_t)(args.slot0 + fold) * args.Np + gj0) * args.Mp + gi;
+            int32_t* pp = f.P + ((size_t)(args.slot0 + fold) * f.Np + gj0) * f.Mp + gi;
 #pragma unroll
             for (int e = 0; e < 128; ++e) {
-              pp[(size_t)e * args.Mp] = c[e];
+              pp[(size_t)e * f.Mp] = c[e];
               c[e] = 0;
             }
             ++fold;
@@ -496,6 +539,62 @@ int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, 
   a.timeout_cycles = 4000000000LL;  // about 2 s at 2 GHz
   const int ntiles = a.tiles_m * a.tiles_n;
   const int nitems = mode == OZ_MID ? ntiles : ntiles * a.pl.ngroups;
+  const int grid = nitems < num_sms() ? nitems : num_sms();
+  oz_slice_gemm_kernel<<<grid, NTHREADS, oz_dyn_smem(), st>>>(a);
+  VCPCU_LAUNCH_CHECK("oz_slice_gemm_kernel");
+  return VCPCU_OK;
+}
+
+// One launch of the slice GEMM over all problems of a bucket: radius product
+// 1 (OZ_RAD_SET), 2 (OZ_RAD_ADD) or the residue GEMMs (OZ_CRT).  `shape`
+// supplies the pair lists (radius digit pairs, Lmax moduli), the fold count
+// and the padded inner dimension shared by the bucket.
+int oz_grun_gemm(const OzGBucket& b, const OzPlan& shape, int mode, int nitems, cudaStream_t st) {
+  if (nitems <= 0) return VCPCU_OK;
+  static bool attr_set = false;
+  if (!attr_set) {
+    VCPCU_CUDA_TRY(cudaFuncSetAttribute(oz_slice_gemm_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)oz_dyn_smem()));
+    attr_set = true;
+  }
+  OzGemmArgs a;
+  memset(&a, 0, sizeof(a));
+  const size_t psA = (size_t)b.Mtot * b.Kp, psB = (size_t)b.Ntot * b.Kp;
+  const uint16_t* ap;
+  const uint16_t* bp;
+  int apl, bpl;
+  if (mode == OZ_RAD_SET) {  // (|mA| + rA) * rB
+    ap = b.planesA + (size_t)b.Lmax * psA;
+    bp = b.planesB + (size_t)b.Lmax * psB;
+    apl = bpl = 2;
+    a.pl = shape.rad;
+  } else if (mode == OZ_RAD_ADD) {  // rA * |mB|
+    ap = b.planesA + (size_t)(b.Lmax + 2) * psA;
+    bp = b.planesB + (size_t)(b.Lmax + 2) * psB;
+    apl = bpl = 2;
+    a.pl = shape.rad;
+  } else {
+    ap = b.planesA;
+    bp = b.planesB;
+    apl = bpl = b.Lmax;
+    a.pl = shape.crt;
+    a.res = b.res;
+    for (int l = 0; l < b.Lmax; ++l) a.moduli[l] = OZ_MODULI[l];
+  }
+  int st_;
+  if ((st_ = make_tmap(&a.tmA, ap, b.Kp, b.Mtot, apl, OZ_BM))) return st_;
+  if ((st_ = make_tmap(&a.tmB, bp, b.Kp, b.Ntot, bpl, OZ_BN))) return st_;
+  a.Kp = b.Kp;
+  a.mode = mode;
+  a.P = b.P;
+  a.slot0 = mode == OZ_RAD_ADD ? shape.rad_slots : 0;
+  a.flag = b.flag;  // problem 0's status words take the (global) timeout bit
+  a.timeout_cycles = 4000000000LL;  // about 2 s at 2 GHz
+  a.gp = b.probs;
+  a.gitem = mode == OZ_CRT ? b.item_crt : b.item_rad;
+  a.gnprob = b.nprob;
+  a.gnitems = nitems;
   const int grid = nitems < num_sms() ? nitems : num_sms();
   oz_slice_gemm_kernel<<<grid, NTHREADS, oz_dyn_smem(), st>>>(a);
   VCPCU_LAUNCH_CHECK("oz_slice_gemm_kernel");

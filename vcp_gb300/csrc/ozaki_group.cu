@@ -1,0 +1,319 @@
+// ozaki_group.cu -- grouped CRT-form interval products (the tensor-core path
+// of a batch of uneven products, vcpcu_igemm_batched_dev / the batch
+// graphs).
+//
+// The problems of a batch are bucketed by their padded inner dimension Kp.
+// A bucket runs in nine launches whatever its size: row maxima, exponents,
+// left and right splits, the two radius slice GEMMs, the residue slice GEMM,
+// the reassembly and the status merge -- each a grouped twin of the
+// single-product kernel that finds its problem by a binary search over a
+// prefix array of blocks or work items (the slice GEMM's work items are the
+// (problem, group, tile) triples of the bucket).  The results are bit for
+// bit those of one vcpcu_igemm_dev call per problem: the same plan (w, L,
+// moduli, digit pairs, folds) and the same arithmetic per entry.  Buckets
+// run one after another on the stream and share one workspace (the largest
+// bucket's); their tables (problem descriptors, prefix arrays) are built on
+// the host and uploaded once by oz_group_plan.
+#include "common.cuh"
+#include "ozaki.cuh"
+#include "ozaki_common.cuh"
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+namespace vcpcu {
+
+namespace {
+
+size_t al256g(size_t x) { return (x + 255) & ~(size_t)255; }
+
+__global__ void g_init_stamps(const OzGProb* probs, int n, unsigned long long* t_first,
+                              unsigned long long* t_last) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    t_first[probs[p].orig] = ~0ULL;
+    t_last[probs[p].orig] = 0ULL;
+  }
+}
+
+struct BucketHost {
+  OzGBucket dev;  // table pointers set at plan time, workspace pointers at record time
+  OzPlan shape;   // radius pair list, Lmax-modulus pair list, fold count
+  OzRadConst rc;
+  int nblk_rowmax = 0, nblk_split = 0, nitem_rad = 0, nitem_crt = 0, nblk_asm = 0;
+  // workspace layout (byte offsets; the first zero_bytes are cleared per run)
+  size_t offRowmax = 0, offAsum = 0, offFlag = 0, zero_bytes = 0;
+  size_t offE3 = 0, offF2 = 0, offBeta = 0, offA = 0, offB = 0, offRes = 0, offP = 0;
+  size_t ws_bytes = 0;
+};
+
+}  // namespace
+
+struct OzGroupPlan {
+  std::vector<BucketHost> buckets;
+  void* tables = nullptr;
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  int persistent = 0;
+};
+
+int oz_group_plan(int count, const BatchProblemView* problems, const char* select, int slices,
+                  int persistent, cudaStream_t s, OzGroupPlan** out) {
+  *out = nullptr;
+  const int nslices = slices > 0 ? slices : 8;
+  // bucket the selected problems by Kp
+  std::map<int, std::vector<int>> byKp;
+  std::vector<OzPlan> plans(count);
+  for (int i = 0; i < count; ++i) {
+    const BatchProblemView& q = problems[i];
+    if ((select && !select[i]) || q.m <= 0 || q.n <= 0 || q.k <= 0) continue;
+    oz_make_plan(q.m, q.n, q.k, nslices, 2, &plans[i], 1);
+    byKp[plans[i].pb.Kp].push_back(i);
+  }
+  OzGroupPlan* g = new OzGroupPlan();
+  g->persistent = persistent;
+  std::vector<uint8_t> host;  // all tables, each part 256-byte aligned
+  auto reserve = [&](size_t bytes) {
+    const size_t off = al256g(host.size());
+    host.resize(off + bytes);
+    return off;
+  };
+  struct Offs { size_t probs, brow, bspl, irad, icrt, basm, cols; };
+  std::vector<Offs> toff;
+  for (auto& kv : byKp) {
+    const std::vector<int>& ids = kv.second;
+    const int n = (int)ids.size();
+    BucketHost b;
+    memset(&b.dev, 0, sizeof(b.dev));
+    const OzPlan& p0 = plans[ids[0]];
+    b.shape = p0;
+    b.dev.nprob = n;
+    b.dev.Kp = kv.first;
+    int Lmax = 0;
+    long long Mtot = 0, Ntot = 0;
+    for (int id : ids) {
+      Lmax = std::max(Lmax, plans[id].pb.L);
+      Mtot += plans[id].pb.Mp;
+      Ntot += plans[id].pb.Np;
+    }
+    // every modulus a group of its own, Lmax of them (a problem uses its first L)
+    OzPairList& crt = b.shape.crt;
+    memset(&crt, 0, sizeof(crt));
+    for (int l = 0; l < Lmax; ++l) {
+      crt.pa[l] = crt.pb[l] = (int8_t)l;
+      crt.gstart[l] = (int16_t)l;
+      crt.gt[l] = (int8_t)l;
+    }
+    crt.gstart[Lmax] = (int16_t)Lmax;
+    crt.npairs = crt.ngroups = Lmax;
+    b.shape.point_mask = 0;
+    b.rc = oz_rad_const(b.shape);
+    b.dev.Lmax = Lmax;
+    Offs o;
+    o.probs = reserve(sizeof(OzGProb) * n);
+    o.brow = reserve(sizeof(int) * (n + 1));
+    o.bspl = reserve(sizeof(int) * (n + 1));
+    o.irad = reserve(sizeof(int) * (n + 1));
+    o.icrt = reserve(sizeof(int) * (n + 1));
+    o.basm = reserve(sizeof(int) * (n + 1));
+    o.cols = reserve(sizeof(int) * (size_t)Ntot);
+    long long brow = 0, bspl = 0, irad = 0, icrt = 0, basm = 0, res = 0, P = 0;
+    int rowoff = 0, coloff = 0;
+    for (int t = 0; t < n; ++t) {
+      const int id = ids[t];
+      const BatchProblemView& q = problems[id];
+      const OzPlan& pl = plans[id];
+      OzGProb gp;
+      memset(&gp, 0, sizeof(gp));
+      gp.m = q.m;
+      gp.n = q.n;
+      gp.k = q.k;
+      gp.A = q.A;
+      gp.lda = q.lda;
+      gp.B = q.B;
+      gp.ldb = q.ldb;
+      gp.C = q.C;
+      gp.ldc = q.ldc;
+      gp.Mp = pl.pb.Mp;
+      gp.Np = pl.pb.Np;
+      gp.L = pl.pb.L;
+      gp.w = pl.pb.w;
+      gp.rowoff = rowoff;
+      gp.coloff = coloff;
+      gp.tiles_m = pl.pb.Mp / OZ_BM;
+      gp.tiles_n = pl.pb.Np / OZ_BN;
+      gp.res_off = res;
+      gp.P_off = P;
+      gp.orig = id;
+      for (int l = 0; l < 16; ++l)
+        for (int c = 0; c < 4; ++c) gp.Q[l][c] = l < pl.pb.L ? pl.Q[l][c] : 0u;
+      for (int c = 0; c < 4; ++c) gp.Mlimb[c] = pl.Mlimb[c];
+      const double Md = (double)pl.Mlimb[3] * 0x1p96 + (double)pl.Mlimb[2] * 0x1p64 +
+                        (double)pl.Mlimb[1] * 0x1p32 + (double)pl.Mlimb[0];
+      gp.invMf = (float)(0x1p64 / Md);
+      memcpy(host.data() + o.probs + sizeof(OzGProb) * t, &gp, sizeof(gp));
+      int* v;
+      v = (int*)(host.data() + o.brow); v[t] = (int)brow;
+      v = (int*)(host.data() + o.bspl); v[t] = (int)bspl;
+      v = (int*)(host.data() + o.irad); v[t] = (int)irad;
+      v = (int*)(host.data() + o.icrt); v[t] = (int)icrt;
+      v = (int*)(host.data() + o.basm); v[t] = (int)basm;
+      int* cols = (int*)(host.data() + o.cols);
+      for (int j = 0; j < gp.Np; ++j) cols[coloff + j] = t;
+      const long long tiles = (long long)gp.tiles_m * gp.tiles_n;
+      brow += (long long)((q.m + 31) / 32) * ((q.k + 255) / 256);
+      bspl += (long long)(kv.first / 64) * (gp.Mp / 32);
+      irad += b.shape.rad.ngroups * tiles;
+      icrt += gp.L * tiles;
+      basm += (((long long)(q.m + 3) / 4) * q.n + 255) / 256;
+      res += (long long)gp.L * gp.Np * gp.Mp;
+      P += 2LL * b.shape.rad_slots * gp.Np * gp.Mp;
+      rowoff += gp.Mp;
+      coloff += gp.Np;
+    }
+    if (std::max({brow, bspl, irad, icrt, basm}) >= INT_MAX || Mtot >= INT_MAX ||
+        Ntot >= INT_MAX) {
+      delete g;
+      set_error("igemm_batched: the tensor-core batch is too large for one group");
+      return VCPCU_ERR_INVALID_ARG;
+    }
+    int* v;
+    v = (int*)(host.data() + o.brow); v[n] = (int)brow;
+    v = (int*)(host.data() + o.bspl); v[n] = (int)bspl;
+    v = (int*)(host.data() + o.irad); v[n] = (int)irad;
+    v = (int*)(host.data() + o.icrt); v[n] = (int)icrt;
+    v = (int*)(host.data() + o.basm); v[n] = (int)basm;
+    b.nblk_rowmax = (int)brow;
+    b.nblk_split = (int)bspl;
+    b.nitem_rad = (int)irad;
+    b.nitem_crt = (int)icrt;
+    b.nblk_asm = (int)basm;
+    b.dev.Mtot = (int)Mtot;
+    b.dev.Ntot = (int)Ntot;
+    // workspace layout
+    size_t w = 0;
+    auto take = [&](size_t bytes) {
+      const size_t off = w;
+      w = al256g(w + bytes);
+      return off;
+    };
+    b.offRowmax = take(sizeof(unsigned long long) * 3 * Mtot);
+    b.offAsum = take(sizeof(unsigned long long) * 2 * Mtot);
+    b.offFlag = take(sizeof(int) * 4 * (size_t)n);
+    b.zero_bytes = w;
+    b.offE3 = take(sizeof(int) * 3 * Mtot);
+    b.offF2 = take(sizeof(int) * 2 * Ntot);
+    b.offBeta = take(sizeof(double) * Ntot);
+    b.offA = take(sizeof(uint16_t) * (size_t)(Lmax + 4) * Mtot * kv.first);
+    b.offB = take(sizeof(uint16_t) * (size_t)(Lmax + 4) * Ntot * kv.first);
+    b.offRes = take((size_t)res);
+    b.offP = take(sizeof(int32_t) * (size_t)P);
+    b.ws_bytes = w;
+    g->ws_bytes = std::max(g->ws_bytes, w);
+    g->buckets.push_back(b);
+    toff.push_back(o);
+  }
+  if (g->buckets.empty()) {
+    *out = g;
+    return VCPCU_OK;
+  }
+  // device memory: the tables and one workspace
+  cudaError_t e;
+  if (persistent) {
+    e = cudaMalloc(&g->tables, host.size());
+    if (e == cudaSuccess) e = cudaMalloc(&g->ws, g->ws_bytes);
+  } else {
+    e = cudaMallocAsync(&g->tables, host.size(), s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&g->ws, g->ws_bytes, s);
+  }
+  if (e != cudaSuccess) {
+    oz_group_free(g, s);
+    return cuda_fail(e, "igemm_batched: tensor-core workspace");
+  }
+  e = cudaMemcpyAsync(g->tables, host.data(), host.size(), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // `host` is freed on return
+  if (e != cudaSuccess) {
+    oz_group_free(g, s);
+    return cuda_fail(e, "igemm_batched: upload of the group tables");
+  }
+  uint8_t* tb = (uint8_t*)g->tables;
+  for (size_t i = 0; i < g->buckets.size(); ++i) {
+    OzGBucket& d = g->buckets[i].dev;
+    const Offs& o = toff[i];
+    d.probs = (const OzGProb*)(tb + o.probs);
+    d.blk_rowmax = (const int*)(tb + o.brow);
+    d.blk_split = (const int*)(tb + o.bspl);
+    d.item_rad = (const int*)(tb + o.irad);
+    d.item_crt = (const int*)(tb + o.icrt);
+    d.blk_asm = (const int*)(tb + o.basm);
+    d.col_prob = (const int*)(tb + o.cols);
+  }
+  *out = g;
+  return VCPCU_OK;
+}
+
+int oz_group_record(OzGroupPlan* g, unsigned long long* t_first, unsigned long long* t_last,
+                    cudaStream_t s) {
+  uint8_t* ws = (uint8_t*)g->ws;
+  for (BucketHost& b : g->buckets) {
+    OzGBucket d = b.dev;
+    d.rowmax = (unsigned long long*)(ws + b.offRowmax);
+    d.asum = (unsigned long long*)(ws + b.offAsum);
+    d.flag = (int*)(ws + b.offFlag);
+    d.E3 = (int*)(ws + b.offE3);
+    d.F2 = (int*)(ws + b.offF2);
+    d.beta = (double*)(ws + b.offBeta);
+    d.planesA = (uint16_t*)(ws + b.offA);
+    d.planesB = (uint16_t*)(ws + b.offB);
+    d.res = ws + b.offRes;
+    d.P = (int32_t*)(ws + b.offP);
+    d.t_first = t_first;
+    d.t_last = t_last;
+    VCPCU_CUDA_TRY(cudaMemsetAsync(ws, 0, b.zero_bytes, s));
+    if (t_first && t_last) {
+      g_init_stamps<<<(d.nprob + 255) / 256, 256, 0, s>>>(d.probs, d.nprob, t_first, t_last);
+      VCPCU_LAUNCH_CHECK("g_init_stamps");
+    }
+    int st;
+    {
+      PhaseTimer t(0, s);
+      if ((st = oz_gprep(d, b.nblk_rowmax, b.nblk_split, s))) return st;
+    }
+    {
+      PhaseTimer t(1, s);
+      if ((st = oz_grun_gemm(d, b.shape, OZ_RAD_SET, b.nitem_rad, s))) return st;
+    }
+    {
+      PhaseTimer t(2, s);
+      if ((st = oz_grun_gemm(d, b.shape, OZ_RAD_ADD, b.nitem_rad, s))) return st;
+    }
+    {
+      PhaseTimer t(3, s);
+      if ((st = oz_grun_gemm(d, b.shape, OZ_CRT, b.nitem_crt, s))) return st;
+    }
+    {
+      PhaseTimer t(4, s);
+      if ((st = oz_gassemble(d, b.rc, b.nblk_asm, s))) return st;
+    }
+    oz_merge_status_n(d.flag, d.nprob, s);
+    VCPCU_LAUNCH_CHECK("oz_status_merge_n");
+  }
+  return VCPCU_OK;
+}
+
+void oz_group_free(OzGroupPlan* g, cudaStream_t s) {
+  if (!g) return;
+  if (g->persistent) {
+    if (g->tables) cudaFree(g->tables);
+    if (g->ws) cudaFree(g->ws);
+  } else {
+    if (g->tables) cudaFreeAsync(g->tables, s);
+    if (g->ws) cudaFreeAsync(g->ws, s);
+  }
+  delete g;
+}
+
+}  // namespace vcpcu

@@ -421,23 +421,30 @@ __device__ __forceinline__ long long crt_int(double x, int E, int w) {
 // Block: 32 rows x 64 k; lane = row, warp q takes k0 + 8q .. k0 + 8q + 7, so
 // the loads of mA / rA are coalesced across the warp and each lane writes 8
 // bf16 (16 bytes) per plane -- no shared-memory transpose, full occupancy.
-template <int SR, int NL>
-__global__ void __launch_bounds__(256, 4)
-oz_split_left_crt(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
-                  const double* __restrict__ rA, int L, int w, const int* __restrict__ E3,
-                  uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_p,
-                  uint16_t* __restrict__ planes_r, unsigned long long* __restrict__ asum) {
+// FROM_A: midrad again from the interval matrix X (ld ldx) instead of the
+// stored planes mA = X, rA (ld M).  Planes rows are rowbase + i (stacked
+// problems), pstride elements apart; E3 and asum point at row 0 of this
+// problem.
+template <int SR, int NL, bool FROM_A>
+__device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K, int Kp,
+                                                    size_t pstride, int rowbase,
+                                                    const double* __restrict__ X,
+                                                    const double* __restrict__ rA, long ldx,
+                                                    int L, int w, const int* __restrict__ E3,
+                                                    uint16_t* __restrict__ planes_m,
+                                                    uint16_t* __restrict__ planes_p,
+                                                    uint16_t* __restrict__ planes_r,
+                                                    unsigned long long* __restrict__ asum) {
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
-  const int i = blockIdx.y * 32 + lane;
-  const int k0 = blockIdx.x * 64 + wq * 8;
+  const int i = by * 32 + lane;
+  const int k0 = bx * 64 + wq * 8;
   int Em = OZ_ZERO_EXP, Ep = OZ_ZERO_EXP, Er = OZ_ZERO_EXP;
   if (i < M) {
     Em = E3[3 * i + 0];
     Ep = E3[3 * i + 1];
     Er = E3[3 * i + 2];
   }
-  const size_t rowoff = (size_t)i * Kp + k0;
-  const size_t pstride = (size_t)Mp * Kp;
+  const size_t rowoff = (size_t)(rowbase + i) * Kp + k0;
   long long a[8];
   unsigned long long shi = 0, slo = 0;
   {
@@ -451,9 +458,14 @@ oz_split_left_crt(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
         const int k = k0 + t + u;
         double m = 0.0, r = 0.0, p = 0.0;
         if (i < M && k < K) {
-          m = mA[i + (long)k * M];
-          r = rA[i + (long)k * M];
-          p = sw_add_ru_pos(oz_abs(m), r);
+          if (FROM_A) {
+            const double2 e = *reinterpret_cast<const double2*>(X + 2 * (i + (long)k * ldx));
+            if (sw_finite(e.x) && sw_finite(e.y)) sw_midrad(e.x, e.y, m, r, p);
+          } else {
+            m = X[i + (long)k * M];
+            r = rA[i + (long)k * M];
+            p = sw_add_ru_pos(oz_abs(m), r);
+          }
         }
         a[t + u] = crt_int(m, Em, w);
         digits_of<SR>(p, Ep, 1, u ? d1 : d0);
@@ -501,20 +513,36 @@ oz_split_left_crt(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
   }
 }
 
-// Right factor, CRT form.  One block per column j < Np.  Pass 1 (thread t
-// takes k = t, t+256, ...): midrad into mB, rB (k contiguous) and the column
-// maxima.  Pass 2: B' = round(mB 2^(w - Fm)), its residues, the radius
-// digits, and sum_k |B'| (as >> 32 / & 0xffffffff parts); then
-// beta_j = RU((sum_k |B'| + ceil(K/2)) 2^(Fm - w)) >= sum_k |mB|.  No FP64
-// instruction on the common path (midrad on the integer pipe).
 template <int SR, int NL>
-__global__ void __launch_bounds__(256, 3)
-oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb,
-                   int L, int w, double* __restrict__ mBp, double* __restrict__ rBp,
-                   uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_r,
-                   uint16_t* __restrict__ planes_s, int* __restrict__ F2,
-                   double* __restrict__ beta, int* __restrict__ flag) {
-  const int j = blockIdx.x;
+__global__ void __launch_bounds__(256, 4)
+oz_split_left_crt(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
+                  const double* __restrict__ rA, int L, int w, const int* __restrict__ E3,
+                  uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_p,
+                  uint16_t* __restrict__ planes_r, unsigned long long* __restrict__ asum) {
+  split_left_crt_body<SR, NL, false>(blockIdx.x, blockIdx.y, M, K, Kp, (size_t)Mp * Kp, 0, mA,
+                                     rA, M, L, w, E3, planes_m, planes_p, planes_r, asum);
+}
+
+// Right factor, CRT form, one block per column.  Pass 1 (thread t takes
+// k = t, t+256, ...): midrad, the column maxima, and -- STORE_MID -- the
+// planes mB, rB (k contiguous).  Pass 2: B' = round(mB 2^(w - Fm)), its
+// residues, the radius digits, and sum_k |B'| (as >> 32 / & 0xffffffff
+// parts); then beta_j = RU((sum_k |B'| + ceil(K/2)) 2^(Fm - w)) >= sum_k |mB|.
+// Without STORE_MID pass 2 reads the column again (an L2 hit) and repeats
+// the midrad.  j is the column of B, jst its row in the (stacked) planes and
+// its index in F2 / beta.  No FP64 instruction on the common path.
+template <int SR, int NL, bool STORE_MID>
+__device__ __forceinline__ void split_right_crt_body(int j, int jst, int K, int N, int Kp,
+                                                     size_t pstride,
+                                                     const double* __restrict__ B, long ldb,
+                                                     int L, int w, double* __restrict__ mBp,
+                                                     double* __restrict__ rBp,
+                                                     uint16_t* __restrict__ planes_m,
+                                                     uint16_t* __restrict__ planes_r,
+                                                     uint16_t* __restrict__ planes_s,
+                                                     int* __restrict__ F2,
+                                                     double* __restrict__ beta,
+                                                     int* __restrict__ flag) {
   const int tid = threadIdx.x;
   __shared__ unsigned long long smax[2];
   __shared__ unsigned long long bs[2];
@@ -522,11 +550,12 @@ oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, l
   __syncthreads();
   unsigned long long am = 0, ar = 0;
   bool bad = false;
-  double* mcol = mBp + (size_t)j * Kp;
-  double* rcol = rBp + (size_t)j * Kp;
+  const double* bcol = B + 2 * (long)j * ldb;
+  double* mcol = STORE_MID ? mBp + (size_t)j * Kp : nullptr;
+  double* rcol = STORE_MID ? rBp + (size_t)j * Kp : nullptr;
   if (j < N) {
     for (int k = tid; k < K; k += 256) {
-      const double2 e = *reinterpret_cast<const double2*>(B + 2 * (k + (long)j * ldb));
+      const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
       double m = 0.0, r = 0.0, p;
       if (sw_finite(e.x) && sw_finite(e.y)) {
         sw_midrad(e.x, e.y, m, r, p);
@@ -535,8 +564,10 @@ oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, l
       } else {
         bad = true;
       }
-      mcol[k] = m;
-      rcol[k] = r;
+      if (STORE_MID) {
+        mcol[k] = m;
+        rcol[k] = r;
+      }
     }
   }
   if (bad) atomicOr(flag, 1);
@@ -545,15 +576,14 @@ oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, l
   __syncthreads();
   const int Fm = oz_exponent(__longlong_as_double((long long)smax[0]));
   const int Fr = oz_exponent(__longlong_as_double((long long)smax[1]));
-  if (tid == 0 && j < N) {
-    F2[2 * j + 0] = Fm;
-    F2[2 * j + 1] = Fr;
+  if (tid == 0) {
+    F2[2 * jst + 0] = j < N ? Fm : OZ_ZERO_EXP;
+    F2[2 * jst + 1] = j < N ? Fr : OZ_ZERO_EXP;
   }
   // pass 2: thread t takes the 8 consecutive k of 8 (t + 256 it) .. + 7
   unsigned long long shi = 0, slo = 0;
-  const size_t pstride = (size_t)Np * Kp;
   for (int k0 = 8 * tid; k0 < Kp; k0 += 8 * 256) {
-    const size_t off = (size_t)j * Kp + k0;
+    const size_t off = (size_t)jst * Kp + k0;
     float hl[8][NL];
     uint32_t hr[SR][4], hs[SR][4];
 #pragma unroll
@@ -564,8 +594,14 @@ oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, l
         const int k = k0 + t + u;
         double m = 0.0, r = 0.0;
         if (j < N && k < K) {
-          m = mcol[k];
-          r = rcol[k];
+          if (STORE_MID) {
+            m = mcol[k];
+            r = rcol[k];
+          } else {
+            const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
+            double p;
+            if (sw_finite(e.x) && sw_finite(e.y)) sw_midrad(e.x, e.y, m, r, p);
+          }
         }
         const long long b = crt_int(m, Fm, w);
         const unsigned long long ub = (unsigned long long)(b < 0 ? -b : b);
@@ -601,15 +637,134 @@ oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, l
   atomicAdd(&bs[0], shi);
   atomicAdd(&bs[1], slo);
   __syncthreads();
-  if (tid == 0 && j < N) {
+  if (tid == 0) {
     double bj = 0.0;
-    if (Fm != OZ_ZERO_EXP) {
+    if (j < N && Fm != OZ_ZERO_EXP) {
       const double v = __fma_ru((double)bs[0], 0x1p32,
                                 (double)(bs[1] + (unsigned long long)(K + 1) / 2));
       bj = dev_scale_dir(v, Fm - w, true);
     }
-    beta[j] = bj;
+    beta[jst] = bj;
   }
+}
+
+template <int SR, int NL>
+__global__ void __launch_bounds__(256, 3)
+oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb,
+                   int L, int w, double* __restrict__ mBp, double* __restrict__ rBp,
+                   uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_r,
+                   uint16_t* __restrict__ planes_s, int* __restrict__ F2,
+                   double* __restrict__ beta, int* __restrict__ flag) {
+  split_right_crt_body<SR, NL, true>(blockIdx.x, blockIdx.x, K, N, Kp, (size_t)Np * Kp, B, ldb,
+                                     L, w, mBp, rBp, planes_m, planes_r, planes_s, F2, beta,
+                                     flag);
+}
+
+// ---------------------------------------------------------- grouped products
+__device__ __forceinline__ int g_find(const int* __restrict__ prefix, int nprob, int x) {
+  int lo = 0, hi = nprob - 1;  // largest p with prefix[p] <= x
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= x)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ unsigned long long g_timer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Row maxima of every problem of a bucket (no midrad planes are kept: the
+// left split repeats the midrad); the first block of a problem to run
+// stamps its start.
+__global__ void __launch_bounds__(256)
+oz_rowmax_left_g(const __grid_constant__ OzGBucket b) {
+  const int p = g_find(b.blk_rowmax, b.nprob, blockIdx.x);
+  const OzGProb& q = b.probs[p];
+  const int nbx = (q.m + 31) / 32;
+  const int local = blockIdx.x - b.blk_rowmax[p];
+  if (threadIdx.x == 0 && b.t_first) atomicMin(&b.t_first[q.orig], g_timer());
+  __shared__ unsigned long long red[3][32];
+  const int lane = threadIdx.x & 31, ph = threadIdx.x >> 5;
+  const int i = (local % nbx) * 32 + lane;
+  if (threadIdx.x < 32) red[0][lane] = red[1][lane] = red[2][lane] = 0;
+  __syncthreads();
+  unsigned long long am = 0, ap = 0, ar = 0;
+  bool bad = false;
+  if (i < q.m) {
+    const int c0 = (local / nbx) * 256;
+    const int c1 = min(q.k, c0 + 256);
+    for (int c = c0 + ph; c < c1; c += 8) {
+      const double2 e = *reinterpret_cast<const double2*>(q.A + 2 * (i + (long)c * q.lda));
+      double m, r, pp;
+      if (sw_finite(e.x) && sw_finite(e.y)) {
+        sw_midrad(e.x, e.y, m, r, pp);
+        am = max(am, dbits(oz_abs(m)));
+        ap = max(ap, dbits(pp));
+        ar = max(ar, dbits(r));
+      } else {
+        bad = true;
+      }
+    }
+  }
+  if (bad) atomicOr(&b.flag[4 * p], 1);
+  atomicMax(&red[0][lane], am);
+  atomicMax(&red[1][lane], ap);
+  atomicMax(&red[2][lane], ar);
+  __syncthreads();
+  if (threadIdx.x < 32 && i < q.m) {
+    unsigned long long* mx = b.rowmax + 3 * (size_t)(q.rowoff + i);
+    atomicMax(&mx[0], red[0][lane]);
+    atomicMax(&mx[1], red[1][lane]);
+    atomicMax(&mx[2], red[2][lane]);
+  }
+}
+
+template <int NL>
+__global__ void __launch_bounds__(256, 4) oz_split_left_crt_g(const __grid_constant__ OzGBucket b) {
+  const int p = g_find(b.blk_split, b.nprob, blockIdx.x);
+  const OzGProb& q = b.probs[p];
+  const int nbx = b.Kp / 64;
+  const int local = blockIdx.x - b.blk_split[p];
+  const size_t pstride = (size_t)b.Mtot * b.Kp;
+  split_left_crt_body<2, NL, true>(local % nbx, local / nbx, q.m, q.k, b.Kp, pstride, q.rowoff,
+                                   q.A, nullptr, q.lda, q.L, q.w, b.E3 + 3 * (size_t)q.rowoff,
+                                   b.planesA, b.planesA + (size_t)b.Lmax * pstride,
+                                   b.planesA + (size_t)(b.Lmax + 2) * pstride,
+                                   b.asum + 2 * (size_t)q.rowoff);
+}
+
+template <int NL>
+__global__ void __launch_bounds__(256, 3) oz_split_right_crt_g(const __grid_constant__ OzGBucket b) {
+  const int jst = blockIdx.x;
+  const int p = b.col_prob[jst];
+  const OzGProb& q = b.probs[p];
+  const size_t pstride = (size_t)b.Ntot * b.Kp;
+  split_right_crt_body<2, NL, false>(jst - q.coloff, jst, q.k, q.n, b.Kp, pstride, q.B, q.ldb,
+                                     q.L, q.w, nullptr, nullptr, b.planesB,
+                                     b.planesB + (size_t)b.Lmax * pstride,
+                                     b.planesB + (size_t)(b.Lmax + 2) * pstride, b.F2, b.beta,
+                                     &b.flag[4 * p]);
+}
+
+int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, cudaStream_t st) {
+  if (nblk_rowmax > 0) {
+    oz_rowmax_left_g<<<nblk_rowmax, 256, 0, st>>>(b);
+    VCPCU_LAUNCH_CHECK("oz_rowmax_left_g");
+  }
+  oz_exponents<<<(b.Mtot + 255) / 256, 256, 0, st>>>(b.Mtot, b.rowmax, 3, b.E3);
+  VCPCU_LAUNCH_CHECK("oz_exponents");
+  // six 12-bit limbs hold every |A'|, |B'| < 2^61 (w <= 62)
+  oz_split_left_crt_g<6><<<nblk_split, 256, 0, st>>>(b);
+  VCPCU_LAUNCH_CHECK("oz_split_left_crt_g");
+  oz_split_right_crt_g<6><<<b.Ntot, 256, 0, st>>>(b);
+  VCPCU_LAUNCH_CHECK("oz_split_right_crt_g");
+  return VCPCU_OK;
 }
 
 // ------------------------------------------------------------------ launchers
