@@ -559,7 +559,8 @@ def bench_batch(dev, stream, steps=1, count=4096, seed=4096, forms=("plain", "oz
                "graph_create_s": t_create}
         if name == "auto":
             rec["problems_on_tensor_cores"] = int(sum(
-                pidcuda.autotune_choice(int(m[i]), int(n[i]), int(k[i])) != pidcuda.FORM_PLAIN
+                pidcuda.autotune_choice(int(m[i]), int(n[i]), int(k[i]), batched=True)
+                != pidcuda.FORM_PLAIN
                 for i in range(count)))
         if check:
             fails, ws = 0, []

@@ -232,9 +232,11 @@ int vcpcu_igemm_fma(int m, int n, int k, const double* A, const double* B, doubl
  * VCPCU_AUTOTUNE_CACHE (read back at the first AUTO decision of a later
  * process), and writes {fp64_rate, tc_rate, prep_bw, t_launch} to
  * constants[4] if non-NULL.  No counterpart in the reference.
- * vcpcu_autotune_choice returns the form AUTO would use for m x n x k. */
+ * vcpcu_autotune_choice returns the form AUTO would use for m x n x k, as
+ * a single product (batched = 0) or as one problem of a batch (batched != 0:
+ * the batch's grouped launches carry no per-product launch cost). */
 int vcpcu_autotune(void* stream, double* constants);
-int vcpcu_autotune_choice(int m, int n, int k);
+int vcpcu_autotune_choice(int m, int n, int k, int batched);
 
 /* ---- batches of uneven interval GEMMs -------------------------------------- */
 

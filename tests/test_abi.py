@@ -46,7 +46,8 @@ def test_error_mapping():
 def test_autotune_choice_host_model(cuda_lib):
     """The AUTO choice is a host-side cost model: tiny products stay on the
     FP64 plain kernel, large ones go to the tensor-core form.  No GPU call."""
-    choose = cuda_lib.vcpcu_autotune_choice
+    def choose(m, n, k, batched=0):
+        return cuda_lib.vcpcu_autotune_choice(m, n, k, batched)
     assert choose(8, 8, 8) == 0
     assert choose(32, 1, 32) == 0
     assert choose(4096, 4096, 4096) == 1
@@ -54,3 +55,6 @@ def test_autotune_choice_host_model(cuda_lib):
     # monotone along the diagonal: once Ozaki wins it keeps winning
     picks = [choose(n, n, n) for n in (16, 64, 128, 256, 512, 1024, 2048)]
     assert picks == sorted(picks)
+    # without launch costs (a batch) the tensor cores win no later
+    for n in (16, 64, 128, 256, 512):
+        assert choose(n, n, n, 1) >= choose(n, n, n)

@@ -38,18 +38,20 @@ def test_auto_batch_mixes_forms(cuda_lib):
     import torch
     rng = np.random.default_rng(7)
     probs = []
-    for (m, n, k) in [(20, 30, 40), (700, 650, 900), (5, 1, 3), (1024, 1024, 1024), (64, 64, 64)]:
+    for (m, n, k) in [(20, 30, 40), (700, 650, 900), (5, 1, 3), (1024, 1024, 1024), (64, 64, 64),
+                      (1, 1, 2)]:
         A = torch.from_numpy(W.interval_uniform(rng, m, k, 1e-12)).cuda()
         B = torch.from_numpy(W.interval_uniform(rng, k, n, 1e-12)).cuda()
         C = torch.full((2 * m * n,), float("nan"), dtype=torch.float64, device="cuda")
         probs.append((m, n, k, A, m, B, k, C, m))
-    forms = {pidcuda.autotune_choice(p[0], p[1], p[2]) for p in probs}
+    forms = {pidcuda.autotune_choice(p[0], p[1], p[2], batched=True) for p in probs}
     g = batch.BatchGraph(probs, pidcuda.FORM_AUTO)
     g.launch()
     torch.cuda.synchronize()
     for (m, n, k, A, lda, B, ldb, C, ldc) in probs:
         ref = torch.empty_like(C)
-        pidcuda.mulmm_dev(m, n, k, A, lda, B, ldb, ref, ldc, pidcuda.autotune_choice(m, n, k))
+        pidcuda.mulmm_dev(m, n, k, A, lda, B, ldb, ref, ldc,
+                          pidcuda.autotune_choice(m, n, k, batched=True))
         torch.cuda.synchronize()
         assert torch.equal(C.view(torch.int64), ref.view(torch.int64)), (m, n, k)
     g.close()

@@ -81,20 +81,22 @@ __global__ void fill_intervals(long n, double* X, unsigned seed) {
 
 }  // namespace
 
-// Predicted seconds of a product in each form (for the AUTO choice).
-int autotune_choose(int m, int n, int k) {
+// Predicted seconds of a product in each form (for the AUTO choice).  In a
+// batch (grouped launches) the per-product launch costs of both forms vanish.
+int autotune_choose(int m, int n, int k, bool batched) {
   std::lock_guard<std::mutex> lk(g_model_mu);
   load_cache_locked();
   const Model& md = g_model;
   const double mnk = (double)m * n * (k > 0 ? k : 0);
-  const double tp = 8.0 * mnk / md.fp64_rate + md.t_launch;
+  const double tl = batched ? 0.0 : md.t_launch;
+  const double tp = 8.0 * mnk / md.fp64_rate + tl;
   const double Mp = std::ceil(m / 128.0) * 128.0, Np = std::ceil(n / 256.0) * 256.0,
                Kp = std::ceil((k > 0 ? k : 1) / 64.0) * 64.0;
   OzPlan plan;
   oz_make_plan(m, n, k, 8, 2, &plan, 1);
   const double gemms = plan.pb.L + 8.0;
   const double to = gemms * 2.0 * Mp * Np * Kp / md.tc_rate +
-                    16.0 * ((double)m * k + (double)k * n) / md.prep_bw + 12.0 * md.t_launch;
+                    16.0 * ((double)m * k + (double)k * n) / md.prep_bw + 12.0 * tl;
   return to < tp ? VCPCU_FORM_OZAKI : VCPCU_FORM_PLAIN;
 }
 
@@ -160,4 +162,6 @@ extern "C" int vcpcu_autotune(void* stream, double* constants) {
   return VCPCU_OK;
 }
 
-extern "C" int vcpcu_autotune_choice(int m, int n, int k) { return autotune_choose(m, n, k); }
+extern "C" int vcpcu_autotune_choice(int m, int n, int k, int batched) {
+  return autotune_choose(m, n, k, batched != 0);
+}

@@ -367,6 +367,26 @@ int batch_record(BatchGraph& g, cudaStream_t s) {
   return st;
 }
 
+// Leading dimensions of every problem; the tensor-core forms read the
+// intervals of A and B as 16-byte pairs (AUTO sends misaligned problems to
+// the plain form instead).
+int batch_check(const std::vector<BatchProblem>& probs, int form) {
+  for (const BatchProblem& q : probs) {
+    if (q.m <= 0 || q.n <= 0) continue;
+    if (q.lda < q.m || q.ldc < q.m || (q.k > 0 && q.ldb < q.k) || !q.C ||
+        (q.k > 0 && (!q.A || !q.B))) {
+      set_error("igemm_batched: null pointer or leading dimension too small in a problem");
+      return VCPCU_ERR_INVALID_ARG;
+    }
+    if ((form == VCPCU_FORM_OZAKI || form == VCPCU_FORM_OZAKI_SLICES) && q.k > 0 &&
+        ((((uintptr_t)q.A) | ((uintptr_t)q.B)) & 15) != 0) {
+      set_error("igemm_batched: the tensor-core forms need 16-byte aligned A and B");
+      return VCPCU_ERR_INVALID_ARG;
+    }
+  }
+  return VCPCU_OK;
+}
+
 // The grouped tensor-core plan of a CRT / AUTO batch (null otherwise).
 int batch_group_plan(BatchGraph& g, int persistent, cudaStream_t s) {
   if (g.form != VCPCU_FORM_OZAKI && g.form != VCPCU_FORM_AUTO) return VCPCU_OK;
@@ -384,7 +404,7 @@ void batch_split_auto(BatchGraph& g, std::vector<BatchProblem>& plain_view) {
   if (g.form != VCPCU_FORM_AUTO) return;
   for (int i = 0; i < g.count; ++i) {
     const BatchProblem& q = g.probs[i];
-    if (q.m > 0 && q.n > 0 && autotune_choose(q.m, q.n, q.k > 0 ? q.k : 0) != VCPCU_FORM_PLAIN &&
+    if (q.m > 0 && q.n > 0 && autotune_choose(q.m, q.n, q.k > 0 ? q.k : 0, true) != VCPCU_FORM_PLAIN &&
         ((((uintptr_t)q.A) | ((uintptr_t)q.B)) & 15) == 0) {
       g.ozaki[i] = 1;
       plain_view[i].m = 0;
@@ -416,11 +436,7 @@ int vcpcu_igemm_batched_dev(int count, const vcpcu_problem* problems, int form, 
   g.form = form;
   g.slices = slices;
   g.probs.assign((const BatchProblem*)problems, (const BatchProblem*)problems + count);
-  for (const BatchProblem& q : g.probs)
-    if (q.m > 0 && q.n > 0 && (q.lda < q.m || q.ldc < q.m || (q.k > 0 && q.ldb < q.k))) {
-      set_error("igemm_batched: leading dimension too small in a problem");
-      return VCPCU_ERR_INVALID_ARG;
-    }
+  if ((st = batch_check(g.probs, form))) return st;
   std::vector<BatchProblem> plain_view;
   batch_split_auto(g, plain_view);
   Scratch mem;
@@ -449,6 +465,10 @@ int vcpcu_batch_graph_create(int count, const vcpcu_problem* problems, int form,
   g->form = form;
   g->slices = slices;
   g->probs.assign((const BatchProblem*)problems, (const BatchProblem*)problems + count);
+  if ((st = batch_check(g->probs, form))) {
+    delete g;
+    return st;
+  }
   std::vector<BatchProblem> plain_view;
   batch_split_auto(*g, plain_view);
   cudaError_t e = cudaMalloc(&g->state, batch_state_bytes(count));

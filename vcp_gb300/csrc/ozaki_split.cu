@@ -739,17 +739,122 @@ __global__ void __launch_bounds__(256, 4) oz_split_left_crt_g(const __grid_const
                                    b.asum + 2 * (size_t)q.rowoff);
 }
 
+// Grouped right split: one warp per stacked column (most columns of a batch
+// are short), 8 columns per block.  Pass 1: midrad and the column maxima
+// (warp reductions).  Pass 2: lane t takes the 8 consecutive k of
+// 8 (t + 32 it) .. + 7, reads the column again (an L1 / L2 hit) and writes
+// the residue and digit planes 16 bytes at a time; beta_j as in
+// split_right_crt_body.
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+    v = u > v ? u : v;
+  }
+  return v;
+}
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 template <int NL>
-__global__ void __launch_bounds__(256, 3) oz_split_right_crt_g(const __grid_constant__ OzGBucket b) {
-  const int jst = blockIdx.x;
+__global__ void __launch_bounds__(256) oz_split_right_crt_g(const __grid_constant__ OzGBucket b) {
+  const int lane = threadIdx.x & 31;
+  const int jst = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (jst >= b.Ntot) return;  // whole warps only: no block-level barrier below
   const int p = b.col_prob[jst];
   const OzGProb& q = b.probs[p];
-  const size_t pstride = (size_t)b.Ntot * b.Kp;
-  split_right_crt_body<2, NL, false>(jst - q.coloff, jst, q.k, q.n, b.Kp, pstride, q.B, q.ldb,
-                                     q.L, q.w, nullptr, nullptr, b.planesB,
-                                     b.planesB + (size_t)b.Lmax * pstride,
-                                     b.planesB + (size_t)(b.Lmax + 2) * pstride, b.F2, b.beta,
-                                     &b.flag[4 * p]);
+  const int j = jst - q.coloff, K = q.k, N = q.n, Kp = b.Kp, L = q.L, w = q.w;
+  const size_t pstride = (size_t)b.Ntot * Kp;
+  uint16_t* planes_m = b.planesB;
+  uint16_t* planes_r = b.planesB + (size_t)b.Lmax * pstride;
+  uint16_t* planes_s = b.planesB + (size_t)(b.Lmax + 2) * pstride;
+  const double* bcol = q.B + 2 * (long)j * q.ldb;
+  unsigned long long am = 0, ar = 0;
+  bool bad = false;
+  if (j < N) {
+    for (int k = lane; k < K; k += 32) {
+      const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
+      double m, r, pp;
+      if (sw_finite(e.x) && sw_finite(e.y)) {
+        sw_midrad(e.x, e.y, m, r, pp);
+        am = max(am, dbits(oz_abs(m)));
+        ar = max(ar, dbits(r));
+      } else {
+        bad = true;
+      }
+    }
+  }
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&b.flag[4 * p], 1);
+  am = warp_max_u64(am);
+  ar = warp_max_u64(ar);
+  const int Fm = oz_exponent(__longlong_as_double((long long)am));
+  const int Fr = oz_exponent(__longlong_as_double((long long)ar));
+  if (lane == 0) {
+    b.F2[2 * jst + 0] = j < N ? Fm : OZ_ZERO_EXP;
+    b.F2[2 * jst + 1] = j < N ? Fr : OZ_ZERO_EXP;
+  }
+  unsigned long long shi = 0, slo = 0;
+  for (int k0 = 8 * lane; k0 < Kp; k0 += 8 * 32) {
+    const size_t off = (size_t)jst * Kp + k0;
+    float hl[8][NL];
+    uint32_t hr[2][4], hs[2][4];
+#pragma unroll
+    for (int t = 0; t < 8; t += 2) {
+      int d0[2], d1[2], e0[2], e1[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int k = k0 + t + u;
+        double m = 0.0, r = 0.0;
+        if (j < N && k < K) {
+          const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
+          double pp;
+          if (sw_finite(e.x) && sw_finite(e.y)) sw_midrad(e.x, e.y, m, r, pp);
+        }
+        const long long bb = crt_int(m, Fm, w);
+        const unsigned long long ub = (unsigned long long)(bb < 0 ? -bb : bb);
+        shi += ub >> 32;
+        slo += ub & 0xffffffffULL;
+        limbs12<NL>(ub, bb < 0, hl[t + u]);
+        digits_of<2>(r, Fr, 1, u ? d1 : d0);
+        digits_of<2>(oz_abs(m), Fm, 1, u ? e1 : e0);
+      }
+#pragma unroll
+      for (int qq = 0; qq < 2; ++qq) {
+        hr[qq][t / 2] = bf16_bits(d0[qq]) | (bf16_bits(d1[qq]) << 16);
+        hs[qq][t / 2] = bf16_bits(e0[qq]) | (bf16_bits(e1[qq]) << 16);
+      }
+    }
+#pragma unroll
+    for (int qq = 0; qq < 2; ++qq) {
+      *reinterpret_cast<uint4*>(planes_r + qq * pstride + off) =
+          make_uint4(hr[qq][0], hr[qq][1], hr[qq][2], hr[qq][3]);
+      *reinterpret_cast<uint4*>(planes_s + qq * pstride + off) =
+          make_uint4(hs[qq][0], hs[qq][1], hs[qq][2], hs[qq][3]);
+    }
+#pragma unroll
+    for (int l = 0; l < OZ_MAX_MODULI_128; ++l) {
+      if (l >= L) break;
+      uint32_t h[4];
+#pragma unroll
+      for (int t = 0; t < 8; t += 2)
+        h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
+      *reinterpret_cast<uint4*>(planes_m + l * pstride + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    }
+  }
+  shi = warp_sum_u64(shi);
+  slo = warp_sum_u64(slo);
+  if (lane == 0) {
+    double bj = 0.0;
+    if (j < N && Fm != OZ_ZERO_EXP) {
+      const double v = __fma_ru((double)shi, 0x1p32,
+                                (double)(slo + (unsigned long long)(K + 1) / 2));
+      bj = dev_scale_dir(v, Fm - w, true);
+    }
+    b.beta[jst] = bj;
+  }
 }
 
 int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, cudaStream_t st) {
@@ -762,7 +867,7 @@ int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, cudaStream_t s
   // six 12-bit limbs hold every |A'|, |B'| < 2^61 (w <= 62)
   oz_split_left_crt_g<6><<<nblk_split, 256, 0, st>>>(b);
   VCPCU_LAUNCH_CHECK("oz_split_left_crt_g");
-  oz_split_right_crt_g<6><<<b.Ntot, 256, 0, st>>>(b);
+  oz_split_right_crt_g<6><<<(b.Ntot + 7) / 8, 256, 0, st>>>(b);
   VCPCU_LAUNCH_CHECK("oz_split_right_crt_g");
   return VCPCU_OK;
 }

@@ -5,8 +5,9 @@
 namespace vcpcu {
 
 // VCPCU_FORM_PLAIN or VCPCU_FORM_OZAKI, whichever the cost model of the
-// autotuner predicts faster (autotune.cu).
-int autotune_choose(int m, int n, int k);
+// autotuner predicts faster (autotune.cu); batched: as one problem of a
+// grouped batch (no per-product launch cost).
+int autotune_choose(int m, int n, int k, bool batched = false);
 
 // Interval product of either form on device pointers (defined in capi.cu).
 // point_mask bit 0 / bit 1: A / B has zero radii (the tensor-core form then

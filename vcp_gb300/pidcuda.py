@@ -121,9 +121,10 @@ def autotune(stream=None) -> dict:
     return dict(fp64_rate=c[0], tc_rate=c[1], prep_bw=c[2], t_launch=c[3])
 
 
-def autotune_choice(m: int, n: int, k: int) -> int:
-    """The form (FORM_PLAIN or FORM_OZAKI) that FORM_AUTO uses for m x n x k."""
-    return int(_lib.load().vcpcu_autotune_choice(int(m), int(n), int(k)))
+def autotune_choice(m: int, n: int, k: int, batched: bool = False) -> int:
+    """The form (FORM_PLAIN or FORM_OZAKI) that FORM_AUTO uses for m x n x k,
+    as a single product or as one problem of a batch."""
+    return int(_lib.load().vcpcu_autotune_choice(int(m), int(n), int(k), int(bool(batched))))
 
 
 # ---- inf-sup interval FMA (vcp::ifma) and its product (vcp::pidblas_fma) ------------
