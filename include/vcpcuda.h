@@ -255,9 +255,16 @@ typedef struct {
  * generator of the reference emit; no single reference entry point: each
  * would be a pidblas::mulmm call).  Form PLAIN: one persistent grouped
  * launch over all problems' 64 x 64 tiles (work counter, no waits),
- * bit-identical per problem to vcpcu_igemm_dev PLAIN.  Ozaki forms: the
- * problems in sequence on the stream.  The table is read from host memory
- * during the call; stream-ordered. */
+ * bit-identical per problem to vcpcu_igemm_dev PLAIN.  Form OZAKI: grouped
+ * products -- the problems bucketed by padded inner dimension, nine launches
+ * per bucket over all its problems -- bit-identical per problem to
+ * vcpcu_igemm_dev OZAKI.  OZAKI_SLICES: product by product on forked
+ * streams.  AUTO: each problem in the form the cost model picks for a batch
+ * problem (vcpcu_autotune_choice with batched = 1), both parts concurrent.
+ * The tensor-core forms need 16-byte aligned A and B.  The table is read
+ * from host memory during the call; the call plans the grouped products and
+ * uploads their tables (it synchronises the stream once, so it cannot run
+ * inside a stream capture: use the batch graphs below). */
 int vcpcu_igemm_batched_dev(int count, const vcpcu_problem* problems, int form,
                             int slices, void* stream);
 
