@@ -726,7 +726,7 @@ oz_rowmax_left_g(const __grid_constant__ OzGBucket b) {
 }
 
 template <int NL>
-__global__ void __launch_bounds__(256, 4) oz_split_left_crt_g(const __grid_constant__ OzGBucket b) {
+__global__ void __launch_bounds__(256, 3) oz_split_left_crt_g(const __grid_constant__ OzGBucket b) {
   const int p = g_find(b.blk_split, b.nprob, blockIdx.x);
   const OzGProb& q = b.probs[p];
   const int nbx = b.Kp / 64;
@@ -1058,49 +1058,58 @@ dd_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long l
   }
 }
 
-// Right dd factor: one block per column; exponent, then residue planes
-// [L][Np][Kp].
+// Right dd factor: one warp per column, 8 columns per block.  Pass 1: the
+// column maximum of |hi| (warp reduction) and its exponent.  Pass 2: lane t
+// takes the 4 consecutive k of 4 (t + 32 it) .. + 3, reads the column again
+// (an L1 / L2 hit) and writes each residue plane [L][Np][Kp] 8 bytes at a
+// time (256 contiguous bytes per warp).
 __global__ void __launch_bounds__(256)
 dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb, int L, int w,
                int* __restrict__ F, uint16_t* __restrict__ planes, int* __restrict__ flag) {
-  const int j = blockIdx.x, tid = threadIdx.x;
-  __shared__ unsigned long long smax;
-  if (tid == 0) smax = 0;
-  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (j >= Np) return;  // whole warps only: no block-level barrier below
+  const double* bcol = B + 2 * (long)j * ldb;
   unsigned long long am = 0;
   bool bad = false;
   if (j < N) {
-    for (int k = tid; k < K; k += 256) {
-      const double2 e = *reinterpret_cast<const double2*>(B + 2 * (k + (long)j * ldb));
-      if (isfinite(e.x) && isfinite(e.y))
+    for (int k = lane; k < K; k += 32) {
+      const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
+      if (sw_finite(e.x) && sw_finite(e.y))
         am = max(am, dbits(oz_abs(e.x)));
       else
         bad = true;
     }
   }
-  if (bad) atomicOr(flag, 1);
-  atomicMax(&smax, am);
-  __syncthreads();
-  int Fj = oz_exponent(__longlong_as_double((long long)smax));
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flag, 1);
+  am = warp_max_u64(am);
+  int Fj = oz_exponent(__longlong_as_double((long long)am));
   if (Fj != OZ_ZERO_EXP) Fj += 1;
-  if (tid == 0 && j < N) F[j] = Fj;
-  for (int k = tid; k < Kp; k += 256) {
-    double hi = 0.0, lo = 0.0;
-    if (j < N && k < K) {
-      const double2 e = *reinterpret_cast<const double2*>(B + 2 * (k + (long)j * ldb));
-      if (isfinite(e.x) && isfinite(e.y)) {
-        hi = e.x;
-        lo = e.y;
+  if (lane == 0 && j < N) F[j] = Fj;
+  const size_t pstride = (size_t)Np * Kp;
+  for (int k0 = 4 * lane; k0 < Kp; k0 += 4 * 32) {
+    float hl[4][10];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int k = k0 + t;
+      double hi = 0.0, lo = 0.0;
+      if (j < N && k < K) {
+        const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
+        if (sw_finite(e.x) && sw_finite(e.y)) {
+          hi = e.x;
+          lo = e.y;
+        }
       }
+      const __int128 b = dd_int(hi, lo, Fj, w);
+      limbs12<10>((unsigned __int128)(b < 0 ? -b : b), b < 0, hl[t]);
     }
-    const __int128 b = dd_int(hi, lo, Fj, w);
-    const unsigned __int128 ub = (unsigned __int128)(b < 0 ? -b : b);
-    float hb[10];
-    limbs12<10>(ub, b < 0, hb);
+    const size_t off = (size_t)j * Kp + k0;
 #pragma unroll
     for (int l = 0; l < OZ_MAX_MODULI; ++l) {
       if (l >= L) break;
-      planes[((size_t)l * Np + j) * Kp + k] = (uint16_t)(__float_as_uint(res_sym<10>(hb, l)) >> 16);
+      *reinterpret_cast<uint2*>(planes + l * pstride + off) =
+          make_uint2(pack_bf16x2(res_sym<10>(hl[0], l), res_sym<10>(hl[1], l)),
+                     pack_bf16x2(res_sym<10>(hl[2], l), res_sym<10>(hl[3], l)));
     }
   }
 }
@@ -1121,7 +1130,7 @@ int dd_prepare(int M, int N, int K, int Mp, int Np, int Kp, int L, int w, const 
   dim3 g2(Kp / 64, Mp / 32);
   dd_split_left<<<g2, 256, 0, st>>>(M, K, Mp, Kp, A, lda, L, w, E, planesA);
   VCPCU_LAUNCH_CHECK("dd_split_left");
-  dd_split_right<<<Np, 256, 0, st>>>(K, N, Kp, Np, B, ldb, L, w, F, planesB, flag);
+  dd_split_right<<<(Np + 7) / 8, 256, 0, st>>>(K, N, Kp, Np, B, ldb, L, w, F, planesB, flag);
   VCPCU_LAUNCH_CHECK("dd_split_right");
   return VCPCU_OK;
 }
