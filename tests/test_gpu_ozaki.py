@@ -206,3 +206,50 @@ def test_ozaki_midrad_paths(cuda_lib, oracle, crt):
     assert st == 0
     assert np.array_equal(bits(C), bits(ref))
     check_contains(oracle, m, n, k, A, B, C)
+
+
+@pytest.mark.parametrize("shape,panels", [((300, 2048, 500), None), ((129, 700, 1100), "2"),
+                                          ((64, 1300, 70), "5"), ((33, 600, 0), "3")])
+def test_ozaki_host_pipeline_bitexact(cuda_lib, shape, panels, monkeypatch):
+    """The host-pointer call overlaps its copies with the panels of the
+    product (column panels of B and C, A in column chunks); the result is
+    bit-identical to the one-shot device call, including a last panel of
+    smaller padded width and an empty inner dimension."""
+    import torch
+    from vcp_gb300 import _lib
+    m, n, k = shape
+    if panels is not None:
+        monkeypatch.setenv("VCPCU_HOST_PANELS", panels)
+    rng = np.random.default_rng(m + n + k)
+    A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40) if k else np.zeros(0)
+    B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40) if k else np.zeros(0)
+    hA = torch.from_numpy(A).pin_memory() if k else torch.zeros(2, dtype=torch.float64)
+    hB = torch.from_numpy(B).pin_memory() if k else torch.zeros(2, dtype=torch.float64)
+    hC = torch.full((2 * m * n,), 7.0, dtype=torch.float64).pin_memory()
+    _lib.call("vcpcu_igemm", m, n, k, hA.data_ptr(), hB.data_ptr(), hC.data_ptr(),
+              pidcuda.FORM_OZAKI, 0)
+    dA = hA.cuda(); dB = hB.cuda()
+    dC = torch.zeros(2 * m * n, dtype=torch.float64, device="cuda")
+    pidcuda.mulmm_dev(m, n, k, dA, m, dB, max(k, 1), dC, m, pidcuda.FORM_OZAKI, 0)
+    _lib.call("vcpcu_status", 0)
+    assert np.array_equal(bits(hC.numpy()), bits(dC.cpu().numpy()))
+
+
+def test_ozaki_host_pipeline_nonfinite_late_panel(cuda_lib, monkeypatch):
+    """A non-finite entry in the last column panel of B still makes every
+    entry NaN (earlier panels were already copied back finite)."""
+    import torch
+    from vcp_gb300 import _lib
+    monkeypatch.setenv("VCPCU_HOST_PANELS", "4")
+    m, n, k = 40, 1024, 50
+    rng = np.random.default_rng(11)
+    A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
+    B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
+    B[2 * (5 + (n - 1) * k) + 1] = np.inf
+    hA = torch.from_numpy(A).pin_memory()
+    hB = torch.from_numpy(B).pin_memory()
+    hC = torch.zeros(2 * m * n, dtype=torch.float64).pin_memory()
+    with pytest.raises(NonFiniteError):
+        _lib.call("vcpcu_igemm", m, n, k, hA.data_ptr(), hB.data_ptr(), hC.data_ptr(),
+                  pidcuda.FORM_OZAKI, 0)
+    assert np.all(np.isnan(hC.numpy()))

@@ -376,6 +376,137 @@ int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long ld
   return VCPCU_OK;
 }
 
+namespace {
+
+__global__ void oz_fill_nan(size_t count, double* C) {
+  const double nan = __longlong_as_double(0x7ff8000000000000LL);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (size_t)gridDim.x * blockDim.x)
+    C[i] = nan;
+}
+
+// Events of one pipelined call, and the streams it must drain before its
+// device memory goes back to the pool (also on error paths).
+struct PipeGuard {
+  std::vector<cudaEvent_t> ev;
+  cudaStream_t streams[3];
+  explicit PipeGuard(cudaStream_t a, cudaStream_t b, cudaStream_t c) : streams{a, b, c} {}
+  cudaEvent_t make() {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+    ev.push_back(e);
+    return e;
+  }
+  ~PipeGuard() {
+    for (cudaStream_t x : streams) cudaStreamSynchronize(x);
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  }
+};
+
+int pipe_event(PipeGuard& g, cudaStream_t rec, cudaStream_t waiter) {
+  cudaEvent_t e = g.make();
+  if (!e) {
+    set_error("cudaEventCreateWithFlags failed");
+    cudaGetLastError();
+    return VCPCU_ERR_CUDA;
+  }
+  VCPCU_CUDA_TRY(cudaEventRecord(e, rec));
+  VCPCU_CUDA_TRY(cudaStreamWaitEvent(waiter, e, 0));
+  return VCPCU_OK;
+}
+
+}  // namespace
+
+int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const double* B, double* C,
+                               int slices, int panels, cudaStream_t s, cudaStream_t up,
+                               cudaStream_t down) {
+  const int nslices = slices > 0 ? slices : 8;
+  if (k > (1 << 20)) {
+    set_error("igemm (Ozaki form): inner dimension %d above the supported 2^20", k);
+    return VCPCU_ERR_UNSUPPORTED;
+  }
+  if (m <= 0 || n <= 0) return VCPCU_OK;
+  if (k < 0) k = 0;
+  if (panels < 1) panels = 1;
+  int nb = (n + panels - 1) / panels;
+  nb = (nb + OZ_BN - 1) / OZ_BN * OZ_BN;  // whole column tiles per panel
+  panels = (n + nb - 1) / nb;
+  OzPlan plan;  // the widest panel; the left factor whole
+  oz_make_plan(m, nb < n ? nb : n, k, nslices, 2, &plan, 1);
+  const size_t na = 2 * (size_t)m * k, nbe = 2 * (size_t)k * n, nc = 2 * (size_t)m * n;
+  const size_t off_b = al256(na * 8), off_c = off_b + al256(nbe * 8),
+               off_w = off_c + al256(nc * 8);
+  Scratch buf;
+  int st = buf.alloc(off_w + oz_workspace_bytes(plan.pb), s);
+  if (st) return st;
+  PipeGuard g(s, up, down);  // destroyed before buf: drains every stream first
+  double* dA = (double*)buf.ptr;
+  double* dB = (double*)((uint8_t*)buf.ptr + off_b);
+  double* dC = (double*)((uint8_t*)buf.ptr + off_c);
+  OzWorkspace ws;
+  oz_carve_workspace(plan.pb, (uint8_t*)buf.ptr + off_w, &ws);
+  // the copy streams may touch the memory only after its allocation on s
+  if ((st = pipe_event(g, s, up)) || (st = pipe_event(g, s, down))) return st;
+
+  // A in column chunks, each one's midrad / row maxima as soon as it lands
+  const int achunks = k >= 4 ? 4 : k;
+  if ((st = oz_prepare_left_begin(plan.pb, ws, s))) return st;
+  for (int c = 0; c < achunks; ++c) {
+    const int k0 = (int)((long long)k * c / achunks), k1 = (int)((long long)k * (c + 1) / achunks);
+    VCPCU_CUDA_TRY(cudaMemcpyAsync(dA + 2 * (size_t)k0 * m, A + 2 * (size_t)k0 * m,
+                                   2 * (size_t)(k1 - k0) * m * sizeof(double),
+                                   cudaMemcpyHostToDevice, up));
+    if ((st = pipe_event(g, up, s))) return st;
+    if ((st = oz_prepare_left_rowmax(plan.pb, dA, m, k0, k1, ws, s))) return st;
+  }
+  if ((st = oz_prepare_left_finish(plan.pb, ws, s))) return st;
+  long long flops = 0;
+  for (int J = 0; J < panels; ++J) {
+    const int j0 = J * nb, wj = (n - j0 < nb) ? n - j0 : nb;
+    if (k > 0) {
+      VCPCU_CUDA_TRY(cudaMemcpyAsync(dB + 2 * (size_t)j0 * k, B + 2 * (size_t)j0 * k,
+                                     2 * (size_t)wj * k * sizeof(double), cudaMemcpyHostToDevice,
+                                     up));
+    }
+    if ((st = pipe_event(g, up, s))) return st;
+    OzPlan pj;
+    if (wj == plan.pb.N) {
+      pj = plan;
+    } else {
+      oz_make_plan(m, wj, k, nslices, 2, &pj, 1);
+    }
+    OzWorkspace wsj = ws;  // the panel's planes use its own padded width
+    wsj.b_r = ws.b_mid + (size_t)pj.pb.mplanes * pj.pb.Np * pj.pb.Kp;
+    wsj.b_s = wsj.b_r + (size_t)pj.pb.sr * pj.pb.Np * pj.pb.Kp;
+    if ((st = oz_prepare_right_crt(pj.pb, dB + 2 * (size_t)j0 * k, k > 0 ? k : 1, wsj, s)))
+      return st;
+    if ((st = oz_run_gemm(pj, OZ_RAD_SET, wsj, nullptr, 0, s))) return st;
+    if ((st = oz_run_gemm(pj, OZ_RAD_ADD, wsj, nullptr, 0, s))) return st;
+    if ((st = oz_run_gemm(pj, OZ_CRT, wsj, nullptr, 0, s))) return st;
+    if ((st = oz_crt_assemble(pj, wsj, dC + 2 * (size_t)j0 * m, m, s))) return st;
+    if ((st = pipe_event(g, s, down))) return st;
+    VCPCU_CUDA_TRY(cudaMemcpyAsync(C + 2 * (size_t)j0 * m, dC + 2 * (size_t)j0 * m,
+                                   2 * (size_t)wj * m * sizeof(double), cudaMemcpyDeviceToHost,
+                                   down));
+    flops += 2LL * m * wj * (long long)k * (pj.pb.L + 2LL * pj.rad.npairs);
+  }
+  oz_profile_add_flops(flops);
+  oz_merge_status(ws.flag, s);
+  // A non-finite entry of a later B panel leaves earlier panels finite; the
+  // whole result is NaN then, as in the one-shot product.
+  int hflag[2] = {0, 0};
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(hflag, ws.flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(down));
+  if ((hflag[0] != 0 || hflag[1] != 0) && panels > 1) {
+    oz_fill_nan<<<152 * 8, 256, 0, s>>>(nc, dC);
+    VCPCU_LAUNCH_CHECK("oz_fill_nan");
+    VCPCU_CUDA_TRY(cudaMemcpyAsync(C, dC, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+    VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  return VCPCU_OK;
+}
+
 int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
                 double* C, long ldc, int form, int slices, cudaStream_t s, int point_mask) {
   const int nslices = slices > 0 ? slices : 8;

@@ -126,6 +126,17 @@ int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long l
                     cudaStream_t st);
 int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, long ldb,
                OzWorkspace& ws, cudaStream_t st);
+// oz_prepare in parts: clear the row maxima, sums and status words; midrad
+// and row maxima of the columns [k0, k1) of A (any order of column ranges,
+// the maxima accumulate); row exponents and the left planes; the right
+// planes (CRT form) of B, whose columns may be any column panel of a larger
+// right factor.
+int oz_prepare_left_begin(const OzProblem& pb, OzWorkspace& ws, cudaStream_t st);
+int oz_prepare_left_rowmax(const OzProblem& pb, const double* A, long lda, int k0, int k1,
+                           OzWorkspace& ws, cudaStream_t st);
+int oz_prepare_left_finish(const OzProblem& pb, OzWorkspace& ws, cudaStream_t st);
+int oz_prepare_right_crt(const OzProblem& pb, const double* B, long ldb, OzWorkspace& ws,
+                         cudaStream_t st);
 // t_set < 0: the radius product of OZ_RAD_SET writes T, that of OZ_RAD_ADD
 // adds to it; 0 / 1 force add / write.
 int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, long ldc,
@@ -243,6 +254,18 @@ int oz_group_plan(int count, const BatchProblemView* problems, const char* selec
 int oz_group_record(OzGroupPlan* g, unsigned long long* t_first, unsigned long long* t_last,
                     cudaStream_t s);
 void oz_group_free(OzGroupPlan* g, cudaStream_t s);
+
+// CRT-form product of host matrices (column-major, lda = m, ldb = k,
+// ldc = m) with the host<->device copies overlapped: A goes up in column
+// chunks (its row maxima computed as each arrives), B in column panels;
+// each panel's planes, slice GEMMs and reassembly run as soon as it is on the
+// device, and its result columns go down on `down` while the next panel
+// computes.  Streams: `s` computes, `up` / `down` copy.  Bit-identical to
+// ozaki_igemm on the same operands (every entry depends on its row of A and
+// column of B only).  Synchronises before returning.
+int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const double* B, double* C,
+                               int slices, int panels, cudaStream_t s, cudaStream_t up,
+                               cudaStream_t down);
 
 // point_mask as OzPlan::point_mask (the caller guarantees the zero radii).
 int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,

@@ -890,49 +890,69 @@ int launch_splits(const OzProblem& pb, const double* B, long ldb, OzWorkspace& w
   return VCPCU_OK;
 }
 
-int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, long ldb,
-               OzWorkspace& ws, cudaStream_t st) {
-  const int M = pb.M, N = pb.N, K = pb.K;
+int oz_prepare_left_begin(const OzProblem& pb, OzWorkspace& ws, cudaStream_t st) {
   VCPCU_CUDA_TRY(cudaMemsetAsync(ws.rowmax, 0, sizeof(unsigned long long) * 3 * (size_t)pb.Mp, st));
   VCPCU_CUDA_TRY(cudaMemsetAsync(ws.delta, 0, sizeof(unsigned long long) * (size_t)pb.Mp, st));
   VCPCU_CUDA_TRY(cudaMemsetAsync(ws.flag, 0, 4 * sizeof(int), st));  // every status word
-  if (M > 0 && K > 0) {
-    const int cpb = 256;
-    dim3 g1((M + 31) / 32, (K + cpb - 1) / cpb);
-    oz_rowmax_left<<<g1, 256, 0, st>>>(M, K, A, lda, cpb, ws.midA, ws.radA, ws.rowmax, ws.flag);
-    VCPCU_LAUNCH_CHECK("oz_rowmax_left");
-  }
+  if (pb.crt)
+    VCPCU_CUDA_TRY(cudaMemsetAsync(ws.asum, 0, sizeof(unsigned long long) * 2 * (size_t)pb.Mp, st));
+  return VCPCU_OK;
+}
+
+int oz_prepare_left_rowmax(const OzProblem& pb, const double* A, long lda, int k0, int k1,
+                           OzWorkspace& ws, cudaStream_t st) {
+  const int M = pb.M, kc = k1 - k0;
+  if (M <= 0 || kc <= 0) return VCPCU_OK;
+  const int cpb = 256;
+  dim3 g1((M + 31) / 32, (kc + cpb - 1) / cpb);
+  oz_rowmax_left<<<g1, 256, 0, st>>>(M, kc, A + 2 * (long)k0 * lda, lda, cpb,
+                                     ws.midA + (size_t)k0 * M, ws.radA + (size_t)k0 * M,
+                                     ws.rowmax, ws.flag);
+  VCPCU_LAUNCH_CHECK("oz_rowmax_left");
+  return VCPCU_OK;
+}
+
+int oz_prepare_left_finish(const OzProblem& pb, OzWorkspace& ws, cudaStream_t st) {
   oz_exponents<<<(pb.Mp + 255) / 256, 256, 0, st>>>(pb.Mp, ws.rowmax, 3, ws.E3);
   VCPCU_LAUNCH_CHECK("oz_exponents");
   if (pb.sr != 2) {
     set_error("Ozaki form: radius slice count %d is not built (2 is)", pb.sr);
     return VCPCU_ERR_UNSUPPORTED;
   }
-  int st_ = VCPCU_OK;
-  if (pb.crt) {
-    VCPCU_CUDA_TRY(cudaMemsetAsync(ws.asum, 0, sizeof(unsigned long long) * 2 * (size_t)pb.Mp, st));
-    // |A'|, |B'| < 2^(w-1): five 12-bit limbs up to w = 61, six up to 73
-    dim3 g2(pb.Kp / 64, pb.Mp / 32);
-    if (pb.w <= 61) {
-      oz_split_left_crt<2, 5><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA,
-                                                  pb.L, pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r,
-                                                  ws.asum);
-      VCPCU_LAUNCH_CHECK("oz_split_left_crt");
-      oz_split_right_crt<2, 5><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L,
-                                                      pb.w, ws.midB, ws.radB, ws.b_mid, ws.b_r,
-                                                      ws.b_s, ws.F2, ws.beta, ws.flag);
-    } else {
-      oz_split_left_crt<2, 6><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA,
-                                                  pb.L, pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r,
-                                                  ws.asum);
-      VCPCU_LAUNCH_CHECK("oz_split_left_crt");
-      oz_split_right_crt<2, 6><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L,
-                                                      pb.w, ws.midB, ws.radB, ws.b_mid, ws.b_r,
-                                                      ws.b_s, ws.F2, ws.beta, ws.flag);
-    }
-    VCPCU_LAUNCH_CHECK("oz_split_right_crt");
-    return VCPCU_OK;
-  }
+  if (!pb.crt) return VCPCU_OK;  // the slice form splits both factors in launch_splits
+  // |A'| < 2^(w-1): five 12-bit limbs up to w = 61, six up to 73
+  dim3 g2(pb.Kp / 64, pb.Mp / 32);
+  if (pb.w <= 61)
+    oz_split_left_crt<2, 5><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, pb.L,
+                                                pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r, ws.asum);
+  else
+    oz_split_left_crt<2, 6><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, pb.L,
+                                                pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r, ws.asum);
+  VCPCU_LAUNCH_CHECK("oz_split_left_crt");
+  return VCPCU_OK;
+}
+
+int oz_prepare_right_crt(const OzProblem& pb, const double* B, long ldb, OzWorkspace& ws,
+                         cudaStream_t st) {
+  if (pb.w <= 61)
+    oz_split_right_crt<2, 5><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L, pb.w,
+                                                    ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,
+                                                    ws.F2, ws.beta, ws.flag);
+  else
+    oz_split_right_crt<2, 6><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L, pb.w,
+                                                    ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,
+                                                    ws.F2, ws.beta, ws.flag);
+  VCPCU_LAUNCH_CHECK("oz_split_right_crt");
+  return VCPCU_OK;
+}
+
+int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, long ldb,
+               OzWorkspace& ws, cudaStream_t st) {
+  int st_ = oz_prepare_left_begin(pb, ws, st);
+  if (!st_) st_ = oz_prepare_left_rowmax(pb, A, lda, 0, pb.K, ws, st);
+  if (!st_) st_ = oz_prepare_left_finish(pb, ws, st);
+  if (st_) return st_;
+  if (pb.crt) return oz_prepare_right_crt(pb, B, ldb, ws, st);
   switch (pb.s) {
 #define OZ_SPLIT_CASE(S)                                                          \
   case S:                                                                         \
@@ -946,10 +966,8 @@ int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, 
       set_error("Ozaki form: slice count %d outside [2, 12]", pb.s);
       return VCPCU_ERR_INVALID_ARG;
   }
-  if (st_) return st_;
-  return VCPCU_OK;
+  return st_;
 }
-
 
 // ------------------------------------------------------------ dd (pddcuda)
 // Symmetric residue of (neg ? -a : a) mod m_l for a < 2^128 (Horner over
