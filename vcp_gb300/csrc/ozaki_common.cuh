@@ -32,7 +32,9 @@ constexpr int OZ_FOLD_CHUNKS = 64;    // chunks per int32 fold (64 * 2^24 = 2^30
 
 OZ_HD uint64_t oz_bits(double x) {
 #ifdef __CUDA_ARCH__
-  return (uint64_t)__double_as_longlong(x);
+  uint64_t b;  // an opaque move: keeps integer tests of the bits on the integer pipe
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+  return b;
 #else
   uint64_t b;
   memcpy(&b, &x, 8);

@@ -100,41 +100,50 @@ __device__ __forceinline__ void add_M(uint32_t* r, const uint32_t* m) {
 }
 
 // Directed conversion of (-1)^neg * mag * 2^e (mag: 4 limbs) to double.
-__device__ __forceinline__ void big_to_dir(const uint32_t* mag, int neg, int e, double& lo,
+// Limbs are picked by unrolled selects (no dynamically indexed array, which
+// would live in local memory).
+__device__ __forceinline__ void big_to_dir(const uint32_t (&mag)[4], int neg, int e, double& lo,
                                            double& up) {
-  int top = 3;
-  while (top >= 0 && mag[top] == 0) --top;
-  if (top < 0) {
+  int bl = 0;  // bit length, 0..128
+#pragma unroll
+  for (int t = 0; t < 4; ++t)
+    if (mag[t]) bl = 32 * t + (32 - __clz(mag[t]));
+  if (bl == 0) {
     lo = up = 0.0;
     return;
   }
-  const int bl = 32 * top + (32 - __clz(mag[top]));  // bit length, 1..128
-  unsigned long long t;
-  int sh = 0;
-  bool sticky = false;
-  if (bl <= 64) {
-    t = (unsigned long long)mag[0] | ((unsigned long long)mag[1] << 32);
-  } else {
-    sh = bl - 64;
-    // t = mag >> sh (top 64 bits), sticky = any bit below sh
-    const int wq = sh >> 5, bq = sh & 31;
-    unsigned long long w0 = mag[wq], w1 = (wq + 1 < 4) ? mag[wq + 1] : 0u,
-                       w2 = (wq + 2 < 4) ? mag[wq + 2] : 0u;
-    unsigned long long lo64 = w0 | (w1 << 32);
-    t = bq ? ((lo64 >> bq) | (w2 << (64 - bq))) : lo64;
-    for (int q = 0; q < wq; ++q) sticky |= mag[q] != 0;
-    if (bq) sticky |= (mag[wq] & ((1u << bq) - 1u)) != 0;
+  const int sh = bl > 64 ? bl - 64 : 0;
+  const int wq = sh >> 5, bq = sh & 31;
+  unsigned long long w0 = 0, w1 = 0, w2 = 0;
+  uint32_t below = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if (q == wq) w0 = mag[q];
+    if (q == wq + 1) w1 = mag[q];
+    if (q == wq + 2) w2 = mag[q];
+    if (q < wq) below |= mag[q];
   }
-  if (sticky) t |= 1ULL;
+  const unsigned long long lo64 = w0 | (w1 << 32);
+  unsigned long long t = bq ? ((lo64 >> bq) | (w2 << (64 - bq))) : lo64;
+  if (bq) below |= (uint32_t)w0 & ((1u << bq) - 1u);
+  if (below) t |= 1ULL;
   double a_dn, a_up;
   u64_to_dir(t, e + sh, a_dn, a_up);
   if (!neg) {
     lo = a_dn;
     up = a_up;
   } else {
-    lo = -a_up;
-    up = -a_dn;
+    lo = sw_neg(a_up);
+    up = sw_neg(a_dn);
   }
+}
+
+// u32 -> float rounded to nearest (equal to __uint2float_rn) on the FP32
+// pipe: the two 16-bit halves are exact floats, one FMA rounds their sum.
+__device__ __forceinline__ float u32_to_f(uint32_t v) {
+  const float h = __fsub_rn(__uint_as_float(0x4B000000u | (v >> 16)), 8388608.0f);
+  const float l = __fsub_rn(__uint_as_float(0x4B000000u | (v & 0xffffu)), 8388608.0f);
+  return __fmaf_rn(h, 65536.0f, l);
 }
 
 // Exact X = (A'B')(i, j) from its residues (see the file comment); returns
@@ -160,9 +169,8 @@ __device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const uint32_t
   r[4] = (uint32_t)carry;
   // q = floor(S / M) < 2^12 estimated in fp32 (relative error < 2^-20, so
   // off by at most one), then corrected exactly
-  const float Sf = __uint2float_rn(r[4]) * 0x1p64f + __uint2float_rn(r[3]) * 0x1p32f +
-                   __uint2float_rn(r[2]) + __uint2float_rn(r[1]) * 0x1p-32f +
-                   __uint2float_rn(r[0]) * 0x1p-64f;
+  const float Sf = u32_to_f(r[4]) * 0x1p64f + u32_to_f(r[3]) * 0x1p32f + u32_to_f(r[2]) +
+                   u32_to_f(r[1]) * 0x1p-32f + u32_to_f(r[0]) * 0x1p-64f;
   const unsigned int q = (unsigned int)(Sf * invMf);
   if (q) {
     unsigned long long qm[5];

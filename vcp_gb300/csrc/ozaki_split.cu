@@ -27,9 +27,12 @@ __device__ __forceinline__ unsigned long long dbits(double x) {
 }
 
 // bf16 bit pattern of an integer digit |d| <= 256 (exact: the float has at
-// most 9 significant bits, so its low 16 bits are zero).
+// most 9 significant bits, so its low 16 bits are zero).  The float is made
+// on the FP32 pipe -- 1.5 2^23 + d by adding d to the bit pattern, minus
+// 1.5 2^23 (exact for |d| < 2^22) -- instead of an integer conversion, which
+// GB300 issues on its narrow FP64 / conversion pipe.
 __device__ __forceinline__ uint32_t bf16_bits(int d) {
-  return __float_as_uint(__int2float_rn(d)) >> 16;
+  return __float_as_uint(__fadd_rn(__int_as_float(0x4B400000 + d), -12582912.0f)) >> 16;
 }
 
 template <int S>
@@ -331,43 +334,55 @@ __device__ __forceinline__ int dev_sym_residue(unsigned long long a, int neg, in
 }
 
 // Residues on the FP32 pipe (the integer multiply pipe is half as wide).
-// |a| is cut into 12-bit limbs h_t, exact as floats; x = sum_t h_t c_lt with
-// c_lt = 2^(12t) mod m_l < 256 stays below 10 2^20 < 2^24, an exact float;
-// x mod m_l follows from a rounded quotient (off by at most one) and one
-// exact FMA.  The symmetric residue is that of dev_sym_residue, returned as
-// its bf16 bit pattern (|r| <= 128 has at most 8 significant bits).
-constexpr float oz_limb_c(unsigned long long m, int t) {
+// |a| is cut into b-bit limbs h_t (b = 12; b = 14 for the four-limb form,
+// which holds magnitudes <= 2^55), exact as floats, and
+// x = sum_t h_t c_lt with c_lt = 2^(b t) mod m_l taken in [-m_l/2, m_l/2]:
+// |x| <= 128 sum_t |h_t| < 2^23 for every limb form used here (at most 16
+// twelve-bit limbs; four 14-bit limbs whose top one is <= 2^13), an exact
+// float.  One rounded quotient q = rint(RN(x RN(1/m))) then lands within
+// |x / m| 2^-23 (1 + 2^-25) < 1 / m of the exact one, so
+// r = x - q m (one exact FMA) has |r| <= m/2 + 1 - 1/8, i.e. |r| <= 128:
+// a residue of a in the range the slice GEMM's exact chunk sums allow
+// (|r_a r_b| <= 2^14 over 1024 terms), and exact in bf16.
+__host__ __device__ constexpr int oz_limb_bits(int NL) { return NL == 4 ? 14 : 12; }
+constexpr float oz_limb_c(unsigned long long m, int b, int t) {
   unsigned long long c = 1 % m;
-  for (int i = 0; i < t; ++i) c = (c << 12) % m;
-  return (float)c;
+  for (int i = 0; i < t; ++i) c = (c << b) % m;
+  return 2 * c > m ? (float)c - (float)m : (float)c;
 }
 #define OZ_LIMB_ROW(m)                                                                 \
-  {oz_limb_c(m, 0), oz_limb_c(m, 1), oz_limb_c(m, 2), oz_limb_c(m, 3), oz_limb_c(m, 4), \
-   oz_limb_c(m, 5), oz_limb_c(m, 6), oz_limb_c(m, 7), oz_limb_c(m, 8), oz_limb_c(m, 9)}
+  {oz_limb_c(m, 12, 0), oz_limb_c(m, 12, 1), oz_limb_c(m, 12, 2), oz_limb_c(m, 12, 3),   \
+   oz_limb_c(m, 12, 4), oz_limb_c(m, 12, 5), oz_limb_c(m, 12, 6), oz_limb_c(m, 12, 7),   \
+   oz_limb_c(m, 12, 8), oz_limb_c(m, 12, 9)}
+#define OZ_LIMB14_ROW(m) \
+  {oz_limb_c(m, 14, 0), oz_limb_c(m, 14, 1), oz_limb_c(m, 14, 2), oz_limb_c(m, 14, 3)}
 #define OZ_MODF(m) ((float)(m))
 #define OZ_INVF(m) (1.0f / (float)(m))
 __constant__ float c_limbf[OZ_MAX_MODULI][10] = {OZ_MOD_LIST(OZ_LIMB_ROW)};
+__constant__ float c_limbf14[OZ_MAX_MODULI][4] = {OZ_MOD_LIST(OZ_LIMB14_ROW)};
 __constant__ float c_modf[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_MODF)};
 __constant__ float c_invf[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_INVF)};
 
-// Signed 12-bit limbs of (neg ? -a : a) as exact floats:
+// Signed limbs of (neg ? -a : a) as exact floats (b = oz_limb_bits(NL)):
 // h_t = sg (2^23 + v_t) - sg 2^23 with sg = -1 or 1.
 template <int NL>
 __device__ __forceinline__ void limbs12(unsigned long long a, bool neg, float (&h)[NL]) {
-  static_assert(NL <= 6, "64-bit magnitudes have at most 6 limbs");
+  constexpr int B = oz_limb_bits(NL);
+  static_assert(NL * B <= 72, "64-bit magnitudes have at most 6 twelve-bit limbs");
   const float sg = neg ? -1.0f : 1.0f;
 #pragma unroll
   for (int t = 0; t < NL; ++t) {
-    const unsigned v = (unsigned)((a >> (12 * t)) & 0xfffULL);
+    const unsigned v = (unsigned)((a >> (B * t)) & ((1ULL << B) - 1));
     h[t] = __fmaf_rn(sg, __uint_as_float(0x4B000000u | v), -8388608.0f * sg);
   }
 }
 template <int NL>
 __device__ __forceinline__ void limbs12(unsigned __int128 a, bool neg, float (&h)[NL]) {
+  constexpr int B = oz_limb_bits(NL);
   const float sg = neg ? -1.0f : 1.0f;
 #pragma unroll
   for (int t = 0; t < NL; ++t) {
-    const unsigned v = (unsigned)((a >> (12 * t)) & 0xfffULL);
+    const unsigned v = (unsigned)((a >> (B * t)) & ((1ULL << B) - 1));
     h[t] = __fmaf_rn(sg, __uint_as_float(0x4B000000u | v), -8388608.0f * sg);
   }
 }
@@ -377,17 +392,16 @@ __device__ __forceinline__ float rint_small(float v) {
   return __fsub_rn(__fadd_rn(v, 12582912.0f), 12582912.0f);
 }
 
-// Residue r = x mod m_l with |r| <= m_l / 2 <= 128 of the integer given by
-// its signed limbs: two rounded-quotient steps, all on the FP32 pipe (the
-// first leaves |r0| < m/2 + 2, the second lands in [-m/2, m/2]).
+// Residue r of the integer given by its signed limbs, |r| <= 128 (see
+// above); all on the FP32 pipe.
 template <int NL>
 __device__ __forceinline__ float res_sym(const float (&h)[NL], int l) {
   const float m = c_modf[l], inv = c_invf[l];
   float x = h[0];
 #pragma unroll
-  for (int t = 1; t < NL; ++t) x = __fmaf_rn(h[t], c_limbf[l][t], x);
-  const float r0 = __fmaf_rn(-rint_small(__fmul_rn(x, inv)), m, x);
-  return __fmaf_rn(-rint_small(__fmul_rn(r0, inv)), m, r0);
+  for (int t = 1; t < NL; ++t)
+    x = __fmaf_rn(h[t], NL == 4 ? c_limbf14[l][t] : c_limbf[l][t], x);
+  return __fmaf_rn(-rint_small(__fmul_rn(x, inv)), m, x);
 }
 
 // bf16 patterns of two small integers (exact: at most 8 significant bits) in
@@ -920,9 +934,13 @@ int oz_prepare_left_finish(const OzProblem& pb, OzWorkspace& ws, cudaStream_t st
     return VCPCU_ERR_UNSUPPORTED;
   }
   if (!pb.crt) return VCPCU_OK;  // the slice form splits both factors in launch_splits
-  // |A'| < 2^(w-1): five 12-bit limbs up to w = 61, six up to 73
+  // |A'| <= 2^(w-1): four 14-bit limbs up to w = 56, five 12-bit limbs up to
+  // w = 61, six up to 73
   dim3 g2(pb.Kp / 64, pb.Mp / 32);
-  if (pb.w <= 61)
+  if (pb.w <= 56)
+    oz_split_left_crt<2, 4><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, pb.L,
+                                                pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r, ws.asum);
+  else if (pb.w <= 61)
     oz_split_left_crt<2, 5><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, pb.L,
                                                 pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r, ws.asum);
   else
@@ -934,7 +952,11 @@ int oz_prepare_left_finish(const OzProblem& pb, OzWorkspace& ws, cudaStream_t st
 
 int oz_prepare_right_crt(const OzProblem& pb, const double* B, long ldb, OzWorkspace& ws,
                          cudaStream_t st) {
-  if (pb.w <= 61)
+  if (pb.w <= 56)
+    oz_split_right_crt<2, 4><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L, pb.w,
+                                                    ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,
+                                                    ws.F2, ws.beta, ws.flag);
+  else if (pb.w <= 61)
     oz_split_right_crt<2, 5><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L, pb.w,
                                                     ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,
                                                     ws.F2, ws.beta, ws.flag);
