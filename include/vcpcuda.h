@@ -154,13 +154,15 @@ int vcpcu_igemm_dev(int m, int n, int k, const double* A, int lda,
 /* Host-pointer, synchronous form of vcpcu_igemm_dev (lda = m, ldb = k,
  * ldc = m): the drop-in for a std::vector<kv::interval<double>> product.
  * When the tensor-core CRT form runs (form OZAKI, or AUTO choosing it) and
- * n >= 2048, the copies overlap the computation: A goes to the device in
- * column chunks, B in column panels (one per 1024 columns, at most 4; the
- * environment variable VCPCU_HOST_PANELS overrides the count, 1 turns the
- * overlap off), each panel is prepared, multiplied and reassembled as soon
- * as it lands, and its columns of C come back while the next panel
- * computes.  The result is bit-identical to one vcpcu_igemm_dev call.
- * Pinned (page-locked) host buffers let the copies run asynchronously. */
+ * n >= 2048, the copies overlap the computation: C is cut into blocks (row
+ * blocks of 2048 rows and column blocks of 1024 columns, at most 4 of each;
+ * the environment variables VCPCU_HOST_ROW_PANELS and VCPCU_HOST_PANELS
+ * override the counts, 1 and 1 turn the overlap off), A goes to the device in
+ * row blocks and B in column blocks, interleaved, each block of C is
+ * prepared, multiplied and reassembled as soon as its operands have landed,
+ * and it comes back while the next block computes.  The result is
+ * bit-identical to one vcpcu_igemm_dev call.  Pinned (page-locked) host
+ * buffers let the copies run asynchronously. */
 int vcpcu_igemm(int m, int n, int k, const double* A, const double* B,
                 double* C, int form, int slices);
 

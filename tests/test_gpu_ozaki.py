@@ -208,18 +208,22 @@ def test_ozaki_midrad_paths(cuda_lib, oracle, crt):
     check_contains(oracle, m, n, k, A, B, C)
 
 
-@pytest.mark.parametrize("shape,panels", [((300, 2048, 500), None), ((129, 700, 1100), "2"),
-                                          ((64, 1300, 70), "5"), ((33, 600, 0), "3")])
-def test_ozaki_host_pipeline_bitexact(cuda_lib, shape, panels, monkeypatch):
-    """The host-pointer call overlaps its copies with the panels of the
-    product (column panels of B and C, A in column chunks); the result is
-    bit-identical to the one-shot device call, including a last panel of
-    smaller padded width and an empty inner dimension."""
+@pytest.mark.parametrize("shape,panels,row_panels", [
+    ((300, 2048, 500), None, None), ((129, 700, 1100), "2", "2"), ((64, 1300, 70), "5", "1"),
+    ((33, 600, 0), "3", "2"), ((700, 900, 300), "2", "3"), ((4096, 256, 64), "1", "4")])
+def test_ozaki_host_pipeline_bitexact(cuda_lib, shape, panels, row_panels, monkeypatch):
+    """The host-pointer call overlaps its copies with blocks of the product
+    (row blocks of A, column blocks of B, interleaved uploads, each block of
+    C sent down when done); the result is bit-identical to the one-shot
+    device call, including last blocks of smaller padded size, a row block
+    of one row and an empty inner dimension."""
     import torch
     from vcp_gb300 import _lib
     m, n, k = shape
     if panels is not None:
         monkeypatch.setenv("VCPCU_HOST_PANELS", panels)
+    if row_panels is not None:
+        monkeypatch.setenv("VCPCU_HOST_ROW_PANELS", row_panels)
     rng = np.random.default_rng(m + n + k)
     A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40) if k else np.zeros(0)
     B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40) if k else np.zeros(0)

@@ -418,8 +418,8 @@ int pipe_event(PipeGuard& g, cudaStream_t rec, cudaStream_t waiter) {
 }  // namespace
 
 int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const double* B, double* C,
-                               int slices, int panels, cudaStream_t s, cudaStream_t up,
-                               cudaStream_t down) {
+                               int slices, int panels, int row_panels, cudaStream_t s,
+                               cudaStream_t up, cudaStream_t down) {
   const int nslices = slices > 0 ? slices : 8;
   if (k > (1 << 20)) {
     set_error("igemm (Ozaki form): inner dimension %d above the supported 2^20", k);
@@ -428,77 +428,120 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
   if (m <= 0 || n <= 0) return VCPCU_OK;
   if (k < 0) k = 0;
   if (panels < 1) panels = 1;
+  if (row_panels < 1) row_panels = 1;
+  OzPlan plan;  // the whole product: its workspace holds every block's planes
+  oz_make_plan(m, n, k, nslices, 2, &plan, 1);
+  const OzProblem& pb = plan.pb;
   int nb = (n + panels - 1) / panels;
-  nb = (nb + OZ_BN - 1) / OZ_BN * OZ_BN;  // whole column tiles per panel
+  nb = (nb + OZ_BN - 1) / OZ_BN * OZ_BN;  // whole column tiles per block
   panels = (n + nb - 1) / nb;
-  OzPlan plan;  // the widest panel; the left factor whole
-  oz_make_plan(m, nb < n ? nb : n, k, nslices, 2, &plan, 1);
+  int mb = (m + row_panels - 1) / row_panels;
+  mb = (mb + OZ_BM - 1) / OZ_BM * OZ_BM;  // whole row tiles per block
+  row_panels = (m + mb - 1) / mb;
   const size_t na = 2 * (size_t)m * k, nbe = 2 * (size_t)k * n, nc = 2 * (size_t)m * n;
   const size_t off_b = al256(na * 8), off_c = off_b + al256(nbe * 8),
                off_w = off_c + al256(nc * 8);
   Scratch buf;
-  int st = buf.alloc(off_w + oz_workspace_bytes(plan.pb), s);
+  int st = buf.alloc(off_w + oz_workspace_bytes(pb), s);
   if (st) return st;
   PipeGuard g(s, up, down);  // destroyed before buf: drains every stream first
   double* dA = (double*)buf.ptr;
   double* dB = (double*)((uint8_t*)buf.ptr + off_b);
   double* dC = (double*)((uint8_t*)buf.ptr + off_c);
   OzWorkspace ws;
-  oz_carve_workspace(plan.pb, (uint8_t*)buf.ptr + off_w, &ws);
+  oz_carve_workspace(pb, (uint8_t*)buf.ptr + off_w, &ws);
   // the copy streams may touch the memory only after its allocation on s
   if ((st = pipe_event(g, s, up)) || (st = pipe_event(g, s, down))) return st;
+  if ((st = oz_prepare_left_begin(pb, ws, s))) return st;
 
-  // A in column chunks, each one's midrad / row maxima as soon as it lands
-  const int achunks = k >= 4 ? 4 : k;
-  if ((st = oz_prepare_left_begin(plan.pb, ws, s))) return st;
-  for (int c = 0; c < achunks; ++c) {
-    const int k0 = (int)((long long)k * c / achunks), k1 = (int)((long long)k * (c + 1) / achunks);
-    VCPCU_CUDA_TRY(cudaMemcpyAsync(dA + 2 * (size_t)k0 * m, A + 2 * (size_t)k0 * m,
-                                   2 * (size_t)(k1 - k0) * m * sizeof(double),
-                                   cudaMemcpyHostToDevice, up));
-    if ((st = pipe_event(g, up, s))) return st;
-    if ((st = oz_prepare_left_rowmax(plan.pb, dA, m, k0, k1, ws, s))) return st;
+  // uploads, interleaved: A's row block t, then B's column block t
+  const size_t rowb = 2 * sizeof(double);  // bytes of one interval
+  std::vector<cudaEvent_t> evA(row_panels), evB(panels);
+  for (int t = 0; t < row_panels || t < panels; ++t) {
+    if (t < row_panels) {
+      const int i0 = t * mb, mv = (m - i0 < mb) ? m - i0 : mb;
+      if (k > 0)
+        VCPCU_CUDA_TRY(cudaMemcpy2DAsync(dA + 2 * (size_t)i0, m * rowb, A + 2 * (size_t)i0,
+                                         m * rowb, mv * rowb, k, cudaMemcpyHostToDevice, up));
+      if (!(evA[t] = g.make())) return cuda_fail(cudaErrorUnknown, "cudaEventCreate");
+      VCPCU_CUDA_TRY(cudaEventRecord(evA[t], up));
+    }
+    if (t < panels) {
+      const int j0 = t * nb, wj = (n - j0 < nb) ? n - j0 : nb;
+      if (k > 0)
+        VCPCU_CUDA_TRY(cudaMemcpyAsync(dB + 2 * (size_t)j0 * k, B + 2 * (size_t)j0 * k,
+                                       2 * (size_t)wj * k * sizeof(double),
+                                       cudaMemcpyHostToDevice, up));
+      if (!(evB[t] = g.make())) return cuda_fail(cudaErrorUnknown, "cudaEventCreate");
+      VCPCU_CUDA_TRY(cudaEventRecord(evB[t], up));
+    }
   }
-  if ((st = oz_prepare_left_finish(plan.pb, ws, s))) return st;
+
+  // block (I, J) of C: its slice GEMMs on views of the whole planes, its
+  // reassembly, and its download
   long long flops = 0;
-  for (int J = 0; J < panels; ++J) {
+  auto block = [&](int I, int J) -> int {
+    const int i0 = I * mb, mv = (m - i0 < mb) ? m - i0 : mb;
     const int j0 = J * nb, wj = (n - j0 < nb) ? n - j0 : nb;
-    if (k > 0) {
-      VCPCU_CUDA_TRY(cudaMemcpyAsync(dB + 2 * (size_t)j0 * k, B + 2 * (size_t)j0 * k,
-                                     2 * (size_t)wj * k * sizeof(double), cudaMemcpyHostToDevice,
-                                     up));
-    }
-    if ((st = pipe_event(g, up, s))) return st;
     OzPlan pj;
-    if (wj == plan.pb.N) {
-      pj = plan;
-    } else {
-      oz_make_plan(m, wj, k, nslices, 2, &pj, 1);
+    oz_make_plan(mv, wj, k, nslices, 2, &pj, 1);
+    OzWorkspace v = ws;
+    const size_t Kp = (size_t)pb.Kp;
+    v.a_mid = ws.a_mid + (size_t)i0 * Kp;
+    v.a_p = ws.a_p + (size_t)i0 * Kp;
+    v.a_r = ws.a_r + (size_t)i0 * Kp;
+    v.a_pstride = (size_t)pb.Mp * Kp;
+    v.b_mid = ws.b_mid + (size_t)j0 * Kp;
+    v.b_r = ws.b_r + (size_t)j0 * Kp;
+    v.b_s = ws.b_s + (size_t)j0 * Kp;
+    v.b_pstride = (size_t)pb.Np * Kp;
+    v.rowmax = ws.rowmax + 3 * (size_t)i0;
+    v.E3 = ws.E3 + 3 * (size_t)i0;
+    v.delta = ws.delta + i0;
+    v.asum = ws.asum + 2 * (size_t)i0;
+    v.F2 = ws.F2 + 2 * (size_t)j0;
+    v.beta = ws.beta + j0;
+    int e;
+    if ((e = oz_run_gemm(pj, OZ_RAD_SET, v, nullptr, 0, s))) return e;
+    if ((e = oz_run_gemm(pj, OZ_RAD_ADD, v, nullptr, 0, s))) return e;
+    if ((e = oz_run_gemm(pj, OZ_CRT, v, nullptr, 0, s))) return e;
+    double* cblk = dC + 2 * ((size_t)i0 + (size_t)j0 * m);
+    if ((e = oz_crt_assemble(pj, v, cblk, m, s))) return e;
+    if ((e = pipe_event(g, s, down))) return e;
+    VCPCU_CUDA_TRY(cudaMemcpy2DAsync(C + 2 * ((size_t)i0 + (size_t)j0 * m), m * rowb, cblk,
+                                     m * rowb, mv * rowb, wj, cudaMemcpyDeviceToHost, down));
+    flops += 2LL * mv * wj * (long long)k * (pj.pb.L + 2LL * pj.rad.npairs);
+    return VCPCU_OK;
+  };
+  // compute in arrival order: each new row block of A meets the column
+  // blocks of B already prepared, and each new column block the row blocks
+  for (int t = 0; t < row_panels || t < panels; ++t) {
+    if (t < row_panels) {
+      const int i0 = t * mb, rows = (pb.Mp - i0 < mb) ? pb.Mp - i0 : mb;
+      VCPCU_CUDA_TRY(cudaStreamWaitEvent(s, evA[t], 0));
+      if ((st = oz_prepare_left_rows(pb, dA, m, i0, rows, ws, s))) return st;
+      for (int J = 0; J < t && J < panels; ++J)
+        if ((st = block(t, J))) return st;
     }
-    OzWorkspace wsj = ws;  // the panel's planes use its own padded width
-    wsj.b_r = ws.b_mid + (size_t)pj.pb.mplanes * pj.pb.Np * pj.pb.Kp;
-    wsj.b_s = wsj.b_r + (size_t)pj.pb.sr * pj.pb.Np * pj.pb.Kp;
-    if ((st = oz_prepare_right_crt(pj.pb, dB + 2 * (size_t)j0 * k, k > 0 ? k : 1, wsj, s)))
-      return st;
-    if ((st = oz_run_gemm(pj, OZ_RAD_SET, wsj, nullptr, 0, s))) return st;
-    if ((st = oz_run_gemm(pj, OZ_RAD_ADD, wsj, nullptr, 0, s))) return st;
-    if ((st = oz_run_gemm(pj, OZ_CRT, wsj, nullptr, 0, s))) return st;
-    if ((st = oz_crt_assemble(pj, wsj, dC + 2 * (size_t)j0 * m, m, s))) return st;
-    if ((st = pipe_event(g, s, down))) return st;
-    VCPCU_CUDA_TRY(cudaMemcpyAsync(C + 2 * (size_t)j0 * m, dC + 2 * (size_t)j0 * m,
-                                   2 * (size_t)wj * m * sizeof(double), cudaMemcpyDeviceToHost,
-                                   down));
-    flops += 2LL * m * wj * (long long)k * (pj.pb.L + 2LL * pj.rad.npairs);
+    if (t < panels) {
+      const int j0 = t * nb, cols = (pb.Np - j0 < nb) ? pb.Np - j0 : nb;
+      VCPCU_CUDA_TRY(cudaStreamWaitEvent(s, evB[t], 0));
+      if ((st = oz_prepare_right_crt(pb, dB, k > 0 ? k : 1, ws, s, j0, cols,
+                                     (size_t)pb.Np * pb.Kp)))
+        return st;
+      for (int I = 0; I <= t && I < row_panels; ++I)
+        if ((st = block(I, t))) return st;
+    }
   }
   oz_profile_add_flops(flops);
   oz_merge_status(ws.flag, s);
-  // A non-finite entry of a later B panel leaves earlier panels finite; the
-  // whole result is NaN then, as in the one-shot product.
+  // A non-finite entry seen late leaves earlier blocks finite; the whole
+  // result is NaN then, as in the one-shot product.
   int hflag[2] = {0, 0};
   VCPCU_CUDA_TRY(cudaMemcpyAsync(hflag, ws.flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
   VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
   VCPCU_CUDA_TRY(cudaStreamSynchronize(down));
-  if ((hflag[0] != 0 || hflag[1] != 0) && panels > 1) {
+  if ((hflag[0] != 0 || hflag[1] != 0) && panels * row_panels > 1) {
     oz_fill_nan<<<152 * 8, 256, 0, s>>>(nc, dC);
     VCPCU_LAUNCH_CHECK("oz_fill_nan");
     VCPCU_CUDA_TRY(cudaMemcpyAsync(C, dC, nc * sizeof(double), cudaMemcpyDeviceToHost, s));

@@ -40,6 +40,9 @@ struct OzWorkspace {
   long long* W;                       // [Np][Mp] int64 fold buffer (slice form)
   int32_t* P;                         // [2 slots][Np][Mp] folds of the two radius products
   int* flag;                          // [0] non-finite input, [1] device wait timeout
+  // Plane strides (elements) of the left / right digit planes when they are
+  // a row / column block of larger planes; 0: Mp Kp / Np Kp.
+  size_t a_pstride = 0, b_pstride = 0;
 };
 
 // Ordered list of slice pairs grouped by t = p + q (1-based slice numbers).
@@ -136,7 +139,14 @@ int oz_prepare_left_rowmax(const OzProblem& pb, const double* A, long lda, int k
                            OzWorkspace& ws, cudaStream_t st);
 int oz_prepare_left_finish(const OzProblem& pb, OzWorkspace& ws, cudaStream_t st);
 int oz_prepare_right_crt(const OzProblem& pb, const double* B, long ldb, OzWorkspace& ws,
-                         cudaStream_t st);
+                         cudaStream_t st, int colbase = 0, int cols = -1, size_t pstride = 0);
+// Left planes of the row block [i0, i0 + rows) (i0 and rows multiples of
+// 128, padding rows included) from the rows of A alone: midrad, row maxima,
+// exponents and planes (CRT form), after oz_prepare_left_begin.  B's column
+// blocks: oz_prepare_right_crt with colbase = j0 and cols its padded width
+// (B points at column 0; planes, F2 and beta of the whole right factor).
+int oz_prepare_left_rows(const OzProblem& pb, const double* A, long lda, int i0, int rows,
+                         OzWorkspace& ws, cudaStream_t st);
 // t_set < 0: the radius product of OZ_RAD_SET writes T, that of OZ_RAD_ADD
 // adds to it; 0 / 1 force add / write.
 int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, long ldc,
@@ -256,16 +266,16 @@ int oz_group_record(OzGroupPlan* g, unsigned long long* t_first, unsigned long l
 void oz_group_free(OzGroupPlan* g, cudaStream_t s);
 
 // CRT-form product of host matrices (column-major, lda = m, ldb = k,
-// ldc = m) with the host<->device copies overlapped: A goes up in column
-// chunks (its row maxima computed as each arrives), B in column panels;
-// each panel's planes, slice GEMMs and reassembly run as soon as it is on the
-// device, and its result columns go down on `down` while the next panel
-// computes.  Streams: `s` computes, `up` / `down` copy.  Bit-identical to
-// ozaki_igemm on the same operands (every entry depends on its row of A and
-// column of B only).  Synchronises before returning.
+// ldc = m) with the host<->device copies overlapped: C is cut into
+// row_panels x panels blocks; A goes up in row blocks and B in column
+// blocks, interleaved, and each block of C is multiplied, reassembled and
+// sent down as soon as its row block of A and column block of B are on the
+// device and prepared.  Streams: `s` computes, `up` / `down` copy.
+// Bit-identical to ozaki_igemm on the same operands (every entry depends on
+// its row of A and column of B only).  Synchronises before returning.
 int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const double* B, double* C,
-                               int slices, int panels, cudaStream_t s, cudaStream_t up,
-                               cudaStream_t down);
+                               int slices, int panels, int row_panels, cudaStream_t s,
+                               cudaStream_t up, cudaStream_t down);
 
 // point_mask as OzPlan::point_mask (the caller guarantees the zero radii).
 int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,

@@ -344,6 +344,8 @@ __device__ __forceinline__ void assemble_quad(
   }
 }
 
+// Thread = 4 consecutive rows of one column; blockIdx.y strides over the
+// columns (no 64-bit index division).
 __global__ void __launch_bounds__(256)
 oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __restrict__ res,
                        size_t plane, const int* __restrict__ E3, const int* __restrict__ F2,
@@ -353,11 +355,11 @@ oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __rest
                        const __grid_constant__ CrtConst cc, const __grid_constant__ OzRadConst rc) {
   const bool nonfinite = flag[0] != 0 || flag[1] != 0;
   const int Mq = (M + 3) >> 2;
-  const long total = (long)Mq * N;
-  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long)gridDim.x * blockDim.x)
-    assemble_quad(4 * (int)(idx % Mq), (int)(idx / Mq), M, Mp, L, w, res, plane, E3, F2, asum,
-                  beta, P, C, ldc, nonfinite, cc.Q, cc.M, cc.invMf, rc);
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= Mq) return;
+  for (int j = blockIdx.y; j < N; j += gridDim.y)
+    assemble_quad(4 * q, j, M, Mp, L, w, res, plane, E3, F2, asum, beta, P, C, ldc, nonfinite,
+                  cc.Q, cc.M, cc.invMf, rc);
 }
 
 __device__ __forceinline__ int gfind(const int* __restrict__ prefix, int nprob, int x) {
@@ -410,11 +412,10 @@ int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long l
   const double Md = (double)cc.M[3] * 0x1p96 + (double)cc.M[2] * 0x1p64 +
                     (double)cc.M[1] * 0x1p32 + (double)cc.M[0];
   cc.invMf = (float)(0x1p64 / Md);
-  const long total = (long)((pb.M + 3) / 4) * pb.N;
-  long blocks = (total + 255) / 256;
-  if (blocks > 152L * 64) blocks = 152L * 64;
-  if (blocks < 1) blocks = 1;
-  oz_crt_assemble_kernel<<<(int)blocks, 256, 0, st>>>(
+  if (pb.M <= 0 || pb.N <= 0) return VCPCU_OK;
+  const int Mq = (pb.M + 3) / 4;
+  dim3 grid((Mq + 255) / 256, pb.N < 65535 ? pb.N : 65535);
+  oz_crt_assemble_kernel<<<grid, 256, 0, st>>>(
       pb.M, pb.N, pb.Mp, pb.L, pb.w, ws.res, (size_t)pb.Np * pb.Mp, ws.E3, ws.F2, ws.asum,
       ws.beta, ws.P, C, ldc, ws.flag, cc, oz_rad_const(plan));
   VCPCU_LAUNCH_CHECK("oz_crt_assemble_kernel");

@@ -446,14 +446,16 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-int make_tmap(CUtensorMap* m, const void* base, int Kp, int rows, int planes, int box_rows) {
+int make_tmap(CUtensorMap* m, const void* base, int Kp, int rows, int planes, int box_rows,
+              size_t pstride = 0) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) {
     set_error("cuTensorMapEncodeTiled is not available from the driver");
     return VCPCU_ERR_CUDA;
   }
   cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)planes};
-  cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)Kp * rows * 2};
+  cuuint64_t strides[2] = {(cuuint64_t)Kp * 2,
+                           (cuuint64_t)(pstride ? pstride : (size_t)Kp * rows) * 2};
   cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides,
@@ -517,8 +519,8 @@ int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, 
     a.res = ws.res;
     for (int l = 0; l < pb.L; ++l) a.moduli[l] = OZ_MODULI[l];
   }
-  if ((st_ = make_tmap(&a.tmA, ap, pb.Kp, pb.Mp, apl, OZ_BM))) return st_;
-  if ((st_ = make_tmap(&a.tmB, bp, pb.Kp, pb.Np, bpl, OZ_BN))) return st_;
+  if ((st_ = make_tmap(&a.tmA, ap, pb.Kp, pb.Mp, apl, OZ_BM, ws.a_pstride))) return st_;
+  if ((st_ = make_tmap(&a.tmB, bp, pb.Kp, pb.Np, bpl, OZ_BN, ws.b_pstride))) return st_;
   a.M = pb.M; a.N = pb.N; a.Mp = pb.Mp; a.Np = pb.Np; a.Kp = pb.Kp;
   a.tiles_m = pb.Mp / OZ_BM;
   a.tiles_n = pb.Np / OZ_BN;

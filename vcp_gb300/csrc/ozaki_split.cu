@@ -65,12 +65,12 @@ __device__ __forceinline__ void digits_of(double x, int E, int up, int (&d)[S]) 
 
 // ---------------------------------------------------------------- left factor
 // Pass 1: kv midrad of every entry, stored as the planes mA, rA (column-major,
-// ld = M), and the row maxima of |mA|, P = |mA| +ru rA and rA as double bit
+// ld = ldm), and the row maxima of |mA|, P = |mA| +ru rA and rA as double bit
 // patterns (non-negative doubles order like their bit patterns).
 // Block: 32 rows x 8 column phases over a column range.
 __global__ void __launch_bounds__(256)
 oz_rowmax_left(int M, int K, const double* __restrict__ A, long lda, int cols_per_block,
-               double* __restrict__ mA, double* __restrict__ rA,
+               double* __restrict__ mA, double* __restrict__ rA, long ldm,
                unsigned long long* __restrict__ mx, int* __restrict__ flag) {
   __shared__ unsigned long long red[3][32];
   const int lane = threadIdx.x & 31, ph = threadIdx.x >> 5;
@@ -93,8 +93,8 @@ oz_rowmax_left(int M, int K, const double* __restrict__ A, long lda, int cols_pe
       } else {
         bad = true;
       }
-      mA[i + (long)c * M] = m;
-      rA[i + (long)c * M] = r;
+      mA[i + (long)c * ldm] = m;
+      rA[i + (long)c * ldm] = r;
     }
   }
   if (bad) atomicOr(flag, 1);
@@ -436,7 +436,7 @@ __device__ __forceinline__ long long crt_int(double x, int E, int w) {
 // the loads of mA / rA are coalesced across the warp and each lane writes 8
 // bf16 (16 bytes) per plane -- no shared-memory transpose, full occupancy.
 // FROM_A: midrad again from the interval matrix X (ld ldx) instead of the
-// stored planes mA = X, rA (ld M).  Planes rows are rowbase + i (stacked
+// stored planes mA = X, rA (ld ldx).  Planes rows are rowbase + i (stacked
 // problems), pstride elements apart; E3 and asum point at row 0 of this
 // problem.
 template <int SR, int NL, bool FROM_A>
@@ -476,8 +476,8 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
             const double2 e = *reinterpret_cast<const double2*>(X + 2 * (i + (long)k * ldx));
             if (sw_finite(e.x) && sw_finite(e.y)) sw_midrad(e.x, e.y, m, r, p);
           } else {
-            m = X[i + (long)k * M];
-            r = rA[i + (long)k * M];
+            m = X[i + (long)k * ldx];
+            r = rA[i + (long)k * ldx];
             p = sw_add_ru_pos(oz_abs(m), r);
           }
         }
@@ -527,14 +527,18 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
   }
 }
 
+// One row range of the left factor: rows [0, M) of this launch are rows
+// rowbase.. of the planes (pstride elements apart); mA / rA (ld ldx), E3
+// and asum point at the range's first row.
 template <int SR, int NL>
 __global__ void __launch_bounds__(256, 4)
-oz_split_left_crt(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
-                  const double* __restrict__ rA, int L, int w, const int* __restrict__ E3,
-                  uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_p,
-                  uint16_t* __restrict__ planes_r, unsigned long long* __restrict__ asum) {
-  split_left_crt_body<SR, NL, false>(blockIdx.x, blockIdx.y, M, K, Kp, (size_t)Mp * Kp, 0, mA,
-                                     rA, M, L, w, E3, planes_m, planes_p, planes_r, asum);
+oz_split_left_crt(int M, int K, int Kp, size_t pstride, int rowbase,
+                  const double* __restrict__ mA, const double* __restrict__ rA, long ldx, int L,
+                  int w, const int* __restrict__ E3, uint16_t* __restrict__ planes_m,
+                  uint16_t* __restrict__ planes_p, uint16_t* __restrict__ planes_r,
+                  unsigned long long* __restrict__ asum) {
+  split_left_crt_body<SR, NL, false>(blockIdx.x, blockIdx.y, M, K, Kp, pstride, rowbase, mA, rA,
+                                     ldx, L, w, E3, planes_m, planes_p, planes_r, asum);
 }
 
 // Right factor, CRT form, one block per column.  Pass 1 (thread t takes
@@ -664,12 +668,13 @@ __device__ __forceinline__ void split_right_crt_body(int j, int jst, int K, int 
 
 template <int SR, int NL>
 __global__ void __launch_bounds__(256, 3)
-oz_split_right_crt(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb,
-                   int L, int w, double* __restrict__ mBp, double* __restrict__ rBp,
+oz_split_right_crt(int K, int N, int Kp, int colbase, size_t pstride,
+                   const double* __restrict__ B, long ldb, int L, int w,
+                   double* __restrict__ mBp, double* __restrict__ rBp,
                    uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_r,
                    uint16_t* __restrict__ planes_s, int* __restrict__ F2,
                    double* __restrict__ beta, int* __restrict__ flag) {
-  split_right_crt_body<SR, NL, true>(blockIdx.x, blockIdx.x, K, N, Kp, (size_t)Np * Kp, B, ldb,
+  split_right_crt_body<SR, NL, true>(blockIdx.x, colbase + blockIdx.x, K, N, Kp, pstride, B, ldb,
                                      L, w, mBp, rBp, planes_m, planes_r, planes_s, F2, beta,
                                      flag);
 }
@@ -920,11 +925,44 @@ int oz_prepare_left_rowmax(const OzProblem& pb, const double* A, long lda, int k
   const int cpb = 256;
   dim3 g1((M + 31) / 32, (kc + cpb - 1) / cpb);
   oz_rowmax_left<<<g1, 256, 0, st>>>(M, kc, A + 2 * (long)k0 * lda, lda, cpb,
-                                     ws.midA + (size_t)k0 * M, ws.radA + (size_t)k0 * M,
+                                     ws.midA + (size_t)k0 * M, ws.radA + (size_t)k0 * M, M,
                                      ws.rowmax, ws.flag);
   VCPCU_LAUNCH_CHECK("oz_rowmax_left");
   return VCPCU_OK;
 }
+
+namespace {
+// Residue and radius-digit planes (CRT form) of rows [i0, i0 + rows) of the
+// left factor, rows a multiple of 32 (padding rows at the end of A give zero
+// planes); the exponents of those rows are set.
+int split_left_rows(const OzProblem& pb, int i0, int rows, OzWorkspace& ws, cudaStream_t st) {
+  if (pb.sr != 2) {
+    set_error("Ozaki form: radius slice count %d is not built (2 is)", pb.sr);
+    return VCPCU_ERR_UNSUPPORTED;
+  }
+  if (rows <= 0) return VCPCU_OK;
+  const int mv = pb.M - i0 < rows ? (pb.M - i0 > 0 ? pb.M - i0 : 0) : rows;  // valid rows
+  const size_t pstride = (size_t)pb.Mp * pb.Kp;
+  dim3 g2(pb.Kp / 64, rows / 32);
+  const double* mA = ws.midA + i0;
+  const double* rA = ws.radA + i0;
+  const int* E3 = ws.E3 + 3 * (size_t)i0;
+  unsigned long long* asum = ws.asum + 2 * (size_t)i0;
+  // |A'| <= 2^(w-1): four 14-bit limbs up to w = 56, five 12-bit limbs up to
+  // w = 61, six up to 73
+  if (pb.w <= 56)
+    oz_split_left_crt<2, 4><<<g2, 256, 0, st>>>(mv, pb.K, pb.Kp, pstride, i0, mA, rA, pb.M, pb.L,
+                                                pb.w, E3, ws.a_mid, ws.a_p, ws.a_r, asum);
+  else if (pb.w <= 61)
+    oz_split_left_crt<2, 5><<<g2, 256, 0, st>>>(mv, pb.K, pb.Kp, pstride, i0, mA, rA, pb.M, pb.L,
+                                                pb.w, E3, ws.a_mid, ws.a_p, ws.a_r, asum);
+  else
+    oz_split_left_crt<2, 6><<<g2, 256, 0, st>>>(mv, pb.K, pb.Kp, pstride, i0, mA, rA, pb.M, pb.L,
+                                                pb.w, E3, ws.a_mid, ws.a_p, ws.a_r, asum);
+  VCPCU_LAUNCH_CHECK("oz_split_left_crt");
+  return VCPCU_OK;
+}
+}  // namespace
 
 int oz_prepare_left_finish(const OzProblem& pb, OzWorkspace& ws, cudaStream_t st) {
   oz_exponents<<<(pb.Mp + 255) / 256, 256, 0, st>>>(pb.Mp, ws.rowmax, 3, ws.E3);
@@ -934,36 +972,43 @@ int oz_prepare_left_finish(const OzProblem& pb, OzWorkspace& ws, cudaStream_t st
     return VCPCU_ERR_UNSUPPORTED;
   }
   if (!pb.crt) return VCPCU_OK;  // the slice form splits both factors in launch_splits
-  // |A'| <= 2^(w-1): four 14-bit limbs up to w = 56, five 12-bit limbs up to
-  // w = 61, six up to 73
-  dim3 g2(pb.Kp / 64, pb.Mp / 32);
-  if (pb.w <= 56)
-    oz_split_left_crt<2, 4><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, pb.L,
-                                                pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r, ws.asum);
-  else if (pb.w <= 61)
-    oz_split_left_crt<2, 5><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, pb.L,
-                                                pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r, ws.asum);
-  else
-    oz_split_left_crt<2, 6><<<g2, 256, 0, st>>>(pb.M, pb.K, pb.Mp, pb.Kp, ws.midA, ws.radA, pb.L,
-                                                pb.w, ws.E3, ws.a_mid, ws.a_p, ws.a_r, ws.asum);
-  VCPCU_LAUNCH_CHECK("oz_split_left_crt");
-  return VCPCU_OK;
+  return split_left_rows(pb, 0, pb.Mp, ws, st);
+}
+
+int oz_prepare_left_rows(const OzProblem& pb, const double* A, long lda, int i0, int rows,
+                         OzWorkspace& ws, cudaStream_t st) {
+  const int mv = pb.M - i0 < rows ? (pb.M - i0 > 0 ? pb.M - i0 : 0) : rows;
+  if (mv > 0 && pb.K > 0) {
+    const int cpb = 256;
+    dim3 g1((mv + 31) / 32, (pb.K + cpb - 1) / cpb);
+    oz_rowmax_left<<<g1, 256, 0, st>>>(mv, pb.K, A + 2 * (long)i0, lda, cpb, ws.midA + i0,
+                                       ws.radA + i0, pb.M, ws.rowmax + 3 * (size_t)i0, ws.flag);
+    VCPCU_LAUNCH_CHECK("oz_rowmax_left");
+  }
+  oz_exponents<<<(rows + 255) / 256, 256, 0, st>>>(rows, ws.rowmax + 3 * (size_t)i0, 3,
+                                                   ws.E3 + 3 * (size_t)i0);
+  VCPCU_LAUNCH_CHECK("oz_exponents");
+  return split_left_rows(pb, i0, rows, ws, st);
 }
 
 int oz_prepare_right_crt(const OzProblem& pb, const double* B, long ldb, OzWorkspace& ws,
-                         cudaStream_t st) {
+                         cudaStream_t st, int colbase, int cols, size_t pstride) {
+  if (cols < 0) cols = pb.Np;
+  if (!pstride) pstride = (size_t)pb.Np * pb.Kp;
+  const int nv = pb.N - colbase < cols ? (pb.N - colbase > 0 ? pb.N - colbase : 0) : cols;
+  if (cols <= 0) return VCPCU_OK;
+#define OZ_RIGHT_CRT(NL)                                                                         \
+  oz_split_right_crt<2, NL><<<cols, 256, 0, st>>>(pb.K, nv, pb.Kp, colbase, pstride,             \
+                                                  B + 2 * (size_t)colbase * ldb, ldb, pb.L, pb.w, \
+                                                  ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,     \
+                                                  ws.F2, ws.beta, ws.flag)
   if (pb.w <= 56)
-    oz_split_right_crt<2, 4><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L, pb.w,
-                                                    ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,
-                                                    ws.F2, ws.beta, ws.flag);
+    OZ_RIGHT_CRT(4);
   else if (pb.w <= 61)
-    oz_split_right_crt<2, 5><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L, pb.w,
-                                                    ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,
-                                                    ws.F2, ws.beta, ws.flag);
+    OZ_RIGHT_CRT(5);
   else
-    oz_split_right_crt<2, 6><<<pb.Np, 256, 0, st>>>(pb.K, pb.N, pb.Kp, pb.Np, B, ldb, pb.L, pb.w,
-                                                    ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,
-                                                    ws.F2, ws.beta, ws.flag);
+    OZ_RIGHT_CRT(6);
+#undef OZ_RIGHT_CRT
   VCPCU_LAUNCH_CHECK("oz_split_right_crt");
   return VCPCU_OK;
 }
