@@ -430,11 +430,30 @@ __device__ __forceinline__ long long crt_int(double x, int E, int w) {
   return oz_scaled_int64(x, E, w, 0);
 }
 
+// Stores of a left split's plane tiles (32 rows x 64 k of bf16; lane = row,
+// warp q holds k 8q .. 8q + 7 as 16 bytes) through shared memory, so that
+// each warp writes 4 rows x 128 contiguous bytes instead of 32 separate
+// 16-byte pieces (the planes are k-contiguous, A row-contiguous).  Double
+// buffered: one barrier per tile; every thread of the block calls put() the
+// same number of times.
+struct TileStore {
+  uint4 (*T)[32][9];  // [2][32 rows][8 chunks + 1 pad]: conflict-free both ways
+  int buf;
+  __device__ __forceinline__ void put(uint4 v, uint16_t* tile, int Kp) {
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+    T[buf][lane][wq] = v;
+    __syncthreads();
+    const int r = threadIdx.x >> 3, c = threadIdx.x & 7;
+    *reinterpret_cast<uint4*>(tile + (size_t)r * Kp + 8 * c) = T[buf][r][c];
+    buf ^= 1;
+  }
+};
+
 // Left factor, CRT form: residues of A' (L planes) + radius digits, and
 // sum_k |A'(i,k)| split as (|A'| >> 32, |A'| & 0xffffffff) sums.
 // Block: 32 rows x 64 k; lane = row, warp q takes k0 + 8q .. k0 + 8q + 7, so
-// the loads of mA / rA are coalesced across the warp and each lane writes 8
-// bf16 (16 bytes) per plane -- no shared-memory transpose, full occupancy.
+// the loads of mA / rA are coalesced across the warp; each lane's 8 bf16
+// (16 bytes) per plane go out through shared memory (TileStore).
 // FROM_A: midrad again from the interval matrix X (ld ldx) instead of the
 // stored planes mA = X, rA (ld ldx).  Planes rows are rowbase + i (stacked
 // problems), pstride elements apart; E3 and asum point at row 0 of this
@@ -458,7 +477,9 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
     Ep = E3[3 * i + 1];
     Er = E3[3 * i + 2];
   }
-  const size_t rowoff = (size_t)(rowbase + i) * Kp + k0;
+  __shared__ uint4 tile_smem[2][32][9];
+  TileStore ts{tile_smem, 0};
+  const size_t tile0 = (size_t)(rowbase + by * 32) * Kp + bx * 64;
   long long a[8];
   unsigned long long shi = 0, slo = 0;
   {
@@ -493,10 +514,10 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
     }
 #pragma unroll
     for (int q = 0; q < SR; ++q) {
-      *reinterpret_cast<uint4*>(planes_p + q * pstride + rowoff) =
-          make_uint4(hp[q][0], hp[q][1], hp[q][2], hp[q][3]);
-      *reinterpret_cast<uint4*>(planes_r + q * pstride + rowoff) =
-          make_uint4(hr[q][0], hr[q][1], hr[q][2], hr[q][3]);
+      ts.put(make_uint4(hp[q][0], hp[q][1], hp[q][2], hp[q][3]), planes_p + q * pstride + tile0,
+             Kp);
+      ts.put(make_uint4(hr[q][0], hr[q][1], hr[q][2], hr[q][3]), planes_r + q * pstride + tile0,
+             Kp);
     }
   }
   float hl[8][NL];
@@ -523,7 +544,7 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
     uint32_t h[4];
 #pragma unroll
     for (int t = 0; t < 8; t += 2) h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
-    *reinterpret_cast<uint4*>(planes_m + l * pstride + rowoff) = make_uint4(h[0], h[1], h[2], h[3]);
+    ts.put(make_uint4(h[0], h[1], h[2], h[3]), planes_m + l * pstride + tile0, Kp);
   }
 }
 
@@ -1102,7 +1123,7 @@ __global__ void dd_exponents(int R, const unsigned long long* __restrict__ mx,
 
 // Left dd factor -> residue planes [L][Mp][Kp].  Block: 32 rows x 64 k;
 // lane = row, warp q takes k0 + 8q .. k0 + 8q + 7 (coalesced loads across
-// the warp, 16-byte stores per plane, no shared memory).
+// the warp); the plane tiles go out through shared memory (TileStore).
 __global__ void __launch_bounds__(256)
 dd_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long lda, int L, int w,
               const int* __restrict__ E, uint16_t* __restrict__ planes) {
@@ -1127,7 +1148,9 @@ dd_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long l
     ua[t] = (unsigned __int128)(a < 0 ? -a : a);
     if (a < 0) negm |= 1u << t;
   }
-  const size_t rowoff = (size_t)i * Kp + k0;
+  __shared__ uint4 tile_smem[2][32][9];
+  TileStore ts{tile_smem, 0};
+  const size_t tile0 = (size_t)(blockIdx.y * 32) * Kp + blockIdx.x * 64;
   const size_t pstride = (size_t)Mp * Kp;
   float hl[8][10];
 #pragma unroll
@@ -1139,25 +1162,23 @@ dd_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long l
 #pragma unroll
     for (int t = 0; t < 8; t += 2)
       h[t / 2] = pack_bf16x2(res_sym<10>(hl[t], l), res_sym<10>(hl[t + 1], l));
-    *reinterpret_cast<uint4*>(planes + l * pstride + rowoff) = make_uint4(h[0], h[1], h[2], h[3]);
+    ts.put(make_uint4(h[0], h[1], h[2], h[3]), planes + l * pstride + tile0, Kp);
   }
 }
 
-// Right dd factor: one warp per column, 8 columns per block.  Pass 1: the
-// column maximum of |hi| (warp reduction) and its exponent.  Pass 2: lane t
-// takes the 4 consecutive k of 4 (t + 32 it) .. + 3, reads the column again
-// (an L1 / L2 hit) and writes each residue plane [L][Np][Kp] 8 bytes at a
-// time (256 contiguous bytes per warp).
+// Right dd factor, pass 1: one warp per column (8 per block), the column
+// maximum of |hi| (warp reduction) and its exponent; padding columns get
+// the zero exponent.
 __global__ void __launch_bounds__(256)
-dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb, int L, int w,
-               int* __restrict__ F, uint16_t* __restrict__ planes, int* __restrict__ flag) {
+dd_colmax(int K, int N, int Np, const double* __restrict__ B, long ldb, int* __restrict__ F,
+          int* __restrict__ flag) {
   const int lane = threadIdx.x & 31;
   const int j = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (j >= Np) return;  // whole warps only: no block-level barrier below
-  const double* bcol = B + 2 * (long)j * ldb;
+  if (j >= Np) return;  // whole warps only
   unsigned long long am = 0;
   bool bad = false;
   if (j < N) {
+    const double* bcol = B + 2 * (long)j * ldb;
     for (int k = lane; k < K; k += 32) {
       const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
       if (sw_finite(e.x) && sw_finite(e.y))
@@ -1170,32 +1191,46 @@ dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
   am = warp_max_u64(am);
   int Fj = oz_exponent(__longlong_as_double((long long)am));
   if (Fj != OZ_ZERO_EXP) Fj += 1;
-  if (lane == 0 && j < N) F[j] = Fj;
-  const size_t pstride = (size_t)Np * Kp;
-  for (int k0 = 4 * lane; k0 < Kp; k0 += 4 * 32) {
-    float hl[4][10];
+  if (lane == 0) F[j] = j < N ? Fj : OZ_ZERO_EXP;
+}
+
+// Right dd factor, pass 2 -> residue planes [L][Np][Kp].  Block: 8 columns x
+// 256 k; warp q takes column 8 bx.y + q, lane t the 8 consecutive k of
+// 256 bx.x + 8 t .. + 7 (each warp reads 4 KB of its column contiguously and
+// writes 512 contiguous bytes per plane).
+__global__ void __launch_bounds__(256)
+dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb, int L, int w,
+               const int* __restrict__ F, uint16_t* __restrict__ planes) {
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int k0 = blockIdx.x * 256 + 8 * lane;
+  if (j >= Np || k0 >= Kp) return;
+  const int Fj = F[j];
+  const double* bcol = B + 2 * (long)j * ldb;
+  float hl[8][10];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      const int k = k0 + t;
-      double hi = 0.0, lo = 0.0;
-      if (j < N && k < K) {
-        const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
-        if (sw_finite(e.x) && sw_finite(e.y)) {
-          hi = e.x;
-          lo = e.y;
-        }
+  for (int t = 0; t < 8; ++t) {
+    const int k = k0 + t;
+    double hi = 0.0, lo = 0.0;
+    if (j < N && k < K) {
+      const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
+      if (sw_finite(e.x) && sw_finite(e.y)) {
+        hi = e.x;
+        lo = e.y;
       }
-      const __int128 b = dd_int(hi, lo, Fj, w);
-      limbs12<10>((unsigned __int128)(b < 0 ? -b : b), b < 0, hl[t]);
     }
-    const size_t off = (size_t)j * Kp + k0;
+    const __int128 b = dd_int(hi, lo, Fj, w);
+    limbs12<10>((unsigned __int128)(b < 0 ? -b : b), b < 0, hl[t]);
+  }
+  const size_t pstride = (size_t)Np * Kp, off = (size_t)j * Kp + k0;
 #pragma unroll
-    for (int l = 0; l < OZ_MAX_MODULI; ++l) {
-      if (l >= L) break;
-      *reinterpret_cast<uint2*>(planes + l * pstride + off) =
-          make_uint2(pack_bf16x2(res_sym<10>(hl[0], l), res_sym<10>(hl[1], l)),
-                     pack_bf16x2(res_sym<10>(hl[2], l), res_sym<10>(hl[3], l)));
-    }
+  for (int l = 0; l < OZ_MAX_MODULI; ++l) {
+    if (l >= L) break;
+    uint32_t h[4];
+#pragma unroll
+    for (int t = 0; t < 8; t += 2)
+      h[t / 2] = pack_bf16x2(res_sym<10>(hl[t], l), res_sym<10>(hl[t + 1], l));
+    *reinterpret_cast<uint4*>(planes + l * pstride + off) = make_uint4(h[0], h[1], h[2], h[3]);
   }
 }
 
@@ -1215,7 +1250,10 @@ int dd_prepare(int M, int N, int K, int Mp, int Np, int Kp, int L, int w, const 
   dim3 g2(Kp / 64, Mp / 32);
   dd_split_left<<<g2, 256, 0, st>>>(M, K, Mp, Kp, A, lda, L, w, E, planesA);
   VCPCU_LAUNCH_CHECK("dd_split_left");
-  dd_split_right<<<(Np + 7) / 8, 256, 0, st>>>(K, N, Kp, Np, B, ldb, L, w, F, planesB, flag);
+  dd_colmax<<<(Np + 7) / 8, 256, 0, st>>>(K, N, Np, B, ldb, F, flag);
+  VCPCU_LAUNCH_CHECK("dd_colmax");
+  dim3 g3((Kp + 255) / 256, Np / 8);
+  dd_split_right<<<g3, 256, 0, st>>>(K, N, Kp, Np, B, ldb, L, w, F, planesB);
   VCPCU_LAUNCH_CHECK("dd_split_right");
   return VCPCU_OK;
 }
