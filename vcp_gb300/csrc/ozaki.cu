@@ -287,6 +287,7 @@ size_t oz_workspace_bytes(const OzProblem& pb) {
   b += al256(sizeof(int) * 4);
   b += 2 * al256(sizeof(double) * (size_t)pb.M * (pb.K > 0 ? pb.K : 1));
   b += 2 * al256(sizeof(double) * (size_t)pb.Np * pb.Kp);
+  if (pb.crt) b += al256(sizeof(unsigned long long) * 2 * pb.Np);
   b += al256(sizeof(unsigned long long) * 2 * pb.Mp);
   if (pb.crt) b += al256((size_t)pb.L * pb.Np * pb.Mp);
   return b;
@@ -337,6 +338,11 @@ int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws) {
   p += al256(sizeof(double) * (size_t)pb.Np * pb.Kp);
   ws->radB = (double*)p;
   p += al256(sizeof(double) * (size_t)pb.Np * pb.Kp);
+  ws->bsum = nullptr;
+  if (pb.crt) {
+    ws->bsum = (unsigned long long*)p;
+    p += al256(sizeof(unsigned long long) * 2 * pb.Np);
+  }
   ws->asum = (unsigned long long*)p;
   p += al256(sizeof(unsigned long long) * 2 * pb.Mp);
   ws->res = pb.crt ? (uint8_t*)p : nullptr;

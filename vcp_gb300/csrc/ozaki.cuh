@@ -36,6 +36,7 @@ struct OzWorkspace {
   uint8_t* res;                       // [L][Np][Mp] CRT form: residues of A'B' mod m_l
   double *midA, *radA;                // [K][M] midpoints / radii of A (column-major)
   double *midB, *radB;                // [Np][Kp] midpoints / radii of B (k contiguous)
+  unsigned long long* bsum;           // [Np][2] CRT form: sum_k |B'(k,j)| as (bits >= 32, bits < 32)
   double* T;                          // [N][Mp] upper bound of the radius product (slice form)
   long long* W;                       // [Np][Mp] int64 fold buffer (slice form)
   int32_t* P;                         // [2 slots][Np][Mp] folds of the two radius products
@@ -59,7 +60,7 @@ constexpr int OZ_MAX_RAD_SLOTS = 64;  // K <= 2^20: at most 64 folds of 64 chunk
 
 enum OzMode { OZ_RAD_SET = 0, OZ_RAD_ADD = 1, OZ_MID = 2, OZ_CRT = 3 };
 
-struct alignas(64) OzGemmArgs {
+struct alignas(128) OzGemmArgs {
   CUtensorMap tmA;  // left digit planes, dims {Kp, Mp, planes}
   CUtensorMap tmB;  // right digit planes, dims {Kp, Np, planes}
   int M, N, Mp, Np, Kp;

@@ -562,144 +562,6 @@ oz_split_left_crt(int M, int K, int Kp, size_t pstride, int rowbase,
                                      ldx, L, w, E3, planes_m, planes_p, planes_r, asum);
 }
 
-// Right factor, CRT form, one block per column.  Pass 1 (thread t takes
-// k = t, t+256, ...): midrad, the column maxima, and -- STORE_MID -- the
-// planes mB, rB (k contiguous).  Pass 2: B' = round(mB 2^(w - Fm)), its
-// residues, the radius digits, and sum_k |B'| (as >> 32 / & 0xffffffff
-// parts); then beta_j = RU((sum_k |B'| + ceil(K/2)) 2^(Fm - w)) >= sum_k |mB|.
-// Without STORE_MID pass 2 reads the column again (an L2 hit) and repeats
-// the midrad.  j is the column of B, jst its row in the (stacked) planes and
-// its index in F2 / beta.  No FP64 instruction on the common path.
-template <int SR, int NL, bool STORE_MID>
-__device__ __forceinline__ void split_right_crt_body(int j, int jst, int K, int N, int Kp,
-                                                     size_t pstride,
-                                                     const double* __restrict__ B, long ldb,
-                                                     int L, int w, double* __restrict__ mBp,
-                                                     double* __restrict__ rBp,
-                                                     uint16_t* __restrict__ planes_m,
-                                                     uint16_t* __restrict__ planes_r,
-                                                     uint16_t* __restrict__ planes_s,
-                                                     int* __restrict__ F2,
-                                                     double* __restrict__ beta,
-                                                     int* __restrict__ flag) {
-  const int tid = threadIdx.x;
-  __shared__ unsigned long long smax[2];
-  __shared__ unsigned long long bs[2];
-  if (tid == 0) smax[0] = smax[1] = bs[0] = bs[1] = 0;
-  __syncthreads();
-  unsigned long long am = 0, ar = 0;
-  bool bad = false;
-  const double* bcol = B + 2 * (long)j * ldb;
-  double* mcol = STORE_MID ? mBp + (size_t)j * Kp : nullptr;
-  double* rcol = STORE_MID ? rBp + (size_t)j * Kp : nullptr;
-  if (j < N) {
-    for (int k = tid; k < K; k += 256) {
-      const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
-      double m = 0.0, r = 0.0, p;
-      if (sw_finite(e.x) && sw_finite(e.y)) {
-        sw_midrad(e.x, e.y, m, r, p);
-        am = max(am, dbits(oz_abs(m)));
-        ar = max(ar, dbits(r));
-      } else {
-        bad = true;
-      }
-      if (STORE_MID) {
-        mcol[k] = m;
-        rcol[k] = r;
-      }
-    }
-  }
-  if (bad) atomicOr(flag, 1);
-  atomicMax(&smax[0], am);
-  atomicMax(&smax[1], ar);
-  __syncthreads();
-  const int Fm = oz_exponent(__longlong_as_double((long long)smax[0]));
-  const int Fr = oz_exponent(__longlong_as_double((long long)smax[1]));
-  if (tid == 0) {
-    F2[2 * jst + 0] = j < N ? Fm : OZ_ZERO_EXP;
-    F2[2 * jst + 1] = j < N ? Fr : OZ_ZERO_EXP;
-  }
-  // pass 2: thread t takes the 8 consecutive k of 8 (t + 256 it) .. + 7
-  unsigned long long shi = 0, slo = 0;
-  for (int k0 = 8 * tid; k0 < Kp; k0 += 8 * 256) {
-    const size_t off = (size_t)jst * Kp + k0;
-    float hl[8][NL];
-    uint32_t hr[SR][4], hs[SR][4];
-#pragma unroll
-    for (int t = 0; t < 8; t += 2) {
-      int d0[SR], d1[SR], e0[SR], e1[SR];
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int k = k0 + t + u;
-        double m = 0.0, r = 0.0;
-        if (j < N && k < K) {
-          if (STORE_MID) {
-            m = mcol[k];
-            r = rcol[k];
-          } else {
-            const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
-            double p;
-            if (sw_finite(e.x) && sw_finite(e.y)) sw_midrad(e.x, e.y, m, r, p);
-          }
-        }
-        const long long b = crt_int(m, Fm, w);
-        const unsigned long long ub = (unsigned long long)(b < 0 ? -b : b);
-        shi += ub >> 32;
-        slo += ub & 0xffffffffULL;
-        limbs12<NL>(ub, b < 0, hl[t + u]);
-        digits_of<SR>(r, Fr, 1, u ? d1 : d0);
-        digits_of<SR>(oz_abs(m), Fm, 1, u ? e1 : e0);
-      }
-#pragma unroll
-      for (int q = 0; q < SR; ++q) {
-        hr[q][t / 2] = bf16_bits(d0[q]) | (bf16_bits(d1[q]) << 16);
-        hs[q][t / 2] = bf16_bits(e0[q]) | (bf16_bits(e1[q]) << 16);
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < SR; ++q) {
-      *reinterpret_cast<uint4*>(planes_r + q * pstride + off) =
-          make_uint4(hr[q][0], hr[q][1], hr[q][2], hr[q][3]);
-      *reinterpret_cast<uint4*>(planes_s + q * pstride + off) =
-          make_uint4(hs[q][0], hs[q][1], hs[q][2], hs[q][3]);
-    }
-#pragma unroll
-    for (int l = 0; l < OZ_MAX_MODULI_128; ++l) {
-      if (l >= L) break;
-      uint32_t h[4];
-#pragma unroll
-      for (int t = 0; t < 8; t += 2)
-        h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
-      *reinterpret_cast<uint4*>(planes_m + l * pstride + off) = make_uint4(h[0], h[1], h[2], h[3]);
-    }
-  }
-  atomicAdd(&bs[0], shi);
-  atomicAdd(&bs[1], slo);
-  __syncthreads();
-  if (tid == 0) {
-    double bj = 0.0;
-    if (j < N && Fm != OZ_ZERO_EXP) {
-      const double v = __fma_ru((double)bs[0], 0x1p32,
-                                (double)(bs[1] + (unsigned long long)(K + 1) / 2));
-      bj = dev_scale_dir(v, Fm - w, true);
-    }
-    beta[jst] = bj;
-  }
-}
-
-template <int SR, int NL>
-__global__ void __launch_bounds__(256, 3)
-oz_split_right_crt(int K, int N, int Kp, int colbase, size_t pstride,
-                   const double* __restrict__ B, long ldb, int L, int w,
-                   double* __restrict__ mBp, double* __restrict__ rBp,
-                   uint16_t* __restrict__ planes_m, uint16_t* __restrict__ planes_r,
-                   uint16_t* __restrict__ planes_s, int* __restrict__ F2,
-                   double* __restrict__ beta, int* __restrict__ flag) {
-  split_right_crt_body<SR, NL, true>(blockIdx.x, colbase + blockIdx.x, K, N, Kp, pstride, B, ldb,
-                                     L, w, mBp, rBp, planes_m, planes_r, planes_s, F2, beta,
-                                     flag);
-}
-
 // ---------------------------------------------------------- grouped products
 __device__ __forceinline__ int g_find(const int* __restrict__ prefix, int nprob, int x) {
   int lo = 0, hi = nprob - 1;  // largest p with prefix[p] <= x
@@ -784,7 +646,7 @@ __global__ void __launch_bounds__(256, 3) oz_split_left_crt_g(const __grid_const
 // (warp reductions).  Pass 2: lane t takes the 8 consecutive k of
 // 8 (t + 32 it) .. + 7, reads the column again (an L1 / L2 hit) and writes
 // the residue and digit planes 16 bytes at a time; beta_j as in
-// split_right_crt_body.
+// oz_beta_right.
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -930,6 +792,145 @@ int launch_splits(const OzProblem& pb, const double* B, long ldb, OzWorkspace& w
   return VCPCU_OK;
 }
 
+// ------------------------------------------- right factor, CRT form, 2 passes
+// Pass 1: one warp per column (8 per block): kv midrad of the column, stored
+// as the planes mB, rB ([cols][Kp], k contiguous), the column maxima of
+// |mB| and rB and their exponents (zero exponent for padding columns);
+// clears the column's sums of |B'|.  Columns are colbase + j of F2 / bsum.
+__global__ void __launch_bounds__(256)
+oz_colmax_right(int K, int N, int Kp, int cols, int colbase, const double* __restrict__ B,
+                long ldb, double* __restrict__ mB, double* __restrict__ rB,
+                int* __restrict__ F2, unsigned long long* __restrict__ bsum,
+                int* __restrict__ flag) {
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (j >= cols) return;  // whole warps only
+  unsigned long long am = 0, ar = 0;
+  bool bad = false;
+  if (j < N) {
+    const double* bcol = B + 2 * (long)j * ldb;
+    double* mcol = mB + (size_t)j * Kp;
+    double* rcol = rB + (size_t)j * Kp;
+    for (int k = lane; k < K; k += 32) {
+      const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
+      double m = 0.0, r = 0.0;
+      if (sw_finite(e.x) && sw_finite(e.y)) {
+        double p;
+        sw_midrad(e.x, e.y, m, r, p);
+        am = max(am, dbits(oz_abs(m)));
+        ar = max(ar, dbits(r));
+      } else {
+        bad = true;
+      }
+      mcol[k] = m;
+      rcol[k] = r;
+    }
+  }
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flag, 1);
+  am = warp_max_u64(am);
+  ar = warp_max_u64(ar);
+  if (lane == 0) {
+    const int jst = colbase + j;
+    F2[2 * jst + 0] = j < N ? oz_exponent(__longlong_as_double((long long)am)) : OZ_ZERO_EXP;
+    F2[2 * jst + 1] = j < N ? oz_exponent(__longlong_as_double((long long)ar)) : OZ_ZERO_EXP;
+    bsum[2 * jst + 0] = 0;
+    bsum[2 * jst + 1] = 0;
+  }
+}
+
+// Pass 2 -> residue planes of B' = round(mB 2^(w - Fm)) and the radius
+// digit planes of rB and |mB|.  Block: 8 columns x 256 k; warp q takes column
+// 8 by + q, lane t the 8 consecutive k of 256 bx + 8 t .. + 7 (2 KB of the
+// stored mB and rB read contiguously per warp, 512 contiguous bytes written
+// per plane); sum_k |B'| accumulates per column.
+template <int NL>
+__global__ void __launch_bounds__(256)
+oz_split_right_crt2(int K, int N, int Kp, int cols, int colbase, size_t pstride,
+                    const double* __restrict__ mB, const double* __restrict__ rB, int L, int w,
+                    const int* __restrict__ F2, uint16_t* __restrict__ planes_m,
+                    uint16_t* __restrict__ planes_r, uint16_t* __restrict__ planes_s,
+                    unsigned long long* __restrict__ bsum) {
+  constexpr int SR = 2;
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int k0 = blockIdx.x * 256 + 8 * lane;
+  if (j >= cols) return;  // whole warps only (no barrier below)
+  const int jst = colbase + j;
+  const int Fm = F2[2 * jst], Fr = F2[2 * jst + 1];
+  const double* mcol = mB + (size_t)j * Kp;
+  const double* rcol = rB + (size_t)j * Kp;
+  unsigned long long shi = 0, slo = 0;
+  if (k0 < Kp) {
+    const size_t off = (size_t)jst * Kp + k0;
+    float hl[8][NL];
+    uint32_t hr[SR][4], hs[SR][4];
+#pragma unroll
+    for (int t = 0; t < 8; t += 2) {
+      int d0[SR], d1[SR], e0[SR], e1[SR];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int k = k0 + t + u;
+        double m = 0.0, r = 0.0;
+        if (j < N && k < K) {
+          m = mcol[k];
+          r = rcol[k];
+        }
+        const long long bb = crt_int(m, Fm, w);
+        const unsigned long long ub = (unsigned long long)(bb < 0 ? -bb : bb);
+        shi += ub >> 32;
+        slo += ub & 0xffffffffULL;
+        limbs12<NL>(ub, bb < 0, hl[t + u]);
+        digits_of<SR>(r, Fr, 1, u ? d1 : d0);
+        digits_of<SR>(oz_abs(m), Fm, 1, u ? e1 : e0);
+      }
+#pragma unroll
+      for (int q = 0; q < SR; ++q) {
+        hr[q][t / 2] = bf16_bits(d0[q]) | (bf16_bits(d1[q]) << 16);
+        hs[q][t / 2] = bf16_bits(e0[q]) | (bf16_bits(e1[q]) << 16);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < SR; ++q) {
+      *reinterpret_cast<uint4*>(planes_r + q * pstride + off) =
+          make_uint4(hr[q][0], hr[q][1], hr[q][2], hr[q][3]);
+      *reinterpret_cast<uint4*>(planes_s + q * pstride + off) =
+          make_uint4(hs[q][0], hs[q][1], hs[q][2], hs[q][3]);
+    }
+#pragma unroll
+    for (int l = 0; l < OZ_MAX_MODULI_128; ++l) {
+      if (l >= L) break;
+      uint32_t h[4];
+#pragma unroll
+      for (int t = 0; t < 8; t += 2)
+        h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
+      *reinterpret_cast<uint4*>(planes_m + l * pstride + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    }
+  }
+  shi = warp_sum_u64(shi);
+  slo = warp_sum_u64(slo);
+  if (lane == 0 && (shi | slo)) {
+    atomicAdd(&bsum[2 * jst + 0], shi);
+    atomicAdd(&bsum[2 * jst + 1], slo);
+  }
+}
+
+// beta_j = RU((sum_k |B'| + ceil(K/2)) 2^(Fm - w)) >= sum_k |mB(k, j)|.
+__global__ void oz_beta_right(int K, int N, int cols, int colbase, int w,
+                              const int* __restrict__ F2,
+                              const unsigned long long* __restrict__ bsum,
+                              double* __restrict__ beta) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= cols) return;
+  const int jst = colbase + j, Fm = F2[2 * jst];
+  double bj = 0.0;
+  if (j < N && Fm != OZ_ZERO_EXP) {
+    const double v = __fma_ru((double)bsum[2 * jst], 0x1p32,
+                              (double)(bsum[2 * jst + 1] + (unsigned long long)(K + 1) / 2));
+    bj = dev_scale_dir(v, Fm - w, true);
+  }
+  beta[jst] = bj;
+}
+
 int oz_prepare_left_begin(const OzProblem& pb, OzWorkspace& ws, cudaStream_t st) {
   VCPCU_CUDA_TRY(cudaMemsetAsync(ws.rowmax, 0, sizeof(unsigned long long) * 3 * (size_t)pb.Mp, st));
   VCPCU_CUDA_TRY(cudaMemsetAsync(ws.delta, 0, sizeof(unsigned long long) * (size_t)pb.Mp, st));
@@ -1018,11 +1019,17 @@ int oz_prepare_right_crt(const OzProblem& pb, const double* B, long ldb, OzWorks
   if (!pstride) pstride = (size_t)pb.Np * pb.Kp;
   const int nv = pb.N - colbase < cols ? (pb.N - colbase > 0 ? pb.N - colbase : 0) : cols;
   if (cols <= 0) return VCPCU_OK;
-#define OZ_RIGHT_CRT(NL)                                                                         \
-  oz_split_right_crt<2, NL><<<cols, 256, 0, st>>>(pb.K, nv, pb.Kp, colbase, pstride,             \
-                                                  B + 2 * (size_t)colbase * ldb, ldb, pb.L, pb.w, \
-                                                  ws.midB, ws.radB, ws.b_mid, ws.b_r, ws.b_s,     \
-                                                  ws.F2, ws.beta, ws.flag)
+  const double* Bc = B + 2 * (size_t)colbase * ldb;
+  oz_colmax_right<<<(cols + 7) / 8, 256, 0, st>>>(pb.K, nv, pb.Kp, cols, colbase, Bc, ldb,
+                                                  ws.midB, ws.radB, ws.F2, ws.bsum, ws.flag);
+  VCPCU_LAUNCH_CHECK("oz_colmax_right");
+  dim3 g((pb.Kp + 255) / 256, (cols + 7) / 8);
+  // |B'| <= 2^(w-1): four 14-bit limbs up to w = 56, five 12-bit limbs up to
+  // w = 61, six up to 73
+#define OZ_RIGHT_CRT(NL)                                                                       \
+  oz_split_right_crt2<NL><<<g, 256, 0, st>>>(pb.K, nv, pb.Kp, cols, colbase, pstride, ws.midB, \
+                                             ws.radB, pb.L, pb.w, ws.F2, ws.b_mid, ws.b_r,      \
+                                             ws.b_s, ws.bsum)
   if (pb.w <= 56)
     OZ_RIGHT_CRT(4);
   else if (pb.w <= 61)
@@ -1030,7 +1037,10 @@ int oz_prepare_right_crt(const OzProblem& pb, const double* B, long ldb, OzWorks
   else
     OZ_RIGHT_CRT(6);
 #undef OZ_RIGHT_CRT
-  VCPCU_LAUNCH_CHECK("oz_split_right_crt");
+  VCPCU_LAUNCH_CHECK("oz_split_right_crt2");
+  oz_beta_right<<<(cols + 255) / 256, 256, 0, st>>>(pb.K, nv, cols, colbase, pb.w, ws.F2,
+                                                    ws.bsum, ws.beta);
+  VCPCU_LAUNCH_CHECK("oz_beta_right");
   return VCPCU_OK;
 }
 
