@@ -183,68 +183,6 @@ __device__ __forceinline__ double sw_add_ru_pos(double a, double b) {
   return sw_double(((unsigned long long)B << 52) | (M & (H - 1)));
 }
 
-static __device__ __noinline__ double sw_dadd_dir_slow(double a, double b, bool up) {
-  return up ? __dadd_ru(a, b) : __dadd_rd(a, b);
-}
-
-// RU (up) or RD of a + b for finite a, b, equal bit for bit to __dadd_ru /
-// __dadd_rd: the integer pipe when both are normal and the result is normal
-// (an exact cancellation gives +0 upward, -0 downward), else the FP64
-// instruction.  x is the operand of larger magnitude, y the other; both
-// significands are held with 10 guard bits, y's shifted out bits become a
-// sticky flag (only when the exponents differ by more than 10, and then the
-// difference keeps at least 62 bits).
-__device__ __forceinline__ double sw_add_dir(double a, double b, bool up) {
-  const unsigned long long S1 = 1ULL << 63, H = 1ULL << 52;
-  unsigned long long bx = sw_bits(a), by = sw_bits(b);
-  if ((bx & ~S1) < (by & ~S1)) {
-    const unsigned long long t = bx;
-    bx = by;
-    by = t;
-  }
-  const int ex = (int)((bx >> 52) & 0x7ff), ey = (int)((by >> 52) & 0x7ff);
-  if (ey == 0 || ex >= 2046) return sw_dadd_dir_slow(a, b, up);
-  const unsigned long long sx = bx >> 63, sy = by >> 63;
-  const bool away = up != (sx != 0);  // round the magnitude away from zero
-  const unsigned long long MX = ((bx & (H - 1)) | H) << 10;  // units 2^(ex - 1085)
-  const unsigned long long MY0 = ((by & (H - 1)) | H) << 10;
-  const int d = ex - ey;
-  unsigned long long MY;
-  bool sticky;
-  if (d >= 64) {
-    MY = 0;
-    sticky = true;
-  } else {
-    MY = MY0 >> d;
-    sticky = d > 0 && (MY0 & ((1ULL << d) - 1)) != 0;
-  }
-  unsigned long long D;
-  if (sx == sy) {
-    D = MX + MY;  // < 2^64; a sticky y adds a fraction in (0, 1)
-  } else {
-    if (!sticky && MX == MY) return sw_double(up ? 0ULL : S1);
-    D = MX - MY - (sticky ? 1 : 0);  // a sticky y leaves a fraction in (0, 1)
-  }
-  const int bd = 64 - __clzll(D);
-  int field = ex - 63 + bd;  // exponent field of a 53-bit significand
-  unsigned long long M;
-  if (bd <= 53) {
-    M = D << (53 - bd);  // exact (no sticky: then bd >= 62)
-  } else {
-    const int s = bd - 53;
-    M = D >> s;
-    if (away && (sticky || (D & ((1ULL << s) - 1)))) {
-      ++M;
-      if (M >> 53) {
-        M >>= 1;
-        ++field;
-      }
-    }
-  }
-  if (field < 1 || field > 2046) return sw_dadd_dir_slow(a, b, up);
-  return sw_double((sx << 63) | ((unsigned long long)field << 52) | (M & (H - 1)));
-}
-
 // RU(v * 2^ex) for an int64 v >= 0 built on the integer pipe (equal to
 // RU-scaling of __ll2double_ru(v)); false when the result is not normal or
 // v < 0.
