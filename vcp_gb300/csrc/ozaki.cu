@@ -423,6 +423,23 @@ int pipe_event(PipeGuard& g, cudaStream_t rec, cudaStream_t waiter) {
 
 }  // namespace
 
+namespace {
+// Boundaries of about `parts` blocks over `len` entries, multiples of
+// `unit` except the end; the first block is half the size of the others.
+std::vector<int> block_bounds(int len, int parts, int unit) {
+  std::vector<int> b{0};
+  if (parts > 1) {
+    for (int t = 1; t < parts; ++t) {
+      const double x = (double)len * (t - 0.5) / (parts - 0.5);
+      const int c = ((int)x + unit - 1) / unit * unit;
+      if (c > b.back() && c < len) b.push_back(c);
+    }
+  }
+  b.push_back(len);
+  return b;
+}
+}  // namespace
+
 int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const double* B, double* C,
                                int slices, int panels, int row_panels, cudaStream_t s,
                                cudaStream_t up, cudaStream_t down) {
@@ -438,12 +455,12 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
   OzPlan plan;  // the whole product: its workspace holds every block's planes
   oz_make_plan(m, n, k, nslices, 2, &plan, 1);
   const OzProblem& pb = plan.pb;
-  int nb = (n + panels - 1) / panels;
-  nb = (nb + OZ_BN - 1) / OZ_BN * OZ_BN;  // whole column tiles per block
-  panels = (n + nb - 1) / nb;
-  int mb = (m + row_panels - 1) / row_panels;
-  mb = (mb + OZ_BM - 1) / OZ_BM * OZ_BM;  // whole row tiles per block
-  row_panels = (m + mb - 1) / mb;
+  // block boundaries (whole row / column tiles); the first blocks, waited
+  // for before anything computes, are half the size of the others
+  const std::vector<int> rb = block_bounds(m, row_panels, OZ_BM),
+                         cb = block_bounds(n, panels, OZ_BN);
+  row_panels = (int)rb.size() - 1;
+  panels = (int)cb.size() - 1;
   const size_t na = 2 * (size_t)m * k, nbe = 2 * (size_t)k * n, nc = 2 * (size_t)m * n;
   const size_t off_b = al256(na * 8), off_c = off_b + al256(nbe * 8),
                off_w = off_c + al256(nc * 8);
@@ -465,7 +482,7 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
   std::vector<cudaEvent_t> evA(row_panels), evB(panels);
   for (int t = 0; t < row_panels || t < panels; ++t) {
     if (t < row_panels) {
-      const int i0 = t * mb, mv = (m - i0 < mb) ? m - i0 : mb;
+      const int i0 = rb[t], mv = rb[t + 1] - rb[t];
       if (k > 0)
         VCPCU_CUDA_TRY(cudaMemcpy2DAsync(dA + 2 * (size_t)i0, m * rowb, A + 2 * (size_t)i0,
                                          m * rowb, mv * rowb, k, cudaMemcpyHostToDevice, up));
@@ -473,7 +490,7 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
       VCPCU_CUDA_TRY(cudaEventRecord(evA[t], up));
     }
     if (t < panels) {
-      const int j0 = t * nb, wj = (n - j0 < nb) ? n - j0 : nb;
+      const int j0 = cb[t], wj = cb[t + 1] - cb[t];
       if (k > 0)
         VCPCU_CUDA_TRY(cudaMemcpyAsync(dB + 2 * (size_t)j0 * k, B + 2 * (size_t)j0 * k,
                                        2 * (size_t)wj * k * sizeof(double),
@@ -483,12 +500,13 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
     }
   }
 
-  // block (I, J) of C: its slice GEMMs on views of the whole planes, its
-  // reassembly, and its download
+  // the part of C over row blocks [I0, I1) and column blocks [J0, J1): its
+  // slice GEMMs on views of the whole planes, its reassembly, its download
   long long flops = 0;
-  auto block = [&](int I, int J) -> int {
-    const int i0 = I * mb, mv = (m - i0 < mb) ? m - i0 : mb;
-    const int j0 = J * nb, wj = (n - j0 < nb) ? n - j0 : nb;
+  auto block = [&](int I0, int I1, int J0, int J1) -> int {
+    const int i0 = rb[I0], mv = rb[I1] - rb[I0];
+    const int j0 = cb[J0], wj = cb[J1] - cb[J0];
+    if (mv <= 0 || wj <= 0) return VCPCU_OK;
     OzPlan pj;
     oz_make_plan(mv, wj, k, nslices, 2, &pj, 1);
     OzWorkspace v = ws;
@@ -520,23 +538,37 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
     return VCPCU_OK;
   };
   // compute in arrival order: each new row block of A meets the column
-  // blocks of B already prepared, and each new column block the row blocks
+  // blocks of B already prepared (one product over their contiguous
+  // columns), each new column block the row blocks (one product over their
+  // rows); after the last upload, block by block, so that the download of
+  // one overlaps the next
+  const bool last_is_b = panels >= row_panels;
   for (int t = 0; t < row_panels || t < panels; ++t) {
     if (t < row_panels) {
-      const int i0 = t * mb, rows = (pb.Mp - i0 < mb) ? pb.Mp - i0 : mb;
+      const int i0 = rb[t], rows = (t + 1 < row_panels ? rb[t + 1] : pb.Mp) - i0;
       VCPCU_CUDA_TRY(cudaStreamWaitEvent(s, evA[t], 0));
       if ((st = oz_prepare_left_rows(pb, dA, m, i0, rows, ws, s))) return st;
-      for (int J = 0; J < t && J < panels; ++J)
-        if ((st = block(t, J))) return st;
+      const int nj = t < panels ? t : panels;
+      if (!last_is_b && t == row_panels - 1) {
+        for (int J = 0; J < nj; ++J)
+          if ((st = block(t, t + 1, J, J + 1))) return st;
+      } else if ((st = block(t, t + 1, 0, nj))) {
+        return st;
+      }
     }
     if (t < panels) {
-      const int j0 = t * nb, cols = (pb.Np - j0 < nb) ? pb.Np - j0 : nb;
+      const int j0 = cb[t], cols = (t + 1 < panels ? cb[t + 1] : pb.Np) - j0;
       VCPCU_CUDA_TRY(cudaStreamWaitEvent(s, evB[t], 0));
       if ((st = oz_prepare_right_crt(pb, dB, k > 0 ? k : 1, ws, s, j0, cols,
                                      (size_t)pb.Np * pb.Kp)))
         return st;
-      for (int I = 0; I <= t && I < row_panels; ++I)
-        if ((st = block(I, t))) return st;
+      const int ni = t + 1 < row_panels ? t + 1 : row_panels;
+      if (last_is_b && t == panels - 1) {
+        for (int I = 0; I < ni; ++I)
+          if ((st = block(I, I + 1, t, t + 1))) return st;
+      } else if ((st = block(0, ni, t, t + 1))) {
+        return st;
+      }
     }
   }
   oz_profile_add_flops(flops);
