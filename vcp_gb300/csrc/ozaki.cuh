@@ -243,7 +243,8 @@ struct OzGBucket {
 };
 
 // Kernels of the grouped form (ozaki_split.cu, ozaki_gemm.cu, ozaki_crt.cu).
-int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, cudaStream_t st);
+// wmax: the largest operand width w of the bucket (selects the limb form)
+int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, int wmax, cudaStream_t st);
 int oz_grun_gemm(const OzGBucket& b, const OzPlan& shape, int mode, int nitems,
                  cudaStream_t st);
 int oz_gassemble(const OzGBucket& b, const OzRadConst& rc, int nblk, cudaStream_t st);

@@ -44,6 +44,7 @@ struct BucketHost {
   OzPlan shape;   // radius pair list, Lmax-modulus pair list, fold count
   OzRadConst rc;
   int nblk_rowmax = 0, nblk_split = 0, nitem_rad = 0, nitem_crt = 0, nblk_asm = 0;
+  int wmax = 0;  // largest operand width w of the bucket's problems
   // workspace layout (byte offsets; the first zero_bytes are cleared per run)
   size_t offRowmax = 0, offAsum = 0, offFlag = 0, zero_bytes = 0;
   size_t offE3 = 0, offF2 = 0, offBeta = 0, offA = 0, offB = 0, offRes = 0, offP = 0;
@@ -141,6 +142,7 @@ int oz_group_plan(int count, const BatchProblemView* problems, const char* selec
       gp.Np = pl.pb.Np;
       gp.L = pl.pb.L;
       gp.w = pl.pb.w;
+      b.wmax = std::max(b.wmax, gp.w);
       gp.rowoff = rowoff;
       gp.coloff = coloff;
       gp.tiles_m = pl.pb.Mp / OZ_BM;
@@ -280,7 +282,7 @@ int oz_group_record(OzGroupPlan* g, unsigned long long* t_first, unsigned long l
     int st;
     {
       PhaseTimer t(0, s);
-      if ((st = oz_gprep(d, b.nblk_rowmax, b.nblk_split, s))) return st;
+      if ((st = oz_gprep(d, b.nblk_rowmax, b.nblk_split, b.wmax, s))) return st;
     }
     {
       PhaseTimer t(1, s);

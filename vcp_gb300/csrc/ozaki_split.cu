@@ -480,13 +480,19 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
   __shared__ uint4 tile_smem[2][32][9];
   TileStore ts{tile_smem, 0};
   const size_t tile0 = (size_t)(rowbase + by * 32) * Kp + bx * 64;
+  // the warp's 8 k past K, or all 32 rows past M: zero planes, nothing to
+  // compute (the stores still go through the tile, every thread calls put)
+  const bool pad = k0 >= K || by * 32 >= M;
   long long a[8];
   unsigned long long shi = 0, slo = 0;
   {
     // radius digit planes first, so that the doubles die before the residues
-    uint32_t hp[SR][4], hr[SR][4];
+    uint32_t hp[SR][4] = {}, hr[SR][4] = {};
+#pragma unroll
+    for (int t = 0; t < 8; ++t) a[t] = 0;
 #pragma unroll
     for (int t = 0; t < 8; t += 2) {
+      if (pad) break;
       int d0[SR], d1[SR], e0[SR], e1[SR];
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
@@ -541,9 +547,12 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
 #pragma unroll
   for (int l = 0; l < OZ_MAX_MODULI_128; ++l) {
     if (l >= L) break;
-    uint32_t h[4];
+    uint32_t h[4] = {0u, 0u, 0u, 0u};
+    if (!pad) {
 #pragma unroll
-    for (int t = 0; t < 8; t += 2) h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
+      for (int t = 0; t < 8; t += 2)
+        h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
+    }
     ts.put(make_uint4(h[0], h[1], h[2], h[3]), planes_m + l * pstride + tile0, Kp);
   }
 }
@@ -661,7 +670,18 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
   return v;
 }
 
-template <int NL>
+// KPL consecutive bf16 (KPL = 2, 4 or 8: 4, 8 or 16 bytes) in one store.
+template <int KPL>
+__device__ __forceinline__ void store_bf16s(uint16_t* dst, const uint32_t (&h)[KPL / 2]) {
+  if constexpr (KPL == 8)
+    *reinterpret_cast<uint4*>(dst) = make_uint4(h[0], h[1], h[2], h[3]);
+  else if constexpr (KPL == 4)
+    *reinterpret_cast<uint2*>(dst) = make_uint2(h[0], h[1]);
+  else
+    *reinterpret_cast<uint32_t*>(dst) = h[0];
+}
+
+template <int NL, int KPL>
 __global__ void __launch_bounds__(256) oz_split_right_crt_g(const __grid_constant__ OzGBucket b) {
   const int lane = threadIdx.x & 31;
   const int jst = blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -673,20 +693,36 @@ __global__ void __launch_bounds__(256) oz_split_right_crt_g(const __grid_constan
   uint16_t* planes_m = b.planesB;
   uint16_t* planes_r = b.planesB + (size_t)b.Lmax * pstride;
   uint16_t* planes_s = b.planesB + (size_t)(b.Lmax + 2) * pstride;
+  constexpr int HW = KPL / 2;  // 32-bit words per lane and plane
+  const uint32_t zero[HW] = {};
+  if (j >= N) {  // a padding column: zero planes, zero exponents, zero beta
+    if (lane == 0) {
+      b.F2[2 * jst + 0] = b.F2[2 * jst + 1] = OZ_ZERO_EXP;
+      b.beta[jst] = 0.0;
+    }
+    for (int k0 = KPL * lane; k0 < Kp; k0 += KPL * 32) {
+      const size_t off = (size_t)jst * Kp + k0;
+#pragma unroll
+      for (int qq = 0; qq < 2; ++qq) {
+        store_bf16s<KPL>(planes_r + qq * pstride + off, zero);
+        store_bf16s<KPL>(planes_s + qq * pstride + off, zero);
+      }
+      for (int l = 0; l < L; ++l) store_bf16s<KPL>(planes_m + l * pstride + off, zero);
+    }
+    return;
+  }
   const double* bcol = q.B + 2 * (long)j * q.ldb;
   unsigned long long am = 0, ar = 0;
   bool bad = false;
-  if (j < N) {
-    for (int k = lane; k < K; k += 32) {
-      const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
-      double m, r, pp;
-      if (sw_finite(e.x) && sw_finite(e.y)) {
-        sw_midrad(e.x, e.y, m, r, pp);
-        am = max(am, dbits(oz_abs(m)));
-        ar = max(ar, dbits(r));
-      } else {
-        bad = true;
-      }
+  for (int k = lane; k < K; k += 32) {
+    const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
+    double m, r, pp;
+    if (sw_finite(e.x) && sw_finite(e.y)) {
+      sw_midrad(e.x, e.y, m, r, pp);
+      am = max(am, dbits(oz_abs(m)));
+      ar = max(ar, dbits(r));
+    } else {
+      bad = true;
     }
   }
   if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&b.flag[4 * p], 1);
@@ -695,22 +731,31 @@ __global__ void __launch_bounds__(256) oz_split_right_crt_g(const __grid_constan
   const int Fm = oz_exponent(__longlong_as_double((long long)am));
   const int Fr = oz_exponent(__longlong_as_double((long long)ar));
   if (lane == 0) {
-    b.F2[2 * jst + 0] = j < N ? Fm : OZ_ZERO_EXP;
-    b.F2[2 * jst + 1] = j < N ? Fr : OZ_ZERO_EXP;
+    b.F2[2 * jst + 0] = Fm;
+    b.F2[2 * jst + 1] = Fr;
   }
   unsigned long long shi = 0, slo = 0;
-  for (int k0 = 8 * lane; k0 < Kp; k0 += 8 * 32) {
+  for (int k0 = KPL * lane; k0 < Kp; k0 += KPL * 32) {
     const size_t off = (size_t)jst * Kp + k0;
-    float hl[8][NL];
-    uint32_t hr[2][4], hs[2][4];
+    if (k0 >= K) {  // padding of the inner dimension: zeros, nothing to compute
 #pragma unroll
-    for (int t = 0; t < 8; t += 2) {
+      for (int qq = 0; qq < 2; ++qq) {
+        store_bf16s<KPL>(planes_r + qq * pstride + off, zero);
+        store_bf16s<KPL>(planes_s + qq * pstride + off, zero);
+      }
+      for (int l = 0; l < L; ++l) store_bf16s<KPL>(planes_m + l * pstride + off, zero);
+      continue;
+    }
+    float hl[KPL][NL];
+    uint32_t hr[2][HW], hs[2][HW];
+#pragma unroll
+    for (int t = 0; t < KPL; t += 2) {
       int d0[2], d1[2], e0[2], e1[2];
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
         const int k = k0 + t + u;
         double m = 0.0, r = 0.0;
-        if (j < N && k < K) {
+        if (k < K) {
           const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
           double pp;
           if (sw_finite(e.x) && sw_finite(e.y)) sw_midrad(e.x, e.y, m, r, pp);
@@ -731,26 +776,24 @@ __global__ void __launch_bounds__(256) oz_split_right_crt_g(const __grid_constan
     }
 #pragma unroll
     for (int qq = 0; qq < 2; ++qq) {
-      *reinterpret_cast<uint4*>(planes_r + qq * pstride + off) =
-          make_uint4(hr[qq][0], hr[qq][1], hr[qq][2], hr[qq][3]);
-      *reinterpret_cast<uint4*>(planes_s + qq * pstride + off) =
-          make_uint4(hs[qq][0], hs[qq][1], hs[qq][2], hs[qq][3]);
+      store_bf16s<KPL>(planes_r + qq * pstride + off, hr[qq]);
+      store_bf16s<KPL>(planes_s + qq * pstride + off, hs[qq]);
     }
 #pragma unroll
     for (int l = 0; l < OZ_MAX_MODULI_128; ++l) {
       if (l >= L) break;
-      uint32_t h[4];
+      uint32_t h[HW];
 #pragma unroll
-      for (int t = 0; t < 8; t += 2)
+      for (int t = 0; t < KPL; t += 2)
         h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
-      *reinterpret_cast<uint4*>(planes_m + l * pstride + off) = make_uint4(h[0], h[1], h[2], h[3]);
+      store_bf16s<KPL>(planes_m + l * pstride + off, h);
     }
   }
   shi = warp_sum_u64(shi);
   slo = warp_sum_u64(slo);
   if (lane == 0) {
     double bj = 0.0;
-    if (j < N && Fm != OZ_ZERO_EXP) {
+    if (Fm != OZ_ZERO_EXP) {
       const double v = __fma_ru((double)shi, 0x1p32,
                                 (double)(slo + (unsigned long long)(K + 1) / 2));
       bj = dev_scale_dir(v, Fm - w, true);
@@ -759,17 +802,36 @@ __global__ void __launch_bounds__(256) oz_split_right_crt_g(const __grid_constan
   }
 }
 
-int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, cudaStream_t st) {
+int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, int wmax, cudaStream_t st) {
   if (nblk_rowmax > 0) {
     oz_rowmax_left_g<<<nblk_rowmax, 256, 0, st>>>(b);
     VCPCU_LAUNCH_CHECK("oz_rowmax_left_g");
   }
   oz_exponents<<<(b.Mtot + 255) / 256, 256, 0, st>>>(b.Mtot, b.rowmax, 3, b.E3);
   VCPCU_LAUNCH_CHECK("oz_exponents");
-  // six 12-bit limbs hold every |A'|, |B'| < 2^61 (w <= 62)
-  oz_split_left_crt_g<6><<<nblk_split, 256, 0, st>>>(b);
-  VCPCU_LAUNCH_CHECK("oz_split_left_crt_g");
-  oz_split_right_crt_g<6><<<(b.Ntot + 7) / 8, 256, 0, st>>>(b);
+  // |A'|, |B'| <= 2^(w-1): four 14-bit limbs up to w = 56, six 12-bit limbs
+  // up to w = 73; lanes of the right split take 2, 4 or 8 consecutive k so
+  // that short columns keep the warp busy
+  const int nbr = (b.Ntot + 7) / 8;
+#define OZ_GRIGHT(NL)                                                           \
+  do {                                                                          \
+    if (b.Kp <= 64)                                                             \
+      oz_split_right_crt_g<NL, 2><<<nbr, 256, 0, st>>>(b);                      \
+    else if (b.Kp <= 128)                                                       \
+      oz_split_right_crt_g<NL, 4><<<nbr, 256, 0, st>>>(b);                      \
+    else                                                                        \
+      oz_split_right_crt_g<NL, 8><<<nbr, 256, 0, st>>>(b);                      \
+  } while (0)
+  if (wmax <= 56) {
+    oz_split_left_crt_g<4><<<nblk_split, 256, 0, st>>>(b);
+    VCPCU_LAUNCH_CHECK("oz_split_left_crt_g");
+    OZ_GRIGHT(4);
+  } else {
+    oz_split_left_crt_g<6><<<nblk_split, 256, 0, st>>>(b);
+    VCPCU_LAUNCH_CHECK("oz_split_left_crt_g");
+    OZ_GRIGHT(6);
+  }
+#undef OZ_GRIGHT
   VCPCU_LAUNCH_CHECK("oz_split_right_crt_g");
   return VCPCU_OK;
 }
