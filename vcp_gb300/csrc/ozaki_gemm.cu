@@ -151,6 +151,23 @@ __device__ __forceinline__ ItemInfo item_info(const OzGemmArgs& a, int item, int
   return f;
 }
 
+// Residue of a one-chunk CRT group on the FP32 pipe (no float-to-int
+// conversion, which GB300 issues on its narrow XU pipe, and no integer
+// reduction).  The chunk value v is an exact integer with |v| <= 2^24;
+// q = rint(RN(v RN(1/m))) is within 0.52 of v / m, so r = v - q m (one
+// exact FMA) is an integer with |r| <= 0.52 m <= 133, and the fold reduces
+// it into [0, m).
+__device__ __forceinline__ float rint_f(float x) {  // |x| < 2^22
+  return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
+}
+__device__ __forceinline__ float chunk_residue(float v, float m, float inv) {
+  return __fmaf_rn(-rint_f(__fmul_rn(v, inv)), m, v);
+}
+__device__ __forceinline__ float fold_residue(float x, float m, float inv) {  // |x| < 2^22
+  float r = __fmaf_rn(-rint_f(__fmul_rn(x, inv)), m, x);  // |r| <= m / 2
+  return r < 0.0f ? r + m : r;
+}
+
 __device__ __forceinline__ long long shift_t(int c, int sh) {
   const long long v = (long long)c;
   return sh >= 0 ? (v << sh) : (v >> (-sh));
@@ -308,9 +325,16 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
         const int sh = 8 * (args.t_ref - t);
         const int npg = args.pl.gstart[g + 1] - args.pl.gstart[g];
         const int total = npg * nchunks;
+        // per-element sums: int32 of the chunk values, or (CRT form with one
+        // chunk per group, where the integer reduction would dominate) the
+        // fp32 bits of the chunk residue; with several chunks the two-
+        // instruction int32 accumulation per chunk is cheaper
         int c[128];
 #pragma unroll
         for (int e = 0; e < 128; ++e) c[e] = 0;
+        const bool crt = args.mode == OZ_CRT && nchunks == 1;
+        const float mf = crt ? (float)args.moduli[g] : 1.0f;
+        const float invf = __frcp_rn(mf);
         int cnt = 0;
         for (int idx = 0; idx < total; ++idx, ++acc) {
           const int buf = acc & 1;
@@ -326,8 +350,15 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
             uint32_t r[32];
             ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c4 * 32, r);
             ptx::tmem_ld_wait();
+            if (crt) {
 #pragma unroll
-            for (int e = 0; e < 32; ++e) c[c4 * 32 + e] += __float2int_rn(__uint_as_float(r[e]));
+              for (int e = 0; e < 32; ++e)
+                c[c4 * 32 + e] = __float_as_int(__fadd_rn(
+                    __int_as_float(c[c4 * 32 + e]), chunk_residue(__uint_as_float(r[e]), mf, invf)));
+            } else {
+#pragma unroll
+              for (int e = 0; e < 32; ++e) c[c4 * 32 + e] += __float2int_rn(__uint_as_float(r[e]));
+            }
           }
           ptx::tc_fence_before();
           __syncwarp();
@@ -337,24 +368,34 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
           if ((cnt == OZ_FOLD_CHUNKS || last_of_group) && args.mode == OZ_CRT) {
             // CRT form: group g is modulus m_g; keep (A'B') mod m_g as a byte
             // in res[g][col][row], adding to an earlier fold of the group
-            const uint32_t m = (uint32_t)args.moduli[g];
-            const uint32_t mg = 0xFFFFFFFFu / m;
             uint8_t* rp = f.res + (size_t)g * f.Np * f.Mp + (size_t)gj0 * f.Mp + gi;
-            const bool first = cnt == idx + 1;  // no earlier fold in this group
+            if (crt) {  // one chunk: the fold is the whole group
 #pragma unroll
-            for (int e = 0; e < 128; ++e) {
-              const int v = c[e];
-              const uint32_t a = (uint32_t)(v < 0 ? -v : v);
-              uint32_t r = a - __umulhi(a, mg) * m;
-              if (r >= m) r -= m;
-              if (r >= m) r -= m;
-              if (v < 0 && r) r = m - r;
-              if (!first) {
-                r += rp[(size_t)e * f.Mp];
-                if (r >= m) r -= m;
+              for (int e = 0; e < 128; ++e) {
+                const float r = fold_residue(__int_as_float(c[e]), mf, invf);  // [0, m)
+                // r < 256 is the low byte of the bits of r + 2^23
+                rp[(size_t)e * f.Mp] = (uint8_t)__float_as_uint(__fadd_rn(r, 8388608.0f));
+                c[e] = 0;
               }
-              rp[(size_t)e * f.Mp] = (uint8_t)r;
-              c[e] = 0;
+            } else {
+              const uint32_t m = (uint32_t)args.moduli[g];
+              const uint32_t mg = 0xFFFFFFFFu / m;
+              const bool first = cnt == idx + 1;  // no earlier fold in this group
+#pragma unroll
+              for (int e = 0; e < 128; ++e) {
+                const int v = c[e];
+                const uint32_t a = (uint32_t)(v < 0 ? -v : v);
+                uint32_t r = a - __umulhi(a, mg) * m;
+                if (r >= m) r -= m;
+                if (r >= m) r -= m;
+                if (v < 0 && r) r = m - r;
+                if (!first) {
+                  r += rp[(size_t)e * f.Mp];
+                  if (r >= m) r -= m;
+                }
+                rp[(size_t)e * f.Mp] = (uint8_t)r;
+                c[e] = 0;
+              }
             }
             cnt = 0;
           } else if ((cnt == OZ_FOLD_CHUNKS || last_of_group) && args.mode != OZ_MID) {
