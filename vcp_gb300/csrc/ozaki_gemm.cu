@@ -98,6 +98,7 @@ struct ItemInfo {
   int arow, bcol;   // TMA row of the A tile / of the B tile in the planes
   int tm, tn, g0, g1;
   int Mp, Np;       // output layout of this item's problem
+  int M, N;         // its valid rows / columns
   uint8_t* res;
   int32_t* P;
 };
@@ -128,6 +129,8 @@ __device__ __forceinline__ ItemInfo item_info(const OzGemmArgs& a, int item, int
     f.bcol = q.coloff + f.tn * OZ_BN;
     f.Mp = q.Mp;
     f.Np = q.Np;
+    f.M = q.m;
+    f.N = q.n;
     f.res = a.res ? a.res + q.res_off : nullptr;
     f.P = a.P ? a.P + q.P_off : nullptr;
     return f;
@@ -146,6 +149,8 @@ __device__ __forceinline__ ItemInfo item_info(const OzGemmArgs& a, int item, int
   f.bcol = f.tn * OZ_BN;
   f.Mp = a.Mp;
   f.Np = a.Np;
+  f.M = a.M;
+  f.N = a.N;
   f.res = a.res;
   f.P = a.P;
   return f;
@@ -153,18 +158,16 @@ __device__ __forceinline__ ItemInfo item_info(const OzGemmArgs& a, int item, int
 
 // Residue of a one-chunk CRT group on the FP32 pipe (no float-to-int
 // conversion, which GB300 issues on its narrow XU pipe, and no integer
-// reduction).  The chunk value v is an exact integer with |v| <= 2^24;
-// q = rint(RN(v RN(1/m))) is within 0.52 of v / m, so r = v - q m (one
-// exact FMA) is an integer with |r| <= 0.52 m <= 133, and the fold reduces
-// it into [0, m).
+// reduction).  The chunk value x is an exact integer with |x| <= 2^24, so
+// |RN(x RN(1/m)) - x/m| <= (2^24/m) 2^-23 (1 + 2^-25) and q = rint of it is
+// within 1/2 + 2.0000002/m of x/m: r = x - q m (one FMA, exact) is an
+// integer with |r| <= m/2 + 2, and adding m to a negative r gives [0, m)
+// (m >= 107).
 __device__ __forceinline__ float rint_f(float x) {  // |x| < 2^22
   return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
 }
-__device__ __forceinline__ float chunk_residue(float v, float m, float inv) {
-  return __fmaf_rn(-rint_f(__fmul_rn(v, inv)), m, v);
-}
-__device__ __forceinline__ float fold_residue(float x, float m, float inv) {  // |x| < 2^22
-  float r = __fmaf_rn(-rint_f(__fmul_rn(x, inv)), m, x);  // |r| <= m / 2
+__device__ __forceinline__ float fold_residue(float x, float m, float inv) {
+  const float r = __fmaf_rn(-rint_f(__fmul_rn(x, inv)), m, x);
   return r < 0.0f ? r + m : r;
 }
 
@@ -321,20 +324,51 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
         fold += ((args.pl.gstart[g + 1] - args.pl.gstart[g]) * nchunks + OZ_FOLD_CHUNKS - 1) /
                 OZ_FOLD_CHUNKS;
       for (int g = g0; g < g1 && ok; ++g) {
+        if (args.mode == OZ_CRT && nchunks == 1) {
+          // residue group (one modulus) of one chunk: the residue goes
+          // straight from TMEM to res on the FP32 pipe, for the valid rows
+          // and columns only (the reassembly reads no other); with several
+          // chunks the int32 accumulation below is cheaper per chunk
+          const int buf = acc & 1;
+          const uint32_t par = (acc >> 1) & 1;
+          ++acc;
+          if (*(volatile int*)&sm.abort || !ptx::mbar_wait(&sm.tfull[buf], par, lim)) {
+            if (!*(volatile int*)&sm.abort) raise_timeout(&sm, args.flag, 3);
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+          const float mf = (float)args.moduli[g];
+          const float invf = __frcp_rn(mf);
+          uint8_t* rp = f.res + (size_t)g * f.Np * f.Mp + (size_t)gj0 * f.Mp + gi;
+          const size_t ld = (size_t)f.Mp;
+          const int ncol = gi < f.M ? f.N - gj0 : 0;  // 0: a padding row
+#pragma unroll 1
+          for (int c4 = 0; c4 < 4; ++c4, rp += 32 * ld) {
+            uint32_t r[32];
+            ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c4 * 32, r);
+            ptx::tmem_ld_wait();
+#pragma unroll
+            for (int e = 0; e < 32; ++e) {
+              if (c4 * 32 + e < ncol) {
+                const float rr = fold_residue(__uint_as_float(r[e]), mf, invf);  // [0, m)
+                // rr < 256 is the low byte of the bits of rr + 2^23
+                rp[e * ld] = (uint8_t)__float_as_uint(__fadd_rn(rr, 8388608.0f));
+              }
+            }
+          }
+          ptx::tc_fence_before();
+          __syncwarp();
+          if (lane == 0) ptx::mbar_arrive(&sm.tempty[buf]);
+          continue;
+        }
         const int t = args.pl.gt[g];
         const int sh = 8 * (args.t_ref - t);
         const int npg = args.pl.gstart[g + 1] - args.pl.gstart[g];
         const int total = npg * nchunks;
-        // per-element sums: int32 of the chunk values, or (CRT form with one
-        // chunk per group, where the integer reduction would dominate) the
-        // fp32 bits of the chunk residue; with several chunks the two-
-        // instruction int32 accumulation per chunk is cheaper
         int c[128];
 #pragma unroll
         for (int e = 0; e < 128; ++e) c[e] = 0;
-        const bool crt = args.mode == OZ_CRT && nchunks == 1;
-        const float mf = crt ? (float)args.moduli[g] : 1.0f;
-        const float invf = __frcp_rn(mf);
         int cnt = 0;
         for (int idx = 0; idx < total; ++idx, ++acc) {
           const int buf = acc & 1;
@@ -350,15 +384,8 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
             uint32_t r[32];
             ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c4 * 32, r);
             ptx::tmem_ld_wait();
-            if (crt) {
 #pragma unroll
-              for (int e = 0; e < 32; ++e)
-                c[c4 * 32 + e] = __float_as_int(__fadd_rn(
-                    __int_as_float(c[c4 * 32 + e]), chunk_residue(__uint_as_float(r[e]), mf, invf)));
-            } else {
-#pragma unroll
-              for (int e = 0; e < 32; ++e) c[c4 * 32 + e] += __float2int_rn(__uint_as_float(r[e]));
-            }
+            for (int e = 0; e < 32; ++e) c[c4 * 32 + e] += __float2int_rn(__uint_as_float(r[e]));
           }
           ptx::tc_fence_before();
           __syncwarp();
@@ -369,15 +396,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
             // CRT form: group g is modulus m_g; keep (A'B') mod m_g as a byte
             // in res[g][col][row], adding to an earlier fold of the group
             uint8_t* rp = f.res + (size_t)g * f.Np * f.Mp + (size_t)gj0 * f.Mp + gi;
-            if (crt) {  // one chunk: the fold is the whole group
-#pragma unroll
-              for (int e = 0; e < 128; ++e) {
-                const float r = fold_residue(__int_as_float(c[e]), mf, invf);  // [0, m)
-                // r < 256 is the low byte of the bits of r + 2^23
-                rp[(size_t)e * f.Mp] = (uint8_t)__float_as_uint(__fadd_rn(r, 8388608.0f));
-                c[e] = 0;
-              }
-            } else {
+            {
               const uint32_t m = (uint32_t)args.moduli[g];
               const uint32_t mg = 0xFFFFFFFFu / m;
               const bool first = cnt == idx + 1;  // no earlier fold in this group
