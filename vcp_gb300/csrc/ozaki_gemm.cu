@@ -344,13 +344,14 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
           const size_t ld = (size_t)f.Mp;
           const int ncol = gi < f.M ? f.N - gj0 : 0;  // 0: a padding row
 #pragma unroll 1
-          for (int c4 = 0; c4 < 4; ++c4, rp += 32 * ld) {
-            uint32_t r[32];
-            ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c4 * 32, r);
+          for (int c8 = 0; c8 < 2; ++c8, rp += 64 * ld) {
+            uint32_t r[64];  // two loads in flight per wait
+            ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c8 * 64, r);
+            ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c8 * 64 + 32, r + 32);
             ptx::tmem_ld_wait();
 #pragma unroll
-            for (int e = 0; e < 32; ++e) {
-              if (c4 * 32 + e < ncol) {
+            for (int e = 0; e < 64; ++e) {
+              if (c8 * 64 + e < ncol) {
                 const float rr = fold_residue(__uint_as_float(r[e]), mf, invf);  // [0, m)
                 // rr < 256 is the low byte of the bits of rr + 2^23
                 rp[e * ld] = (uint8_t)__float_as_uint(__fadd_rn(rr, 8388608.0f));
