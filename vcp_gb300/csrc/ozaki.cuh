@@ -234,6 +234,8 @@ struct OzGBucket {
   int* E3;                 // [Mtot][3]
   int* F2;                 // [Ntot][2]
   double* beta;            // [Ntot]
+  double *midB, *radB;     // [Ntot][Kp] midrad of the stacked B columns
+  unsigned long long* bsum;  // [Ntot][2] sum_k |B'| as (bits >= 32, bits < 32)
   unsigned long long* asum;  // [Mtot][2]
   uint8_t* res;
   int32_t* P;

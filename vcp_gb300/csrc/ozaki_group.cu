@@ -48,6 +48,7 @@ struct BucketHost {
   // workspace layout (byte offsets; the first zero_bytes are cleared per run)
   size_t offRowmax = 0, offAsum = 0, offFlag = 0, zero_bytes = 0;
   size_t offE3 = 0, offF2 = 0, offBeta = 0, offA = 0, offB = 0, offRes = 0, offP = 0;
+  size_t offMidB = 0, offRadB = 0, offBsum = 0;
   size_t ws_bytes = 0;
 };
 
@@ -209,6 +210,9 @@ int oz_group_plan(int count, const BatchProblemView* problems, const char* selec
     b.offE3 = take(sizeof(int) * 3 * Mtot);
     b.offF2 = take(sizeof(int) * 2 * Ntot);
     b.offBeta = take(sizeof(double) * Ntot);
+    b.offMidB = take(sizeof(double) * (size_t)Ntot * kv.first);
+    b.offRadB = take(sizeof(double) * (size_t)Ntot * kv.first);
+    b.offBsum = take(sizeof(unsigned long long) * 2 * Ntot);
     b.offA = take(sizeof(uint16_t) * (size_t)(Lmax + 4) * Mtot * kv.first);
     b.offB = take(sizeof(uint16_t) * (size_t)(Lmax + 4) * Ntot * kv.first);
     b.offRes = take((size_t)res);
@@ -268,6 +272,9 @@ int oz_group_record(OzGroupPlan* g, unsigned long long* t_first, unsigned long l
     d.E3 = (int*)(ws + b.offE3);
     d.F2 = (int*)(ws + b.offF2);
     d.beta = (double*)(ws + b.offBeta);
+    d.midB = (double*)(ws + b.offMidB);
+    d.radB = (double*)(ws + b.offRadB);
+    d.bsum = (unsigned long long*)(ws + b.offBsum);
     d.planesA = (uint16_t*)(ws + b.offA);
     d.planesB = (uint16_t*)(ws + b.offB);
     d.res = ws + b.offRes;

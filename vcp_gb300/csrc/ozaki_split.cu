@@ -650,12 +650,7 @@ __global__ void __launch_bounds__(256, 3) oz_split_left_crt_g(const __grid_const
                                    b.asum + 2 * (size_t)q.rowoff);
 }
 
-// Grouped right split: one warp per stacked column (most columns of a batch
-// are short), 8 columns per block.  Pass 1: midrad and the column maxima
-// (warp reductions).  Pass 2: lane t takes the 8 consecutive k of
-// 8 (t + 32 it) .. + 7, reads the column again (an L1 / L2 hit) and writes
-// the residue and digit planes 16 bytes at a time; beta_j as in
-// oz_beta_right.
+// Warp reductions of 64-bit maxima and sums.
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -681,125 +676,147 @@ __device__ __forceinline__ void store_bf16s(uint16_t* dst, const uint32_t (&h)[K
     *reinterpret_cast<uint32_t*>(dst) = h[0];
 }
 
-template <int NL, int KPL>
-__global__ void __launch_bounds__(256) oz_split_right_crt_g(const __grid_constant__ OzGBucket b) {
+// Grouped right factor in three passes, as for one product.  Pass 1: one
+// warp per stacked column (8 per block): midrad stored as midB / radB
+// ([Ntot][Kp]), the column maxima and exponents, the column sums cleared;
+// padding columns get the zero exponent.
+__global__ void __launch_bounds__(256) oz_colmax_right_g(const __grid_constant__ OzGBucket b) {
   const int lane = threadIdx.x & 31;
   const int jst = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (jst >= b.Ntot) return;  // whole warps only: no block-level barrier below
+  if (jst >= b.Ntot) return;  // whole warps only
   const int p = b.col_prob[jst];
   const OzGProb& q = b.probs[p];
-  const int j = jst - q.coloff, K = q.k, N = q.n, Kp = b.Kp, L = q.L, w = q.w;
-  const size_t pstride = (size_t)b.Ntot * Kp;
-  uint16_t* planes_m = b.planesB;
-  uint16_t* planes_r = b.planesB + (size_t)b.Lmax * pstride;
-  uint16_t* planes_s = b.planesB + (size_t)(b.Lmax + 2) * pstride;
-  constexpr int HW = KPL / 2;  // 32-bit words per lane and plane
-  const uint32_t zero[HW] = {};
-  if (j >= N) {  // a padding column: zero planes, zero exponents, zero beta
-    if (lane == 0) {
-      b.F2[2 * jst + 0] = b.F2[2 * jst + 1] = OZ_ZERO_EXP;
-      b.beta[jst] = 0.0;
-    }
-    for (int k0 = KPL * lane; k0 < Kp; k0 += KPL * 32) {
-      const size_t off = (size_t)jst * Kp + k0;
-#pragma unroll
-      for (int qq = 0; qq < 2; ++qq) {
-        store_bf16s<KPL>(planes_r + qq * pstride + off, zero);
-        store_bf16s<KPL>(planes_s + qq * pstride + off, zero);
-      }
-      for (int l = 0; l < L; ++l) store_bf16s<KPL>(planes_m + l * pstride + off, zero);
-    }
-    return;
-  }
-  const double* bcol = q.B + 2 * (long)j * q.ldb;
+  const int j = jst - q.coloff, K = q.k;
   unsigned long long am = 0, ar = 0;
   bool bad = false;
-  for (int k = lane; k < K; k += 32) {
-    const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
-    double m, r, pp;
-    if (sw_finite(e.x) && sw_finite(e.y)) {
-      sw_midrad(e.x, e.y, m, r, pp);
-      am = max(am, dbits(oz_abs(m)));
-      ar = max(ar, dbits(r));
-    } else {
-      bad = true;
+  if (j < q.n) {
+    const double* bcol = q.B + 2 * (long)j * q.ldb;
+    double* mcol = b.midB + (size_t)jst * b.Kp;
+    double* rcol = b.radB + (size_t)jst * b.Kp;
+    for (int k = lane; k < K; k += 32) {
+      const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
+      double m = 0.0, r = 0.0;
+      if (sw_finite(e.x) && sw_finite(e.y)) {
+        double pp;
+        sw_midrad(e.x, e.y, m, r, pp);
+        am = max(am, dbits(oz_abs(m)));
+        ar = max(ar, dbits(r));
+      } else {
+        bad = true;
+      }
+      mcol[k] = m;
+      rcol[k] = r;
     }
   }
   if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&b.flag[4 * p], 1);
   am = warp_max_u64(am);
   ar = warp_max_u64(ar);
-  const int Fm = oz_exponent(__longlong_as_double((long long)am));
-  const int Fr = oz_exponent(__longlong_as_double((long long)ar));
   if (lane == 0) {
-    b.F2[2 * jst + 0] = Fm;
-    b.F2[2 * jst + 1] = Fr;
+    b.F2[2 * jst + 0] = j < q.n ? oz_exponent(__longlong_as_double((long long)am)) : OZ_ZERO_EXP;
+    b.F2[2 * jst + 1] = j < q.n ? oz_exponent(__longlong_as_double((long long)ar)) : OZ_ZERO_EXP;
+    b.bsum[2 * jst + 0] = 0;
+    b.bsum[2 * jst + 1] = 0;
   }
+}
+
+// Pass 2: residue and radius-digit planes.  Block: 8 stacked columns x
+// 32 KPL k; warp q takes column 8 bx + q, lane t the KPL consecutive k of
+// 32 KPL by + KPL t (KPL = 2, 4, 8 by the bucket's Kp, so that short
+// columns keep the lanes busy); padding (columns past n, k past K) is
+// written as zeros without computing; sum_k |B'| accumulates per column.
+template <int NL, int KPL>
+__global__ void __launch_bounds__(256) oz_split_right2_g(const __grid_constant__ OzGBucket b) {
+  const int lane = threadIdx.x & 31;
+  const int jst = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int k0 = (blockIdx.y * 32 + lane) * KPL;
+  if (jst >= b.Ntot) return;  // whole warps only (no barrier below)
+  const int p = b.col_prob[jst];
+  const OzGProb& q = b.probs[p];
+  const int j = jst - q.coloff, K = q.k, Kp = b.Kp, L = q.L, w = q.w;
+  const size_t pstride = (size_t)b.Ntot * Kp;
+  uint16_t* planes_m = b.planesB;
+  uint16_t* planes_r = b.planesB + (size_t)b.Lmax * pstride;
+  uint16_t* planes_s = b.planesB + (size_t)(b.Lmax + 2) * pstride;
+  constexpr int HW = KPL / 2;  // 32-bit words per lane and plane
   unsigned long long shi = 0, slo = 0;
-  for (int k0 = KPL * lane; k0 < Kp; k0 += KPL * 32) {
+  if (k0 < Kp) {
     const size_t off = (size_t)jst * Kp + k0;
-    if (k0 >= K) {  // padding of the inner dimension: zeros, nothing to compute
+    if (j >= q.n || k0 >= K) {  // padding: zeros, nothing to compute
+      const uint32_t zero[HW] = {};
 #pragma unroll
       for (int qq = 0; qq < 2; ++qq) {
         store_bf16s<KPL>(planes_r + qq * pstride + off, zero);
         store_bf16s<KPL>(planes_s + qq * pstride + off, zero);
       }
       for (int l = 0; l < L; ++l) store_bf16s<KPL>(planes_m + l * pstride + off, zero);
-      continue;
-    }
-    float hl[KPL][NL];
-    uint32_t hr[2][HW], hs[2][HW];
+    } else {
+      const int Fm = b.F2[2 * jst], Fr = b.F2[2 * jst + 1];
+      const double* mcol = b.midB + (size_t)jst * Kp;
+      const double* rcol = b.radB + (size_t)jst * Kp;
+      float hl[KPL][NL];
+      uint32_t hr[2][HW], hs[2][HW];
 #pragma unroll
-    for (int t = 0; t < KPL; t += 2) {
-      int d0[2], d1[2], e0[2], e1[2];
+      for (int t = 0; t < KPL; t += 2) {
+        int d0[2], d1[2], e0[2], e1[2];
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int k = k0 + t + u;
-        double m = 0.0, r = 0.0;
-        if (k < K) {
-          const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
-          double pp;
-          if (sw_finite(e.x) && sw_finite(e.y)) sw_midrad(e.x, e.y, m, r, pp);
+        for (int u = 0; u < 2; ++u) {
+          const int k = k0 + t + u;
+          double m = 0.0, r = 0.0;
+          if (k < K) {
+            m = mcol[k];
+            r = rcol[k];
+          }
+          const long long bb = crt_int(m, Fm, w);
+          const unsigned long long ub = (unsigned long long)(bb < 0 ? -bb : bb);
+          shi += ub >> 32;
+          slo += ub & 0xffffffffULL;
+          limbs12<NL>(ub, bb < 0, hl[t + u]);
+          digits_of<2>(r, Fr, 1, u ? d1 : d0);
+          digits_of<2>(oz_abs(m), Fm, 1, u ? e1 : e0);
         }
-        const long long bb = crt_int(m, Fm, w);
-        const unsigned long long ub = (unsigned long long)(bb < 0 ? -bb : bb);
-        shi += ub >> 32;
-        slo += ub & 0xffffffffULL;
-        limbs12<NL>(ub, bb < 0, hl[t + u]);
-        digits_of<2>(r, Fr, 1, u ? d1 : d0);
-        digits_of<2>(oz_abs(m), Fm, 1, u ? e1 : e0);
+#pragma unroll
+        for (int qq = 0; qq < 2; ++qq) {
+          hr[qq][t / 2] = bf16_bits(d0[qq]) | (bf16_bits(d1[qq]) << 16);
+          hs[qq][t / 2] = bf16_bits(e0[qq]) | (bf16_bits(e1[qq]) << 16);
+        }
       }
 #pragma unroll
       for (int qq = 0; qq < 2; ++qq) {
-        hr[qq][t / 2] = bf16_bits(d0[qq]) | (bf16_bits(d1[qq]) << 16);
-        hs[qq][t / 2] = bf16_bits(e0[qq]) | (bf16_bits(e1[qq]) << 16);
+        store_bf16s<KPL>(planes_r + qq * pstride + off, hr[qq]);
+        store_bf16s<KPL>(planes_s + qq * pstride + off, hs[qq]);
       }
-    }
 #pragma unroll
-    for (int qq = 0; qq < 2; ++qq) {
-      store_bf16s<KPL>(planes_r + qq * pstride + off, hr[qq]);
-      store_bf16s<KPL>(planes_s + qq * pstride + off, hs[qq]);
-    }
+      for (int l = 0; l < OZ_MAX_MODULI_128; ++l) {
+        if (l >= L) break;
+        uint32_t h[HW];
 #pragma unroll
-    for (int l = 0; l < OZ_MAX_MODULI_128; ++l) {
-      if (l >= L) break;
-      uint32_t h[HW];
-#pragma unroll
-      for (int t = 0; t < KPL; t += 2)
-        h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
-      store_bf16s<KPL>(planes_m + l * pstride + off, h);
+        for (int t = 0; t < KPL; t += 2)
+          h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
+        store_bf16s<KPL>(planes_m + l * pstride + off, h);
+      }
     }
   }
   shi = warp_sum_u64(shi);
   slo = warp_sum_u64(slo);
-  if (lane == 0) {
-    double bj = 0.0;
-    if (Fm != OZ_ZERO_EXP) {
-      const double v = __fma_ru((double)shi, 0x1p32,
-                                (double)(slo + (unsigned long long)(K + 1) / 2));
-      bj = dev_scale_dir(v, Fm - w, true);
-    }
-    b.beta[jst] = bj;
+  if (lane == 0 && (shi | slo)) {
+    atomicAdd(&b.bsum[2 * jst + 0], shi);
+    atomicAdd(&b.bsum[2 * jst + 1], slo);
   }
+}
+
+// Pass 3: beta_j = RU((sum_k |B'| + ceil(K/2)) 2^(Fm - w)) per stacked column.
+__global__ void oz_beta_right_g(const __grid_constant__ OzGBucket b) {
+  const int jst = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jst >= b.Ntot) return;
+  const OzGProb& q = b.probs[b.col_prob[jst]];
+  const int j = jst - q.coloff, Fm = b.F2[2 * jst];
+  double bj = 0.0;
+  if (j < q.n && Fm != OZ_ZERO_EXP) {
+    const double v = __fma_ru((double)b.bsum[2 * jst], 0x1p32,
+                              (double)(b.bsum[2 * jst + 1] + (unsigned long long)(q.k + 1) / 2));
+    bj = dev_scale_dir(v, Fm - q.w, true);
+  }
+  b.beta[jst] = bj;
 }
 
 int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, int wmax, cudaStream_t st) {
@@ -812,15 +829,18 @@ int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, int wmax, cuda
   // |A'|, |B'| <= 2^(w-1): four 14-bit limbs up to w = 56, six 12-bit limbs
   // up to w = 73; lanes of the right split take 2, 4 or 8 consecutive k so
   // that short columns keep the warp busy
-  const int nbr = (b.Ntot + 7) / 8;
-#define OZ_GRIGHT(NL)                                                           \
-  do {                                                                          \
-    if (b.Kp <= 64)                                                             \
-      oz_split_right_crt_g<NL, 2><<<nbr, 256, 0, st>>>(b);                      \
-    else if (b.Kp <= 128)                                                       \
-      oz_split_right_crt_g<NL, 4><<<nbr, 256, 0, st>>>(b);                      \
-    else                                                                        \
-      oz_split_right_crt_g<NL, 8><<<nbr, 256, 0, st>>>(b);                      \
+  oz_colmax_right_g<<<(b.Ntot + 7) / 8, 256, 0, st>>>(b);
+  VCPCU_LAUNCH_CHECK("oz_colmax_right_g");
+  const int kpl = b.Kp <= 64 ? 2 : (b.Kp <= 128 ? 4 : 8);
+  const dim3 g2((b.Ntot + 7) / 8, (b.Kp + 32 * kpl - 1) / (32 * kpl));
+#define OZ_GRIGHT(NL)                                             \
+  do {                                                            \
+    if (kpl == 2)                                                 \
+      oz_split_right2_g<NL, 2><<<g2, 256, 0, st>>>(b);            \
+    else if (kpl == 4)                                            \
+      oz_split_right2_g<NL, 4><<<g2, 256, 0, st>>>(b);            \
+    else                                                          \
+      oz_split_right2_g<NL, 8><<<g2, 256, 0, st>>>(b);            \
   } while (0)
   if (wmax <= 56) {
     oz_split_left_crt_g<4><<<nblk_split, 256, 0, st>>>(b);
@@ -832,7 +852,9 @@ int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, int wmax, cuda
     OZ_GRIGHT(6);
   }
 #undef OZ_GRIGHT
-  VCPCU_LAUNCH_CHECK("oz_split_right_crt_g");
+  VCPCU_LAUNCH_CHECK("oz_split_right2_g");
+  oz_beta_right_g<<<(b.Ntot + 255) / 256, 256, 0, st>>>(b);
+  VCPCU_LAUNCH_CHECK("oz_beta_right_g");
   return VCPCU_OK;
 }
 
