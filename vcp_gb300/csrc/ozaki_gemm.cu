@@ -349,13 +349,19 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
             ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c8 * 64, r);
             ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c8 * 64 + 32, r + 32);
             ptx::tmem_ld_wait();
+            // residue bytes: rr < 256 is the low byte of the bits of rr + 2^23
 #pragma unroll
-            for (int e = 0; e < 64; ++e) {
-              if (c8 * 64 + e < ncol) {
-                const float rr = fold_residue(__uint_as_float(r[e]), mf, invf);  // [0, m)
-                // rr < 256 is the low byte of the bits of rr + 2^23
-                rp[e * ld] = (uint8_t)__float_as_uint(__fadd_rn(rr, 8388608.0f));
-              }
+            for (int e = 0; e < 64; ++e)
+              r[e] = __float_as_uint(
+                  __fadd_rn(fold_residue(__uint_as_float(r[e]), mf, invf), 8388608.0f));
+            const int nc = ncol - c8 * 64;
+            if (nc >= 64) {  // the common case: no per-column test
+#pragma unroll
+              for (int e = 0; e < 64; ++e) rp[e * ld] = (uint8_t)r[e];
+            } else {
+#pragma unroll
+              for (int e = 0; e < 64; ++e)
+                if (e < nc) rp[e * ld] = (uint8_t)r[e];
             }
           }
           ptx::tc_fence_before();
