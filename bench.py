@@ -498,7 +498,9 @@ def time_stream(fn, stream, steps, warmup=1):
 def time_profiled(fn, stream, steps, pk):
     """time_stream plus the library's phase timing: (ms per call, roofline of
     the slice GEMMs against the measured bf16 burst peak)."""
+    import torch
     from vcp_gb300 import _lib
+    torch.cuda.synchronize()  # inputs are made on torch's stream, the work runs on `stream`
     fn()
     stream.synchronize()
     _lib.profile(True)
