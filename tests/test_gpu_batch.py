@@ -81,3 +81,20 @@ def test_grouped_tensor_core_batch_edges(cuda_lib):
         pidcuda.mulmm_dev(m, n, k, A, lda, B, ldb, ref, ldc, pidcuda.FORM_OZAKI)
         torch.cuda.synchronize()
         assert torch.equal(C.view(torch.int64), ref.view(torch.int64)), (m, n, k)
+
+
+@pytest.mark.parametrize("slices", [2, 10])
+def test_grouped_batch_slice_counts(cuda_lib, slices):
+    """The grouped tensor-core path at other precisions: 2 slices (14-bit
+    operands, few moduli) and 10 slices (62-bit operands: the 12-bit limb
+    forms of the splits); every product bit-identical to its single call."""
+    import torch
+    rng = np.random.default_rng(90 + slices)
+    probs = make_batch(rng, 30, 20, 400)
+    batch.run(probs, pidcuda.FORM_OZAKI, slices)
+    torch.cuda.synchronize()
+    for (m, n, k, A, lda, B, ldb, C, ldc) in probs:
+        ref = torch.empty_like(C)
+        pidcuda.mulmm_dev(m, n, k, A, lda, B, ldb, ref, ldc, pidcuda.FORM_OZAKI, slices)
+        torch.cuda.synchronize()
+        assert torch.equal(C.view(torch.int64), ref.view(torch.int64)), (m, n, k, slices)

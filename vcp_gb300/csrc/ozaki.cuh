@@ -235,6 +235,7 @@ struct OzGBucket {
   int* F2;                 // [Ntot][2]
   double* beta;            // [Ntot]
   double *midB, *radB;     // [Ntot][Kp] midrad of the stacked B columns
+  double *midA, *radA;     // [Kp][Mtot] midrad of the stacked A rows (column-major)
   unsigned long long* bsum;  // [Ntot][2] sum_k |B'| as (bits >= 32, bits < 32)
   unsigned long long* asum;  // [Mtot][2]
   uint8_t* res;

@@ -48,7 +48,7 @@ struct BucketHost {
   // workspace layout (byte offsets; the first zero_bytes are cleared per run)
   size_t offRowmax = 0, offAsum = 0, offFlag = 0, zero_bytes = 0;
   size_t offE3 = 0, offF2 = 0, offBeta = 0, offA = 0, offB = 0, offRes = 0, offP = 0;
-  size_t offMidB = 0, offRadB = 0, offBsum = 0;
+  size_t offMidB = 0, offRadB = 0, offBsum = 0, offMidA = 0, offRadA = 0;
   size_t ws_bytes = 0;
 };
 
@@ -213,6 +213,8 @@ int oz_group_plan(int count, const BatchProblemView* problems, const char* selec
     b.offMidB = take(sizeof(double) * (size_t)Ntot * kv.first);
     b.offRadB = take(sizeof(double) * (size_t)Ntot * kv.first);
     b.offBsum = take(sizeof(unsigned long long) * 2 * Ntot);
+    b.offMidA = take(sizeof(double) * (size_t)Mtot * kv.first);
+    b.offRadA = take(sizeof(double) * (size_t)Mtot * kv.first);
     b.offA = take(sizeof(uint16_t) * (size_t)(Lmax + 4) * Mtot * kv.first);
     b.offB = take(sizeof(uint16_t) * (size_t)(Lmax + 4) * Ntot * kv.first);
     b.offRes = take((size_t)res);
@@ -275,6 +277,8 @@ int oz_group_record(OzGroupPlan* g, unsigned long long* t_first, unsigned long l
     d.midB = (double*)(ws + b.offMidB);
     d.radB = (double*)(ws + b.offRadB);
     d.bsum = (unsigned long long*)(ws + b.offBsum);
+    d.midA = (double*)(ws + b.offMidA);
+    d.radA = (double*)(ws + b.offRadA);
     d.planesA = (uint16_t*)(ws + b.offA);
     d.planesB = (uint16_t*)(ws + b.offB);
     d.res = ws + b.offRes;

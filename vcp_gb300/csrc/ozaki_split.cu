@@ -454,11 +454,10 @@ struct TileStore {
 // Block: 32 rows x 64 k; lane = row, warp q takes k0 + 8q .. k0 + 8q + 7, so
 // the loads of mA / rA are coalesced across the warp; each lane's 8 bf16
 // (16 bytes) per plane go out through shared memory (TileStore).
-// FROM_A: midrad again from the interval matrix X (ld ldx) instead of the
-// stored planes mA = X, rA (ld ldx).  Planes rows are rowbase + i (stacked
-// problems), pstride elements apart; E3 and asum point at row 0 of this
-// problem.
-template <int SR, int NL, bool FROM_A>
+// X = mA and rA are the stored midrad planes (ld ldx).  Planes rows are
+// rowbase + i (stacked problems), pstride elements apart; E3 and asum point
+// at row 0 of this problem.
+template <int SR, int NL>
 __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K, int Kp,
                                                     size_t pstride, int rowbase,
                                                     const double* __restrict__ X,
@@ -499,14 +498,9 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
         const int k = k0 + t + u;
         double m = 0.0, r = 0.0, p = 0.0;
         if (i < M && k < K) {
-          if (FROM_A) {
-            const double2 e = *reinterpret_cast<const double2*>(X + 2 * (i + (long)k * ldx));
-            if (sw_finite(e.x) && sw_finite(e.y)) sw_midrad(e.x, e.y, m, r, p);
-          } else {
-            m = X[i + (long)k * ldx];
-            r = rA[i + (long)k * ldx];
-            p = sw_add_ru_pos(oz_abs(m), r);
-          }
+          m = X[i + (long)k * ldx];
+          r = rA[i + (long)k * ldx];
+          p = sw_add_ru_pos(oz_abs(m), r);
         }
         a[t + u] = crt_int(m, Em, w);
         digits_of<SR>(p, Ep, 1, u ? d1 : d0);
@@ -567,7 +561,7 @@ oz_split_left_crt(int M, int K, int Kp, size_t pstride, int rowbase,
                   int w, const int* __restrict__ E3, uint16_t* __restrict__ planes_m,
                   uint16_t* __restrict__ planes_p, uint16_t* __restrict__ planes_r,
                   unsigned long long* __restrict__ asum) {
-  split_left_crt_body<SR, NL, false>(blockIdx.x, blockIdx.y, M, K, Kp, pstride, rowbase, mA, rA,
+  split_left_crt_body<SR, NL>(blockIdx.x, blockIdx.y, M, K, Kp, pstride, rowbase, mA, rA,
                                      ldx, L, w, E3, planes_m, planes_p, planes_r, asum);
 }
 
@@ -610,9 +604,10 @@ oz_rowmax_left_g(const __grid_constant__ OzGBucket b) {
   if (i < q.m) {
     const int c0 = (local / nbx) * 256;
     const int c1 = min(q.k, c0 + 256);
+    const size_t row = (size_t)(q.rowoff + i);
     for (int c = c0 + ph; c < c1; c += 8) {
       const double2 e = *reinterpret_cast<const double2*>(q.A + 2 * (i + (long)c * q.lda));
-      double m, r, pp;
+      double m = 0.0, r = 0.0, pp;
       if (sw_finite(e.x) && sw_finite(e.y)) {
         sw_midrad(e.x, e.y, m, r, pp);
         am = max(am, dbits(oz_abs(m)));
@@ -621,6 +616,9 @@ oz_rowmax_left_g(const __grid_constant__ OzGBucket b) {
       } else {
         bad = true;
       }
+      // stored for the split (column-major over the stacked rows)
+      b.midA[row + (size_t)c * b.Mtot] = m;
+      b.radA[row + (size_t)c * b.Mtot] = r;
     }
   }
   if (bad) atomicOr(&b.flag[4 * p], 1);
@@ -643,8 +641,9 @@ __global__ void __launch_bounds__(256, 3) oz_split_left_crt_g(const __grid_const
   const int nbx = b.Kp / 64;
   const int local = blockIdx.x - b.blk_split[p];
   const size_t pstride = (size_t)b.Mtot * b.Kp;
-  split_left_crt_body<2, NL, true>(local % nbx, local / nbx, q.m, q.k, b.Kp, pstride, q.rowoff,
-                                   q.A, nullptr, q.lda, q.L, q.w, b.E3 + 3 * (size_t)q.rowoff,
+  split_left_crt_body<2, NL>(local % nbx, local / nbx, q.m, q.k, b.Kp, pstride, q.rowoff,
+                                    b.midA + q.rowoff, b.radA + q.rowoff, b.Mtot, q.L, q.w,
+                                    b.E3 + 3 * (size_t)q.rowoff,
                                    b.planesA, b.planesA + (size_t)b.Lmax * pstride,
                                    b.planesA + (size_t)(b.Lmax + 2) * pstride,
                                    b.asum + 2 * (size_t)q.rowoff);
