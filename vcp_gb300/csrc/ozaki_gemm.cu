@@ -1,22 +1,23 @@
 // ozaki_gemm.cu -- the slice GEMM of the Ozaki form on tcgen05 tensor cores.
 //
-// For one output tile (128 x 256) the kernel runs an ordered list of digit
-// plane pairs (A_p, B_q), grouped by t = p + q.  Each pair is a bf16 GEMM
-// over the whole (padded) inner dimension, split into chunks of 1024: every
-// chunk accumulates in fp32 in tensor memory, where it is an exact integer
-// (|digit products| <= 2^14, 1024 of them <= 2^24).  Epilogue warps drain
-// each finished chunk (double-buffered TMEM accumulators, so draining
-// overlaps the next chunk's MMAs) into int32 registers, and fold the
-// group's integer sum C_t into an int64 fixed-point value
-//     W = sum_t C_t * 2^(8 (t_ref - t))      (unit 2^(E_i + F_j - 8 t_ref))
-// kept in global memory (one read-modify-write per fold).  Shifts to the
-// right floor, so the exact truncated product lies in [W, W + R] units
-// where R counts the floored folds.  The last fold is merged into the
-// final epilogue:
-//   OZ_RAD_SET / OZ_RAD_ADD  T(i,j) (+)= RU((W + R) * unit)  (radius factors
-//                            were rounded up, so this bounds them from above)
-//   OZ_MID                   [lo, up] = [RD(W unit) - e, RU((W+R) unit) + e],
-//                            e = RU(truncation bound + T(i,j)).
+// A work item is one output tile (128 x 256) and one group of digit / residue
+// plane pairs (A_p, B_q).  Each pair is a bf16 GEMM over the whole (padded)
+// inner dimension, split into chunks of 1024: every chunk accumulates in fp32
+// in tensor memory, where it is an exact integer (|digit products| <= 2^14,
+// 1024 of them <= 2^24).  Epilogue warps drain each finished chunk
+// (double-buffered TMEM accumulators, so draining overlaps the next chunk's
+// MMAs) and, per mode:
+//   OZ_CRT       group g = modulus m_g: the residue of the integer product
+//                mod m_g, one byte per entry in res[g][col][row] (one chunk:
+//                reduced on the FP32 pipe straight from TMEM; several: int32
+//                chunk sums, reduced per fold of 64 chunks);
+//   OZ_RAD_SET / OZ_RAD_ADD  the group's int32 chunk sum, one fold per 64
+//                chunks into P (the reassembly scales and adds the folds:
+//                radius factors were rounded up, so the sum bounds them);
+//   OZ_MID       (slice form) folds into an int64 fixed-point value
+//                W = sum_t C_t 2^(8 (t_ref - t)) in global memory; the last
+//                fold is merged into the final epilogue
+//                [lo, up] = [RD(W unit) - e, RU((W + R) unit) + e].
 //
 // Warp roles (320 threads, one CTA per SM, persistent over tiles):
 //   warp 0      TMA producer (4-stage ring of 48 KB A+B k-blocks)
