@@ -335,16 +335,20 @@ __device__ __forceinline__ int dev_sym_residue(unsigned long long a, int neg, in
 
 // Residues on the FP32 pipe (the integer multiply pipe is half as wide).
 // |a| is cut into b-bit limbs h_t (b = 12; b = 14 for the four-limb form,
-// which holds magnitudes <= 2^55), exact as floats, and
+// which holds magnitudes <= 2^55; b = 13 for the eight-limb form of the dd
+// product, magnitudes < 2^103), exact as floats, and
 // x = sum_t h_t c_lt with c_lt = 2^(b t) mod m_l taken in [-m_l/2, m_l/2]:
 // |x| <= 128 sum_t |h_t| < 2^23 for every limb form used here (at most 16
-// twelve-bit limbs; four 14-bit limbs whose top one is <= 2^13), an exact
+// twelve-bit limbs; four 14-bit limbs whose top one is <= 2^13; eight
+// 13-bit limbs whose top one is < 2^12), an exact
 // float.  One rounded quotient q = rint(RN(x RN(1/m))) then lands within
 // |x / m| 2^-23 (1 + 2^-25) < 1 / m of the exact one, so
 // r = x - q m (one exact FMA) has |r| <= m/2 + 1 - 1/8, i.e. |r| <= 128:
 // a residue of a in the range the slice GEMM's exact chunk sums allow
 // (|r_a r_b| <= 2^14 over 1024 terms), and exact in bf16.
-__host__ __device__ constexpr int oz_limb_bits(int NL) { return NL == 4 ? 14 : 12; }
+__host__ __device__ constexpr int oz_limb_bits(int NL) {
+  return NL == 4 ? 14 : (NL == 8 ? 13 : 12);
+}
 constexpr float oz_limb_c(unsigned long long m, int b, int t) {
   unsigned long long c = 1 % m;
   for (int i = 0; i < t; ++i) c = (c << b) % m;
@@ -356,10 +360,14 @@ constexpr float oz_limb_c(unsigned long long m, int b, int t) {
    oz_limb_c(m, 12, 8), oz_limb_c(m, 12, 9)}
 #define OZ_LIMB14_ROW(m) \
   {oz_limb_c(m, 14, 0), oz_limb_c(m, 14, 1), oz_limb_c(m, 14, 2), oz_limb_c(m, 14, 3)}
+#define OZ_LIMB13_ROW(m)                                                                 \
+  {oz_limb_c(m, 13, 0), oz_limb_c(m, 13, 1), oz_limb_c(m, 13, 2), oz_limb_c(m, 13, 3),   \
+   oz_limb_c(m, 13, 4), oz_limb_c(m, 13, 5), oz_limb_c(m, 13, 6), oz_limb_c(m, 13, 7)}
 #define OZ_MODF(m) ((float)(m))
 #define OZ_INVF(m) (1.0f / (float)(m))
 __constant__ float c_limbf[OZ_MAX_MODULI][10] = {OZ_MOD_LIST(OZ_LIMB_ROW)};
 __constant__ float c_limbf14[OZ_MAX_MODULI][4] = {OZ_MOD_LIST(OZ_LIMB14_ROW)};
+__constant__ float c_limbf13[OZ_MAX_MODULI][8] = {OZ_MOD_LIST(OZ_LIMB13_ROW)};
 __constant__ float c_modf[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_MODF)};
 __constant__ float c_invf[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_INVF)};
 
@@ -400,7 +408,7 @@ __device__ __forceinline__ float res_sym(const float (&h)[NL], int l) {
   float x = h[0];
 #pragma unroll
   for (int t = 1; t < NL; ++t)
-    x = __fmaf_rn(h[t], NL == 4 ? c_limbf14[l][t] : c_limbf[l][t], x);
+    x = __fmaf_rn(h[t], NL == 4 ? c_limbf14[l][t] : (NL == 8 ? c_limbf13[l][t] : c_limbf[l][t]), x);
   return __fmaf_rn(-rint_small(__fmul_rn(x, inv)), m, x);
 }
 
@@ -1217,6 +1225,7 @@ __global__ void dd_exponents(int R, const unsigned long long* __restrict__ mx,
 // Left dd factor -> residue planes [L][Mp][Kp].  Block: 32 rows x 64 k;
 // lane = row, warp q takes k0 + 8q .. k0 + 8q + 7 (coalesced loads across
 // the warp); the plane tiles go out through shared memory (TileStore).
+template <int NL>
 __global__ void __launch_bounds__(256)
 dd_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long lda, int L, int w,
               const int* __restrict__ E, uint16_t* __restrict__ planes) {
@@ -1245,16 +1254,16 @@ dd_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long l
   TileStore ts{tile_smem, 0};
   const size_t tile0 = (size_t)(blockIdx.y * 32) * Kp + blockIdx.x * 64;
   const size_t pstride = (size_t)Mp * Kp;
-  float hl[8][10];
+  float hl[8][NL];
 #pragma unroll
-  for (int t = 0; t < 8; ++t) limbs12<10>(ua[t], (negm >> t) & 1u, hl[t]);
+  for (int t = 0; t < 8; ++t) limbs12<NL>(ua[t], (negm >> t) & 1u, hl[t]);
 #pragma unroll
   for (int l = 0; l < OZ_MAX_MODULI; ++l) {
     if (l >= L) break;
     uint32_t h[4];
 #pragma unroll
     for (int t = 0; t < 8; t += 2)
-      h[t / 2] = pack_bf16x2(res_sym<10>(hl[t], l), res_sym<10>(hl[t + 1], l));
+      h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
     ts.put(make_uint4(h[0], h[1], h[2], h[3]), planes + l * pstride + tile0, Kp);
   }
 }
@@ -1291,6 +1300,7 @@ dd_colmax(int K, int N, int Np, const double* __restrict__ B, long ldb, int* __r
 // 256 k; warp q takes column 8 bx.y + q, lane t the 8 consecutive k of
 // 256 bx.x + 8 t .. + 7 (each warp reads 4 KB of its column contiguously and
 // writes 512 contiguous bytes per plane).
+template <int NL>
 __global__ void __launch_bounds__(256)
 dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long ldb, int L, int w,
                const int* __restrict__ F, uint16_t* __restrict__ planes) {
@@ -1300,7 +1310,7 @@ dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
   if (j >= Np || k0 >= Kp) return;
   const int Fj = F[j];
   const double* bcol = B + 2 * (long)j * ldb;
-  float hl[8][10];
+  float hl[8][NL];
 #pragma unroll
   for (int t = 0; t < 8; ++t) {
     const int k = k0 + t;
@@ -1313,7 +1323,7 @@ dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
       }
     }
     const __int128 b = dd_int(hi, lo, Fj, w);
-    limbs12<10>((unsigned __int128)(b < 0 ? -b : b), b < 0, hl[t]);
+    limbs12<NL>((unsigned __int128)(b < 0 ? -b : b), b < 0, hl[t]);
   }
   const size_t pstride = (size_t)Np * Kp, off = (size_t)j * Kp + k0;
 #pragma unroll
@@ -1322,7 +1332,7 @@ dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
     uint32_t h[4];
 #pragma unroll
     for (int t = 0; t < 8; t += 2)
-      h[t / 2] = pack_bf16x2(res_sym<10>(hl[t], l), res_sym<10>(hl[t + 1], l));
+      h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
     *reinterpret_cast<uint4*>(planes + l * pstride + off) = make_uint4(h[0], h[1], h[2], h[3]);
   }
 }
@@ -1341,12 +1351,20 @@ int dd_prepare(int M, int N, int K, int Mp, int Np, int Kp, int L, int w, const 
   dd_exponents<<<(Mp + 255) / 256, 256, 0, st>>>(Mp, rowmax, E);
   VCPCU_LAUNCH_CHECK("dd_exponents");
   dim3 g2(Kp / 64, Mp / 32);
-  dd_split_left<<<g2, 256, 0, st>>>(M, K, Mp, Kp, A, lda, L, w, E, planesA);
+  // |A'|, |B'| < 2^(w-1): eight 13-bit limbs up to w = 104, ten 12-bit ones
+  // up to w = 120
+  if (w <= 104)
+    dd_split_left<8><<<g2, 256, 0, st>>>(M, K, Mp, Kp, A, lda, L, w, E, planesA);
+  else
+    dd_split_left<10><<<g2, 256, 0, st>>>(M, K, Mp, Kp, A, lda, L, w, E, planesA);
   VCPCU_LAUNCH_CHECK("dd_split_left");
   dd_colmax<<<(Np + 7) / 8, 256, 0, st>>>(K, N, Np, B, ldb, F, flag);
   VCPCU_LAUNCH_CHECK("dd_colmax");
   dim3 g3((Kp + 255) / 256, Np / 8);
-  dd_split_right<<<g3, 256, 0, st>>>(K, N, Kp, Np, B, ldb, L, w, F, planesB);
+  if (w <= 104)
+    dd_split_right<8><<<g3, 256, 0, st>>>(K, N, Kp, Np, B, ldb, L, w, F, planesB);
+  else
+    dd_split_right<10><<<g3, 256, 0, st>>>(K, N, Kp, Np, B, ldb, L, w, F, planesB);
   VCPCU_LAUNCH_CHECK("dd_split_right");
   return VCPCU_OK;
 }
