@@ -257,3 +257,20 @@ def test_ozaki_host_pipeline_nonfinite_late_panel(cuda_lib, monkeypatch):
         _lib.call("vcpcu_igemm", m, n, k, hA.data_ptr(), hB.data_ptr(), hC.data_ptr(),
                   pidcuda.FORM_OZAKI, 0)
     assert np.all(np.isnan(hC.numpy()))
+
+
+def test_ozaki_host_pipeline_pageable(cuda_lib):
+    """The blocked host-pointer path with ordinary (pageable) numpy buffers:
+    the copies are staged, the result is the same bits as the device call."""
+    import torch
+    from vcp_gb300 import _lib
+    m, n, k = 300, 2300, 700
+    rng = np.random.default_rng(33)
+    A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
+    B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
+    C = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI)
+    dA = torch.from_numpy(A).cuda(); dB = torch.from_numpy(B).cuda()
+    dC = torch.zeros(2 * m * n, dtype=torch.float64, device="cuda")
+    pidcuda.mulmm_dev(m, n, k, dA, m, dB, k, dC, m, pidcuda.FORM_OZAKI, 0)
+    _lib.call("vcpcu_status", 0)
+    assert np.array_equal(bits(C), bits(dC.cpu().numpy()))
