@@ -27,7 +27,11 @@ Our arm (default) prints one JSON line with
                         the tightness of the returned bound;
                  point  up/down point GEMM (udmatmul shape), entries E(phi):
                         plain RU/RD FMA chains vs the Ozaki enclosure at
-                        slice counts s, width ratio and containment.
+                        slice counts s, width ratio and containment;
+                 lss    the verification of imats::linearsolve on the GPU
+                        (vcpcu_ilss_verify), n x n with nrhs right-hand
+                        sides (--phis carries nrhs): plain vs Ozaki time,
+                        width ratio, CPU restatement.
 --impl reference times that CPU path alone as the reference arm.
 
 Inputs are 1 GiB per operand (larger than the 129 MB L2), so no L2 flush is
@@ -67,7 +71,7 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=0, help="row sample of the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="interval",
-                    choices=["interval", "batch", "dd", "point"],
+                    choices=["interval", "batch", "dd", "point", "lss"],
                     help="interval: the headline line (default); the others print their own "
                          "line at the full sizes of that workload")
     ap.add_argument("--sizes", default="", help="point / dd: comma-separated n (or m:n:k)")
@@ -677,6 +681,63 @@ def bench_point(dev, stream, m, n, k, phi, slice_list, steps=2, plain=True, seed
     return out
 
 
+def bench_lss(dev, stream, n, nrhs=1, steps=2, plain_steps=1, seed=91, cpu_n=768):
+    """The verification of imats::linearsolve (vcpcu_ilss_verify) at n x n,
+    nrhs right-hand sides: A = I + U[-1,1]/sqrt(n) (well conditioned), b
+    U[-1,1], radii 2^-40 |mid|; R and mx formed on the device in FP64
+    (setup, untimed).  Time per verification (four interval products, the
+    norms, the enclosure), plain vs tensor-core form; the CPU leg is the
+    oracle's restatement of the same steps at cpu_n (its time scaled by
+    (n / cpu_n)^3, the R [A] product's share)."""
+    import torch
+    from vcp_gb300 import pidcuda
+    from oracle import oracle as O
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed + n)
+
+    def system(nn):
+        mid = torch.rand(nn, nn, generator=gen, device=dev, dtype=torch.float64) * 2 - 1
+        mid = mid / nn ** 0.5 + torch.eye(nn, device=dev, dtype=torch.float64)
+        bm = torch.rand(nn, nrhs, generator=gen, device=dev, dtype=torch.float64) * 2 - 1
+
+        def kv(m):
+            r = m.abs() * 2.0 ** -40
+            return torch.stack((m - r, m + r), dim=-1).transpose(0, 1).contiguous().reshape(-1)
+
+        R = torch.linalg.inv(mid)
+        mx = R @ bm
+        return (kv(mid), kv(bm), R.t().contiguous().reshape(-1),
+                mx.t().contiguous().reshape(-1))
+
+    A, b, R, mx = system(n)
+    x = torch.empty(2 * n * nrhs, dtype=torch.float64, device=dev)
+    G = torch.empty(1, dtype=torch.float64, device=dev)
+    out = {"n": n, "nrhs": nrhs}
+    res = {}
+    for name, form, st_ in (("plain", pidcuda.FORM_PLAIN, plain_steps),
+                            ("ozaki", pidcuda.FORM_OZAKI, steps)):
+        ms = time_stream(lambda: pidcuda.linearsolve_verify_dev(
+            n, nrhs, A, n, b, n, R, n, mx, n, x, n, G, form=form, stream=stream), stream, st_)
+        res[name] = (x.cpu().numpy(), float(G.cpu()[0]))
+        out[name] = {"ms": ms, "tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12,
+                     "bound_RA_minus_I": res[name][1]}
+    xp, xo = res["plain"][0], res["ozaki"][0]
+    wp, wo = xp[1::2] - xp[0::2], xo[1::2] - xo[0::2]
+    out["width_ozaki_vs_plain_median"] = float(np.median(wo / wp))
+    out["width_ozaki_vs_plain_max"] = float(np.max(wo / wp))
+    out["speedup_ozaki_vs_plain"] = out["plain"]["ms"] / out["ozaki"]["ms"]
+    # CPU: the restatement of the same steps at cpu_n, scaled by (n / cpu_n)^3
+    Ac, bc, Rc, mc = (t.cpu().numpy() for t in system(cpu_n))
+    t0 = time.perf_counter()
+    st, _, _ = O.ilss_verify(cpu_n, nrhs, Ac, bc, Rc, mc, threads=cpu_count())
+    dt = time.perf_counter() - t0
+    out["cpu_baseline"] = {"ms_scaled": dt * 1e3 * (n / cpu_n) ** 3, "ms_sample": dt * 1e3,
+                           "status": st, "cores": cpu_count(), "kind": "port",
+                           "sample": f"n = {cpu_n}, nrhs = {nrhs}, oracle restatement of "
+                                     f"imats::linearsolve's verification, time x (n/{cpu_n})^3"}
+    return out
+
+
 def parse_list(text, default, conv=int):
     return [conv(x) for x in text.split(",") if x] if text else default
 
@@ -692,6 +753,13 @@ def run_workload(args, dev, stream):
             res = bench_batch(dev, stream, steps=args.steps)
             metric, unit = "batched interval GEMM TFLOP/s (4096 uneven problems)", "TFLOP/s"
             value = res["ozaki"]["tflops"]
+        elif args.workload == "lss":
+            res = {"cases": [bench_lss(dev, stream, n, nrhs, steps=args.steps)
+                             for n in parse_list(args.sizes, [8192])
+                             for nrhs in parse_list(args.phis, [1])]}
+            metric, unit = ("verified linear solve, device-resident verification "
+                            "(imats::linearsolve after R, mx): ms"), "ms"
+            value = min(c["ozaki"]["ms"] for c in res["cases"])
         elif args.workload == "dd":
             res = {"cases": [bench_dd(dev, stream, n, phi, steps=args.steps)
                              for n in parse_list(args.sizes, [2048, 8192])
@@ -727,6 +795,7 @@ def bench_also(dev, stream):
     for key, fn in (("autotune", lambda: pidcuda.autotune(stream)),
                     ("batch", lambda: bench_batch(dev, stream, steps=1)),
                     ("dd", lambda: [bench_dd(dev, stream, 2048, phi, steps=2) for phi in (0, 16)]),
+                    ("lss", lambda: bench_lss(dev, stream, 2048, 1, steps=3)),
                     ("point", lambda: bench_point(dev, stream, 4096, 4096, 4096, 0, [6, 8],
                                                   steps=2))):
         t0 = time.perf_counter()

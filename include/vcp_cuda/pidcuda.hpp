@@ -4,11 +4,12 @@
 //     vcp::matrix< kv::interval<double>, vcp::pidcuda > A, B, C;
 //     C = A * B;                  // pidcuda::mulmm        (pidblas.hpp:239)
 //     C = ltransmul(A);           // pidcuda::mulltmm      (pidblas.hpp:296)
-//     x = lss(A, b);              // imats::linearsolve -> mul_im_m / mul_m_im
+//     x = lss(A, b);              // pidcuda::linearsolve -> vcpcu_ilss_verify
 //     vcp::matrix< kv::interval<double>, vcp::pidcuda_fma > F;  // pidblas_fma drop-in
 // The class derives from vcp::imats<double, vcp::pdblas> as pidblas does, so
-// every imats algorithm (linearsolve, eigsym, eigsymge) routes its interval
-// products through the hooks below to libvcpcuda (include/vcpcuda.h).
+// every imats algorithm (eigsym, eigsymge, ...) routes its interval products
+// through the hooks below to libvcpcuda (include/vcpcuda.h); linearsolve is
+// replaced by a version whose whole verification stays on the GPU.
 //
 // Form and precision are process-wide settings:
 //     vcp::pidcuda_settings::form()   = VCPCU_FORM_OZAKI;   // default
@@ -20,6 +21,8 @@
 // (vcp/error.hpp).  Scalar ('S') operands keep the host shortcuts of pidblas.
 #ifndef VCP_CUDA_PIDCUDA_HPP
 #define VCP_CUDA_PIDCUDA_HPP
+
+#include <iostream>
 
 #include <kv/interval.hpp>
 #include <vcp/error.hpp>
@@ -129,6 +132,42 @@ class pidcuda : public vcp::imats<double, vcp::pdblas> {
                     pidcuda_detail::cd(B.v), pidcuda_detail::md(c.v), pidcuda_settings::form(),
                     pidcuda_settings::slices()),
         "pidcuda::mulmm");
+  }
+  // x = A \ b, verified (imats::linearsolve, vcp/imats.hpp:293-364).  R =
+  // inv(mid A) and mx = R mid(b) are formed on the host as the reference
+  // forms them (pdblas: LAPACK inverse, BLAS product); the verification --
+  // four interval products, the norms and the enclosure -- runs on the GPU
+  // in one call without host round trips (vcpcu_ilss_verify).  Found by
+  // name from vcp::matrix's lss() (vcp/matrix.hpp:607-634) in place of the
+  // base class's; n = 1 keeps the reference's scalar path.
+  void linearsolve(base& b, base& x) {
+    if (this->row != this->column || b.row != this->row)
+      vcp::throw_error<vcp::dimension_error>("linearsolve: invalid dimensions: A=(", this->row,
+                                             ", ", this->column, "), b=(", b.row, ", ",
+                                             b.column, ")");
+    if (this->row < 2) {
+      base::linearsolve(b, x);
+      return;
+    }
+    vcp::pdblas mx, mb, R;
+    this->imid(R);
+    mb.zeros(b.row, b.column);
+    for (int i = 0; i < b.n; i++) mb.v[i] = mid(b.v[i]);
+    R.inv();
+    R.mulmm(mb, mx);
+    mb.clear();
+    x.zeros(b.row, b.column);
+    double G = 0.0;
+    const int st = vcpcu_ilss_verify(this->row, b.column, pidcuda_detail::cd(this->v),
+                                     pidcuda_detail::cd(b.v), R.v.data(), mx.v.data(),
+                                     pidcuda_detail::md(x.v), &G, pidcuda_settings::form(),
+                                     pidcuda_settings::slices());
+    if (st == VCPCU_OK || st == VCPCU_ERR_VERIFY)
+      std::cout << "Linear solver Check || I - RA || < 1: " << G << " < 1 ?" << std::endl;
+    if (st == VCPCU_ERR_VERIFY)
+      vcp::throw_error<vcp::verification_error>("linearsolve verification failed: ||RA - I|| <= ",
+                                                G);
+    pidcuda_detail::check(st, "pidcuda::linearsolve");
   }
   // C = [A]^T [A] (pidblas::mulltmm)
   void mulltmm(vcp::mats<kv::interval<double> >& c) const override {

@@ -35,6 +35,7 @@ extern "C" {
 #define VCPCU_ERR_TIMEOUT      5  /* a bounded device-side wait gave up              */
 #define VCPCU_ERR_UNSUPPORTED  6  /* no usable sm_103 device, or option not built    */
 #define VCPCU_ERR_ALLOC        7  /* device or pinned host allocation failed         */
+#define VCPCU_ERR_VERIFY       8  /* a verification condition failed (||RA - I|| >= 1) */
 
 /* rounding_mode values, identical to vblas rmatmul (vblas/rmatmul.hpp:100-102) */
 #define VCPCU_ROUND_UP      1
@@ -209,6 +210,29 @@ int vcpcu_norm_I_minus_RA_dev(int n, const double* R, int ldr, const double* A,
                               void* stream);
 int vcpcu_norm_I_minus_RA(int n, const double* R, const double* A, double* bound,
                           int form, int slices);
+
+/* The verification of imats::linearsolve (vcp/imats.hpp:293-364) once its
+ * approximate inverse R = inv(mid [A]) and approximate solution
+ * mx = R mid([b]) are formed (the reference forms both on the host: LAPACK
+ * inverse, BLAS product, :299-302).  A is n x n interval, b and x n x nrhs
+ * interval, R n x n point, mx n x nrhs point, all column-major (kv layout
+ * for intervals).  Steps, each with the reference's kv arithmetic:
+ *   P = [A] mx - [b];  r = R P;  E = R [A] - I;  G = ||E||_inf (upper);
+ *   t = || |r| ||_inf;  g = [t, t] / (1 - [G, G]);
+ *   H = |E| (g ... g);  x = mx + [-u, u] with u = sup|r| + sup H (upward).
+ * R[A] runs in `form`; the three products with nrhs columns run in the
+ * plain form when nrhs <= 4 (a thin FP64 kernel), else in `form` too.  In
+ * the plain form every bit of x and G equals the reference's (for n >= 2:
+ * with n = 1 the reference takes its scalar shortcuts).  *bound receives G;
+ * the reference throws vcp::verification_error when G >= 1 (x is then
+ * meaningless): the host form returns VCPCU_ERR_VERIFY in that case, the
+ * _dev form leaves the test to the caller (*bound in device memory).
+ * Inputs must be finite. */
+int vcpcu_ilss_verify_dev(int n, int nrhs, const double* A, int lda, const double* b, int ldb,
+                          const double* R, int ldr, const double* mx, int ldmx, double* x,
+                          int ldx, double* bound, int form, int slices, void* stream);
+int vcpcu_ilss_verify(int n, int nrhs, const double* A, const double* b, const double* R,
+                      const double* mx, double* x, double* bound, int form, int slices);
 
 /* ---- inf-sup interval FMA (vcp/ifma.hpp, vcp/pidblas_fma.hpp) ------------- */
 

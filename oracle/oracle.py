@@ -48,6 +48,8 @@ def lib() -> C.CDLL:
         L.orc_pidblas_vmulmm.restype = _i
         L.orc_norm_I_minus_RA.argtypes = [_i, _v, _v, _i]
         L.orc_norm_I_minus_RA.restype = C.c_double
+        L.orc_ilss_verify.argtypes = [_i, _i, _v, _v, _v, _v, _v, _v, _v, _i]
+        L.orc_ilss_verify.restype = _i
         _lib = L
     return _lib
 
@@ -71,6 +73,8 @@ def ref_lib() -> C.CDLL | None:
         R.ref_pidblas_fma_mulmm.argtypes = [_i, _i, _i, _v, _v, _v]
         R.ref_pidblas_fma_mulmm.restype = _i
         R.ref_norm_I_minus_RA.restype = _i
+        R.ref_imats_linearsolve.argtypes = [_i, _i, _v, _v, _v, _v, _v]
+        R.ref_imats_linearsolve.restype = _i
         _ref = R
     return _ref
 
@@ -168,6 +172,31 @@ def pidblas_vmulmm(n, k, A, threads=0):
 
 def norm_I_minus_RA(n, R, A, threads=0) -> float:
     return float(lib().orc_norm_I_minus_RA(n, _p(R), _p(A), threads))
+
+
+def ilss_verify(n, nrhs, A, b, R, mx, E=None, threads=0):
+    """imats::linearsolve's verification (restatement) for given R, mx:
+    (status, x kv buffer, G); status 2 when G >= 1.  E (kv, n x n) replaces
+    the product R [A] when given."""
+    x = np.zeros(2 * n * nrhs)
+    g = np.zeros(1)
+    st = lib().orc_ilss_verify(n, nrhs, _p(A), _p(b), _p(R), _p(mx),
+                               None if E is None else _p(E), _p(x), _p(g), int(threads))
+    return int(st), x, float(g[0])
+
+
+def ref_imats_linearsolve(n, nrhs, A, b):
+    """The reference's imats<double, pidblas>::linearsolve run as is:
+    (status, x, R, mx) with R, mx the approximate inverse and solution it
+    used; None where the reference build is absent."""
+    Rl = ref_lib()
+    if Rl is None:
+        return None
+    x = np.zeros(2 * n * nrhs)
+    R = np.zeros(n * n)
+    mx = np.zeros(n * nrhs)
+    st = Rl.ref_imats_linearsolve(n, nrhs, _p(A), _p(b), _p(x), _p(R), _p(mx))
+    return int(st), x, R, mx
 
 
 def ifma(A, B, C_) -> np.ndarray:

@@ -10,8 +10,11 @@
 // the Fortran BLAS symbol dgemm_; this file provides dgemm_ (and ddot_,
 // dgemv_, dsyrk_) on top of the reference rmatmul with the direction taken
 // from the calling thread's current rounding mode, which is what pidblas sets
-// through kv::hwround before each call (vcp/pidblas.hpp:264-281).
+// through kv::hwround before each call (vcp/pidblas.hpp:264-281), and
+// dgetrf_ / dgetri_ (a plain LU) for the inverse of imats::linearsolve.
+#include <algorithm>
 #include <cfenv>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -79,12 +82,60 @@ void dsyrk_(char* uplo, char* trans, int* n, int* k, double* alpha, const double
     for (int i = 0; i <= j; ++i) C[i + (size_t)j * (*ldc)] = full[i + (size_t)j * (*n)];
 }
 
-// LAPACK and the remaining BLAS routines are referenced by pdblas's solver
+// The approximate inverse R = inv(mid A) of imats::linearsolve
+// (vcp/imats.hpp:299-300) comes from pdblas::inv (vcp/pdblas.hpp:180-205):
+// dgetrf_ then dgetri_.  LAPACK is absent here; these two are a
+// project-written LU with partial pivoting (first largest pivot) and the
+// inverse by forward / back substitution of the unit columns, under the
+// caller's rounding mode.  Any approximate inverse serves the verification;
+// the same R is handed to the GPU path, so results are compared on equal R.
+void dgetrf_(int* m, int* n, double* A, int* lda, int* ipiv, int* info) {
+  const int M = *m, N = *n, ld = *lda;
+  *info = 0;
+  for (int j = 0; j < (M < N ? M : N); ++j) {
+    int p = j;
+    for (int i = j + 1; i < M; ++i)
+      if (std::fabs(A[i + (long)j * ld]) > std::fabs(A[p + (long)j * ld])) p = i;
+    ipiv[j] = p + 1;
+    if (A[p + (long)j * ld] == 0.0) {
+      if (*info == 0) *info = j + 1;
+      continue;
+    }
+    if (p != j)
+      for (int c = 0; c < N; ++c) std::swap(A[j + (long)c * ld], A[p + (long)c * ld]);
+    for (int i = j + 1; i < M; ++i) A[i + (long)j * ld] /= A[j + (long)j * ld];
+    for (int c = j + 1; c < N; ++c)
+      for (int i = j + 1; i < M; ++i) A[i + (long)c * ld] -= A[i + (long)j * ld] * A[j + (long)c * ld];
+  }
+}
+
+void dgetri_(int* n, double* A, int* lda, int* ipiv, double* work, int* lwork, int* info) {
+  const int N = *n, ld = *lda;
+  *info = 0;
+  if (*lwork == -1) {  // workspace query
+    work[0] = N > 0 ? N : 1;
+    return;
+  }
+  std::vector<double> X((size_t)N * N, 0.0), e(N);
+  for (int c = 0; c < N; ++c) {
+    for (int i = 0; i < N; ++i) e[i] = i == c ? 1.0 : 0.0;
+    for (int j = 0; j < N; ++j) std::swap(e[j], e[ipiv[j] - 1]);  // P e
+    for (int i = 0; i < N; ++i)                                   // L y = P e
+      for (int j = 0; j < i; ++j) e[i] -= A[i + (long)j * ld] * e[j];
+    for (int i = N - 1; i >= 0; --i) {                            // U x = y
+      for (int j = i + 1; j < N; ++j) e[i] -= A[i + (long)j * ld] * e[j];
+      e[i] /= A[i + (long)i * ld];
+    }
+    for (int i = 0; i < N; ++i) X[i + (size_t)c * N] = e[i];
+  }
+  for (int c = 0; c < N; ++c)
+    for (int i = 0; i < N; ++i) A[i + (long)c * ld] = X[i + (size_t)c * N];
+}
+
+// The remaining LAPACK / BLAS routines are referenced by pdblas's solver
 // members (vcp/pdblas.hpp:159-376), which are off the GEMM path: they abort.
 void dsymm_(char*, char*, int*, int*, double*, const double*, int*, const double*, int*, double*,
             double*, int*) { unsupported("dsymm_"); }
-void dgetrf_(int*, int*, double*, int*, int*, int*) { unsupported("dgetrf_"); }
-void dgetri_(int*, double*, int*, int*, double*, int*, int*) { unsupported("dgetri_"); }
 void dsyev_(char*, char*, int*, double*, int*, double*, double*, int*, int*) { unsupported("dsyev_"); }
 void dgesv_(int*, int*, double*, int*, int*, double*, int*, int*) { unsupported("dgesv_"); }
 void dsygv_(int*, char*, char*, int*, double*, int*, double*, int*, double*, double*, int*, int*) {
@@ -127,6 +178,10 @@ struct pidblas_open : vcp::pidblas {
   using vcp::pidblas::mul_im_m;
   using vcp::pidblas::mul_m_im;
   using vcp::pidblas::vmulmm;
+  using vcp::pidblas::imid;
+};
+struct imats_open : vcp::imats<double, vcp::pdblas> {
+  using vcp::imats<double, vcp::pdblas>::imid;
 };
 typedef kv::interval<double> I;
 void fill_iv(vcp::mats<I>& X, int r, int c, const double* kvp) {
@@ -213,6 +268,36 @@ int ref_norm_I_minus_RA(int n, const double* R, const double* A, double* bound) 
     b.norminf(g);
     *bound = g.v[0].upper();
     return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// imats<double, pidblas>::linearsolve (vcp/imats.hpp:293-364), run as is: x
+// (n x nrhs, kv layout).  R and mx receive the approximate inverse and
+// solution it works with, formed the same way (imid, pdblas::inv,
+// pdblas::mulmm; :299-302).  Returns 0, 2 when the reference throws
+// vcp::verification_error (||RA - I|| >= 1), 1 on any other exception.
+int ref_imats_linearsolve(int n, int nrhs, const double* A, const double* b, double* x,
+                          double* R, double* mx) {
+  try {
+    pidblas_open a;
+    fill_iv(a, n, n, A);
+    imats_open bb;
+    fill_iv(bb, n, nrhs, b);
+    vcp::pdblas Rm, mb, mxm;
+    a.imid(Rm);
+    bb.imid(mb);
+    Rm.inv();
+    Rm.mulmm(mb, mxm);
+    for (long t = 0; t < (long)n * n; ++t) R[t] = Rm.v[t];
+    for (long t = 0; t < (long)n * nrhs; ++t) mx[t] = mxm.v[t];
+    vcp::imats<double, vcp::pdblas> xx;
+    a.linearsolve(bb, xx);
+    out_iv(xx, x);
+    return 0;
+  } catch (vcp::verification_error&) {
+    return 2;
   } catch (...) {
     return 1;
   }

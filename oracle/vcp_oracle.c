@@ -23,6 +23,10 @@
  *   orc_pidblas_mulmm
  *       pidblas::mulmm (vcp/pidblas.hpp:239-294) with orc_rmatmul as its
  *       dgemm_, in the reference's exact operation order.
+ *   orc_ilss_verify
+ *       the verification of imats::linearsolve (vcp/imats.hpp:293-364) for a
+ *       given approximate inverse R and solution mx, step by step with the
+ *       reference's pidblas products and kv interval operations.
  *   orc_exact_hull / orc_exact_dot
  *       exact long-accumulator dot products (a Kulisch-style fixed-point
  *       accumulator over the whole binary64 product range) rounded down/up
@@ -636,6 +640,130 @@ double orc_norm_I_minus_RA(int n, const double* R, const double* A, int nthreads
   fesetround(prev);
   free(b);
   return g;
+}
+
+/* ---------------------------------------------------------------------------
+ * imats::linearsolve's verification (vcp/imats.hpp:293-364) given its
+ * approximate inverse R of mid(A) and approximate solution mx = R mid(b).
+ * A n x n, b n x nrhs kv intervals; R, mx point; x n x nrhs kv.  Steps and
+ * the kv operations they use (kv interval arithmetic as in the kv stand-in:
+ * outward-rounded endpoints, abs, max of upper ends in std::max order):
+ *   P = [A] mx        pidblas::mul_im_m                         :305
+ *   P = P - [b]       subsmmA, [RD(P.lo - b.up), RU(P.up - b.lo)] :307
+ *   r = R P           pidblas::mul_m_im                         :309
+ *   E = R [A]         pidblas::mul_m_im; E(i,i) -= 1             :317-326
+ *   G = sup ||E||_inf mats::norminf (row sums of sup|E| upward)   :329
+ *   t = sup || |r| ||_inf (vector: largest sup|r|; matrix: rows)  :336
+ *   g = [t,t] / (1 - [G,G])                                      :341
+ *   H = |E| (g ... g) pidblas::mulmm                              :353
+ *   x = mx + [-u, u], u = RU(sup|r| + sup H)                       :355-363
+ * E_in (kv, n x n), when given, replaces the product R [A] (so that the
+ * steps can be checked on the tensor-core form's R [A]).  Returns 0, or 2
+ * when G >= 1 (the reference throws vcp::verification_error; x untouched).
+ * ------------------------------------------------------------------------- */
+static double rnd_op(int mode, double a, double b, char op) {
+  volatile double va = a, vb = b;
+  const int prev = fegetround();
+  fesetround(mode);
+  volatile double r = op == '+' ? va + vb : op == '-' ? va - vb : va / vb;
+  fesetround(prev);
+  return r;
+}
+static double kv_abs_sup(double lo, double up) {
+  if (lo >= 0.0) return up;
+  if (up <= 0.0) return -lo;
+  return (-lo < up) ? up : -lo;
+}
+/* sup of mats::norminf over an interval matrix (rows x cols, kv, ld = rows) */
+static double norminf_sup(int rows, int cols, const double* X) {
+  const int mat = rows > 1 && cols > 1;
+  double c = 0.0;
+  if (!mat) {  /* 'S', 'C', 'R': the largest |x| */
+    const long cnt = (long)rows * cols;
+    c = kv_abs_sup(X[0], X[1]);
+    for (long i = 1; i < cnt; ++i) {
+      const double a = kv_abs_sup(X[2 * i], X[2 * i + 1]);
+      c = (a < c) ? c : a;
+    }
+    return c;
+  }
+  for (int i = 0; i < rows; ++i) {
+    double s = kv_abs_sup(X[2 * i], X[2 * i + 1]);
+    for (int j = 1; j < cols; ++j) {
+      const long o = i + (long)j * rows;
+      s = rnd_op(FE_UPWARD, s, kv_abs_sup(X[2 * o], X[2 * o + 1]), '+');
+    }
+    c = (i == 0) ? s : ((s < c) ? c : s);
+  }
+  return c;
+}
+
+int orc_ilss_verify(int n, int nrhs, const double* A, const double* b, const double* R,
+                    const double* mx, const double* E_in, double* x, double* bound,
+                    int nthreads) {
+  const long nv = (long)n * nrhs, nn = (long)n * n;
+  double* buf = (double*)malloc(sizeof(double) * (2 * nn + 8 * nv + 2));
+  if (!buf) return 1;
+  double *E = buf, *P = E + 2 * nn, *r = P + 2 * nv, *T = r + 2 * nv, *H = T + 2 * nv;
+  orc_pidblas_mul_point(0, n, nrhs, n, A, mx, P, nthreads);
+  for (long i = 0; i < nv; ++i) {
+    const double lo = rnd_op(FE_DOWNWARD, P[2 * i], b[2 * i + 1], '-');
+    const double up = rnd_op(FE_UPWARD, P[2 * i + 1], b[2 * i], '-');
+    P[2 * i] = lo;
+    P[2 * i + 1] = up;
+  }
+  orc_pidblas_mul_point(1, n, nrhs, n, R, P, r, nthreads);
+  if (E_in)
+    memcpy(E, E_in, sizeof(double) * 2 * nn);
+  else
+    orc_pidblas_mul_point(1, n, n, n, R, A, E, nthreads);
+  for (int i = 0; i < n; ++i) {
+    const long o = i + (long)i * n;
+    const double lo = rnd_op(FE_DOWNWARD, E[2 * o], 1.0, '-');
+    const double up = rnd_op(FE_UPWARD, E[2 * o + 1], 1.0, '-');
+    E[2 * o] = lo;
+    E[2 * o + 1] = up;
+  }
+  const double G = norminf_sup(n, n, E);
+  *bound = G;
+  if (G >= 1.0) {
+    free(buf);
+    return 2;
+  }
+  const double t = norminf_sup(n, nrhs, r);
+  const double d_lo = rnd_op(FE_DOWNWARD, 1.0, G, '-'), d_up = rnd_op(FE_UPWARD, 1.0, G, '-');
+  const double q[4] = {rnd_op(FE_DOWNWARD, t, d_lo, '/'), rnd_op(FE_DOWNWARD, t, d_up, '/'),
+                       rnd_op(FE_DOWNWARD, t, d_lo, '/'), rnd_op(FE_DOWNWARD, t, d_up, '/')};
+  const double u4[4] = {rnd_op(FE_UPWARD, t, d_lo, '/'), rnd_op(FE_UPWARD, t, d_up, '/'),
+                        rnd_op(FE_UPWARD, t, d_lo, '/'), rnd_op(FE_UPWARD, t, d_up, '/')};
+  double g_lo = q[0], g_up = u4[0];
+  for (int c = 1; c < 4; ++c) {
+    if (q[c] < g_lo) g_lo = q[c];
+    if (g_up < u4[c]) g_up = u4[c];
+  }
+  for (long i = 0; i < nn; ++i) {  /* E -> kv abs(E) */
+    const double lo = E[2 * i], up = E[2 * i + 1];
+    if (lo >= 0.0) continue;
+    if (up <= 0.0) {
+      E[2 * i] = -up;
+      E[2 * i + 1] = -lo;
+    } else {
+      E[2 * i] = 0.0;
+      E[2 * i + 1] = (-lo < up) ? up : -lo;
+    }
+  }
+  for (long i = 0; i < nv; ++i) {
+    T[2 * i] = g_lo;
+    T[2 * i + 1] = g_up;
+  }
+  orc_pidblas_mulmm(n, nrhs, n, E, T, H, nthreads);
+  for (long i = 0; i < nv; ++i) {
+    const double u = rnd_op(FE_UPWARD, kv_abs_sup(r[2 * i], r[2 * i + 1]), H[2 * i + 1], '+');
+    x[2 * i] = rnd_op(FE_DOWNWARD, -u, mx[i], '+');
+    x[2 * i + 1] = rnd_op(FE_UPWARD, u, mx[i], '+');
+  }
+  free(buf);
+  return 0;
 }
 
 /* ---------------------------------------------------------------------------

@@ -116,6 +116,26 @@ def main() -> None:
         assert O.ref_lib().ref_pidblas_fma_mulmm(m, n, k, O._p(A), O._p(B), O._p(C_)) == 0
         data[f"fm{idx}_shape"] = np.array([m, n, k])
         data[f"fm{idx}_A"], data[f"fm{idx}_B"], data[f"fm{idx}_C"] = A, B, C_
+    # imats<double, pidblas>::linearsolve (own seed again): inputs, the R and
+    # mx it works with, its enclosure x and the bound ||RA - I||; the last
+    # case fails the check (the reference throws, status 2)
+    rng3 = np.random.default_rng(20261205)
+    lcases = [(2, 1, 2.0 ** -30), (16, 1, 2.0 ** -30), (33, 3, 2.0 ** -24), (48, 1, 2.0 ** -40),
+              (64, 5, 2.0 ** -30), (8, 1, 0.5)]
+    for idx, (n, nrhs, rel) in enumerate(lcases):
+        Am = rng3.uniform(-1.0, 1.0, (n, n)) + (2.0 if rel > 0.1 else 4.0) * np.eye(n)
+        A = W._kv(Am.ravel(order="F"), np.abs(Am.ravel(order="F")) * rel)
+        bm = rng3.uniform(-1.0, 1.0, n * nrhs)
+        b = W._kv(bm, np.abs(bm) * 2.0 ** -35)
+        st, x, R, mx = O.ref_imats_linearsolve(n, nrhs, A, b)
+        g = ctypes.c_double(0.0)
+        assert O.ref_call("ref_norm_I_minus_RA", n, O._p(R), O._p(A), ctypes.addressof(g)) == 0
+        data[f"ls{idx}_shape"] = np.array([n, nrhs])
+        data[f"ls{idx}_A"], data[f"ls{idx}_b"] = A, b
+        data[f"ls{idx}_R"], data[f"ls{idx}_mx"], data[f"ls{idx}_x"] = R, mx, x
+        data[f"ls{idx}_status"] = np.array([st])
+        data[f"ls{idx}_bound"] = np.array([g.value])
+    data["n_ls"] = np.array([len(lcases)])
     data["n_fm"] = np.array([len(fcases)])
     data["n_mp"] = np.array([len(pcases)])
     data["n_sy"] = np.array([2])

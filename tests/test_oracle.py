@@ -247,3 +247,67 @@ def test_ifma_oracle_vs_reference_build(oracle):
     assert R.ref_pidblas_fma_mulmm(m, nn, k, oracle._p(A), oracle._p(B), oracle._p(ref)) == 0
     assert np.array_equal(oracle.pidblas_fma_mulmm(m, nn, k, A, B).view(np.int64),
                           ref.view(np.int64))
+
+
+def _lss_case(rng, n, nrhs, rel, shift=4.0):
+    Am = rng.uniform(-1.0, 1.0, (n, n)) + shift * np.eye(n)
+    A = W._kv(Am.ravel(order="F"), np.abs(Am.ravel(order="F")) * rel)
+    bm = rng.uniform(-1.0, 1.0, n * nrhs)
+    return A, W._kv(bm, np.abs(bm) * 2.0 ** -35)
+
+
+def test_oracle_linearsolve_matches_golden(oracle, golden):
+    """imats::linearsolve's verification (restated) on the reference's own
+    R, mx: every bit of x, the bound, and the failing check."""
+    for idx in range(int(golden["n_ls"][0])):
+        n, nrhs = map(int, golden[f"ls{idx}_shape"])
+        st, x, G = oracle.ilss_verify(n, nrhs, golden[f"ls{idx}_A"], golden[f"ls{idx}_b"],
+                                      golden[f"ls{idx}_R"], golden[f"ls{idx}_mx"])
+        assert st == int(golden[f"ls{idx}_status"][0]), idx
+        assert G == float(golden[f"ls{idx}_bound"][0]), idx
+        if st == 0:
+            assert np.array_equal(bits(x), bits(golden[f"ls{idx}_x"])), idx
+
+
+def test_oracle_linearsolve_matches_reference_build(oracle):
+    """Live: the reference's imats<double, pidblas>::linearsolve (LU shim for
+    its LAPACK inverse) against the restatement on the R, mx it used."""
+    if oracle.ref_lib() is None:
+        from oracle.build import build_reference
+        if build_reference() is None:
+            pytest.skip("reference sources not mounted")
+    rng = np.random.default_rng(31)
+    for n, nrhs, rel in [(2, 1, 2.0 ** -30), (3, 2, 2.0 ** -30), (17, 3, 2.0 ** -20),
+                         (40, 1, 2.0 ** -44), (65, 6, 2.0 ** -30), (9, 1, 0.4)]:
+        A, b = _lss_case(rng, n, nrhs, rel, 2.0 if rel > 0.1 else 4.0)
+        st, xr, R, mx = oracle.ref_imats_linearsolve(n, nrhs, A, b)
+        st2, xo, G = oracle.ilss_verify(n, nrhs, A, b, R, mx)
+        assert st == st2, (n, nrhs)
+        if st == 0:
+            assert np.array_equal(bits(xo), bits(xr)), (n, nrhs)
+    # an exact point system: the enclosure holds the rational solution
+    n = 6
+    M = np.round(rng.uniform(-5, 5, (n, n))) + 20 * np.eye(n)
+    bb = np.round(rng.uniform(-5, 5, n))
+    A = W._kv(M.ravel(order="F"), np.zeros(n * n))
+    b = W._kv(bb, np.zeros(n))
+    st, xr, R, mx = oracle.ref_imats_linearsolve(n, 1, A, b)
+    assert st == 0
+    exact = _rational_solve(M, bb)
+    for i in range(n):
+        assert Fraction(xr[2 * i]) <= exact[i] <= Fraction(xr[2 * i + 1])
+
+
+def _rational_solve(M, b):
+    """Exact solution of M x = b (integer entries) by Gaussian elimination
+    over the rationals."""
+    n = len(b)
+    a = [[Fraction(int(M[i, j])) for j in range(n)] + [Fraction(int(b[i]))] for i in range(n)]
+    for c in range(n):
+        p = next(r for r in range(c, n) if a[r][c] != 0)
+        a[c], a[p] = a[p], a[c]
+        for r in range(n):
+            if r != c and a[r][c] != 0:
+                f = a[r][c] / a[c][c]
+                a[r] = [x - f * y for x, y in zip(a[r], a[c])]
+    return [a[i][n] / a[i][i] for i in range(n)]

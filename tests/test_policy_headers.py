@@ -23,20 +23,29 @@ PROGRAM = r'''
 #include <vcp_cuda/pidcuda.hpp>
 #include <vcp_cuda/rmatmul_cuda.hpp>
 
-// Fortran BLAS/LAPACK symbols pdblas references; never reached here.
+// Fortran BLAS/LAPACK symbols pdblas references.  linearsolve forms R and
+// mx on the host before its GPU call: these stubs give it some R and mx (an
+// identity "inverse", a zero product); the rest are never reached.
 extern "C" {
-void dgemm_(char*, char*, int*, int*, int*, double*, const double*, int*, const double*, int*,
-            double*, double*, int*) { std::abort(); }
+void dgemm_(char*, char*, int* m, int* n, int*, double*, const double*, int*, const double*,
+            int*, double*, double* C, int*) {
+  for (int i = 0; i < *m * *n; ++i) C[i] = 0.0;
+}
 double ddot_(int*, const double*, int*, const double*, int*) { std::abort(); }
-void dgemv_(char*, int*, int*, double*, const double*, int*, const double*, int*, double*,
-            double*, int*) { std::abort(); }
+void dgemv_(char*, int* m, int*, double*, const double*, int*, const double*, int*, double*,
+            double* y, int*) {
+  for (int i = 0; i < *m; ++i) y[i] = 0.0;
+}
 void dsyrk_(char*, char*, int*, int*, double*, const double*, int*, double*, double*, int*) {
   std::abort();
 }
 void dsymm_(char*, char*, int*, int*, double*, const double*, int*, const double*, int*,
             double*, double*, int*) { std::abort(); }
-void dgetrf_(int*, int*, double*, int*, int*, int*) { std::abort(); }
-void dgetri_(int*, double*, int*, int*, double*, int*, int*) { std::abort(); }
+void dgetrf_(int*, int*, double*, int*, int*, int* info) { *info = 0; }
+void dgetri_(int* n, double*, int*, int*, double* work, int* lwork, int* info) {
+  if (*lwork == -1) work[0] = *n;
+  *info = 0;
+}
 void dsyev_(char*, char*, int*, double*, int*, double*, double*, int*, int*) { std::abort(); }
 void dgesv_(int*, int*, double*, int*, int*, double*, int*, int*) { std::abort(); }
 void dsygv_(int*, char*, char*, int*, double*, int*, double*, int*, double*, double*, int*,
@@ -48,7 +57,7 @@ typedef kv::interval<double> I;
 typedef vcp::matrix<I, vcp::pidcuda> M;
 typedef vcp::matrix<I, vcp::pidcuda_fma> MF;
 
-int main(int argc, char**) {
+int main() {
   M A, B, C;
   A.zeros(4, 3);
   B.zeros(3, 5);
@@ -79,11 +88,17 @@ int main(int argc, char**) {
     std::printf("STATE_ERROR mulmm_fma: %s\n", e.what());
     ++errors;
   }
-  if (argc > 99) {  // never run: instantiates imats::linearsolve over the pidcuda hooks
-    M S;
+  try {
+    M S, b1;
     S.zeros(3, 3);
-    M x = lss(S, B);
+    b1.zeros(3, 1);
+    for (int i = 0; i < 3; ++i) S.data()[4 * i] = I(2.0, 2.5);
+    M x = lss(S, b1);                     // pidcuda::linearsolve -> vcpcu_ilss_verify
     (void)x;
+    std::printf("NO_ERROR lss\n");
+  } catch (vcp::state_error& e) {
+    std::printf("STATE_ERROR lss: %s\n", e.what());
+    ++errors;
   }
   std::fflush(stdout);
   double a[4] = {1, 2, 3, 4}, b[4] = {1, 0, 0, 1}, c[4];
@@ -94,7 +109,7 @@ int main(int argc, char**) {
     std::printf("RUNTIME_ERROR rmatmul: %s\n", e.what());
     ++errors;
   }
-  return errors == 4 ? 0 : 1;
+  return errors == 5 ? 0 : 1;
 }
 '''
 
@@ -121,6 +136,7 @@ def test_policy_headers_compile_link_and_map_errors(tmp_path, cuda_lib):
     assert run.returncode == 0, run.stdout + run.stderr
     assert "STATE_ERROR mulmm" in run.stdout and "STATE_ERROR mulltmm" in run.stdout
     assert "STATE_ERROR mulmm_fma" in run.stdout
+    assert "STATE_ERROR lss" in run.stdout
     assert "RUNTIME_ERROR rmatmul" in run.stdout
 
 

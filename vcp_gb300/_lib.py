@@ -40,6 +40,9 @@ SIGNATURES: dict[str, tuple] = {
     "vcpcu_vsyrk": (_i, [_i, _i, _v, _v]),
     "vcpcu_norm_I_minus_RA_dev": (_i, [_i, _v, _i, _v, _i, _v, _i, _i, _v]),
     "vcpcu_norm_I_minus_RA": (_i, [_i, _v, _v, _v, _i, _i]),
+    "vcpcu_ilss_verify_dev": (_i, [_i, _i, _v, _i, _v, _i, _v, _i, _v, _i, _v, _i, _v, _i, _i,
+                                   _v]),
+    "vcpcu_ilss_verify": (_i, [_i, _i, _v, _v, _v, _v, _v, _v, _i, _i]),
     "vcpcu_ddgemm_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _v, _i, _i, _v]),
     "vcpcu_ddgemm": (_i, [_i, _i, _i, _v, _v, _v, _v, _i]),
     "vcpcu_udmatmul_ozaki_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _v, _i, _i, _v]),

@@ -612,6 +612,63 @@ int vcpcu_norm_I_minus_RA(int n, const double* R, const double* A, double* bound
   return form != VCPCU_FORM_PLAIN ? take_status() : VCPCU_OK;
 }
 
+int vcpcu_ilss_verify_dev(int n, int nrhs, const double* A, int lda, const double* b, int ldb,
+                          const double* R, int ldr, const double* mx, int ldmx, double* x,
+                          int ldx, double* bound, int form, int slices, void* stream) {
+  clear_error();
+  int st = form_check(form, slices);
+  if (st) return st;
+  if (n <= 0 || nrhs <= 0 || !A || !b || !R || !mx || !x || !bound || lda < n || ldb < n ||
+      ldr < n || ldmx < n || ldx < n) {
+    set_error("ilss_verify: n, nrhs must be positive, pointers non-null, ld >= n");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (form != VCPCU_FORM_PLAIN && (misaligned16(A) || misaligned16(b))) {
+    set_error("ilss_verify: A and b must be 16-byte aligned for the Ozaki form");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  return ilss_verify_dispatch(n, nrhs, A, lda, b, ldb, R, ldr, mx, ldmx, x, ldx, bound, form,
+                              slices, (cudaStream_t)stream);
+}
+
+int vcpcu_ilss_verify(int n, int nrhs, const double* A, const double* b, const double* R,
+                      const double* mx, double* x, double* bound, int form, int slices) {
+  clear_error();
+  int st = form_check(form, slices);
+  if (st) return st;
+  if (n <= 0 || nrhs <= 0 || !A || !b || !R || !mx || !x || !bound) {
+    set_error("ilss_verify: n, nrhs must be positive and pointers non-null");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  cudaStream_t s = host_stream();
+  const size_t na = 2 * (size_t)n * n, nv = 2 * (size_t)n * nrhs, nr = (size_t)n * n,
+               nm = (size_t)n * nrhs;
+  Scratch buf;
+  if ((st = buf.alloc(sizeof(double) * (na + 2 * nv + nr + nm + 2), s))) return st;
+  double* dA = (double*)buf.ptr;  // interval arrays first: 16-byte aligned
+  double* db = dA + na;
+  double* dx = db + nv;
+  double* dR = dx + nv;
+  double* dm = dR + nr;
+  double* dG = dm + nm;
+  if ((st = h2d(dA, A, na, s)) || (st = h2d(db, b, nv, s)) || (st = h2d(dR, R, nr, s)) ||
+      (st = h2d(dm, mx, nm, s)))
+    return st;
+  if ((st = ilss_verify_dispatch(n, nrhs, dA, n, db, n, dR, n, dm, n, dx, n, dG, form, slices, s)))
+    return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(x, dx, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(bound, dG, sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  if (form != VCPCU_FORM_PLAIN && (st = take_status())) return st;
+  if (*bound >= 1.0) {
+    set_error("ilss_verify: ||RA - I|| <= %.17g is not below 1", *bound);
+    return VCPCU_ERR_VERIFY;
+  }
+  return VCPCU_OK;
+}
+
 int vcpcu_ddgemm_dev(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
                      double* C, int ldc, double* Cerr, int lde, int slices, void* stream) {
   clear_error();

@@ -19,8 +19,11 @@
 //     t2 = chain_ru(rA*|mB|)        (:281)
 //     T  = t1 +ru t2 ; up = up +ru T ; lo = lo -rd T   (:283-286)
 // with mA, rA, mB, rB from kv-style midrad (pidblas.hpp:43-51).
+#include <type_traits>
+
 #include "common.cuh"
 #include "plain_gemm.cuh"
+#include "swfp.cuh"
 
 namespace vcpcu {
 
@@ -421,6 +424,165 @@ inline int grid_1d(long total) {
   return (int)b;
 }
 
+// ---------------------------------------------------------------------------
+// Thin right factor (N <= kThinN columns: the matrix-vector products of
+// imats::linearsolve, vcp/imats.hpp:305-309, which pdblas hands to dgemv_,
+// vcp/pdblas.hpp:96-100).  The tile kernel would spend all but N of its 64
+// columns of FP64 work on padding.  Here two lanes own one row of C and run
+// its four chains in ascending k: the even lane the two midpoint chains, the
+// odd lane the two radius chains.  Both issue the same instructions: the
+// round-down chain runs negated as a round-up chain,
+// RD(a b + c) = -RU((-a) b + (-c)) (signed zeros included), each lane loads
+// its own pair of left operands -- (-mA, mA) or (|mA| +ru rA, rA), written
+// by thin_prep_left from A's kv intervals (midrad on the integer pipe,
+// sw_midrad, bit-identical to midrad_dev), or formed from a point A -- and
+// reads its own copy of B's planes from shared memory (even: mB, mB; odd:
+// rB, |mB|), so no lane diverges.  There are only 2 M lanes, each one
+// sequential chain: GB300's FP64 unit (one warp-DFMA per 64 cycles per
+// sub-partition) bounds the kernel, and the operands are streamed ahead in
+// registers so that loads do not add their latency to every step.
+constexpr int THIN_KC = 64, THIN_NT = 64;  // THIN_KC a multiple of the prefetch depth
+
+template <int NB, bool A_POINT>
+__global__ void __launch_bounds__(THIN_NT)
+interval_gemm_thin_kernel(int M, int N, int K, const double* __restrict__ A, long lda,
+                          const double* __restrict__ mB, const double* __restrict__ rB,
+                          double* __restrict__ C, long ldc) {
+  // [parity][k][j] with the odd lanes' copy one double further on (no bank
+  // conflict between the two broadcast addresses of a warp)
+  constexpr int PLANE = THIN_KC * NB + 1;
+  __shared__ double s0[2 * PLANE], s1[2 * PLANE];
+  const int t = blockIdx.x * THIN_NT + threadIdx.x;
+  const int row = t >> 1;
+  const int i = row < M ? row : M - 1;  // lanes past the last row shadow it, store nothing
+  const int odd = t & 1;
+  const double* y0p = s0 + odd * PLANE;
+  const double* y1p = s1 + odd * PLANE;
+  double c0[NB], c1[NB];
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    c0[j] = odd ? 0.0 : -0.0;  // the even lane's c0 is the negated round-down chain
+    c1[j] = 0.0;
+  }
+  // point A: A[i + k lda]; intervals: the prepared pairs X[k][i][parity]
+  constexpr int PF = 16;
+  typedef typename std::conditional<A_POINT, double, double2>::type AT;
+  const AT* ap = reinterpret_cast<const AT*>(A);
+  auto load = [&](int k) -> AT {
+    if constexpr (A_POINT) {
+      return k < K ? ap[i + (long)k * lda] : 0.0;
+    } else {
+      return k < K ? ap[2 * ((long)k * M + i) + odd] : make_double2(0.0, 0.0);
+    }
+  };
+  AT cur[PF], nxt[PF];
+#pragma unroll
+  for (int p = 0; p < PF; ++p) cur[p] = load(p);
+  for (int kb = 0; kb < K; kb += PF) {
+    const int kbase = kb % THIN_KC;
+    if (kbase == 0) {  // stage the next THIN_KC steps of B
+      const int kc = min(THIN_KC, K - kb);
+      __syncthreads();
+      for (int q = threadIdx.x; q < THIN_KC * NB; q += THIN_NT) {
+        const int kk = q % THIN_KC, j = q / THIN_KC;
+        const bool ok = kk < kc && j < N;
+        const double bm = ok ? mB[kb + kk + (long)j * K] : 0.0;
+        const double br = ok ? rB[kb + kk + (long)j * K] : 0.0;
+        const int o = kk * NB + j;
+        s0[o] = bm;
+        s1[o] = bm;
+        s0[PLANE + o] = br;
+        s1[PLANE + o] = sw_double(sw_bits(bm) & 0x7fffffffffffffffULL);
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int p = 0; p < PF; ++p) nxt[p] = load(kb + PF + p);
+#pragma unroll
+    for (int p = 0; p < PF; ++p) {
+      if (kb + p < K) {
+        double x0, x1;
+        if constexpr (A_POINT) {  // midrad of [a, a]: (a, +0), |a| +ru 0 = |a|
+          x0 = odd ? sw_double(sw_bits(cur[p]) & 0x7fffffffffffffffULL) : sw_neg(cur[p]);
+          x1 = odd ? 0.0 : cur[p];
+        } else {
+          x0 = cur[p].x;
+          x1 = cur[p].y;
+        }
+        const int kk = kbase + p;
+#pragma unroll
+        for (int j = 0; j < NB; ++j) {
+          c0[j] = __fma_ru(x0, y0p[kk * NB + j], c0[j]);
+          c1[j] = __fma_ru(x1, y1p[kk * NB + j], c1[j]);
+        }
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < PF; ++p) cur[p] = nxt[p];
+  }
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    const double T = __dadd_ru(c0[j], c1[j]);  // odd lane: t1 +ru t2
+    const double To = __shfl_xor_sync(0xffffffffu, T, 1);
+    if (!odd && row < M && j < N) {
+      double* e = C + 2 * (i + (long)j * ldc);
+      e[0] = __dsub_rd(sw_neg(c0[j]), To);
+      e[1] = __dadd_ru(c1[j], To);
+    }
+  }
+}
+
+// The left operands of the thin kernel for an interval A (M x K, lda): per
+// entry the even lane's pair (-mA, mA) and the odd lane's (|mA| +ru rA, rA),
+// X[k][i][parity] (midrad on the integer pipe, many lanes).
+__global__ void thin_prep_left(int M, int K, const double* __restrict__ A, long lda,
+                               double2* __restrict__ X) {
+  const long total = (long)M * K;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    const long i = idx % M, k = idx / M;
+    const double2 e = reinterpret_cast<const double2*>(A)[i + k * lda];
+    double m, r, p;
+    sw_midrad(e.x, e.y, m, r, p);
+    X[2 * idx] = make_double2(sw_neg(m), m);
+    X[2 * idx + 1] = make_double2(p, r);
+  }
+}
+
+// Planes of the thin right factor (K x N, ld = K): kv midrad of an interval
+// B, or the point entries with zero radii (the midrad of [b, b]).
+template <bool B_POINT>
+__global__ void thin_prep_right(int K, int N, const double* __restrict__ B, long ldb,
+                                double* __restrict__ mB, double* __restrict__ rB) {
+  const long total = (long)K * N;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    const long p = idx % K, j = idx / K;
+    if (B_POINT) {
+      mB[idx] = B[p + j * ldb];
+      rB[idx] = 0.0;
+    } else {
+      const double* e = B + 2 * (p + j * ldb);
+      double m, r;
+      midrad_dev(e[0], e[1], m, r);
+      mB[idx] = m;
+      rB[idx] = r;
+    }
+  }
+}
+
+template <int NB>
+void thin_launch(int M, int N, int K, const double* A, long lda, bool a_point,
+                 const double* mB, const double* rB, double* C, long ldc, cudaStream_t s) {
+  const long threads = 2L * M;
+  const int blocks = (int)((threads + THIN_NT - 1) / THIN_NT);
+  if (a_point)
+    interval_gemm_thin_kernel<NB, true><<<blocks, THIN_NT, 0, s>>>(M, N, K, A, lda, mB, rB, C, ldc);
+  else
+    interval_gemm_thin_kernel<NB, false><<<blocks, THIN_NT, 0, s>>>(M, N, K, A, lda, mB, rB, C,
+                                                                   ldc);
+}
+
 }  // namespace
 
 int launch_point_gemm(int M, int N, int K, const double* A, long lda, const double* B,
@@ -458,6 +620,8 @@ int launch_point_gemm(int M, int N, int K, const double* A, long lda, const doub
 int launch_interval_gemm_plain(int M, int N, int K, const double* A, long lda,
                                const double* B, long ldb, double* C, long ldc,
                                double* ws, cudaStream_t s) {
+  if (N <= kThinN)
+    return launch_interval_gemm_thin(M, N, K, A, lda, false, B, ldb, false, C, ldc, ws, s);
   // ws holds 3*M*K + 2*K*N doubles.
   double* mA = ws;
   double* pA = mA + (size_t)M * K;
@@ -513,7 +677,54 @@ int launch_isyrk_plain(int N, int K, const double* A, long lda, double* C, long 
 size_t isyrk_plain_ws_bytes(int N, int K) { return sizeof(double) * 7 * (size_t)N * K; }
 
 size_t interval_gemm_plain_ws_bytes(int M, int N, int K) {
+  if (N <= kThinN) return interval_gemm_thin_ws_bytes(M, N, K, false);
   return sizeof(double) * (3 * (size_t)M * K + 2 * (size_t)K * N);
+}
+
+int launch_interval_gemm_thin(int M, int N, int K, const double* A, long lda, bool a_point,
+                              const double* B, long ldb, bool b_point, double* C, long ldc,
+                              double* ws, cudaStream_t s) {
+  if (M <= 0 || N <= 0) return VCPCU_OK;
+  if (N > kThinN) {
+    set_error("interval_gemm_thin: N = %d exceeds %d", N, kThinN);
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (K < 0) K = 0;
+  double* mB = ws;
+  double* rB = mB + (size_t)K * N;
+  const double* Al = A;
+  long ldl = lda;
+  if (!a_point && K > 0) {  // the left operand pairs, after B's planes (16-byte aligned)
+    double2* X = reinterpret_cast<double2*>(ws + round_up(2 * (size_t)K * N, 2));
+    thin_prep_left<<<grid_1d((long)M * K), 256, 0, s>>>(M, K, A, lda, X);
+    VCPCU_LAUNCH_CHECK("thin_prep_left");
+    Al = reinterpret_cast<const double*>(X);
+    ldl = 0;
+  }
+  if (K > 0) {
+    if (b_point)
+      thin_prep_right<true><<<grid_1d((long)K * N), 256, 0, s>>>(K, N, B, ldb, mB, rB);
+    else
+      thin_prep_right<false><<<grid_1d((long)K * N), 256, 0, s>>>(K, N, B, ldb, mB, rB);
+    VCPCU_LAUNCH_CHECK("thin_prep_right");
+  }
+  if (N == 1)
+    thin_launch<1>(M, N, K, Al, ldl, a_point, mB, rB, C, ldc, s);
+  else if (N == 2)
+    thin_launch<2>(M, N, K, Al, ldl, a_point, mB, rB, C, ldc, s);
+  else if (N <= 4)
+    thin_launch<4>(M, N, K, Al, ldl, a_point, mB, rB, C, ldc, s);
+  else if (N <= 8)
+    thin_launch<8>(M, N, K, Al, ldl, a_point, mB, rB, C, ldc, s);
+  else
+    thin_launch<16>(M, N, K, Al, ldl, a_point, mB, rB, C, ldc, s);
+  VCPCU_LAUNCH_CHECK("interval_gemm_thin_kernel");
+  return VCPCU_OK;
+}
+
+size_t interval_gemm_thin_ws_bytes(int M, int N, int K, bool a_point) {
+  const size_t k = K > 0 ? K : 1, b = round_up(2 * k * (N > 0 ? N : 1), 2);
+  return sizeof(double) * (b + (a_point ? 0 : 4 * (size_t)(M > 0 ? M : 1) * k));
 }
 
 }  // namespace vcpcu

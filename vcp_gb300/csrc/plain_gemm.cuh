@@ -20,6 +20,18 @@ int launch_interval_gemm_plain(int M, int N, int K, const double* A, long lda,
                                double* ws, cudaStream_t s);
 size_t interval_gemm_plain_ws_bytes(int M, int N, int K);
 
+// Thin right factor: products with N <= kThinN columns run in
+// interval_gemm_thin_kernel (two lanes per row of C, no tile padding), with
+// the same chains and results as the tile kernel.  a_point / b_point: A / B
+// hold point entries (doubles, radius 0) instead of kv intervals.  ws holds
+// interval_gemm_thin_ws_bytes(M, N, K, a_point) bytes (with an interval A:
+// 32 bytes per entry of A for the operand pairs of the two lanes).
+constexpr int kThinN = 16;
+int launch_interval_gemm_thin(int M, int N, int K, const double* A, long lda, bool a_point,
+                              const double* B, long ldb, bool b_point, double* C, long ldc,
+                              double* ws, cudaStream_t s);
+size_t interval_gemm_thin_ws_bytes(int M, int N, int K, bool a_point);
+
 // C = [A]ᵀ[A] (A K x N interval) with pidblas::mulltmm semantics, full
 // symmetric output; ws holds isyrk_plain_ws_bytes(N, K).
 int launch_isyrk_plain(int N, int K, const double* A, long lda, double* C, long ldc, double* ws,

@@ -35,6 +35,37 @@ __device__ __forceinline__ bool sw_finite(double x) {
   return ((sw_bits(x) >> 52) & 0x7ff) != 0x7ff;
 }
 
+// Comparisons with zero and the kv absolute value on bit patterns (GB300
+// runs FP64 compares and negations on its narrow FP64 pipe).  NaN compares
+// false, as in IEEE.
+__device__ __forceinline__ bool sw_isnan_b(unsigned long long b) {
+  return (b & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL;
+}
+__device__ __forceinline__ bool sw_ge0_b(unsigned long long b) {  // x >= 0
+  return !sw_isnan_b(b) && ((b >> 63) == 0 || b == 0x8000000000000000ULL);
+}
+__device__ __forceinline__ bool sw_le0_b(unsigned long long b) {  // x <= 0
+  return !sw_isnan_b(b) && ((b >> 63) != 0 || b == 0);
+}
+// kv abs([lo, up]): [lo, up] if lo >= 0; [-up, -lo] if up <= 0; else
+// [+0, std::max(-lo, up)] (std::max(a, b) = a < b ? b : a).
+// Branch-free (selects only), so that lanes of a warp taking different cases
+// do not diverge.
+__device__ __forceinline__ void sw_abs_iv(double lo, double up, double& alo, double& aup) {
+  const unsigned long long bl = sw_bits(lo), bu = sw_bits(up), S = 1ULL << 63;
+  const bool ge = sw_ge0_b(bl), le = sw_le0_b(bu);
+  const unsigned long long a = bl ^ S;  // -lo
+  // lo < 0 < up (or a NaN): -lo < up compares two positive doubles
+  const unsigned long long mx = (!sw_isnan_b(a) && !sw_isnan_b(bu) && a < bu) ? bu : a;
+  alo = sw_double(ge ? bl : (le ? (bu ^ S) : 0ULL));
+  aup = sw_double(ge ? bu : (le ? a : mx));
+}
+__device__ __forceinline__ double sw_abs_sup(double lo, double up) {
+  double alo, aup;
+  sw_abs_iv(lo, up, alo, aup);
+  return aup;
+}
+
 // RU(X * 2^(g - 1075)) for an integer X > 0 (< 2^63) as a normal double:
 // returns false if the result would be subnormal.  Also returns the rounded
 // value as an integer multiple of 2^(g - 1075) in *Xr (exact when X has at

@@ -14,6 +14,7 @@
 #include "common.cuh"
 #include "ozaki.cuh"
 #include "plain_gemm.cuh"
+#include "swfp.cuh"
 #include "variants.cuh"
 
 namespace vcpcu {
@@ -88,21 +89,59 @@ __global__ void mirror_upper(int n, double* __restrict__ C, long ldc) {
   }
 }
 
+// The upper end of kv abs([lo, up]), on the integer pipe (swfp.cuh).
+__device__ __forceinline__ double abs_sup(double lo, double up) { return sw_abs_sup(lo, up); }
+
 // Row sums of |RA - I| rounded upward, column order ascending (one thread per
-// row; a warp reads 32 consecutive rows of one column).
+// row; a warp reads 32 consecutive rows of one column).  The sums are
+// sequential chains, so there are only n threads: each keeps two groups of
+// PF columns in flight ahead of its additions.
 __global__ void norm_rows(int n, const double* __restrict__ C, long ldc,
                           double* __restrict__ rows) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  constexpr int PF = 16;
+  const double2* c2 = reinterpret_cast<const double2*>(C);
+  auto load = [&](int j) -> double2 {
+    return j < n ? c2[i + (long)j * ldc] : make_double2(0.0, 0.0);
+  };
+  double2 cur[PF], nxt[PF];
+#pragma unroll
+  for (int p = 0; p < PF; ++p) cur[p] = load(p);
+  // the warp's rows i0 .. i0 + 31 meet the diagonal only in the column
+  // groups that overlap them (a warp-uniform test): elsewhere no FP64
+  // subtraction is issued, not even predicated off
+  const int i0 = i & ~31;
   double s = 0.0;
-  for (int j = 0; j < n; ++j) {
-    double lo = C[2 * (i + (long)j * ldc)], up = C[2 * (i + (long)j * ldc) + 1];
-    if (i == j) {
-      lo = __dsub_rd(lo, 1.0);
-      up = __dsub_ru(up, 1.0);
+  for (int jb = 0; jb < n; jb += PF) {
+#pragma unroll
+    for (int p = 0; p < PF; ++p) nxt[p] = load(jb + PF + p);
+    if (jb + PF <= i0 || jb >= i0 + 32) {
+#pragma unroll
+      for (int p = 0; p < PF; ++p) {
+        const int j = jb + p;
+        if (j < n) {
+          const double mg = abs_sup(cur[p].x, cur[p].y);
+          s = (j == 0) ? mg : __dadd_ru(s, mg);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int p = 0; p < PF; ++p) {
+        const int j = jb + p;
+        if (j < n) {
+          double lo = cur[p].x, up = cur[p].y;
+          if (i == j) {
+            lo = __dsub_rd(lo, 1.0);
+            up = __dsub_ru(up, 1.0);
+          }
+          const double mg = abs_sup(lo, up);
+          s = (j == 0) ? mg : __dadd_ru(s, mg);
+        }
+      }
     }
-    const double mg = fmax(fabs(lo), fabs(up));
-    s = (j == 0) ? mg : __dadd_ru(s, mg);
+#pragma unroll
+    for (int p = 0; p < PF; ++p) cur[p] = nxt[p];
   }
   rows[i] = s;
 }
@@ -135,6 +174,16 @@ __global__ void max_of(int n, const double* __restrict__ v, double* __restrict__
 int igemm_point_dispatch(int interval_side, int m, int n, int k, const double* L, long ldl,
                          const double* R, long ldr, double* C, long ldc, int form, int slices,
                          cudaStream_t s) {
+  const int f = form == VCPCU_FORM_AUTO ? autotune_choose(m, n, k) : form;
+  if (f == VCPCU_FORM_PLAIN && n <= kThinN) {
+    // thin plain product: the kernel reads the point factor as is
+    if (m <= 0 || n <= 0) return VCPCU_OK;
+    Scratch ws;
+    int st = ws.alloc(interval_gemm_thin_ws_bytes(m, n, k, interval_side == 1), s);
+    if (st) return st;
+    return launch_interval_gemm_thin(m, n, k > 0 ? k : 0, L, ldl, interval_side == 1, R, ldr,
+                                     interval_side == 0, C, ldc, (double*)ws.ptr, s);
+  }
   // widen the point factor into scratch, then the interval product
   const long prow = interval_side == 0 ? k : m, pcol = interval_side == 0 ? n : k;
   Scratch wide;
@@ -252,6 +301,194 @@ int norm_dispatch(int n, const double* R, long ldr, const double* A, long lda, d
   VCPCU_LAUNCH_CHECK("norm_rows");
   max_of<<<1, 256, 0, s>>>(n, rows, bound);
   VCPCU_LAUNCH_CHECK("max_of");
+  return VCPCU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The verification of imats::linearsolve (vcp/imats.hpp:293-364) after its
+// approximate inverse R = inv(mid A) and approximate solution mx = R mid(b):
+//   P = [A] mx - [b]                     (mul_im_m, subsmmA       :305-307)
+//   r = R P                              (mul_m_im                :309)
+//   E = R [A] - I, G = ||E||_inf         (mul_m_im, norminf       :317-329)
+//   t = || |r| ||_inf, g = t / (1 - G)   (norminf, division       :336-345)
+//   H = |E| (g ... g)                    (abs, mulmm              :341-353)
+//   x = mx + [-u, u], u = |r| + H        (addmm, add_im_m         :355-363)
+// with kv interval arithmetic step by step, so that the plain form gives
+// the reference's bits.
+namespace {
+
+// P -= Q elementwise (kv interval subtraction), P rows x cols with ld = rows.
+__global__ void iv_sub(int rows, int cols, double* __restrict__ P, const double* __restrict__ Q,
+                       long ldq) {
+  const long total = (long)rows * cols;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    const long i = idx % rows, j = idx / rows;
+    const double2 p = reinterpret_cast<const double2*>(P)[idx];
+    const double* q = Q + 2 * (i + j * ldq);
+    reinterpret_cast<double2*>(P)[idx] = make_double2(__dsub_rd(p.x, q[1]), __dsub_ru(p.y, q[0]));
+  }
+}
+
+// Row values of mats::norminf (vcp/mats.hpp:1565-1600) for |r|: a matrix
+// (rows, cols > 1) sums |r(i, j)| upward in ascending j; a vector or a scalar
+// takes the largest |r| (std::max order) -- max_last then picks the largest
+// row value as the reference's loop over rows does.
+__global__ void mag_rows(int rows, int cols, const double* __restrict__ R, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (rows > 1 && cols == 1) {  // a column vector: one entry per row
+    if (i < rows) out[i] = abs_sup(R[2 * (long)i], R[2 * (long)i + 1]);
+    return;
+  }
+  if (i >= rows) return;
+  const bool sum = rows > 1 && cols > 1;
+  double s = 0.0;
+  for (int j = 0; j < cols; ++j) {
+    const double* e = R + 2 * (i + (long)j * rows);
+    const double mg = abs_sup(e[0], e[1]);
+    s = j == 0 ? mg : (sum ? __dadd_ru(s, mg) : (mg < s ? s : mg));
+  }
+  out[i] = s;
+}
+
+// c = v[0]; c = std::max(v[i], c) for i = 1..n-1 (kv max of the intervals'
+// upper ends): the largest value, and of equal ones the last.  One block;
+// the (value, index) reduction is order-independent.
+__global__ void max_last(int n, const double* __restrict__ v, double* __restrict__ out) {
+  __shared__ double rv[256];
+  __shared__ int ri[256];
+  double bv = v[0];
+  int bi = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double x = v[i];
+    if (!(x < bv) && (bv < x || i > bi)) {
+      bv = x;
+      bi = i;
+    }
+  }
+  rv[threadIdx.x] = bv;
+  ri[threadIdx.x] = bi;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      const double x = rv[threadIdx.x + w];
+      const int xi = ri[threadIdx.x + w];
+      const double y = rv[threadIdx.x];
+      const int yi = ri[threadIdx.x];
+      if (y < x || (!(x < y) && xi > yi)) {
+        rv[threadIdx.x] = x;
+        ri[threadIdx.x] = xi;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = rv[0];
+}
+
+// g = [t, t] / (1 - [G, G]) by kv's interval division with both operands
+// positive: [RD(t / RU(1 - G)), RU(t / RD(1 - G))]; then E -> |E| with the
+// diagonal shifted (E = RA - I) is done by abs_shift, and H's factor
+// (g ... g) by fill_iv.
+__global__ void lss_scale(const double* __restrict__ G, const double* __restrict__ t,
+                          double* __restrict__ g) {
+  const double d_lo = __dsub_rd(1.0, *G), d_up = __dsub_ru(1.0, *G);
+  const double tt = *t;
+  const double q[4] = {__ddiv_rd(tt, d_lo), __ddiv_rd(tt, d_up), __ddiv_rd(tt, d_lo),
+                       __ddiv_rd(tt, d_up)};
+  const double u[4] = {__ddiv_ru(tt, d_lo), __ddiv_ru(tt, d_up), __ddiv_ru(tt, d_lo),
+                       __ddiv_ru(tt, d_up)};
+  double lo = q[0], up = u[0];  // std::min_element / max_element: the first extreme
+  for (int c = 1; c < 4; ++c) {
+    if (q[c] < lo) lo = q[c];
+    if (up < u[c]) up = u[c];
+  }
+  g[0] = lo;
+  g[1] = up;
+}
+
+// E(i, i) -= 1 (interval minus point), then E -> kv abs(E), in place.
+__global__ void abs_shift(int n, double* __restrict__ E) {
+  const long total = (long)n * n;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    const long i = idx % n, j = idx / n;
+    double2 e = reinterpret_cast<const double2*>(E)[idx];
+    if (i == j) {
+      e.x = __dsub_rd(e.x, 1.0);
+      e.y = __dsub_ru(e.y, 1.0);
+    }
+    double lo, up;
+    sw_abs_iv(e.x, e.y, lo, up);
+    reinterpret_cast<double2*>(E)[idx] = make_double2(lo, up);
+  }
+}
+
+__global__ void fill_iv(long count, const double* __restrict__ g, double* __restrict__ T) {
+  const double2 v = make_double2(g[0], g[1]);
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < count;
+       idx += (long)gridDim.x * blockDim.x)
+    reinterpret_cast<double2*>(T)[idx] = v;
+}
+
+// x = mx + [-u, u], u = RU(sup|r| + sup H) (addmm, the symmetric widening and
+// add_im_m of vcp/imats.hpp:355-363).
+__global__ void lss_final(int rows, int cols, const double* __restrict__ r,
+                          const double* __restrict__ H, const double* __restrict__ mx, long ldmx,
+                          double* __restrict__ x, long ldx) {
+  const long total = (long)rows * cols;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    const long i = idx % rows, j = idx / rows;
+    const double u = __dadd_ru(abs_sup(r[2 * idx], r[2 * idx + 1]), H[2 * idx + 1]);
+    const double m = mx[i + j * ldmx];
+    x[2 * (i + j * ldx)] = __dadd_rd(-u, m);
+    x[2 * (i + j * ldx) + 1] = __dadd_ru(u, m);
+  }
+}
+
+}  // namespace
+
+int ilss_thin_form(int form, int nrhs) {
+  return (form == VCPCU_FORM_PLAIN || nrhs <= kLssPlainRhs) ? VCPCU_FORM_PLAIN : form;
+}
+
+int ilss_verify_dispatch(int n, int nrhs, const double* A, long lda, const double* b, long ldb,
+                         const double* R, long ldr, const double* mx, long ldmx, double* x,
+                         long ldx, double* bound, int form, int slices, cudaStream_t s) {
+  const size_t nv = 2 * (size_t)n * nrhs, nn = 2 * (size_t)n * n;
+  Scratch ws;
+  int st = ws.alloc(sizeof(double) * (nn + 4 * nv + n + 4), s);
+  if (st) return st;
+  double* E = (double*)ws.ptr;  // R[A] - I, then |R[A] - I|
+  double* P = E + nn;
+  double* r = P + nv;
+  double* T = r + nv;
+  double* H = T + nv;
+  double* rows = H + nv;
+  double* sc = rows + n;  // t, g_lo, g_up
+  const int tf = ilss_thin_form(form, nrhs);
+  if ((st = igemm_point_dispatch(0, n, nrhs, n, A, lda, mx, ldmx, P, n, tf, slices, s))) return st;
+  iv_sub<<<grid1((long)n * nrhs), 256, 0, s>>>(n, nrhs, P, b, ldb);
+  VCPCU_LAUNCH_CHECK("iv_sub");
+  if ((st = igemm_point_dispatch(1, n, nrhs, n, R, ldr, P, n, r, n, tf, slices, s))) return st;
+  if ((st = igemm_point_dispatch(1, n, n, n, R, ldr, A, lda, E, n, form, slices, s))) return st;
+  norm_rows<<<(n + 127) / 128, 128, 0, s>>>(n, E, n, rows);
+  VCPCU_LAUNCH_CHECK("norm_rows");
+  max_of<<<1, 256, 0, s>>>(n, rows, bound);
+  VCPCU_LAUNCH_CHECK("max_of");
+  mag_rows<<<(n + 127) / 128, 128, 0, s>>>(n, nrhs, r, rows);
+  VCPCU_LAUNCH_CHECK("mag_rows");
+  max_last<<<1, 256, 0, s>>>(n, rows, sc);
+  VCPCU_LAUNCH_CHECK("max_last");
+  lss_scale<<<1, 1, 0, s>>>(bound, sc, sc + 1);
+  VCPCU_LAUNCH_CHECK("lss_scale");
+  abs_shift<<<grid1((long)n * n), 256, 0, s>>>(n, E);
+  VCPCU_LAUNCH_CHECK("abs_shift");
+  fill_iv<<<grid1((long)n * nrhs), 256, 0, s>>>((long)n * nrhs, sc + 1, T);
+  VCPCU_LAUNCH_CHECK("fill_iv");
+  if ((st = igemm_any(n, nrhs, n, E, n, T, n, H, n, tf, slices, s))) return st;
+  lss_final<<<grid1((long)n * nrhs), 256, 0, s>>>(n, nrhs, r, H, mx, ldmx, x, ldx);
+  VCPCU_LAUNCH_CHECK("lss_final");
   return VCPCU_OK;
 }
 

@@ -30,6 +30,16 @@ int vsyrk_dispatch(int n, int k, const double* A, long lda, double* C, long ldc,
 int norm_dispatch(int n, const double* R, long ldr, const double* A, long lda, double* bound,
                   int form, int slices, cudaStream_t s);
 
+// The verification steps of imats::linearsolve given R and mx (variants.cu).
+// The n^3 product R[A] runs in `form`; the three products with nrhs columns
+// run in the plain form when nrhs <= kLssPlainRhs (FP64 thin kernel: faster
+// there than padding nrhs to a 256-column tensor-core tile, and tighter).
+constexpr int kLssPlainRhs = 4;
+int ilss_thin_form(int form, int nrhs);
+int ilss_verify_dispatch(int n, int nrhs, const double* A, long lda, const double* b, long ldb,
+                         const double* R, long ldr, const double* mx, long ldmx, double* x,
+                         long ldx, double* bound, int form, int slices, cudaStream_t s);
+
 // ifma.cu: elementwise inf-sup interval FMA and the ifma-chain product.
 int launch_ifma(long count, const double* A, const double* B, const double* C, double* R,
                 cudaStream_t s);

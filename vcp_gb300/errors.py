@@ -15,6 +15,7 @@ ERR_RANGE = 4
 ERR_TIMEOUT = 5
 ERR_UNSUPPORTED = 6
 ERR_ALLOC = 7
+ERR_VERIFY = 8
 
 
 class VcpError(RuntimeError):
@@ -30,7 +31,7 @@ class StateError(VcpError):
 
 
 class VerificationError(VcpError):
-    pass
+    status = ERR_VERIFY
 
 
 class CudaError(StateError):
@@ -58,7 +59,8 @@ class AllocError(StateError):
 
 
 _BY_STATUS = {c.status: c for c in (DimensionError, CudaError, NonFiniteError, RangeError,
-                                     TimeoutError_, UnsupportedError, AllocError)}
+                                     TimeoutError_, UnsupportedError, AllocError,
+                                     VerificationError)}
 
 
 def raise_for_status(status: int, msg: str) -> None:

@@ -110,6 +110,38 @@ def norm_I_minus_RA(R: np.ndarray, A: np.ndarray, n: int, form: int = FORM_PLAIN
     return out.value
 
 
+def linearsolve_verify(A: np.ndarray, b: np.ndarray, R: np.ndarray, mx: np.ndarray, n: int,
+                       nrhs: int, form: int = FORM_PLAIN, slices: int = 0,
+                       check: bool = True) -> tuple[np.ndarray, float]:
+    """The verification of imats::linearsolve (vcp/imats.hpp:293-364) for the
+    approximate inverse R of mid(A) and the approximate solution mx = R mid(b):
+    returns (x, G) with x the kv buffer of the enclosure (n x nrhs) and G the
+    upper bound of ||RA - I||_inf.  With check, G >= 1 raises
+    VerificationError as the reference throws vcp::verification_error."""
+    import ctypes
+    x = np.empty(2 * n * nrhs, dtype=np.float64)
+    g = ctypes.c_double(0.0)
+    lib = _lib.load()
+    st = lib.vcpcu_ilss_verify(n, nrhs, _host_ptr(A, 2 * n * n, "A"),
+                               _host_ptr(b, 2 * n * nrhs, "b"), _host_ptr(R, n * n, "R"),
+                               _host_ptr(mx, n * nrhs, "mx"), x.ctypes.data, ctypes.addressof(g),
+                               int(form), int(slices))
+    if st != 0 and (check or st != 8):
+        from .errors import raise_for_status
+        raise_for_status(st, "vcpcu_ilss_verify: " +
+                         lib.vcpcu_last_error_string().decode(errors="replace"))
+    return x, g.value
+
+
+def linearsolve_verify_dev(n, nrhs, A, lda, b, ldb, R, ldr, mx, ldmx, x, ldx, bound,
+                           form=FORM_PLAIN, slices=0, stream=None) -> None:
+    """Device-pointer form on a CUDA stream; bound (one double) stays on the
+    device, the caller tests bound < 1."""
+    _lib.call("vcpcu_ilss_verify_dev", n, nrhs, _dev_ptr(A, "A"), lda, _dev_ptr(b, "b"), ldb,
+              _dev_ptr(R, "R"), ldr, _dev_ptr(mx, "mx"), ldmx, _dev_ptr(x, "x"), ldx,
+              _dev_ptr(bound, "bound"), int(form), int(slices), _stream_ptr(stream))
+
+
 # ---- AUTO form -------------------------------------------------------------------
 
 def autotune(stream=None) -> dict:
