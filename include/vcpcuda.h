@@ -36,6 +36,7 @@ extern "C" {
 #define VCPCU_ERR_UNSUPPORTED  6  /* no usable sm_103 device, or option not built    */
 #define VCPCU_ERR_ALLOC        7  /* device or pinned host allocation failed         */
 #define VCPCU_ERR_VERIFY       8  /* a verification condition failed (||RA - I|| >= 1) */
+#define VCPCU_ERR_IO           9  /* a .vcpmat file could not be read or written       */
 
 /* rounding_mode values, identical to vblas rmatmul (vblas/rmatmul.hpp:100-102) */
 #define VCPCU_ROUND_UP      1
@@ -368,6 +369,32 @@ int vcpcu_ddgemm(int m, int n, int k, const double* A, const double* B,
 int vcpcu_igemm_noalloc_dev(int m, int n, int k, const double* A, int lda,
                             const double* B, int ldb, double* C, int ldc,
                             int slices, void* stream);
+
+/* ---- portable matrix files (vcp/vcp_portable_fio.hpp) ----------------- */
+
+/* Element types of a .vcpmat file (vcp/vcp_portable_fio.hpp:60-66) and their
+ * in-memory layout (column-major, one element after the other). */
+#define VCPCU_MAT_INT32       1  /* int32                                      */
+#define VCPCU_MAT_DOUBLE      2  /* double                                     */
+#define VCPCU_MAT_INTERVAL    3  /* kv::interval<double>: {lower, upper}        */
+#define VCPCU_MAT_DD          4  /* kv::dd: {a1, a2}                            */
+#define VCPCU_MAT_INTERVAL_DD 5  /* kv::interval<kv::dd>: {lo.a1, lo.a2, up.a1, up.a2} */
+
+/* <name>.vcpmat in the format of vcp::save_portable / load_portable
+ * (vcp/vcp_portable_fio.hpp:476-565): same bytes as the reference writes,
+ * written through <name>.vcpmat.tmp and a rename; a load checks magic,
+ * version, layout, type, sizes, CRC-64 and trailing data and returns
+ * VCPCU_ERR_IO where the reference throws vcp::io_error.  rows and cols must
+ * match the file (vcpcu_vcpmat_info reads them); 0 x 0 is allowed.  The
+ * _dev forms stream the matrix to / from device memory (leading dimension
+ * ld, in elements) through pinned chunks on `stream` and return after it. */
+int vcpcu_vcpmat_save(const char* name, int type, int rows, int cols, const void* data);
+int vcpcu_vcpmat_info(const char* name, int* type, int* rows, int* cols);
+int vcpcu_vcpmat_load(const char* name, int type, int rows, int cols, void* data);
+int vcpcu_vcpmat_save_dev(const char* name, int type, int rows, int cols, const void* ddata,
+                          int ld, void* stream);
+int vcpcu_vcpmat_load_dev(const char* name, int type, int rows, int cols, void* ddata, int ld,
+                          void* stream);
 
 #ifdef __cplusplus
 }

@@ -26,12 +26,19 @@ struct mode_guard {
 };
 // Operands are read through volatile copies after the mode switch and the
 // result is stored to a volatile before it is restored, so the arithmetic
-// cannot move across the fesetround calls.
+// cannot move across the fesetround calls (double; other endpoint types,
+// such as kv::dd in interval<kv::dd>, only pass through the file I/O here).
 #define KVSHIM_DIR(name, mode, expr)                 \
   template <class T> inline T name(T a, T b) {       \
-    volatile T x = a, y = b;                         \
+    T x = a, y = b;                                  \
     mode_guard g(mode);                              \
-    volatile T r = expr;                             \
+    T r = expr;                                      \
+    return r;                                        \
+  }                                                  \
+  inline double name(double a, double b) {           \
+    volatile double x = a, y = b;                    \
+    mode_guard g(mode);                              \
+    volatile double r = expr;                        \
     return r;                                        \
   }
 KVSHIM_DIR(add_dn, FE_DOWNWARD, x + y)
@@ -43,8 +50,10 @@ KVSHIM_DIR(mul_up, FE_UPWARD, x * y)
 KVSHIM_DIR(div_dn, FE_DOWNWARD, x / y)
 KVSHIM_DIR(div_up, FE_UPWARD, x / y)
 #undef KVSHIM_DIR
-template <class T> inline T sqrt_dn(T a) { volatile T x = a; mode_guard g(FE_DOWNWARD); volatile T r = std::sqrt((T)x); return r; }
-template <class T> inline T sqrt_up(T a) { volatile T x = a; mode_guard g(FE_UPWARD); volatile T r = std::sqrt((T)x); return r; }
+template <class T> inline T sqrt_dn(T a) { using std::sqrt; mode_guard g(FE_DOWNWARD); return sqrt(a); }
+template <class T> inline T sqrt_up(T a) { using std::sqrt; mode_guard g(FE_UPWARD); return sqrt(a); }
+inline double sqrt_dn(double a) { volatile double x = a; mode_guard g(FE_DOWNWARD); volatile double r = std::sqrt((double)x); return r; }
+inline double sqrt_up(double a) { volatile double x = a; mode_guard g(FE_UPWARD); volatile double r = std::sqrt((double)x); return r; }
 }  // namespace shim
 
 template <class T> class interval {
@@ -59,6 +68,12 @@ template <class T> class interval {
   template <class C1, class C2> interval(const C1& l, const C2& u) : inf(T(l)), sup(T(u)) {}
   interval& operator=(const interval& x) = default;
   template <class C> interval& operator=(const C& x) { inf = sup = T(x); return *this; }
+
+  interval& assign(const T& l, const T& u) {
+    inf = l;
+    sup = u;
+    return *this;
+  }
 
   T& lower() { return inf; }
   const T& lower() const { return inf; }

@@ -27,6 +27,8 @@
 #include <vcp/pidblas_fma.hpp>
 #include <vcp/ifma.hpp>
 #include <vcp/matrix.hpp>
+#include <kv/dd.hpp>
+#include <vcp/vcp_portable_fio.hpp>
 
 namespace {
 int current_direction() {
@@ -302,6 +304,116 @@ int ref_imats_linearsolve(int n, int nrhs, const double* A, const double* b, dou
     return 1;
   }
 }
+
+}  // extern "C"
+
+// vcp::save_portable / load_portable (vcp/vcp_portable_fio.hpp) of a
+// vcp::matrix of each element type, the data in flat element layouts
+// (type 1 int32, 2 double, 3 {lower, upper}, 4 {a1, a2}, 5 {lo.a1, lo.a2,
+// up.a1, up.a2}).  Returns 0, 3 on vcp::io_error, 1 on anything else; a load
+// also reports the file's rows and columns (and fills data when it is not
+// null and large enough).
+namespace {
+typedef kv::interval<kv::dd> IDD;
+void put_el(int& x, const void* d, long t) { x = ((const int*)d)[t]; }
+void put_el(double& x, const void* d, long t) { x = ((const double*)d)[t]; }
+void put_el(I& x, const void* d, long t) {
+  const double* p = (const double*)d + 2 * t;
+  x.assign(p[0], p[1]);
+}
+void put_el(kv::dd& x, const void* d, long t) {
+  const double* p = (const double*)d + 2 * t;
+  x.a1 = p[0];
+  x.a2 = p[1];
+}
+void put_el(IDD& x, const void* d, long t) {
+  const double* p = (const double*)d + 4 * t;
+  x.lower().a1 = p[0];
+  x.lower().a2 = p[1];
+  x.upper().a1 = p[2];
+  x.upper().a2 = p[3];
+}
+void get_el(const int& x, void* d, long t) { ((int*)d)[t] = x; }
+void get_el(const double& x, void* d, long t) { ((double*)d)[t] = x; }
+void get_el(const I& x, void* d, long t) {
+  ((double*)d)[2 * t] = x.lower();
+  ((double*)d)[2 * t + 1] = x.upper();
+}
+void get_el(const kv::dd& x, void* d, long t) {
+  ((double*)d)[2 * t] = x.a1;
+  ((double*)d)[2 * t + 1] = x.a2;
+}
+void get_el(const IDD& x, void* d, long t) {
+  double* p = (double*)d + 4 * t;
+  p[0] = x.lower().a1;
+  p[1] = x.lower().a2;
+  p[2] = x.upper().a1;
+  p[3] = x.upper().a2;
+}
+template <class T> int vcpmat_save_t(const char* name, int rows, int cols, const void* data) {
+  vcp::matrix<T> A;
+  A.zeros(rows, cols);
+  for (int j = 0; j < cols; ++j)
+    for (int i = 0; i < rows; ++i) put_el(A(i, j), data, i + (long)j * rows);
+  vcp::save_portable(A, name);
+  return 0;
+}
+template <class T> int vcpmat_load_t(const char* name, int* rows, int* cols, void* data,
+                                     long capacity) {
+  vcp::matrix<T> A;
+  vcp::load_portable(A, name);
+  *rows = A.rowsize();
+  *cols = A.columnsize();
+  if (data && (long)A.rowsize() * A.columnsize() <= capacity)
+    for (int j = 0; j < A.columnsize(); ++j)
+      for (int i = 0; i < A.rowsize(); ++i) {
+        const vcp::matrix<T>& cA = A;
+        get_el(cA(i, j), data, i + (long)j * A.rowsize());
+      }
+  return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int ref_vcpmat_save(const char* name, int type, int rows, int cols, const void* data) {
+  try {
+    switch (type) {
+      case 1: return vcpmat_save_t<int>(name, rows, cols, data);
+      case 2: return vcpmat_save_t<double>(name, rows, cols, data);
+      case 3: return vcpmat_save_t<I>(name, rows, cols, data);
+      case 4: return vcpmat_save_t<kv::dd>(name, rows, cols, data);
+      case 5: return vcpmat_save_t<IDD>(name, rows, cols, data);
+      default: return 1;
+    }
+  } catch (vcp::io_error&) {
+    return 3;
+  } catch (...) {
+    return 1;
+  }
+}
+
+int ref_vcpmat_load(const char* name, int type, int* rows, int* cols, void* data,
+                    long capacity) {
+  try {
+    switch (type) {
+      case 1: return vcpmat_load_t<int>(name, rows, cols, data, capacity);
+      case 2: return vcpmat_load_t<double>(name, rows, cols, data, capacity);
+      case 3: return vcpmat_load_t<I>(name, rows, cols, data, capacity);
+      case 4: return vcpmat_load_t<kv::dd>(name, rows, cols, data, capacity);
+      case 5: return vcpmat_load_t<IDD>(name, rows, cols, data, capacity);
+      default: return 1;
+    }
+  } catch (vcp::io_error&) {
+    return 3;
+  } catch (...) {
+    return 1;
+  }
+}
+
+}  // extern "C"
+
+extern "C" {
 
 // vcp::ifma (vcp/ifma.hpp, the portable branch: VCP_USE_AVX512 undefined),
 // elementwise over kv pairs.

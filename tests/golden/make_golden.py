@@ -144,6 +144,35 @@ def main() -> None:
     data["n_iv"] = np.array([len(icases)])
     np.savez_compressed(OUT, **data)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
+    write_vcpmat_fixtures()
+
+
+def write_vcpmat_fixtures() -> None:
+    """.vcpmat files written by the reference's own vcp::save_portable
+    (tests/golden/vcpmat/): an interval product A (33 x 17) * B (17 x 20) = C
+    from vcp::matrix<interval, pidblas>, and one small matrix of every other
+    element type."""
+    import ctypes
+    R = O.ref_lib()
+    R.ref_vcpmat_save.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_void_p]
+    d = Path(__file__).resolve().parent / "vcpmat"
+    d.mkdir(exist_ok=True)
+    rng = np.random.default_rng(20261206)
+    m, n, k = 33, 20, 17
+    A = W.interval_ephi(rng, m, k, 4, 2.0 ** -30)
+    B = W.interval_ephi(rng, k, n, 4, 2.0 ** -20)
+    C = O.ref_pidblas_mulmm(m, n, k, A, B)
+    mats = [("A", 3, m, k, A), ("B", 3, k, n, B), ("C", 3, m, n, C),
+            ("int32", 1, 5, 4, rng.integers(-1000, 1000, 20).astype(np.int32)),
+            ("double", 2, 4, 6, W.ephi(rng, 24, 30)),
+            ("dd", 4, 3, 5, np.ravel(np.stack([W.ephi(rng, 15, 3), W.ephi(rng, 15, 3) * 2.0 ** -60],
+                                               axis=1))),
+            ("interval_dd", 5, 2, 3, np.sort(W.ephi(rng, 24, 2)))]
+    for name, kind, r, c, buf in mats:
+        buf = np.ascontiguousarray(buf)
+        assert R.ref_vcpmat_save(str(d / name).encode(), kind, r, c, buf.ctypes.data) == 0
+    print(f"wrote {len(mats)} .vcpmat fixtures to {d}")
 
 
 if __name__ == "__main__":

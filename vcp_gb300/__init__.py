@@ -7,8 +7,9 @@ of include/vcpcuda.h); this package is its Python host side:
                  FP64 GEMM);
 * ``pidcuda`` -- interval GEMM with pidblas semantics (plain FP64 form and the
                  Ozaki tensor-core form);
+* ``vcpmat``  -- portable matrix files (.vcpmat) to and from host or device memory;
 * ``build``   -- in-tree nvcc build of the library.
 """
 from . import errors  # noqa: F401
 
-__all__ = ["errors", "vblas", "pidcuda", "build"]
+__all__ = ["errors", "vblas", "pidcuda", "vcpmat", "build"]

@@ -16,6 +16,7 @@ ERR_TIMEOUT = 5
 ERR_UNSUPPORTED = 6
 ERR_ALLOC = 7
 ERR_VERIFY = 8
+ERR_IO = 9
 
 
 class VcpError(RuntimeError):
@@ -58,9 +59,14 @@ class AllocError(StateError):
     status = ERR_ALLOC
 
 
+class IOError_(VcpError):
+    """vcp::io_error (vcp/error.hpp): a .vcpmat file could not be read or written."""
+    status = ERR_IO
+
+
 _BY_STATUS = {c.status: c for c in (DimensionError, CudaError, NonFiniteError, RangeError,
                                      TimeoutError_, UnsupportedError, AllocError,
-                                     VerificationError)}
+                                     VerificationError, IOError_)}
 
 
 def raise_for_status(status: int, msg: str) -> None:
