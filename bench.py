@@ -31,7 +31,9 @@ Our arm (default) prints one JSON line with
                  lss    the verification of imats::linearsolve on the GPU
                         (vcpcu_ilss_verify), n x n with nrhs right-hand
                         sides (--phis carries nrhs): plain vs Ozaki time,
-                        width ratio, CPU restatement.
+                        width ratio, CPU restatement;
+                 eig    the verification of imats::eigsymge on the GPU
+                        (vcpcu_ieigsymge stages), n x n: plain vs Ozaki.
 --impl reference times that CPU path alone as the reference arm.
 
 Inputs are 1 GiB per operand (larger than the 129 MB L2), so no L2 flush is
@@ -71,7 +73,7 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=0, help="row sample of the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="interval",
-                    choices=["interval", "batch", "dd", "point", "lss"],
+                    choices=["interval", "batch", "dd", "point", "lss", "eig"],
                     help="interval: the headline line (default); the others print their own "
                          "line at the full sizes of that workload")
     ap.add_argument("--sizes", default="", help="point / dd: comma-separated n (or m:n:k)")
@@ -738,6 +740,59 @@ def bench_lss(dev, stream, n, nrhs=1, steps=2, plain_steps=1, seed=91, cpu_n=768
     return out
 
 
+def bench_eig(dev, stream, n, steps=2, plain_steps=1, seed=93):
+    """The verification of imats::eigsymge (vcpcu_ieigsymge stages 1 and 2)
+    for A x = l B x, n x n: A symmetric N(0, 1/n), B = I + 0.1 G (G G^T form,
+    positive definite), radii 2^-40 |mid|; the approximate eigenpairs and
+    Y = inv(mid(B X)) formed on the device in FP64 beforehand (setup, as the
+    reference takes them from LAPACK).  Time of the two stages (four n^3
+    interval products, norms, enclosures), plain vs tensor-core form."""
+    import torch
+    from vcp_gb300 import pidcuda
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed + n)
+    f64 = dict(dtype=torch.float64, device=dev)
+    Am = torch.randn(n, n, generator=gen, **f64) / n ** 0.5
+    Am = (Am + Am.t()) / 2
+    G = torch.eye(n, **f64) + 0.1 * torch.randn(n, n, generator=gen, **f64) / n ** 0.5
+    Bm = G @ G.t()
+    Bm = (Bm + Bm.t()) / 2
+    L = torch.linalg.cholesky(Bm)
+    Li = torch.linalg.inv(L)
+    w, V = torch.linalg.eigh(Li @ Am @ Li.t())
+    X = (Li.t() @ V).t().contiguous().reshape(-1)
+
+    def kv(m):
+        r = m.abs() * 2.0 ** -40
+        return torch.stack((m - r, m + r), dim=-1).transpose(0, 1).contiguous().reshape(-1)
+
+    A, B = kv(Am), kv(Bm)
+    C = torch.empty(2 * n * n, **f64)
+    BX = torch.empty_like(C)
+    M = torch.empty(n * n, **f64)
+    pidcuda.eigsymge_stage1_dev(n, A, n, B, n, X, n, C, BX, M, pidcuda.FORM_OZAKI, 0, stream)
+    stream.synchronize()
+    Y = torch.linalg.inv(M.reshape(n, n).t()).t().contiguous().reshape(-1)
+    lam = torch.empty(2 * n, **f64)
+    bound = torch.empty(1, **f64)
+    out = {"n": n}
+    res = {}
+    for name, form, st_ in (("plain", pidcuda.FORM_PLAIN, plain_steps),
+                            ("ozaki", pidcuda.FORM_OZAKI, steps)):
+        def step():
+            pidcuda.eigsymge_stage1_dev(n, A, n, B, n, X, n, C, BX, M, form, 0, stream)
+            pidcuda.eigsymge_stage2_dev(n, w, Y, n, C, BX, lam, bound, form, 0, stream)
+        ms = time_stream(step, stream, st_)
+        res[name] = lam.cpu().numpy()
+        out[name] = {"ms": ms, "bound_YBX_minus_I": float(bound.cpu()[0])}
+    wp = res["plain"][1::2] - res["plain"][0::2]
+    wo = res["ozaki"][1::2] - res["ozaki"][0::2]
+    out["width_ozaki_vs_plain_median"] = float(np.median(wo / wp))
+    out["speedup_ozaki_vs_plain"] = out["plain"]["ms"] / out["ozaki"]["ms"]
+    out["enclosure_width_median"] = float(np.median(wo))
+    return out
+
+
 def parse_list(text, default, conv=int):
     return [conv(x) for x in text.split(",") if x] if text else default
 
@@ -759,6 +814,12 @@ def run_workload(args, dev, stream):
                              for nrhs in parse_list(args.phis, [1])]}
             metric, unit = ("verified linear solve, device-resident verification "
                             "(imats::linearsolve after R, mx): ms"), "ms"
+            value = min(c["ozaki"]["ms"] for c in res["cases"])
+        elif args.workload == "eig":
+            res = {"cases": [bench_eig(dev, stream, n, steps=args.steps)
+                             for n in parse_list(args.sizes, [4096])]}
+            metric, unit = ("verified generalized symmetric eigenvalues, device-resident "
+                            "verification (imats::eigsymge after X, lambda, Y): ms"), "ms"
             value = min(c["ozaki"]["ms"] for c in res["cases"])
         elif args.workload == "dd":
             res = {"cases": [bench_dd(dev, stream, n, phi, steps=args.steps)

@@ -7,9 +7,9 @@
 //     x = lss(A, b);              // pidcuda::linearsolve -> vcpcu_ilss_verify
 //     vcp::matrix< kv::interval<double>, vcp::pidcuda_fma > F;  // pidblas_fma drop-in
 // The class derives from vcp::imats<double, vcp::pdblas> as pidblas does, so
-// every imats algorithm (eigsym, eigsymge, ...) routes its interval products
-// through the hooks below to libvcpcuda (include/vcpcuda.h); linearsolve is
-// replaced by a version whose whole verification stays on the GPU.
+// every imats algorithm (eigsym, ...) routes its interval products through
+// the hooks below to libvcpcuda (include/vcpcuda.h); linearsolve and
+// eigsymge are replaced by versions whose verification stays on the GPU.
 //
 // Form and precision are process-wide settings:
 //     vcp::pidcuda_settings::form()   = VCPCU_FORM_OZAKI;   // default
@@ -23,6 +23,7 @@
 #define VCP_CUDA_PIDCUDA_HPP
 
 #include <iostream>
+#include <vector>
 
 #include <kv/interval.hpp>
 #include <vcp/error.hpp>
@@ -58,6 +59,19 @@ inline void check(int st, const char* what) {
   if (st == VCPCU_ERR_INVALID_ARG)
     vcp::throw_error<vcp::dimension_error>(what, ": ", vcpcu_last_error_string());
   vcp::throw_error<vcp::state_error>(what, ": ", vcpcu_last_error_string());
+}
+// The inverse callback of vcpcu_ieigsymge: pdblas::inv (LAPACK) in place.
+inline int pdblas_inverse(int n, double* M, void*) {
+  try {
+    vcp::pdblas Y;
+    Y.zeros(n, n);
+    for (long i = 0; i < (long)n * n; ++i) Y.v[i] = M[i];
+    Y.inv();
+    for (long i = 0; i < (long)n * n; ++i) M[i] = Y.v[i];
+    return 0;
+  } catch (...) {
+    return 1;
+  }
 }
 }  // namespace pidcuda_detail
 
@@ -168,6 +182,42 @@ class pidcuda : public vcp::imats<double, vcp::pdblas> {
       vcp::throw_error<vcp::verification_error>("linearsolve verification failed: ||RA - I|| <= ",
                                                 G);
     pidcuda_detail::check(st, "pidcuda::linearsolve");
+  }
+  // Enclosures of the eigenvalues of A x = lambda B x (imats::eigsymge,
+  // vcp/imats.hpp:419-522; Miyajima's theorem).  The approximate eigenpairs
+  // come from the host LAPACK as in the reference (pdblas::eigsymge), the
+  // inverse of mid(B X) from pdblas::inv; the four interval products, the
+  // norms and the enclosures run on the GPU (vcpcu_ieigsymge).  *this
+  // becomes the diagonal matrix of the enclosures; n = 1 keeps the
+  // reference's scalar path.
+  void eigsymge(base& B, int itep = 1) {
+    const int n = this->row;
+    if (n < 2) {
+      base::eigsymge(B, itep);
+      return;
+    }
+    vcp::pdblas X, lambda;
+    {
+      vcp::pdblas mA, mB;
+      this->imid(mA);
+      mB.zeros(B.row, B.column);
+      for (int i = 0; i < B.n; i++) mB.v[i] = mid(B.v[i]);
+      mA.eigsymge(mB, X);
+      mA.diag(lambda);
+    }
+    std::vector<double> lam(2 * (size_t)n);
+    double bound = 0.0;
+    const int st = vcpcu_ieigsymge(n, pidcuda_detail::cd(this->v), pidcuda_detail::cd(B.v),
+                                   X.v.data(), lambda.v.data(), &pidcuda_detail::pdblas_inverse,
+                                   nullptr, lam.data(), &bound, pidcuda_settings::form(),
+                                   pidcuda_settings::slices());
+    if (st == VCPCU_ERR_VERIFY)
+      vcp::throw_error<vcp::verification_error>("eigsymge verification failed: ||YBX - I|| <= ",
+                                                bound);
+    pidcuda_detail::check(st, "pidcuda::eigsymge");
+    this->zeros(n, n);
+    for (int i = 0; i < n; i++)
+      this->v[i + n * i] = kv::interval<double>(lam[2 * i], lam[2 * i + 1]);
   }
   // C = [A]^T [A] (pidblas::mulltmm)
   void mulltmm(vcp::mats<kv::interval<double> >& c) const override {

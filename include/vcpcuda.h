@@ -370,6 +370,38 @@ int vcpcu_igemm_noalloc_dev(int m, int n, int k, const double* A, int lda,
                             const double* B, int ldb, double* C, int ldc,
                             int slices, void* stream);
 
+/* The verification of imats::eigsymge (vcp/imats.hpp:419-522; Miyajima's
+ * enclosure of every eigenvalue of A x = lambda B x, A, B symmetric n x n
+ * interval, mid B positive definite) around the approximate eigenvectors X
+ * (n x n) and eigenvalues lambda (n) of the midpoint problem, which the
+ * reference takes from LAPACK dsygv on the host (:427-434):
+ *   stage 1: C = [A] X, BX = [B] X (kv layout, ld n) and mid(BX) (ld n);
+ *   the caller forms Y = inv(mid(BX)) (the reference: pdblas::inv);
+ *   stage 2: C -= BX diag(lambda); R = Y C; S = Y BX - I; from their norms
+ *   and |R| e, |S| e the enclosures lam[2i], lam[2i+1] (before the overlap
+ *   merge) and *bound = sup ||S|| (the reference throws
+ *   vcp::verification_error when it is >= 1).
+ * Every step uses the reference's kv operation; in the plain form R = Y C is
+ * the base class's term-by-term kv loop, as in the reference, so all bits
+ * match it (for n >= 2); the tensor-core forms enclose the same products.
+ * Device pointers; C is overwritten by stage 2; lam, bound in device memory.
+ * vcpcu_eig_merge is the reference's final overlap merge (host memory).
+ * vcpcu_ieigsymge (host memory) runs both stages, calls inv(n, M, ctx) to
+ * turn M = mid(BX) (column-major) into its inverse in place (non-zero
+ * return: VCPCU_ERR_INVALID_ARG), merges, and returns VCPCU_ERR_VERIFY
+ * when *bound >= 1 (lam then meaningless). */
+typedef int (*vcpcu_inverse_fn)(int n, double* M, void* ctx);
+int vcpcu_ieigsymge_stage1_dev(int n, const double* A, int lda, const double* B, int ldb,
+                               const double* X, int ldx, double* C, double* BX, double* midBX,
+                               int form, int slices, void* stream);
+int vcpcu_ieigsymge_stage2_dev(int n, const double* lambda, const double* Y, int ldy, double* C,
+                               const double* BX, double* lam, double* bound, int form,
+                               int slices, void* stream);
+int vcpcu_eig_merge(int n, double* lam);
+int vcpcu_ieigsymge(int n, const double* A, const double* B, const double* X,
+                    const double* lambda, vcpcu_inverse_fn inv, void* ctx, double* lam,
+                    double* bound, int form, int slices);
+
 /* ---- portable matrix files (vcp/vcp_portable_fio.hpp) ----------------- */
 
 /* Element types of a .vcpmat file (vcp/vcp_portable_fio.hpp:60-66) and their

@@ -50,6 +50,10 @@ def lib() -> C.CDLL:
         L.orc_norm_I_minus_RA.restype = C.c_double
         L.orc_ilss_verify.argtypes = [_i, _i, _v, _v, _v, _v, _v, _v, _v, _i]
         L.orc_ilss_verify.restype = _i
+        L.orc_ieigsymge.argtypes = [_i, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v, _i, _i]
+        L.orc_ieigsymge.restype = _i
+        L.orc_imats_mul_m_im_naive.argtypes = [_i, _i, _i, _v, _v, _v]
+        L.orc_eig_merge.argtypes = [_i, _v]
         _lib = L
     return _lib
 
@@ -75,6 +79,8 @@ def ref_lib() -> C.CDLL | None:
         R.ref_norm_I_minus_RA.restype = _i
         R.ref_imats_linearsolve.argtypes = [_i, _i, _v, _v, _v, _v, _v]
         R.ref_imats_linearsolve.restype = _i
+        R.ref_imats_eigsymge.argtypes = [_i, _v, _v, _v, _v, _v, _v]
+        R.ref_imats_eigsymge.restype = _i
         _ref = R
     return _ref
 
@@ -197,6 +203,39 @@ def ref_imats_linearsolve(n, nrhs, A, b):
     mx = np.zeros(n * nrhs)
     st = Rl.ref_imats_linearsolve(n, nrhs, _p(A), _p(b), _p(x), _p(R), _p(mx))
     return int(st), x, R, mx
+
+
+def ieigsymge(n, A, B, X, lam, Y, C=None, BX=None, R=None, S=None, merge=True, threads=0):
+    """imats::eigsymge's verification (restatement) for given X, lambda, Y:
+    (status, enclosures kv (n), bound ||YBX - I||); status 2 when the bound
+    is >= 1.  C, BX, R, S replace the products [A]X, [B]X, YC, Y[BX]."""
+    out = np.zeros(2 * n)
+    g = np.zeros(1)
+    opt = [None if v is None else _p(v) for v in (C, BX, R, S)]
+    st = lib().orc_ieigsymge(n, _p(A), _p(B), _p(X), _p(lam), _p(Y), *opt, _p(out), _p(g),
+                             int(merge), int(threads))
+    return int(st), out, float(g[0])
+
+
+def imats_mul_m_im_naive(m, n, k, Y, C):
+    """imats::mul_m_im 'M' x 'M' (restatement): Y point (m x k) times C kv."""
+    R = np.zeros(2 * m * n)
+    lib().orc_imats_mul_m_im_naive(m, n, k, _p(Y), _p(C), _p(R))
+    return R
+
+
+def ref_imats_eigsymge(n, A, B):
+    """The reference's imats<double, pidblas>::eigsymge run as is:
+    (status, enclosures kv (n), X, lambda, Y); None without the reference."""
+    Rl = ref_lib()
+    if Rl is None:
+        return None
+    lam = np.zeros(2 * n)
+    X = np.zeros(n * n)
+    lmb = np.zeros(n)
+    Y = np.zeros(n * n)
+    st = Rl.ref_imats_eigsymge(n, _p(A), _p(B), _p(lam), _p(X), _p(lmb), _p(Y))
+    return int(st), lam, X, lmb, Y
 
 
 def ifma(A, B, C_) -> np.ndarray:

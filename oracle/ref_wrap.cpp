@@ -134,15 +134,107 @@ void dgetri_(int* n, double* A, int* lda, int* ipiv, double* work, int* lwork, i
     for (int i = 0; i < N; ++i) A[i + (long)c * ld] = X[i + (size_t)c * N];
 }
 
+// The approximate eigenpairs of imats::eigsymge (vcp/imats.hpp:427-434) come
+// from pdblas::eigsymge (vcp/pdblas.hpp:334-375): dsygv_ with itype 1, jobz
+// "V", uplo "U".  Project-written: Cholesky B = U^T U (upper triangle),
+// cyclic Jacobi on U^-T A U^-1 to convergence, eigenvalues ascending in W,
+// B-orthonormal eigenvectors X = U^-1 V in A, U in B.  Any approximate
+// eigenpairs serve the verification; the same X is handed to the GPU path.
+void dsygv_(int* itype, char* jobz, char* uplo, int* n, double* A, int* lda, double* B, int* ldb,
+            double* W, double* work, int* lwork, int* info) {
+  const int N = *n, la = *lda, lb = *ldb;
+  *info = 0;
+  if (*lwork == -1) {
+    work[0] = 3.0 * (N > 0 ? N : 1);
+    return;
+  }
+  if (*itype != 1 || jobz[0] != 'V' || uplo[0] != 'U') unsupported("dsygv_");
+  std::vector<double> U((size_t)N * N, 0.0), M((size_t)N * N), V((size_t)N * N, 0.0);
+  auto u = [&](int i, int j) -> double& { return U[i + (size_t)j * N]; };
+  auto m = [&](int i, int j) -> double& { return M[i + (size_t)j * N]; };
+  auto v = [&](int i, int j) -> double& { return V[i + (size_t)j * N]; };
+  for (int j = 0; j < N; ++j) {  // B = U^T U
+    for (int i = 0; i <= j; ++i) {
+      double t = B[i + (long)j * lb];
+      for (int k = 0; k < i; ++k) t -= u(k, i) * u(k, j);
+      if (i == j) {
+        if (!(t > 0.0)) {
+          *info = N + j + 1;
+          return;
+        }
+        u(j, j) = std::sqrt(t);
+      } else {
+        u(i, j) = t / u(i, i);
+      }
+    }
+  }
+  // M = U^-T A U^-1 (A symmetric from its upper triangle)
+  std::vector<double> T((size_t)N * N);
+  for (int j = 0; j < N; ++j)
+    for (int i = 0; i < N; ++i)
+      T[i + (size_t)j * N] = i <= j ? A[i + (long)j * la] : A[j + (long)i * la];
+  for (int j = 0; j < N; ++j)  // T <- U^-T T (forward substitution, column j)
+    for (int i = 0; i < N; ++i) {
+      double t = T[i + (size_t)j * N];
+      for (int k = 0; k < i; ++k) t -= u(k, i) * T[k + (size_t)j * N];
+      T[i + (size_t)j * N] = t / u(i, i);
+    }
+  for (int i = 0; i < N; ++i)  // M <- T U^-1 (row i)
+    for (int j = 0; j < N; ++j) {
+      double t = T[i + (size_t)j * N];
+      for (int k = 0; k < j; ++k) t -= m(i, k) * u(k, j);
+      m(i, j) = t / u(j, j);
+    }
+  for (int i = 0; i < N; ++i) v(i, i) = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {  // cyclic Jacobi
+    double off = 0.0;
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < j; ++i) off += m(i, j) * m(i, j);
+    if (off == 0.0) break;
+    for (int p = 0; p < N; ++p)
+      for (int q = p + 1; q < N; ++q) {
+        if (m(p, q) == 0.0) continue;
+        const double th = (m(q, q) - m(p, p)) / (2.0 * m(p, q));
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s_ = t * c;
+        for (int k = 0; k < N; ++k) {  // columns p, q
+          const double a = m(k, p), b = m(k, q);
+          m(k, p) = c * a - s_ * b;
+          m(k, q) = s_ * a + c * b;
+        }
+        for (int k = 0; k < N; ++k) {  // rows p, q
+          const double a = m(p, k), b = m(q, k);
+          m(p, k) = c * a - s_ * b;
+          m(q, k) = s_ * a + c * b;
+        }
+        for (int k = 0; k < N; ++k) {
+          const double a = v(k, p), b = v(k, q);
+          v(k, p) = c * a - s_ * b;
+          v(k, q) = s_ * a + c * b;
+        }
+      }
+  }
+  std::vector<int> ord(N);
+  for (int i = 0; i < N; ++i) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return m(a, a) < m(b, b); });
+  for (int c = 0; c < N; ++c) {  // X(:, c) = U^-1 V(:, ord[c]) (back substitution)
+    W[c] = m(ord[c], ord[c]);
+    for (int i = N - 1; i >= 0; --i) {
+      double t = v(i, ord[c]);
+      for (int k = i + 1; k < N; ++k) t -= u(i, k) * A[k + (long)c * la];
+      A[i + (long)c * la] = t / u(i, i);
+    }
+  }
+  for (int j = 0; j < N; ++j)
+    for (int i = 0; i < N; ++i) B[i + (long)j * lb] = i <= j ? u(i, j) : 0.0;
+}
+
 // The remaining LAPACK / BLAS routines are referenced by pdblas's solver
 // members (vcp/pdblas.hpp:159-376), which are off the GEMM path: they abort.
 void dsymm_(char*, char*, int*, int*, double*, const double*, int*, const double*, int*, double*,
             double*, int*) { unsupported("dsymm_"); }
 void dsyev_(char*, char*, int*, double*, int*, double*, double*, int*, int*) { unsupported("dsyev_"); }
 void dgesv_(int*, int*, double*, int*, int*, double*, int*, int*) { unsupported("dgesv_"); }
-void dsygv_(int*, char*, char*, int*, double*, int*, double*, int*, double*, double*, int*, int*) {
-  unsupported("dsygv_");
-}
 void dpotrf_(char*, int*, double*, int*, int*) { unsupported("dpotrf_"); }
 
 // The reference vblas entry point, unchanged.
@@ -306,6 +398,47 @@ int ref_imats_linearsolve(int n, int nrhs, const double* A, const double* b, dou
 }
 
 }  // extern "C"
+
+// imats<double, pidblas>::eigsymge (vcp/imats.hpp:419-522), run as is on A, B
+// (n x n kv): lam receives the n eigenvalue enclosures (the diagonal it
+// leaves), X, lambda and Y the approximate eigenvectors, eigenvalues and
+// inverse of mid(B X) it works with, formed the same way (imid,
+// pdblas::eigsymge, diag, pidblas::mul_im_m, imid, pdblas::inv).  Returns
+// 0, 2 when the reference throws vcp::verification_error, 1 otherwise.
+extern "C" int ref_imats_eigsymge(int n, const double* A, const double* B, double* lam,
+                                  double* X, double* lambda, double* Y) {
+  try {
+    pidblas_open a, b;
+    fill_iv(a, n, n, A);
+    fill_iv(b, n, n, B);
+    {
+      vcp::pdblas mA, mB, Xm, app, Ym;
+      a.imid(mA);
+      b.imid(mB);
+      mA.eigsymge(mB, Xm);
+      mA.diag(app);
+      pidblas_open bx;
+      b.mul_im_m(Xm, bx);
+      bx.imid(Ym);
+      Ym.inv();
+      for (long t = 0; t < (long)n * n; ++t) {
+        X[t] = Xm.v[t];
+        Y[t] = Ym.v[t];
+      }
+      for (int i = 0; i < n; ++i) lambda[i] = app.v[i];
+    }
+    a.eigsymge(b);
+    for (int i = 0; i < n; ++i) {
+      lam[2 * i] = a.v[i + (long)n * i].lower();
+      lam[2 * i + 1] = a.v[i + (long)n * i].upper();
+    }
+    return 0;
+  } catch (vcp::verification_error&) {
+    return 2;
+  } catch (...) {
+    return 1;
+  }
+}
 
 // vcp::save_portable / load_portable (vcp/vcp_portable_fio.hpp) of a
 // vcp::matrix of each element type, the data in flat element layouts

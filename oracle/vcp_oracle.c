@@ -669,6 +669,14 @@ static double rnd_op(int mode, double a, double b, char op) {
   fesetround(prev);
   return r;
 }
+static double rnd_op2(int mode, double a, double b) {
+  volatile double va = a, vb = b;
+  const int prev = fegetround();
+  fesetround(mode);
+  volatile double r = va * vb;
+  fesetround(prev);
+  return r;
+}
 static double kv_abs_sup(double lo, double up) {
   if (lo >= 0.0) return up;
   if (up <= 0.0) return -lo;
@@ -762,6 +770,164 @@ int orc_ilss_verify(int n, int nrhs, const double* A, const double* b, const dou
     x[2 * i] = rnd_op(FE_DOWNWARD, -u, mx[i], '+');
     x[2 * i + 1] = rnd_op(FE_UPWARD, u, mx[i], '+');
   }
+  free(buf);
+  return 0;
+}
+
+/* ---------------------------------------------------------------------------
+ * imats::eigsymge's verification (vcp/imats.hpp:419-522, Miyajima's
+ * enclosure of the eigenvalues of A x = lambda B x) given the approximate
+ * eigenvectors X and eigenvalues lambda of the midpoints and Y = inv(mid(B X)).
+ * The reference's products are of two kinds: on its pidblas matrices the
+ * pidblas hooks (midrad dgemm chains: [A] X, [B] X, Y [BX]); on its local
+ * imats objects the base class's loops in kv interval arithmetic:
+ *   R = Y C     imats::mul_m_im 'M' x 'M' (:203-213): c = 0; c += Y(i,j) * C(j,k)
+ *               for j ascending, each product the kv product of [y, y] and C(j,k)
+ *   |R| e       imats::mul_im_m 'M' x 'C' (:88-97): c = R(i,0); c = R(i,j) + c
+ * C_in, BX_in, R_in, S_in (kv, n x n), when given, replace [A] X, [B] X,
+ * Y C and Y [BX] (the tensor-core form's products).  lam (n kv) receives the
+ * enclosures after the overlap merge (merge = 1) or before it; *bound the
+ * sup of ||Y BX - I||.  Returns 0, or 2 when that bound is >= 1.
+ * ------------------------------------------------------------------------- */
+static void kv_mul_iv(double xl, double xu, double yl, double yu, double* lo, double* up) {
+  const double a[4] = {rnd_op2(FE_DOWNWARD, xl, yl), rnd_op2(FE_DOWNWARD, xl, yu),
+                       rnd_op2(FE_DOWNWARD, xu, yl), rnd_op2(FE_DOWNWARD, xu, yu)};
+  const double b[4] = {rnd_op2(FE_UPWARD, xl, yl), rnd_op2(FE_UPWARD, xl, yu),
+                       rnd_op2(FE_UPWARD, xu, yl), rnd_op2(FE_UPWARD, xu, yu)};
+  double l = a[0], u = b[0];
+  for (int c = 1; c < 4; ++c) {  /* std::min_element / max_element: first extreme */
+    if (a[c] < l) l = a[c];
+    if (u < b[c]) u = b[c];
+  }
+  *lo = l;
+  *up = u;
+}
+static void kv_abs_inplace(long count, double* X) {
+  for (long i = 0; i < count; ++i) {
+    const double lo = X[2 * i], up = X[2 * i + 1];
+    if (lo >= 0.0) continue;
+    if (up <= 0.0) {
+      X[2 * i] = -up;
+      X[2 * i + 1] = -lo;
+    } else {
+      X[2 * i] = 0.0;
+      X[2 * i + 1] = (-lo < up) ? up : -lo;
+    }
+  }
+}
+/* imats::mul_im_m 'M' x 'C' with the ones vector: interval row sums */
+static void kv_row_sums(int n, const double* X, double* out) {
+  for (int i = 0; i < n; ++i) {
+    double lo = X[2 * i], up = X[2 * i + 1];
+    for (int j = 1; j < n; ++j) {
+      const long o = i + (long)j * n;
+      lo = rnd_op(FE_DOWNWARD, X[2 * o], lo, '+');
+      up = rnd_op(FE_UPWARD, X[2 * o + 1], up, '+');
+    }
+    out[2 * i] = lo;
+    out[2 * i + 1] = up;
+  }
+}
+
+void orc_imats_mul_m_im_naive(int m, int n, int k, const double* Y, const double* C, double* R) {
+  /* R (m x n) = Y (m x k point) C (k x n kv), kv arithmetic, j ascending */
+  for (long t = 0; t < 2L * m * n; ++t) R[t] = 0.0;
+  for (int kk = 0; kk < n; ++kk)
+    for (int j = 0; j < k; ++j)
+      for (int i = 0; i < m; ++i) {
+        const double y = Y[i + (long)j * m];
+        const long cj = j + (long)kk * k, o = i + (long)kk * m;
+        double pl, pu;
+        kv_mul_iv(y, y, C[2 * cj], C[2 * cj + 1], &pl, &pu);
+        R[2 * o] = rnd_op(FE_DOWNWARD, R[2 * o], pl, '+');
+        R[2 * o + 1] = rnd_op(FE_UPWARD, R[2 * o + 1], pu, '+');
+      }
+}
+
+void orc_eig_merge(int n, double* lam) {
+  for (int i = 0; i < n; ++i) {
+    int j = 0;
+    for (;;) {
+      if (i != j) {
+        double *x = lam + 2 * i, *y = lam + 2 * j;
+        const int ov = x[0] <= y[1] && y[0] <= x[1];
+        if (ov && (x[0] != y[0] || x[1] != y[1])) {
+          x[0] = (y[0] < x[0]) ? y[0] : x[0];  /* std::min(x, y) = y < x ? y : x */
+          x[1] = (x[1] < y[1]) ? y[1] : x[1];  /* std::max(x, y) = x < y ? y : x */
+          y[0] = x[0];
+          y[1] = x[1];
+          j = 0;
+          continue;
+        }
+      }
+      if (++j == n) break;
+    }
+  }
+}
+
+int orc_ieigsymge(int n, const double* A, const double* B, const double* X, const double* lambda,
+                  const double* Y, const double* C_in, const double* BX_in, const double* R_in,
+                  const double* S_in, double* lam, double* bound, int merge, int nthreads) {
+  const long nn = (long)n * n;
+  double* buf = (double*)malloc(sizeof(double) * (8 * nn + 4 * n + n));
+  if (!buf) return 1;
+  double *C = buf, *BX = C + 2 * nn, *R = BX + 2 * nn, *S = R + 2 * nn, *Re = S + 2 * nn;
+  double *Se = Re + 2 * n, *e = Se + 2 * n;
+  for (int i = 0; i < n; ++i) e[i] = 1.0;
+  if (C_in) memcpy(C, C_in, sizeof(double) * 2 * nn);
+  else orc_pidblas_mul_point(0, n, n, n, A, X, C, nthreads);
+  if (BX_in) memcpy(BX, BX_in, sizeof(double) * 2 * nn);
+  else orc_pidblas_mul_point(0, n, n, n, B, X, BX, nthreads);
+  for (int j = 0; j < n; ++j)  /* C(i,j) -= BX(i,j) * [lambda_j, lambda_j] */
+    for (int i = 0; i < n; ++i) {
+      const long o = i + (long)j * n;
+      double pl, pu;
+      kv_mul_iv(BX[2 * o], BX[2 * o + 1], lambda[j], lambda[j], &pl, &pu);
+      const double lo = rnd_op(FE_DOWNWARD, C[2 * o], pu, '-');
+      const double up = rnd_op(FE_UPWARD, C[2 * o + 1], pl, '-');
+      C[2 * o] = lo;
+      C[2 * o + 1] = up;
+    }
+  if (R_in) memcpy(R, R_in, sizeof(double) * 2 * nn);
+  else orc_imats_mul_m_im_naive(n, n, n, Y, C, R);
+  const double Rinf = norminf_sup(n, n, R);
+  kv_abs_inplace(nn, R);
+  kv_row_sums(n, R, Re);
+  if (S_in) memcpy(S, S_in, sizeof(double) * 2 * nn);
+  else orc_pidblas_mul_point(1, n, n, n, Y, BX, S, nthreads);
+  for (int i = 0; i < n; ++i) {
+    const long o = i + (long)i * n;
+    const double lo = rnd_op(FE_DOWNWARD, S[2 * o], 1.0, '-');
+    const double up = rnd_op(FE_UPWARD, S[2 * o + 1], 1.0, '-');
+    S[2 * o] = lo;
+    S[2 * o + 1] = up;
+  }
+  const double Sinf = norminf_sup(n, n, S);
+  *bound = Sinf;
+  if (Sinf >= 1.0) {
+    free(buf);
+    return 2;
+  }
+  kv_abs_inplace(nn, S);
+  kv_row_sums(n, S, Se);
+  const double d_lo = rnd_op(FE_DOWNWARD, 1.0, Sinf, '-'), d_up = rnd_op(FE_UPWARD, 1.0, Sinf, '-');
+  const double q[4] = {rnd_op(FE_DOWNWARD, Rinf, d_lo, '/'), rnd_op(FE_DOWNWARD, Rinf, d_up, '/'),
+                       rnd_op(FE_DOWNWARD, Rinf, d_lo, '/'), rnd_op(FE_DOWNWARD, Rinf, d_up, '/')};
+  const double u4[4] = {rnd_op(FE_UPWARD, Rinf, d_lo, '/'), rnd_op(FE_UPWARD, Rinf, d_up, '/'),
+                        rnd_op(FE_UPWARD, Rinf, d_lo, '/'), rnd_op(FE_UPWARD, Rinf, d_up, '/')};
+  double g_lo = q[0], g_up = u4[0];
+  for (int c = 1; c < 4; ++c) {
+    if (q[c] < g_lo) g_lo = q[c];
+    if (g_up < u4[c]) g_up = u4[c];
+  }
+  for (int i = 0; i < n; ++i) {
+    double sl, su;
+    kv_mul_iv(g_lo, g_up, Se[2 * i], Se[2 * i + 1], &sl, &su);  /* Se.mulsm(g): g * Se_i */
+    const double u = rnd_op(FE_UPWARD, Re[2 * i + 1], su, '+');   /* Re.addmm(Se), sup */
+    lam[2 * i] = rnd_op(FE_DOWNWARD, -u, lambda[i], '+');
+    lam[2 * i + 1] = rnd_op(FE_UPWARD, u, lambda[i], '+');
+  }
+  if (merge) orc_eig_merge(n, lam);
   free(buf);
   return 0;
 }

@@ -136,6 +136,26 @@ def main() -> None:
         data[f"ls{idx}_status"] = np.array([st])
         data[f"ls{idx}_bound"] = np.array([g.value])
     data["n_ls"] = np.array([len(lcases)])
+    # imats<double, pidblas>::eigsymge (own seed): A, B symmetric, mid B
+    # positive definite; the X, lambda, Y it works with and its enclosures
+    rng4 = np.random.default_rng(20261207)
+    gcases = [(2, 2.0 ** -30), (6, 2.0 ** -40), (17, 2.0 ** -30), (40, 2.0 ** -24)]
+    for idx, (n, rel) in enumerate(gcases):
+        Am = rng4.standard_normal((n, n))
+        Am = (Am + Am.T) / 2
+        Bm = np.eye(n) + 0.1 * rng4.standard_normal((n, n))
+        Bm = Bm @ Bm.T
+        A = W._kv(Am.ravel(order="F"), np.abs(Am.ravel(order="F")) * rel)
+        B = W._kv(Bm.ravel(order="F"), np.abs(Bm.ravel(order="F")) * rel)
+        st, lam, X, lmb, Y = O.ref_imats_eigsymge(n, A, B)
+        assert st == 0
+        _, _, bound = O.ieigsymge(n, A, B, X, lmb, Y)
+        data[f"ge{idx}_n"] = np.array([n])
+        data[f"ge{idx}_A"], data[f"ge{idx}_B"] = A, B
+        data[f"ge{idx}_X"], data[f"ge{idx}_lambda"], data[f"ge{idx}_Y"] = X, lmb, Y
+        data[f"ge{idx}_lam"] = lam
+        data[f"ge{idx}_bound"] = np.array([bound])
+    data["n_ge"] = np.array([len(gcases)])
     data["n_fm"] = np.array([len(fcases)])
     data["n_mp"] = np.array([len(pcases)])
     data["n_sy"] = np.array([2])

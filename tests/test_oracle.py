@@ -311,3 +311,39 @@ def _rational_solve(M, b):
                 f = a[r][c] / a[c][c]
                 a[r] = [x - f * y for x, y in zip(a[r], a[c])]
     return [a[i][n] / a[i][i] for i in range(n)]
+
+
+def test_oracle_eigsymge_matches_golden(oracle, golden):
+    """imats::eigsymge's verification (restated) on the reference's own X,
+    lambda, Y: every bit of the merged enclosures."""
+    for idx in range(int(golden["n_ge"][0])):
+        n = int(golden[f"ge{idx}_n"][0])
+        st, lam, bound = oracle.ieigsymge(n, golden[f"ge{idx}_A"], golden[f"ge{idx}_B"],
+                                          golden[f"ge{idx}_X"], golden[f"ge{idx}_lambda"],
+                                          golden[f"ge{idx}_Y"])
+        assert st == 0 and bound == float(golden[f"ge{idx}_bound"][0]), idx
+        assert np.array_equal(bits(lam), bits(golden[f"ge{idx}_lam"])), idx
+
+
+def test_oracle_eigsymge_matches_reference_build(oracle):
+    """Live: the reference's imats<double, pidblas>::eigsymge (project-written
+    dsygv for its LAPACK call) against the restatement on its X, lambda, Y,
+    including its base-class kv loops and the overlap merge."""
+    if oracle.ref_lib() is None:
+        from oracle.build import build_reference
+        if build_reference() is None:
+            pytest.skip("reference sources not mounted")
+    rng = np.random.default_rng(41)
+    for n, rel in [(3, 2.0 ** -30), (9, 2.0 ** -20), (25, 2.0 ** -36), (33, 2.0 ** -10)]:
+        Am = rng.standard_normal((n, n))
+        Am = (Am + Am.T) / 2
+        if n == 9:  # a repeated eigenvalue: overlapping enclosures get merged
+            Am = np.diag(np.repeat([1.0, 2.0, 3.0], 3))
+        Bm = np.eye(n) + 0.05 * rng.standard_normal((n, n))
+        Bm = Bm @ Bm.T
+        A = W._kv(Am.ravel(order="F"), np.abs(Am.ravel(order="F")) * rel)
+        B = W._kv(Bm.ravel(order="F"), np.abs(Bm.ravel(order="F")) * rel)
+        st, lam_r, X, lmb, Y = oracle.ref_imats_eigsymge(n, A, B)
+        st2, lam_o, _ = oracle.ieigsymge(n, A, B, X, lmb, Y)
+        assert st == st2 == 0, n
+        assert np.array_equal(bits(lam_o), bits(lam_r)), n

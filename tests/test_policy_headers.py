@@ -48,8 +48,19 @@ void dgetri_(int* n, double*, int*, int*, double* work, int* lwork, int* info) {
 }
 void dsyev_(char*, char*, int*, double*, int*, double*, double*, int*, int*) { std::abort(); }
 void dgesv_(int*, int*, double*, int*, int*, double*, int*, int*) { std::abort(); }
-void dsygv_(int*, char*, char*, int*, double*, int*, double*, int*, double*, double*, int*,
-            int*) { std::abort(); }
+void dsygv_(int*, char*, char*, int* n, double* A, int*, double*, int*, double* W, double* work,
+            int* lwork, int* info) {  // W = diag(A), X = I
+  *info = 0;
+  if (*lwork == -1) {
+    work[0] = 1;
+    return;
+  }
+  for (int i = 0; i < *n; ++i)
+    for (int j = 0; j < *n; ++j) {
+      if (i == j) W[i] = A[i + *n * i];
+      A[i + *n * j] = i == j ? 1.0 : 0.0;
+    }
+}
 void dpotrf_(char*, int*, double*, int*, int*) { std::abort(); }
 }
 
@@ -100,6 +111,21 @@ int main() {
     std::printf("STATE_ERROR lss: %s\n", e.what());
     ++errors;
   }
+  try {
+    M S, T;
+    S.zeros(3, 3);
+    T.zeros(3, 3);
+    for (int i = 0; i < 3; ++i) {
+      S.data()[4 * i] = I(1.0 + i);
+      T.data()[4 * i] = I(1.0);
+    }
+    M E;
+    eigsymge(S, T, E);                    // pidcuda::eigsymge -> vcpcu_ieigsymge
+    std::printf("NO_ERROR eigsymge\n");
+  } catch (vcp::state_error& e) {
+    std::printf("STATE_ERROR eigsymge: %s\n", e.what());
+    ++errors;
+  }
   std::fflush(stdout);
   double a[4] = {1, 2, 3, 4}, b[4] = {1, 0, 0, 1}, c[4];
   try {
@@ -109,7 +135,7 @@ int main() {
     std::printf("RUNTIME_ERROR rmatmul: %s\n", e.what());
     ++errors;
   }
-  return errors == 5 ? 0 : 1;
+  return errors == 6 ? 0 : 1;
 }
 '''
 
@@ -137,6 +163,7 @@ def test_policy_headers_compile_link_and_map_errors(tmp_path, cuda_lib):
     assert "STATE_ERROR mulmm" in run.stdout and "STATE_ERROR mulltmm" in run.stdout
     assert "STATE_ERROR mulmm_fma" in run.stdout
     assert "STATE_ERROR lss" in run.stdout
+    assert "STATE_ERROR eigsymge" in run.stdout
     assert "RUNTIME_ERROR rmatmul" in run.stdout
 
 

@@ -43,6 +43,10 @@ SIGNATURES: dict[str, tuple] = {
     "vcpcu_ilss_verify_dev": (_i, [_i, _i, _v, _i, _v, _i, _v, _i, _v, _i, _v, _i, _v, _i, _i,
                                    _v]),
     "vcpcu_ilss_verify": (_i, [_i, _i, _v, _v, _v, _v, _v, _v, _i, _i]),
+    "vcpcu_ieigsymge_stage1_dev": (_i, [_i, _v, _i, _v, _i, _v, _i, _v, _v, _v, _i, _i, _v]),
+    "vcpcu_ieigsymge_stage2_dev": (_i, [_i, _v, _v, _i, _v, _v, _v, _v, _i, _i, _v]),
+    "vcpcu_eig_merge": (_i, [_i, _v]),
+    "vcpcu_ieigsymge": (_i, [_i, _v, _v, _v, _v, _v, _v, _v, _v, _i, _i]),
     "vcpcu_vcpmat_save": (_i, [C.c_char_p, _i, _i, _i, _v]),
     "vcpcu_vcpmat_info": (_i, [C.c_char_p, _v, _v, _v]),
     "vcpcu_vcpmat_load": (_i, [C.c_char_p, _i, _i, _i, _v]),

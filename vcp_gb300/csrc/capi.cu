@@ -1,5 +1,7 @@
 // capi.cu -- the exported C ABI (include/vcpcuda.h): argument checks,
 // host<->device staging for the host-pointer entry points, dispatch.
+#include <vector>
+
 #include "common.cuh"
 #include "plain_gemm.cuh"
 #include "ozaki.cuh"
@@ -666,6 +668,110 @@ int vcpcu_ilss_verify(int n, int nrhs, const double* A, const double* b, const d
     set_error("ilss_verify: ||RA - I|| <= %.17g is not below 1", *bound);
     return VCPCU_ERR_VERIFY;
   }
+  return VCPCU_OK;
+}
+
+int vcpcu_ieigsymge_stage1_dev(int n, const double* A, int lda, const double* B, int ldb,
+                               const double* X, int ldx, double* C, double* BX, double* midBX,
+                               int form, int slices, void* stream) {
+  clear_error();
+  int st = form_check(form, slices);
+  if (st) return st;
+  if (n <= 0 || !A || !B || !X || !C || !BX || !midBX || lda < n || ldb < n || ldx < n) {
+    set_error("ieigsymge: n must be positive, pointers non-null, ld >= n");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (misaligned16(C) || misaligned16(BX) ||
+      (form != VCPCU_FORM_PLAIN && (misaligned16(A) || misaligned16(B)))) {
+    set_error("ieigsymge: interval arrays must be 16-byte aligned");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  return ieig_stage1_dispatch(n, A, lda, B, ldb, X, ldx, C, BX, midBX, form, slices,
+                              (cudaStream_t)stream);
+}
+
+int vcpcu_ieigsymge_stage2_dev(int n, const double* lambda, const double* Y, int ldy, double* C,
+                               const double* BX, double* lam, double* bound, int form,
+                               int slices, void* stream) {
+  clear_error();
+  int st = form_check(form, slices);
+  if (st) return st;
+  if (n <= 0 || !lambda || !Y || !C || !BX || !lam || !bound || ldy < n) {
+    set_error("ieigsymge: n must be positive, pointers non-null, ldy >= n");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (misaligned16(C) || misaligned16(BX) || misaligned16(lam)) {
+    set_error("ieigsymge: interval arrays must be 16-byte aligned");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  return ieig_stage2_dispatch(n, lambda, Y, ldy, C, BX, lam, bound, form, slices,
+                              (cudaStream_t)stream);
+}
+
+int vcpcu_eig_merge(int n, double* lam) {
+  clear_error();
+  if (n < 0 || (n > 0 && !lam)) {
+    set_error("eig_merge: n must be non-negative and lam non-null");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  eig_merge_host(n, lam);
+  return VCPCU_OK;
+}
+
+int vcpcu_ieigsymge(int n, const double* A, const double* B, const double* X,
+                    const double* lambda, vcpcu_inverse_fn inv, void* ctx, double* lam,
+                    double* bound, int form, int slices) {
+  clear_error();
+  int st = form_check(form, slices);
+  if (st) return st;
+  if (n <= 0 || !A || !B || !X || !lambda || !inv || !lam || !bound) {
+    set_error("ieigsymge: n must be positive and pointers non-null");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = check_device())) return st;
+  cudaStream_t s = host_stream();
+  const size_t nn = (size_t)n * n;
+  // interval arrays first (16-byte aligned): A, B, C, BX (2 nn each), lam (2 n);
+  // then X, mid(BX) / Y (nn each), lambda (n), the bound (1)
+  const size_t oB = 2 * nn, oC = 4 * nn, oBX = 6 * nn, oLam = 8 * nn, oX = oLam + 2 * (size_t)n,
+               oM = oX + nn, oL = oM + nn, oG = oL + n, total = oG + 1;
+  Scratch buf;
+  if ((st = buf.alloc(sizeof(double) * total, s))) return st;
+  double* dA = (double*)buf.ptr;
+  double* dB = dA + oB;
+  double* dC = dA + oC;
+  double* dBX = dA + oBX;
+  double* dlam = dA + oLam;
+  double* dX = dA + oX;
+  double* dM = dA + oM;  // mid(BX), then Y
+  double* dl = dA + oL;
+  double* dG = dA + oG;
+  if ((st = h2d(dA, A, 2 * nn, s)) || (st = h2d(dB, B, 2 * nn, s)) || (st = h2d(dX, X, nn, s)) ||
+      (st = h2d(dl, lambda, n, s)))
+    return st;
+  if ((st = ieig_stage1_dispatch(n, dA, n, dB, n, dX, n, dC, dBX, dM, form, slices, s))) return st;
+  std::vector<double> M(nn);
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(M.data(), dM, nn * sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  if (form != VCPCU_FORM_PLAIN && (st = take_status())) return st;
+  if (inv(n, M.data(), ctx) != 0) {
+    set_error("ieigsymge: the caller's inverse of mid(B X) failed");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if ((st = h2d(dM, M.data(), nn, s))) return st;
+  if ((st = ieig_stage2_dispatch(n, dl, dM, n, dC, dBX, dlam, dG, form, slices, s))) return st;
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(lam, dlam, 2 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                                 s));
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(bound, dG, sizeof(double), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  if (form != VCPCU_FORM_PLAIN && (st = take_status())) return st;
+  if (*bound >= 1.0) {
+    set_error("ieigsymge: ||Y B X - I|| <= %.17g is not below 1", *bound);
+    return VCPCU_ERR_VERIFY;
+  }
+  eig_merge_host(n, lam);
   return VCPCU_OK;
 }
 

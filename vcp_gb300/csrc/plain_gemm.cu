@@ -302,6 +302,97 @@ interval_gemm_kernel(int M, int N, int K, const double* __restrict__ mA,
     }
 }
 
+// R = Y [C] with imats::mul_m_im's own loop (vcp/imats.hpp:203-213), the
+// product the base class runs on its local interval matrices (imats::eigsymge
+// forms R = Y (A X - B X Lambda) with it): per entry c = [0, 0], then
+// c = c + [y, y] * C(j, k) for j ascending, every step with kv's interval
+// operations -- the product as the first smallest of RD(y cl), RD(y cu) and
+// the first largest of RU(y cl), RU(y cu) (std::min_element / max_element
+// over kv's four candidates), the sum rounded outward.  Eight FP64
+// operations per term.  Padding terms are [+0, +0] and leave c unchanged.
+__global__ void __launch_bounds__(NT)
+imats_mulmm_kernel(int M, int N, int K, const double* __restrict__ Y, long ldy,
+                   const double* __restrict__ C, long ldc, double* __restrict__ R, long ldr) {
+  __shared__ double Ys[2][BKI][BM], Cl[2][BKI][BN], Cu[2][BKI][BN];
+  const int tid = threadIdx.x;
+  const int tr = tid / 16, tc = tid % 16;
+  const int row0 = blockIdx.x * BM, col0 = blockIdx.y * BN;
+  const int a_i = tid % BM, a_k = tid / BM;
+  const int b_k = tid % BKI, b_j = tid / BKI;
+  constexpr int QA = BKI / (NT / BM), QB = BN / (NT / BKI);
+  double lo[4][4], up[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) lo[i][j] = up[i][j] = 0.0;
+  double ry[QA], rl[QB], ru[QB];
+  auto load_tile = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < QA; ++q) {
+      const int gi = row0 + a_i, gk = k0 + a_k + (NT / BM) * q;
+      ry[q] = (gi < M && gk < K) ? Y[gi + (long)gk * ldy] : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < QB; ++q) {
+      const int hk = k0 + b_k, hj = col0 + b_j + (NT / BKI) * q;
+      const bool ok = hk < K && hj < N;
+      const double* e = C + 2 * (hk + (long)hj * ldc);
+      rl[q] = ok ? e[0] : 0.0;
+      ru[q] = ok ? e[1] : 0.0;
+    }
+  };
+  auto store_tile = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < QA; ++q) Ys[buf][a_k + (NT / BM) * q][a_i] = ry[q];
+#pragma unroll
+    for (int q = 0; q < QB; ++q) {
+      Cl[buf][b_k][b_j + (NT / BKI) * q] = rl[q];
+      Cu[buf][b_k][b_j + (NT / BKI) * q] = ru[q];
+    }
+  };
+  const int nk = (K + BKI - 1) / BKI;
+  load_tile(0);
+  store_tile(0);
+  __syncthreads();
+  for (int t = 0; t < nk; ++t) {
+    const int buf = t & 1;
+    if (t + 1 < nk) load_tile((t + 1) * BKI);
+#pragma unroll 2
+    for (int kk = 0; kk < BKI; ++kk) {
+      double y[4], cl[4], cu[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) y[i] = Ys[buf][kk][tr + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        cl[j] = Cl[buf][kk][tc + 16 * j];
+        cu[j] = Cu[buf][kk][tc + 16 * j];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const double p1 = __dmul_rd(y[i], cl[j]), p2 = __dmul_rd(y[i], cu[j]);
+          const double q1 = __dmul_ru(y[i], cl[j]), q2 = __dmul_ru(y[i], cu[j]);
+          lo[i][j] = __dadd_rd(lo[i][j], p2 < p1 ? p2 : p1);
+          up[i][j] = __dadd_ru(up[i][j], q1 < q2 ? q2 : q1);
+        }
+    }
+    if (t + 1 < nk) store_tile(buf ^ 1);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gi = row0 + tr + 16 * i, gj = col0 + tc + 16 * j;
+      if (gi < M && gj < N) {
+        double* e = R + 2 * (gi + (long)gj * ldr);
+        e[0] = lo[i][j];
+        e[1] = up[i][j];
+      }
+    }
+}
+
 // [A]ᵀ[A] with pidblas::mulltmm semantics (vcp/pidblas.hpp:296-358) over
 // prepped planes: X = Aᵀ (n x k: mX, aX = |mX|, rX), Y = A (k x n: mY, rY).
 // Five chains per entry (i, j):
@@ -675,6 +766,15 @@ int launch_isyrk_plain(int N, int K, const double* A, long lda, double* C, long 
 }
 
 size_t isyrk_plain_ws_bytes(int N, int K) { return sizeof(double) * 7 * (size_t)N * K; }
+
+int launch_imats_mulmm(int M, int N, int K, const double* Y, long ldy, const double* C, long ldc,
+                       double* R, long ldr, cudaStream_t s) {
+  if (M <= 0 || N <= 0) return VCPCU_OK;
+  dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
+  imats_mulmm_kernel<<<grid, NT, 0, s>>>(M, N, K > 0 ? K : 0, Y, ldy, C, ldc, R, ldr);
+  VCPCU_LAUNCH_CHECK("imats_mulmm_kernel");
+  return VCPCU_OK;
+}
 
 size_t interval_gemm_plain_ws_bytes(int M, int N, int K) {
   if (N <= kThinN) return interval_gemm_thin_ws_bytes(M, N, K, false);

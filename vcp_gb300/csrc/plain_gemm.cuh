@@ -32,6 +32,11 @@ int launch_interval_gemm_thin(int M, int N, int K, const double* A, long lda, bo
                               double* ws, cudaStream_t s);
 size_t interval_gemm_thin_ws_bytes(int M, int N, int K, bool a_point);
 
+// R (M x N) = Y (M x K point) [C] (K x N kv) with imats::mul_m_im's loop
+// (vcp/imats.hpp:203-213): kv interval products and sums term by term.
+int launch_imats_mulmm(int M, int N, int K, const double* Y, long ldy, const double* C, long ldc,
+                       double* R, long ldr, cudaStream_t s);
+
 // C = [A]ᵀ[A] (A K x N interval) with pidblas::mulltmm semantics, full
 // symmetric output; ws holds isyrk_plain_ws_bytes(N, K).
 int launch_isyrk_plain(int N, int K, const double* A, long lda, double* C, long ldc, double* ws,

@@ -96,6 +96,7 @@ __device__ __forceinline__ double abs_sup(double lo, double up) { return sw_abs_
 // row; a warp reads 32 consecutive rows of one column).  The sums are
 // sequential chains, so there are only n threads: each keeps two groups of
 // PF columns in flight ahead of its additions.
+template <bool SHIFT = true>
 __global__ void norm_rows(int n, const double* __restrict__ C, long ldc,
                           double* __restrict__ rows) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -116,7 +117,7 @@ __global__ void norm_rows(int n, const double* __restrict__ C, long ldc,
   for (int jb = 0; jb < n; jb += PF) {
 #pragma unroll
     for (int p = 0; p < PF; ++p) nxt[p] = load(jb + PF + p);
-    if (jb + PF <= i0 || jb >= i0 + 32) {
+    if (!SHIFT || jb + PF <= i0 || jb >= i0 + 32) {
 #pragma unroll
       for (int p = 0; p < PF; ++p) {
         const int j = jb + p;
@@ -406,14 +407,15 @@ __global__ void lss_scale(const double* __restrict__ G, const double* __restrict
   g[1] = up;
 }
 
-// E(i, i) -= 1 (interval minus point), then E -> kv abs(E), in place.
+// E(i, i) -= 1 (interval minus point; SHIFT), then E -> kv abs(E), in place.
+template <bool SHIFT = true>
 __global__ void abs_shift(int n, double* __restrict__ E) {
   const long total = (long)n * n;
   for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (long)gridDim.x * blockDim.x) {
     const long i = idx % n, j = idx / n;
     double2 e = reinterpret_cast<const double2*>(E)[idx];
-    if (i == j) {
+    if (SHIFT && i == j) {
       e.x = __dsub_rd(e.x, 1.0);
       e.y = __dsub_ru(e.y, 1.0);
     }
@@ -447,6 +449,190 @@ __global__ void lss_final(int rows, int cols, const double* __restrict__ r,
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// The verification of imats::eigsymge (vcp/imats.hpp:419-522, Miyajima's
+// eigenvalue enclosure for A x = lambda B x) around the caller's approximate
+// eigenpairs (X, lambda) of the midpoints and its approximate inverse
+// Y = inv(mid(B X)):
+//   stage 1   C = [A] X, BX = [B] X (pidblas::mul_im_m, :430-435), mid(BX)
+//   stage 2   C = C - BX (lambda ... lambda)              (:440-445)
+//             R = Y C (the base class's kv loop, :448), Rinf = ||R||, Re = |R| e
+//             S = Y BX - I (pidblas::mul_m_im, :458-462), Sinf = ||S||, Se = |S| e
+//             g = Rinf / (1 - Sinf); lam = lambda + [-u, u], u = sup(Re + g Se)
+// with kv's operation at every step.  In the plain form R = Y C runs the base
+// class's term-by-term loop (imats_mulmm_kernel), so all bits are the
+// reference's; the tensor-core form encloses it by the CRT product.
+namespace {
+
+// kv midpoints of an interval matrix (count entries), integer pipe.
+__global__ void mid_of(long count, const double* __restrict__ X, double* __restrict__ M) {
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < count;
+       idx += (long)gridDim.x * blockDim.x) {
+    const double2 e = reinterpret_cast<const double2*>(X)[idx];
+    double m, r, p;
+    sw_midrad(e.x, e.y, m, r, p);
+    M[idx] = m;
+  }
+}
+
+// kv's product of intervals x * y: the first smallest of the four round-down
+// products and the first largest of the four round-up ones (std::min_element
+// / max_element over x.inf y.inf, x.inf y.sup, x.sup y.inf, x.sup y.sup).
+__device__ __forceinline__ void kv_mul_iv(double xl, double xu, double yl, double yu, double& lo,
+                                          double& up) {
+  const double a[4] = {__dmul_rd(xl, yl), __dmul_rd(xl, yu), __dmul_rd(xu, yl),
+                       __dmul_rd(xu, yu)};
+  const double b[4] = {__dmul_ru(xl, yl), __dmul_ru(xl, yu), __dmul_ru(xu, yl),
+                       __dmul_ru(xu, yu)};
+  lo = a[0];
+  up = b[0];
+#pragma unroll
+  for (int c = 1; c < 4; ++c) {
+    if (a[c] < lo) lo = a[c];
+    if (up < b[c]) up = b[c];
+  }
+}
+
+// C(i, j) -= BX(i, j) * [lambda_j, lambda_j] (kv product, kv subtraction).
+__global__ void sub_lambda(int n, double* __restrict__ C, const double* __restrict__ BX,
+                           const double* __restrict__ lambda) {
+  const long total = (long)n * n;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    const double l = lambda[idx / n];
+    const double2 b = reinterpret_cast<const double2*>(BX)[idx];
+    const double2 c = reinterpret_cast<const double2*>(C)[idx];
+    // [l, l] is the second factor: x.inf y.inf, x.inf y.sup, x.sup y.inf, ...
+    const double p1 = __dmul_rd(b.x, l), p3 = __dmul_rd(b.y, l);
+    const double q1 = __dmul_ru(b.x, l), q3 = __dmul_ru(b.y, l);
+    const double pl = p3 < p1 ? p3 : p1, pu = q1 < q3 ? q3 : q1;
+    reinterpret_cast<double2*>(C)[idx] = make_double2(__dsub_rd(c.x, pu), __dsub_ru(c.y, pl));
+  }
+}
+
+// imats::mul_im_m 'M' x 'C' with the ones vector (vcp/imats.hpp:88-97): per row
+// c = X(i, 0), then c = X(i, j) + c outward, j ascending.
+__global__ void iv_row_sums(int n, const double* __restrict__ X, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  constexpr int PF = 16;
+  const double2* x2 = reinterpret_cast<const double2*>(X);
+  auto load = [&](int j) -> double2 { return j < n ? x2[i + (long)j * n] : make_double2(0.0, 0.0); };
+  double2 cur[PF], nxt[PF];
+#pragma unroll
+  for (int p = 0; p < PF; ++p) cur[p] = load(p);
+  double lo = 0.0, up = 0.0;
+  for (int jb = 0; jb < n; jb += PF) {
+#pragma unroll
+    for (int p = 0; p < PF; ++p) nxt[p] = load(jb + PF + p);
+#pragma unroll
+    for (int p = 0; p < PF; ++p) {
+      const int j = jb + p;
+      if (j < n) {
+        lo = j == 0 ? cur[p].x : __dadd_rd(cur[p].x, lo);
+        up = j == 0 ? cur[p].y : __dadd_ru(cur[p].y, up);
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < PF; ++p) cur[p] = nxt[p];
+  }
+  out[2 * i] = lo;
+  out[2 * i + 1] = up;
+}
+
+// lam_i = lambda_i + [-u, u], u = RU(sup Re_i + sup(g * Se_i)) (mulsm, addmm and
+// the symmetric widening of vcp/imats.hpp:488-499); g = sc[0..1].
+__global__ void eig_final(int n, const double* __restrict__ Re, const double* __restrict__ Se,
+                          const double* __restrict__ g, const double* __restrict__ lambda,
+                          double* __restrict__ lam) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double sl, su;
+  kv_mul_iv(g[0], g[1], Se[2 * i], Se[2 * i + 1], sl, su);
+  const double u = __dadd_ru(Re[2 * i + 1], su);
+  lam[2 * i] = __dadd_rd(-u, lambda[i]);
+  lam[2 * i + 1] = __dadd_ru(u, lambda[i]);
+}
+
+}  // namespace
+
+int ieig_stage1_dispatch(int n, const double* A, long lda, const double* B, long ldb,
+                         const double* X, long ldx, double* C, double* BX, double* M, int form,
+                         int slices, cudaStream_t s) {
+  int st;
+  if ((st = igemm_point_dispatch(0, n, n, n, A, lda, X, ldx, C, n, form, slices, s))) return st;
+  if ((st = igemm_point_dispatch(0, n, n, n, B, ldb, X, ldx, BX, n, form, slices, s))) return st;
+  mid_of<<<grid1((long)n * n), 256, 0, s>>>((long)n * n, BX, M);
+  VCPCU_LAUNCH_CHECK("mid_of");
+  return VCPCU_OK;
+}
+
+int ieig_stage2_dispatch(int n, const double* lambda, const double* Y, long ldy, double* C,
+                         const double* BX, double* lam, double* bound, int form, int slices,
+                         cudaStream_t s) {
+  const size_t nn = 2 * (size_t)n * n;
+  Scratch ws;
+  int st = ws.alloc(sizeof(double) * (nn + 5 * (size_t)n + 8), s);
+  if (st) return st;
+  double* P = (double*)ws.ptr;  // R, then S
+  double* Re = P + nn;
+  double* Se = Re + 2 * n;
+  double* rows = Se + 2 * n;
+  double* sc = rows + n;  // Rinf, g_lo, g_up
+  sub_lambda<<<grid1((long)n * n), 256, 0, s>>>(n, C, BX, lambda);
+  VCPCU_LAUNCH_CHECK("sub_lambda");
+  if (form == VCPCU_FORM_PLAIN)
+    st = launch_imats_mulmm(n, n, n, Y, ldy, C, n, P, n, s);
+  else
+    st = igemm_point_dispatch(1, n, n, n, Y, ldy, C, n, P, n, form, slices, s);
+  if (st) return st;
+  norm_rows<false><<<(n + 127) / 128, 128, 0, s>>>(n, P, n, rows);
+  VCPCU_LAUNCH_CHECK("norm_rows");
+  max_last<<<1, 256, 0, s>>>(n, rows, sc);
+  VCPCU_LAUNCH_CHECK("max_last");
+  abs_shift<false><<<grid1((long)n * n), 256, 0, s>>>(n, P);
+  VCPCU_LAUNCH_CHECK("abs_shift");
+  iv_row_sums<<<(n + 127) / 128, 128, 0, s>>>(n, P, Re);
+  VCPCU_LAUNCH_CHECK("iv_row_sums");
+  if ((st = igemm_point_dispatch(1, n, n, n, Y, ldy, BX, n, P, n, form, slices, s))) return st;
+  norm_rows<true><<<(n + 127) / 128, 128, 0, s>>>(n, P, n, rows);
+  VCPCU_LAUNCH_CHECK("norm_rows");
+  max_last<<<1, 256, 0, s>>>(n, rows, bound);
+  VCPCU_LAUNCH_CHECK("max_last");
+  abs_shift<true><<<grid1((long)n * n), 256, 0, s>>>(n, P);
+  VCPCU_LAUNCH_CHECK("abs_shift");
+  iv_row_sums<<<(n + 127) / 128, 128, 0, s>>>(n, P, Se);
+  VCPCU_LAUNCH_CHECK("iv_row_sums");
+  lss_scale<<<1, 1, 0, s>>>(bound, sc, sc + 1);  // g = [Rinf, Rinf] / (1 - [Sinf, Sinf])
+  VCPCU_LAUNCH_CHECK("lss_scale");
+  eig_final<<<(n + 127) / 128, 128, 0, s>>>(n, Re, Se, sc + 1, lambda, lam);
+  VCPCU_LAUNCH_CHECK("eig_final");
+  return VCPCU_OK;
+}
+
+// The overlap merge of imats::eigsymge (vcp/imats.hpp:502-519), on the host.
+void eig_merge_host(int n, double* lam) {
+  for (int i = 0; i < n; ++i) {
+    int j = 0;
+    for (;;) {
+      if (i != j) {
+        double* x = lam + 2 * i;
+        double* y = lam + 2 * j;
+        const bool ov = x[0] <= y[1] && y[0] <= x[1];
+        if (ov && (x[0] != y[0] || x[1] != y[1])) {
+          x[0] = y[0] < x[0] ? y[0] : x[0];
+          x[1] = x[1] < y[1] ? y[1] : x[1];
+          y[0] = x[0];
+          y[1] = x[1];
+          j = 0;
+          continue;
+        }
+      }
+      if (++j == n) break;
+    }
+  }
+}
 
 int ilss_thin_form(int form, int nrhs) {
   return (form == VCPCU_FORM_PLAIN || nrhs <= kLssPlainRhs) ? VCPCU_FORM_PLAIN : form;

@@ -35,10 +35,22 @@ int norm_dispatch(int n, const double* R, long ldr, const double* A, long lda, d
 // run in the plain form when nrhs <= kLssPlainRhs (FP64 thin kernel: faster
 // there than padding nrhs to a 256-column tensor-core tile, and tighter).
 constexpr int kLssPlainRhs = 4;
+
 int ilss_thin_form(int form, int nrhs);
 int ilss_verify_dispatch(int n, int nrhs, const double* A, long lda, const double* b, long ldb,
                          const double* R, long ldr, const double* mx, long ldmx, double* x,
                          long ldx, double* bound, int form, int slices, cudaStream_t s);
+
+// The verification of imats::eigsymge in two device stages around the
+// caller's inverse of mid(B X) (variants.cu); eig_merge_host is its final
+// overlap merge.
+int ieig_stage1_dispatch(int n, const double* A, long lda, const double* B, long ldb,
+                         const double* X, long ldx, double* C, double* BX, double* M, int form,
+                         int slices, cudaStream_t s);
+int ieig_stage2_dispatch(int n, const double* lambda, const double* Y, long ldy, double* C,
+                         const double* BX, double* lam, double* bound, int form, int slices,
+                         cudaStream_t s);
+void eig_merge_host(int n, double* lam);
 
 // ifma.cu: elementwise inf-sup interval FMA and the ifma-chain product.
 int launch_ifma(long count, const double* A, const double* B, const double* C, double* R,

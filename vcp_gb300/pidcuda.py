@@ -142,6 +142,74 @@ def linearsolve_verify_dev(n, nrhs, A, lda, b, ldb, R, ldr, mx, ldmx, x, ldx, bo
               _dev_ptr(bound, "bound"), int(form), int(slices), _stream_ptr(stream))
 
 
+_INVERSE_FN = None
+
+
+def _inverse_fn_type():
+    global _INVERSE_FN
+    if _INVERSE_FN is None:
+        import ctypes
+        _INVERSE_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.c_void_p)
+    return _INVERSE_FN
+
+
+def eigsymge_verify(A: np.ndarray, B: np.ndarray, X: np.ndarray, lam: np.ndarray, n: int,
+                    inverse=None, form: int = FORM_PLAIN, slices: int = 0,
+                    check: bool = True) -> tuple[np.ndarray, float]:
+    """The verification of imats::eigsymge (vcp/imats.hpp:419-522) around the
+    approximate eigenvectors X (n x n, column-major) and eigenvalues lam of
+    mid(A) x = lam mid(B) x: returns (kv buffer of the n merged eigenvalue
+    enclosures, sup ||Y B X - I||).  ``inverse(M)`` turns mid(B X) (n x n
+    numpy array) into Y ~ inv(mid(B X)) (default numpy.linalg.inv).  With
+    check, a bound >= 1 raises VerificationError as the reference throws."""
+    import ctypes
+    inv = np.linalg.inv if inverse is None else inverse
+
+    def cb(nn, ptr, _ctx):
+        try:
+            M = np.ctypeslib.as_array(ptr, shape=(nn * nn,))
+            Y = np.asarray(inv(M.reshape(nn, nn, order="F").copy()), dtype=np.float64)
+            M[:] = Y.ravel(order="F")
+            return 0
+        except Exception:
+            return 1
+
+    fn = _inverse_fn_type()(cb)
+    out = np.empty(2 * n, dtype=np.float64)
+    g = ctypes.c_double(0.0)
+    lib = _lib.load()
+    st = lib.vcpcu_ieigsymge(n, _host_ptr(A, 2 * n * n, "A"), _host_ptr(B, 2 * n * n, "B"),
+                             _host_ptr(X, n * n, "X"), _host_ptr(lam, n, "lambda"),
+                             ctypes.cast(fn, ctypes.c_void_p), None, out.ctypes.data,
+                             ctypes.addressof(g), int(form), int(slices))
+    if st != 0 and (check or st != 8):
+        from .errors import raise_for_status
+        raise_for_status(st, "vcpcu_ieigsymge: " +
+                         lib.vcpcu_last_error_string().decode(errors="replace"))
+    return out, g.value
+
+
+def eigsymge_stage1_dev(n, A, lda, B, ldb, X, ldx, C, BX, midBX, form=FORM_PLAIN, slices=0,
+                        stream=None) -> None:
+    _lib.call("vcpcu_ieigsymge_stage1_dev", n, _dev_ptr(A, "A"), lda, _dev_ptr(B, "B"), ldb,
+              _dev_ptr(X, "X"), ldx, _dev_ptr(C, "C"), _dev_ptr(BX, "BX"),
+              _dev_ptr(midBX, "midBX"), int(form), int(slices), _stream_ptr(stream))
+
+
+def eigsymge_stage2_dev(n, lam, Y, ldy, C, BX, out, bound, form=FORM_PLAIN, slices=0,
+                        stream=None) -> None:
+    _lib.call("vcpcu_ieigsymge_stage2_dev", n, _dev_ptr(lam, "lambda"), _dev_ptr(Y, "Y"), ldy,
+              _dev_ptr(C, "C"), _dev_ptr(BX, "BX"), _dev_ptr(out, "lam"),
+              _dev_ptr(bound, "bound"), int(form), int(slices), _stream_ptr(stream))
+
+
+def eig_merge(lam_kv: np.ndarray, n: int) -> np.ndarray:
+    """The overlap merge of imats::eigsymge, in place on a kv buffer of n."""
+    _lib.call("vcpcu_eig_merge", n, _host_ptr(lam_kv, 2 * n, "lam", writable=True))
+    return lam_kv
+
+
 # ---- AUTO form -------------------------------------------------------------------
 
 def autotune(stream=None) -> dict:
