@@ -683,7 +683,18 @@ def bench_point(dev, stream, m, n, k, phi, slice_list, steps=2, plain=True, seed
     return out
 
 
-def bench_lss(dev, stream, n, nrhs=1, steps=2, plain_steps=1, seed=91, cpu_n=768):
+def _setup_inv(M):
+    """Approximate inverse for a workload's setup (untimed): torch's linalg
+    on the device, numpy on the host when that library cannot be loaded."""
+    import torch
+    try:
+        return torch.linalg.inv(M)
+    except RuntimeError:
+        return torch.from_numpy(np.linalg.inv(M.cpu().numpy())).to(M.device)
+
+
+def bench_lss(dev, stream, n, nrhs=1, steps=2, plain_steps=1, seed=91, cpu_n=768,
+              forms=("plain", "ozaki"), cpu=True):
     """The verification of imats::linearsolve (vcpcu_ilss_verify) at n x n,
     nrhs right-hand sides: A = I + U[-1,1]/sqrt(n) (well conditioned), b
     U[-1,1], radii 2^-40 |mid|; R and mx formed on the device in FP64
@@ -706,7 +717,7 @@ def bench_lss(dev, stream, n, nrhs=1, steps=2, plain_steps=1, seed=91, cpu_n=768
             r = m.abs() * 2.0 ** -40
             return torch.stack((m - r, m + r), dim=-1).transpose(0, 1).contiguous().reshape(-1)
 
-        R = torch.linalg.inv(mid)
+        R = _setup_inv(mid)
         mx = R @ bm
         return (kv(mid), kv(bm), R.t().contiguous().reshape(-1),
                 mx.t().contiguous().reshape(-1))
@@ -718,16 +729,21 @@ def bench_lss(dev, stream, n, nrhs=1, steps=2, plain_steps=1, seed=91, cpu_n=768
     res = {}
     for name, form, st_ in (("plain", pidcuda.FORM_PLAIN, plain_steps),
                             ("ozaki", pidcuda.FORM_OZAKI, steps)):
+        if name not in forms:
+            continue
         ms = time_stream(lambda: pidcuda.linearsolve_verify_dev(
             n, nrhs, A, n, b, n, R, n, mx, n, x, n, G, form=form, stream=stream), stream, st_)
         res[name] = (x.cpu().numpy(), float(G.cpu()[0]))
         out[name] = {"ms": ms, "tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12,
                      "bound_RA_minus_I": res[name][1]}
-    xp, xo = res["plain"][0], res["ozaki"][0]
-    wp, wo = xp[1::2] - xp[0::2], xo[1::2] - xo[0::2]
-    out["width_ozaki_vs_plain_median"] = float(np.median(wo / wp))
-    out["width_ozaki_vs_plain_max"] = float(np.max(wo / wp))
-    out["speedup_ozaki_vs_plain"] = out["plain"]["ms"] / out["ozaki"]["ms"]
+    if len(res) == 2:
+        xp, xo = res["plain"][0], res["ozaki"][0]
+        wp, wo = xp[1::2] - xp[0::2], xo[1::2] - xo[0::2]
+        out["width_ozaki_vs_plain_median"] = float(np.median(wo / wp))
+        out["width_ozaki_vs_plain_max"] = float(np.max(wo / wp))
+        out["speedup_ozaki_vs_plain"] = out["plain"]["ms"] / out["ozaki"]["ms"]
+    if not cpu:
+        return out
     # CPU: the restatement of the same steps at cpu_n, scaled by (n / cpu_n)^3
     Ac, bc, Rc, mc = (t.cpu().numpy() for t in system(cpu_n))
     t0 = time.perf_counter()
@@ -740,7 +756,7 @@ def bench_lss(dev, stream, n, nrhs=1, steps=2, plain_steps=1, seed=91, cpu_n=768
     return out
 
 
-def bench_eig(dev, stream, n, steps=2, plain_steps=1, seed=93):
+def bench_eig(dev, stream, n, steps=2, plain_steps=1, seed=93, forms=("plain", "ozaki")):
     """The verification of imats::eigsymge (vcpcu_ieigsymge stages 1 and 2)
     for A x = l B x, n x n: A symmetric N(0, 1/n), B = I + 0.1 G (G G^T form,
     positive definite), radii 2^-40 |mid|; the approximate eigenpairs and
@@ -757,9 +773,15 @@ def bench_eig(dev, stream, n, steps=2, plain_steps=1, seed=93):
     G = torch.eye(n, **f64) + 0.1 * torch.randn(n, n, generator=gen, **f64) / n ** 0.5
     Bm = G @ G.t()
     Bm = (Bm + Bm.t()) / 2
-    L = torch.linalg.cholesky(Bm)
-    Li = torch.linalg.inv(L)
-    w, V = torch.linalg.eigh(Li @ Am @ Li.t())
+    try:
+        L = torch.linalg.cholesky(Bm)
+        Li = torch.linalg.inv(L)
+        w, V = torch.linalg.eigh(Li @ Am @ Li.t())
+    except RuntimeError:  # torch's linalg library not loadable (e.g. under a profiler)
+        Ln = np.linalg.cholesky(Bm.cpu().numpy())
+        Lin = np.linalg.inv(Ln)
+        wn, Vn = np.linalg.eigh(Lin @ Am.cpu().numpy() @ Lin.T)
+        Li, w, V = (torch.from_numpy(v).to(dev) for v in (Lin, wn, Vn))
     X = (Li.t() @ V).t().contiguous().reshape(-1)
 
     def kv(m):
@@ -772,24 +794,28 @@ def bench_eig(dev, stream, n, steps=2, plain_steps=1, seed=93):
     M = torch.empty(n * n, **f64)
     pidcuda.eigsymge_stage1_dev(n, A, n, B, n, X, n, C, BX, M, pidcuda.FORM_OZAKI, 0, stream)
     stream.synchronize()
-    Y = torch.linalg.inv(M.reshape(n, n).t()).t().contiguous().reshape(-1)
+    Y = _setup_inv(M.reshape(n, n).t()).t().contiguous().reshape(-1)
     lam = torch.empty(2 * n, **f64)
     bound = torch.empty(1, **f64)
     out = {"n": n}
     res = {}
     for name, form, st_ in (("plain", pidcuda.FORM_PLAIN, plain_steps),
                             ("ozaki", pidcuda.FORM_OZAKI, steps)):
+        if name not in forms:
+            continue
+
         def step():
             pidcuda.eigsymge_stage1_dev(n, A, n, B, n, X, n, C, BX, M, form, 0, stream)
             pidcuda.eigsymge_stage2_dev(n, w, Y, n, C, BX, lam, bound, form, 0, stream)
         ms = time_stream(step, stream, st_)
         res[name] = lam.cpu().numpy()
         out[name] = {"ms": ms, "bound_YBX_minus_I": float(bound.cpu()[0])}
-    wp = res["plain"][1::2] - res["plain"][0::2]
-    wo = res["ozaki"][1::2] - res["ozaki"][0::2]
-    out["width_ozaki_vs_plain_median"] = float(np.median(wo / wp))
-    out["speedup_ozaki_vs_plain"] = out["plain"]["ms"] / out["ozaki"]["ms"]
-    out["enclosure_width_median"] = float(np.median(wo))
+    if len(res) == 2:
+        wp = res["plain"][1::2] - res["plain"][0::2]
+        wo = res["ozaki"][1::2] - res["ozaki"][0::2]
+        out["width_ozaki_vs_plain_median"] = float(np.median(wo / wp))
+        out["speedup_ozaki_vs_plain"] = out["plain"]["ms"] / out["ozaki"]["ms"]
+        out["enclosure_width_median"] = float(np.median(wo))
     return out
 
 
@@ -809,14 +835,17 @@ def run_workload(args, dev, stream):
             metric, unit = "batched interval GEMM TFLOP/s (4096 uneven problems)", "TFLOP/s"
             value = res["ozaki"]["tflops"]
         elif args.workload == "lss":
-            res = {"cases": [bench_lss(dev, stream, n, nrhs, steps=args.steps)
+            forms = ("ozaki",) if args.form == "ozaki" else ("plain", "ozaki")
+            res = {"cases": [bench_lss(dev, stream, n, nrhs, steps=args.steps, forms=forms,
+                                       cpu=not args.no_cpu)
                              for n in parse_list(args.sizes, [8192])
                              for nrhs in parse_list(args.phis, [1])]}
             metric, unit = ("verified linear solve, device-resident verification "
                             "(imats::linearsolve after R, mx): ms"), "ms"
             value = min(c["ozaki"]["ms"] for c in res["cases"])
         elif args.workload == "eig":
-            res = {"cases": [bench_eig(dev, stream, n, steps=args.steps)
+            forms = ("ozaki",) if args.form == "ozaki" else ("plain", "ozaki")
+            res = {"cases": [bench_eig(dev, stream, n, steps=args.steps, forms=forms)
                              for n in parse_list(args.sizes, [4096])]}
             metric, unit = ("verified generalized symmetric eigenvalues, device-resident "
                             "verification (imats::eigsymge after X, lambda, Y): ms"), "ms"

@@ -68,6 +68,14 @@ long long vcpcu_launch_count(void);
  * themselves. */
 int vcpcu_status(void* stream);
 
+/* Self-test of that timeout path: one thread waits, with the same bounded
+ * mbarrier wait as the tensor-core kernels, on a barrier that nothing ever
+ * arrives on; after limit_cycles (0: 2e9, about 1 s) it gives up, sets the
+ * timeout status and returns, and the call returns what vcpcu_status then
+ * reports: VCPCU_ERR_TIMEOUT when the path works.  No fault, trap or hang;
+ * the context stays usable. */
+int vcpcu_selftest_timeout(long long limit_cycles, void* stream);
+
 /* Per-phase timing of Ozaki-form calls: while enabled, every call records
  * CUDA events on its own stream around its phases (0 operand preparation,
  * 1 and 2 the two radius slice GEMMs, 3 the midpoint slice GEMM, 4 the

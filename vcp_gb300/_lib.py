@@ -46,6 +46,7 @@ SIGNATURES: dict[str, tuple] = {
     "vcpcu_ieigsymge_stage1_dev": (_i, [_i, _v, _i, _v, _i, _v, _i, _v, _v, _v, _i, _i, _v]),
     "vcpcu_ieigsymge_stage2_dev": (_i, [_i, _v, _v, _i, _v, _v, _v, _v, _i, _i, _v]),
     "vcpcu_eig_merge": (_i, [_i, _v]),
+    "vcpcu_selftest_timeout": (_i, [C.c_longlong, _v]),
     "vcpcu_ieigsymge": (_i, [_i, _v, _v, _v, _v, _v, _v, _v, _v, _i, _i]),
     "vcpcu_vcpmat_save": (_i, [C.c_char_p, _i, _i, _i, _v]),
     "vcpcu_vcpmat_info": (_i, [C.c_char_p, _v, _v, _v]),

@@ -228,6 +228,20 @@ int vcpcu_status(void* stream) {
   return VCPCU_OK;
 }
 
+int vcpcu_selftest_timeout(long long limit_cycles, void* stream) {
+  clear_error();
+  int st = check_device();
+  if (st) return st;
+  if (limit_cycles <= 0) limit_cycles = 2000000000LL;
+  if (limit_cycles > 8000000000LL) {
+    set_error("selftest_timeout: limit above 8e9 cycles");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if ((st = oz_selftest_timeout(limit_cycles, s))) return st;
+  return vcpcu_status(stream);
+}
+
 int vcpcu_profile(int enable) { return oz_profile_enable(enable); }
 
 int vcpcu_profile_read(double* ms, int nphases, long long* tensor_flops) {

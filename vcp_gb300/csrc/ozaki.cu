@@ -11,6 +11,7 @@
 #include "common.cuh"
 #include "ozaki.cuh"
 #include "ozaki_common.cuh"
+#include "tc_ptx.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -142,6 +143,31 @@ int oz_profile_read(double* ms, int nphases, long long* flops) {
   }
   if (flops) *flops = g_prof.flops;
   g_prof.flops = 0;
+  return VCPCU_OK;
+}
+
+// Self-test of the timeout path: one thread waits, with the bounded wait of
+// the slice GEMM (mbar_wait), on an mbarrier that nothing ever arrives on;
+// the wait gives up after `limit` cycles and the kernel sets the timeout
+// word (flag[1]) and returns -- no fault, trap or hang.
+__global__ void oz_wait_selftest(int* flag, long long limit) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    ptx::mbar_init(&bar, 1);
+    ptx::fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && !ptx::mbar_wait(&bar, 0, limit)) flag[1] = 1;
+}
+
+int oz_selftest_timeout(long long limit, cudaStream_t s) {
+  Scratch fl;
+  int st = fl.alloc(4 * sizeof(int), s);
+  if (st) return st;
+  VCPCU_CUDA_TRY(cudaMemsetAsync(fl.ptr, 0, 4 * sizeof(int), s));
+  oz_wait_selftest<<<1, 32, 0, s>>>((int*)fl.ptr, limit);
+  VCPCU_LAUNCH_CHECK("oz_wait_selftest");
+  oz_merge_status((const int*)fl.ptr, s);
   return VCPCU_OK;
 }
 

@@ -158,6 +158,8 @@ int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws);
 // Read and clear the sticky status (bit 0 non-finite input, bit 1 timeout);
 // synchronises the stream.
 int oz_take_status(cudaStream_t s, int* status);
+// A bounded wait on an mbarrier nothing arrives on: sets the timeout status.
+int oz_selftest_timeout(long long limit, cudaStream_t s);
 // Merge a product's status words into the sticky device status.
 void oz_merge_status(const int* flag, cudaStream_t s);
 // ... of n products (status words 4 ints apart).
