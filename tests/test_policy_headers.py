@@ -186,14 +186,31 @@ void dsyrk_(char*, char*, int*, int*, double*, const double*, int*, double*, dou
 }
 void dsymm_(char*, char*, int*, int*, double*, const double*, int*, const double*, int*,
             double*, double*, int*) { std::abort(); }
-void dgetrf_(int*, int*, double*, int*, int*, int*) { std::abort(); }
-void dgetrs_(char*, int*, int*, double*, int*, int*, double*, int*, int*) { std::abort(); }
+// The LAPACK steps of the refinements run on the host before their first GPU
+// product: these stubs let them through (identity factors).
+void dgetrf_(int* m, int*, double*, int*, int* ipiv, int* info) {
+  for (int i = 0; i < *m; ++i) ipiv[i] = i + 1;
+  *info = 0;
+}
+void dgetrs_(char*, int*, int*, double*, int*, int*, double*, int*, int* info) { *info = 0; }
 void dgetri_(int*, double*, int*, int*, double*, int*, int*) { std::abort(); }
-void dsyev_(char*, char*, int*, double*, int*, double*, double*, int*, int*) { std::abort(); }
+void dsyev_(char*, char*, int* n, double* A, int*, double* W, double* work, int* lwork, int* info) {
+  *info = 0;
+  if (*lwork == -1) {
+    work[0] = 1;
+    return;
+  }
+  for (int i = 0; i < *n; ++i)
+    for (int j = 0; j < *n; ++j) {
+      if (i == j) W[i] = A[i + *n * i];
+      A[i + *n * j] = i == j ? 1.0 : 0.0;
+    }
+}
 void dgesv_(int*, int*, double*, int*, int*, double*, int*, int*) { std::abort(); }
 void dsygv_(int*, char*, char*, int*, double*, int*, double*, int*, double*, double*, int*,
             int*) { std::abort(); }
-void dpotrf_(char*, int*, double*, int*, int*) { std::abort(); }
+void dpotrf_(char*, int*, double*, int*, int* info) { *info = 0; }
+void dtrsm_(char*, char*, char*, char*, int*, int*, double*, double*, int*, double*, int*) {}
 }
 
 typedef vcp::matrix<kv::dd, vcp::pddcuda> M;
@@ -219,13 +236,46 @@ int main() {
     std::printf("STATE_ERROR mulltmm: %s\n", e.what());
     ++errors;
   }
+  M S, bv, x, E, V;
+  S.zeros(3, 3);
+  bv.zeros(3, 1);
+  for (int i = 0; i < 3; ++i) S.data()[4 * i] = kv::dd(2.0 + i);
+  bv.data()[0] = kv::dd(1.0);
+  try {
+    x = lss(S, bv);                       // pddcuda::linearsolve -> vcpcu_ddgemm residuals
+    std::printf("NO_ERROR lss\n");
+  } catch (vcp::state_error& e) {
+    std::printf("STATE_ERROR lss: %s\n", e.what());
+    ++errors;
+  }
+  try {
+    M R = inv(S);                         // pddcuda::inv
+    std::printf("NO_ERROR inv\n");
+  } catch (vcp::state_error& e) {
+    std::printf("STATE_ERROR inv: %s\n", e.what());
+    ++errors;
+  }
+  try {
+    E = Cholesky(S);                      // pddcuda::Cholesky
+    std::printf("NO_ERROR Cholesky\n");
+  } catch (vcp::state_error& e) {
+    std::printf("STATE_ERROR Cholesky: %s\n", e.what());
+    ++errors;
+  }
+  try {
+    eigsym(S, E, V);                      // pddcuda::eigsym -> Ogita-Aishima on the GPU
+    std::printf("NO_ERROR eigsym\n");
+  } catch (vcp::state_error& e) {
+    std::printf("STATE_ERROR eigsym: %s\n", e.what());
+    ++errors;
+  }
   M s, t;                                 // the scalar shortcut of pddblas stays on the host
   s.zeros(1, 1);
   s.data()[0] = kv::dd(3.0);
   t = s * A;
   if (t.data()[5].a1 != 12.0) ++errors;
   std::fflush(stdout);
-  return errors == 2 ? 0 : 1;
+  return errors == 6 ? 0 : 1;
 }
 '''
 
@@ -251,3 +301,5 @@ def test_pddcuda_header_compile_link_and_map_errors(tmp_path, cuda_lib):
     run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert run.returncode == 0, run.stdout + run.stderr
     assert "STATE_ERROR mulmm" in run.stdout and "STATE_ERROR mulltmm" in run.stdout
+    for what in ("lss", "inv", "Cholesky", "eigsym"):
+        assert f"STATE_ERROR {what}" in run.stdout, run.stdout
