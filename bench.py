@@ -886,6 +886,7 @@ def bench_also(dev, stream):
                     ("batch", lambda: bench_batch(dev, stream, steps=1)),
                     ("dd", lambda: [bench_dd(dev, stream, 2048, phi, steps=2) for phi in (0, 16)]),
                     ("lss", lambda: bench_lss(dev, stream, 2048, 1, steps=3)),
+                    ("eig", lambda: bench_eig(dev, stream, 1024, steps=3)),
                     ("point", lambda: bench_point(dev, stream, 4096, 4096, 4096, 0, [6, 8],
                                                   steps=2))):
         t0 = time.perf_counter()

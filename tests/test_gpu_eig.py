@@ -170,3 +170,43 @@ def test_eigsymge_failed_check_raises(cuda_lib):
     assert bound >= 1.0
     with pytest.raises(VerificationError):
         pidcuda.eigsymge_verify(A, B, X, lmb, n, form=pidcuda.FORM_PLAIN)
+
+
+def test_eigsymge_stages_padded_leading_dimensions(cuda_lib):
+    import torch
+    n = 50
+    rng = np.random.default_rng(31)
+    A, B, Am, Bm = problem(rng, n, 2.0 ** -30)
+    X, lmb = eigenpairs(Am, Bm)
+    used = {}
+
+    def inverse(M):
+        used["Y"] = np.linalg.inv(M)
+        return used["Y"]
+
+    lam_ref, bound_ref = pidcuda.eigsymge_verify(A, B, X, lmb, n, inverse,
+                                                 form=pidcuda.FORM_PLAIN)
+    Y = used["Y"].ravel(order="F").copy()
+
+    def pad(v, ld, width):
+        out = np.full((n, ld, width), np.nan)
+        out[:, :n, :] = np.asarray(v).reshape(n, n, width)
+        return out.reshape(-1)
+
+    lda, ldb, ldx, ldy = n + 2, n + 7, n + 1, n + 3
+    dev = torch.device("cuda")
+    t = lambda v: torch.from_numpy(v).to(dev)
+    tA, tB, tX, tY, tl = t(pad(A, lda, 2)), t(pad(B, ldb, 2)), t(pad(X, ldx, 1)), \
+        t(pad(Y, ldy, 1)), t(lmb)
+    C = torch.empty(2 * n * n, dtype=torch.float64, device=dev)
+    BX = torch.empty_like(C)
+    M = torch.empty(n * n, dtype=torch.float64, device=dev)
+    lam = torch.empty(2 * n, dtype=torch.float64, device=dev)
+    bound = torch.empty(1, dtype=torch.float64, device=dev)
+    s = torch.cuda.current_stream()
+    pidcuda.eigsymge_stage1_dev(n, tA, lda, tB, ldb, tX, ldx, C, BX, M, pidcuda.FORM_PLAIN, 0, s)
+    pidcuda.eigsymge_stage2_dev(n, tl, tY, ldy, C, BX, lam, bound, pidcuda.FORM_PLAIN, 0, s)
+    s.synchronize()
+    merged = pidcuda.eig_merge(lam.cpu().numpy().copy(), n)
+    assert np.array_equal(bits(merged), bits(lam_ref))
+    assert float(bound.cpu()[0]) == bound_ref

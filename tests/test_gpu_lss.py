@@ -175,3 +175,44 @@ def test_ilss_device_form_matches_host_form(cuda_lib, form):
     s.synchronize()
     assert np.array_equal(bits(tx.cpu().numpy()), bits(x))
     assert float(tg.cpu()[0]) == G
+
+
+def _pad(vec_kv_or_pt, rows, cols, ld, width):
+    """Column-major (rows x cols) buffer of `width` doubles per entry -> ld-padded copy."""
+    src = np.asarray(vec_kv_or_pt).reshape(cols, rows, width)
+    out = np.full((cols, ld, width), np.nan)
+    out[:, :rows, :] = src
+    return out.reshape(-1)
+
+
+@pytest.mark.parametrize("form", [pidcuda.FORM_PLAIN, pidcuda.FORM_OZAKI])
+def test_ilss_device_form_padded_leading_dimensions(cuda_lib, form):
+    import torch
+    n, nrhs = 70, 3
+    rng = np.random.default_rng(77 + form)
+    A, b, R, mx = system(rng, n, nrhs, 2.0 ** -30)
+    x, G = pidcuda.linearsolve_verify(A, b, R, mx, n, nrhs, form=form)
+    lda, ldb, ldr, ldm, ldx = n + 3, n + 5, n + 2, n + 1, n + 4
+    dev = torch.device("cuda")
+    t = lambda v: torch.from_numpy(v).to(dev)
+    tA, tb = t(_pad(A, n, n, lda, 2)), t(_pad(b, n, nrhs, ldb, 2))
+    tR, tm = t(_pad(R, n, n, ldr, 1)), t(_pad(mx, n, nrhs, ldm, 1))
+    tx = torch.full((ldx * nrhs * 2,), float("nan"), dtype=torch.float64, device=dev)
+    tg = torch.empty(1, dtype=torch.float64, device=dev)
+    s = torch.cuda.current_stream()
+    pidcuda.linearsolve_verify_dev(n, nrhs, tA, lda, tb, ldb, tR, ldr, tm, ldm, tx, ldx, tg,
+                                   form=form, stream=s)
+    s.synchronize()
+    got = tx.cpu().numpy().reshape(nrhs, ldx, 2)[:, :n, :].reshape(-1)
+    assert np.array_equal(bits(got), bits(x))
+    assert float(tg.cpu()[0]) == G
+
+
+def test_ilss_nonfinite_input_reported(cuda_lib):
+    from vcp_gb300.errors import NonFiniteError
+    n = 40
+    rng = np.random.default_rng(4)
+    A, b, R, mx = system(rng, n, 1, 2.0 ** -30)
+    A[2 * 17 + 1] = np.inf
+    with pytest.raises(NonFiniteError):
+        pidcuda.linearsolve_verify(A, b, R, mx, n, 1, form=pidcuda.FORM_OZAKI)
