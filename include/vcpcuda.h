@@ -165,7 +165,8 @@ int vcpcu_igemm_dev(int m, int n, int k, const double* A, int lda,
  * ldc = m): the drop-in for a std::vector<kv::interval<double>> product.
  * When the tensor-core CRT form runs (form OZAKI, or AUTO choosing it) and
  * n >= 2048, the copies overlap the computation: C is cut into blocks (row
- * blocks of 2048 rows and column blocks of 1024 columns, at most 4 of each;
+ * blocks of about 1365 rows, at most 6, and column blocks of 1024 columns,
+ * at most 4;
  * the environment variables VCPCU_HOST_ROW_PANELS and VCPCU_HOST_PANELS
  * override the counts, 1 and 1 turn the overlap off), A goes to the device in
  * row blocks and B in column blocks, interleaved, each block of C is

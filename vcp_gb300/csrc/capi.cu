@@ -43,11 +43,15 @@ int host_panels(int n) {
   if (n < 2048) return 1;
   return n / 1024 < 4 ? n / 1024 : 4;
 }
+// Row blocks of about 1365 rows, at most 6 (n = 8192: 6 x 4 blocks, 25.27 ms
+// end to end against 25.61 for 4 x 4 on one box; more column blocks were
+// slower).
 int host_row_panels(int m, int n) {
   const int env = env_int("VCPCU_HOST_ROW_PANELS");
   if (env > 0) return env;
   if (n < 2048) return 1;
-  return m / 2048 < 4 ? (m / 2048 > 1 ? m / 2048 : 1) : 4;
+  const int r = m / 1365;
+  return r < 1 ? 1 : (r > 6 ? 6 : r);
 }
 
 int point_kind(int rounding_mode) {
