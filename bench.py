@@ -18,6 +18,8 @@ Our arm (default) prints one JSON line with
                  reference path) on the host cores, bounded row sample.
   also           short runs of the other benchmark workloads in the same
                  process (``--workload`` runs one of them at full size):
+                 cfg1   the n = 512 interval product: CPU port of pidblas vs
+                        the GPU's plain form (bits compared) and Ozaki form;
                  batch  4096 uneven interval GEMMs, m, n, k log-uniform in
                         [32, 1024], mid U[-1, 1], rad 1e-12 |mid|: throughput
                         and p50 / p99 per-problem latency from device stamps,
@@ -819,6 +821,33 @@ def bench_eig(dev, stream, n, steps=2, plain_steps=1, seed=93, forms=("plain", "
     return out
 
 
+def bench_cfg1(dev, stream, n=512, steps=3, seed=5):
+    """cfg1: the n = 512 interval product, CPU (the oracle port of
+    pidblas::mulmm, all host cores) against the GPU's plain form (every bit
+    compared) and its tensor-core form; mid E(4), radius 2^-40 |mid|."""
+    import torch
+    from vcp_gb300 import pidcuda, workloads as W
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    A = W.interval_ephi(rng, n, n, 4, 2.0 ** -40)
+    B = W.interval_ephi(rng, n, n, 4, 2.0 ** -40)
+    t0 = time.perf_counter()
+    C_cpu = O.pidblas_mulmm(n, n, n, A, B, cpu_count())
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    dA, dB = (torch.from_numpy(v).to(dev) for v in (A, B))
+    dC = torch.empty(2 * n * n, dtype=torch.float64, device=dev)
+    out = {"n": n, "cpu_port_ms": cpu_ms, "cpu_cores": cpu_count()}
+    for name, form in (("plain", pidcuda.FORM_PLAIN), ("ozaki", pidcuda.FORM_OZAKI)):
+        ms = time_stream(lambda: pidcuda.mulmm_dev(n, n, n, dA, n, dB, n, dC, n, form, 0, stream),
+                         stream, steps)
+        out[name] = {"ms": ms, "tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12}
+        if name == "plain":
+            out[name]["bit_identical_to_cpu"] = bool(
+                np.array_equal(dC.cpu().numpy().view(np.int64), C_cpu.view(np.int64)))
+    out["speedup_plain_vs_cpu"] = cpu_ms / out["plain"]["ms"]
+    return out
+
+
 def parse_list(text, default, conv=int):
     return [conv(x) for x in text.split(",") if x] if text else default
 
@@ -885,6 +914,7 @@ def bench_also(dev, stream):
     for key, fn in (("autotune", lambda: pidcuda.autotune(stream)),
                     ("batch", lambda: bench_batch(dev, stream, steps=1)),
                     ("dd", lambda: [bench_dd(dev, stream, 2048, phi, steps=2) for phi in (0, 16)]),
+                    ("cfg1", lambda: bench_cfg1(dev, stream)),
                     ("lss", lambda: bench_lss(dev, stream, 2048, 1, steps=3)),
                     ("eig", lambda: bench_eig(dev, stream, 1024, steps=3)),
                     ("point", lambda: bench_point(dev, stream, 4096, 4096, 4096, 0, [6, 8],
