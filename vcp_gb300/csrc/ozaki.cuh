@@ -90,6 +90,7 @@ struct alignas(128) OzGemmArgs {
   // write res + gp[p].res_off / P + gp[p].P_off (null gp: one product)
   const struct OzGProb* gp;
   const int* gitem;
+  const int* gprob;  // item -> problem (one load per item)
   int gnprob, gnitems;
   OzPairList pl;
 };
@@ -228,6 +229,8 @@ struct OzGBucket {
   const int* blk_split;    // [nprob + 1] prefix of split_left blocks
   const int* item_rad;     // [nprob + 1] prefix of radius work items (groups x tiles)
   const int* item_crt;     // [nprob + 1] prefix of residue work items (L x tiles)
+  const int* prob_rad;     // [radius items] the problem of each item
+  const int* prob_crt;     // [residue items] the problem of each item
   const int* blk_asm;      // [nprob + 1] prefix of reassembly blocks
   const int* col_prob;     // [Ntot] problem of each stacked B column
   uint16_t* planesA;       // [Lmax + 4][Mtot][Kp]: residues, |mA|+rA digits, rA digits

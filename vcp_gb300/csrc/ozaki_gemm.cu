@@ -119,7 +119,7 @@ __device__ __forceinline__ int gfind_item(const int* __restrict__ prefix, int np
 __device__ __forceinline__ ItemInfo item_info(const OzGemmArgs& a, int item, int ntiles) {
   ItemInfo f;
   if (a.gp) {
-    const int p = gfind_item(a.gitem, a.gnprob, item);
+    const int p = a.gprob ? a.gprob[item] : gfind_item(a.gitem, a.gnprob, item);
     const OzGProb& q = a.gp[p];
     const int nt = q.tiles_m * q.tiles_n;
     const int local = item - a.gitem[p];
@@ -663,6 +663,7 @@ int oz_grun_gemm(const OzGBucket& b, const OzPlan& shape, int mode, int nitems, 
   a.timeout_cycles = 4000000000LL;  // about 2 s at 2 GHz
   a.gp = b.probs;
   a.gitem = mode == OZ_CRT ? b.item_crt : b.item_rad;
+  a.gprob = mode == OZ_CRT ? b.prob_crt : b.prob_rad;
   a.gnprob = b.nprob;
   a.gnitems = nitems;
   const int grid = nitems < num_sms() ? nitems : num_sms();

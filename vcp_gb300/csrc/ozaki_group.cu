@@ -83,7 +83,7 @@ int oz_group_plan(int count, const BatchProblemView* problems, const char* selec
     host.resize(off + bytes);
     return off;
   };
-  struct Offs { size_t probs, brow, bspl, irad, icrt, basm, cols; };
+  struct Offs { size_t probs, brow, bspl, irad, icrt, basm, cols, prad, pcrt; };
   std::vector<Offs> toff;
   for (auto& kv : byKp) {
     const std::vector<int>& ids = kv.second;
@@ -193,6 +193,20 @@ int oz_group_plan(int count, const BatchProblemView* problems, const char* selec
     b.nblk_split = (int)bspl;
     b.nitem_rad = (int)irad;
     b.nitem_crt = (int)icrt;
+    // item -> problem maps of the two kinds of slice GEMM launches (one load
+    // per work item instead of a binary search over the prefixes above)
+    o.prad = reserve(sizeof(int) * (size_t)(irad > 0 ? irad : 1));
+    o.pcrt = reserve(sizeof(int) * (size_t)(icrt > 0 ? icrt : 1));
+    {
+      const int* pr = (const int*)(host.data() + o.irad);
+      const int* pc = (const int*)(host.data() + o.icrt);
+      int* mr = (int*)(host.data() + o.prad);
+      int* mc = (int*)(host.data() + o.pcrt);
+      for (int t = 0; t < n; ++t) {
+        for (int it = pr[t]; it < pr[t + 1]; ++it) mr[it] = t;
+        for (int it = pc[t]; it < pc[t + 1]; ++it) mc[it] = t;
+      }
+    }
     b.nblk_asm = (int)basm;
     b.dev.Mtot = (int)Mtot;
     b.dev.Ntot = (int)Ntot;
@@ -256,6 +270,8 @@ int oz_group_plan(int count, const BatchProblemView* problems, const char* selec
     d.blk_split = (const int*)(tb + o.bspl);
     d.item_rad = (const int*)(tb + o.irad);
     d.item_crt = (const int*)(tb + o.icrt);
+    d.prob_rad = (const int*)(tb + o.prad);
+    d.prob_crt = (const int*)(tb + o.pcrt);
     d.blk_asm = (const int*)(tb + o.basm);
     d.col_prob = (const int*)(tb + o.cols);
   }
