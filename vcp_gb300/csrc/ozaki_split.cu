@@ -82,19 +82,31 @@ oz_rowmax_left(int M, int K, const double* __restrict__ A, long lda, int cols_pe
   if (i < M) {
     const int c0 = blockIdx.y * cols_per_block;
     const int c1 = min(K, c0 + cols_per_block);
-    for (int c = c0 + ph; c < c1; c += 8) {
-      const double2 e = *reinterpret_cast<const double2*>(A + 2 * (i + (long)c * lda));
-      double m = 0.0, r = 0.0, p;
-      if (sw_finite(e.x) && sw_finite(e.y)) {
-        sw_midrad(e.x, e.y, m, r, p);
-        am = max(am, dbits(oz_abs(m)));
-        ap = max(ap, dbits(p));
-        ar = max(ar, dbits(r));
-      } else {
-        bad = true;
+    constexpr int U = 4;  // loads in flight per thread (see oz_colmax_right)
+    for (int cb = c0 + ph; cb < c1; cb += 8 * U) {
+      double2 e[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int c = cb + 8 * u;
+        e[u] = c < c1 ? *reinterpret_cast<const double2*>(A + 2 * (i + (long)c * lda))
+                      : make_double2(0.0, 0.0);
       }
-      mA[i + (long)c * ldm] = m;
-      rA[i + (long)c * ldm] = r;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int c = cb + 8 * u;
+        if (c >= c1) break;
+        double m = 0.0, r = 0.0, p;
+        if (sw_finite(e[u].x) && sw_finite(e[u].y)) {
+          sw_midrad(e[u].x, e[u].y, m, r, p);
+          am = max(am, dbits(oz_abs(m)));
+          ap = max(ap, dbits(p));
+          ar = max(ar, dbits(r));
+        } else {
+          bad = true;
+        }
+        mA[i + (long)c * ldm] = m;
+        rA[i + (long)c * ldm] = r;
+      }
     }
   }
   if (bad) atomicOr(flag, 1);
@@ -902,19 +914,34 @@ oz_colmax_right(int K, int N, int Kp, int cols, int colbase, const double* __res
     const double* bcol = B + 2 * (long)j * ldb;
     double* mcol = mB + (size_t)j * Kp;
     double* rcol = rB + (size_t)j * Kp;
-    for (int k = lane; k < K; k += 32) {
-      const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
-      double m = 0.0, r = 0.0;
-      if (sw_finite(e.x) && sw_finite(e.y)) {
-        double p;
-        sw_midrad(e.x, e.y, m, r, p);
-        am = max(am, dbits(oz_abs(m)));
-        ar = max(ar, dbits(r));
-      } else {
-        bad = true;
+    // four loads in flight per lane before they are used: with one warp per
+    // column a launch over a narrow column block has few warps to hide the
+    // latency with (the midrad's out-of-line FP64 fallback keeps the
+    // compiler from hoisting loads across iterations by itself)
+    constexpr int U = 4;
+    for (int k0 = lane; k0 < K; k0 += 32 * U) {
+      double2 e[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int k = k0 + 32 * u;
+        e[u] = k < K ? *reinterpret_cast<const double2*>(bcol + 2 * k) : make_double2(0.0, 0.0);
       }
-      mcol[k] = m;
-      rcol[k] = r;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int k = k0 + 32 * u;
+        if (k >= K) break;
+        double m = 0.0, r = 0.0;
+        if (sw_finite(e[u].x) && sw_finite(e[u].y)) {
+          double p;
+          sw_midrad(e[u].x, e[u].y, m, r, p);
+          am = max(am, dbits(oz_abs(m)));
+          ar = max(ar, dbits(r));
+        } else {
+          bad = true;
+        }
+        mcol[k] = m;
+        rcol[k] = r;
+      }
     }
   }
   if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flag, 1);
