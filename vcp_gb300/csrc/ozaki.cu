@@ -386,20 +386,23 @@ int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long ld
   // half of ws.P.  A product with a zero factor would give exactly 0 (its
   // exponent is the zero sentinel), so it is skipped; the reassembly (CRT
   // form) or oz_radius_T (slice form) combines what ran.
-  if (!(plan.point_mask & 2)) {
-    PhaseTimer t(1, s);
-    if ((st = oz_run_gemm(plan, OZ_RAD_SET, ws, nullptr, 0, s))) return st;
-  }
-  if (!(plan.point_mask & 1)) {
-    PhaseTimer t(2, s);
-    if ((st = oz_run_gemm(plan, OZ_RAD_ADD, ws, nullptr, 0, s))) return st;
-  }
-  if (!plan.pb.crt && (st = oz_radius_T(plan, ws, s))) return st;
-  {
+  if (plan.pb.crt) {
+    // CRT form: the radius products and the residue GEMMs in one launch
+    // (phase 3 times all of them)
     PhaseTimer t(3, s);
-    if ((st = oz_run_gemm(plan, plan.pb.crt ? OZ_CRT : OZ_MID, ws, plan.pb.crt ? nullptr : C,
-                          ldc, s)))
-      return st;
+    if ((st = oz_run_gemm(plan, OZ_ALL, ws, nullptr, 0, s))) return st;
+  } else {
+    if (!(plan.point_mask & 2)) {
+      PhaseTimer t(1, s);
+      if ((st = oz_run_gemm(plan, OZ_RAD_SET, ws, nullptr, 0, s))) return st;
+    }
+    if (!(plan.point_mask & 1)) {
+      PhaseTimer t(2, s);
+      if ((st = oz_run_gemm(plan, OZ_RAD_ADD, ws, nullptr, 0, s))) return st;
+    }
+    if ((st = oz_radius_T(plan, ws, s))) return st;
+    PhaseTimer t(3, s);
+    if ((st = oz_run_gemm(plan, OZ_MID, ws, C, ldc, s))) return st;
   }
   if (plan.pb.crt) {
     PhaseTimer t(4, s);
@@ -552,9 +555,7 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
     v.F2 = ws.F2 + 2 * (size_t)j0;
     v.beta = ws.beta + j0;
     int e;
-    if ((e = oz_run_gemm(pj, OZ_RAD_SET, v, nullptr, 0, s))) return e;
-    if ((e = oz_run_gemm(pj, OZ_RAD_ADD, v, nullptr, 0, s))) return e;
-    if ((e = oz_run_gemm(pj, OZ_CRT, v, nullptr, 0, s))) return e;
+    if ((e = oz_run_gemm(pj, OZ_ALL, v, nullptr, 0, s))) return e;
     double* cblk = dC + 2 * ((size_t)i0 + (size_t)j0 * m);
     if ((e = oz_crt_assemble(pj, v, cblk, m, s))) return e;
     if ((e = pipe_event(g, s, down))) return e;

@@ -58,7 +58,11 @@ struct OzPairList {
 // product 2, rA * |mB|.  Each writes T or adds to it (OzGemmArgs::t_set).
 constexpr int OZ_MAX_RAD_SLOTS = 64;  // K <= 2^20: at most 64 folds of 64 chunks per product
 
-enum OzMode { OZ_RAD_SET = 0, OZ_RAD_ADD = 1, OZ_MID = 2, OZ_CRT = 3 };
+enum OzMode { OZ_RAD_SET = 0, OZ_RAD_ADD = 1, OZ_MID = 2, OZ_CRT = 3, OZ_ALL = 4 };
+// OZ_ALL (CRT form): both radius products and the residue GEMMs in one
+// launch -- one pair list over all planes, the mode of each group in
+// OzGemmArgs::gkind (fewer launch tails, most of all for the blocks of the
+// host-pointer pipeline).
 
 struct alignas(128) OzGemmArgs {
   CUtensorMap tmA;  // left digit planes, dims {Kp, Mp, planes}
@@ -83,8 +87,10 @@ struct alignas(128) OzGemmArgs {
   long long timeout_cycles;
   uint8_t* res;                 // OZ_CRT: residue planes [L][Np][Mp]
   int moduli[32];               // OZ_CRT: modulus of group g
-  int32_t* P;                   // radius modes: fold f of a tile -> slot slot0 + f
-  int slot0;
+  int32_t* P;                   // radius groups: fold f of a tile -> slot f (product 1) or
+  int slot_add;                 //   slot_add + f (product 2, OZ_RAD_ADD)
+  int8_t gkind[OZ_MAX_GROUPS];  // mode of group g (OZ_RAD_SET / _ADD / OZ_CRT / OZ_MID)
+  int8_t gres[OZ_MAX_GROUPS];   // OZ_CRT groups: residue plane (modulus index) of group g
   // grouped products: items of problem p are [gitem[p], gitem[p+1]); its
   // tiles read rows gp[p].rowoff.. / gp[p].coloff.. of the stacked planes and
   // write res + gp[p].res_off / P + gp[p].P_off (null gp: one product)

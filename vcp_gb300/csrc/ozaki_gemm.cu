@@ -319,13 +319,17 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
       const int gi = f.tm * OZ_BM + row_in_tile;
       const int gj0 = f.tn * OZ_BN + half * 128;
       bool have_w = false;
-      // radius modes: slot of the next fold = folds of the earlier groups
+      // radius groups: slot of the next fold = folds of the earlier groups
+      // of the same product
       int fold = 0;
+      const int kind0 = args.gkind[g0];
       for (int g = 0; g < g0; ++g)
-        fold += ((args.pl.gstart[g + 1] - args.pl.gstart[g]) * nchunks + OZ_FOLD_CHUNKS - 1) /
-                OZ_FOLD_CHUNKS;
+        if (args.gkind[g] == kind0)
+          fold += ((args.pl.gstart[g + 1] - args.pl.gstart[g]) * nchunks + OZ_FOLD_CHUNKS - 1) /
+                  OZ_FOLD_CHUNKS;
       for (int g = g0; g < g1 && ok; ++g) {
-        if (args.mode == OZ_CRT && nchunks == 1) {
+        const int kind = args.gkind[g];
+        if (kind == OZ_CRT && nchunks == 1) {
           // residue group (one modulus) of one chunk: the residue goes
           // straight from TMEM to res on the FP32 pipe, for the valid rows
           // and columns only (the reassembly reads no other); with several
@@ -341,7 +345,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
           ptx::tc_fence_after();
           const float mf = (float)args.moduli[g];
           const float invf = __frcp_rn(mf);
-          uint8_t* rp = f.res + (size_t)g * f.Np * f.Mp + (size_t)gj0 * f.Mp + gi;
+          uint8_t* rp = f.res + (size_t)args.gres[g] * f.Np * f.Mp + (size_t)gj0 * f.Mp + gi;
           const size_t ld = (size_t)f.Mp;
           const int ncol = gi < f.M ? f.N - gj0 : 0;  // 0: a padding row
 #pragma unroll 1
@@ -400,10 +404,11 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
           if (lane == 0) ptx::mbar_arrive(&sm.tempty[buf]);
           ++cnt;
           const bool last_of_group = idx == total - 1;
-          if ((cnt == OZ_FOLD_CHUNKS || last_of_group) && args.mode == OZ_CRT) {
+          if ((cnt == OZ_FOLD_CHUNKS || last_of_group) && kind == OZ_CRT) {
             // CRT form: group g is modulus m_g; keep (A'B') mod m_g as a byte
-            // in res[g][col][row], adding to an earlier fold of the group
-            uint8_t* rp = f.res + (size_t)g * f.Np * f.Mp + (size_t)gj0 * f.Mp + gi;
+            // in its residue plane [col][row], adding to an earlier fold of the group
+            uint8_t* rp =
+                f.res + (size_t)args.gres[g] * f.Np * f.Mp + (size_t)gj0 * f.Mp + gi;
             {
               const uint32_t m = (uint32_t)args.moduli[g];
               const uint32_t mg = 0xFFFFFFFFu / m;
@@ -425,10 +430,11 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
               }
             }
             cnt = 0;
-          } else if ((cnt == OZ_FOLD_CHUNKS || last_of_group) && args.mode != OZ_MID) {
-            // radius modes: the fold is stored, never read back here -- the
+          } else if ((cnt == OZ_FOLD_CHUNKS || last_of_group) && kind != OZ_MID) {
+            // radius groups: the fold is stored, never read back here -- the
             // reassembly combines the slots (no load stalls the drain)
-            int32_t* pp = f.P + ((size_t)(args.slot0 + fold) * f.Np + gj0) * f.Mp + gi;
+            const int slot = (kind == OZ_RAD_ADD ? args.slot_add : 0) + fold;
+            int32_t* pp = f.P + ((size_t)slot * f.Np + gj0) * f.Mp + gi;
 #pragma unroll
             for (int e = 0; e < 128; ++e) {
               pp[(size_t)e * f.Mp] = c[e];
@@ -580,6 +586,37 @@ int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, 
     ap = ws.a_r; bp = ws.b_s; apl = pb.sr; bpl = pb.sr;
     a.Erow = ws.E3 + 2; a.Fcol = ws.F2 + 0;
     a.pl = plan.rad; a.t_ref = plan.t_ref_rad; a.R = plan.R_rad;
+  } else if (mode == OZ_ALL) {
+    // the radius products and the residue GEMMs together: the A planes are
+    // [residues (mplanes) | |mA| + rA digits (sr) | rA digits (sr)] at one
+    // plane stride, the B planes [residues | rB digits | |mB| digits]
+    ap = ws.a_mid; bp = ws.b_mid;
+    apl = bpl = pb.mplanes + 2 * pb.sr;
+    a.Erow = ws.E3 + 0; a.Fcol = ws.F2 + 0;
+    a.t_ref = plan.t_ref_rad; a.R = plan.R_rad;
+    a.res = ws.res;
+    OzPairList& m = a.pl;
+    int ng = 0, np = 0;
+    auto add = [&](const OzPairList& src, int offA, int offB, int kind) {
+      for (int g = 0; g < src.ngroups; ++g) {
+        m.gstart[ng] = (int16_t)np;
+        m.gt[ng] = src.gt[g];
+        a.gkind[ng] = (int8_t)kind;
+        a.gres[ng] = (int8_t)(kind == OZ_CRT ? g : 0);
+        if (kind == OZ_CRT) a.moduli[ng] = OZ_MODULI[g];
+        for (int q = src.gstart[g]; q < src.gstart[g + 1]; ++q, ++np) {
+          m.pa[np] = (int8_t)(src.pa[q] + offA);
+          m.pb[np] = (int8_t)(src.pb[q] + offB);
+        }
+        ++ng;
+      }
+    };
+    if (!(plan.point_mask & 2)) add(plan.rad, pb.mplanes, pb.mplanes, OZ_RAD_SET);
+    if (!(plan.point_mask & 1)) add(plan.rad, pb.mplanes + pb.sr, pb.mplanes + pb.sr, OZ_RAD_ADD);
+    add(plan.crt, 0, 0, OZ_CRT);
+    m.gstart[ng] = (int16_t)np;
+    m.ngroups = ng;
+    m.npairs = np;
   } else {  // OZ_CRT: residue products, one modulus per group
     ap = ws.a_mid; bp = ws.b_mid; apl = pb.L; bpl = pb.L;
     a.Erow = ws.E3 + 0; a.Fcol = ws.F2 + 0;
@@ -587,6 +624,11 @@ int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, 
     a.res = ws.res;
     for (int l = 0; l < pb.L; ++l) a.moduli[l] = OZ_MODULI[l];
   }
+  if (mode != OZ_ALL)
+    for (int g = 0; g < a.pl.ngroups; ++g) {
+      a.gkind[g] = (int8_t)mode;
+      a.gres[g] = (int8_t)g;
+    }
   if ((st_ = make_tmap(&a.tmA, ap, pb.Kp, pb.Mp, apl, OZ_BM, ws.a_pstride))) return st_;
   if ((st_ = make_tmap(&a.tmB, bp, pb.Kp, pb.Np, bpl, OZ_BN, ws.b_pstride))) return st_;
   a.M = pb.M; a.N = pb.N; a.Mp = pb.Mp; a.Np = pb.Np; a.Kp = pb.Kp;
@@ -602,7 +644,7 @@ int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, 
   a.W = ws.W;
   a.T = ws.T;
   a.P = ws.P;
-  a.slot0 = mode == OZ_RAD_ADD ? plan.rad_slots : 0;
+  a.slot_add = plan.rad_slots;
   a.C = C;
   a.ldc = ldc;
   a.flag = ws.flag;
@@ -658,7 +700,11 @@ int oz_grun_gemm(const OzGBucket& b, const OzPlan& shape, int mode, int nitems, 
   a.Kp = b.Kp;
   a.mode = mode;
   a.P = b.P;
-  a.slot0 = mode == OZ_RAD_ADD ? shape.rad_slots : 0;
+  a.slot_add = shape.rad_slots;
+  for (int g = 0; g < a.pl.ngroups; ++g) {
+    a.gkind[g] = (int8_t)mode;
+    a.gres[g] = (int8_t)g;
+  }
   a.flag = b.flag;  // problem 0's status words take the (global) timeout bit
   a.timeout_cycles = 4000000000LL;  // about 2 s at 2 GHz
   a.gp = b.probs;
