@@ -422,29 +422,33 @@ def measure_fp64_peak(dev):
         return 1.25, "nominal"
 
 
-# DRAM bytes (read + write) of the three oz_slice_gemm_kernel launches of one
-# n = 8192 product at the default precision, from a one-pass ncu capture of
-# dram__bytes_read.sum and dram__bytes_write.sum on a GB300 (radius 1:
-# 5.29 + 0.83 GB, radius 2: 5.27 + 0.83 GB, midpoint residues: 15.19 + 1.31 GB).
-GEMM_TRAFFIC_N8192 = 28.73e9
+# DRAM bytes (read + write) of the oz_slice_gemm_kernel launch of one
+# n = 8192 product at the default precision (radius digit pairs and residue
+# GEMMs in one launch), from a one-pass ncu capture of dram__bytes_read.sum
+# and dram__bytes_write.sum on a GB300 (25.73 + 3.23 GB).
+GEMM_TRAFFIC_N8192 = 28.96e9
 
 
 def ozaki_roofline(phases, tc_flops, steps, pk, pk_kind, n=8192, default_form=True):
-    """Dominant kernel oz_slice_gemm_kernel (three launches per call): the
-    algorithmic bf16 tensor flops (2 m n k per slice pair or modulus) over
-    their summed CUDA-event time on the launching stream."""
+    """Dominant kernel oz_slice_gemm_kernel (one launch per call for the
+    default CRT form, three for the slice form): the algorithmic bf16 tensor
+    flops (2 m n k per slice pair or modulus) over the summed CUDA-event time
+    of its phases on the launching stream."""
     gemm_ms = sum(phases[1:4])
+    phase_ms = {"prep": phases[0] / steps, "slice_gemm": gemm_ms / steps,
+                "reassembly": phases[4] / steps}
+    if phases[1] > 0 or phases[2] > 0:  # slice form: radius products run as launches of their own
+        phase_ms.update(radius1=phases[1] / steps, radius2=phases[2] / steps,
+                        midpoint=phases[3] / steps)
     achieved = tc_flops / (gemm_ms * 1e-3) / 1e12 if gemm_ms > 0 else None
     peak = pk.get("bf16_tflops", 1900.0)
     return {"bound": "tensor", "kernel": "oz_slice_gemm_kernel", "achieved": achieved,
             "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
             "traffic": GEMM_TRAFFIC_N8192 if (n == 8192 and default_form) else None,
-            "traffic_unit": "bytes per call (3 launches)",
+            "traffic_unit": "bytes per call (1 launch)",
             "peak_kind": f"{pk_kind} bf16 dense (burst); sustained {pk.get('bf16_tflops_sustained')}",
             "algorithmic": "2*m*n*k per bf16 product: L residue GEMMs + 2 x 4 radius digit pairs",
-            "phase_ms_per_call": {"prep": phases[0] / steps, "radius1": phases[1] / steps,
-                                  "radius2": phases[2] / steps, "midpoint": phases[3] / steps,
-                                  "reassembly": phases[4] / steps}}
+            "phase_ms_per_call": phase_ms}
 
 
 # ---------------------------------------------------------------- other workloads

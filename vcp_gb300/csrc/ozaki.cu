@@ -1,9 +1,11 @@
 // ozaki.cu -- orchestration of the Ozaki-form interval product:
 //   plan (slice counts, pair lists, fixed-point scaling), scratch layout,
-//   operand preparation, the three slice-GEMM launches
+//   operand preparation, the three slice-GEMM phases
 //     1. T  = RU(P^ * rB^)        P = |mA| +ru rA, both factors rounded up
 //     2. T += RU(rA^ * |mB|^)
 //     3. C  = [RD(mA mB) - e, RU(mA mB) + e], e = RU(truncation + T)
+//   (one launch for the CRT form, whose phase 3 is the residue GEMMs and
+//   the reassembly; three for the slices form)
 // which together enclose pidblas's midpoint-radius product
 // (vcp/pidblas.hpp:239-294): mA*mB from the truncated slice expansion plus
 // its rigorous truncation bound, and the radius term
