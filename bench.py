@@ -729,6 +729,7 @@ def bench_lss(dev, stream, n, nrhs=1, steps=2, plain_steps=1, seed=91, cpu_n=768
                 mx.t().contiguous().reshape(-1))
 
     A, b, R, mx = system(n)
+    torch.cuda.synchronize()  # set up on the current stream, verified on `stream`
     x = torch.empty(2 * n * nrhs, dtype=torch.float64, device=dev)
     G = torch.empty(1, dtype=torch.float64, device=dev)
     out = {"n": n, "nrhs": nrhs}
@@ -798,9 +799,12 @@ def bench_eig(dev, stream, n, steps=2, plain_steps=1, seed=93, forms=("plain", "
     C = torch.empty(2 * n * n, **f64)
     BX = torch.empty_like(C)
     M = torch.empty(n * n, **f64)
+    # the setup ran on the current stream, the stages run on `stream`
+    torch.cuda.synchronize()
     pidcuda.eigsymge_stage1_dev(n, A, n, B, n, X, n, C, BX, M, pidcuda.FORM_OZAKI, 0, stream)
     stream.synchronize()
     Y = _setup_inv(M.reshape(n, n).t()).t().contiguous().reshape(-1)
+    torch.cuda.synchronize()
     lam = torch.empty(2 * n, **f64)
     bound = torch.empty(1, **f64)
     out = {"n": n}
