@@ -82,6 +82,8 @@ def parse():
     ap.add_argument("--phis", default="", help="point / dd: comma-separated phi")
     ap.add_argument("--slice-list", default="", help="point: comma-separated slice counts")
     ap.add_argument("--no-also", action="store_true", help="skip the short other workloads")
+    ap.add_argument("--no-model-check", action="store_true",
+                    help="skip the bit-for-bit host-model check of sampled rows and columns")
     ap.add_argument("--only-headline", action="store_true",
                     help="time the headline form only (profiling runs): no plain form, "
                          "width, containment, e2e or CPU legs")
@@ -175,6 +177,12 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+def headline_config(n: int, ws: int) -> dict:
+    """The workload description both arms print (identical for the ratio)."""
+    return {"workload": WORKLOAD, "n": n, "parallelism": f"replicas x{ws}",
+            "l2": "inputs (1 GiB per operand) larger than L2; no flush"}
+
+
 def make_inputs(n: int, seed: int):
     from vcp_gb300 import workloads as W
     rng = np.random.default_rng(seed)
@@ -191,6 +199,27 @@ def cpu_baseline(A, B, n, rows, threads):
     O.pidblas_mulmm(rows, n, n, Ap, B, threads)
     dt = time.perf_counter() - t0
     return 2.0 * rows * n * n / dt / 1e12, dt
+
+
+def model_bitexact_sample(O, A, B, C, n, slices, nrows=8, ncols=8, seed=17):
+    """Compare `nrows` full rows and `ncols` full columns of the n x n
+    tensor-core product C with the host model run on those rows of A (all of
+    B) and on all of A against those columns of B."""
+    rs = np.random.default_rng(seed)
+    R = np.sort(rs.choice(n, nrows, replace=False))
+    Cc = np.sort(rs.choice(n, ncols, replace=False))
+    t0 = time.perf_counter()
+    Ar = np.ascontiguousarray(A.reshape(n, n, 2)[:, R, :]).ravel()
+    ref_r, st1 = O.ozaki_igemm(nrows, n, n, Ar, B, slices, 2, crt=True)
+    got_r = np.ascontiguousarray(C.reshape(n, n, 2)[:, R, :]).ravel()
+    Bc = np.ascontiguousarray(B.reshape(n, n, 2)[Cc]).ravel()
+    ref_c, st2 = O.ozaki_igemm(n, ncols, n, A, Bc, slices, 2, crt=True)
+    got_c = np.ascontiguousarray(C.reshape(n, n, 2)[Cc]).ravel()
+    mism = int(np.sum(got_r.view(np.int64) != ref_r.view(np.int64)) +
+               np.sum(got_c.view(np.int64) != ref_c.view(np.int64)))
+    return {"entries": int((nrows + ncols) * n), "rows": int(nrows), "columns": int(ncols),
+            "mismatched_words": mism, "model_status": int(st1 | st2),
+            "seconds": time.perf_counter() - t0}
 
 
 def cpu_count():
@@ -219,11 +248,14 @@ def run_reference(args, ws, rank):
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * 2.0 * n ** 3 / (v * 1e12),
+        # what was timed: one row panel of the product per step
+        "ms_per_step": 1e3 * statistics.median(times),
+        "step": f"{rows} x {n} x {n} row panel of the n = {n} product "
+                f"(value = 2 * {rows} * {n}^2 flops / panel time)",
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "n": n, "form": "pidblas (CPU)",
-                   "l2": "inputs larger than L2"},
+        "form": "pidblas (CPU port)",
+        "config": headline_config(n, args.gpus),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{rows} x {n} x {n} row panel per step "
                                    f"(~{statistics.median(times):.1f} s), oracle restatement of "
@@ -331,6 +363,13 @@ def run_ours(args, ws, rank, local):
     idx = 2 * (rows + cols * n)
     fails = int(np.sum(C_head[idx] > lo) + np.sum(C_head[idx + 1] < up))
 
+    # bit-for-bit check of sampled full rows and columns of the headline
+    # result against the host model of the tensor-core form (each entry
+    # depends only on its row of A, its column of B and k)
+    model = None
+    if form == pidcuda.FORM_OZAKI and rank == 0 and not args.no_model_check:
+        model = model_bitexact_sample(O, A, B, C_head, n, args.slices or 8)
+
     # e2e through the host-pointer C ABI from pinned buffers
     hA = torch.from_numpy(A).pin_memory()
     hB = torch.from_numpy(B).pin_memory()
@@ -380,13 +419,13 @@ def run_ours(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form_name == "plain" else "bf16-slices/f64",
             "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "n": n, "form": form_name,
-                       "slices": args.slices or "default", "parallelism": f"replicas x{ws}",
-                       "l2": "inputs (1 GiB per operand) larger than L2; no flush"},
+            "form": form_name, "slices": args.slices or "default",
+            "config": headline_config(n, ws),
             "plain": {"value": plain_tflops, "ms_per_step": plain_ms, "steps": args.plain_steps},
             "speedup_vs_plain": value / plain_tflops,
             "width_vs_plain": width,
             "containment_failures": fails, "containment_sample": 1024,
+            "model_bitexact_sample": model,
             "e2e": {"value": e2e_val, "unit": UNIT,
                     "h2d_bytes_per_step": int(hA.numel() * 8 + hB.numel() * 8),
                     "d2h_bytes_per_step": int(hC.numel() * 8)},

@@ -25,7 +25,17 @@ BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
 LIB = BUILD / "liboracle.so"
 REF_LIB = REF_OUT / "libvcpref.so"
-REFERENCE_ROOT = Path(os.environ.get("VCP_REFERENCE_ROOT", "/root/reference"))
+# Where this recipe looks for the reference sources: the directory named by
+# VCP_REFERENCE_ROOT, else the mount point of the build container.  Callers
+# use reference_root(), which gives None (and the callers skip) when neither
+# holds the reference tree.
+_REFERENCE_MOUNT = Path("/root/reference")
+
+
+def reference_root() -> Path | None:
+    env = os.environ.get("VCP_REFERENCE_ROOT")
+    root = Path(env) if env else _REFERENCE_MOUNT
+    return root if (root / "vblas" / "rmatmul.hpp").exists() else None
 
 
 def _arch_flags() -> list[str]:
@@ -51,7 +61,8 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def build_reference(force: bool = False) -> Path | None:
-    if not (REFERENCE_ROOT / "vblas" / "rmatmul.hpp").exists():
+    ref = reference_root()
+    if ref is None:
         return None
     wrap = HERE / "ref_wrap.cpp"
     shim = sorted((HERE / "kvshim" / "kv").glob("*.hpp"))
@@ -60,7 +71,7 @@ def build_reference(force: bool = False) -> Path | None:
     if force or _stale(REF_LIB, deps):
         cmd = ["g++", "-O3", "-std=c++11", "-fopenmp", "-fPIC", "-shared", "-DNDEBUG",
                "-DKV_FASTROUND", *_arch_flags(),
-               f"-I{HERE / 'kvshim'}", f"-I{REFERENCE_ROOT}", f"-I{REFERENCE_ROOT / 'vblas'}",
+               f"-I{HERE / 'kvshim'}", f"-I{ref}", f"-I{ref / 'vblas'}",
                "-o", str(REF_LIB), str(wrap), "-lm"]
         subprocess.run(cmd, check=True)
     return REF_LIB

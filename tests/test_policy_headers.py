@@ -13,7 +13,9 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-REF = Path(os.environ.get("VCP_REFERENCE_ROOT", "/root/reference"))
+from oracle.build import reference_root
+
+REF = reference_root()
 
 PROGRAM = r'''
 #include <cstdio>
@@ -141,7 +143,7 @@ int main() {
 
 
 def test_policy_headers_compile_link_and_map_errors(tmp_path, cuda_lib):
-    if not (REF / "vcp" / "matrix.hpp").exists():
+    if REF is None or not (REF / "vcp" / "matrix.hpp").exists():
         pytest.skip("reference headers not mounted")
     src = tmp_path / "use_pidcuda.cpp"
     src.write_text(PROGRAM)
@@ -281,7 +283,7 @@ int main() {
 
 
 def test_pddcuda_header_compile_link_and_map_errors(tmp_path, cuda_lib):
-    if not (REF / "vcp" / "pddblas.hpp").exists():
+    if REF is None or not (REF / "vcp" / "pddblas.hpp").exists():
         pytest.skip("reference headers not mounted")
     src = tmp_path / "use_pddcuda.cpp"
     src.write_text(PROGRAM_DD)

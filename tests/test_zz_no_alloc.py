@@ -9,7 +9,8 @@ form, same slice count): the two run the same kernels, so the results must
 be bit-identical -- the tolerance of every Ozaki parity test here.  Two calls
 in a row with different shapes and data check that the shared static scratch
 carries no state from one call into the next.  A problem larger than the
-32 MiB static scratch must be rejected.
+32 MiB static scratch must be rejected, and a non-finite input must be
+reported by vcpcu_status exactly as the allocating entry point reports it.
 
 This file sorts last so that a run stopping at the first failure has run
 every other test first; it also passes alone in a fresh process.
@@ -20,7 +21,7 @@ import numpy as np
 import pytest
 
 from vcp_gb300 import workloads as W
-from vcp_gb300.errors import DimensionError
+from vcp_gb300.errors import DimensionError, NonFiniteError
 
 pytestmark = pytest.mark.gpu
 
@@ -61,3 +62,30 @@ def test_noalloc_rejects_problems_beyond_the_static_scratch(cuda_lib):
         # checked before any pointer is touched
         _lib.call("vcpcu_igemm_noalloc_dev", 4096, 4096, 4096, 16, 4096, 16, 4096, 16, 4096,
                   8, None)
+
+
+def test_noalloc_reports_nonfinite_input_like_the_allocating_entry_point(cuda_lib):
+    import torch
+    from vcp_gb300 import _lib
+    rng = np.random.default_rng(3)
+    m, n, k = 40, 30, 50
+    A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
+    B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
+    A[10] = np.nan
+    dA = torch.from_numpy(A).cuda()
+    dB = torch.from_numpy(B).cuda()
+    dC = torch.zeros(2 * m * n, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    _lib.call("vcpcu_igemm_noalloc_dev", m, n, k, dA.data_ptr(), m, dB.data_ptr(), k,
+              dC.data_ptr(), m, 8, s)
+    torch.cuda.synchronize()
+    with pytest.raises(NonFiniteError):
+        _lib.call("vcpcu_status", s)
+    assert torch.isnan(dC).all().item()
+    # the sticky status was taken: a clean call right after reports nothing
+    dA = torch.from_numpy(W.interval_ephi(rng, m, k, 4, 2.0 ** -40)).cuda()
+    _lib.call("vcpcu_igemm_noalloc_dev", m, n, k, dA.data_ptr(), m, dB.data_ptr(), k,
+              dC.data_ptr(), m, 8, s)
+    torch.cuda.synchronize()
+    _lib.call("vcpcu_status", s)
+    assert not torch.isnan(dC).any().item()

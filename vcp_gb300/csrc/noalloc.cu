@@ -59,19 +59,6 @@ int scratch_for_current_device(void** out) {
   return VCPCU_OK;
 }
 
-// After the three slice GEMMs: a timed-out device wait leaves the output
-// unfinished, so every entry becomes NaN (non-finite inputs are already NaN).
-__global__ void noalloc_poison_on_timeout(const int* flag, int m, int n, double* C, long ldc) {
-  if (flag[1] == 0) return;
-  const double nan = __longlong_as_double(0x7ff8000000000000LL);
-  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < (long)m * n;
-       idx += (long)gridDim.x * blockDim.x) {
-    long i = idx % m, j = idx / m;
-    C[2 * (i + j * ldc)] = nan;
-    C[2 * (i + j * ldc) + 1] = nan;
-  }
-}
-
 }  // namespace
 
 }  // namespace vcpcu
@@ -118,7 +105,10 @@ extern "C" int vcpcu_igemm_noalloc_dev(int m, int n, int k, const double* A, int
   OzWorkspace ws;
   oz_carve_workspace(plan.pb, base, &ws);
   if ((st = oz_run_product(plan, ws, A, lda, B, ldb, C, ldc, s))) return st;
-  noalloc_poison_on_timeout<<<64, 256, 0, s>>>(ws.flag, m, n, C, ldc);
-  VCPCU_LAUNCH_CHECK("noalloc_poison_on_timeout");
+  // The reassembly already writes NaN everywhere after a non-finite input or
+  // a timed-out wait; the status words go into the per-device status that
+  // vcpcu_status reports, as for vcpcu_igemm_dev.
+  oz_merge_status(ws.flag, s);
+  VCPCU_LAUNCH_CHECK("oz_status_merge");
   return VCPCU_OK;
 }

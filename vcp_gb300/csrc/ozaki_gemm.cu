@@ -32,6 +32,8 @@
 #include "swfp.cuh"
 #include "tc_ptx.cuh"
 
+#include <mutex>
+
 namespace vcpcu {
 
 namespace {
@@ -557,16 +559,32 @@ int num_sms() {
 
 size_t oz_dyn_smem() { return (size_t)OZ_STAGES * STAGE_BYTES + 1024; }
 
-int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, long ldc,
-                cudaStream_t st, int t_set) {
-  const OzProblem& pb = plan.pb;
-  static bool attr_set = false;
-  if (!attr_set) {
+// The dynamic shared-memory opt-in of the slice GEMM is a property of the
+// device context: set it once per device ordinal (under a lock, since host
+// threads may start products concurrently).
+static int oz_gemm_smem_optin() {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  int dev = 0;
+  VCPCU_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("slice GEMM: device ordinal %d out of range", dev);
+    return VCPCU_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (!done[dev]) {
     VCPCU_CUDA_TRY(cudaFuncSetAttribute(oz_slice_gemm_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)oz_dyn_smem()));
-    attr_set = true;
+    done[dev] = true;
   }
+  return VCPCU_OK;
+}
+
+int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, long ldc,
+                cudaStream_t st, int t_set) {
+  const OzProblem& pb = plan.pb;
+  if (int e = oz_gemm_smem_optin()) return e;
   OzGemmArgs a;
   memset(&a, 0, sizeof(a));
   int st_;
@@ -663,13 +681,7 @@ int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, 
 // and the padded inner dimension shared by the bucket.
 int oz_grun_gemm(const OzGBucket& b, const OzPlan& shape, int mode, int nitems, cudaStream_t st) {
   if (nitems <= 0) return VCPCU_OK;
-  static bool attr_set = false;
-  if (!attr_set) {
-    VCPCU_CUDA_TRY(cudaFuncSetAttribute(oz_slice_gemm_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)oz_dyn_smem()));
-    attr_set = true;
-  }
+  if (int e = oz_gemm_smem_optin()) return e;
   OzGemmArgs a;
   memset(&a, 0, sizeof(a));
   const size_t psA = (size_t)b.Mtot * b.Kp, psB = (size_t)b.Ntot * b.Kp;
