@@ -35,7 +35,13 @@ Our arm (default) prints one JSON line with
                         sides (--phis carries nrhs): plain vs Ozaki time,
                         width ratio, CPU restatement;
                  eig    the verification of imats::eigsymge on the GPU
-                        (vcpcu_ieigsymge stages), n x n: plain vs Ozaki.
+                        (vcpcu_ieigsymge stages), n x n: plain vs Ozaki;
+                 emden  the verified solution of -Laplace u = u^2 on the
+                        unit square (test_PDE/test_Emden.cpp), Legendre
+                        orders M (--sizes, default 30, 50, 70): Newton, the
+                        inverse-norm, residual and Kantorovich bounds, plain
+                        vs Ozaki vs the CPU pipeline; wall time per stage
+                        and the verified H^1_0 error bound.
 --impl reference times that CPU path alone as the reference arm.
 
 Inputs are 1 GiB per operand (larger than the 129 MB L2), so no L2 flush is
@@ -75,7 +81,7 @@ def parse():
     ap.add_argument("--cpu-rows", type=int, default=0, help="row sample of the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="interval",
-                    choices=["interval", "batch", "dd", "point", "lss", "eig"],
+                    choices=["interval", "batch", "dd", "point", "lss", "eig", "emden"],
                     help="interval: the headline line (default); the others print their own "
                          "line at the full sizes of that workload")
     ap.add_argument("--sizes", default="", help="point / dd: comma-separated n (or m:n:k)")
@@ -895,6 +901,60 @@ def bench_cfg1(dev, stream, n=512, steps=3, seed=5):
     return out
 
 
+def bench_emden(dev, Ms=(30, 50, 70), cpu_Ms=(30,), repeats=2):
+    """End-to-end Emden verification (-Laplace u = u^2 on the unit square,
+    test_PDE/test_Emden.cpp): Newton on the GPU (FP64), then the
+    verification in the plain and in the tensor-core form from the same
+    Newton solution; the CPU pipeline (oracle products, all host cores) on
+    the orders in cpu_Ms.  Wall times are of the last of `repeats` runs."""
+    import torch
+    from vcp_gb300 import emden as E
+    from vcp_gb300 import legendre, pidcuda
+    cases = []
+    for M in Ms:
+        rec = {"M": M, "n": ((M + 1) // 2) ** 2,
+               "points_per_dim": [E.npts_inverse(M), E.npts_residual(M)]}
+        t0 = time.perf_counter()
+        legendre.basis_tables(M, E.npts_inverse(M))
+        legendre.basis_tables(M, E.npts_residual(M))
+        rec["legendre_tables_s"] = time.perf_counter() - t0
+        g = E.GpuProducts(pidcuda.FORM_PLAIN)
+        for _ in range(repeats):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            c, it, step = E.newton(M, g)
+            torch.cuda.synchronize()
+            rec["newton"] = {"s": time.perf_counter() - t0, "iterations": it, "last_step": step}
+        for name, form in (("plain", pidcuda.FORM_PLAIN), ("ozaki", pidcuda.FORM_OZAKI)):
+            for _ in range(repeats):
+                r = E.verify(M, E.GpuProducts(form), c=c, newton_info=(it, step))
+            d = r.as_dict()
+            t_up = d["seconds"]["uhphiphi_product"]
+            rec[name] = {k: d[k] for k in ("verified", "error_bound_H10", "K", "residual_L2",
+                                           "residual_Hm1", "kantorovich", "uh_max",
+                                           "lambda_min", "lambda_max", "CN", "Cs3")}
+            rec[name]["seconds"] = d["seconds"]
+            rec[name]["verification_s"] = d["seconds"]["total"] - d["seconds"]["newton"]
+            rec[name]["uhphiphi_tflops"] = d["sizes"]["uhphiphi_flops"] / t_up / 1e12
+            torch.cuda.empty_cache()
+        rec["bound_ozaki_over_plain"] = rec["ozaki"]["error_bound_H10"] / \
+            rec["plain"]["error_bound_H10"]
+        rec["verification_speedup_ozaki_vs_plain"] = rec["plain"]["verification_s"] / \
+            rec["ozaki"]["verification_s"]
+        if M in cpu_Ms:
+            from oracle.emden_host import HostProducts
+            hp = HostProducts(cpu_count())
+            t0 = time.perf_counter()
+            cc, itc, stc = E.newton(M, hp)
+            rc = E.verify(M, hp, c=cc, newton_info=(itc, stc))
+            d = rc.as_dict()
+            rec["cpu"] = {k: d[k] for k in ("verified", "error_bound_H10", "K", "residual_L2")}
+            rec["cpu"].update({"wall_s": time.perf_counter() - t0, "cores": cpu_count(),
+                               "kind": "port", "seconds": d["seconds"]})
+        cases.append(rec)
+    return {"cases": cases}
+
+
 def parse_list(text, default, conv=int):
     return [conv(x) for x in text.split(",") if x] if text else default
 
@@ -926,6 +986,12 @@ def run_workload(args, dev, stream):
             metric, unit = ("verified generalized symmetric eigenvalues, device-resident "
                             "verification (imats::eigsymge after X, lambda, Y): ms"), "ms"
             value = min(c["ozaki"]["ms"] for c in res["cases"])
+        elif args.workload == "emden":
+            res = bench_emden(dev, tuple(parse_list(args.sizes, [30, 50, 70])),
+                              () if args.no_cpu else (30, 50))
+            metric, unit = ("Emden verification wall time (s), tensor-core form, "
+                            "largest order"), "s"
+            value = res["cases"][-1]["ozaki"]["verification_s"]
         elif args.workload == "dd":
             res = {"cases": [bench_dd(dev, stream, n, phi, steps=args.steps)
                              for n in parse_list(args.sizes, [2048, 8192])
@@ -965,7 +1031,8 @@ def bench_also(dev, stream):
                     ("lss", lambda: bench_lss(dev, stream, 2048, 1, steps=3)),
                     ("eig", lambda: bench_eig(dev, stream, 1024, steps=3)),
                     ("point", lambda: bench_point(dev, stream, 4096, 4096, 4096, 0, [6, 8],
-                                                  steps=2))):
+                                                  steps=2)),
+                    ("emden", lambda: bench_emden(dev, (30,), (30,)))):
         t0 = time.perf_counter()
         try:
             out[key] = fn()

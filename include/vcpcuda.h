@@ -244,6 +244,29 @@ int vcpcu_ilss_verify_dev(int n, int nrhs, const double* A, int lda, const doubl
 int vcpcu_ilss_verify(int n, int nrhs, const double* A, const double* b, const double* R,
                       const double* mx, double* x, double* bound, int form, int slices);
 
+/* ---- Legendre generator: tensor-product basis matrices --------------------- */
+
+/* Replaces the element loops that build the two-dimensional Legendre basis
+ * at the Gauss-Legendre points, Legendre_Bases_Generator::phi_point_set
+ * (vcp/ldbase.hpp:355-374), and the weight * uh^p scaling inside
+ * uhphiphi's element loop (vcp/ldbase.hpp:994-1001), so that uhphiphi
+ * becomes the interval product Phi diag(w uh^p) Phi^T.  Writes the n x P
+ * interval matrix (kv layout; P = nqa * nqb)
+ *   out(i, q) = Ta(ia[i], qa) * Tb(ib[i], qb) [* s1(q)] [* s2(q)],
+ *   q = qa * nqb + qb (the reference's Pointlist order),
+ * at out + 2 (i + q ld), or at out + 2 (q + i ld) when transposed (P x n).
+ * Ta, Tb: nt x nqa and nt x nqb interval tables (one-dimensional basis
+ * values, row = basis index), column-major; ia, ib: nb device ints in
+ * [0, nt) (an index outside gives a NaN entry); s1, s2: optional interval
+ * vectors of length P (NULL to skip).  Every factor is an interval product
+ * with directed rounding; accumulate adds the result to the entry already
+ * in out (round down / up).  All pointers are device pointers; interval
+ * arrays 16-byte aligned. */
+int vcpcu_tensor_basis_dev(int nb, const int* ia, const int* ib, int nt, const double* Ta,
+                           const double* Tb, int nqa, int nqb, const double* s1,
+                           const double* s2, double* out, long ld, int transposed,
+                           int accumulate, void* stream);
+
 /* ---- inf-sup interval FMA (vcp/ifma.hpp, vcp/pidblas_fma.hpp) ------------- */
 
 /* Replaces vcp::ifma (vcp/ifma.hpp:48-139), elementwise over kv pairs:

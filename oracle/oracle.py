@@ -54,6 +54,9 @@ def lib() -> C.CDLL:
         L.orc_ieigsymge.restype = _i
         L.orc_imats_mul_m_im_naive.argtypes = [_i, _i, _i, _v, _v, _v]
         L.orc_eig_merge.argtypes = [_i, _v]
+        L.orc_tensor_basis.argtypes = [_i, _v, _v, _i, _v, _v, _i, _i, _v, _v, _v, _l, _i, _i,
+                                       _i]
+        L.orc_tensor_basis.restype = _i
         _lib = L
     return _lib
 
@@ -251,6 +254,21 @@ def pidblas_fma_mulmm(m, n, k, A, B, threads=0) -> np.ndarray:
     C_ = np.empty(2 * m * n)
     lib().orc_pidblas_fma_mulmm(m, n, k, _p(A), _p(B), _p(C_), int(threads))
     return C_
+
+
+def tensor_basis(nb, ia, ib, nt, Ta, Tb, nqa, nqb, out, ld, s1=None, s2=None,
+                 transposed=False, accumulate=False, offset=0, threads=0):
+    """The tensor-product basis matrix of the GPU's vcpcu_tensor_basis_dev
+    (restatement, same roundings): writes into the kv buffer out from
+    double offset `offset`."""
+    ia = np.ascontiguousarray(ia, dtype=np.int32)
+    ib = np.ascontiguousarray(ib, dtype=np.int32)
+    o = out[offset:]
+    lib().orc_tensor_basis(int(nb), _p(ia), _p(ib), int(nt), _p(Ta), _p(Tb), int(nqa), int(nqb),
+                           None if s1 is None else _p(s1), None if s2 is None else _p(s2),
+                           _p(o), C.c_long(int(ld)), int(transposed), int(accumulate),
+                           int(threads))
+    return out
 
 
 def ref_call(name, *args):

@@ -1027,3 +1027,98 @@ int orc_pidblas_fma_mulmm(int m, int n, int k, const double* A, const double* B,
   (void)nthreads;
   return 0;
 }
+
+/* ---------------------------------------------------------------------------
+ * Tensor-product basis matrices of the Legendre generator (the GPU's
+ * vcpcu_tensor_basis_dev, restating phi_point_set, vcp/ldbase.hpp:355-374,
+ * and the weight * uh^p factor of uhphiphi's element loop, :994-1001):
+ *   out(i, q) = Ta(ia[i], qa) * Tb(ib[i], qb) [* s1(q)] [* s2(q)],
+ *   q = qa * nqb + qb, each product the min of the four endpoint products
+ *   rounded down and the max of the four rounded up; accumulate adds the
+ *   entry already in out (rounded down / up).  Row by row: every rounding
+ *   mode is set once per pass over a row's P entries.
+ * ------------------------------------------------------------------------- */
+static void imul_row(long P, const double* alo, const double* ahi, const double* b, long bstep,
+                     double* lo, double* hi) {
+  /* (alo, ahi)[q] times the kv pair b[q * bstep] for q < P */
+  fesetround(FE_DOWNWARD);
+  for (long q = 0; q < P; ++q) {
+    volatile double a0 = alo[q], a1 = ahi[q], b0 = b[2 * q * bstep], b1 = b[2 * q * bstep + 1];
+    volatile double p0 = a0 * b0, p1 = a0 * b1, p2 = a1 * b0, p3 = a1 * b1;
+    lo[q] = fmin(fmin(p0, p1), fmin(p2, p3));
+  }
+  fesetround(FE_UPWARD);
+  for (long q = 0; q < P; ++q) {
+    volatile double a0 = alo[q], a1 = ahi[q], b0 = b[2 * q * bstep], b1 = b[2 * q * bstep + 1];
+    volatile double p0 = a0 * b0, p1 = a0 * b1, p2 = a1 * b0, p3 = a1 * b1;
+    hi[q] = fmax(fmax(p0, p1), fmax(p2, p3));
+  }
+  fesetround(FE_TONEAREST);
+}
+
+int orc_tensor_basis(int nb, const int* ia, const int* ib, int nt, const double* Ta,
+                     const double* Tb, int nqa, int nqb, const double* s1, const double* s2,
+                     double* out, long ld, int transposed, int accumulate, int nthreads) {
+  const long P = (long)nqa * nqb;
+  if (nb <= 0 || P <= 0) return 0;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+#endif
+  {
+    double* buf = malloc(sizeof(double) * 6 * P);
+    double *alo = buf, *ahi = buf + P, *blo = buf + 2 * P, *bhi = buf + 3 * P;
+    double* tb = buf + 4 * P; /* kv of Tb(ib[i], qb) expanded over q */
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 4)
+#endif
+    for (int i = 0; i < nb; ++i) {
+      const int a = ia[i], b = ib[i];
+      double* o0 = transposed ? out + 2 * (long)i * ld : out + 2 * (long)i;
+      const long ostep = transposed ? 1 : ld;
+      if (a < 0 || a >= nt || b < 0 || b >= nt) {
+        for (long q = 0; q < P; ++q) o0[2 * q * ostep] = o0[2 * q * ostep + 1] = NAN;
+        continue;
+      }
+      for (long q = 0; q < P; ++q) {
+        const long qa = q / nqb, qb = q - qa * nqb;
+        alo[q] = Ta[2 * (a + qa * nt)];
+        ahi[q] = Ta[2 * (a + qa * nt) + 1];
+        tb[2 * q] = Tb[2 * (b + qb * nt)];
+        tb[2 * q + 1] = Tb[2 * (b + qb * nt) + 1];
+      }
+      imul_row(P, alo, ahi, tb, 1, blo, bhi);
+      double *clo = blo, *chi = bhi, *dlo = alo, *dhi = ahi;
+      if (s1) {
+        imul_row(P, clo, chi, s1, 1, dlo, dhi);
+        double* t = clo; clo = dlo; dlo = t;
+        t = chi; chi = dhi; dhi = t;
+      }
+      if (s2) {
+        imul_row(P, clo, chi, s2, 1, dlo, dhi);
+        double* t = clo; clo = dlo; dlo = t;
+        t = chi; chi = dhi; dhi = t;
+      }
+      if (accumulate) {
+        fesetround(FE_DOWNWARD);
+        for (long q = 0; q < P; ++q) {
+          volatile double x = clo[q], y = o0[2 * q * ostep];
+          clo[q] = x + y;
+        }
+        fesetround(FE_UPWARD);
+        for (long q = 0; q < P; ++q) {
+          volatile double x = chi[q], y = o0[2 * q * ostep + 1];
+          chi[q] = x + y;
+        }
+        fesetround(FE_TONEAREST);
+      }
+      for (long q = 0; q < P; ++q) {
+        o0[2 * q * ostep] = clo[q];
+        o0[2 * q * ostep + 1] = chi[q];
+      }
+    }
+    free(buf);
+  }
+  (void)nthreads;
+  return 0;
+}

@@ -69,6 +69,8 @@ SIGNATURES: dict[str, tuple] = {
     "vcpcu_batch_graph_latencies": (_i, [_v, _v, _v, _v]),
     "vcpcu_batch_graph_destroy": (_i, [_v]),
     "vcpcu_igemm_noalloc_dev": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _i, _i, _v]),
+    "vcpcu_tensor_basis_dev": (_i, [_i, _v, _v, _i, _v, _v, _i, _i, _v, _v, _v, C.c_long, _i,
+                                    _i, _v]),
 }
 
 
