@@ -47,15 +47,27 @@ class HostProducts:
                              np.ascontiguousarray(B[b_off:b_off + 2 * k * n]), self.threads)
         C[c_off:c_off + 2 * m * n] = Cm
 
-    def eig_verify(self, A, B, X, lam, n):
-        midB = 0.5 * (B[0::2] + B[1::2])
-        Xm = X.reshape(n, n, order="F")
-        Y = np.linalg.inv(midB.reshape(n, n, order="F") @ Xm)
-        st, out, g = O.ieigsymge(n, A, B, X, lam, np.asfortranarray(Y).ravel(order="F"),
-                                 threads=self.threads)
+    def sym_intersect(self, X, n):
+        v = X.reshape(n, n, 2)
+        lo = np.maximum(v[:, :, 0], v[:, :, 0].T)
+        hi = np.minimum(v[:, :, 1], v[:, :, 1].T)
+        v[:, :, 0] = lo
+        v[:, :, 1] = hi
+
+    def eig_enclose(self, A, B, n):
+        import time
+        import scipy.linalg
+        t0 = time.perf_counter()
+        midA = (0.5 * (A[0::2] + A[1::2])).reshape(n, n, order="F")
+        midB = (0.5 * (B[0::2] + B[1::2])).reshape(n, n, order="F")
+        lam, Xm = scipy.linalg.eigh(midA, midB)
+        Y = np.linalg.inv(midB @ Xm)
+        t1 = time.perf_counter()
+        st, out, g = O.ieigsymge(n, A, B, np.asfortranarray(Xm).ravel(order="F"), lam,
+                                 np.asfortranarray(Y).ravel(order="F"), threads=self.threads)
         if st != 0:
             raise RuntimeError(f"eigenvalue verification failed (||YBX - I|| bound {g})")
-        return out, g
+        return out, g, t1 - t0, time.perf_counter() - t1
 
     def newton_setup(self, Phi, w2, DL):
         self._Phi, self._w2, self._DL = Phi, w2, DL

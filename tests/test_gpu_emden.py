@@ -6,8 +6,9 @@
   a list index outside the table gives NaN entries instead of a read out of
   bounds;
 * the interval matrix 2 (uh phi_i, phi_j) = 2 Phi diag(w uh) Phi^T of the
-  M = 30 problem: the plain form bit-identical to the CPU pipeline (oracle
-  pidblas), the tensor-core form bit-identical to its host model;
+  M = 30 problem (entries (i, j) and (j, i) intersected): the plain form
+  bit-identical to the CPU pipeline (oracle pidblas), the tensor-core form
+  bit-identical to its host model;
 * M = 30 end to end from one Newton solution: the plain and the tensor-core
   forms both close the Kantorovich check, the tensor-core bound is no
   looser than the plain one (tolerance 1e-9 relative: the two differ only
@@ -52,13 +53,15 @@ def test_tensor_basis_bitexact_oracle(cuda_lib, oracle, flags):
     cols = nb if tr else P
     init = ivtab(ld, cols)
     ref = oracle.tensor_basis(nb, ia, ib, nt, Ta, Tb, nqa, nqb, init.copy(), ld, s1, s2, tr, acc)
-    d = lambda x: torch.from_numpy(x).cuda()  # noqa: E731
-    out = d(init.copy())
+    # keep every device copy alive until the kernel has run
+    dev = {k: torch.from_numpy(v).cuda() for k, v in
+           dict(ia=ia, ib=ib, Ta=Ta, Tb=Tb, s1=s1, s2=s2, out=init.copy()).items()
+           if v is not None}
+    ptr = lambda k: dev[k].data_ptr() if k in dev else None  # noqa: E731
     s = torch.cuda.current_stream().cuda_stream
-    _lib.call("vcpcu_tensor_basis_dev", nb, d(ia).data_ptr(), d(ib).data_ptr(), nt,
-              d(Ta).data_ptr(), d(Tb).data_ptr(), nqa, nqb,
-              None if s1 is None else d(s1).data_ptr(), None if s2 is None else d(s2).data_ptr(),
-              out.data_ptr(), ld, int(tr), int(acc), s)
+    _lib.call("vcpcu_tensor_basis_dev", nb, ptr("ia"), ptr("ib"), nt, ptr("Ta"), ptr("Tb"), nqa,
+              nqb, ptr("s1"), ptr("s2"), ptr("out"), ld, int(tr), int(acc), s)
+    out = dev["out"]
     torch.cuda.synchronize()
     assert np.array_equal(bits(out.cpu().numpy()), bits(ref))
 
@@ -92,9 +95,11 @@ def test_uhphiphi_plain_matches_cpu_and_ozaki_matches_model(cuda_lib, oracle, ne
     c = newton30[0]
     A_cpu, B_cpu, _, sz = E.inverse_norm_matrices(30, c, HostProducts())
     A_pl, B_pl, _, _ = E.inverse_norm_matrices(30, c, E.GpuProducts(pidcuda.FORM_PLAIN))
+    A_pl, B_pl = A_pl.cpu().numpy(), B_pl.cpu().numpy()
     assert np.array_equal(bits(A_pl), bits(A_cpu))
     assert np.array_equal(bits(B_pl), bits(B_cpu))
     A_oz, _, _, _ = E.inverse_norm_matrices(30, c, E.GpuProducts(pidcuda.FORM_OZAKI))
+    A_oz = A_oz.cpu().numpy()
     # the tensor-core product of the same factors, on the host model
     n, P = sz["n"], sz["points"]
     hp = HostProducts()
@@ -120,6 +125,7 @@ def test_uhphiphi_plain_matches_cpu_and_ozaki_matches_model(cuda_lib, oracle, ne
     hp.tensor(n, ia, ib, 30, Tphi, Tphi, N, N, PhiT, P, transposed=True)
     ref, st = oracle.ozaki_igemm(n, n, P, Phi, PhiT, 8, 2, crt=True)
     assert st == 0
+    hp.sym_intersect(ref, n)
     assert np.array_equal(bits(A_oz), bits(2.0 * ref))
     # both enclose the same matrix: the enclosures intersect
     assert np.all(A_oz[0::2] <= A_pl[1::2]) and np.all(A_pl[0::2] <= A_oz[1::2])

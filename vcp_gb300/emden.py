@@ -102,21 +102,25 @@ def _frac_up(fr: Fraction) -> float:
 def stiffness(M: int, ia: np.ndarray, ib: np.ndarray):
     """DL = ((grad phi_r, grad phi_s))_{r,s} for the basis list (ia, ib):
     D1 (x) L1 + L1 (x) D1 evaluated exactly, rounded outward.  Returns
-    (lo, hi, mid) n x n arrays (mid = nearest double)."""
+    (lo, hi, mid) n x n arrays (mid = nearest double).  Only |a - c| and
+    |b - d| in {0, 2} give non-zero entries (L1 is pentadiagonal with a zero
+    first off-diagonal, D1 diagonal), so each row visits nine neighbours."""
     L1, D1 = _one_dim(M)
     n = ia.size
+    where = {(int(a), int(b)): r for r, (a, b) in enumerate(zip(ia, ib))}
     lo = np.zeros((n, n))
     hi = np.zeros((n, n))
     mid = np.zeros((n, n))
     for r in range(n):
         a, b = int(ia[r]), int(ib[r])
-        for s in range(n):
-            c, d = int(ia[s]), int(ib[s])
-            if abs(a - c) > 2 or abs(b - d) > 2:
-                continue
-            v = (D1[a] if a == c else 0) * L1[b][d] + L1[a][c] * (D1[b] if b == d else 0)
-            if v != 0:
-                lo[r, s], hi[r, s], mid[r, s] = _frac_down(v), _frac_up(v), float(v)
+        for c in (a - 2, a, a + 2):
+            for d in (b - 2, b, b + 2):
+                s = where.get((c, d))
+                if s is None:
+                    continue
+                v = (D1[a] if a == c else 0) * L1[b][d] + L1[a][c] * (D1[b] if b == d else 0)
+                if v != 0:
+                    lo[r, s], hi[r, s], mid[r, s] = _frac_down(v), _frac_up(v), float(v)
     return lo, hi, mid
 
 
@@ -213,8 +217,60 @@ class GpuProducts:
         self.pid.mulmm_dev(m, n, k, A[a_off:], lda, B[b_off:], ldb, C[c_off:], ldc, self.form,
                            self.slices)
 
-    def eig_verify(self, A: np.ndarray, B: np.ndarray, X: np.ndarray, lam: np.ndarray, n: int):
-        return self.pid.eigsymge_verify(A, B, X, lam, n, form=self.form, slices=self.slices)
+    def sym_intersect(self, X, n: int):
+        """In place: entries (i, j) and (j, i) of the n x n interval matrix X
+        both enclose one value of a symmetric matrix; keep their
+        intersection (symmetric, no wider than either)."""
+        t = self.torch
+        v = X.view(n, n, 2)
+        lo = t.maximum(v[:, :, 0], v[:, :, 0].T)
+        hi = t.minimum(v[:, :, 1], v[:, :, 1].T)
+        v[:, :, 0] = lo
+        v[:, :, 1] = hi
+
+    def eig_enclose(self, A, B, n: int):
+        """Verified eigenvalues of A x = lambda B x (device kv buffers):
+        approximate eigenpairs of the midpoint problem by Cholesky reduction
+        and a symmetric eigensolver on the GPU (the reference: LAPACK
+        dsygv), then imats::eigsymge's verification on the device, Y the
+        inverse of mid(B X), and the reference's overlap merge.  Returns
+        (kv enclosures on the host, sup ||Y B X - I||, seconds of the
+        approximation, seconds of the verification)."""
+        t = self.torch
+        from . import _lib
+        t0 = time.perf_counter()
+        Av, Bv = A.view(n, n, 2), B.view(n, n, 2)
+        midA = 0.5 * (Av[:, :, 0] + Av[:, :, 1])   # symmetric: row- / column-major alike
+        midB = 0.5 * (Bv[:, :, 0] + Bv[:, :, 1])
+        Lc = t.linalg.cholesky(midB)
+        Li = t.linalg.solve_triangular(Lc, t.eye(n, dtype=t.float64, device=self.dev),
+                                       upper=False)
+        lam, Vec = t.linalg.eigh(Li @ midA @ Li.T)
+        Xr = Li.T @ Vec                                # columns: eigenvectors
+        X = Xr.T.contiguous()                          # row-major (n, n) = column-major X
+        lam = lam.contiguous()
+        self.sync()
+        t1 = time.perf_counter()
+        s = t.cuda.current_stream().cuda_stream
+        C = self.empty(2 * n * n)
+        BX = self.empty(2 * n * n)
+        midBX = self.empty(n * n)
+        _lib.call("vcpcu_ieigsymge_stage1_dev", n, A.data_ptr(), n, B.data_ptr(), n,
+                  X.data_ptr(), n, C.data_ptr(), BX.data_ptr(), midBX.data_ptr(), self.form,
+                  self.slices, s)
+        Y = t.linalg.inv(midBX.view(n, n).T).T.contiguous()   # column-major inverse
+        enc = self.empty(2 * n)
+        bound = self.empty(1)
+        _lib.call("vcpcu_ieigsymge_stage2_dev", n, lam.data_ptr(), Y.data_ptr(), n,
+                  C.data_ptr(), BX.data_ptr(), enc.data_ptr(), bound.data_ptr(), self.form,
+                  self.slices, s)
+        E = enc.cpu().numpy()
+        g = float(bound.cpu().item())
+        if not g < 1.0:
+            from .errors import VerificationError
+            raise VerificationError(f"eigenvalue verification failed: ||YBX - I|| <= {g}")
+        _lib.call("vcpcu_eig_merge", n, E.ctypes.data)
+        return E, g, t1 - t0, time.perf_counter() - t1
 
     def sync(self):
         self.torch.cuda.synchronize()
@@ -316,7 +372,7 @@ def uh_max_bound(M: int, c: np.ndarray, prod, h_exp: int = 9) -> float:
     h = 2.0 ** -h_exp
     g = 2 ** (h_exp - 1)
     centres = (np.arange(g) + 0.5) * h
-    lo, hi = legendre.basis_at_points(M, centres)
+    lo, hi = legendre.basis_at_points(M, centres, cache_key=f"grid_h{h_exp}")
     lo, hi = lo[0::2], hi[0::2]                      # the even basis functions, mn x g
     Cm = c.reshape(mn, mn)                           # C[i0, i1] = c[i0 * mn + i1]
     Ckv = table_kv(Cm, Cm)                           # mn x mn, column-major
@@ -362,10 +418,11 @@ def inverse_norm_matrices(M: int, c: np.ndarray, prod, tables=None):
     prod.igemm(nb, nb, P, Phi, nb, PhiT, P, UPP, nb)              # the n x n x P product
     prod.sync()
     t2 = time.perf_counter()
-    A = 2.0 * prod.to_host(UPP)                                  # exact doubling
     del Phi, PhiT
+    prod.sym_intersect(UPP, nb)
+    A = 2.0 * UPP                                                 # exact doubling
     lo, hi, _ = stiffness(M, ia, ib)
-    B = table_kv(lo, hi)
+    B = prod.to_dev(table_kv(lo, hi))
     return A, B, {"basis_tables_to_factors": t1 - t0, "uhphiphi_product": t2 - t1}, \
         {"n": nb, "points": P, "uhphiphi_flops": 2.0 * nb * nb * P}
 
@@ -421,16 +478,9 @@ def verify(M: int, prod, c: np.ndarray | None = None, newton_info=(0, 0.0)) -> E
     A, B, s_inv, sizes = inverse_norm_matrices(M, c, prod, T1)
     secs.update(s_inv)
     n = sizes["n"]
-    # approximate eigenpairs of mid(A) x = lambda mid(B) x (the reference:
-    # LAPACK dsygv inside imats::eigsymge)
-    import scipy.linalg
-    midA = 0.5 * (A[0::2] + A[1::2])
-    midB = 0.5 * (B[0::2] + B[1::2])
-    lam, X = scipy.linalg.eigh(midA.reshape(n, n, order="F"), midB.reshape(n, n, order="F"))
-    t2 = time.perf_counter()
-    E, _ = prod.eig_verify(A, B, np.asfortranarray(X).ravel(order="F"), lam, n)
-    prod.sync()
-    secs["eigsymge_verify"] = time.perf_counter() - t2
+    E, _, t_apx, t_ver = prod.eig_enclose(A, B, n)
+    secs["eig_approximate"] = t_apx
+    secs["eigsymge_verify"] = t_ver
     secs["inverse_norm_total"] = time.perf_counter() - t
     CN = ritz_constant(M)
     Cp = poincare_constant(2)

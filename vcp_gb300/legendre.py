@@ -198,12 +198,31 @@ def basis_tables(M: int, npts: int, use_cache: bool = True) -> dict:
     return out
 
 
-def basis_at_points(M: int, t: np.ndarray):
+def basis_at_points(M: int, t: np.ndarray, cache_key: str | None = None):
     """Double-interval enclosures of phi_2..phi_{M+1} at the points t of
     [0, 1] (doubles, taken as exact): s = 2 t - 1 is exact in double, the
-    recurrences run in iv at s.  Returns (lo, hi), each (M x len(t))."""
-    mpmath = _setup_precision()
+    recurrences run in iv at s.  Returns (lo, hi), each (M x len(t)); with
+    cache_key, cached like the Gauss tables under that name."""
     t = np.asarray(t, dtype=np.float64)
+    path = _CACHE / f"points_{cache_key}_M{M}_n{t.size}_v{_VERSION}.npz" if cache_key else None
+    if path is not None and path.exists():
+        with np.load(path) as z:
+            if np.array_equal(z["t"], t):
+                return z["lo"], z["hi"]
+    lo, hi = _basis_at_points(M, t)
+    if path is not None:
+        try:
+            _CACHE.mkdir(parents=True, exist_ok=True)
+            tmp = path.with_suffix(".tmp.npz")
+            np.savez(tmp, t=t, lo=lo, hi=hi)
+            os.replace(tmp, path)
+        except OSError:
+            pass
+    return lo, hi
+
+
+def _basis_at_points(M: int, t: np.ndarray):
+    mpmath = _setup_precision()
     lo = np.empty((M, t.size))
     hi = np.empty_like(lo)
     for q, tq in enumerate(t):
