@@ -303,6 +303,23 @@ int vcpcu_igemm_fma(int m, int n, int k, const double* A, const double* B, doubl
  * a single product (batched = 0) or as one problem of a batch (batched != 0:
  * the batch's grouped launches carry no per-product launch cost). */
 int vcpcu_autotune(void* stream, double* constants);
+
+/* The AUTO decision for a product C = [A] [B] (A m x k, B k x n, kv layout,
+ * host or device pointers): *form = VCPCU_FORM_PLAIN or VCPCU_FORM_OZAKI
+ * and *slices the tensor-core slice count, chosen per (inner dimension,
+ * exponent spread, radius size) as the smallest of 6, 7, 8, 9 whose
+ * enclosures a probe finds no wider than the plain form's -- the probe
+ * multiplies a block of up to 64 rows of A and up to 64 evenly spaced
+ * columns of B in the plain form and at every candidate and compares the
+ * widths (the largest sampled ratio below 1 by at least 2^-16 and by a
+ * fifth of its distance from the 90th percentile, and at most 1/2 where it
+ * exceeds 4 x the median) -- or the plain form when none qualifies;
+ * choices are kept for the process (vcpcu_autotune forgets them).  Replaces the reference's
+ * fixed split geometry of pddblas_assist::split_shift / max_slices
+ * (vcp/pddblas.hpp:54-78), which ignores the width.  Synchronises the
+ * stream. */
+int vcpcu_autotune_pick(int m, int n, int k, const double* A, int lda, const double* B,
+                        int ldb, int* form, int* slices, void* stream);
 int vcpcu_autotune_choice(int m, int n, int k, int batched);
 
 /* ---- batches of uneven interval GEMMs -------------------------------------- */

@@ -1,6 +1,11 @@
-"""GPU tests of FORM_AUTO: the calibration returns sane constants, and an AUTO
-product is bit-identical to the product in the form the cost model picks,
-for single products and for a batch that mixes both forms."""
+"""GPU tests of FORM_AUTO: the calibration returns sane constants; an AUTO
+product is bit-identical to the product in the form and slice count the
+autotuner picks (vcpcu_autotune_pick), for single products and for a batch
+that mixes both forms; over inner dimensions {2048, 8192}, exponent spreads
+{0, 8, 32} and radius ratios {0, 2^-40, 2^-20} the AUTO enclosures are never
+wider than the plain form's (the tuner falls back to the plain form where no
+slice count qualifies: a 2^64 exponent spread at k = 2048, radii of 2^-20),
+and the picks are the ones the host models give for the same probe."""
 import numpy as np
 import pytest
 
@@ -29,7 +34,9 @@ def test_auto_equals_chosen_form(cuda_lib, mnk):
     C = torch.empty(2 * m * n, dtype=torch.float64, device="cuda")
     R = torch.empty_like(C)
     pidcuda.mulmm_dev(m, n, k, A, m, B, k, C, m, pidcuda.FORM_AUTO)
-    pidcuda.mulmm_dev(m, n, k, A, m, B, k, R, m, pidcuda.autotune_choice(m, n, k))
+    form, slices = pidcuda.autotune_pick(A, B, m, n, k)
+    assert form == pidcuda.autotune_choice(m, n, k)
+    pidcuda.mulmm_dev(m, n, k, A, m, B, k, R, m, form, slices)
     torch.cuda.synchronize()
     assert torch.equal(C.view(torch.int64), R.view(torch.int64))
 
@@ -56,3 +63,45 @@ def test_auto_batch_mixes_forms(cuda_lib):
         assert torch.equal(C.view(torch.int64), ref.view(torch.int64)), (m, n, k)
     g.close()
     assert forms == {pidcuda.FORM_PLAIN, pidcuda.FORM_OZAKI}
+
+
+# (k, phi, radius ratio) -> slice count the probe picks (0: plain form); the
+# host models of both forms give these picks for the probe's rows 96..159 and
+# columns 0, 4, .., 252 of these seeded 256 x 256 products.
+AUTO_PICKS = {(2048, 0, 0.0): 8, (2048, 0, 2.0 ** -40): 8, (2048, 0, 2.0 ** -20): 0,
+              (2048, 8, 0.0): 8, (2048, 8, 2.0 ** -40): 8, (2048, 8, 2.0 ** -20): 0,
+              (2048, 32, 0.0): 0, (2048, 32, 2.0 ** -40): 0, (2048, 32, 2.0 ** -20): 0,
+              (8192, 0, 0.0): 8, (8192, 0, 2.0 ** -40): 8, (8192, 0, 2.0 ** -20): 0,
+              (8192, 8, 0.0): 8, (8192, 8, 2.0 ** -40): 8, (8192, 8, 2.0 ** -20): 0,
+              (8192, 32, 0.0): 8, (8192, 32, 2.0 ** -40): 0, (8192, 32, 2.0 ** -20): 0}
+
+
+@pytest.mark.parametrize("case", sorted(AUTO_PICKS), ids=lambda c: f"k{c[0]}-phi{c[1]}-r{c[2]:.0e}")
+def test_auto_never_wider_than_plain(cuda_lib, case):
+    k, phi, rr = case
+    m = n = 256
+    pidcuda.autotune()  # forget choices other tests made for the same key
+    rng = np.random.default_rng(2000 * phi + k + (rr > 0) + (rr > 1e-9))
+    A = W.interval_ephi(rng, m, k, phi, rr)
+    B = W.interval_ephi(rng, k, n, phi, rr)
+    form, slices = pidcuda.autotune_pick(A, B, m, n, k)
+    assert slices == AUTO_PICKS[case]
+    assert form == (pidcuda.FORM_OZAKI if slices else pidcuda.FORM_PLAIN)
+    Ca = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_AUTO)
+    Cp = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_PLAIN)
+    assert np.all(Ca[1::2] - Ca[0::2] <= Cp[1::2] - Cp[0::2])
+    if slices:
+        Co = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=slices)
+        assert np.array_equal(Ca.view(np.int64), Co.view(np.int64))
+
+
+def test_auto_pick_same_from_host_and_device_pointers(cuda_lib):
+    import torch
+    rng = np.random.default_rng(11)
+    m, n, k = 300, 280, 4000
+    pidcuda.autotune()
+    A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
+    B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
+    h = pidcuda.autotune_pick(A, B, m, n, k)
+    d = pidcuda.autotune_pick(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda(), m, n, k)
+    assert h == d == (pidcuda.FORM_OZAKI, 8)

@@ -63,6 +63,7 @@ SIGNATURES: dict[str, tuple] = {
     "vcpcu_igemm_fma": (_i, [_i, _i, _i, _v, _v, _v]),
     "vcpcu_autotune": (_i, [_v, _v]),
     "vcpcu_autotune_choice": (_i, [_i, _i, _i, _i]),
+    "vcpcu_autotune_pick": (_i, [_i, _i, _i, _v, _i, _v, _i, _v, _v, _v]),
     "vcpcu_igemm_batched_dev": (_i, [_i, _v, _i, _i, _v]),
     "vcpcu_batch_graph_create": (_i, [_i, _v, _i, _i, _v, _v]),
     "vcpcu_batch_graph_launch": (_i, [_v, _v]),

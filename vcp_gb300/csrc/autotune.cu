@@ -8,14 +8,29 @@
 // plain and two Ozaki products), kept for the process and optionally stored
 // in / loaded from the file named by VCPCU_AUTOTUNE_CACHE.  Until a
 // calibration runs, conservative GB300 defaults are used.
+//
+// When the tensor-core form is the faster one, autotune_pick also chooses
+// its slice count from the operands: the smallest s in {6, 7, 8, 9}
+// (w = 42, 49, 56, 62 bit midpoints) whose enclosures are no wider than the
+// plain form's, else the plain form itself.  The choice is made per key
+// (ceil log2 k, exponent spread of the rows of A plus the columns of B in
+// steps of 4, radius-to-midpoint exponent in steps of 4), on a probe: a
+// block of up to 64 rows of A and up to 64 evenly spaced columns of B,
+// multiplied in the plain form and at every candidate s, the width ratios
+// compared on the host; the result is kept for the process.
 #include "common.cuh"
 #include "ozaki.cuh"
 #include "variants.cuh"
 
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <map>
 #include <mutex>
+#include <tuple>
+#include <vector>
 
 namespace vcpcu {
 
@@ -79,6 +94,78 @@ __global__ void fill_intervals(long n, double* X, unsigned seed) {
   }
 }
 
+// Exponent statistics of a sample: out[0] = max over the rows of the
+// S_r x K block As (kv, ld S_r) of (largest - smallest exponent of a
+// non-zero midpoint), out[1] the same over the columns of the K x S_c block
+// Bs (ld K), out[2] = max over both of (exponent of the radius - exponent
+// of the midpoint) where both are non-zero (INT_MIN + 1 if none).  One warp
+// per row / column; midpoint and radius are (lo + up) / 2 and (up - lo) / 2
+// in round-to-nearest (statistics only).
+__device__ __forceinline__ void mid_rad_exp(const double* p, int* em, int* er) {
+  const double lo = p[0], up = p[1];
+  const double m = 0.5 * lo + 0.5 * up, r = 0.5 * up - 0.5 * lo;
+  *em = m != 0.0 ? ilogb(m) : INT_MIN;
+  *er = r > 0.0 ? ilogb(r) : INT_MIN;
+}
+
+__global__ void spread_stats_kernel(int Sr, int K, const double* __restrict__ As, int Sc,
+                                    const double* __restrict__ Bs, int* __restrict__ out) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= Sr + Sc) return;
+  const bool row = warp < Sr;
+  const int idx = row ? warp : warp - Sr;
+  int emax = INT_MIN, emin = INT_MAX, rr = INT_MIN + 1;
+  for (int p = lane; p < K; p += 32) {
+    const double* e = row ? As + 2 * ((long)idx + (long)p * Sr) : Bs + 2 * ((long)p + (long)idx * K);
+    int em, er;
+    mid_rad_exp(e, &em, &er);
+    if (em != INT_MIN) {
+      emax = max(emax, em);
+      emin = min(emin, em);
+      if (er != INT_MIN) rr = max(rr, er - em);
+    }
+  }
+  for (int o = 16; o; o >>= 1) {
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    emin = min(emin, __shfl_xor_sync(0xffffffffu, emin, o));
+    rr = max(rr, __shfl_xor_sync(0xffffffffu, rr, o));
+  }
+  if (lane == 0) {
+    if (emax != INT_MIN) atomicMax(out + (row ? 0 : 1), emax - emin);
+    atomicMax(out + 2, rr);
+  }
+}
+
+struct TuneKey {
+  int klog, phi, rr;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(klog, phi, rr) < std::tie(o.klog, o.phi, o.rr);
+  }
+};
+std::map<TuneKey, int> g_slices;  // key -> slice count, 0 = plain form
+std::mutex g_slices_mu;
+
+// Accept slice count s on the probe's width ratios r (tensor-core / plain):
+// the largest ratio must stay below 1 by at least 2^-16 and by a fifth of
+// its distance from the 90th percentile (entries of the full product lie
+// further out in the same tail), and when the ratios spread widely (largest
+// above 4 x the median: large exponent spreads, whose tails are long) the
+// largest must be at most 1/2.  Calibrated on the host models over inner
+// dimensions 512 - 8192, exponent spreads 0 - 32 and radius ratios 0 -
+// 2^-20: no accepted choice gave a wider entry of a 256 x 256 product.
+bool probe_accepts(std::vector<double>& r) {
+  if (r.empty()) return true;
+  for (double v : r)
+    if (!(v == v) || v == INFINITY) return false;
+  std::sort(r.begin(), r.end());
+  const size_t n = r.size();
+  const double mx = r[n - 1], med = r[n / 2], q90 = r[(9 * n) / 10];
+  const double gap = 1.0 - mx;
+  if (gap < 0x1p-16 || gap < 0.2 * (mx - q90)) return false;
+  if (mx > 4.0 * med && mx > 0.5) return false;
+  return true;
+}
+
 }  // namespace
 
 // Predicted seconds of a product in each form (for the AUTO choice).  In a
@@ -100,9 +187,98 @@ int autotune_choose(int m, int n, int k, bool batched) {
   return to < tp ? VCPCU_FORM_OZAKI : VCPCU_FORM_PLAIN;
 }
 
+int autotune_pick(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
+                  cudaStream_t s, int* form, int* slices) {
+  *form = autotune_choose(m, n, k);
+  *slices = 0;
+  if (*form == VCPCU_FORM_PLAIN || m <= 0 || n <= 0 || k <= 0) return VCPCU_OK;
+  const int Sr = m < 64 ? m : 64, Sc = n < 64 ? n : 64;
+  const int i0 = (m - Sr) / 2, cstride = n / Sc;
+  const size_t na = 2 * (size_t)Sr * k, nb = 2 * (size_t)k * Sc, nc = 2 * (size_t)Sr * Sc;
+  Scratch buf;
+  int st = buf.alloc(sizeof(double) * (na + nb + 5 * nc) + 64, s);
+  if (st) return st;
+  double* As = (double*)buf.ptr;
+  double* Bs = As + na;
+  double* Cs = Bs + nb;  // plain, then s = 6, 7, 8, 9
+  int* stats = (int*)(Cs + 5 * nc);
+  VCPCU_CUDA_TRY(cudaMemcpy2DAsync(As, Sr * 16, A + 2 * (size_t)i0, lda * 16, Sr * 16, k,
+                                   cudaMemcpyDefault, s));
+  for (int c = 0; c < Sc; ++c)  // column c * cstride of B (contiguous)
+    VCPCU_CUDA_TRY(cudaMemcpyAsync(Bs + 2 * (size_t)k * c, B + 2 * (size_t)c * cstride * ldb,
+                                   (size_t)k * 16, cudaMemcpyDefault, s));
+  const int init[3] = {0, 0, INT_MIN + 1};
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(stats, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  spread_stats_kernel<<<(Sr + Sc + 7) / 8, 256, 0, s>>>(Sr, k, As, Sc, Bs, stats);
+  VCPCU_LAUNCH_CHECK("spread_stats_kernel");
+  int h[3];
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(h, stats, sizeof(h), cudaMemcpyDeviceToHost, s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  int klog = 0;
+  while ((1L << klog) < k) ++klog;
+  const int phi = (h[0] + h[1] + 3) / 4;
+  const int rr = h[2] <= -80 ? -1000 : (h[2] >= 0 ? 0 : -((-h[2]) / 4));
+  const TuneKey key{klog, phi, rr};
+  {
+    std::lock_guard<std::mutex> lk(g_slices_mu);
+    auto it = g_slices.find(key);
+    if (it != g_slices.end()) {
+      *slices = it->second;
+      *form = it->second ? VCPCU_FORM_OZAKI : VCPCU_FORM_PLAIN;
+      return VCPCU_OK;
+    }
+  }
+  // probe: the plain form and every candidate on the sampled block
+  if ((st = igemm_any(Sr, Sc, k, As, Sr, Bs, k, Cs, Sr, VCPCU_FORM_PLAIN, 0, s))) return st;
+  const int cand[4] = {6, 7, 8, 9};
+  for (int c = 0; c < 4; ++c)
+    if ((st = ozaki_igemm(Sr, Sc, k, As, Sr, Bs, k, Cs + (c + 1) * nc, Sr, VCPCU_FORM_OZAKI,
+                          cand[c], s)))
+      return st;
+  std::vector<double> hc(5 * nc);
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(hc.data(), Cs, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost,
+                                 s));
+  VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
+  int choice = 0;
+  for (int c = 0; c < 4 && !choice; ++c) {
+    std::vector<double> r;
+    r.reserve(nc / 2);
+    const double* P = hc.data();
+    const double* O = hc.data() + (c + 1) * nc;
+    for (size_t e = 0; e < nc / 2; ++e) {
+      const double wp = P[2 * e + 1] - P[2 * e], wo = O[2 * e + 1] - O[2 * e];
+      r.push_back(wp > 0.0 ? wo / wp : (wo > 0.0 ? INFINITY : 0.0));
+    }
+    if (probe_accepts(r)) choice = cand[c];
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_slices_mu);
+    g_slices[key] = choice;
+  }
+  *slices = choice;
+  *form = choice ? VCPCU_FORM_OZAKI : VCPCU_FORM_PLAIN;
+  return VCPCU_OK;
+}
+
 }  // namespace vcpcu
 
 using namespace vcpcu;
+
+extern "C" int vcpcu_autotune_pick(int m, int n, int k, const double* A, int lda, const double* B,
+                                   int ldb, int* form, int* slices, void* stream) {
+  clear_error();
+  if (!form || !slices) {
+    set_error("autotune_pick: null output pointer");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  if (m > 0 && n > 0 && k > 0 && (!A || !B || lda < m || ldb < k)) {
+    set_error("autotune_pick: null operand or leading dimension too small");
+    return VCPCU_ERR_INVALID_ARG;
+  }
+  int st = check_device();
+  if (st) return st;
+  return autotune_pick(m, n, k, A, lda, B, ldb, (cudaStream_t)stream, form, slices);
+}
 
 extern "C" int vcpcu_autotune(void* stream, double* constants) {
   clear_error();
@@ -140,6 +316,10 @@ extern "C" int vcpcu_autotune(void* stream, double* constants) {
   const double prep_t = b - 12.0 * m.t_launch;
   m.prep_bw = prep_t > 0 ? 16.0 * 2.0 * n2 * (double)n2 / prep_t : 5e12;
   m.calibrated = true;
+  {
+    std::lock_guard<std::mutex> lk(g_slices_mu);
+    g_slices.clear();  // slice choices are re-made under the new constants
+  }
   {
     std::lock_guard<std::mutex> lk(g_model_mu);
     g_model = m;

@@ -156,9 +156,12 @@ int vcpcu::igemm_any(int m, int n, int k, const double* A, long lda, const doubl
                      double* C, long ldc, int form, int slices, cudaStream_t s, int point_mask) {
   if (k < 0) k = 0;
   if (form == VCPCU_FORM_AUTO) {
-    form = autotune_choose(m, n, k);
-    if (form != VCPCU_FORM_PLAIN && k > 0 && ((((uintptr_t)A) | ((uintptr_t)B)) & 15) != 0)
+    if (k > 0 && ((((uintptr_t)A) | ((uintptr_t)B)) & 15) != 0) {
       form = VCPCU_FORM_PLAIN;  // the tensor-core form reads 16-byte pairs
+    } else {
+      int st = autotune_pick(m, n, k, A, lda, B, ldb, s, &form, &slices);
+      if (st) return st;
+    }
   }
   if (form == VCPCU_FORM_PLAIN) {
     Scratch ws;
@@ -431,7 +434,16 @@ int vcpcu_igemm(int m, int n, int k, const double* A, const double* B, double* C
   if (st) return st;
   if (k < 0) k = 0;
   cudaStream_t s = host_stream();
-  const int resolved = form == VCPCU_FORM_AUTO ? autotune_choose(m, n, k) : form;
+  int resolved = form;
+  if (form == VCPCU_FORM_AUTO) {
+    if (k > 0 && ((((uintptr_t)A) | ((uintptr_t)B)) & 15) != 0) {
+      resolved = VCPCU_FORM_PLAIN;
+    } else {
+      st = autotune_pick(m, n, k, A, m, B, k, s, &resolved, &slices);
+      if (st) return st;
+    }
+    form = resolved;
+  }
   const int panels = host_panels(n), row_panels = host_row_panels(m, n);
   if (resolved == VCPCU_FORM_OZAKI && panels * row_panels > 1) {
     st = ozaki_igemm_host_pipelined(m, n, k, A, B, C, slices, panels, row_panels, s,

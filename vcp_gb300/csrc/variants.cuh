@@ -9,6 +9,13 @@ namespace vcpcu {
 // grouped batch (no per-product launch cost).
 int autotune_choose(int m, int n, int k, bool batched = false);
 
+// The AUTO decision for these operands (host or device pointers): the form
+// of autotune_choose and, for the tensor-core form, the slice count whose
+// enclosures the probe finds no wider than the plain form's (*slices = 0
+// with *form = VCPCU_FORM_PLAIN when no candidate qualifies).
+int autotune_pick(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
+                  cudaStream_t s, int* form, int* slices);
+
 // Interval product of either form on device pointers (defined in capi.cu).
 // point_mask bit 0 / bit 1: A / B has zero radii (the tensor-core form then
 // skips the radius product that vanishes; the result is the same).

@@ -227,6 +227,21 @@ def autotune_choice(m: int, n: int, k: int, batched: bool = False) -> int:
     return int(_lib.load().vcpcu_autotune_choice(int(m), int(n), int(k), int(bool(batched))))
 
 
+def autotune_pick(A, B, m: int, n: int, k: int, stream=None) -> tuple[int, int]:
+    """(form, slices) that FORM_AUTO uses for [A] [B] (kv buffers: numpy
+    host arrays or float64 CUDA tensors): the tensor-core slice count whose
+    enclosures are no wider than the plain form's on a probe, or FORM_PLAIN."""
+    import ctypes
+    f, s = ctypes.c_int(0), ctypes.c_int(0)
+    if isinstance(A, np.ndarray):
+        pa, pb = _host_ptr(A, 2 * m * k, "A"), _host_ptr(B, 2 * k * n, "B")
+    else:
+        pa, pb = _dev_ptr(A, "A"), _dev_ptr(B, "B")
+    _lib.call("vcpcu_autotune_pick", m, n, k, pa, m, pb, k, ctypes.addressof(f),
+              ctypes.addressof(s), _stream_ptr(stream))
+    return f.value, s.value
+
+
 # ---- inf-sup interval FMA (vcp::ifma) and its product (vcp::pidblas_fma) ------------
 
 def ifma(A: np.ndarray, B: np.ndarray, C: np.ndarray) -> np.ndarray:
