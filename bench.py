@@ -376,6 +376,22 @@ def run_ours(args, ws, rank, local):
     if form == pidcuda.FORM_OZAKI and rank == 0 and not args.no_model_check:
         model = model_bitexact_sample(O, A, B, C_head, n, args.slices or 8)
 
+    # the autotuner's pick (form, slice count) for the headline operands and
+    # for square 2048 products at exponent spreads 0, 8, 32
+    auto_pick = None
+    if rank == 0:
+        from vcp_gb300 import workloads as W
+        f0, s0 = pidcuda.autotune_pick(dA, dB, n, n, n, stream)
+        auto_pick = {"headline": {"form": "ozaki" if f0 == pidcuda.FORM_OZAKI else "plain",
+                                  "slices": s0}}
+        for phi in (0, 8, 32):
+            rg = np.random.default_rng(phi)
+            Ap = W.interval_ephi(rg, 2048, 2048, phi, 2.0 ** -40)
+            Bp = W.interval_ephi(rg, 2048, 2048, phi, 2.0 ** -40)
+            f1, s1 = pidcuda.autotune_pick(Ap, Bp, 2048, 2048, 2048)
+            auto_pick[f"n2048_phi{phi}_rad2^-40"] = {
+                "form": "ozaki" if f1 == pidcuda.FORM_OZAKI else "plain", "slices": s1}
+
     # e2e through the host-pointer C ABI from pinned buffers
     hA = torch.from_numpy(A).pin_memory()
     hB = torch.from_numpy(B).pin_memory()
@@ -432,6 +448,7 @@ def run_ours(args, ws, rank, local):
             "width_vs_plain": width,
             "containment_failures": fails, "containment_sample": 1024,
             "model_bitexact_sample": model,
+            "auto_pick": auto_pick,
             "e2e": {"value": e2e_val, "unit": UNIT,
                     "h2d_bytes_per_step": int(hA.numel() * 8 + hB.numel() * 8),
                     "d2h_bytes_per_step": int(hC.numel() * 8)},
