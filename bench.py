@@ -228,6 +228,26 @@ def model_bitexact_sample(O, A, B, C, n, slices, nrows=8, ncols=8, seed=17):
             "seconds": time.perf_counter() - t0}
 
 
+def host_fp64_peak_gflops(cores: int):
+    """FP64 peak of `cores` host cores in GFLOP/s where the core is known:
+    Neoverse V2 (Grace; /proc/cpuinfo part 0xd4f) issues four 128-bit FMA
+    per cycle = 16 FP64 flops; the clock is cpuinfo_max_freq.  None
+    elsewhere."""
+    try:
+        part = None
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("cpu part"):
+                part = line.split(":")[1].strip().lower()
+                break
+        if part != "0xd4f":
+            return None
+        khz = int(open("/sys/devices/system/cpu/cpu0/cpufreq/cpuinfo_max_freq").read())
+        return {"gflops": cores * khz * 1e-6 * 16.0, "ghz": khz * 1e-6,
+                "assumption": "Neoverse V2: 4 x 128-bit FMA pipes = 16 FP64 flops/cycle/core"}
+    except Exception:
+        return None
+
+
 def cpu_count():
     try:
         return len(os.sched_getaffinity(0))
@@ -265,7 +285,9 @@ def run_reference(args, ws, rank):
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{rows} x {n} x {n} row panel per step "
                                    f"(~{statistics.median(times):.1f} s), oracle restatement of "
-                                   "pidblas::mulmm over the vblas sequential-chain dgemm"},
+                                   "pidblas::mulmm over the vblas sequential-chain dgemm "
+                                   "(NEON micro-kernel on aarch64)",
+                         "fp64_gflops": 4e3 * v, "host_fp64_peak": host_fp64_peak_gflops(threads)},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -427,7 +449,9 @@ def run_ours(args, ws, rank, local):
         v, dt = cpu_baseline(A, B, n, rows_s, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{rows_s} x {n} x {n} row panel ({dt:.1f} s), oracle restatement of "
-                         "pidblas::mulmm over the vblas sequential-chain dgemm"}
+                         "pidblas::mulmm over the vblas sequential-chain dgemm (NEON "
+                         "micro-kernel on aarch64)",
+               "fp64_gflops": 4e3 * v, "host_fp64_peak": host_fp64_peak_gflops(threads)}
 
     also = None
     if rank == 0 and not args.no_also:
@@ -672,7 +696,7 @@ def bench_batch(dev, stream, steps=1, count=4096, seed=4096, forms=("plain", "oz
     return out
 
 
-def bench_dd(dev, stream, n, phi, steps=2, seed=77, sample=256):
+def bench_dd(dev, stream, n, phi, steps=2, seed=77, sample=256, cpu_rows=0):
     import torch
     from vcp_gb300 import pddcuda
     from oracle import oracle as O
@@ -692,12 +716,36 @@ def bench_dd(dev, stream, n, phi, steps=2, seed=77, sample=256):
     bnd = Eh[r + c * n]
     rel = err / np.where(ab > 0, ab, 1.0)
     nz = err > 0
-    return {"n": n, "phi": phi, "tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12, "ms": ms,
-            "rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel)),
-            "bound_failures": int(np.sum(err > bnd)),
-            "bound_over_err_median": float(np.median(bnd[nz] / err[nz])) if nz.any() else None,
-            "bound_rel_median": float(np.median(bnd / np.where(ab > 0, ab, 1.0))),
-            "sample": sample, "slices": "default (13, w = 104)", "roofline": roof}
+    out = {"n": n, "phi": phi, "tflops": 2.0 * n ** 3 / (ms * 1e-3) / 1e12, "ms": ms,
+           "rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel)),
+           "bound_failures": int(np.sum(err > bnd)),
+           "bound_over_err_median": float(np.median(bnd[nz] / err[nz])) if nz.any() else None,
+           "bound_rel_median": float(np.median(bnd / np.where(ab > 0, ab, 1.0))),
+           "sample": sample, "slices": "default (14, w = 112)", "roofline": roof}
+    if cpu_rows:
+        # pddblas::mulmm (oracle restatement: Ozaki slices, RN dgemm, dd sums)
+        # on a row panel: its time and, on the panel's entries, its error
+        # next to the GPU's
+        Ap = np.ascontiguousarray(Ah.reshape(n, n, 2)[:, :cpu_rows, :]).ravel()
+        t0 = time.perf_counter()
+        Pp = O.pddblas_mulmm(cpu_rows, n, n, Ap, Bh, cpu_count())
+        dt = time.perf_counter() - t0
+        pr = rs.integers(0, cpu_rows, sample).astype(np.int32)
+        pc = rs.integers(0, n, sample).astype(np.int32)
+        ep, abp = O.dd_residual(cpu_rows, n, n, Ap, Bh, Pp, pr, pc)
+        Cp = np.ascontiguousarray(Ch.reshape(n, n, 2)[:, :cpu_rows, :]).ravel()
+        eg, _ = O.dd_residual(cpu_rows, n, n, Ap, Bh, Cp, pr, pc)
+        sc = np.where(abp > 0, abp, 1.0)
+        out["cpu_baseline"] = {"value": 2.0 * cpu_rows * n * n / dt / 1e12, "unit": "TFLOP/s",
+                               "cores": cpu_count(), "kind": "port",
+                               "sample": f"{cpu_rows} x {n} x {n} row panel ({dt:.2f} s), "
+                                         "oracle restatement of pddblas::mulmm"}
+        out["accuracy_vs_pddblas"] = {
+            "entries": sample, "gpu_rel_err_median": float(np.median(eg / sc)),
+            "gpu_rel_err_max": float(np.max(eg / sc)),
+            "pddblas_rel_err_median": float(np.median(ep / sc)),
+            "pddblas_rel_err_max": float(np.max(ep / sc))}
+    return out
 
 
 def bench_point(dev, stream, m, n, k, phi, slice_list, steps=2, plain=True, seed=11,
@@ -1010,7 +1058,8 @@ def run_workload(args, dev, stream):
                             "largest order"), "s"
             value = res["cases"][-1]["ozaki"]["verification_s"]
         elif args.workload == "dd":
-            res = {"cases": [bench_dd(dev, stream, n, phi, steps=args.steps)
+            res = {"cases": [bench_dd(dev, stream, n, phi, steps=args.steps,
+                                      cpu_rows=0 if args.no_cpu else (64 if n <= 2048 else 16))
                              for n in parse_list(args.sizes, [2048, 8192])
                              for phi in parse_list(args.phis, [0, 16])]}
             metric, unit = "dd GEMM TFLOP/s (pddblas semantics)", "TFLOP/s"
@@ -1043,7 +1092,8 @@ def bench_also(dev, stream):
     out = {}
     for key, fn in (("autotune", lambda: pidcuda.autotune(stream)),
                     ("batch", lambda: bench_batch(dev, stream, steps=1)),
-                    ("dd", lambda: [bench_dd(dev, stream, 2048, phi, steps=2) for phi in (0, 16)]),
+                    ("dd", lambda: [bench_dd(dev, stream, 2048, phi, steps=2, cpu_rows=64)
+                                    for phi in (0, 16)]),
                     ("cfg1", lambda: bench_cfg1(dev, stream)),
                     ("lss", lambda: bench_lss(dev, stream, 2048, 1, steps=3)),
                     ("eig", lambda: bench_eig(dev, stream, 1024, steps=3)),

@@ -373,7 +373,8 @@ int vcpcu_batch_graph_destroy(vcpcu_batch_graph g);
  * A m x k, B k x n, C m x n) -- replaces pddblas::mulmm and, with A^T as
  * the left factor, pddblas::mulltmm (:379-409).  Each dd entry is scaled
  * per row (A) / column (B) to a w-bit integer, w = 8 * slices (7 <= slices
- * <= 14; 0 = default 13, w = 104; lowered for very long k); the integer
+ * <= 14; 0 = default 14, w = 112 -- the most the 32 moduli carry; lowered
+ * for very long k); the integer
  * product is exact (residues modulo up to 32 moduli <= 256 on the bf16
  * tensor cores, Chinese remaindering in 256-bit arithmetic) and is rounded
  * to the dd C = c.a1 + c.a2 (round to nearest, then the exact remainder to

@@ -58,7 +58,9 @@ class dd {
   friend dd operator*(const dd& x, const dd& y) {
     double p, e;
     twoproduct(x.a1, y.a1, p, e);
-    e += x.a1 * y.a2 + x.a2 * y.a1;
+    // the cross terms as one explicit fused multiply-add, so that the result
+    // does not depend on the compiler's contraction setting
+    e += std::fma(x.a1, y.a2, x.a2 * y.a1);
     dd r;
     fasttwosum(p, e, r.a1, r.a2);
     return r;

@@ -57,6 +57,10 @@ def lib() -> C.CDLL:
         L.orc_tensor_basis.argtypes = [_i, _v, _v, _i, _v, _v, _i, _i, _v, _v, _v, _l, _i, _i,
                                        _i]
         L.orc_tensor_basis.restype = _i
+        L.orc_pddblas_mulmm.argtypes = [_i, _i, _i, _v, _v, _v, _i]
+        L.orc_pddblas_mulmm.restype = _i
+        L.orc_pddblas_mulltmm.argtypes = [_i, _i, _v, _v, _i]
+        L.orc_pddblas_mulltmm.restype = _i
         _lib = L
     return _lib
 
@@ -80,6 +84,10 @@ def ref_lib() -> C.CDLL | None:
         R.ref_pidblas_fma_mulmm.argtypes = [_i, _i, _i, _v, _v, _v]
         R.ref_pidblas_fma_mulmm.restype = _i
         R.ref_norm_I_minus_RA.restype = _i
+        R.ref_pddblas_mulmm.argtypes = [_i, _i, _i, _v, _v, _v]
+        R.ref_pddblas_mulmm.restype = _i
+        R.ref_pddblas_mulltmm.argtypes = [_i, _i, _v, _v]
+        R.ref_pddblas_mulltmm.restype = _i
         R.ref_imats_linearsolve.argtypes = [_i, _i, _v, _v, _v, _v, _v]
         R.ref_imats_linearsolve.restype = _i
         R.ref_imats_eigsymge.argtypes = [_i, _v, _v, _v, _v, _v, _v]
@@ -269,6 +277,39 @@ def tensor_basis(nb, ia, ib, nt, Ta, Tb, nqa, nqb, out, ld, s1=None, s2=None,
                            _p(o), C.c_long(int(ld)), int(transposed), int(accumulate),
                            int(threads))
     return out
+
+
+def pddblas_mulmm(m, n, k, A, B, threads=0) -> np.ndarray:
+    """pddblas::mulmm (restatement): dd kv pairs, GEMM naming."""
+    C_ = np.empty(2 * m * n)
+    lib().orc_pddblas_mulmm(m, n, k, _p(A), _p(B), _p(C_), int(threads))
+    return C_
+
+
+def pddblas_mulltmm(m, nc, A, threads=0) -> np.ndarray:
+    """pddblas::mulltmm (restatement): A^T A for a dd A (m x nc)."""
+    C_ = np.empty(2 * nc * nc)
+    lib().orc_pddblas_mulltmm(m, nc, _p(A), _p(C_), int(threads))
+    return C_
+
+
+def ref_pddblas_mulmm(m, n, k, A, B):
+    """The reference's pddblas::mulmm as built here; None without it."""
+    R = ref_lib()
+    if R is None:
+        return None
+    C_ = np.empty(2 * m * n)
+    assert R.ref_pddblas_mulmm(m, n, k, _p(A), _p(B), _p(C_)) == 0
+    return C_
+
+
+def ref_pddblas_mulltmm(m, nc, A):
+    R = ref_lib()
+    if R is None:
+        return None
+    C_ = np.empty(2 * nc * nc)
+    assert R.ref_pddblas_mulltmm(m, nc, _p(A), _p(C_)) == 0
+    return C_
 
 
 def ref_call(name, *args):

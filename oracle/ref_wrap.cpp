@@ -28,6 +28,7 @@
 #include <vcp/ifma.hpp>
 #include <vcp/matrix.hpp>
 #include <kv/dd.hpp>
+#include <vcp/pddblas.hpp>
 #include <vcp/vcp_portable_fio.hpp>
 
 namespace {
@@ -48,12 +49,31 @@ extern "C" {
 
 // C = A * B for the pattern pdblas::mulmm uses (vcp/pdblas.hpp:91-110):
 // trans "N","N", alpha 1, beta 0, lda = m, ldb = k, ldc = m.
+// Also trans "T","N" with lda = k, the slice products of pddblas::mulltmm
+// (vcp/pddblas.hpp:160-193): op(A) = A^T is transposed into a copy first.
 void dgemm_(char* ta, char* tb, int* m, int* n, int* k, double* alpha, const double* A, int* lda,
             const double* B, int* ldb, double* beta, double* C, int* ldc) {
-  if (ta[0] != 'N' || tb[0] != 'N' || *alpha != 1.0 || *beta != 0.0 || *lda != *m ||
-      *ldb != *k || *ldc != *m)
+  const bool tA = ta[0] == 'T';
+  if ((ta[0] != 'N' && !tA) || tb[0] != 'N' || *alpha != 1.0 || *beta != 0.0 ||
+      *lda != (tA ? *k : *m) || *ldb != *k || *ldc != *m)
     unsupported("dgemm_");
-  rmatmul(*m, *k, *n, A, B, C, current_direction());
+  if (!tA) {
+    rmatmul(*m, *k, *n, A, B, C, current_direction());
+    return;
+  }
+  std::vector<double> At((size_t)(*m) * (*k));
+  for (int i = 0; i < *m; ++i)
+    for (int p = 0; p < *k; ++p) At[i + (size_t)p * (*m)] = A[p + (size_t)i * (*lda)];
+  rmatmul(*m, *k, *n, At.data(), B, C, current_direction());
+}
+
+// pddblas's linear-system and Cholesky refinements reference these two;
+// only its products are run here.
+void dgetrs_(char*, int*, int*, double*, int*, int*, double*, int*, int*) {
+  unsupported("dgetrs_");
+}
+void dtrsm_(char*, char*, char*, char*, int*, int*, double*, double*, int*, double*, int*) {
+  unsupported("dtrsm_");
 }
 
 double ddot_(int* n, const double* x, int* incx, const double* y, int* incy) {
@@ -572,6 +592,54 @@ int ref_pidblas_fma_mulmm(int m, int n, int k, const double* A, const double* B,
     for (long i = 0; i < (long)m * n; ++i) {
       C[2 * i] = c.data()[i].lower();
       C[2 * i + 1] = c.data()[i].upper();
+    }
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// The pair as given (no renormalisation), as the restatement reads it.
+static void set_dd(kv::dd& x, const double* p) {
+  x.a1 = p[0];
+  x.a2 = p[1];
+}
+
+// C = A * B through vcp::matrix<kv::dd, vcp::pddblas> (pddblas::mulmm,
+// vcp/pddblas.hpp:318-376: Ozaki slices, RN dgemm, dd accumulation).
+// GEMM naming, kv::dd pairs, column-major.
+int ref_pddblas_mulmm(int m, int n, int k, const double* A, const double* B, double* C) {
+  try {
+    vcp::matrix<kv::dd, vcp::pddblas> a, b, c;
+    a.zeros(m, k);
+    b.zeros(k, n);
+    for (long i = 0; i < (long)m * k; ++i) set_dd(a.data()[i], A + 2 * i);
+    for (long i = 0; i < (long)k * n; ++i) set_dd(b.data()[i], B + 2 * i);
+    c = a * b;
+    for (long i = 0; i < (long)m * n; ++i) {
+      C[2 * i] = c.data()[i].a1;
+      C[2 * i + 1] = c.data()[i].a2;
+    }
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// C = A^T A through pddblas::mulltmm (vcp/pddblas.hpp:379-409); A is m x nc.
+int ref_pddblas_mulltmm(int m, int nc, const double* A, double* C) {
+  try {
+    vcp::matrix<kv::dd, vcp::pddblas> a, c;
+    a.zeros(m, nc);
+    for (long i = 0; i < (long)m * nc; ++i) set_dd(a.data()[i], A + 2 * i);
+    c = ltransmul(a);
+    for (long i = 0; i < (long)nc * nc; ++i) {
+      C[2 * i] = c.data()[i].a1;
+      C[2 * i + 1] = c.data()[i].a2;
     }
     return 0;
   } catch (...) {

@@ -54,17 +54,71 @@ static int fe_mode(int rnd) {
 /* ---------------------------------------------------------------------------
  * Directed-rounding GEMM (vblas naming: A m x n, B n x k, C m x k).
  * Blocking: column blocks of NR=4 C columns are distributed over threads;
- * inside, row blocks of MR=16 and inner blocks of KC keep the A panel hot.
+ * inside, row blocks of MR=8 and inner blocks of KC keep the A panel hot.
  * The chain of each C entry runs over the inner index in ascending order,
  * continuing through C between inner blocks, so blocking never changes it.
  * ------------------------------------------------------------------------- */
-#define ORC_MR 16
+#define ORC_MR 8
 #define ORC_NR 4
 #define ORC_KC 256
 #define ORC_MC 512
 
+#if defined(__aarch64__)
+#include <arm_neon.h>
+/* Full 8 x 4 tile with NEON: every lane runs one entry's chain, each step a
+ * fused multiply-add rounded in the current (FPCR) rounding mode -- the same
+ * operation, in the same order, as the scalar fma() below, so the bits do
+ * not change (the reference's vblas/rmatmul_neon.hpp organises its tiles the
+ * same way).  16 accumulator registers, 4 for A, 4 broadcast B values. */
+static void micro_chain_8x4_neon(int kc, const double* A, long lda, const double* B, long ldb,
+                                 double* C, long ldc, int first) {
+  float64x2_t c0[4], c1[4], c2[4], c3[4];
+  for (int r = 0; r < 4; ++r) {
+    if (first) {
+      c0[r] = c1[r] = c2[r] = c3[r] = vdupq_n_f64(0.0);
+    } else {
+      c0[r] = vld1q_f64(C + 2 * r);
+      c1[r] = vld1q_f64(C + ldc + 2 * r);
+      c2[r] = vld1q_f64(C + 2 * ldc + 2 * r);
+      c3[r] = vld1q_f64(C + 3 * ldc + 2 * r);
+    }
+  }
+  const double* b0p = B;
+  const double* b1p = B + ldb;
+  const double* b2p = B + 2 * ldb;
+  const double* b3p = B + 3 * ldb;
+  for (int p = 0; p < kc; ++p) {
+    const double* ap = A + p * lda;
+    const float64x2_t a0 = vld1q_f64(ap), a1 = vld1q_f64(ap + 2), a2 = vld1q_f64(ap + 4),
+                      a3 = vld1q_f64(ap + 6);
+    const float64x2_t b0 = vdupq_n_f64(b0p[p]), b1 = vdupq_n_f64(b1p[p]),
+                      b2 = vdupq_n_f64(b2p[p]), b3 = vdupq_n_f64(b3p[p]);
+    c0[0] = vfmaq_f64(c0[0], a0, b0); c0[1] = vfmaq_f64(c0[1], a1, b0);
+    c0[2] = vfmaq_f64(c0[2], a2, b0); c0[3] = vfmaq_f64(c0[3], a3, b0);
+    c1[0] = vfmaq_f64(c1[0], a0, b1); c1[1] = vfmaq_f64(c1[1], a1, b1);
+    c1[2] = vfmaq_f64(c1[2], a2, b1); c1[3] = vfmaq_f64(c1[3], a3, b1);
+    c2[0] = vfmaq_f64(c2[0], a0, b2); c2[1] = vfmaq_f64(c2[1], a1, b2);
+    c2[2] = vfmaq_f64(c2[2], a2, b2); c2[3] = vfmaq_f64(c2[3], a3, b2);
+    c3[0] = vfmaq_f64(c3[0], a0, b3); c3[1] = vfmaq_f64(c3[1], a1, b3);
+    c3[2] = vfmaq_f64(c3[2], a2, b3); c3[3] = vfmaq_f64(c3[3], a3, b3);
+  }
+  for (int r = 0; r < 4; ++r) {
+    vst1q_f64(C + 2 * r, c0[r]);
+    vst1q_f64(C + ldc + 2 * r, c1[r]);
+    vst1q_f64(C + 2 * ldc + 2 * r, c2[r]);
+    vst1q_f64(C + 3 * ldc + 2 * r, c3[r]);
+  }
+}
+#endif
+
 static void micro_chain(int mr, int nr, int kc, const double* A, long lda, const double* B,
                         long ldb, double* C, long ldc, int first) {
+#if defined(__aarch64__)
+  if (mr == ORC_MR && nr == ORC_NR) {
+    micro_chain_8x4_neon(kc, A, lda, B, ldb, C, ldc, first);
+    return;
+  }
+#endif
   double acc[ORC_NR][ORC_MR];
   for (int j = 0; j < ORC_NR; ++j)
     for (int i = 0; i < ORC_MR; ++i)
@@ -1120,5 +1174,195 @@ int orc_tensor_basis(int nb, const int* ia, const int* ib, int nt, const double*
     free(buf);
   }
   (void)nthreads;
+  return 0;
+}
+
+/* ---------------------------------------------------------------------------
+ * pddblas (vcp/pddblas.hpp): the Ozaki-scheme dd product of the reference,
+ * restated for the CPU baseline and for the accuracy comparison with the
+ * GPU's dd product.  dd values are kv-layout pairs {a1, a2}; the dd addition
+ * is the one of the project's kv stand-in (oracle/kvshim/kv/dd.hpp: TwoSum
+ * of both words, Dekker renormalisations), in round-to-nearest.
+ *   split geometry  pddblas_assist::ceil_log2 / split_shift / split_bits /
+ *                   max_slices (:54-78)
+ *   split_row/col   one sigma = 2^(e + s) per row / column, q = (a1 + sigma)
+ *                   - sigma, the remainder T -= q in dd (:82-154)
+ *   ozaki_acc       t = p + q ascending, p ascending, each slice product a
+ *                   round-to-nearest dgemm (exact by construction), its
+ *                   non-zero entries added into C in dd (:160-193)
+ * ------------------------------------------------------------------------- */
+static void dd_twosum(double a, double b, double* s, double* e) {
+  volatile double vs = a + b;
+  volatile double bb = vs - a;
+  *s = vs;
+  *e = (a - (vs - bb)) + (b - bb);
+}
+static void dd_fasttwosum(double a, double b, double* s, double* e) {
+  volatile double vs = a + b;
+  *s = vs;
+  *e = b - (vs - a);
+}
+static void dd_add(double x1, double x2, double y1, double y2, double* r1, double* r2) {
+  double s, e, t, f;
+  dd_twosum(x1, y1, &s, &e);
+  dd_twosum(x2, y2, &t, &f);
+  e += t;
+  dd_fasttwosum(s, e, &s, &e);
+  e += f;
+  dd_fasttwosum(s, e, r1, r2);
+}
+
+static int pdd_ceil_log2(int k) {
+  int r = 0, t = 1;
+  while (t < k) {
+    t *= 2;
+    ++r;
+  }
+  return r;
+}
+static int pdd_split_shift(int k) { return (51 + pdd_ceil_log2(k) + 1) / 2; }
+static int pdd_split_bits(int k) {
+  int b = 52 - pdd_split_shift(k);
+  return b < 1 ? 1 : b;
+}
+static int pdd_max_slices(int k) { return 110 / pdd_split_bits(k) + 2; }
+
+/* Split the dd array X (rows x cols, column-major, kv pairs) into slices
+ * (rows x cols doubles each, appended to *D), one sigma per row (by_row) or
+ * per column, with split parameter kk (the inner dimension).  Returns the
+ * number of slices. */
+static int pdd_split(const double* X, int rows, int cols, int by_row, int kk, double** D) {
+  const int s = pdd_split_shift(kk), smax = pdd_max_slices(kk);
+  const long cnt = (long)rows * cols;
+  double* T = malloc(sizeof(double) * 2 * (cnt > 0 ? cnt : 1));
+  memcpy(T, X, sizeof(double) * 2 * cnt);
+  double* out = malloc(sizeof(double) * (size_t)smax * (cnt > 0 ? cnt : 1));
+  int ns = 0;
+  for (int p = 0; p < smax; ++p) {
+    double* S = out + (size_t)p * cnt;
+    memset(S, 0, sizeof(double) * cnt);
+    int nonzero = 0;
+    const int outer = by_row ? rows : cols, inner = by_row ? cols : rows;
+    for (int o = 0; o < outer; ++o) {
+      double mu = 0.0;
+      for (int t = 0; t < inner; ++t) {
+        const long idx = by_row ? o + (long)t * rows : t + (long)o * rows;
+        const double a = fabs(T[2 * idx]);
+        if (a > mu) mu = a;
+      }
+      if (mu == 0.0) continue;
+      int e;
+      frexp(mu, &e);
+      const double sigma = ldexp(1.0, e + s);
+      for (int t = 0; t < inner; ++t) {
+        const long idx = by_row ? o + (long)t * rows : t + (long)o * rows;
+        volatile double v = T[2 * idx] + sigma;
+        volatile double q = v - sigma;
+        if (q != 0.0) {
+          S[idx] = q;
+          double r1, r2;
+          dd_add(T[2 * idx], T[2 * idx + 1], -q, -0.0, &r1, &r2);
+          T[2 * idx] = r1;
+          T[2 * idx + 1] = r2;
+          nonzero = 1;
+        }
+      }
+    }
+    if (!nonzero) break;
+    ++ns;
+  }
+  free(T);
+  *D = out;
+  return ns;
+}
+
+/* C (m x n dd) += sum of op(DA[p]) DB[q] over slice pairs, op(DA[p]) m x k
+ * (stored k x m when transA). */
+static void pdd_ozaki_acc(const double* DA, int na, long sa, int transA, const double* DB, int nb,
+                          long sb, int m, int n, int k, double* C, int nthreads) {
+  if (na == 0 || nb == 0) return;
+  const int limit = pdd_max_slices(k);
+  const long mn = (long)m * n;
+  double* P = malloc(sizeof(double) * (mn > 0 ? mn : 1));
+  double* At = transA ? malloc(sizeof(double) * ((long)m * k > 0 ? (long)m * k : 1)) : NULL;
+  for (int t = 0; t < limit; ++t) {
+    for (int p = 0; p <= t; ++p) {
+      const int q = t - p;
+      if (p >= na || q >= nb) continue;
+      const double* Ap = DA + (size_t)p * sa;
+      if (transA) { /* the k x m slice transposed to m x k */
+        for (int i = 0; i < m; ++i)
+          for (int l = 0; l < k; ++l) At[i + (long)l * m] = Ap[l + (long)i * k];
+        Ap = At;
+      }
+      orc_rmatmul_ld(m, k, n, Ap, m, DB + (size_t)q * sb, k, P, m, 0, nthreads);
+      for (long idx = 0; idx < mn; ++idx)
+        if (P[idx] != 0.0) {
+          double r1, r2;
+          dd_add(C[2 * idx], C[2 * idx + 1], P[idx], 0.0, &r1, &r2);
+          C[2 * idx] = r1;
+          C[2 * idx + 1] = r2;
+        }
+    }
+  }
+  free(P);
+  free(At);
+}
+
+/* pddblas::mulmm (vcp/pddblas.hpp:318-376), GEMM naming: C (m x n) = A (m x k)
+ * B (k x n), dd kv pairs, column-major. */
+static void dd_mul(double x1, double x2, double y1, double y2, double* r1, double* r2) {
+  volatile double p = x1 * y1;
+  double e = fma(x1, y1, -p);
+  volatile double t2 = x2 * y1;
+  volatile double t = fma(x1, y2, t2);
+  e += t;
+  dd_fasttwosum(p, e, r1, r2);
+}
+
+int orc_pddblas_mulmm(int m, int n, int k, const double* A, const double* B, double* C,
+                      int nthreads) {
+  for (long i = 0; i < 2L * m * n; ++i) C[i] = 0.0;
+  if (m <= 0 || n <= 0 || k <= 0) return 0;
+  /* the scalar ('S', 1 x 1) shortcuts of pddblas::mulmm (:319-336) */
+  if (m == 1 && k == 1 && n == 1) { /* c = a * b */
+    dd_mul(A[0], A[1], B[0], B[1], C, C + 1);
+    return 0;
+  }
+  if (m == 1 && k == 1) { /* c = B, c[i] *= a */
+    for (long i = 0; i < (long)n; ++i) dd_mul(B[2 * i], B[2 * i + 1], A[0], A[1], C + 2 * i, C + 2 * i + 1);
+    return 0;
+  }
+  if (k == 1 && n == 1) { /* c = A, c[i] *= b */
+    for (long i = 0; i < (long)m; ++i) dd_mul(A[2 * i], A[2 * i + 1], B[0], B[1], C + 2 * i, C + 2 * i + 1);
+    return 0;
+  }
+  double *DA, *DB;
+  const int na = pdd_split(A, m, k, 1, k, &DA);
+  const int nb = pdd_split(B, k, n, 0, k, &DB);
+  pdd_ozaki_acc(DA, na, (long)m * k, 0, DB, nb, (long)k * n, m, n, k, C, nthreads);
+  free(DA);
+  free(DB);
+  return 0;
+}
+
+/* pddblas::mulltmm (vcp/pddblas.hpp:379-409): C (nc x nc) = A^T A for A
+ * (m x nc), the lower triangle then copied from the upper one. */
+int orc_pddblas_mulltmm(int m, int nc, const double* A, double* C, int nthreads) {
+  for (long i = 0; i < 2L * nc * nc; ++i) C[i] = 0.0;
+  if (m <= 0 || nc <= 0) return 0;
+  if (m == 1 && nc == 1) { /* 'S': a * a (:380-384) */
+    dd_mul(A[0], A[1], A[0], A[1], C, C + 1);
+    return 0;
+  }
+  double* DA;
+  const int na = pdd_split(A, m, nc, 0, m, &DA);
+  pdd_ozaki_acc(DA, na, (long)m * nc, 1, DA, na, (long)m * nc, nc, nc, m, C, nthreads);
+  free(DA);
+  for (int i = 0; i < nc; ++i)
+    for (int j = i + 1; j < nc; ++j) {
+      C[2 * (j + (long)nc * i)] = C[2 * (i + (long)nc * j)];
+      C[2 * (j + (long)nc * i) + 1] = C[2 * (i + (long)nc * j) + 1];
+    }
   return 0;
 }

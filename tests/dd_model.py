@@ -62,7 +62,7 @@ def ru(v: Fraction) -> float:
     return d
 
 
-def ddgemm(m, n, k, A, B, slices=13):
+def ddgemm(m, n, k, A, B, slices=14):
     """A, B: flat kv dd buffers (column-major).  Returns (C list, err list)."""
     w, _ = plan_bits(k, slices)
     E = []

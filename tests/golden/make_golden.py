@@ -1,9 +1,10 @@
 """Generate the golden vectors in tests/golden/ from the reference itself.
 
 The reference ships no golden vectors (its tests are print-only mains), so
-this script runs the reference's own code -- vblas rmatmul and
-vcp::matrix<kv::interval<double>, vcp::pidblas> compiled from the reference
-tree by oracle/build.py (kv from the project's kvshim) -- on small seeded
+this script runs the reference's own code -- vblas rmatmul,
+vcp::matrix<kv::interval<double>, vcp::pidblas> and
+vcp::matrix<kv::dd, vcp::pddblas> compiled from the reference tree by
+oracle/build.py (kv from the project's kvshim) -- on small seeded
 inputs and stores inputs and outputs as golden.npz.  It needs the reference
 sources, so it runs only where they are mounted; the .npz travels with the
 repository.
@@ -43,6 +44,15 @@ def mixed_intervals(rng, n: int) -> np.ndarray:
     up[zer] = np.where(rng.random(int(zer.sum())) < 0.5, 0.0, np.abs(up[zer]))
     out = np.empty(2 * n)
     out[0::2], out[1::2] = lo, up
+    return out
+
+
+def dd_matrix(rng, rows: int, cols: int, phi: int) -> np.ndarray:
+    """kv::dd pairs (column-major): hi from E(phi), lo = hi 2^-53 u, u in [-1, 1]."""
+    hi = W.ephi(rng, rows * cols, phi)
+    out = np.empty(2 * rows * cols)
+    out[0::2] = hi
+    out[1::2] = hi * 2.0 ** -53 * rng.uniform(-1.0, 1.0, rows * cols)
     return out
 
 
@@ -155,6 +165,19 @@ def main() -> None:
         data[f"ge{idx}_X"], data[f"ge{idx}_lambda"], data[f"ge{idx}_Y"] = X, lmb, Y
         data[f"ge{idx}_lam"] = lam
         data[f"ge{idx}_bound"] = np.array([bound])
+    # pddblas::mulmm / mulltmm (the dd Ozaki products, vcp/pddblas.hpp:318-409)
+    # through vcp::matrix<kv::dd, vcp::pddblas>: hi words E(phi), lo = hi 2^-53 u
+    rng5 = np.random.default_rng(20261208)
+    dcases = [(1, 1, 1, 0), (1, 7, 1, 3), (6, 1, 1, 2), (9, 7, 13, 0), (20, 12, 300, 16),
+              (6, 5, 2100, 4)]
+    for idx, (m, n, k, phi) in enumerate(dcases):
+        A = dd_matrix(rng5, m, k, phi)
+        B = dd_matrix(rng5, k, n, phi)
+        data[f"dd{idx}_shape"] = np.array([m, n, k])
+        data[f"dd{idx}_A"], data[f"dd{idx}_B"] = A, B
+        data[f"dd{idx}_C"] = O.ref_pddblas_mulmm(m, n, k, A, B)
+        data[f"dd{idx}_T"] = O.ref_pddblas_mulltmm(k, n, B)
+    data["n_dd"] = np.array([len(dcases)])
     data["n_ge"] = np.array([len(gcases)])
     data["n_fm"] = np.array([len(fcases)])
     data["n_mp"] = np.array([len(pcases)])

@@ -347,3 +347,33 @@ def test_oracle_eigsymge_matches_reference_build(oracle):
         st2, lam_o, _ = oracle.ieigsymge(n, A, B, X, lmb, Y)
         assert st == st2 == 0, n
         assert np.array_equal(bits(lam_o), bits(lam_r)), n
+
+
+def test_oracle_pddblas_matches_golden(oracle, golden):
+    """pddblas::mulmm / mulltmm restated (oracle/vcp_oracle.c) against the
+    reference's own products (golden vectors, scalar shortcuts included)."""
+    for idx in range(int(golden["n_dd"][0])):
+        m, n, k = (int(x) for x in golden[f"dd{idx}_shape"])
+        A, B = golden[f"dd{idx}_A"], golden[f"dd{idx}_B"]
+        C = oracle.pddblas_mulmm(m, n, k, A, B)
+        assert np.array_equal(C.view(np.int64), golden[f"dd{idx}_C"].view(np.int64)), idx
+        T = oracle.pddblas_mulltmm(k, n, B)
+        assert np.array_equal(T.view(np.int64), golden[f"dd{idx}_T"].view(np.int64)), idx
+
+
+def test_oracle_pddblas_matches_reference_build(oracle):
+    if oracle.ref_lib() is None:
+        pytest.skip("reference build absent")
+    rng = np.random.default_rng(31)
+    for (m, n, k, phi) in [(17, 13, 70, 8), (64, 3, 900, 0), (2, 2, 5000, 32)]:
+        hi = lambda r, c: rng.uniform(1, 2, r * c) * np.ldexp(1.0, rng.integers(-phi, phi + 1, r * c))  # noqa: E731
+        def dd(r, c):
+            h = hi(r, c) * rng.choice([-1.0, 1.0], r * c)
+            out = np.empty(2 * r * c)
+            out[0::2], out[1::2] = h, h * 2.0 ** -53 * rng.uniform(-1, 1, r * c)
+            return out
+        A, B = dd(m, k), dd(k, n)
+        C = oracle.pddblas_mulmm(m, n, k, A, B)
+        assert np.array_equal(C.view(np.int64), oracle.ref_pddblas_mulmm(m, n, k, A, B).view(np.int64))
+        T = oracle.pddblas_mulltmm(k, n, B)
+        assert np.array_equal(T.view(np.int64), oracle.ref_pddblas_mulltmm(k, n, B).view(np.int64))

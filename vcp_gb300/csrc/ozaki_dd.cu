@@ -5,7 +5,7 @@
 // pair with dgemm and accumulates the exact products in dd
 // (pddblas_assist::split_row / split_col / ozaki_acc, vcp/pddblas.hpp:82-193).
 // Here each dd entry hi + lo is scaled per row (A) / column (B) to a w-bit
-// integer (w = 8 * slices, default 104 bits), the integer product A'B' is
+// integer (w = 8 * slices, default 112 bits), the integer product A'B' is
 // formed exactly from its residues modulo L <= 32 pairwise-coprime moduli
 // <= 256 (one bf16 tensor-core GEMM per modulus, exact fp32 chunks, int32
 // folds), recovered by Chinese remaindering in 256-bit arithmetic, and
@@ -378,7 +378,7 @@ int dd_plan_bits(int k, int slices, int* w, int* L) {
 int ozaki_ddgemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
                  double* C, long ldc, double* Cerr, long lde, int slices, cudaStream_t s,
                  void* static_scratch, size_t static_bytes) {
-  int w = 8 * (slices > 0 ? slices : 13), L = 0;
+  int w = 8 * (slices > 0 ? slices : 14), L = 0;
   DdCrt cc;
   dd_crt_setup(k, &w, &L, &cc);
   OzPlan plan;
