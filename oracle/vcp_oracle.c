@@ -195,20 +195,33 @@ void orc_udmatmul(int m, int n, int k, const double* A, const double* B, double*
 /* kv layout (pairs {inf,sup}) -> mid / rad planes, count entries.  The
  * midpoints are formed in one round-to-nearest pass, the radii in one
  * round-upward pass. */
+/* Elementwise passes run on all threads (each sets its own rounding mode;
+ * the results do not depend on the partition). */
 void orc_midrad(long count, const double* X, double* mid, double* rad) {
-  const int prev = fegetround();
-  fesetround(FE_TONEAREST);
-  for (long i = 0; i < count; ++i) {
-    const double lo = X[2 * i], up = X[2 * i + 1];
-    double s = lo + up;
-    mid[i] = isfinite(s) ? s * 0.5 : lo * 0.5 + up * 0.5;
+#ifdef _OPENMP
+#pragma omp parallel if (count > 65536)
+#endif
+  {
+    const int prev = fegetround();
+    fesetround(FE_TONEAREST);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (long i = 0; i < count; ++i) {
+      const double lo = X[2 * i], up = X[2 * i + 1];
+      double s = lo + up;
+      mid[i] = isfinite(s) ? s * 0.5 : lo * 0.5 + up * 0.5;
+    }
+    fesetround(FE_UPWARD);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (long i = 0; i < count; ++i) {
+      const double lo = X[2 * i], up = X[2 * i + 1];
+      rad[i] = fmax(mid[i] - lo, up - mid[i]);
+    }
+    fesetround(prev);
   }
-  fesetround(FE_UPWARD);
-  for (long i = 0; i < count; ++i) {
-    const double lo = X[2 * i], up = X[2 * i + 1];
-    rad[i] = fmax(mid[i] - lo, up - mid[i]);
-  }
-  fesetround(prev);
 }
 
 /* pidblas::mulmm, GEMM naming: C (m x n) = A (m x k) * B (k x n); A, B, C in
@@ -230,18 +243,44 @@ int orc_pidblas_mulmm(int m, int n, int k, const double* A, const double* B, dou
   orc_midrad(nb, B, mB, rB);
   orc_rmatmul(m, k, n, mA, mB, lC, -1, nthreads);
   orc_rmatmul(m, k, n, mA, mB, uC, 1, nthreads);
-  fesetround(FE_UPWARD);
-  for (long i = 0; i < na; ++i) mA[i] = fabs(mA[i]) + rA[i];
-  for (long i = 0; i < nb; ++i) mB[i] = fabs(mB[i]);
+#ifdef _OPENMP
+#pragma omp parallel if (na + nb > 65536)
+#endif
+  {
+    const int pv = fegetround();
+    fesetround(FE_UPWARD);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (long i = 0; i < na; ++i) mA[i] = fabs(mA[i]) + rA[i];
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (long i = 0; i < nb; ++i) mB[i] = fabs(mB[i]);
+    fesetround(pv);
+  }
   orc_rmatmul(m, k, n, mA, rB, temp, 1, nthreads);
   orc_rmatmul(m, k, n, rA, mB, t2, 1, nthreads);
-  fesetround(FE_UPWARD);
-  for (long i = 0; i < nc; ++i) {
-    temp[i] = temp[i] + t2[i];
-    uC[i] = uC[i] + temp[i];
+#ifdef _OPENMP
+#pragma omp parallel if (nc > 65536)
+#endif
+  {
+    const int pv = fegetround();
+    fesetround(FE_UPWARD);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (long i = 0; i < nc; ++i) {
+      temp[i] = temp[i] + t2[i];
+      uC[i] = uC[i] + temp[i];
+    }
+    fesetround(FE_DOWNWARD);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (long i = 0; i < nc; ++i) lC[i] = lC[i] - temp[i];
+    fesetround(pv);
   }
-  fesetround(FE_DOWNWARD);
-  for (long i = 0; i < nc; ++i) lC[i] = lC[i] - temp[i];
   fesetround(prev);
   for (long i = 0; i < nc; ++i) {
     C[2 * i] = lC[i];
@@ -1243,7 +1282,11 @@ static int pdd_split(const double* X, int rows, int cols, int by_row, int kk, do
     memset(S, 0, sizeof(double) * cnt);
     int nonzero = 0;
     const int outer = by_row ? rows : cols, inner = by_row ? cols : rows;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(| : nonzero) if (cnt > 65536)
+#endif
     for (int o = 0; o < outer; ++o) {
+      fesetround(FE_TONEAREST);
       double mu = 0.0;
       for (int t = 0; t < inner; ++t) {
         const long idx = by_row ? o + (long)t * rows : t + (long)o * rows;
@@ -1296,6 +1339,9 @@ static void pdd_ozaki_acc(const double* DA, int na, long sa, int transA, const d
         Ap = At;
       }
       orc_rmatmul_ld(m, k, n, Ap, m, DB + (size_t)q * sb, k, P, m, 0, nthreads);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) if (mn > 65536) num_threads(nthreads > 0 ? nthreads : omp_get_max_threads())
+#endif
       for (long idx = 0; idx < mn; ++idx)
         if (P[idx] != 0.0) {
           double r1, r2;
