@@ -61,6 +61,8 @@ def lib() -> C.CDLL:
         L.orc_pddblas_mulmm.restype = _i
         L.orc_pddblas_mulltmm.argtypes = [_i, _i, _v, _v, _i]
         L.orc_pddblas_mulltmm.restype = _i
+        L.orc_fp64_peak.argtypes = [C.c_double, _i]
+        L.orc_fp64_peak.restype = C.c_double
         _lib = L
     return _lib
 
@@ -291,6 +293,11 @@ def pddblas_mulltmm(m, nc, A, threads=0) -> np.ndarray:
     C_ = np.empty(2 * nc * nc)
     lib().orc_pddblas_mulltmm(m, nc, _p(A), _p(C_), int(threads))
     return C_
+
+
+def fp64_peak_gflops(seconds=0.5, threads=0) -> float:
+    """Measured FP64 FMA throughput of the host cores (GFLOP/s)."""
+    return float(lib().orc_fp64_peak(float(seconds), int(threads)))
 
 
 def ref_pddblas_mulmm(m, n, k, A, B):

@@ -1412,3 +1412,52 @@ int orc_pddblas_mulltmm(int m, int nc, const double* A, double* C, int nthreads)
     }
   return 0;
 }
+
+/* ---------------------------------------------------------------------------
+ * Measured FP64 peak of the host cores (the denominator of the CPU port's
+ * fraction of peak): every thread runs 16 independent fused multiply-add
+ * chains (two lanes each on NEON) for about `seconds`; returns the aggregate
+ * GFLOP/s (2 flops per lane per FMA).
+ * ------------------------------------------------------------------------- */
+#include <time.h>
+static double orc_now(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+double orc_fp64_peak(double seconds, int nthreads) {
+  double total_flops = 0.0;
+  const double t0 = orc_now();
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads) reduction(+ : total_flops)
+#endif
+  {
+    double flops = 0.0, sink = 0.0;
+#if defined(__aarch64__)
+    float64x2_t acc[16];
+    for (int i = 0; i < 16; ++i) acc[i] = vdupq_n_f64(0.5 + i);
+    const float64x2_t a = vdupq_n_f64(0.9999999), b = vdupq_n_f64(1e-9);
+    do {
+      for (int it = 0; it < (1 << 16); ++it)
+        for (int i = 0; i < 16; ++i) acc[i] = vfmaq_f64(acc[i], a, b);
+      flops += 16.0 * 2 * 2 * (1 << 16);
+    } while (orc_now() - t0 < seconds);
+    for (int i = 0; i < 16; ++i) sink += vgetq_lane_f64(acc[i], 0) + vgetq_lane_f64(acc[i], 1);
+#else
+    double acc[16];
+    for (int i = 0; i < 16; ++i) acc[i] = 0.5 + i;
+    do {
+      for (int it = 0; it < (1 << 16); ++it)
+        for (int i = 0; i < 16; ++i) acc[i] = fma(acc[i], 0.9999999, 1e-9);
+      flops += 16.0 * 2 * (1 << 16);
+    } while (orc_now() - t0 < seconds);
+    for (int i = 0; i < 16; ++i) sink += acc[i];
+#endif
+    if (sink == 12345.678) flops += 1.0; /* keeps the chains live */
+    total_flops += flops;
+  }
+  (void)nthreads;
+  return total_flops / (orc_now() - t0) * 1e-9;
+}

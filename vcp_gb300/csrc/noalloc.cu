@@ -90,7 +90,6 @@ extern "C" int vcpcu_igemm_noalloc_dev(int m, int n, int k, const double* A, int
   }
   OzPlan plan;
   oz_make_plan(m, n, k, slices > 0 ? slices : 8, 2, &plan, /*crt=*/1);
-  plan.pb.one_stream = 1;  // no second stream or events: nothing is created per call
   const size_t need = oz_workspace_bytes(plan.pb);
   if (need > (size_t)VCPCU_NOALLOC_SCRATCH_BYTES) {
     set_error("igemm_noalloc: %d x %d x %d with %d slices needs %zu bytes of scratch, more than "

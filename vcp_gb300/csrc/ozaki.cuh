@@ -21,8 +21,6 @@ struct OzProblem {
   int crt;         // 1: midpoint by the CRT form (w-bit integers, L moduli)
   int w, L;        // CRT form: integer bits per operand, number of moduli
   int mplanes;     // midpoint planes per operand: s (slice form) or L (CRT form)
-  int one_stream;  // 1: prepare both factors on the caller's stream only (no
-                   //    second stream or events are created)
 };
 
 // Device scratch of one Ozaki-form product (pointers into one allocation).

@@ -20,8 +20,6 @@
 #include "ozaki_common.cuh"
 #include "swfp.cuh"
 
-#include <mutex>
-
 namespace vcpcu {
 
 __device__ __forceinline__ unsigned long long dbits(double x) {
@@ -1164,66 +1162,13 @@ int oz_prepare_right_crt(const OzProblem& pb, const double* B, long ldb, OzWorks
   return VCPCU_OK;
 }
 
-namespace {
-// A second stream per device for the right factor's preparation, which runs
-// beside the left factor's (both kernels are issue-bound at 35-50 % of the
-// warp slots; together they fill the SMs).
-cudaStream_t oz_side_stream() {
-  static std::mutex mu;
-  static cudaStream_t side[64] = {nullptr};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  std::lock_guard<std::mutex> lk(mu);
-  if (!side[dev] && cudaStreamCreateWithFlags(&side[dev], cudaStreamNonBlocking) != cudaSuccess) {
-    cudaGetLastError();
-    side[dev] = nullptr;
-  }
-  return side[dev];
-}
-
-struct EventPair {
-  cudaEvent_t e[2] = {nullptr, nullptr};
-  ~EventPair() {
-    for (cudaEvent_t x : e)
-      if (x) cudaEventDestroy(x);
-  }
-};
-}  // namespace
-
 int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, long ldb,
                OzWorkspace& ws, cudaStream_t st) {
   int st_ = oz_prepare_left_begin(pb, ws, st);
-  if (st_) return st_;
-  if (pb.crt) {
-    // right factor on the side stream after the status words are cleared,
-    // left factor here, then join
-    cudaStream_t side = pb.one_stream ? nullptr : oz_side_stream();
-    EventPair ev;
-    if (side) {
-      for (cudaEvent_t& x : ev.e)
-        if (cudaEventCreateWithFlags(&x, cudaEventDisableTiming) != cudaSuccess) {
-          cudaGetLastError();
-          x = nullptr;
-        }
-    }
-    if (side && ev.e[0] && ev.e[1]) {
-      VCPCU_CUDA_TRY(cudaEventRecord(ev.e[0], st));
-      VCPCU_CUDA_TRY(cudaStreamWaitEvent(side, ev.e[0], 0));
-      const int sr = oz_prepare_right_crt(pb, B, ldb, ws, side);
-      VCPCU_CUDA_TRY(cudaEventRecord(ev.e[1], side));
-      st_ = oz_prepare_left_rowmax(pb, A, lda, 0, pb.K, ws, st);
-      if (!st_) st_ = oz_prepare_left_finish(pb, ws, st);
-      VCPCU_CUDA_TRY(cudaStreamWaitEvent(st, ev.e[1], 0));
-      return st_ ? st_ : sr;
-    }
-    st_ = oz_prepare_left_rowmax(pb, A, lda, 0, pb.K, ws, st);
-    if (!st_) st_ = oz_prepare_left_finish(pb, ws, st);
-    if (st_) return st_;
-    return oz_prepare_right_crt(pb, B, ldb, ws, st);
-  }
-  st_ = oz_prepare_left_rowmax(pb, A, lda, 0, pb.K, ws, st);
+  if (!st_) st_ = oz_prepare_left_rowmax(pb, A, lda, 0, pb.K, ws, st);
   if (!st_) st_ = oz_prepare_left_finish(pb, ws, st);
   if (st_) return st_;
+  if (pb.crt) return oz_prepare_right_crt(pb, B, ldb, ws, st);
   switch (pb.s) {
 #define OZ_SPLIT_CASE(S)                                                          \
   case S:                                                                         \
