@@ -67,13 +67,73 @@ void dgemm_(char* ta, char* tb, int* m, int* n, int* k, double* alpha, const dou
   rmatmul(*m, *k, *n, At.data(), B, C, current_direction());
 }
 
-// pddblas's linear-system and Cholesky refinements reference these two;
-// only its products are run here.
-void dgetrs_(char*, int*, int*, double*, int*, int*, double*, int*, int*) {
-  unsupported("dgetrs_");
+// The double-precision solves of pddblas's refinements
+// (vcp/pddblas.hpp:413-563).  LAPACK is absent here: project-written
+// substitutions on the project-written LU above (dgetrs_, trans "N"), an
+// upper Cholesky factor (dpotrf_, uplo "U", as pdblas::Cholesky calls it,
+// vcp/pdblas.hpp:207-222) and the two triangular solves pddblas::Cholesky
+// makes (dtrsm_ "L","U","T","N" and "R","U","N","N", alpha 1).  Any
+// approximate solves serve the refinement: it converges to the same dd
+// result within its accuracy.
+void dgetrs_(char* trans, int* n, int* nrhs, double* A, int* lda, int* ipiv, double* B,
+             int* ldb, int* info) {
+  if (trans[0] != 'N') unsupported("dgetrs_");
+  const int N = *n, ld = *lda;
+  *info = 0;
+  for (int c = 0; c < *nrhs; ++c) {
+    double* e = B + (long)c * (*ldb);
+    for (int j = 0; j < N; ++j) std::swap(e[j], e[ipiv[j] - 1]);
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < i; ++j) e[i] -= A[i + (long)j * ld] * e[j];
+    for (int i = N - 1; i >= 0; --i) {
+      for (int j = i + 1; j < N; ++j) e[i] -= A[i + (long)j * ld] * e[j];
+      e[i] /= A[i + (long)i * ld];
+    }
+  }
 }
-void dtrsm_(char*, char*, char*, char*, int*, int*, double*, double*, int*, double*, int*) {
-  unsupported("dtrsm_");
+
+void dpotrf_(char* uplo, int* n, double* A, int* lda, int* info) {
+  if (uplo[0] != 'U') unsupported("dpotrf_");
+  const int N = *n, ld = *lda;
+  *info = 0;
+  for (int j = 0; j < N; ++j) {  // A = U^T U, U in the upper triangle
+    double d = A[j + (long)j * ld];
+    for (int p = 0; p < j; ++p) d -= A[p + (long)j * ld] * A[p + (long)j * ld];
+    if (!(d > 0.0)) {
+      *info = j + 1;
+      return;
+    }
+    d = std::sqrt(d);
+    A[j + (long)j * ld] = d;
+    for (int c = j + 1; c < N; ++c) {
+      double t = A[j + (long)c * ld];
+      for (int p = 0; p < j; ++p) t -= A[p + (long)j * ld] * A[p + (long)c * ld];
+      A[j + (long)c * ld] = t / d;
+    }
+  }
+}
+
+void dtrsm_(char* side, char* uplo, char* transa, char* diag, int* m, int* n, double* alpha,
+            double* A, int* lda, double* B, int* ldb) {
+  const int M = *m, N = *n, la = *lda, lb = *ldb;
+  if (uplo[0] != 'U' || diag[0] != 'N' || *alpha != 1.0) unsupported("dtrsm_");
+  if (side[0] == 'L' && transa[0] == 'T') {  // U^T X = B, column by column
+    for (int c = 0; c < N; ++c)
+      for (int i = 0; i < M; ++i) {
+        double t = B[i + (long)c * lb];
+        for (int p = 0; p < i; ++p) t -= A[p + (long)i * la] * B[p + (long)c * lb];
+        B[i + (long)c * lb] = t / A[i + (long)i * la];
+      }
+  } else if (side[0] == 'R' && transa[0] == 'N') {  // X U = B, row by row
+    for (int r = 0; r < M; ++r)
+      for (int j = 0; j < N; ++j) {
+        double t = B[r + (long)j * lb];
+        for (int p = 0; p < j; ++p) t -= B[r + (long)p * lb] * A[p + (long)j * la];
+        B[r + (long)j * lb] = t / A[j + (long)j * la];
+      }
+  } else {
+    unsupported("dtrsm_");
+  }
 }
 
 double ddot_(int* n, const double* x, int* incx, const double* y, int* incy) {
@@ -255,7 +315,6 @@ void dsymm_(char*, char*, int*, int*, double*, const double*, int*, const double
             double*, int*) { unsupported("dsymm_"); }
 void dsyev_(char*, char*, int*, double*, int*, double*, double*, int*, int*) { unsupported("dsyev_"); }
 void dgesv_(int*, int*, double*, int*, int*, double*, int*, int*) { unsupported("dgesv_"); }
-void dpotrf_(char*, int*, double*, int*, int*) { unsupported("dpotrf_"); }
 
 // The reference vblas entry point, unchanged.
 void ref_rmatmul(int m, int n, int k, const double* A, const double* B, double* C, int rnd) {
@@ -640,6 +699,51 @@ int ref_pddblas_mulltmm(int m, int nc, const double* A, double* C) {
     for (long i = 0; i < (long)nc * nc; ++i) {
       C[2 * i] = c.data()[i].a1;
       C[2 * i + 1] = c.data()[i].a2;
+    }
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// x = A \ b through vcp::matrix<kv::dd, vcp::pddblas> (pddblas::linearsolve,
+// vcp/pddblas.hpp:413-474): LU in double, dd residuals by the Ozaki scheme.
+int ref_pddblas_linearsolve(int n, int nrhs, const double* A, const double* b, double* x) {
+  try {
+    vcp::matrix<kv::dd, vcp::pddblas> a, bb, xx;
+    a.zeros(n, n);
+    bb.zeros(n, nrhs);
+    for (long i = 0; i < (long)n * n; ++i) set_dd(a.data()[i], A + 2 * i);
+    for (long i = 0; i < (long)n * nrhs; ++i) set_dd(bb.data()[i], b + 2 * i);
+    xx = lss(a, bb);
+    for (long i = 0; i < (long)n * nrhs; ++i) {
+      x[2 * i] = xx.data()[i].a1;
+      x[2 * i + 1] = xx.data()[i].a2;
+    }
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// inv(A) (pddblas::inv, :477-486) and the upper Cholesky factor
+// (pddblas::Cholesky, :490-563): which = 0 / 1.
+int ref_pddblas_unary(int which, int n, const double* A, double* R) {
+  try {
+    vcp::matrix<kv::dd, vcp::pddblas> a, r;
+    a.zeros(n, n);
+    for (long i = 0; i < (long)n * n; ++i) set_dd(a.data()[i], A + 2 * i);
+    if (which == 0)
+      r = inv(a);
+    else
+      r = Cholesky(a);
+    for (long i = 0; i < (long)n * n; ++i) {
+      R[2 * i] = r.data()[i].a1;
+      R[2 * i + 1] = r.data()[i].a2;
     }
     return 0;
   } catch (...) {

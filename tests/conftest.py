@@ -43,3 +43,11 @@ def cuda_lib():
     build()
     from vcp_gb300 import _lib
     return _lib.load()
+
+
+@pytest.fixture(scope="session")
+def golden():
+    """The golden vectors the reference's own code produced
+    (tests/golden/golden.npz, written by tests/golden/make_golden.py)."""
+    import numpy as np
+    return np.load(ROOT / "tests" / "golden" / "golden.npz")

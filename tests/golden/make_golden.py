@@ -178,6 +178,42 @@ def main() -> None:
         data[f"dd{idx}_C"] = O.ref_pddblas_mulmm(m, n, k, A, B)
         data[f"dd{idx}_T"] = O.ref_pddblas_mulltmm(k, n, B)
     data["n_dd"] = np.array([len(dcases)])
+    # pddblas's refinement consumers (vcp/pddblas.hpp:413-563) as the
+    # reference runs them: linearsolve, inv, Cholesky on well-conditioned
+    # dd matrices (LU / Cholesky / triangular solves project-written)
+    import ctypes
+    R = O.ref_lib()
+    R.ref_pddblas_linearsolve.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 3
+    R.ref_pddblas_unary.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 2
+    rng6 = np.random.default_rng(20261209)
+    lcases = [(12, 1), (40, 3)]
+    for idx, (n, nrhs) in enumerate(lcases):
+        A = dd_matrix(rng6, n, n, 2)
+        A[0::2][np.arange(n) * (n + 1)] += 4.0 * n   # diagonally dominant
+        b = dd_matrix(rng6, n, nrhs, 2)
+        x = np.empty(2 * n * nrhs)
+        assert R.ref_pddblas_linearsolve(n, nrhs, A.ctypes.data, b.ctypes.data, x.ctypes.data) == 0
+        data[f"pls{idx}_shape"] = np.array([n, nrhs])
+        data[f"pls{idx}_A"], data[f"pls{idx}_b"], data[f"pls{idx}_x"] = A, b, x
+    data["n_pls"] = np.array([len(lcases)])
+    n = 16
+    A = dd_matrix(rng6, n, n, 1)
+    A[0::2][np.arange(n) * (n + 1)] += 3.0 * n
+    Ri = np.empty(2 * n * n)
+    assert R.ref_pddblas_unary(0, n, A.ctypes.data, Ri.ctypes.data) == 0
+    data["inv_n"], data["inv_A"], data["inv_R"] = np.array([n]), A, Ri
+    n = 24
+    G = dd_matrix(rng6, n, n, 1)
+    Gm = G[0::2].reshape(n, n, order="F")
+    S = Gm @ Gm.T + n * np.eye(n)
+    Sd = np.empty(2 * n * n)
+    Sd[0::2] = S.ravel(order="F")
+    lo = (S * 2.0 ** -53 * rng6.uniform(-1, 1, (n, n)))
+    lo = np.triu(lo) + np.triu(lo, 1).T             # symmetric dd
+    Sd[1::2] = lo.ravel(order="F")
+    U = np.empty(2 * n * n)
+    assert R.ref_pddblas_unary(1, n, Sd.ctypes.data, U.ctypes.data) == 0
+    data["chol_n"], data["chol_A"], data["chol_U"] = np.array([n]), Sd, U
     data["n_ge"] = np.array([len(gcases)])
     data["n_fm"] = np.array([len(fcases)])
     data["n_mp"] = np.array([len(pcases)])

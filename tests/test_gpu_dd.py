@@ -111,3 +111,38 @@ def test_dd_mulltmm_on_gpu(cuda_lib, oracle):
     scale = np.where(ab > 0, ab, 1.0)
     assert np.median(eg / scale) <= np.median(ep / scale)
     assert np.max(eg / scale) <= 2.0 ** -96
+
+
+def _close(X, Y, tol=2.0 ** -96):
+    scale = max(1.0, float(np.max(np.abs(Y[0::2]))))
+    return float(np.max(np.abs((X[0::2] - Y[0::2]) + (X[1::2] - Y[1::2])))) <= tol * scale
+
+
+def test_pddblas_refinements_on_gpu_reach_reference(cuda_lib, golden):
+    """pddblas::linearsolve / inv / Cholesky (vcp/pddblas.hpp:413-563) with
+    their accurate products on the GPU reach the reference's own results on
+    the golden systems (to 2^-96 relative: the double-precision steps differ
+    in last bits between LAPACK and the reference build's solves)."""
+    for idx in range(int(golden["n_pls"][0])):
+        n, nrhs = (int(v) for v in golden[f"pls{idx}_shape"])
+        x = pddcuda.linearsolve(golden[f"pls{idx}_A"], golden[f"pls{idx}_b"], n, nrhs)
+        assert _close(x, golden[f"pls{idx}_x"]), idx
+    n = int(golden["inv_n"][0])
+    assert _close(pddcuda.inv(golden["inv_A"], n), golden["inv_R"])
+    n = int(golden["chol_n"][0])
+    assert _close(pddcuda.cholesky(golden["chol_A"], n), golden["chol_U"])
+
+
+def test_pddblas_linearsolve_on_gpu_residual(cuda_lib, oracle):
+    """A 600 x 600 dd system solved with the GPU products: the exact residual
+    |A x - b| (long accumulator) is at dd level."""
+    rng = np.random.default_rng(9)
+    n, nrhs = 600, 2
+    A = dd_matrix(rng, n, n, 2)
+    A[0::2][np.arange(n) * (n + 1)] += 4.0 * n
+    b = dd_matrix(rng, n, nrhs, 2)
+    x = pddcuda.linearsolve(A, b, n, nrhs)
+    rows = np.repeat(np.arange(n), nrhs).astype(np.int32)
+    cols = np.tile(np.arange(nrhs), n).astype(np.int32)
+    err, ab = oracle.dd_residual(n, nrhs, n, A, x, b, rows, cols)
+    assert np.max(err) <= 2.0 ** -95 * np.max(ab)

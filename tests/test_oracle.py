@@ -25,11 +25,6 @@ def bits(x):
     return np.asarray(x, dtype=np.float64).view(np.int64)
 
 
-@pytest.fixture(scope="module")
-def golden():
-    return np.load(GOLDEN)
-
-
 def test_oracle_rmatmul_matches_golden(oracle, golden):
     for idx in range(int(golden["n_rm"][0])):
         m, n, k = map(int, golden[f"rm{idx}_shape"])

@@ -4,7 +4,8 @@ dd matrices use the kv::dd memory layout: column-major, each entry a pair
 {a1, a2} of doubles (value a1 + a2).  ``mulmm(A, B, m, n, k)`` returns the dd
 product C (kv buffer) and a rigorous per-entry upper bound of |AB - C|
 (vcp/pddblas.hpp:318-376 computes the same product, approximately, with
-double slices and dd accumulation).
+double slices and dd accumulation).  ``linearsolve``, ``inv`` and
+``cholesky`` are pddblas's refinement loops with their products here.
 """
 from __future__ import annotations
 
@@ -16,6 +17,8 @@ from .vblas import _dev_ptr, _host_ptr, _stream_ptr
 
 def mulmm(A: np.ndarray, B: np.ndarray, m: int, n: int, k: int, slices: int = 0,
           with_bound: bool = True):
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
     C = np.empty(2 * m * n, dtype=np.float64)
     E = np.empty(m * n, dtype=np.float64) if with_bound else None
     if m <= 0 or n <= 0:
@@ -44,3 +47,112 @@ def mulltmm(A: np.ndarray, n: int, k: int, slices: int = 0):
     Cm[iu[0], iu[1]] = Cm[iu[1], iu[0]]
     Em[iu[0], iu[1]] = Em[iu[1], iu[0]]
     return C, E
+
+
+# ---- the refinement consumers of pddblas (vcp/pddblas.hpp:413-563) ----------------
+#
+# pddblas's linear solve, inverse and Cholesky factor run their approximate
+# steps in double (LAPACK) and every accurate residual through the Ozaki
+# product (pddblas_assist::ozaki_acc).  These are the same loops with each
+# such product on the GPU (vcpcu_ddgemm) and the dd arithmetic of the kv
+# type, elementwise in numpy (round to nearest: TwoSum, Dekker's
+# renormalisation).  The C++ drop-in (include/vcp_cuda/pddcuda.hpp) runs the
+# same loops behind vcp::matrix<kv::dd, vcp::pddcuda>.
+
+def _twosum(a, b):
+    s = a + b
+    bb = s - a
+    return s, (a - (s - bb)) + (b - bb)
+
+
+def _fasttwosum(a, b):
+    s = a + b
+    return s, b - (s - a)
+
+
+def dd_add(x1, x2, y1, y2):
+    """x + y for dd arrays (kv::dd addition: TwoSum of both words, two
+    renormalisations)."""
+    s, e = _twosum(x1, y1)
+    t, f = _twosum(x2, y2)
+    e = e + t
+    s, e = _fasttwosum(s, e)
+    e = e + f
+    return _fasttwosum(s, e)
+
+
+def _kv(hi, lo):
+    out = np.empty(2 * hi.size, dtype=np.float64)
+    out[0::2] = hi.ravel(order="F")
+    out[1::2] = lo.ravel(order="F")
+    return out
+
+
+def _words(X, rows, cols):
+    return (X[0::2].reshape(rows, cols, order="F").copy(),
+            X[1::2].reshape(rows, cols, order="F").copy())
+
+
+def linearsolve(A: np.ndarray, b: np.ndarray, n: int, nrhs: int, slices: int = 0,
+                itmax: int = 10) -> np.ndarray:
+    """x = A \\ b for dd A (n x n) and b (n x nrhs), kv buffers, as
+    pddblas::linearsolve (vcp/pddblas.hpp:413-474): LU of double(A), then up
+    to itmax corrections d = LU \\ double(r), x += d, r = b - A x with A x
+    the dd product on the GPU; stops at dd accuracy (|d| <= 0.25e-32 |x|) or
+    when a correction fails to halve.  Returns the kv buffer of x."""
+    import scipy.linalg
+    Ah, _ = _words(A, n, n)
+    lu = scipy.linalg.lu_factor(Ah)
+    bh, bl = _words(b, n, nrhs)
+    xh = np.zeros((n, nrhs))
+    xl = np.zeros((n, nrhs))
+    rh, rl = bh.copy(), bl.copy()
+    prev = np.inf
+    for _ in range(itmax):
+        d = scipy.linalg.lu_solve(lu, rh)
+        xh, xl = dd_add(xh, xl, d, np.zeros_like(d))
+        normd = float(np.max(np.abs(d))) if d.size else 0.0
+        normx = float(np.max(np.abs(xh))) if xh.size else 0.0
+        if normd == 0.0 or normd <= 0.25e-32 * normx or normd >= 0.5 * prev:
+            break
+        prev = normd
+        Ax, _ = mulmm(A, _kv(xh, xl), n, nrhs, n, slices, with_bound=False)
+        axh, axl = _words(Ax, n, nrhs)
+        rh, rl = dd_add(bh, bl, -axh, -axl)
+    return _kv(xh, xl)
+
+
+def inv(A: np.ndarray, n: int, slices: int = 0) -> np.ndarray:
+    """inv(A) for a dd A (pddblas::inv, vcp/pddblas.hpp:477-486): A X = I by
+    linearsolve."""
+    eye = _kv(np.eye(n), np.zeros((n, n)))
+    return linearsolve(A, eye, n, n, slices)
+
+
+def cholesky(A: np.ndarray, n: int, slices: int = 0, itep: int = 2) -> np.ndarray:
+    """Upper Cholesky factor U (A = U^T U) of a symmetric dd A, as
+    pddblas::Cholesky (vcp/pddblas.hpp:490-563): U from the double factor,
+    then itep refinements E = A - U^T U (dd product on the GPU),
+    G = U^-T E U^-1 in double, W = triu(G, 1) + diag(G) / 2, U += W U
+    (GPU); the entries below the diagonal exact zeros."""
+    import scipy.linalg
+    Ah, Al = _words(A, n, n)
+    Ud = scipy.linalg.cholesky(Ah, lower=False)   # dpotrf "U", lower triangle zero
+    uh, ul = Ud.copy(), np.zeros((n, n))
+    for _ in range(itep):
+        U = _kv(uh, ul)
+        Ut = _kv(uh.T.copy(), ul.T.copy())
+        UtU, _ = mulmm(Ut, U, n, n, n, slices, with_bound=False)
+        th, tl = _words(UtU, n, n)
+        eh, el = dd_add(Ah, Al, -th, -tl)
+        Udh = uh
+        G = scipy.linalg.solve_triangular(Udh, eh, trans="T", lower=False)   # U^-T E
+        G = scipy.linalg.solve_triangular(Udh, G.T, trans="T", lower=False).T  # ... U^-1
+        W = np.triu(G, 1) + np.diag(np.diag(G)) * 0.5
+        F, _ = mulmm(_kv(W, np.zeros((n, n))), U, n, n, n, slices, with_bound=False)
+        fh, fl = _words(F, n, n)
+        uh, ul = dd_add(uh, ul, fh, fl)
+    il = np.tril_indices(n, -1)
+    uh[il] = 0.0
+    ul[il] = 0.0
+    return _kv(uh, ul)
