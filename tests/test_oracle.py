@@ -18,9 +18,6 @@ import pytest
 
 from vcp_gb300 import workloads as W
 
-GOLDEN = Path(__file__).resolve().parent / "golden" / "golden.npz"
-
-
 def bits(x):
     return np.asarray(x, dtype=np.float64).view(np.int64)
 
