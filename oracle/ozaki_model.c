@@ -249,7 +249,7 @@ static int crt_bits(int K, int s) {
   if (w > 62) w = 62; /* |A'|, |B'| <= 2^61 stay 64-bit integers */
   const int Keff = K > 1 ? K : 1;
   for (;;) {
-    double need = (2.0 * w - 1.0) + log2((double)Keff) + 0.01, bits = 0.0;
+    double need = 2.0 * w + log2((double)Keff) + 0.01, bits = 0.0;
     int L = 0;
     while (L < 16 && bits <= need) bits += log2((double)OZ_MOD[L++]);
     if (bits > need) return w;

@@ -195,11 +195,13 @@ int oz_take_status(cudaStream_t s, int* status) {
 }
 
 // CRT form: number of moduli L and basis Q_l for w-bit operands and inner
-// dimension K: the product A'B' satisfies |A'B'| <= K 2^(2w-2), and it is
-// recovered from its residues iff prod m_l > 2 K 2^(2w-2) = K 2^(2w-1).
+// dimension K: the product A'B' satisfies |A'B'| <= K 2^(2w-2); the moduli
+// are taken with prod m_l > K 2^(2w) = 4 max |A'B'|, so the centred value
+// lies within a quarter of M of zero and the reassembly's quotient needs no
+// correction step.
 // Returns 0, or -1 if 16 moduli do not suffice.
 int crt_setup(int K, int w, OzPlan* plan) {
-  const double need = (2.0 * w - 1.0) + std::log2((double)(K > 1 ? K : 1)) + 0.01;
+  const double need = 2.0 * w + std::log2((double)(K > 1 ? K : 1)) + 0.01;
   double bits = 0.0;
   int L = 0;
   while (L < OZ_MAX_MODULI_128 && bits <= need) bits += std::log2((double)OZ_MODULI[L++]);

@@ -5,7 +5,7 @@
 // (l < L) of the exact integer product of the w-bit operands
 // A' = round(mA 2^(w-E_i)), B' = round(mB 2^(w-F_j)).  Chinese remaindering
 // gives X = sum_l c_l Q_l mod M (Q_l = (M/m_l) ((M/m_l)^-1 mod m_l)), taken
-// in (-M/2, M/2]; since prod m_l > 2 |A'B'|, X = (A'B')(i,j) exactly.  Then
+// in (-M/4, M/4); since prod m_l > 4 |A'B'|, X = (A'B')(i,j) exactly.  Then
 //   mA mB = 2^(E+F-2w) X + ΔA mB + Â ΔB,   |ΔA| <= 2^(E-w-1), |ΔB| <= 2^(F-w-1),
 //   |ΔA mB| <= 2^(E-w-1) beta_j,   |Â ΔB| <= 2^(E+F-2w-1) sum_k |A'(i,k)|,
 // and the enclosure is [RD(2^(E+F-2w) X) - e, RU(2^(E+F-2w) X) + e] with
@@ -70,35 +70,6 @@ __device__ __forceinline__ void u64_to_dir(unsigned long long t, int e, double& 
   upv = scale_dir2(__ull2double_ru(t), e, true);
 }
 
-// r (5 limbs of 32 bits, little endian) >= m (4 limbs)?
-__device__ __forceinline__ bool ge_M(const uint32_t* r, const uint32_t* m) {
-  if (r[4]) return true;
-  for (int t = 3; t >= 0; --t) {
-    if (r[t] != m[t]) return r[t] > m[t];
-  }
-  return true;
-}
-
-__device__ __forceinline__ void sub_M(uint32_t* r, const uint32_t* m) {
-  unsigned long long borrow = 0;
-  for (int t = 0; t < 5; ++t) {
-    const unsigned long long mt = t < 4 ? m[t] : 0u;
-    const unsigned long long d = (unsigned long long)r[t] - mt - borrow;
-    r[t] = (uint32_t)d;
-    borrow = (d >> 63) & 1ULL;
-  }
-}
-
-__device__ __forceinline__ void add_M(uint32_t* r, const uint32_t* m) {
-  unsigned long long carry = 0;
-  for (int t = 0; t < 5; ++t) {
-    const unsigned long long mt = t < 4 ? m[t] : 0u;
-    const unsigned long long s = (unsigned long long)r[t] + mt + carry;
-    r[t] = (uint32_t)s;
-    carry = s >> 32;
-  }
-}
-
 // Directed conversion of (-1)^neg * mag * 2^e (mag: 4 limbs) to double.
 // Limbs are picked by unrolled selects (no dynamically indexed array, which
 // would live in local memory).
@@ -138,6 +109,11 @@ __device__ __forceinline__ void big_to_dir(const uint32_t (&mag)[4], int neg, in
   }
 }
 
+// Nearest integer of |x| < 2^22 on the FP32 pipe (ties to even).
+__device__ __forceinline__ float rint_f(float x) {
+  return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
+}
+
 // u32 -> float rounded to nearest (equal to __uint2float_rn) on the FP32
 // pipe: the two 16-bit halves are exact floats, one FMA rounds their sum.
 __device__ __forceinline__ float u32_to_f(uint32_t v) {
@@ -148,7 +124,12 @@ __device__ __forceinline__ float u32_to_f(uint32_t v) {
 
 // Exact X = (A'B')(i, j) from its residues (see the file comment); returns
 // the magnitude in mag[4] and the sign.
-// c[l] = 0 and Q_l = 0 for l >= L.
+// c[l] = 0 and Q_l = 0 for l >= L.  S = sum_l c_l Q_l < 2^12 M is formed
+// exactly in five 32-bit limbs; the plan keeps |X| <= K 2^(2w-2) < M / 4
+// (prod m_l > K 2^(2w)), so S / M lies within 1/4 of the integer q with
+// S = q M + X, and the fp32 estimate of S / M (relative error below 2^-20,
+// absolute below 2^-8) rounds to exactly that q: X = S - q M in one
+// multiply-subtract, already centred, with no correction step.
 __device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const uint32_t (&Q)[16][4],
                                          const uint32_t (&Mm)[4], float invMf,
                                          uint32_t (&mag)[4]) {
@@ -167,51 +148,32 @@ __device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const uint32_t
     carry = v >> 32;
   }
   r[4] = (uint32_t)carry;
-  // q = floor(S / M) < 2^12 estimated in fp32 (relative error < 2^-20, so
-  // off by at most one), then corrected exactly
   const float Sf = u32_to_f(r[4]) * 0x1p64f + u32_to_f(r[3]) * 0x1p32f + u32_to_f(r[2]) +
                    u32_to_f(r[1]) * 0x1p-32f + u32_to_f(r[0]) * 0x1p-64f;
-  const unsigned int q = (unsigned int)(Sf * invMf);
-  if (q) {
-    unsigned long long qm[5];
-    unsigned long long c2 = 0;
+  const unsigned int q = (unsigned int)rint_f(Sf * invMf);  // nearest integer to S / M
+  unsigned long long c2 = 0, borrow = 0;
+#pragma unroll
+  for (int t = 0; t < 5; ++t) {  // r = S - q M in five-limb two's complement
+    const unsigned long long v = (t < 4 ? (unsigned long long)q * Mm[t] : 0ULL) + c2;
+    c2 = v >> 32;
+    const unsigned long long d = (unsigned long long)r[t] - (uint32_t)v - borrow;
+    r[t] = (uint32_t)d;
+    borrow = (d >> 63) & 1ULL;
+  }
+  const int neg = (int)(r[4] >> 31);  // |X| < 2^125: the top limb is 0 or all ones
+  if (neg) {  // magnitude = -r
+    unsigned long long cy = 1;
+#pragma unroll
     for (int t = 0; t < 4; ++t) {
-      const unsigned long long v = (unsigned long long)q * Mm[t] + c2;
-      qm[t] = (uint32_t)v;
-      c2 = v >> 32;
+      const unsigned long long v = (unsigned long long)(~r[t]) + cy;
+      mag[t] = (uint32_t)v;
+      cy = v >> 32;
     }
-    qm[4] = c2;
-    unsigned long long borrow = 0;
-    for (int t = 0; t < 5; ++t) {
-      const unsigned long long d = (unsigned long long)r[t] - qm[t] - borrow;
-      r[t] = (uint32_t)d;
-      borrow = (d >> 63) & 1ULL;
-    }
-    for (int it = 0; it < 4 && borrow; ++it) {  // q was too large
-      add_M(r, Mm);
-      borrow = (r[4] >> 31) & 1u;  // still negative (two's complement in 5 limbs)
-    }
+  } else {
+#pragma unroll
+    for (int t = 0; t < 4; ++t) mag[t] = r[t];
   }
-  for (int it = 0; it < 4 && ge_M(r, Mm); ++it) sub_M(r, Mm);
-  // centre: X = r if 2r < M, else r - M (magnitude M - r)
-  uint32_t twice[5];
-  unsigned long long cy = 0;
-  for (int t = 0; t < 5; ++t) {
-    const unsigned long long v = ((unsigned long long)r[t] << 1) + cy;
-    twice[t] = (uint32_t)v;
-    cy = v >> 32;
-  }
-  if (ge_M(twice, Mm)) {
-    unsigned long long b = 0;
-    for (int t = 0; t < 4; ++t) {
-      const unsigned long long d = (unsigned long long)Mm[t] - r[t] - b;
-      mag[t] = (uint32_t)d;
-      b = (d >> 63) & 1ULL;
-    }
-    return 1;
-  }
-  for (int t = 0; t < 4; ++t) mag[t] = r[t];
-  return 0;
+  return neg;
 }
 
 // W of both radius products for 4 consecutive rows (e0 = j Mp + i0): the
