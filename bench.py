@@ -88,6 +88,8 @@ def parse():
     ap.add_argument("--phis", default="", help="point / dd: comma-separated phi")
     ap.add_argument("--slice-list", default="", help="point: comma-separated slice counts")
     ap.add_argument("--no-also", action="store_true", help="skip the short other workloads")
+    ap.add_argument("--batch-count", type=int, default=4096,
+                    help="batch: number of problems (--form ozaki: the tensor-core form only)")
     ap.add_argument("--no-model-check", action="store_true",
                     help="skip the bit-for-bit host-model check of sampled rows and columns")
     ap.add_argument("--only-headline", action="store_true",
@@ -534,7 +536,7 @@ def ozaki_roofline(phases, tc_flops, steps, pk, pk_kind, n=8192, default_form=Tr
 
 
 # ---------------------------------------------------------------- other workloads
-BATCH_WORKLOAD = ("batched interval GEMMs: 4096 problems, m,n,k log-uniform [32,1024], "
+BATCH_WORKLOAD = ("batched interval GEMMs: {} problems, m,n,k log-uniform [32,1024], "
                   "mid U[-1,1], rad 1e-12|mid|")
 
 
@@ -639,7 +641,7 @@ def bench_batch(dev, stream, steps=1, count=4096, seed=4096, forms=("plain", "oz
               pb[2 * ob[i]:2 * ob[i + 1]], int(k[i]), pc[2 * oc[i]:2 * oc[i + 1]], int(m[i]))
              for i in range(count)]
     flops = float(np.sum(2.0 * m * n * k))
-    out = {"workload": BATCH_WORKLOAD, "problems": count, "gflop_per_batch": flops / 1e9,
+    out = {"workload": BATCH_WORKLOAD.format(count), "problems": count, "gflop_per_batch": flops / 1e9,
            "seed": seed}
     codes = {"plain": pidcuda.FORM_PLAIN, "ozaki": pidcuda.FORM_OZAKI, "auto": pidcuda.FORM_AUTO}
     sample = rng.choice(count, 6, replace=False)
@@ -1028,7 +1030,9 @@ def run_workload(args, dev, stream):
     with ClockSampler(dev.index or 0) as clk:
         if args.workload == "batch":
             pidcuda.autotune(stream)
-            res = bench_batch(dev, stream, steps=args.steps)
+            forms = ("ozaki",) if args.form == "ozaki" else ("plain", "ozaki", "auto")
+            res = bench_batch(dev, stream, steps=args.steps, count=args.batch_count, forms=forms,
+                              check=not args.no_cpu)
             metric, unit = "batched interval GEMM TFLOP/s (4096 uneven problems)", "TFLOP/s"
             value = res["ozaki"]["tflops"]
         elif args.workload == "lss":
