@@ -313,7 +313,23 @@ void dsygv_(int* itype, char* jobz, char* uplo, int* n, double* A, int* lda, dou
 // members (vcp/pdblas.hpp:159-376), which are off the GEMM path: they abort.
 void dsymm_(char*, char*, int*, int*, double*, const double*, int*, const double*, int*, double*,
             double*, int*) { unsupported("dsymm_"); }
-void dsyev_(char*, char*, int*, double*, int*, double*, double*, int*, int*) { unsupported("dsyev_"); }
+// pdblas::eigsym's dsyev_ (jobz "V", uplo "U", vcp/pdblas.hpp:259-289): the
+// project-written dsygv_ above with B = I (eigenvalues ascending, orthonormal
+// eigenvectors in A); pddblas::eigsym refines its result.
+void dsyev_(char* jobz, char* uplo, int* n, double* A, int* lda, double* W, double* work,
+            int* lwork, int* info) {
+  const int N = *n;
+  *info = 0;
+  if (*lwork == -1) {
+    work[0] = 3.0 * (N > 0 ? N : 1);
+    return;
+  }
+  if (jobz[0] != 'V' || uplo[0] != 'U') unsupported("dsyev_");
+  std::vector<double> I((size_t)N * N, 0.0);
+  for (int i = 0; i < N; ++i) I[i + (size_t)i * N] = 1.0;
+  int itype = 1, ldi = N;
+  dsygv_(&itype, jobz, uplo, n, A, lda, I.data(), &ldi, W, work, lwork, info);
+}
 void dgesv_(int*, int*, double*, int*, int*, double*, int*, int*) { unsupported("dgesv_"); }
 
 // The reference vblas entry point, unchanged.
@@ -744,6 +760,39 @@ int ref_pddblas_unary(int which, int n, const double* A, double* R) {
     for (long i = 0; i < (long)n * n; ++i) {
       R[2 * i] = r.data()[i].a1;
       R[2 * i + 1] = r.data()[i].a2;
+    }
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// pddblas::eigsym (vcp/pddblas.hpp:566-614) and eigsymge (:616-657) with
+// eigenvectors, itep as given: the eigenvalues lam (n dd pairs) and the
+// eigenvectors X (n x n dd pairs, columns).  B == NULL: the standard problem.
+int ref_pddblas_eig(int n, const double* A, const double* B, int itep, double* lam, double* X) {
+  try {
+    vcp::matrix<kv::dd, vcp::pddblas> a, b, e, v;
+    a.zeros(n, n);
+    for (long i = 0; i < (long)n * n; ++i) set_dd(a.data()[i], A + 2 * i);
+    if (B) {
+      b.zeros(n, n);
+      for (long i = 0; i < (long)n * n; ++i) set_dd(b.data()[i], B + 2 * i);
+      eigsymge(a, b, e, v, itep);
+    } else {
+      eigsym(a, e, v, itep);
+    }
+    for (int i = 0; i < n; ++i) {
+      lam[2 * i] = e.data()[i + (long)i * n].a1;
+      lam[2 * i + 1] = e.data()[i + (long)i * n].a2;
+    }
+    for (long i = 0; i < (long)n * n; ++i) {
+      X[2 * i] = v.data()[i].a1;
+      X[2 * i + 1] = v.data()[i].a2;
     }
     return 0;
   } catch (...) {

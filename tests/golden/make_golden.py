@@ -214,6 +214,34 @@ def main() -> None:
     U = np.empty(2 * n * n)
     assert R.ref_pddblas_unary(1, n, Sd.ctypes.data, U.ctypes.data) == 0
     data["chol_n"], data["chol_A"], data["chol_U"] = np.array([n]), Sd, U
+    # pddblas::eigsym / eigsymge with eigenvectors (Ogita-Aishima refinement
+    # of the double eigenpairs; dsyev / dsygv project-written): symmetric
+    # matrices with well separated eigenvalues
+    R.ref_pddblas_eig.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                  ctypes.c_void_p, ctypes.c_void_p]
+
+    def sym_dd(nn, spectrum):
+        Qm, _ = np.linalg.qr(rng6.standard_normal((nn, nn)))
+        S = (Qm * spectrum) @ Qm.T
+        S = (S + S.T) / 2
+        lo = S * 2.0 ** -53 * rng6.uniform(-1, 1, (nn, nn))
+        lo = np.triu(lo) + np.triu(lo, 1).T
+        out = np.empty(2 * nn * nn)
+        out[0::2], out[1::2] = S.ravel(order="F"), lo.ravel(order="F")
+        return out
+    n = 20
+    A = sym_dd(n, np.arange(1.0, n + 1.0) * 1.5)
+    lam, X = np.empty(2 * n), np.empty(2 * n * n)
+    assert R.ref_pddblas_eig(n, A.ctypes.data, None, 1, lam.ctypes.data, X.ctypes.data) == 0
+    data["eig_n"], data["eig_A"], data["eig_lam"], data["eig_X"] = np.array([n]), A, lam, X
+    n = 16
+    A = sym_dd(n, np.linspace(-3.0, 5.0, n))
+    B = sym_dd(n, np.linspace(1.0, 2.0, n))
+    lam, X = np.empty(2 * n), np.empty(2 * n * n)
+    assert R.ref_pddblas_eig(n, A.ctypes.data, B.ctypes.data, 1, lam.ctypes.data,
+                             X.ctypes.data) == 0
+    data["eigge_n"], data["eigge_A"], data["eigge_B"] = np.array([n]), A, B
+    data["eigge_lam"], data["eigge_X"] = lam, X
     data["n_ge"] = np.array([len(gcases)])
     data["n_fm"] = np.array([len(fcases)])
     data["n_mp"] = np.array([len(pcases)])

@@ -146,3 +146,17 @@ def test_pddblas_linearsolve_on_gpu_residual(cuda_lib, oracle):
     cols = np.tile(np.arange(nrhs), n).astype(np.int32)
     err, ab = oracle.dd_residual(n, nrhs, n, A, x, b, rows, cols)
     assert np.max(err) <= 2.0 ** -95 * np.max(ab)
+
+
+def test_pddblas_eigen_refinements_on_gpu_reach_reference(cuda_lib, golden):
+    """pddblas::eigsym / eigsymge (Ogita-Aishima refinement,
+    vcp/pddblas.hpp:221-314, 566-657) with every product on the GPU: the
+    eigenvalues and (sign-matched) eigenvectors reach the reference's own to
+    2^-90 relative."""
+    from tests.test_pddcuda_host import eig_close
+    n = int(golden["eig_n"][0])
+    lam, X = pddcuda.eigsym(golden["eig_A"], n)
+    assert eig_close(lam, X, golden["eig_lam"], golden["eig_X"], n)
+    n = int(golden["eigge_n"][0])
+    lam, X = pddcuda.eigsymge(golden["eigge_A"], golden["eigge_B"], n)
+    assert eig_close(lam, X, golden["eigge_lam"], golden["eigge_X"], n)

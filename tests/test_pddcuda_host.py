@@ -61,3 +61,30 @@ def test_dd_add_is_kv_addition():
         exact = F(x1[i]) + F(x2[i]) + F(y1[i]) + F(y2[i])
         got = F(s1[i]) + F(s2[i])
         assert abs(got - exact) <= abs(exact) * F(2) ** -100 + F(2) ** -1074
+
+
+def eig_close(lam, X, lam_ref, X_ref, n, tol=2.0 ** -90):
+    """Eigenvalues to tol relative to the largest; eigenvectors to tol per
+    column after matching each column's sign to the reference's."""
+    scale = float(np.max(np.abs(lam_ref[0::2])))
+    dl = np.abs((lam[0::2] - lam_ref[0::2]) + (lam[1::2] - lam_ref[1::2]))
+    if float(np.max(dl)) > tol * scale:
+        return False
+    Xh, Xl = X[0::2].reshape(n, n, order="F"), X[1::2].reshape(n, n, order="F")
+    Rh, Rl = X_ref[0::2].reshape(n, n, order="F"), X_ref[1::2].reshape(n, n, order="F")
+    for j in range(n):
+        i = int(np.argmax(np.abs(Rh[:, j])))
+        sg = 1.0 if (Xh[i, j] > 0) == (Rh[i, j] > 0) else -1.0
+        d = np.abs((sg * Xh[:, j] - Rh[:, j]) + (sg * Xl[:, j] - Rl[:, j]))
+        if float(np.max(d)) > tol * float(np.max(np.abs(Rh[:, j]))):
+            return False
+    return True
+
+
+def test_eigsym_and_eigsymge_reach_reference(cpu_products, golden):
+    n = int(golden["eig_n"][0])
+    lam, X = pddcuda.eigsym(golden["eig_A"], n)
+    assert eig_close(lam, X, golden["eig_lam"], golden["eig_X"], n)
+    n = int(golden["eigge_n"][0])
+    lam, X = pddcuda.eigsymge(golden["eigge_A"], golden["eigge_B"], n)
+    assert eig_close(lam, X, golden["eigge_lam"], golden["eigge_X"], n)

@@ -4,8 +4,9 @@ dd matrices use the kv::dd memory layout: column-major, each entry a pair
 {a1, a2} of doubles (value a1 + a2).  ``mulmm(A, B, m, n, k)`` returns the dd
 product C (kv buffer) and a rigorous per-entry upper bound of |AB - C|
 (vcp/pddblas.hpp:318-376 computes the same product, approximately, with
-double slices and dd accumulation).  ``linearsolve``, ``inv`` and
-``cholesky`` are pddblas's refinement loops with their products here.
+double slices and dd accumulation).  ``linearsolve``, ``inv``,
+``cholesky``, ``eigsym`` and ``eigsymge`` are pddblas's refinement loops
+with their products here.
 """
 from __future__ import annotations
 
@@ -156,3 +157,101 @@ def cholesky(A: np.ndarray, n: int, slices: int = 0, itep: int = 2) -> np.ndarra
     uh[il] = 0.0
     ul[il] = 0.0
     return _kv(uh, ul)
+
+
+def _split(a):
+    c = 134217729.0 * a          # Veltkamp splitting, 2^27 + 1
+    hi = c - (c - a)
+    return hi, a - hi
+
+
+def _twoprod(a, b):
+    """p + e = a b exactly (Dekker)."""
+    p = a * b
+    ah, al = _split(a)
+    bh, bl = _split(b)
+    return p, ((ah * bh - p) + ah * bl + al * bh) + al * bl
+
+
+def dd_mul(x1, x2, y1, y2):
+    """x y for dd arrays (the kv stand-in's product: TwoProduct of the
+    leading words plus the cross terms, renormalised)."""
+    p, e = _twoprod(x1, y1)
+    e = e + (x1 * y2 + x2 * y1)
+    return _fasttwosum(p, e)
+
+
+def dd_div(x1, x2, y1, y2):
+    """x / y for dd arrays: the leading quotient and one correction from the
+    dd remainder x - y q1."""
+    q1 = x1 / y1
+    t1, t2 = dd_mul(y1, y2, q1, np.zeros_like(q1))
+    r1, _ = dd_add(x1, x2, -t1, -t2)
+    return _fasttwosum(q1, r1 / y1)
+
+
+def _oa_step(A, B, xh, xl, n, slices):
+    """One Ogita-Aishima refinement step (pddblas::oa_step,
+    vcp/pddblas.hpp:221-314) for A x = lambda B x (B None: B = I), every
+    product on the GPU.  Returns the refined X and the eigenvalues."""
+    X = _kv(xh, xl)
+    Xt = _kv(xh.T.copy(), xl.T.copy())
+    AX, _ = mulmm(A, X, n, n, n, slices, with_bound=False)
+    S, _ = mulmm(Xt, AX, n, n, n, slices, with_bound=False)
+    if B is not None:
+        BX, _ = mulmm(B, X, n, n, n, slices, with_bound=False)
+        G, _ = mulmm(Xt, BX, n, n, n, slices, with_bound=False)
+    else:
+        G, _ = mulmm(Xt, X, n, n, n, slices, with_bound=False)
+    sh, sl = _words(S, n, n)
+    gh, gl = _words(G, n, n)
+    d = np.arange(n)
+    lh, ll = dd_div(sh[d, d], sl[d, d], gh[d, d], gl[d, d])   # lambda_i = S_ii / G_ii
+    rh, rl = -gh, -gl                                          # R = I - G
+    rh[d, d], rl[d, d] = dd_add(rh[d, d], rl[d, d], np.ones(n), np.zeros(n))
+    normR = float(np.max(np.sum(np.abs(rh), axis=1)))
+    offS = float(np.max(np.sum(np.abs(sh), axis=1) - np.abs(sh[d, d])))
+    delta = 2.0 * (offS + normR * float(np.max(np.abs(lh))))
+    # E_ij = (S_ij + lambda_j R_ij) / (lambda_j - lambda_i) where separated,
+    # R_ij / 2 otherwise (and on the diagonal)
+    Lj1, Lj2 = np.broadcast_to(lh, (n, n)), np.broadcast_to(ll, (n, n))
+    Li1, Li2 = np.broadcast_to(lh[:, None], (n, n)), np.broadcast_to(ll[:, None], (n, n))
+    dh, dl = dd_add(Lj1, Lj2, -Li1, -Li2)
+    nh, nl = dd_add(sh, sl, *dd_mul(Lj1, Lj2, rh, rl))
+    with np.errstate(divide="ignore", invalid="ignore"):   # unseparated pairs: not used
+        qh, ql = dd_div(nh, nl, dh, dl)
+    sep = (np.abs(dh) > delta) & ~np.eye(n, dtype=bool)
+    eh = np.where(sep, qh, rh * 0.5)
+    el = np.where(sep, ql, rl * 0.5)
+    XE, _ = mulmm(X, _kv(eh, el), n, n, n, slices, with_bound=False)
+    fh, fl = _words(XE, n, n)
+    xh, xl = dd_add(xh, xl, fh, fl)
+    return xh, xl, lh, ll
+
+
+def eigsym(A: np.ndarray, n: int, itep: int = 1, slices: int = 0, B: np.ndarray | None = None):
+    """Eigenvalues and eigenvectors of a symmetric dd A (B None) or of
+    A x = lambda B x, as pddblas::eigsym / eigsymge (vcp/pddblas.hpp:566-657):
+    the double eigenpairs of LAPACK (dsyev / dsygv), then max(2, itep)
+    Ogita-Aishima steps with their products on the GPU.  Returns (lambda as
+    a kv buffer of n dd values, X as a kv buffer of n x n, columns the
+    eigenvectors)."""
+    import scipy.linalg
+    Ah, _ = _words(A, n, n)
+    if B is None:
+        w, V = scipy.linalg.eigh(Ah)
+    else:
+        Bh, _ = _words(B, n, n)
+        w, V = scipy.linalg.eigh(Ah, Bh)
+    xh, xl = np.array(V, dtype=np.float64, order="C"), np.zeros((n, n))
+    lh, ll = np.asarray(w, dtype=np.float64), np.zeros(n)
+    for _ in range(max(2, itep)):
+        xh, xl, lh, ll = _oa_step(A, B, xh, xl, n, slices)
+    lam = np.empty(2 * n)
+    lam[0::2], lam[1::2] = lh, ll
+    return lam, _kv(xh, xl)
+
+
+def eigsymge(A: np.ndarray, B: np.ndarray, n: int, itep: int = 1, slices: int = 0):
+    """A x = lambda B x for symmetric dd A, B (pddblas::eigsymge)."""
+    return eigsym(A, n, itep, slices, B=B)
