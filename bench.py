@@ -980,6 +980,7 @@ def bench_emden(dev, Ms=(30, 50, 70), cpu_Ms=(30,), repeats=2, forms=("plain", "
         t0 = time.perf_counter()
         legendre.basis_tables(M, E.npts_inverse(M))
         legendre.basis_tables(M, E.npts_residual(M))
+        E.stiffness(M, *E.even_list(M))
         rec["legendre_tables_s"] = time.perf_counter() - t0
         g = E.GpuProducts(pidcuda.FORM_PLAIN)
         for _ in range(repeats):

@@ -98,3 +98,32 @@ def test_grouped_batch_slice_counts(cuda_lib, slices):
         pidcuda.mulmm_dev(m, n, k, A, lda, B, ldb, ref, ldc, pidcuda.FORM_OZAKI, slices)
         torch.cuda.synchronize()
         assert torch.equal(C.view(torch.int64), ref.view(torch.int64)), (m, n, k, slices)
+
+
+def test_grouped_batch_chunked_buckets(cuda_lib):
+    """A bucket (one padded K) holding more work than one chunk is cut into
+    several chunks that run one after another on the shared workspace: 200
+    problems of k <= 64 (padded K 64; 14 or 15 moduli by k) and m, n in
+    [200, 400] make two buckets of about 0.45 ms of estimated work each, two
+    chunks apiece; every product bit-identical to its single call, and graph
+    replays give each problem a latency."""
+    import torch
+    rng = np.random.default_rng(123)
+    probs = []
+    for _ in range(200):
+        m, n = (int(x) for x in rng.integers(200, 401, 2))
+        k = int(rng.integers(1, 65))
+        A = torch.from_numpy(W.interval_uniform(rng, m, k, 1e-12)).cuda()
+        B = torch.from_numpy(W.interval_uniform(rng, k, n, 1e-12)).cuda()
+        C = torch.full((2 * m * n,), float("nan"), dtype=torch.float64, device="cuda")
+        probs.append((m, n, k, A, m, B, k, C, m))
+    g = batch.BatchGraph(probs, pidcuda.FORM_OZAKI)
+    g.launch()
+    _, lat = g.latencies()
+    assert np.all(lat > 0)
+    g.close()
+    for (m, n, k, A, lda, B, ldb, C, ldc) in probs:
+        ref = torch.empty_like(C)
+        pidcuda.mulmm_dev(m, n, k, A, lda, B, ldb, ref, ldc, pidcuda.FORM_OZAKI)
+        torch.cuda.synchronize()
+        assert torch.equal(C.view(torch.int64), ref.view(torch.int64)), (m, n, k)

@@ -98,6 +98,10 @@ struct alignas(128) OzGemmArgs {
   const int* gitem;
   const int* gprob;  // item -> problem (one load per item)
   int gnprob, gnitems;
+  // bsub != 0 (grouped products): tmB has 64-row boxes and a tile loads and
+  // multiplies only the 64-column blocks that hold columns of its problem
+  // (MMA N = 64, 128, 192 or 256); else one 256-row box, N = 256
+  int bsub;
   OzPairList pl;
 };
 
@@ -201,14 +205,15 @@ int oz_run_product(const OzPlan& plan, OzWorkspace& ws, const double* A, long ld
 
 // ---------------------------------------------------------------------------
 // Grouped CRT-form products (a batch of uneven interval products in a few
-// launches).  Problems with the same padded inner dimension Kp form a
-// bucket; the bucket's operand planes are stacked: the rows of problem p
-// occupy rows [rowoff, rowoff + Mp) of the A planes ([plane][Mtot][Kp]) and
-// [coloff, coloff + Np) of the B planes ([plane][Ntot][Kp]); its residue
-// bytes and radius folds live at res_off / P_off of the bucket's arrays,
-// laid out as in a single product.  Every kernel of the CRT form has a
-// grouped twin that finds its problem by a binary search over a prefix
-// array of blocks or work items.
+// launches).  Problems with the same padded inner dimension Kp, modulus
+// count and operand width form a bucket (cut into chunks of similar work);
+// the bucket's operand planes are stacked: the rows of problem p occupy rows
+// [rowoff, rowoff + Mp) of the A planes ([plane][Mtot][Kp]) and [coloff,
+// coloff + Np) of the B planes ([plane][Ntot][Kp]); its residue bytes and
+// radius folds live at res_off / P_off of the bucket's arrays, laid out as
+// in a single product.  Every kernel of the CRT form has a grouped twin
+// that finds its problem by a binary search over a prefix array of blocks,
+// or by one load from a block / item -> problem table.
 struct OzGProb {
   int m, n, k;
   const double* A;
@@ -238,6 +243,7 @@ struct OzGBucket {
   const int* prob_rad;     // [radius items] the problem of each item
   const int* prob_crt;     // [residue items] the problem of each item
   const int* blk_asm;      // [nprob + 1] prefix of reassembly blocks
+  const int* prob_asm;     // [reassembly blocks] the problem of each block
   const int* col_prob;     // [Ntot] problem of each stacked B column
   uint16_t* planesA;       // [Lmax + 4][Mtot][Kp]: residues, |mA|+rA digits, rA digits
   uint16_t* planesB;       // [Lmax + 4][Ntot][Kp]: residues, rB digits, |mB| digits
@@ -261,7 +267,9 @@ struct OzGBucket {
 int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, int wmax, cudaStream_t st);
 int oz_grun_gemm(const OzGBucket& b, const OzPlan& shape, int mode, int nitems,
                  cudaStream_t st);
-int oz_gassemble(const OzGBucket& b, const OzRadConst& rc, int nblk, cudaStream_t st);
+// shape: the bucket's plan (every problem of a bucket has the same CRT basis)
+int oz_gassemble(const OzGBucket& b, const OzPlan& shape, const OzRadConst& rc, int nblk,
+                 cudaStream_t st);
 // The grouped CRT-form product of a batch (batch.cu's tensor-core path).
 // oz_group_plan builds the buckets and uploads their tables (outside any
 // stream capture); oz_group_record launches the kernels of every bucket on

@@ -328,20 +328,6 @@ __device__ __forceinline__ void assemble_quad_col(
   }
 }
 
-// One quad of rows in one column (the grouped reassembly's unit).  E3, F2,
-// asum and beta point at row / column 0 of this product.
-__device__ __forceinline__ void assemble_quad(
-    int i0, int j, int M, int Mp, int L, int w, const uint8_t* __restrict__ res, size_t plane,
-    const int* __restrict__ E3, const int* __restrict__ F2,
-    const unsigned long long* __restrict__ asum, const double* __restrict__ beta,
-    const int32_t* __restrict__ P, double* __restrict__ C, long ldc, bool nonfinite,
-    const uint32_t (&Q)[16][4], const uint32_t (&Mm)[4], float invMf, const OzRadConst& rc) {
-  QuadRows rw;
-  quad_rows(i0, M, E3, asum, rw);
-  assemble_quad_col(rw, i0, j, M, Mp, L, w, res, plane, F2, beta, P, C, ldc, nonfinite, Q, Mm,
-                    invMf, rc);
-}
-
 // Thread = 4 consecutive rows of about 8 columns; blockIdx.y strides over the
 // columns (no 64-bit index division).  At most 80 registers: three blocks per
 // SM (measured at n = 8192: 1.88 ms; 2.10 ms at the unbounded 94 registers).
@@ -363,33 +349,44 @@ oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __rest
                       cc.Q, cc.M, cc.invMf, rc);
 }
 
-__device__ __forceinline__ int gfind(const int* __restrict__ prefix, int nprob, int x) {
-  int lo = 0, hi = nprob - 1;  // largest p with prefix[p] <= x
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (prefix[mid] <= x)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
-
-// Grouped reassembly: each block works on one problem (blk_asm prefix);
-// every block stamps the problem's end.  A device-wait timeout of the slice
-// GEMM (flag[1] of problem 0) poisons every output of the bucket.
-__global__ void __launch_bounds__(256)
-oz_crt_assemble_g(const __grid_constant__ OzGBucket b, const __grid_constant__ OzRadConst rc) {
-  const int p = gfind(b.blk_asm, b.nprob, blockIdx.x);
+// Grouped reassembly.  The problems of a bucket share one CRT plan (the
+// bucket is keyed by padded K, modulus count and operand width), so the
+// basis comes in the launch parameters as for one product.  A thread takes 4
+// consecutive rows of one problem and the columns cg, cg + NG, cg + 2 NG, ...
+// (NG = ceil(n / 8) column groups): its rows' exponents and sums are set up
+// once for about 8 columns, and consecutive threads take consecutive row
+// quads (coalesced residue and fold reads).  A block finds its problem with
+// one load (prob_asm); every block stamps the problem's end.  117
+// registers: two blocks per SM (the problem's pointers and sizes stay in
+// registers where one product has them in the launch parameters; at 80
+// registers they spill).  A device-wait
+// timeout of the slice GEMM (flag[1] of problem 0) poisons every output of
+// the bucket.
+__global__ void __launch_bounds__(256, 2)
+oz_crt_assemble_g(const __grid_constant__ OzGBucket b, const __grid_constant__ CrtConst cc,
+                  const __grid_constant__ OzRadConst rc) {
+  const int p = b.prob_asm[blockIdx.x];
   const OzGProb& q = b.probs[p];
-  const int Mq = (q.m + 3) >> 2;
-  const long idx = (long)(blockIdx.x - b.blk_asm[p]) * blockDim.x + threadIdx.x;
-  const bool nonfinite = b.flag[4 * p] != 0 || b.flag[1] != 0;
-  if (idx < (long)Mq * q.n)
-    assemble_quad(4 * (int)(idx % Mq), (int)(idx / Mq), q.m, q.Mp, q.L, q.w, b.res + q.res_off,
-                  (size_t)q.Np * q.Mp, b.E3 + 3 * (size_t)q.rowoff, b.F2 + 2 * (size_t)q.coloff,
-                  b.asum + 2 * (size_t)q.rowoff, b.beta + q.coloff, b.P + q.P_off, q.C, q.ldc,
-                  nonfinite, q.Q, q.Mlimb, q.invMf, rc);
+  const int m = q.m, n = q.n;
+  const int Mq = (m + 3) >> 2;
+  const int NG = (n + 7) >> 3;
+  const long u = (long)(blockIdx.x - b.blk_asm[p]) * blockDim.x + threadIdx.x;
+  if (u < (long)Mq * NG) {
+    const bool nonfinite = b.flag[4 * p] != 0 || b.flag[1] != 0;
+    const int qd = (int)(u % Mq), cg = (int)(u / Mq);
+    const int* E3 = b.E3 + 3 * (size_t)q.rowoff;
+    const unsigned long long* asum = b.asum + 2 * (size_t)q.rowoff;
+    const int* F2 = b.F2 + 2 * (size_t)q.coloff;
+    const double* beta = b.beta + q.coloff;
+    const uint8_t* res = b.res + q.res_off;
+    const int32_t* P = b.P + q.P_off;
+    const size_t plane = (size_t)q.Np * q.Mp;
+    QuadRows rw;
+    quad_rows(4 * qd, m, E3, asum, rw);
+    for (int j = cg; j < n; j += NG)
+      assemble_quad_col(rw, 4 * qd, j, m, q.Mp, q.L, q.w, res, plane, F2, beta, P, q.C, q.ldc,
+                        nonfinite, cc.Q, cc.M, cc.invMf, rc);
+  }
   if (b.t_last) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -402,17 +399,25 @@ oz_crt_assemble_g(const __grid_constant__ OzGBucket b, const __grid_constant__ O
 
 }  // namespace
 
-int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long ldc,
-                    cudaStream_t st) {
-  const OzProblem& pb = plan.pb;
+namespace {
+// The CRT basis of a plan's L moduli (Q_l = 0 past L), M and 2^64 / M.
+CrtConst crt_const(const OzPlan& plan) {
   CrtConst cc;
   memset(&cc, 0, sizeof(cc));
-  for (int l = 0; l < pb.L; ++l)
+  for (int l = 0; l < plan.pb.L; ++l)
     for (int t = 0; t < 4; ++t) cc.Q[l][t] = plan.Q[l][t];
   for (int t = 0; t < 4; ++t) cc.M[t] = plan.Mlimb[t];
   const double Md = (double)cc.M[3] * 0x1p96 + (double)cc.M[2] * 0x1p64 +
                     (double)cc.M[1] * 0x1p32 + (double)cc.M[0];
   cc.invMf = (float)(0x1p64 / Md);
+  return cc;
+}
+}  // namespace
+
+int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long ldc,
+                    cudaStream_t st) {
+  const OzProblem& pb = plan.pb;
+  const CrtConst cc = crt_const(plan);
   if (pb.M <= 0 || pb.N <= 0) return VCPCU_OK;
   const int Mq = (pb.M + 3) / 4;
   // about 8 columns per thread: its rows' exponents and sums are set up once
@@ -425,9 +430,10 @@ int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long l
   return VCPCU_OK;
 }
 
-int oz_gassemble(const OzGBucket& b, const OzRadConst& rc, int nblk, cudaStream_t st) {
+int oz_gassemble(const OzGBucket& b, const OzPlan& shape, const OzRadConst& rc, int nblk,
+                 cudaStream_t st) {
   if (nblk <= 0) return VCPCU_OK;
-  oz_crt_assemble_g<<<nblk, 256, 0, st>>>(b, rc);
+  oz_crt_assemble_g<<<nblk, 256, 0, st>>>(b, crt_const(shape), rc);
   VCPCU_LAUNCH_CHECK("oz_crt_assemble_g");
   return VCPCU_OK;
 }

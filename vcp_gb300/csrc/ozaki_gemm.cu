@@ -19,6 +19,12 @@
 //                fold is merged into the final epilogue
 //                [lo, up] = [RD(W unit) - e, RU((W + R) unit) + e].
 //
+// Grouped products (a batch bucket) load B in 64-row boxes and multiply only
+// the 64-column blocks of a tile that hold columns of its problem (MMA N =
+// 64 .. 256): a narrow problem moves and multiplies a quarter to three
+// quarters of a full tile; the epilogue skips the blocks that were not
+// multiplied (their columns are past N and never stored for reassembly).
+//
 // Warp roles (320 threads, one CTA per SM, persistent over tiles):
 //   warp 0      TMA producer (4-stage ring of 48 KB A+B k-blocks)
 //   warp 1      TMEM owner + MMA issuer (one thread)
@@ -41,8 +47,8 @@ namespace {
 constexpr int NTHREADS = 320;
 constexpr int A_STAGE = OZ_BM * OZ_BK * 2;  // 16 KB
 constexpr int B_STAGE = OZ_BN * OZ_BK * 2;  // 32 KB
+constexpr int B_SUB = 64 * OZ_BK * 2;       // 8 KB: one 64-column block of B
 constexpr int STAGE_BYTES = A_STAGE + B_STAGE;
-constexpr uint32_t IDESC = ptx::idesc_bf16_f32(OZ_BM, OZ_BN);
 constexpr int TMEM_COLS = 512;  // two 128 x 256 fp32 accumulators
 
 struct Smem {
@@ -100,6 +106,7 @@ __device__ __forceinline__ void tile_coords(int tile, int tiles_m, int tiles_n, 
 struct ItemInfo {
   int arow, bcol;   // TMA row of the A tile / of the B tile in the planes
   int tm, tn, g0, g1;
+  int nb;           // 64-column blocks of B the tile multiplies (1..4)
   int Mp, Np;       // output layout of this item's problem
   int M, N;         // its valid rows / columns
   uint8_t* res;
@@ -134,6 +141,7 @@ __device__ __forceinline__ ItemInfo item_info(const OzGemmArgs& a, int item, int
     f.Np = q.Np;
     f.M = q.m;
     f.N = q.n;
+    f.nb = a.bsub ? min(4, (f.N - f.tn * OZ_BN + 63) >> 6) : 4;
     f.res = a.res ? a.res + q.res_off : nullptr;
     f.P = a.P ? a.P + q.P_off : nullptr;
     return f;
@@ -154,6 +162,7 @@ __device__ __forceinline__ ItemInfo item_info(const OzGemmArgs& a, int item, int
   f.Np = a.Np;
   f.M = a.M;
   f.N = a.N;
+  f.nb = 4;
   f.res = a.res;
   f.P = a.P;
   return f;
@@ -236,9 +245,17 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
             }
             uint8_t* sA = dsmem + stage * STAGE_BYTES;
             uint8_t* sB = sA + A_STAGE;
-            ptx::mbar_expect_tx(&sm.full[stage], STAGE_BYTES);
+            ptx::mbar_expect_tx(&sm.full[stage], A_STAGE + f.nb * B_SUB);
             ptx::tma_load_3d(sA, &args.tmA, &sm.full[stage], kb * OZ_BK, f.arow, pa);
-            ptx::tma_load_3d(sB, &args.tmB, &sm.full[stage], kb * OZ_BK, f.bcol, pb);
+            if (args.bsub) {
+              // 64-row boxes land back to back: the same SW128 K-major
+              // layout as one box of 64 nb rows
+              for (int i = 0; i < f.nb; ++i)
+                ptx::tma_load_3d(sB + i * B_SUB, &args.tmB, &sm.full[stage], kb * OZ_BK,
+                                 f.bcol + 64 * i, pb);
+            } else {
+              ptx::tma_load_3d(sB, &args.tmB, &sm.full[stage], kb * OZ_BK, f.bcol, pb);
+            }
             used |= 1u << stage;
             lastpar = (lastpar & ~(1u << stage)) | (phase << stage);
             if (++stage == OZ_STAGES) {
@@ -262,6 +279,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
       bool ok = true;
       for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
         const ItemInfo f = item_info(args, item, ntiles);
+        const uint32_t idesc = ptx::idesc_bf16_f32(OZ_BM, 64 * f.nb);
         for (int pi = args.pl.gstart[f.g0]; pi < args.pl.gstart[f.g1] && ok; ++pi) {
           for (int ch = 0; ch < nchunks && ok; ++ch, ++acc) {
             const int buf = acc & 1;
@@ -288,7 +306,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
               for (int kk = 0; kk < OZ_BK / 16; ++kk) {
                 const uint64_t ad = ptx::sw128_kmajor_desc(sA + kk * 32);
                 const uint64_t bd = ptx::sw128_kmajor_desc(sB + kk * 32);
-                ptx::mma_bf16(dt, ad, bd, IDESC, (kb > kb0 || kk > 0) ? 1u : 0u);
+                ptx::mma_bf16(dt, ad, bd, idesc, (kb > kb0 || kk > 0) ? 1u : 0u);
               }
               ptx::mma_commit(&sm.empty[stage]);
               if (++stage == OZ_STAGES) {
@@ -352,6 +370,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
           const int ncol = gi < f.M ? f.N - gj0 : 0;  // 0: a padding row
 #pragma unroll 1
           for (int c8 = 0; c8 < 2; ++c8, rp += 64 * ld) {
+            if (half * 2 + c8 >= f.nb) break;  // columns the tile did not multiply
             uint32_t r[64];  // two loads in flight per wait
             ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c8 * 64, r);
             ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c8 * 64 + 32, r + 32);
@@ -395,6 +414,7 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
           ptx::tc_fence_after();
 #pragma unroll
           for (int c4 = 0; c4 < 4; ++c4) {
+            if (half * 128 + c4 * 32 >= 64 * f.nb) break;  // not multiplied: past N
             uint32_t r[32];
             ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c4 * 32, r);
             ptx::tmem_ld_wait();
@@ -708,7 +728,8 @@ int oz_grun_gemm(const OzGBucket& b, const OzPlan& shape, int mode, int nitems, 
   }
   int st_;
   if ((st_ = make_tmap(&a.tmA, ap, b.Kp, b.Mtot, apl, OZ_BM))) return st_;
-  if ((st_ = make_tmap(&a.tmB, bp, b.Kp, b.Ntot, bpl, OZ_BN))) return st_;
+  if ((st_ = make_tmap(&a.tmB, bp, b.Kp, b.Ntot, bpl, 64))) return st_;
+  a.bsub = 1;
   a.Kp = b.Kp;
   a.mode = mode;
   a.P = b.P;

@@ -37,6 +37,7 @@ with the same methods gives the CPU pipeline.
 from __future__ import annotations
 
 import time
+import os
 from dataclasses import dataclass, field
 from fractions import Fraction
 
@@ -99,19 +100,12 @@ def _frac_up(fr: Fraction) -> float:
     return float(np.nextafter(f, np.inf)) if Fraction(f) < fr else f
 
 
-def stiffness(M: int, ia: np.ndarray, ib: np.ndarray):
-    """DL = ((grad phi_r, grad phi_s))_{r,s} for the basis list (ia, ib):
-    D1 (x) L1 + L1 (x) D1 evaluated exactly, rounded outward.  Returns
-    (lo, hi, mid) n x n arrays (mid = nearest double).  Only |a - c| and
-    |b - d| in {0, 2} give non-zero entries (L1 is pentadiagonal with a zero
-    first off-diagonal, D1 diagonal), so each row visits nine neighbours."""
+def _stiffness_entries(M: int, ia: np.ndarray, ib: np.ndarray):
+    """The non-zero entries of DL: (rows, cols, lo, hi, mid)."""
     L1, D1 = _one_dim(M)
-    n = ia.size
     where = {(int(a), int(b)): r for r, (a, b) in enumerate(zip(ia, ib))}
-    lo = np.zeros((n, n))
-    hi = np.zeros((n, n))
-    mid = np.zeros((n, n))
-    for r in range(n):
+    rows, cols, lo, hi, mid = [], [], [], [], []
+    for r in range(ia.size):
         a, b = int(ia[r]), int(ib[r])
         for c in (a - 2, a, a + 2):
             for d in (b - 2, b, b + 2):
@@ -120,7 +114,49 @@ def stiffness(M: int, ia: np.ndarray, ib: np.ndarray):
                     continue
                 v = (D1[a] if a == c else 0) * L1[b][d] + L1[a][c] * (D1[b] if b == d else 0)
                 if v != 0:
-                    lo[r, s], hi[r, s], mid[r, s] = _frac_down(v), _frac_up(v), float(v)
+                    rows.append(r)
+                    cols.append(s)
+                    lo.append(_frac_down(v))
+                    hi.append(_frac_up(v))
+                    mid.append(float(v))
+    return (np.array(rows, dtype=np.int64), np.array(cols, dtype=np.int64), np.array(lo),
+            np.array(hi), np.array(mid))
+
+
+def stiffness(M: int, ia: np.ndarray, ib: np.ndarray, use_cache: bool = True):
+    """DL = ((grad phi_r, grad phi_s))_{r,s} for the basis list (ia, ib):
+    D1 (x) L1 + L1 (x) D1 evaluated exactly, rounded outward.  Returns
+    (lo, hi, mid) n x n arrays (mid = nearest double).  Only |a - c| and
+    |b - d| in {0, 2} give non-zero entries (L1 is pentadiagonal with a zero
+    first off-diagonal, D1 diagonal), so each row visits nine neighbours.
+    For the even list of M the non-zero entries are cached beside the
+    Legendre tables (they depend on M alone)."""
+    n = ia.size
+    ea, eb = even_list(M)
+    path = None
+    if use_cache and np.array_equal(ia, ea) and np.array_equal(ib, eb):
+        path = legendre._CACHE / f"stiffness_even_M{M}_v1.npz"
+    ent = None
+    if path is not None and path.exists():
+        with np.load(path) as z:
+            ent = tuple(z[k] for k in ("rows", "cols", "lo", "hi", "mid"))
+    if ent is None:
+        ent = _stiffness_entries(M, ia, ib)
+        if path is not None:
+            try:
+                path.parent.mkdir(parents=True, exist_ok=True)
+                tmp = path.with_suffix(".tmp.npz")
+                np.savez(tmp, **dict(zip(("rows", "cols", "lo", "hi", "mid"), ent)))
+                os.replace(tmp, path)
+            except OSError:
+                pass
+    rows, cols, elo, ehi, emid = ent
+    lo = np.zeros((n, n))
+    hi = np.zeros((n, n))
+    mid = np.zeros((n, n))
+    lo[rows, cols] = elo
+    hi[rows, cols] = ehi
+    mid[rows, cols] = emid
     return lo, hi, mid
 
 
