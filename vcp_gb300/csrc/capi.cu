@@ -16,12 +16,13 @@ namespace {
 
 // Non-blocking streams per (host thread, device) for the host-pointer entry
 // points, so they do not serialise with unrelated work: 0 computes, 1 and 2
-// carry the host->device and device->host copies of a pipelined product.
+// carry the host->device and device->host copies of a pipelined product, 3
+// and 4 its block products.
 cudaStream_t host_stream(int which = 0) {
-  thread_local cudaStream_t streams[64][3] = {};
+  thread_local cudaStream_t streams[64][5] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64 || which < 0 || which > 2) return nullptr;
+  if (dev < 0 || dev >= 64 || which < 0 || which > 4) return nullptr;
   if (!streams[dev][which]) cudaStreamCreateWithFlags(&streams[dev][which], cudaStreamNonBlocking);
   return streams[dev][which];
 }
@@ -447,7 +448,8 @@ int vcpcu_igemm(int m, int n, int k, const double* A, const double* B, double* C
   const int panels = host_panels(n), row_panels = host_row_panels(m, n);
   if (resolved == VCPCU_FORM_OZAKI && panels * row_panels > 1) {
     st = ozaki_igemm_host_pipelined(m, n, k, A, B, C, slices, panels, row_panels, s,
-                                    host_stream(1), host_stream(2));
+                                    host_stream(3), host_stream(4), host_stream(1),
+                                    host_stream(2));
     if (st) return st;
     return take_status();
   }

@@ -428,8 +428,9 @@ __global__ void oz_fill_nan(size_t count, double* C) {
 // device memory goes back to the pool (also on error paths).
 struct PipeGuard {
   std::vector<cudaEvent_t> ev;
-  cudaStream_t streams[3];
-  explicit PipeGuard(cudaStream_t a, cudaStream_t b, cudaStream_t c) : streams{a, b, c} {}
+  cudaStream_t streams[5];
+  PipeGuard(cudaStream_t a, cudaStream_t b, cudaStream_t c, cudaStream_t d, cudaStream_t e)
+      : streams{a, b, c, d, e} {}
   cudaEvent_t make() {
     cudaEvent_t e = nullptr;
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
@@ -475,7 +476,8 @@ std::vector<int> block_bounds(int len, int parts, int unit) {
 
 int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const double* B, double* C,
                                int slices, int panels, int row_panels, cudaStream_t s,
-                               cudaStream_t up, cudaStream_t down) {
+                               cudaStream_t c0, cudaStream_t c1, cudaStream_t up,
+                               cudaStream_t down) {
   const int nslices = slices > 0 ? slices : 8;
   if (k > (1 << 20)) {
     set_error("igemm (Ozaki form): inner dimension %d above the supported 2^20", k);
@@ -494,20 +496,51 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
                          cb = block_bounds(n, panels, OZ_BN);
   row_panels = (int)rb.size() - 1;
   panels = (int)cb.size() - 1;
+  // residue bytes and radius folds of one block product (as laid out by
+  // oz_carve_workspace for its plan): the whole product's buffers serve the
+  // products on c0, a second pair sized for the largest block those on c1
+  auto blk_res = [&](int mv, int wj) {
+    const size_t Mp = (size_t)(mv + OZ_BM - 1) / OZ_BM * OZ_BM,
+                 Np = (size_t)(wj + OZ_BN - 1) / OZ_BN * OZ_BN;
+    return al256((size_t)pb.L * Np * Mp);
+  };
+  auto blk_P = [&](int mv, int wj) {
+    const size_t Mp = (size_t)(mv + OZ_BM - 1) / OZ_BM * OZ_BM,
+                 Np = (size_t)(wj + OZ_BN - 1) / OZ_BN * OZ_BN;
+    return al256(sizeof(int32_t) * 2 * (size_t)plan.rad_slots * Mp * Np);
+  };
+  size_t res1 = 0, P1 = 0;  // the largest block of each shape the loop below makes
+  for (int t = 0; t < row_panels || t < panels; ++t) {
+    const int nj = t < panels ? t : panels, ni = t + 1 < row_panels ? t + 1 : row_panels;
+    if (t < row_panels)
+      for (int J = 0; J < nj; ++J) {  // row block t against columns [0, nj) or one block
+        res1 = std::max(res1, blk_res(rb[t + 1] - rb[t], cb[nj] - cb[0]));
+        P1 = std::max(P1, blk_P(rb[t + 1] - rb[t], cb[nj] - cb[0]));
+      }
+    if (t < panels) {
+      res1 = std::max(res1, blk_res(rb[ni] - rb[0], cb[t + 1] - cb[t]));
+      P1 = std::max(P1, blk_P(rb[ni] - rb[0], cb[t + 1] - cb[t]));
+    }
+  }
   const size_t na = 2 * (size_t)m * k, nbe = 2 * (size_t)k * n, nc = 2 * (size_t)m * n;
   const size_t off_b = al256(na * 8), off_c = off_b + al256(nbe * 8),
-               off_w = off_c + al256(nc * 8);
+               off_w = off_c + al256(nc * 8), off_r1 = off_w + al256(oz_workspace_bytes(pb)),
+               off_p1 = off_r1 + res1;
   Scratch buf;
-  int st = buf.alloc(off_w + oz_workspace_bytes(pb), s);
+  int st = buf.alloc(off_p1 + P1, s);
   if (st) return st;
-  PipeGuard g(s, up, down);  // destroyed before buf: drains every stream first
+  PipeGuard g(s, c0, c1, up, down);  // destroyed before buf: drains every stream first
   double* dA = (double*)buf.ptr;
   double* dB = (double*)((uint8_t*)buf.ptr + off_b);
   double* dC = (double*)((uint8_t*)buf.ptr + off_c);
   OzWorkspace ws;
   oz_carve_workspace(pb, (uint8_t*)buf.ptr + off_w, &ws);
-  // the copy streams may touch the memory only after its allocation on s
-  if ((st = pipe_event(g, s, up)) || (st = pipe_event(g, s, down))) return st;
+  uint8_t* res1p = (uint8_t*)buf.ptr + off_r1;
+  int32_t* P1p = (int32_t*)((uint8_t*)buf.ptr + off_p1);
+  // the other streams may touch the memory only after its allocation on s
+  if ((st = pipe_event(g, s, up)) || (st = pipe_event(g, s, down)) ||
+      (st = pipe_event(g, s, c0)) || (st = pipe_event(g, s, c1)))
+    return st;
   if ((st = oz_prepare_left_begin(pb, ws, s))) return st;
 
   // uploads, interleaved: A's row block t, then B's column block t
@@ -534,8 +567,11 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
   }
 
   // the part of C over row blocks [I0, I1) and column blocks [J0, J1): its
-  // slice GEMMs on views of the whole planes, its reassembly, its download
+  // slice GEMMs on views of the whole planes, its reassembly, its download;
+  // products alternate between c0 and c1, each after the preparations
+  // issued on s so far (those of its operand blocks)
   long long flops = 0;
+  int nblk = 0;
   auto block = [&](int I0, int I1, int J0, int J1) -> int {
     const int i0 = rb[I0], mv = rb[I1] - rb[I0];
     const int j0 = cb[J0], wj = cb[J1] - cb[J0];
@@ -558,11 +594,18 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
     v.asum = ws.asum + 2 * (size_t)i0;
     v.F2 = ws.F2 + 2 * (size_t)j0;
     v.beta = ws.beta + j0;
+    const bool odd = (nblk++ & 1) != 0;
+    cudaStream_t c = odd ? c1 : c0;
+    if (odd) {
+      v.res = res1p;
+      v.P = P1p;
+    }
     int e;
-    if ((e = oz_run_gemm(pj, OZ_ALL, v, nullptr, 0, s))) return e;
+    if ((e = pipe_event(g, s, c))) return e;
+    if ((e = oz_run_gemm(pj, OZ_ALL, v, nullptr, 0, c))) return e;
     double* cblk = dC + 2 * ((size_t)i0 + (size_t)j0 * m);
-    if ((e = oz_crt_assemble(pj, v, cblk, m, s))) return e;
-    if ((e = pipe_event(g, s, down))) return e;
+    if ((e = oz_crt_assemble(pj, v, cblk, m, c))) return e;
+    if ((e = pipe_event(g, c, down))) return e;
     VCPCU_CUDA_TRY(cudaMemcpy2DAsync(C + 2 * ((size_t)i0 + (size_t)j0 * m), m * rowb, cblk,
                                      m * rowb, mv * rowb, wj, cudaMemcpyDeviceToHost, down));
     flops += 2LL * mv * wj * (long long)k * (pj.pb.L + 2LL * pj.rad.npairs);
@@ -603,6 +646,7 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
     }
   }
   oz_profile_add_flops(flops);
+  if ((st = pipe_event(g, c0, s)) || (st = pipe_event(g, c1, s))) return st;
   oz_merge_status(ws.flag, s);
   // A non-finite entry seen late leaves earlier blocks finite; the whole
   // result is NaN then, as in the one-shot product.

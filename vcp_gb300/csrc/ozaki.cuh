@@ -294,12 +294,15 @@ void oz_group_free(OzGroupPlan* g, cudaStream_t s);
 // row_panels x panels blocks; A goes up in row blocks and B in column
 // blocks, interleaved, and each block of C is multiplied, reassembled and
 // sent down as soon as its row block of A and column block of B are on the
-// device and prepared.  Streams: `s` computes, `up` / `down` copy.
-// Bit-identical to ozaki_igemm on the same operands (every entry depends on
-// its row of A and column of B only).  Synchronises before returning.
+// device and prepared.  Streams: `s` prepares the operand blocks, the block
+// products alternate between `c0` and `c1` (each with its own residue and
+// fold buffers), `up` / `down` copy.  Bit-identical to ozaki_igemm on the
+// same operands (every entry depends on its row of A and column of B only).
+// Synchronises before returning.
 int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const double* B, double* C,
                                int slices, int panels, int row_panels, cudaStream_t s,
-                               cudaStream_t up, cudaStream_t down);
+                               cudaStream_t c0, cudaStream_t c1, cudaStream_t up,
+                               cudaStream_t down);
 
 // point_mask as OzPlan::point_mask (the caller guarantees the zero radii).
 int ozaki_igemm(int m, int n, int k, const double* A, long lda, const double* B, long ldb,
