@@ -178,6 +178,20 @@ void oz_merge_status(const int* flag, cudaStream_t s) {
   count_launch();
 }
 
+int* oz_status_ptr() {
+  static std::mutex mu;
+  static int* ptr[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_oz_status) != cudaSuccess) return nullptr;
+    ptr[dev] = (int*)p;
+  }
+  return ptr[dev];
+}
+
 void oz_merge_status_n(const int* flag, int n, cudaStream_t s) {
   oz_status_merge_n<<<1, 256, 0, s>>>(flag, n);
   count_launch();

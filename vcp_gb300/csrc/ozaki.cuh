@@ -175,6 +175,9 @@ int oz_selftest_timeout(long long limit, cudaStream_t s);
 void oz_merge_status(const int* flag, cudaStream_t s);
 // ... of n products (status words 4 ints apart).
 void oz_merge_status_n(const int* flag, int n, cudaStream_t s);
+// Device address of the sticky status word of the current device (kernels
+// that merge statuses themselves atomicOr into it); null on error.
+int* oz_status_ptr();
 
 // dd GEMM (pddblas semantics) by the CRT form: C, Cerr as documented in
 // include/vcpcuda.h.  static_scratch != nullptr: use that device buffer of

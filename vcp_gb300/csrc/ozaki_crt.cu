@@ -286,16 +286,13 @@ __device__ __forceinline__ void quad_rows(int i0, int M, const int* __restrict__
 // time, the radius folds 16 bytes, C written as 4 consecutive pairs.  Only
 // the final error sum and the two outward roundings use the FP64 pipe on the
 // common path.  res and P point at row / column 0 of this product; plane =
-// Np Mp of its layout.
+// Np Mp of its layout; Fj, Frj the column's exponents, bj its beta.
 __device__ __forceinline__ void assemble_quad_col(
     const QuadRows& rw, int i0, int j, int M, int Mp, int L, int w,
-    const uint8_t* __restrict__ res, size_t plane, const int* __restrict__ F2,
-    const double* __restrict__ beta, const int32_t* __restrict__ P, double* __restrict__ C,
-    long ldc, bool nonfinite, const uint32_t (&Q)[16][4], const uint32_t (&Mm)[4], float invMf,
-    const OzRadConst& rc) {
+    const uint8_t* __restrict__ res, size_t plane, int Fj, int Frj, double bj,
+    const int32_t* __restrict__ P, double* __restrict__ C, long ldc, bool nonfinite,
+    const uint32_t (&Q)[16][4], const uint32_t (&Mm)[4], float invMf, const OzRadConst& rc) {
   const size_t e0 = (size_t)j * Mp + i0;
-  const int Fj = F2[2 * j], Frj = F2[2 * j + 1];
-  const double bj = beta[j];
   uint32_t pk[16];
 #pragma unroll
   for (int l = 0; l < 16; ++l)
@@ -345,8 +342,8 @@ oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __rest
   QuadRows rw;
   quad_rows(4 * q, M, E3, asum, rw);
   for (int j = blockIdx.y; j < N; j += gridDim.y)
-    assemble_quad_col(rw, 4 * q, j, M, Mp, L, w, res, plane, F2, beta, P, C, ldc, nonfinite,
-                      cc.Q, cc.M, cc.invMf, rc);
+    assemble_quad_col(rw, 4 * q, j, M, Mp, L, w, res, plane, F2[2 * j], F2[2 * j + 1], beta[j],
+                      P, C, ldc, nonfinite, cc.Q, cc.M, cc.invMf, rc);
 }
 
 // Grouped reassembly.  The problems of a bucket share one CRT plan (the
@@ -356,23 +353,24 @@ oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __rest
 // (NG = ceil(n / 8) column groups): its rows' exponents and sums are set up
 // once for about 8 columns, and consecutive threads take consecutive row
 // quads (coalesced residue and fold reads).  A block finds its problem with
-// one load (prob_asm); every block stamps the problem's end.  117
+// one load (prob_asm), stamps the problem's end and merges its status words
+// into the sticky status.  A device-wait timeout of the slice
+// GEMM (flag[1] of problem 0) poisons every output of the bucket.  117
 // registers: two blocks per SM (the problem's pointers and sizes stay in
 // registers where one product has them in the launch parameters; at 80
-// registers they spill).  A device-wait
-// timeout of the slice GEMM (flag[1] of problem 0) poisons every output of
-// the bucket.
+// registers they spill).
 __global__ void __launch_bounds__(256, 2)
 oz_crt_assemble_g(const __grid_constant__ OzGBucket b, const __grid_constant__ CrtConst cc,
-                  const __grid_constant__ OzRadConst rc) {
+                  const __grid_constant__ OzRadConst rc, int* __restrict__ status) {
   const int p = b.prob_asm[blockIdx.x];
   const OzGProb& q = b.probs[p];
   const int m = q.m, n = q.n;
   const int Mq = (m + 3) >> 2;
   const int NG = (n + 7) >> 3;
   const long u = (long)(blockIdx.x - b.blk_asm[p]) * blockDim.x + threadIdx.x;
+  const int f0 = b.flag[4 * p], f1 = b.flag[4 * p + 1];
   if (u < (long)Mq * NG) {
-    const bool nonfinite = b.flag[4 * p] != 0 || b.flag[1] != 0;
+    const bool nonfinite = f0 != 0 || b.flag[1] != 0;
     const int qd = (int)(u % Mq), cg = (int)(u / Mq);
     const int* E3 = b.E3 + 3 * (size_t)q.rowoff;
     const unsigned long long* asum = b.asum + 2 * (size_t)q.rowoff;
@@ -384,9 +382,10 @@ oz_crt_assemble_g(const __grid_constant__ OzGBucket b, const __grid_constant__ C
     QuadRows rw;
     quad_rows(4 * qd, m, E3, asum, rw);
     for (int j = cg; j < n; j += NG)
-      assemble_quad_col(rw, 4 * qd, j, m, q.Mp, q.L, q.w, res, plane, F2, beta, P, q.C, q.ldc,
-                        nonfinite, cc.Q, cc.M, cc.invMf, rc);
+      assemble_quad_col(rw, 4 * qd, j, m, q.Mp, q.L, q.w, res, plane, F2[2 * j], F2[2 * j + 1],
+                        beta[j], P, q.C, q.ldc, nonfinite, cc.Q, cc.M, cc.invMf, rc);
   }
+  if (threadIdx.x == 0 && (f0 | f1)) atomicOr(status, (f0 ? 1 : 0) | (f1 ? 2 : 0));
   if (b.t_last) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -433,7 +432,12 @@ int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long l
 int oz_gassemble(const OzGBucket& b, const OzPlan& shape, const OzRadConst& rc, int nblk,
                  cudaStream_t st) {
   if (nblk <= 0) return VCPCU_OK;
-  oz_crt_assemble_g<<<nblk, 256, 0, st>>>(b, crt_const(shape), rc);
+  int* status = oz_status_ptr();
+  if (!status) {
+    set_error("igemm_batched: no device address of the status word");
+    return VCPCU_ERR_CUDA;
+  }
+  oz_crt_assemble_g<<<nblk, 256, 0, st>>>(b, crt_const(shape), rc, status);
   VCPCU_LAUNCH_CHECK("oz_crt_assemble_g");
   return VCPCU_OK;
 }

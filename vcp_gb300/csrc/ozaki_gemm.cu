@@ -338,6 +338,30 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
       const int g0 = f.g0, g1 = f.g1;
       const int gi = f.tm * OZ_BM + row_in_tile;
       const int gj0 = f.tn * OZ_BN + half * 128;
+      if (args.mode != OZ_MID && f.tm * OZ_BM + quarter * 32 >= f.M) {
+        // this warp's 32 rows are all past M (padding of the tile): release
+        // each accumulator of the item unread -- the reassembly reads no
+        // padding row (midpoint folds keep every row)
+        for (int g = g0; g < g1 && ok; ++g) {
+          const int total = (args.gkind[g] == OZ_CRT && nchunks == 1)
+                                ? 1
+                                : (args.pl.gstart[g + 1] - args.pl.gstart[g]) * nchunks;
+          for (int idx = 0; idx < total; ++idx, ++acc) {
+            const int buf = acc & 1;
+            const uint32_t par = (acc >> 1) & 1;
+            if (*(volatile int*)&sm.abort || !ptx::mbar_wait(&sm.tfull[buf], par, lim)) {
+              if (!*(volatile int*)&sm.abort) raise_timeout(&sm, args.flag, 3);
+              ok = false;
+              break;
+            }
+            ptx::tc_fence_after();
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&sm.tempty[buf]);
+          }
+        }
+        continue;
+      }
       bool have_w = false;
       // radius groups: slot of the next fold = folds of the earlier groups
       // of the same product
@@ -412,14 +436,17 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
             break;
           }
           ptx::tc_fence_after();
+          // columns past N were not multiplied
+          const int ncb = (f.nb * 64 - half * 128) >> 5;
 #pragma unroll
           for (int c4 = 0; c4 < 4; ++c4) {
-            if (half * 128 + c4 * 32 >= 64 * f.nb) break;  // not multiplied: past N
-            uint32_t r[32];
-            ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c4 * 32, r);
-            ptx::tmem_ld_wait();
+            if (c4 < ncb) {
+              uint32_t r[32];
+              ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c4 * 32, r);
+              ptx::tmem_ld_wait();
 #pragma unroll
-            for (int e = 0; e < 32; ++e) c[c4 * 32 + e] += __float2int_rn(__uint_as_float(r[e]));
+              for (int e = 0; e < 32; ++e) c[c4 * 32 + e] += __float2int_rn(__uint_as_float(r[e]));
+            }
           }
           ptx::tc_fence_before();
           __syncwarp();
@@ -575,6 +602,37 @@ int num_sms() {
   return n;
 }
 
+// The radius products and the residue GEMMs in one launch: the A planes are
+// [residues (mpl) | |mA| + rA digits (sr) | rA digits (sr)] at one plane
+// stride, the B planes [residues | rB digits | |mB| digits]; the groups of
+// radius product 1, product 2 (each skipped for a point factor, point_mask
+// as OzPlan's) and the moduli, each tagged with its kind.
+void all_groups(const OzPairList& rad, const OzPairList& crt, int mpl, int sr, int point_mask,
+                OzGemmArgs& a) {
+  OzPairList& m = a.pl;
+  int ng = 0, np = 0;
+  auto add = [&](const OzPairList& src, int offA, int offB, int kind) {
+    for (int g = 0; g < src.ngroups; ++g) {
+      m.gstart[ng] = (int16_t)np;
+      m.gt[ng] = src.gt[g];
+      a.gkind[ng] = (int8_t)kind;
+      a.gres[ng] = (int8_t)(kind == OZ_CRT ? g : 0);
+      if (kind == OZ_CRT) a.moduli[ng] = OZ_MODULI[g];
+      for (int q = src.gstart[g]; q < src.gstart[g + 1]; ++q, ++np) {
+        m.pa[np] = (int8_t)(src.pa[q] + offA);
+        m.pb[np] = (int8_t)(src.pb[q] + offB);
+      }
+      ++ng;
+    }
+  };
+  if (!(point_mask & 2)) add(rad, mpl, mpl, OZ_RAD_SET);
+  if (!(point_mask & 1)) add(rad, mpl + sr, mpl + sr, OZ_RAD_ADD);
+  add(crt, 0, 0, OZ_CRT);
+  m.gstart[ng] = (int16_t)np;
+  m.ngroups = ng;
+  m.npairs = np;
+}
+
 }  // namespace
 
 size_t oz_dyn_smem() { return (size_t)OZ_STAGES * STAGE_BYTES + 1024; }
@@ -625,36 +683,12 @@ int oz_run_gemm(const OzPlan& plan, int mode, const OzWorkspace& ws, double* C, 
     a.Erow = ws.E3 + 2; a.Fcol = ws.F2 + 0;
     a.pl = plan.rad; a.t_ref = plan.t_ref_rad; a.R = plan.R_rad;
   } else if (mode == OZ_ALL) {
-    // the radius products and the residue GEMMs together: the A planes are
-    // [residues (mplanes) | |mA| + rA digits (sr) | rA digits (sr)] at one
-    // plane stride, the B planes [residues | rB digits | |mB| digits]
     ap = ws.a_mid; bp = ws.b_mid;
     apl = bpl = pb.mplanes + 2 * pb.sr;
     a.Erow = ws.E3 + 0; a.Fcol = ws.F2 + 0;
     a.t_ref = plan.t_ref_rad; a.R = plan.R_rad;
     a.res = ws.res;
-    OzPairList& m = a.pl;
-    int ng = 0, np = 0;
-    auto add = [&](const OzPairList& src, int offA, int offB, int kind) {
-      for (int g = 0; g < src.ngroups; ++g) {
-        m.gstart[ng] = (int16_t)np;
-        m.gt[ng] = src.gt[g];
-        a.gkind[ng] = (int8_t)kind;
-        a.gres[ng] = (int8_t)(kind == OZ_CRT ? g : 0);
-        if (kind == OZ_CRT) a.moduli[ng] = OZ_MODULI[g];
-        for (int q = src.gstart[g]; q < src.gstart[g + 1]; ++q, ++np) {
-          m.pa[np] = (int8_t)(src.pa[q] + offA);
-          m.pb[np] = (int8_t)(src.pb[q] + offB);
-        }
-        ++ng;
-      }
-    };
-    if (!(plan.point_mask & 2)) add(plan.rad, pb.mplanes, pb.mplanes, OZ_RAD_SET);
-    if (!(plan.point_mask & 1)) add(plan.rad, pb.mplanes + pb.sr, pb.mplanes + pb.sr, OZ_RAD_ADD);
-    add(plan.crt, 0, 0, OZ_CRT);
-    m.gstart[ng] = (int16_t)np;
-    m.ngroups = ng;
-    m.npairs = np;
+    all_groups(plan.rad, plan.crt, pb.mplanes, pb.sr, plan.point_mask, a);
   } else {  // OZ_CRT: residue products, one modulus per group
     ap = ws.a_mid; bp = ws.b_mid; apl = pb.L; bpl = pb.L;
     a.Erow = ws.E3 + 0; a.Fcol = ws.F2 + 0;

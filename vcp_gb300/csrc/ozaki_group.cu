@@ -35,14 +35,6 @@ namespace {
 
 size_t al256g(size_t x) { return (x + 255) & ~(size_t)255; }
 
-__global__ void g_init_stamps(const OzGProb* probs, int n, unsigned long long* t_first,
-                              unsigned long long* t_last) {
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-    t_first[probs[p].orig] = ~0ULL;
-    t_last[probs[p].orig] = 0ULL;
-  }
-}
-
 struct BucketHost {
   OzGBucket dev;  // table pointers set at plan time, workspace pointers at record time
   OzPlan shape;   // radius pair list, Lmax-modulus pair list, fold count
@@ -355,11 +347,8 @@ int record_chunk(const BucketHost& b, uint8_t* ws, unsigned long long* t_first,
   d.P = (int32_t*)(ws + b.offP);
   d.t_first = t_first;
   d.t_last = t_last;
+  // (the caller resets every problem's stamps once per batch)
   VCPCU_CUDA_TRY(cudaMemsetAsync(ws, 0, b.zero_bytes, s));
-  if (t_first && t_last) {
-    g_init_stamps<<<(d.nprob + 255) / 256, 256, 0, s>>>(d.probs, d.nprob, t_first, t_last);
-    VCPCU_LAUNCH_CHECK("g_init_stamps");
-  }
   int st;
   {
     PhaseTimer t(0, s);
@@ -378,11 +367,9 @@ int record_chunk(const BucketHost& b, uint8_t* ws, unsigned long long* t_first,
     if ((st = oz_grun_gemm(d, b.shape, OZ_CRT, b.nitem_crt, s))) return st;
   }
   {
-    PhaseTimer t(4, s);
+    PhaseTimer t(4, s);  // the reassembly also merges the chunk's status words
     if ((st = oz_gassemble(d, b.shape, b.rc, b.nblk_asm, s))) return st;
   }
-  oz_merge_status_n(d.flag, d.nprob, s);
-  VCPCU_LAUNCH_CHECK("oz_status_merge_n");
   return VCPCU_OK;
 }
 }  // namespace

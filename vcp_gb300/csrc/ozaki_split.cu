@@ -477,24 +477,40 @@ struct TileStore {
 // X = mA and rA are the stored midrad planes (ld ldx).  Planes rows are
 // rowbase + i (stacked problems), pstride elements apart; E3 and asum point
 // at row 0 of this problem.
+// rowmax != null (grouped products): the exponents come from the row maxima
+// here, and the blocks of the first k range store them in E3 for the
+// reassembly (no separate exponent pass); else they are read from E3.
 template <int SR, int NL>
 __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K, int Kp,
                                                     size_t pstride, int rowbase,
                                                     const double* __restrict__ X,
                                                     const double* __restrict__ rA, long ldx,
-                                                    int L, int w, const int* __restrict__ E3,
+                                                    int L, int w, int* __restrict__ E3,
                                                     uint16_t* __restrict__ planes_m,
                                                     uint16_t* __restrict__ planes_p,
                                                     uint16_t* __restrict__ planes_r,
-                                                    unsigned long long* __restrict__ asum) {
+                                                    unsigned long long* __restrict__ asum,
+                                                    const unsigned long long* __restrict__ rowmax =
+                                                        nullptr) {
   const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
   const int i = by * 32 + lane;
   const int k0 = bx * 64 + wq * 8;
   int Em = OZ_ZERO_EXP, Ep = OZ_ZERO_EXP, Er = OZ_ZERO_EXP;
   if (i < M) {
-    Em = E3[3 * i + 0];
-    Ep = E3[3 * i + 1];
-    Er = E3[3 * i + 2];
+    if (rowmax) {
+      Em = oz_exponent(__longlong_as_double((long long)rowmax[3 * i + 0]));
+      Ep = oz_exponent(__longlong_as_double((long long)rowmax[3 * i + 1]));
+      Er = oz_exponent(__longlong_as_double((long long)rowmax[3 * i + 2]));
+      if (bx == 0 && wq == 0) {
+        E3[3 * i + 0] = Em;
+        E3[3 * i + 1] = Ep;
+        E3[3 * i + 2] = Er;
+      }
+    } else {
+      Em = E3[3 * i + 0];
+      Ep = E3[3 * i + 1];
+      Er = E3[3 * i + 2];
+    }
   }
   __shared__ uint4 tile_smem[2][32][9];
   TileStore ts{tile_smem, 0};
@@ -578,11 +594,11 @@ template <int SR, int NL>
 __global__ void __launch_bounds__(256, 4)
 oz_split_left_crt(int M, int K, int Kp, size_t pstride, int rowbase,
                   const double* __restrict__ mA, const double* __restrict__ rA, long ldx, int L,
-                  int w, const int* __restrict__ E3, uint16_t* __restrict__ planes_m,
+                  int w, int* __restrict__ E3, uint16_t* __restrict__ planes_m,
                   uint16_t* __restrict__ planes_p, uint16_t* __restrict__ planes_r,
                   unsigned long long* __restrict__ asum) {
-  split_left_crt_body<SR, NL>(blockIdx.x, blockIdx.y, M, K, Kp, pstride, rowbase, mA, rA,
-                                     ldx, L, w, E3, planes_m, planes_p, planes_r, asum);
+  split_left_crt_body<SR, NL>(blockIdx.x, blockIdx.y, M, K, Kp, pstride, rowbase, mA, rA, ldx,
+                              L, w, E3, planes_m, planes_p, planes_r, asum);
 }
 
 // ---------------------------------------------------------- grouped products
@@ -662,11 +678,11 @@ __global__ void __launch_bounds__(256, 3) oz_split_left_crt_g(const __grid_const
   const int local = blockIdx.x - b.blk_split[p];
   const size_t pstride = (size_t)b.Mtot * b.Kp;
   split_left_crt_body<2, NL>(local % nbx, local / nbx, q.m, q.k, b.Kp, pstride, q.rowoff,
-                                    b.midA + q.rowoff, b.radA + q.rowoff, b.Mtot, q.L, q.w,
-                                    b.E3 + 3 * (size_t)q.rowoff,
-                                   b.planesA, b.planesA + (size_t)b.Lmax * pstride,
-                                   b.planesA + (size_t)(b.Lmax + 2) * pstride,
-                                   b.asum + 2 * (size_t)q.rowoff);
+                             b.midA + q.rowoff, b.radA + q.rowoff, b.Mtot, q.L, q.w,
+                             b.E3 + 3 * (size_t)q.rowoff, b.planesA,
+                             b.planesA + (size_t)b.Lmax * pstride,
+                             b.planesA + (size_t)(b.Lmax + 2) * pstride,
+                             b.asum + 2 * (size_t)q.rowoff, b.rowmax + 3 * (size_t)q.rowoff);
 }
 
 // Warp reductions of 64-bit maxima and sums.
@@ -843,8 +859,6 @@ int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, int wmax, cuda
     oz_rowmax_left_g<<<nblk_rowmax, 256, 0, st>>>(b);
     VCPCU_LAUNCH_CHECK("oz_rowmax_left_g");
   }
-  oz_exponents<<<(b.Mtot + 255) / 256, 256, 0, st>>>(b.Mtot, b.rowmax, 3, b.E3);
-  VCPCU_LAUNCH_CHECK("oz_exponents");
   // |A'|, |B'| <= 2^(w-1): four 14-bit limbs up to w = 56, six 12-bit limbs
   // up to w = 73; lanes of the right split take 2, 4 or 8 consecutive k so
   // that short columns keep the warp busy
@@ -872,6 +886,7 @@ int oz_gprep(const OzGBucket& b, int nblk_rowmax, int nblk_split, int wmax, cuda
   }
 #undef OZ_GRIGHT
   VCPCU_LAUNCH_CHECK("oz_split_right2_g");
+  // (the exponents of the left factor come from its split)
   oz_beta_right_g<<<(b.Ntot + 255) / 256, 256, 0, st>>>(b);
   VCPCU_LAUNCH_CHECK("oz_beta_right_g");
   return VCPCU_OK;
@@ -1086,7 +1101,7 @@ int split_left_rows(const OzProblem& pb, int i0, int rows, OzWorkspace& ws, cuda
   dim3 g2(pb.Kp / 64, rows / 32);
   const double* mA = ws.midA + i0;
   const double* rA = ws.radA + i0;
-  const int* E3 = ws.E3 + 3 * (size_t)i0;
+  int* E3 = ws.E3 + 3 * (size_t)i0;
   unsigned long long* asum = ws.asum + 2 * (size_t)i0;
   // |A'| <= 2^(w-1): four 14-bit limbs up to w = 56, five 12-bit limbs up to
   // w = 61, six up to 73
