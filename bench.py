@@ -1097,14 +1097,14 @@ def bench_also(dev, stream):
     out = {}
     for key, fn in (("autotune", lambda: pidcuda.autotune(stream)),
                     ("batch", lambda: bench_batch(dev, stream, steps=1)),
-                    ("dd", lambda: [bench_dd(dev, stream, 2048, phi, steps=2, cpu_rows=64)
-                                    for phi in (0, 16)]),
+                    ("dd", lambda: [bench_dd(dev, stream, 8192, 0, steps=2, cpu_rows=16),
+                                    bench_dd(dev, stream, 8192, 16, steps=2, cpu_rows=0)]),
                     ("cfg1", lambda: bench_cfg1(dev, stream)),
-                    ("lss", lambda: bench_lss(dev, stream, 2048, 1, steps=3)),
-                    ("eig", lambda: bench_eig(dev, stream, 1024, steps=3)),
-                    ("point", lambda: bench_point(dev, stream, 4096, 4096, 4096, 0, [6, 8],
+                    ("lss", lambda: bench_lss(dev, stream, 8192, 1, steps=3)),
+                    ("eig", lambda: bench_eig(dev, stream, 2048, steps=3)),
+                    ("point", lambda: bench_point(dev, stream, 8192, 8192, 8192, 0, [6, 8],
                                                   steps=2)),
-                    ("emden", lambda: bench_emden(dev, (30,), (30,)))):
+                    ("emden", lambda: bench_emden(dev, (30, 50), (30,)))):
         t0 = time.perf_counter()
         try:
             out[key] = fn()
@@ -1112,6 +1112,8 @@ def bench_also(dev, stream):
             out[key] = {"error": f"{type(e).__name__}: {e}"}
         if isinstance(out[key], dict):
             out[key]["wall_s"] = time.perf_counter() - t0
+        elif isinstance(out[key], list):
+            out[key] = {"cases": out[key], "wall_s": time.perf_counter() - t0}
     return out
 
 
