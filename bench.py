@@ -127,7 +127,10 @@ def max_over_ranks(x: float, ws: int, device=None) -> float:
 
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms during timing."""
+    """nvidia-smi clocks/throttle reasons sampled every 100 ms during timing.
+    The sampler is started, and its first (idle) sample read and dropped,
+    before the timed region begins, so that every kept sample falls inside
+    it."""
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -137,11 +140,15 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
+        import select
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            ready, _, _ = select.select([self.proc.stdout], [], [], 5.0)
+            if ready:
+                self.proc.stdout.readline()  # the sample before the timed region
         except Exception:
             self.proc = None
         return self
