@@ -21,7 +21,10 @@
  *    ozaki_acc (vcp/pddblas.hpp:160-193: t ascending, p ascending);
  *  - reassembly: [RD(W u) - e, RU((W + R) u) + e] with u = 2^(E + F - 8 t_ref),
  *    e = RU(trunc + T), trunc = 2^(E-8s) RU(RU(0.515625 delta) 2^(F-8) +
- *    RU(beta/2)), T = RU(RU((W'+R') u') + RU((W''+R'') u'')).
+ *    RU(beta/2)), T = RU(RU((S'+R') u') + RU((S''+R'') u''));
+ *  - radius products: each fold is stored as the float RU(C) of its exact
+ *    chunk sum and S = RU(fold 2^sh + S) in fp32 over the folds in order
+ *    (an upper bound of the exact W; the GPU's single-rounding FMA chain).
  */
 #include <fenv.h>
 #include <math.h>
@@ -238,6 +241,15 @@ static void choose_scaling(const pairlist* pl, int nchunks, int* t_ref, int* R) 
 }
 
 static long long shift_t(long long c, int sh) { return sh >= 0 ? (c << sh) : (c >> (-sh)); }
+
+/* RU(v) as a float for an integer |v| < 2^62 (the rounding mode is nearest
+   here): the nearest float, moved up one unit if it lies below v (the
+   comparison is exact: the float is an integer). */
+static float i64_to_float_ru(long long v) {
+  float f = (float)v;
+  if ((long long)f < v) f = nextafterf(f, INFINITY);
+  return f;
+}
 
 /* CRT form: integer bits w per operand for precision parameter s (w = 7 s,
  * lowered while 16 moduli cannot hold K 2^(2w-1)); the moduli are those of
@@ -458,6 +470,7 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
       const int trefs[3] = {trr, trr, tm};
       const int16_t* as[3] = {dAp, dAr, dAm};
       const int16_t* bs[3] = {dBr, dBs, dBm};
+      float Sr[2] = {0.0f, 0.0f}; /* radius products: fp32 upward sums of the folds */
       for (int w = 0; w < 3; ++w) {
         const pairlist* pl = pls[w];
         long long acc = 0;
@@ -476,9 +489,17 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
               C += s32;
               ++cnt;
               if (cnt == OZ_FOLD || idx == total - 1) {
-                long long v = shift_t(C, sh);
-                acc = have ? acc + v : v;
-                have = 1;
+                if (w < 2) {
+                  /* the slice GEMM stores RU(float(C)); the reassembly forms
+                     S = RU(fold 2^sh + S) (sh >= 0: exact integers < 2^53
+                     before the one rounding) */
+                  const float fv = i64_to_float_ru(C);
+                  Sr[w] = i64_to_float_ru((long long)fv * (1LL << sh) + (long long)Sr[w]);
+                } else {
+                  long long v = shift_t(C, sh);
+                  acc = have ? acc + v : v;
+                  have = 1;
+                }
                 C = 0;
                 cnt = 0;
               }
@@ -487,14 +508,19 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
         }
         W[w] = acc;
       }
-      /* radius bound */
+      /* radius bound: RU((S + R) 2^ex) per product (S + R >= 0), RU sum */
       double T = 0.0;
       {
-        int z1 = Ep[i] == OZ_ZERO_EXP || Fr[j] == OZ_ZERO_EXP;
-        double b1 = z1 ? 0.0 : scale_dir(ll2d(W[0] + Rr, 1), Ep[i] + Fr[j] - 8 * trr, 1);
-        int z2 = Er[i] == OZ_ZERO_EXP || Fm[j] == OZ_ZERO_EXP;
-        double b2 = z2 ? 0.0 : scale_dir(ll2d(W[1] + Rr, 1), Er[i] + Fm[j] - 8 * trr, 1);
-        T = add_dir(b1, b2, FE_UPWARD);
+        double bb[2] = {0.0, 0.0};
+        const int zz[2] = {Ep[i] == OZ_ZERO_EXP || Fr[j] == OZ_ZERO_EXP,
+                           Er[i] == OZ_ZERO_EXP || Fm[j] == OZ_ZERO_EXP};
+        const int ex[2] = {Ep[i] + Fr[j] - 8 * trr, Er[i] + Fm[j] - 8 * trr};
+        for (int w = 0; w < 2; ++w) {
+          if (zz[w]) continue;
+          const float sv = Rr ? i64_to_float_ru((long long)Sr[w] + Rr) : Sr[w];
+          if (sv > 0.0f) bb[w] = scale_dir((double)sv, ex[w], 1);
+        }
+        T = add_dir(bb[0], bb[1], FE_UPWARD);
       }
       double mlo = 0.0, mup = 0.0, tr = 0.0;
       int z = Em[i] == OZ_ZERO_EXP || Fm[j] == OZ_ZERO_EXP;
@@ -548,4 +574,4 @@ int orc_ozaki2_igemm(int m, int n, int k, const double* A, const double* B, doub
   return ozaki_model(m, n, k, A, B, Cout, s, sr, 1);
 }
 
-int orc_ozaki_model_version(void) { return 1; }
+int orc_ozaki_model_version(void) { return 2; }

@@ -176,49 +176,60 @@ __device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const uint32_t
   return neg;
 }
 
-// W of both radius products for 4 consecutive rows (e0 = j Mp + i0): the
-// sums of their folds, exact in int64 (every shift is >= 0).
+// The radius sums of both products for 4 consecutive rows (e0 = j Mp +
+// i0).  Every fold is the fp32 upward rounding of an exact int32 chunk sum
+// (written so by the slice GEMM), and S = RU(fold 2^sh + S) over the folds in
+// the order they were made: an upper bound of the exact W = sum fold 2^sh,
+// since every term and every partial sum is rounded up.  All values are
+// integers below 2^53 (folds < 2^31, sh <= 16, at most 64 folds), so the
+// single-rounding FMA is the only inexact step.
 __device__ __forceinline__ void rad_folds(const int32_t* __restrict__ P, size_t plane,
-                                          size_t e0, const OzRadConst& rc, long long (&W1)[4],
-                                          long long (&W2)[4]) {
+                                          size_t e0, const OzRadConst& rc, float (&S1)[4],
+                                          float (&S2)[4]) {
 #pragma unroll
-  for (int u = 0; u < 4; ++u) W1[u] = W2[u] = 0;
+  for (int u = 0; u < 4; ++u) S1[u] = S2[u] = 0.0f;
   for (int f = 0; f < rc.nslot; ++f) {
-    const int sh = rc.sh[f];  // >= 0: v 2^sh as a shift of the two's complement
+    const float sc = __int_as_float((127 + rc.sh[f]) << 23);  // 2^sh, 0 <= sh <= 16
     if (rc.run1) {
-      const int4 v = *reinterpret_cast<const int4*>(P + (size_t)f * plane + e0);
-      W1[0] += (long long)((unsigned long long)(long long)v.x << sh);
-      W1[1] += (long long)((unsigned long long)(long long)v.y << sh);
-      W1[2] += (long long)((unsigned long long)(long long)v.z << sh);
-      W1[3] += (long long)((unsigned long long)(long long)v.w << sh);
+      const float4 v = *reinterpret_cast<const float4*>(P + (size_t)f * plane + e0);
+      S1[0] = __fmaf_ru(v.x, sc, S1[0]);
+      S1[1] = __fmaf_ru(v.y, sc, S1[1]);
+      S1[2] = __fmaf_ru(v.z, sc, S1[2]);
+      S1[3] = __fmaf_ru(v.w, sc, S1[3]);
     }
     if (rc.run2) {
-      const int4 v = *reinterpret_cast<const int4*>(P + (size_t)(rc.nslot + f) * plane + e0);
-      W2[0] += (long long)((unsigned long long)(long long)v.x << sh);
-      W2[1] += (long long)((unsigned long long)(long long)v.y << sh);
-      W2[2] += (long long)((unsigned long long)(long long)v.z << sh);
-      W2[3] += (long long)((unsigned long long)(long long)v.w << sh);
+      const float4 v = *reinterpret_cast<const float4*>(P + (size_t)(rc.nslot + f) * plane + e0);
+      S2[0] = __fmaf_ru(v.x, sc, S2[0]);
+      S2[1] = __fmaf_ru(v.y, sc, S2[1]);
+      S2[2] = __fmaf_ru(v.z, sc, S2[2]);
+      S2[3] = __fmaf_ru(v.w, sc, S2[3]);
     }
   }
 }
 
-// RU((W + R) 2^ex), 0 for a zero row or column: what the radius epilogue of
-// one product writes.
-__device__ __forceinline__ double rad_term(long long W, bool zero, int ex, int R) {
-  double b = 0.0;
-  if (!zero && !sw_i64_scale_ru(W + R, ex, &b)) b = scale_dir2(__ll2double_ru(W + R), ex, true);
-  return b;
+// RU((S + R) 2^ex), 0 for a zero row or column.  S + R >= the exact W + R >=
+// 0 (the digits of both radius factors are upward, so every product of
+// their reconstructions is non-negative) and is 0 or an integer >= 1: a
+// normal float, whose double is built on the integer pipe.
+__device__ __forceinline__ double rad_term(float S, bool zero, int ex, int R) {
+  if (zero) return 0.0;
+  const float s = R ? __fadd_ru(S, (float)R) : S;
+  if (!(s > 0.0f)) return 0.0;
+  const unsigned u = __float_as_uint(s);
+  const double d = __longlong_as_double((long long)(((unsigned long long)((u >> 23) + 896) << 52) |
+                                                    ((unsigned long long)(u & 0x7fffffu) << 29)));
+  return scale_pow2(d, ex, true);
 }
 
 // T = RU(RU((|mA| + rA) rB) + RU(rA |mB|)) at (i, j), the products that ran.
-__device__ __forceinline__ double rad_T(long long W1, long long W2, int Ep, int Er, int Fm,
-                                        int Fr, const OzRadConst& rc) {
-  const double b1 = rc.run1 ? rad_term(W1, Ep == OZ_ZERO_EXP || Fr == OZ_ZERO_EXP,
+__device__ __forceinline__ double rad_T(float S1, float S2, int Ep, int Er, int Fm, int Fr,
+                                        const OzRadConst& rc) {
+  const double b1 = rc.run1 ? rad_term(S1, Ep == OZ_ZERO_EXP || Fr == OZ_ZERO_EXP,
                                        Ep + Fr - 8 * rc.t_ref, rc.R)
                             : 0.0;
   if (!rc.run2) return b1;
   const double b2 =
-      rad_term(W2, Er == OZ_ZERO_EXP || Fm == OZ_ZERO_EXP, Er + Fm - 8 * rc.t_ref, rc.R);
+      rad_term(S2, Er == OZ_ZERO_EXP || Fm == OZ_ZERO_EXP, Er + Fm - 8 * rc.t_ref, rc.R);
   return rc.run1 ? sw_add_ru_pos(b1, b2) : b2;
 }
 
@@ -233,7 +244,7 @@ oz_radius_T_kernel(int M, int N, int Mp, size_t plane, const int32_t* __restrict
        idx += (long)gridDim.x * blockDim.x) {
     const int i0 = 4 * (int)(idx % Mq), j = (int)(idx / Mq);
     const size_t e0 = (size_t)j * Mp + i0;
-    long long W1[4], W2[4];
+    float W1[4], W2[4];
     rad_folds(P, plane, e0, rc, W1, W2);
     const int Fm = F2[2 * j], Fr = F2[2 * j + 1];
 #pragma unroll
@@ -297,7 +308,7 @@ __device__ __forceinline__ void assemble_quad_col(
 #pragma unroll
   for (int l = 0; l < 16; ++l)
     pk[l] = l < L ? *reinterpret_cast<const uint32_t*>(res + (size_t)l * plane + e0) : 0u;
-  long long W1[4], W2[4];
+  float W1[4], W2[4];
   rad_folds(P, plane, e0, rc, W1, W2);
 #pragma unroll
   for (int u = 0; u < 4; ++u) {

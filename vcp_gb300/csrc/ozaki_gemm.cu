@@ -175,6 +175,15 @@ __device__ __forceinline__ ItemInfo item_info(const OzGemmArgs& a, int item, int
 // within 1/2 + 2.0000002/m of x/m: r = x - q m (one FMA, exact) is an
 // integer with |r| <= m/2 + 2, and adding m to a negative r gives [0, m)
 // (m >= 107).
+// RU(v) of an int32 v on the FP32 pipe: v = h 2^16 + l with h = v >> 16
+// (floor, |h| < 2^15) and 0 <= l < 2^16; both halves are exact floats (a
+// magic-number subtraction each) and one FMA rounds h 2^16 + l upward.
+__device__ __forceinline__ float int_to_float_ru(int v) {
+  const float hf = __fsub_rn(__int_as_float(0x4B400000 + (v >> 16)), 12582912.0f);
+  const float lf = __fsub_rn(__uint_as_float(0x4B000000u | ((unsigned)v & 0xffffu)), 8388608.0f);
+  return __fmaf_ru(hf, 65536.0f, lf);
+}
+
 __device__ __forceinline__ float rint_f(float x) {  // |x| < 2^22
   return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
 }
@@ -480,13 +489,14 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
             }
             cnt = 0;
           } else if ((cnt == OZ_FOLD_CHUNKS || last_of_group) && kind != OZ_MID) {
-            // radius groups: the fold is stored, never read back here -- the
-            // reassembly combines the slots (no load stalls the drain)
+            // radius groups: the fold is stored as a float rounded up (an
+            // upper bound of the exact int32 sum), never read back here --
+            // the reassembly sums the slots upward in fp32
             const int slot = (kind == OZ_RAD_ADD ? args.slot_add : 0) + fold;
             int32_t* pp = f.P + ((size_t)slot * f.Np + gj0) * f.Mp + gi;
 #pragma unroll
             for (int e = 0; e < 128; ++e) {
-              pp[(size_t)e * f.Mp] = c[e];
+              pp[(size_t)e * f.Mp] = __float_as_int(int_to_float_ru(c[e]));
               c[e] = 0;
             }
             ++fold;
