@@ -22,9 +22,10 @@
  *  - reassembly: [RD(W u) - e, RU((W + R) u) + e] with u = 2^(E + F - 8 t_ref),
  *    e = RU(trunc + T), trunc = 2^(E-8s) RU(RU(0.515625 delta) 2^(F-8) +
  *    RU(beta/2)), T = RU(RU((S'+R') u') + RU((S''+R'') u''));
- *  - radius products: each fold is stored as the float RU(C) of its exact
- *    chunk sum and S = RU(fold 2^sh + S) in fp32 over the folds in order
- *    (an upper bound of the exact W; the GPU's single-rounding FMA chain).
+ *  - radius products: S = RU(chunk 2^(8 (t_ref - t)) + S) in fp32 over the
+ *    digit pairs (t ascending, p ascending) and their exact chunk sums, in
+ *    order (an upper bound of the exact W; the slice GEMM epilogue's
+ *    single-rounding FMA chain, one fold per product and tile).
  */
 #include <fenv.h>
 #include <math.h>
@@ -486,20 +487,20 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
               int k0 = ch * OZ_CHUNK, k1 = k0 + OZ_CHUNK < Kp ? k0 + OZ_CHUNK : Kp;
               int s32 = 0;
               for (int kk = k0; kk < k1; ++kk) s32 += (int)a[kk] * (int)b[kk];
+              if (w < 2) {
+                /* radius products: S = RU(chunk 2^sh + S) over the pairs (t
+                   ascending, p ascending) and their chunks, in fp32 -- the
+                   slice GEMM's epilogue (sh >= 0: exact integers below 2^53
+                   before the one rounding) */
+                Sr[w] = i64_to_float_ru((long long)s32 * (1LL << sh) + (long long)Sr[w]);
+                continue;
+              }
               C += s32;
               ++cnt;
               if (cnt == OZ_FOLD || idx == total - 1) {
-                if (w < 2) {
-                  /* the slice GEMM stores RU(float(C)); the reassembly forms
-                     S = RU(fold 2^sh + S) (sh >= 0: exact integers < 2^53
-                     before the one rounding) */
-                  const float fv = i64_to_float_ru(C);
-                  Sr[w] = i64_to_float_ru((long long)fv * (1LL << sh) + (long long)Sr[w]);
-                } else {
-                  long long v = shift_t(C, sh);
-                  acc = have ? acc + v : v;
-                  have = 1;
-                }
+                long long v = shift_t(C, sh);
+                acc = have ? acc + v : v;
+                have = 1;
                 C = 0;
                 cnt = 0;
               }
@@ -574,4 +575,4 @@ int orc_ozaki2_igemm(int m, int n, int k, const double* A, const double* B, doub
   return ozaki_model(m, n, k, A, B, Cout, s, sr, 1);
 }
 
-int orc_ozaki_model_version(void) { return 2; }
+int orc_ozaki_model_version(void) { return 3; }

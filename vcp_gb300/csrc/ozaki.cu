@@ -36,6 +36,7 @@ void build_pairs(int sa, int sb, bool triangular, OzPairList* pl) {
       if (p > sa || q > sb) continue;
       pl->pa[n] = (int8_t)(p - 1);
       pl->pb[n] = (int8_t)(q - 1);
+      pl->pt[n] = (int8_t)t;
       ++n;
     }
     if (n > start) {
@@ -47,6 +48,16 @@ void build_pairs(int sa, int sb, bool triangular, OzPairList* pl) {
   pl->gstart[g] = (int16_t)n;
   pl->npairs = n;
   pl->ngroups = g;
+}
+
+// The radius products' pairs: all sr x sr digit pairs in one group (t
+// ascending, p ascending), each pair weighted by 2^(8 (t_ref - t)) in the
+// epilogue's fp32 upward sum; gt of the group is the largest t.
+void radius_pairs(int sr, OzPairList* pl) {
+  build_pairs(sr, sr, false, pl);
+  pl->gt[0] = pl->gt[pl->ngroups - 1];
+  pl->gstart[1] = (int16_t)pl->npairs;
+  pl->ngroups = 1;
 }
 
 // Largest t_ref keeping |W| < 2^62, and the number of floored folds.
@@ -252,7 +263,7 @@ int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan, int crt) {
   pb.s = s;
   pb.sr = sr;
   build_pairs(s, s, true, &plan->mid);
-  build_pairs(sr, sr, false, &plan->rad);
+  radius_pairs(sr, &plan->rad);
   pb.mplanes = s;
   if (crt) {
     pb.crt = 1;
@@ -274,15 +285,10 @@ int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan, int crt) {
   const int nchunks = (pb.Kp + OZ_CHUNK - 1) / OZ_CHUNK;
   choose_scaling(plan->mid, nchunks, &plan->t_ref_mid, &plan->R_mid);
   choose_scaling(plan->rad, nchunks, &plan->t_ref_rad, &plan->R_rad);
-  // the folds of a radius product, in the order the epilogue makes them
-  int f = 0;
-  const OzPairList& rl = plan->rad;
-  for (int g = 0; g < rl.ngroups; ++g) {
-    const int total = (rl.gstart[g + 1] - rl.gstart[g]) * nchunks;
-    for (int c = 0; c < total; c += OZ_FOLD_CHUNKS)
-      if (f < OZ_MAX_RAD_SLOTS) plan->rad_sh[f++] = (int8_t)(8 * (plan->t_ref_rad - rl.gt[g]));
-  }
-  plan->rad_slots = f;
+  // one fold per radius product: the slice GEMM's fp32 upward sum of all
+  // its digit pairs, already weighted by 2^(8 (t_ref - t))
+  plan->rad_slots = 1;
+  plan->rad_sh[0] = 0;
   return VCPCU_OK;
 }
 
@@ -299,18 +305,8 @@ OzRadConst oz_rad_const(const OzPlan& plan) {
 }
 
 namespace {
-// folds per radius product of a problem (the count oz_make_plan derives)
-int rad_slot_count(const OzProblem& pb) {
-  OzPairList rl;
-  build_pairs(pb.sr, pb.sr, false, &rl);
-  const int nchunks = (pb.Kp + OZ_CHUNK - 1) / OZ_CHUNK;
-  int f = 0;
-  for (int g = 0; g < rl.ngroups; ++g) {
-    const int total = (rl.gstart[g + 1] - rl.gstart[g]) * nchunks;
-    f += (total + OZ_FOLD_CHUNKS - 1) / OZ_FOLD_CHUNKS;
-  }
-  return f;
-}
+// folds per radius product of a problem (one: the epilogue's fp32 sum)
+int rad_slot_count(const OzProblem&) { return 1; }
 }  // namespace
 
 size_t oz_workspace_bytes(const OzProblem& pb) {

@@ -50,8 +50,9 @@ struct OzWorkspace {
 struct OzPairList {
   int npairs, ngroups;
   int8_t pa[OZ_MAX_PAIRS], pb[OZ_MAX_PAIRS];   // 0-based plane indices
+  int8_t pt[OZ_MAX_PAIRS];                     // t = p + q of pair (1-based digits)
   int16_t gstart[OZ_MAX_GROUPS + 1];           // group g = pairs [gstart[g], gstart[g+1])
-  int8_t gt[OZ_MAX_GROUPS];                    // t of group g
+  int8_t gt[OZ_MAX_GROUPS];                    // t of group g (radius list: the largest)
 };
 
 // OZ_RAD_SET: radius product 1, (|mA| + rA) * rB; OZ_RAD_ADD: radius

@@ -11,9 +11,10 @@
 //                mod m_g, one byte per entry in res[g][col][row] (one chunk:
 //                reduced on the FP32 pipe straight from TMEM; several: int32
 //                chunk sums, reduced per fold of 64 chunks);
-//   OZ_RAD_SET / OZ_RAD_ADD  the group's int32 chunk sum, one fold per 64
-//                chunks into P (the reassembly scales and adds the folds:
-//                radius factors were rounded up, so the sum bounds them);
+//   OZ_RAD_SET / OZ_RAD_ADD  all digit pairs of one radius product form one
+//                group: every chunk is weighted by its pair's 2^(8 (t_ref - t))
+//                and summed upward in fp32, one fold per (product, tile) into
+//                P (radius factors were rounded up, so the sum bounds them);
 //   OZ_MID       (slice form) folds into an int64 fixed-point value
 //                W = sum_t C_t 2^(8 (t_ref - t)) in global memory; the last
 //                fold is merged into the final epilogue
@@ -175,15 +176,6 @@ __device__ __forceinline__ ItemInfo item_info(const OzGemmArgs& a, int item, int
 // within 1/2 + 2.0000002/m of x/m: r = x - q m (one FMA, exact) is an
 // integer with |r| <= m/2 + 2, and adding m to a negative r gives [0, m)
 // (m >= 107).
-// RU(v) of an int32 v on the FP32 pipe: v = h 2^16 + l with h = v >> 16
-// (floor, |h| < 2^15) and 0 <= l < 2^16; both halves are exact floats (a
-// magic-number subtraction each) and one FMA rounds h 2^16 + l upward.
-__device__ __forceinline__ float int_to_float_ru(int v) {
-  const float hf = __fsub_rn(__int_as_float(0x4B400000 + (v >> 16)), 12582912.0f);
-  const float lf = __fsub_rn(__uint_as_float(0x4B000000u | ((unsigned)v & 0xffffu)), 8388608.0f);
-  return __fmaf_ru(hf, 65536.0f, lf);
-}
-
 __device__ __forceinline__ float rint_f(float x) {  // |x| < 2^22
   return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
 }
@@ -372,16 +364,56 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
         continue;
       }
       bool have_w = false;
-      // radius groups: slot of the next fold = folds of the earlier groups
-      // of the same product
-      int fold = 0;
-      const int kind0 = args.gkind[g0];
-      for (int g = 0; g < g0; ++g)
-        if (args.gkind[g] == kind0)
-          fold += ((args.pl.gstart[g + 1] - args.pl.gstart[g]) * nchunks + OZ_FOLD_CHUNKS - 1) /
-                  OZ_FOLD_CHUNKS;
       for (int g = g0; g < g1 && ok; ++g) {
         const int kind = args.gkind[g];
+        if (kind == OZ_RAD_SET || kind == OZ_RAD_ADD) {
+          // radius product (its digit pairs form one group): every chunk, an
+          // exact integer in fp32, is weighted by its pair's 2^(8 (t_ref - t))
+          // and summed upward -- S = RU(chunk 2^sh + S), an upper bound of
+          // the exact weighted integer sum -- and one fold per (product, tile)
+          // goes out, never read back here
+          const int ncb = (f.nb * 64 - half * 128) >> 5;  // column blocks multiplied
+          float S[128];
+#pragma unroll
+          for (int e = 0; e < 128; ++e) S[e] = 0.0f;
+          int pi = args.pl.gstart[g], pc = 0;
+          const int total = (args.pl.gstart[g + 1] - pi) * nchunks;
+          for (int idx = 0; idx < total; ++idx, ++acc) {
+            const int buf = acc & 1;
+            const uint32_t par = (acc >> 1) & 1;
+            if (*(volatile int*)&sm.abort || !ptx::mbar_wait(&sm.tfull[buf], par, lim)) {
+              if (!*(volatile int*)&sm.abort) raise_timeout(&sm, args.flag, 3);
+              ok = false;
+              break;
+            }
+            ptx::tc_fence_after();
+            const float sc = __int_as_float((127 + 8 * (args.t_ref - args.pl.pt[pi])) << 23);
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) {
+              if (c4 < ncb) {
+                uint32_t r[32];
+                ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c4 * 32, r);
+                ptx::tmem_ld_wait();
+#pragma unroll
+                for (int e = 0; e < 32; ++e)
+                  S[c4 * 32 + e] = __fmaf_ru(__uint_as_float(r[e]), sc, S[c4 * 32 + e]);
+              }
+            }
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&sm.tempty[buf]);
+            if (++pc == nchunks) {
+              pc = 0;
+              ++pi;
+            }
+          }
+          if (!ok) break;
+          int32_t* pp = f.P + ((size_t)(kind == OZ_RAD_ADD ? args.slot_add : 0) * f.Np + gj0) *
+                                  f.Mp + gi;
+#pragma unroll
+          for (int e = 0; e < 128; ++e) pp[(size_t)e * f.Mp] = __float_as_int(S[e]);
+          continue;
+        }
         if (kind == OZ_CRT && nchunks == 1) {
           // residue group (one modulus) of one chunk: the residue goes
           // straight from TMEM to res on the FP32 pipe, for the valid rows
@@ -487,19 +519,6 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
                 c[e] = 0;
               }
             }
-            cnt = 0;
-          } else if ((cnt == OZ_FOLD_CHUNKS || last_of_group) && kind != OZ_MID) {
-            // radius groups: the fold is stored as a float rounded up (an
-            // upper bound of the exact int32 sum), never read back here --
-            // the reassembly sums the slots upward in fp32
-            const int slot = (kind == OZ_RAD_ADD ? args.slot_add : 0) + fold;
-            int32_t* pp = f.P + ((size_t)slot * f.Np + gj0) * f.Mp + gi;
-#pragma unroll
-            for (int e = 0; e < 128; ++e) {
-              pp[(size_t)e * f.Mp] = __float_as_int(int_to_float_ru(c[e]));
-              c[e] = 0;
-            }
-            ++fold;
             cnt = 0;
           } else if (cnt == OZ_FOLD_CHUNKS || last_of_group) {
             // fold into W (global, column-major, ld = Mp); the first fold of
@@ -631,6 +650,7 @@ void all_groups(const OzPairList& rad, const OzPairList& crt, int mpl, int sr, i
       for (int q = src.gstart[g]; q < src.gstart[g + 1]; ++q, ++np) {
         m.pa[np] = (int8_t)(src.pa[q] + offA);
         m.pb[np] = (int8_t)(src.pb[q] + offB);
+        m.pt[np] = src.pt[q];
       }
       ++ng;
     }
@@ -757,11 +777,13 @@ int oz_grun_gemm(const OzGBucket& b, const OzPlan& shape, int mode, int nitems, 
     bp = b.planesB + (size_t)b.Lmax * psB;
     apl = bpl = 2;
     a.pl = shape.rad;
+    a.t_ref = shape.t_ref_rad;
   } else if (mode == OZ_RAD_ADD) {  // rA * |mB|
     ap = b.planesA + (size_t)(b.Lmax + 2) * psA;
     bp = b.planesB + (size_t)(b.Lmax + 2) * psB;
     apl = bpl = 2;
     a.pl = shape.rad;
+    a.t_ref = shape.t_ref_rad;
   } else {
     ap = b.planesA;
     bp = b.planesB;
