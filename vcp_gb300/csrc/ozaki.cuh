@@ -39,7 +39,7 @@ struct OzWorkspace {
   unsigned long long* bsum;           // [Np][2] CRT form: sum_k |B'(k,j)| as (bits >= 32, bits < 32)
   double* T;                          // [N][Mp] upper bound of the radius product (slice form)
   long long* W;                       // [Np][Mp] int64 fold buffer (slice form)
-  int32_t* P;                         // [2 slots][Np][Mp] folds of the two radius products
+  int32_t* P;                         // [2 slots][Np][Mp] fp32 folds (bits) of the two radius products
   int* flag;                          // [0] non-finite input, [1] device wait timeout
   // Plane strides (elements) of the left / right digit planes when they are
   // a row / column block of larger planes; 0: Mp Kp / Np Kp.
@@ -57,7 +57,7 @@ struct OzPairList {
 
 // OZ_RAD_SET: radius product 1, (|mA| + rA) * rB; OZ_RAD_ADD: radius
 // product 2, rA * |mB|.  Each writes T or adds to it (OzGemmArgs::t_set).
-constexpr int OZ_MAX_RAD_SLOTS = 64;  // K <= 2^20: at most 64 folds of 64 chunks per product
+constexpr int OZ_MAX_RAD_SLOTS = 64;  // capacity of the fold-slot tables (one slot is used)
 
 enum OzMode { OZ_RAD_SET = 0, OZ_RAD_ADD = 1, OZ_MID = 2, OZ_CRT = 3, OZ_ALL = 4 };
 // OZ_ALL (CRT form): both radius products and the residue GEMMs in one
@@ -88,8 +88,8 @@ struct alignas(128) OzGemmArgs {
   long long timeout_cycles;
   uint8_t* res;                 // OZ_CRT: residue planes [L][Np][Mp]
   int moduli[32];               // OZ_CRT: modulus of group g
-  int32_t* P;                   // radius groups: fold f of a tile -> slot f (product 1) or
-  int slot_add;                 //   slot_add + f (product 2, OZ_RAD_ADD)
+  int32_t* P;                   // radius groups: the fold of a tile -> slot 0 (product 1) or
+  int slot_add;                 //   slot slot_add (product 2, OZ_RAD_ADD)
   int8_t gkind[OZ_MAX_GROUPS];  // mode of group g (OZ_RAD_SET / _ADD / OZ_CRT / OZ_MID)
   int8_t gres[OZ_MAX_GROUPS];   // OZ_CRT groups: residue plane (modulus index) of group g
   // grouped products: items of problem p are [gitem[p], gitem[p+1]); its
@@ -117,8 +117,9 @@ struct OzPlan {
   // bit 0: A is a point matrix (rA = 0), bit 1: B is (rB = 0).  The radius
   // product with a zero factor is skipped; it would add exactly 0 to T.
   int point_mask = 0;
-  // Folds of one radius product: each is an int32 partial sum of one group,
-  // scaled by 2^rad_sh[f] into W (exact: t_ref_rad is the largest t).
+  // Folds of one radius product: one fp32 upper bound per (product, tile),
+  // the epilogue's weighted upward sum of all its digit pairs (rad_slots =
+  // 1, rad_sh[0] = 0).
   int rad_slots;
   int8_t rad_sh[OZ_MAX_RAD_SLOTS];
 };
