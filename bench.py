@@ -425,9 +425,12 @@ def run_ours(args, ws, rank, local):
     _lib.call("vcpcu_igemm", n, n, n, pa, pb, pc, form, args.slices)
     barrier(ws)
     t0 = time.perf_counter()
+    e2e_marks = [t0]
     for _ in range(e2e_steps):
         _lib.call("vcpcu_igemm", n, n, n, pa, pb, pc, form, args.slices)
+        e2e_marks.append(time.perf_counter())  # the call returns synchronised
     t_e2e = (time.perf_counter() - t0) / e2e_steps
+    e2e_step_ms = [1e3 * (b - a) for a, b in zip(e2e_marks, e2e_marks[1:])]
     t_e2e = max_over_ranks(t_e2e, ws, dev)
     e2e_val = ws * 2.0 * n ** 3 / t_e2e / 1e12
 
@@ -480,7 +483,8 @@ def run_ours(args, ws, rank, local):
             "auto_pick": auto_pick,
             "e2e": {"value": e2e_val, "unit": UNIT,
                     "h2d_bytes_per_step": int(hA.numel() * 8 + hB.numel() * 8),
-                    "d2h_bytes_per_step": int(hC.numel() * 8)},
+                    "d2h_bytes_per_step": int(hC.numel() * 8),
+                    "steps": e2e_steps, "step_ms": e2e_step_ms},
             "gpu_launches": int(launches),
             "roofline": roof,
             "cpu_baseline": cpu,

@@ -94,14 +94,6 @@ __global__ void oz_status_merge(const int* flag) {
   if (v) atomicOr(&g_oz_status, v);
 }
 
-// The status words of n products (4 ints each).
-__global__ void oz_status_merge_n(const int* flag, int n) {
-  int v = 0;
-  for (int p = threadIdx.x; p < n; p += blockDim.x)
-    v |= (flag[4 * p] ? 1 : 0) | (flag[4 * p + 1] ? 2 : 0);
-  if (v) atomicOr(&g_oz_status, v);
-}
-
 // Optional per-phase timing (CUDA events recorded on the call's stream).
 struct OzProfile {
   bool on = false;
@@ -201,11 +193,6 @@ int* oz_status_ptr() {
     ptr[dev] = (int*)p;
   }
   return ptr[dev];
-}
-
-void oz_merge_status_n(const int* flag, int n, cudaStream_t s) {
-  oz_status_merge_n<<<1, 256, 0, s>>>(flag, n);
-  count_launch();
 }
 
 int oz_take_status(cudaStream_t s, int* status) {

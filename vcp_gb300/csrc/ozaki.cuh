@@ -175,8 +175,6 @@ int oz_take_status(cudaStream_t s, int* status);
 int oz_selftest_timeout(long long limit, cudaStream_t s);
 // Merge a product's status words into the sticky device status.
 void oz_merge_status(const int* flag, cudaStream_t s);
-// ... of n products (status words 4 ints apart).
-void oz_merge_status_n(const int* flag, int n, cudaStream_t s);
 // Device address of the sticky status word of the current device (kernels
 // that merge statuses themselves atomicOr into it); null on error.
 int* oz_status_ptr();
