@@ -61,9 +61,6 @@ __global__ void check(long n, unsigned long long seed, unsigned long long* bad) 
     const double b = make(r2 * 0x2545F4914F6CDD1DULL, cb, a);
     // sign flip
     if (sw_bits(sw_neg(a)) != sw_bits(-a)) atomicAdd(&bad[0], 1ULL);
-    // upward addition of magnitudes
-    const double pa = sw_double(sw_bits(a) & ~(1ULL << 63)), pb = sw_double(sw_bits(b) & ~(1ULL << 63));
-    if (sw_bits(sw_add_ru_pos(pa, pb)) != sw_bits(__dadd_ru(pa, pb))) atomicAdd(&bad[1], 1ULL);
     // kv midrad of [min, max]
     const bool lt = __dsub_rn(a, b) < 0.0;
     const double lo = lt ? a : b, hi = lt ? b : a;
@@ -71,21 +68,20 @@ __global__ void check(long n, unsigned long long seed, unsigned long long* bad) 
     sw_midrad(lo, hi, m1, r1d, p1);
     sw_midrad_hw(lo, hi, m2, r2d, p2);
     if (sw_bits(m1) != sw_bits(m2) || sw_bits(r1d) != sw_bits(r2d) || sw_bits(p1) != sw_bits(p2))
-      atomicAdd(&bad[2], 1ULL);
+      atomicAdd(&bad[1], 1ULL);
   }
 }
 
 int main() {
   unsigned long long* bad = nullptr;
-  if (cudaMalloc(&bad, 3 * sizeof(unsigned long long)) != cudaSuccess) return 2;
-  cudaMemset(bad, 0, 3 * sizeof(unsigned long long));
+  if (cudaMalloc(&bad, 2 * sizeof(unsigned long long)) != cudaSuccess) return 2;
+  cudaMemset(bad, 0, 2 * sizeof(unsigned long long));
   const long n = 1L << 24;
   for (unsigned long long seed = 1; seed <= 4; ++seed) check<<<152 * 16, 256>>>(n, seed * 0x9E37ULL, bad);
-  unsigned long long h[3] = {0, 0, 0};
+  unsigned long long h[2] = {0, 0};
   if (cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return 3;
   printf("cases %ld\n", 4 * n);
   printf("sw_neg mismatches %llu\n", h[0]);
-  printf("sw_add_ru_pos mismatches %llu\n", h[1]);
-  printf("sw_midrad mismatches %llu\n", h[2]);
+  printf("sw_midrad mismatches %llu\n", h[1]);
   return 0;
 }

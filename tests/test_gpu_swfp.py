@@ -1,7 +1,7 @@
-"""The integer-pipe binary64 helpers of the tensor-core form (sign flip,
-upward addition of magnitudes, kv midrad) equal the FP64 instructions bit
-for bit on 2^26 seeded cases of every operand class (tests/swfp_check.cu,
-built here with nvcc for sm_103a)."""
+"""The integer-pipe binary64 helpers of the tensor-core form (sign flip, kv
+midrad) equal the FP64 instructions bit for bit on 2^26 seeded cases of
+every operand class (tests/swfp_check.cu, built here with nvcc for
+sm_103a)."""
 import os
 import shutil
 import subprocess
@@ -24,5 +24,5 @@ def test_swfp_bitexact():
                        check=True, capture_output=True, text=True)
         out = subprocess.run([exe], check=True, capture_output=True, text=True, timeout=300).stdout
     counts = {ln.split()[0]: int(ln.split()[-1]) for ln in out.splitlines() if "mismatches" in ln}
-    assert set(counts) == {"sw_neg", "sw_add_ru_pos", "sw_midrad"}, out
+    assert set(counts) == {"sw_neg", "sw_midrad"}, out
     assert all(v == 0 for v in counts.values()), out

@@ -230,7 +230,7 @@ __device__ __forceinline__ double rad_T(float S1, float S2, int Ep, int Er, int 
   if (!rc.run2) return b1;
   const double b2 =
       rad_term(S2, Er == OZ_ZERO_EXP || Fm == OZ_ZERO_EXP, Er + Fm - 8 * rc.t_ref, rc.R);
-  return rc.run1 ? sw_add_ru_pos(b1, b2) : b2;
+  return rc.run1 ? __dadd_ru(b1, b2) : b2;
 }
 
 // Slice form: T (ld Mp) from the folds, before the midpoint product.

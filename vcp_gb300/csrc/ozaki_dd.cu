@@ -354,7 +354,7 @@ dd_crt_assemble_kernel(int M, int N, int K, int Mp, int L, int w, const uint8_t*
           else
             tr = scale_ru_slow(kf, et);
         }
-        err = sw_add_ru_pos(err, tr);
+        err = __dadd_ru(err, tr);
         if (!range_ok) err = INFINITY;
       }
       if (bad) hi = lo = err = __longlong_as_double(0x7ff8000000000000LL);

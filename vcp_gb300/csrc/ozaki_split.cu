@@ -160,7 +160,7 @@ oz_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ mA,
     if (i < M && k < K) {
       m = mA[i + (long)k * M];
       rr = rA[i + (long)k * M];
-      p = sw_add_ru_pos(oz_abs(m), rr);
+      p = __dadd_ru(oz_abs(m), rr);
     }
     digits_of<S>(m, Em, 0, d);
 #pragma unroll
@@ -536,7 +536,7 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
         if (i < M && k < K) {
           m = X[i + (long)k * ldx];
           r = rA[i + (long)k * ldx];
-          p = sw_add_ru_pos(oz_abs(m), r);
+          p = __dadd_ru(oz_abs(m), r);
         }
         a[t + u] = crt_int(m, Em, w);
         digits_of<SR>(p, Ep, 1, u ? d1 : d0);

@@ -1,8 +1,11 @@
-// swfp.cuh -- binary64 midrad and upward addition on the integer pipe.
+// swfp.cuh -- binary64 midrad on the integer pipe.
 //
 // GB300 issues FP64 at 1/64 of the FP32 rate, so the operand preparation of
 // the tensor-core form (one kv midrad per interval entry) is bound by the
-// FP64 pipe when it uses FP64 instructions.  The functions below compute the
+// FP64 pipe when it uses FP64 instructions.  (A single FP64 instruction per
+// entry beside integer-bound work is cheaper on the FP64 pipe, which runs in
+// parallel: the upward additions |m| + r of the splits and of the radius
+// term stay FP64 instructions.)  The functions below compute the
 // same bits with integer operations for the common case -- both endpoints
 // normal, of one sign, binary exponents at most one apart (an interval
 // narrower than its midpoint) -- and fall back to the FP64 instructions
@@ -161,75 +164,10 @@ static __device__ __noinline__ void sw_midrad_slow(double lo, double up, double&
                                             double& p) {
   sw_midrad_hw(lo, up, m, r, p);
 }
-static __device__ __noinline__ double sw_dadd_ru_slow(double a, double b) { return __dadd_ru(a, b); }
 
 __device__ __forceinline__ void sw_midrad(double lo, double up, double& m, double& r,
                                           double& p) {
   if (!sw_midrad_fast(lo, up, m, r, p)) sw_midrad_slow(lo, up, m, r, p);
-}
-
-// RU(a + b) for a, b >= 0 (finite): the integer pipe when both are normal
-// and the sum is normal, else __dadd_ru.
-__device__ __forceinline__ double sw_add_ru_pos(double a, double b) {
-  unsigned long long ba = sw_bits(a), bb = sw_bits(b);
-  if (ba < bb) {
-    const unsigned long long t = ba;
-    ba = bb;
-    bb = t;
-  }
-  // a >= b >= +0 now (bit order = value order for non-negative doubles)
-  if (bb == 0) return sw_double(ba);
-  const int ea = (int)(ba >> 52), eb = (int)(bb >> 52);
-  if (eb == 0 || ea >= 2046) return sw_dadd_ru_slow(a, b);
-  const unsigned long long H = 1ULL << 52;
-  const unsigned long long ma = ((ba & (H - 1)) | H) << 10;  // 63 bits
-  const unsigned long long mb0 = ((bb & (H - 1)) | H) << 10;
-  const int d = ea - eb;
-  unsigned long long mb;
-  bool sticky;
-  if (d >= 64) {
-    mb = 0;
-    sticky = true;
-  } else {
-    mb = mb0 >> d;
-    sticky = d > 0 && (mb0 & ((1ULL << d) - 1)) != 0;
-  }
-  // sum in units 2^(ea - 1085), < 2^64
-  unsigned long long S = ma + mb;
-  int B = ea;
-  int low = 10;  // bits below the 53-bit significand
-  if (S >> 63) {
-    low = 11;
-    ++B;
-  }
-  unsigned long long M = S >> low;
-  if (sticky || (S & ((1ULL << low) - 1))) {
-    ++M;
-    if (M >> 53) {
-      M >>= 1;
-      ++B;
-    }
-  }
-  if (B > 2046) return sw_dadd_ru_slow(a, b);
-  return sw_double(((unsigned long long)B << 52) | (M & (H - 1)));
-}
-
-// RU(v * 2^ex) for an int64 v >= 0 built on the integer pipe (equal to
-// RU-scaling of __ll2double_ru(v)); false when the result is not normal or
-// v < 0.
-__device__ __forceinline__ bool sw_i64_scale_ru(long long v, int ex, double* out) {
-  if (v <= 0) {
-    *out = 0.0;
-    return v == 0;
-  }
-  const unsigned long long t = (unsigned long long)v;
-  const int lz = __clzll(t);
-  const unsigned long long tn = t << lz;
-  const int be = 1023 + 63 - lz + ex;
-  if (be < 1 || be > 2046) return false;
-  *out = sw_double(((unsigned long long)be << 52) + ((tn >> 11) & ((1ULL << 52) - 1)) +
-                   ((tn & 0x7ffULL) ? 1ULL : 0ULL));
-  return true;
 }
 
 }  // namespace vcpcu
