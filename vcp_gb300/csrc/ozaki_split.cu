@@ -445,9 +445,23 @@ __device__ __forceinline__ double dev_scale_dir(double x, int e, bool up) {
 }
 
 // w-bit integer of x (|x| <= 2^(E-1)): round to nearest even, |result| <= 2^(w-1).
+// x 2^(w-E) is formed exactly by power-of-two multiplications (no overflow:
+// it stays below 2^(w-1); a subnormal intermediate is below 2^-1022 and
+// converts to 0 either way) and converted with one rounding.
 __device__ __forceinline__ long long crt_int(double x, int E, int w) {
   if (E == OZ_ZERO_EXP || oz_zero(x)) return 0;
-  return oz_scaled_int64(x, E, w, 0);
+  int s = w - E;
+  if (s < -1100) return 0;  // |x| 2^s < 2^-76
+  double y = x;
+  while (s > 1000) {
+    y = __dmul_rn(y, 0x1p1000);
+    s -= 1000;
+  }
+  while (s < -1000) {
+    y = __dmul_rn(y, 0x1p-1000);
+    s += 1000;
+  }
+  return __double2ll_rn(__dmul_rn(y, __longlong_as_double((long long)(s + 1023) << 52)));
 }
 
 // Stores of a left split's plane tiles (32 rows x 64 k of bf16; lane = row,
