@@ -66,7 +66,10 @@ __device__ __forceinline__ void digits_of(double x, int E, int up, int (&d)[S]) 
 // ---------------------------------------------------------------- left factor
 // Pass 1: kv midrad of every entry, stored as the planes mA, rA (column-major,
 // ld = ldm), and the row maxima of |mA|, P = |mA| +ru rA and rA as double bit
-// patterns (non-negative doubles order like their bit patterns).
+// patterns (non-negative doubles order like their bit patterns).  One entry
+// in four takes the FP64 instructions (sw_midrad_hw, the same bits), the
+// others the integer-pipe form: the FP64 pipe then runs beside the integer
+// one (at half, the FP64 pipe became the bound).
 // Block: 32 rows x 8 column phases over a column range.
 __global__ void __launch_bounds__(256)
 oz_rowmax_left(int M, int K, const double* __restrict__ A, long lda, int cols_per_block,
@@ -97,7 +100,10 @@ oz_rowmax_left(int M, int K, const double* __restrict__ A, long lda, int cols_pe
         if (c >= c1) break;
         double m = 0.0, r = 0.0, p;
         if (sw_finite(e[u].x) && sw_finite(e[u].y)) {
-          sw_midrad(e[u].x, e[u].y, m, r, p);
+          if (u == U - 1)
+            sw_midrad_hw(e[u].x, e[u].y, m, r, p);
+          else
+            sw_midrad(e[u].x, e[u].y, m, r, p);
           am = max(am, dbits(oz_abs(m)));
           ap = max(ap, dbits(p));
           ar = max(ar, dbits(r));
@@ -655,11 +661,14 @@ oz_rowmax_left_g(const __grid_constant__ OzGBucket b) {
     const int c0 = (local / nbx) * 256;
     const int c1 = min(q.k, c0 + 256);
     const size_t row = (size_t)(q.rowoff + i);
-    for (int c = c0 + ph; c < c1; c += 8) {
+    for (int c = c0 + ph, it = 0; c < c1; c += 8, ++it) {
       const double2 e = *reinterpret_cast<const double2*>(q.A + 2 * (i + (long)c * q.lda));
       double m = 0.0, r = 0.0, pp;
       if (sw_finite(e.x) && sw_finite(e.y)) {
-        sw_midrad(e.x, e.y, m, r, pp);
+        if ((it & 3) == 3)  // one entry in four on the FP64 pipe (see oz_rowmax_left)
+          sw_midrad_hw(e.x, e.y, m, r, pp);
+        else
+          sw_midrad(e.x, e.y, m, r, pp);
         am = max(am, dbits(oz_abs(m)));
         ap = max(ap, dbits(pp));
         ar = max(ar, dbits(r));
@@ -742,12 +751,15 @@ __global__ void __launch_bounds__(256) oz_colmax_right_g(const __grid_constant__
     const double* bcol = q.B + 2 * (long)j * q.ldb;
     double* mcol = b.midB + (size_t)jst * b.Kp;
     double* rcol = b.radB + (size_t)jst * b.Kp;
-    for (int k = lane; k < K; k += 32) {
+    for (int k = lane, it = 0; k < K; k += 32, ++it) {
       const double2 e = *reinterpret_cast<const double2*>(bcol + 2 * k);
       double m = 0.0, r = 0.0;
       if (sw_finite(e.x) && sw_finite(e.y)) {
         double pp;
-        sw_midrad(e.x, e.y, m, r, pp);
+        if ((it & 3) == 3)  // one entry in four on the FP64 pipe (see oz_rowmax_left)
+          sw_midrad_hw(e.x, e.y, m, r, pp);
+        else
+          sw_midrad(e.x, e.y, m, r, pp);
         am = max(am, dbits(oz_abs(m)));
         ar = max(ar, dbits(r));
       } else {
@@ -962,7 +974,10 @@ oz_colmax_right(int K, int N, int Kp, int cols, int colbase, const double* __res
         double m = 0.0, r = 0.0;
         if (sw_finite(e[u].x) && sw_finite(e[u].y)) {
           double p;
-          sw_midrad(e[u].x, e[u].y, m, r, p);
+          if (u == U - 1)
+            sw_midrad_hw(e[u].x, e[u].y, m, r, p);
+          else
+            sw_midrad(e[u].x, e[u].y, m, r, p);
           am = max(am, dbits(oz_abs(m)));
           ar = max(ar, dbits(r));
         } else {
