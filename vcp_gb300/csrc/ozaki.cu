@@ -275,7 +275,6 @@ int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan, int crt) {
   // one fold per radius product: the slice GEMM's fp32 upward sum of all
   // its digit pairs, already weighted by 2^(8 (t_ref - t))
   plan->rad_slots = 1;
-  plan->rad_sh[0] = 0;
   return VCPCU_OK;
 }
 
@@ -287,7 +286,6 @@ OzRadConst oz_rad_const(const OzPlan& plan) {
   rc.run2 = !(plan.point_mask & 1);
   rc.t_ref = plan.t_ref_rad;
   rc.R = plan.R_rad;
-  for (int f = 0; f < plan.rad_slots; ++f) rc.sh[f] = plan.rad_sh[f];
   return rc;
 }
 

@@ -57,7 +57,6 @@ struct OzPairList {
 
 // OZ_RAD_SET: radius product 1, (|mA| + rA) * rB; OZ_RAD_ADD: radius
 // product 2, rA * |mB|.  Each writes T or adds to it (OzGemmArgs::t_set).
-constexpr int OZ_MAX_RAD_SLOTS = 64;  // capacity of the fold-slot tables (one slot is used)
 
 enum OzMode { OZ_RAD_SET = 0, OZ_RAD_ADD = 1, OZ_MID = 2, OZ_CRT = 3, OZ_ALL = 4 };
 // OZ_ALL (CRT form): both radius products and the residue GEMMs in one
@@ -118,10 +117,8 @@ struct OzPlan {
   // product with a zero factor is skipped; it would add exactly 0 to T.
   int point_mask = 0;
   // Folds of one radius product: one fp32 upper bound per (product, tile),
-  // the epilogue's weighted upward sum of all its digit pairs (rad_slots =
-  // 1, rad_sh[0] = 0).
+  // the epilogue's weighted upward sum of all its digit pairs (rad_slots = 1).
   int rad_slots;
-  int8_t rad_sh[OZ_MAX_RAD_SLOTS];
 };
 
 // The radius bound T(i, j) from the folds of the two radius products (the
@@ -130,7 +127,6 @@ struct OzRadConst {
   int nslot;                    // folds per product (slots [0, n) and [n, 2n))
   int run1, run2;               // which products ran (zero-radius operands skip)
   int t_ref, R;
-  int8_t sh[OZ_MAX_RAD_SLOTS];
 };
 OzRadConst oz_rad_const(const OzPlan& plan);
 // Slice form: T from the folds into ws.T (the CRT form's reassembly

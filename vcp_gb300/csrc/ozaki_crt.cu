@@ -176,35 +176,25 @@ __device__ __forceinline__ int crt_value(const uint32_t (&c)[16], const uint32_t
   return neg;
 }
 
-// The radius sums of both products for 4 consecutive rows (e0 = j Mp +
-// i0).  Every fold is the fp32 upward rounding of an exact int32 chunk sum
-// (written so by the slice GEMM), and S = RU(fold 2^sh + S) over the folds in
-// the order they were made: an upper bound of the exact W = sum fold 2^sh,
-// since every term and every partial sum is rounded up.  All values are
-// integers below 2^53 (folds < 2^31, sh <= 16, at most 64 folds), so the
-// single-rounding FMA is the only inexact step.
+// The radius sums of both products for 4 consecutive rows (e0 = j Mp + i0):
+// one fp32 fold per product (slot 0 and slot nslot = 1), the slice GEMM
+// epilogue's upward sum of every chunk weighted by its digit pair -- an
+// upper bound of the exact integer W of the product.
 __device__ __forceinline__ void rad_folds(const int32_t* __restrict__ P, size_t plane,
                                           size_t e0, const OzRadConst& rc, float (&S1)[4],
                                           float (&S2)[4]) {
-#pragma unroll
-  for (int u = 0; u < 4; ++u) S1[u] = S2[u] = 0.0f;
-  for (int f = 0; f < rc.nslot; ++f) {
-    const float sc = __int_as_float((127 + rc.sh[f]) << 23);  // 2^sh, 0 <= sh <= 16
-    if (rc.run1) {
-      const float4 v = *reinterpret_cast<const float4*>(P + (size_t)f * plane + e0);
-      S1[0] = __fmaf_ru(v.x, sc, S1[0]);
-      S1[1] = __fmaf_ru(v.y, sc, S1[1]);
-      S1[2] = __fmaf_ru(v.z, sc, S1[2]);
-      S1[3] = __fmaf_ru(v.w, sc, S1[3]);
-    }
-    if (rc.run2) {
-      const float4 v = *reinterpret_cast<const float4*>(P + (size_t)(rc.nslot + f) * plane + e0);
-      S2[0] = __fmaf_ru(v.x, sc, S2[0]);
-      S2[1] = __fmaf_ru(v.y, sc, S2[1]);
-      S2[2] = __fmaf_ru(v.z, sc, S2[2]);
-      S2[3] = __fmaf_ru(v.w, sc, S2[3]);
-    }
-  }
+  const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const float4 v1 = rc.run1 ? *reinterpret_cast<const float4*>(P + e0) : z;
+  const float4 v2 =
+      rc.run2 ? *reinterpret_cast<const float4*>(P + (size_t)rc.nslot * plane + e0) : z;
+  S1[0] = v1.x;
+  S1[1] = v1.y;
+  S1[2] = v1.z;
+  S1[3] = v1.w;
+  S2[0] = v2.x;
+  S2[1] = v2.y;
+  S2[2] = v2.z;
+  S2[3] = v2.w;
 }
 
 // RU((S + R) 2^ex), 0 for a zero row or column.  S + R >= the exact W + R >=
