@@ -422,8 +422,11 @@ int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long l
   const int Mq = (pb.M + 3) / 4;
   // about 8 columns per thread: its rows' exponents and sums are set up once
   const int gy = (pb.N + 7) / 8;
-  dim3 grid((Mq + 255) / 256, gy < 65535 ? gy : 65535);
-  oz_crt_assemble_kernel<<<grid, 256, 0, st>>>(
+  // 128-thread blocks: a row count that is not a multiple of 1024 leaves at
+  // most 127 idle threads per column group (the blocks of a host-pointer
+  // product have 768 - 1536 rows)
+  dim3 grid((Mq + 127) / 128, gy < 65535 ? gy : 65535);
+  oz_crt_assemble_kernel<<<grid, 128, 0, st>>>(
       pb.M, pb.N, pb.Mp, pb.L, pb.w, ws.res, (size_t)pb.Np * pb.Mp, ws.E3, ws.F2, ws.asum,
       ws.beta, ws.P, C, ldc, ws.flag, cc, oz_rad_const(plan));
   VCPCU_LAUNCH_CHECK("oz_crt_assemble_kernel");
