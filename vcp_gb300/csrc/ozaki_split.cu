@@ -319,37 +319,11 @@ oz_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
 }
 
 // ------------------------------------------------------ CRT form (residues)
-// Barrett reduction constants of the moduli (x < 2^32): q = umulhi(x, magic)
-// is at most two below floor(x / m).
+// The moduli, largest first (the list the host plan indexes).
 #define OZ_MOD_LIST(F)                                                                   \
   F(256), F(255), F(253), F(251), F(247), F(241), F(239), F(233), F(229), F(227), F(223),     \
       F(217), F(211), F(199), F(197), F(193), F(191), F(181), F(179), F(173), F(167), F(163), \
       F(157), F(151), F(149), F(139), F(137), F(131), F(127), F(113), F(109), F(107)
-#define OZ_ID(m) (m)
-#define OZ_MAGIC(m) (0xFFFFFFFFu / (m))
-#define OZ_P32(m) ((uint32_t)(4294967296ULL % (m)))
-__constant__ uint32_t c_mod[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_ID)};
-__constant__ uint32_t c_magic[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_MAGIC)};
-__constant__ uint32_t c_pow32[OZ_MAX_MODULI] = {OZ_MOD_LIST(OZ_P32)};
-
-__device__ __forceinline__ uint32_t umod32(uint32_t x, uint32_t m, uint32_t magic) {
-  uint32_t r = x - __umulhi(x, magic) * m;
-  if (r >= m) r -= m;
-  if (r >= m) r -= m;
-  return r;
-}
-
-// Symmetric residue of (neg ? -a : a) mod m_l, a < 2^63; equals oz_sym_residue.
-__device__ __forceinline__ int dev_sym_residue(unsigned long long a, int neg, int l) {
-  const uint32_t m = c_mod[l], mg = c_magic[l];
-  const uint32_t rh = umod32((uint32_t)(a >> 32), m, mg);
-  const uint32_t rl = umod32((uint32_t)a, m, mg);
-  uint32_t r = umod32(rh * c_pow32[l] + rl, m, mg);
-  if (neg && r) r = m - r;
-  int rs = (int)r;
-  if (2 * rs >= (int)m) rs -= (int)m;
-  return rs;
-}
 
 // Residues on the FP32 pipe (the integer multiply pipe is half as wide).
 // |a| is cut into b-bit limbs h_t (b = 12; b = 14 for the four-limb form,
@@ -1230,22 +1204,6 @@ int oz_prepare(const OzProblem& pb, const double* A, long lda, const double* B, 
 }
 
 // ------------------------------------------------------------ dd (pddcuda)
-// Symmetric residue of (neg ? -a : a) mod m_l for a < 2^128 (Horner over
-// 32-bit limbs).
-__device__ __forceinline__ int dev_sym_residue128(unsigned __int128 a, int neg, int l) {
-  const uint32_t m = c_mod[l], mg = c_magic[l], p = c_pow32[l];
-  uint32_t r = 0;
-#pragma unroll
-  for (int t = 3; t >= 0; --t) {
-    const uint32_t limb = (uint32_t)(a >> (32 * t));
-    r = umod32(r * p + umod32(limb, m, mg), m, mg);
-  }
-  if (neg && r) r = m - r;
-  int rs = (int)r;
-  if (2 * rs >= (int)m) rs -= (int)m;
-  return rs;
-}
-
 // w-bit integer of a dd value hi + lo against exponent E: the two words are
 // scaled and rounded to integers separately (|error| <= 1 unit).
 __device__ __forceinline__ __int128 dd_int(double hi, double lo, int E, int w) {
