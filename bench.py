@@ -325,9 +325,17 @@ def run_ours(args, ws, rank, local):
     if form_name == "auto":
         form_name = "ozaki" if have_ozaki else "plain"
     form = pidcuda.FORM_OZAKI if form_name == "ozaki" else pidcuda.FORM_PLAIN
+    # slice count of the tensor-core form: --slices, else the autotuner's
+    # pick for these operands (vcpcu_autotune_pick, made once before the
+    # timed region as a caller would; it may add the fast radius products)
+    slices, slices_src = args.slices, "--slices" if args.slices else "default"
+    if form == pidcuda.FORM_OZAKI and not args.slices:
+        f0, s0 = pidcuda.autotune_pick(dA, dB, n, n, n, stream)
+        if f0 == pidcuda.FORM_OZAKI and s0:
+            slices, slices_src = s0, "autotune_pick"
 
-    def one(f, slices=args.slices):
-        pidcuda.mulmm_dev(n, n, n, dA, n, dB, n, dC, n, f, slices, stream)
+    def one(f):
+        pidcuda.mulmm_dev(n, n, n, dA, n, dB, n, dC, n, f, slices if f == form else 0, stream)
 
     def timed(f, steps, warmup):
         for _ in range(warmup):
@@ -367,6 +375,7 @@ def run_ours(args, ws, rank, local):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": ws * 2.0 * n ** 3 / (ms_max * 1e-3) / 1e12,
                               "unit": UNIT, "ms_per_step": ms_max, "form": form_name, "n": n,
+                              "slices": slices, "slices_source": slices_src,
                               "only_headline": True}), flush=True)
         return
     C_head = dC.cpu().numpy().copy()
@@ -398,7 +407,7 @@ def run_ours(args, ws, rank, local):
     # depends only on its row of A, its column of B and k)
     model = None
     if form == pidcuda.FORM_OZAKI and rank == 0 and not args.no_model_check:
-        model = model_bitexact_sample(O, A, B, C_head, n, args.slices or 8)
+        model = model_bitexact_sample(O, A, B, C_head, n, slices or 8)
 
     # the autotuner's pick (form, slice count) for the headline operands and
     # for square 2048 products at exponent spreads 0, 8, 32
@@ -422,12 +431,12 @@ def run_ours(args, ws, rank, local):
     hC = torch.empty(2 * n * n, dtype=torch.float64).pin_memory()
     pa, pb, pc = hA.data_ptr(), hB.data_ptr(), hC.data_ptr()
     e2e_steps = max(1, min(args.steps, 3 if form == pidcuda.FORM_PLAIN else args.steps))
-    _lib.call("vcpcu_igemm", n, n, n, pa, pb, pc, form, args.slices)
+    _lib.call("vcpcu_igemm", n, n, n, pa, pb, pc, form, slices)
     barrier(ws)
     t0 = time.perf_counter()
     e2e_marks = [t0]
     for _ in range(e2e_steps):
-        _lib.call("vcpcu_igemm", n, n, n, pa, pb, pc, form, args.slices)
+        _lib.call("vcpcu_igemm", n, n, n, pa, pb, pc, form, slices)
         e2e_marks.append(time.perf_counter())  # the call returns synchronised
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     e2e_step_ms = [1e3 * (b - a) for a, b in zip(e2e_marks, e2e_marks[1:])]
@@ -445,7 +454,7 @@ def run_ours(args, ws, rank, local):
                 "algorithmic": "8 n^3 FP64 flops per launch (4 directed FMA chains)"}
     else:
         roof = ozaki_roofline(phases, tc_flops, args.steps, pk, pk_kind, n,
-                              args.slices in (0, 8))
+                              slices == 8 | pidcuda.SLICES_FAST_RADIUS)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -473,7 +482,7 @@ def run_ours(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form_name == "plain" else "bf16-slices/f64",
             "data": "synthetic (seeded)",
-            "form": form_name, "slices": args.slices or "default",
+            "form": form_name, "slices": slices or "default", "slices_source": slices_src,
             "config": headline_config(n, ws),
             "plain": {"value": plain_tflops, "ms_per_step": plain_ms, "steps": args.plain_steps},
             "speedup_vs_plain": value / plain_tflops,
@@ -518,13 +527,14 @@ def measure_fp64_peak(dev):
 
 
 # DRAM bytes (read + write) of the oz_slice_gemm_kernel launch of one
-# n = 8192 product at the default precision (radius digit pairs and residue
-# GEMMs in one launch), from a one-pass ncu capture of dram__bytes_read.sum
-# and dram__bytes_write.sum on a GB300 (25.73 + 3.23 GB).
-GEMM_TRAFFIC_N8192 = 28.96e9
+# n = 8192 product at 8 slices with the fast radius products (2 x 3 radius
+# digit pairs and 16 residue GEMMs in one launch), from a one-pass ncu
+# capture of dram__bytes_read.sum and dram__bytes_write.sum on a GB300
+# (21.98 + 2.05 GB).
+GEMM_TRAFFIC_N8192 = 24.04e9
 
 
-def ozaki_roofline(phases, tc_flops, steps, pk, pk_kind, n=8192, default_form=True):
+def ozaki_roofline(phases, tc_flops, steps, pk, pk_kind, n=8192, fast8=True):
     """Dominant kernel oz_slice_gemm_kernel (one launch per call for the
     default CRT form, three for the slice form): the algorithmic bf16 tensor
     flops (2 m n k per slice pair or modulus) over the summed CUDA-event time
@@ -539,10 +549,11 @@ def ozaki_roofline(phases, tc_flops, steps, pk, pk_kind, n=8192, default_form=Tr
     peak = pk.get("bf16_tflops", 1900.0)
     return {"bound": "tensor", "kernel": "oz_slice_gemm_kernel", "achieved": achieved,
             "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
-            "traffic": GEMM_TRAFFIC_N8192 if (n == 8192 and default_form) else None,
+            "traffic": GEMM_TRAFFIC_N8192 if (n == 8192 and fast8) else None,
             "traffic_unit": "bytes per call (1 launch)",
             "peak_kind": f"{pk_kind} bf16 dense (burst); sustained {pk.get('bf16_tflops_sustained')}",
-            "algorithmic": "2*m*n*k per bf16 product: L residue GEMMs + 2 x 4 radius digit pairs",
+            "algorithmic": "2*m*n*k per bf16 product: L residue GEMMs + the radius digit "
+                           "pairs (2 x 3 with the fast radius products, else 2 x 4)",
             "phase_ms_per_call": phase_ms}
 
 

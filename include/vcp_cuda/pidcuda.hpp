@@ -14,6 +14,7 @@
 // Form and precision are process-wide settings:
 //     vcp::pidcuda_settings::form()   = VCPCU_FORM_OZAKI;   // default
 //     vcp::pidcuda_settings::slices() = 0;                  // default precision
+//     (+ VCPCU_SLICES_FAST_RADIUS: fewer radius GEMMs, see include/vcpcuda.h)
 // VCPCU_FORM_PLAIN reproduces pidblas bit for bit over a sequential-chain
 // BLAS; the Ozaki forms enclose the same products on the tensor cores.
 // Non-zero statuses become vcp::dimension_error (bad shapes) or

@@ -49,6 +49,18 @@ extern "C" {
 #define VCPCU_FORM_AUTO  2   /* autotuned choice of form and slice count            */
 #define VCPCU_FORM_OZAKI_SLICES 3 /* tensor cores, midpoint by triangular slice pairs */
 
+/* Added to `slices` of VCPCU_FORM_OZAKI (0x100 + s, or 0x100 alone for the
+ * default s): the two radius products leave out the pair of the two low
+ * digits of their 2-digit factors and add its Cauchy-Schwarz bound instead
+ * (6 bf16 GEMMs instead of 8; the default runs all four pairs).  It costs
+ * about 4e-5 of the enclosure width where the magnitudes of a row / column
+ * of the radius factors lie within one binade, 4e-4 where they spread over
+ * 2^16 and up to 3 % over 2^64, and up to a fifth of the radius term where
+ * most entries lie some 2^7 below their row's largest (R [A] with A near
+ * the identity): FORM_AUTO takes it where a probe finds it no wider than
+ * the plain form. */
+#define VCPCU_SLICES_FAST_RADIUS 0x100
+
 /* ---- diagnostics ----------------------------------------------------------- */
 
 /* Text of the last error raised on the calling host thread ("" if none). */
@@ -148,7 +160,8 @@ int vcpcu_udmatmul_ozaki(int m, int n, int k, const double* A, const double* B,
  *     0 = default 8, w = 56); their product is exact, from residues modulo
  *     up to 16 moduli <= 256 (one bf16 GEMM each, Chinese remaindering);
  *     the rounding of the midpoints to w bits, the radius term (upward bf16
- *     digit slices) and the final roundings are bounded upward.  Requires
+ *     digit slices, see VCPCU_SLICES_FAST_RADIUS) and the final roundings
+ *     are bounded upward.  Requires
  *     finite inputs (NaN results and VCPCU_ERR_NONFINITE otherwise) and
  *     16-byte aligned A and B.
  *   form == VCPCU_FORM_OZAKI_SLICES: as OZAKI, but the midpoint product is
@@ -307,7 +320,8 @@ int vcpcu_autotune(void* stream, double* constants);
 /* The AUTO decision for a product C = [A] [B] (A m x k, B k x n, kv layout,
  * host or device pointers): *form = VCPCU_FORM_PLAIN or VCPCU_FORM_OZAKI
  * and *slices the tensor-core slice count, chosen per (inner dimension,
- * exponent spread, radius size) as the smallest of 6, 7, 8, 9 whose
+ * exponent spread, radius size) as the first of 6, 7, 8, 9 with
+ * VCPCU_SLICES_FAST_RADIUS added, then 8 and 9 without it, whose
  * enclosures a probe finds no wider than the plain form's -- the probe
  * multiplies a block of up to 64 rows of A and up to 64 evenly spaced
  * columns of B in the plain form and at every candidate and compares the

@@ -162,8 +162,9 @@ def dd_residual(m, n, k, A, B, C, rows, cols, threads=0):
 def ozaki_igemm(m, n, k, A, B, s=8, sr=2, crt=True):
     """Host model of the Ozaki-form interval product (kv buffers, GEMM
     naming): crt=True the CRT form (GPU form OZAKI), crt=False the slice form
-    (GPU form OZAKI_SLICES).  Returns (C kv buffer, status) -- status 3 on
-    non-finite input."""
+    (GPU form OZAKI_SLICES).  s may carry the fast-radius flag 0x100 (as
+    the GPU form's slices argument).  Returns (C kv buffer, status) --
+    status 3 on non-finite input."""
     C_ = np.zeros(2 * m * n, dtype=np.float64)
     fn = lib().orc_ozaki2_igemm if crt else lib().orc_ozaki_igemm
     st = fn(m, n, k, _p(A) if k > 0 else None, _p(B) if k > 0 else None, _p(C_), int(s), int(sr))

@@ -13,8 +13,10 @@
  *    pddblas_assist::split_row/split_col (vcp/pddblas.hpp:82-154);
  *  - digits: N = x 2^(8s-E) rounded (nearest-even; upward for the radius
  *    factors) and written as s balanced base-256 digits in [-128, 128];
- *  - products: pairs (p, q) with p + q <= s + 1 (midpoint; all pairs for
- *    the radius factors) in ascending t = p + q, each split into chunks of
+ *  - products: pairs (p, q) with p + q <= s + 1 (midpoint; for the radius
+ *    factors all pairs, or p + q <= 3 in the CRT form with the fast-radius
+ *    flag and sr = 2: the pair of the two low digits left out) in ascending
+ *    t = p + q, each split into chunks of
  *    1024 inner indices; chunk sums are folded into the int64 value
  *    W = sum C_t 2^(8 (t_ref - t)) every 64 chunks and at the end of each
  *    t (right shifts floor) -- the accumulation order of the reference's
@@ -24,8 +26,13 @@
  *    RU(beta/2)), T = RU(RU((S'+R') u') + RU((S''+R'') u''));
  *  - radius products: S = RU(chunk 2^(8 (t_ref - t)) + S) in fp32 over the
  *    digit pairs (t ascending, p ascending) and their exact chunk sums, in
- *    order (an upper bound of the exact W; the slice GEMM epilogue's
- *    single-rounding FMA chain, one fold per product and tile).
+ *    order (the slice GEMM epilogue's single-rounding FMA chain, one fold
+ *    per product and tile); CRT form with the fast-radius flag (s + 0x100):
+ *    the left-out low x low pair,
+ *    sum_k lo_A lo_B 2^(8 (t_ref - 4)) with t_ref = 3, is bounded by Cauchy-
+ *    Schwarz, b = RU(RU(sqrt(RU(QA_i))) 2^-8 RU(sqrt(RU(QB_j)))) with QA_i,
+ *    QB_j the row's / column's sums of squared low digits (RU in fp32), and
+ *    S becomes RU(S + b).
  */
 #include <fenv.h>
 #include <math.h>
@@ -252,6 +259,33 @@ static float i64_to_float_ru(long long v) {
   return f;
 }
 
+/* fp32 operations rounded upward (operands and result through volatiles, as
+   for the double ones) */
+static float fadd_ru(float a, float b) {
+  volatile float x = a, y = b;
+  fesetround(FE_UPWARD);
+  volatile float r = x + y;
+  fesetround(FE_TONEAREST);
+  return r;
+}
+static float fmul_ru(float a, float b) {
+  volatile float x = a, y = b;
+  fesetround(FE_UPWARD);
+  volatile float r = x * y;
+  fesetround(FE_TONEAREST);
+  return r;
+}
+/* RU(sqrt(RU(Q))) scale for a sum Q >= 0 of squared digits (0 for Q = 0),
+   scale a power of two (exact) */
+static float lowpair_root(long long Q, float scale) {
+  if (Q == 0) return 0.0f;
+  volatile float q = i64_to_float_ru(Q);
+  fesetround(FE_UPWARD);
+  volatile float r = sqrtf(q);
+  fesetround(FE_TONEAREST);
+  return r * scale;
+}
+
 /* CRT form: integer bits w per operand for precision parameter s (w = 7 s,
  * lowered while 16 moduli cannot hold K 2^(2w-1)); the moduli are those of
  * the GPU form (pairwise coprime, <= 256). */
@@ -314,6 +348,13 @@ static void big_to_dir(unsigned __int128 mag, int neg, int e, double* lo, double
  */
 static int ozaki_model(int m, int n, int k, const double* A, const double* B, double* Cout,
                        int s, int sr, int crt) {
+  /* s + 0x100: fast radius products (CRT form: the low x low digit pair left
+     out and bounded) */
+  const int fast_rad = (s & 0x100) != 0;
+  s &= ~0x100;
+  if (s <= 0) s = 8;
+  const int lowb = crt && fast_rad; /* the low x low radius pair left out and bounded */
+  if (lowb && sr != 2) return 2;      /* the bound is written for sr = 2 */
   const int prev = fegetround();
   fesetround(FE_TONEAREST);
   const int Kp = k <= 0 ? 64 : (k + 63) / 64 * 64;
@@ -335,6 +376,7 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
   int* Ep = malloc(sizeof(int) * m);
   int* Er = malloc(sizeof(int) * m);
   long long* delta = calloc(m, sizeof(long long));
+  long long* QA = calloc(2 * (size_t)m, sizeof(long long)); /* sum_k lo^2: P, rA per row */
   /* digits stored as int16 in [-128, 128]: planes [p][i][Kp] */
   int16_t* dAm = calloc((size_t)s * m * Kp, sizeof(int16_t));
   int16_t* dAp = calloc((size_t)sr * m * Kp, sizeof(int16_t));
@@ -363,10 +405,12 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
       if (Ep[i] != OZ_ZERO_EXP && pA[t] != 0.0) {
         oz_digits(oz_scaled_int(pA[t], Ep[i], sr, 1), sr, d);
         for (int q = 0; q < sr; ++q) dAp[((size_t)q * m + i) * Kp + p] = (int16_t)d[q];
+        QA[2 * i] += (long long)d[sr - 1] * d[sr - 1];
       }
       if (Er[i] != OZ_ZERO_EXP && rA[t] != 0.0) {
         oz_digits(oz_scaled_int(rA[t], Er[i], sr, 1), sr, d);
         for (int q = 0; q < sr; ++q) dAr[((size_t)q * m + i) * Kp + p] = (int16_t)d[q];
+        QA[2 * i + 1] += (long long)d[sr - 1] * d[sr - 1];
       }
     }
   }
@@ -398,6 +442,7 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
   int16_t* dBm = calloc((size_t)s * n * Kp, sizeof(int16_t));
   int16_t* dBr = calloc((size_t)sr * n * Kp, sizeof(int16_t));
   int16_t* dBs = calloc((size_t)sr * n * Kp, sizeof(int16_t));
+  long long* QB = calloc(2 * (size_t)n, sizeof(long long)); /* sum_k lo^2: rB, |mB| per column */
   double* mcol = malloc(sizeof(double) * (k > 0 ? k : 1));
   double* rcol = malloc(sizeof(double) * (k > 0 ? k : 1));
   for (int j = 0; j < n; ++j) {
@@ -438,10 +483,12 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
         }
         oz_digits(oz_scaled_int(fabs(mcol[p]), Fm[j], sr, 1), sr, d);
         for (int q = 0; q < sr; ++q) dBs[((size_t)q * n + j) * Kp + p] = (int16_t)d[q];
+        QB[2 * j + 1] += (long long)d[sr - 1] * d[sr - 1];
       }
       if (Fr[j] != OZ_ZERO_EXP && rcol[p] != 0.0) {
         oz_digits(oz_scaled_int(rcol[p], Fr[j], sr, 1), sr, d);
         for (int q = 0; q < sr; ++q) dBr[((size_t)q * n + j) * Kp + p] = (int16_t)d[q];
+        QB[2 * j] += (long long)d[sr - 1] * d[sr - 1];
       }
     }
     /* CRT form: beta_j = RU((sum_k |B'| + ceil(K/2)) 2^(F - w)) >= sum_k |mB|,
@@ -454,7 +501,7 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
   }
   pairlist pm, pr;
   build_pairs(s, s, 1, &pm);
-  build_pairs(sr, sr, 0, &pr);
+  build_pairs(sr, sr, lowb, &pr);
   int tm, Rm, trr, Rr;
   choose_scaling(&pm, nchunks, &tm, &Rm);
   choose_scaling(&pr, nchunks, &trr, &Rr);
@@ -518,7 +565,10 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
         const int ex[2] = {Ep[i] + Fr[j] - 8 * trr, Er[i] + Fm[j] - 8 * trr};
         for (int w = 0; w < 2; ++w) {
           if (zz[w]) continue;
-          const float sv = Rr ? i64_to_float_ru((long long)Sr[w] + Rr) : Sr[w];
+          float sv = Rr ? i64_to_float_ru((long long)Sr[w] + Rr) : Sr[w];
+          if (lowb) /* the left-out low x low pair */
+            sv = fadd_ru(sv, fmul_ru(lowpair_root(QA[2 * i + w], 0x1p-8f),
+                                     lowpair_root(QB[2 * j + w], 1.0f)));
           if (sv > 0.0f) bb[w] = scale_dir((double)sv, ex[w], 1);
         }
         T = add_dir(bb[0], bb[1], FE_UPWARD);
@@ -555,7 +605,7 @@ static int ozaki_model(int m, int n, int k, const double* A, const double* B, do
       Cout[2 * ((size_t)i + (size_t)j * m) + 1] = up;
     }
   }
-  free(mA); free(rA); free(pA); free(Em); free(Ep); free(Er); free(delta);
+  free(mA); free(rA); free(pA); free(Em); free(Ep); free(Er); free(delta); free(QA); free(QB);
   free(dAm); free(dAp); free(dAr); free(Fm); free(Fr); free(beta);
   free(dBm); free(dBr); free(dBs); free(mcol); free(rcol);
   free(Ai); free(Ahi); free(Alo); free(Bi);
@@ -575,4 +625,4 @@ int orc_ozaki2_igemm(int m, int n, int k, const double* A, const double* B, doub
   return ozaki_model(m, n, k, A, B, Cout, s, sr, 1);
 }
 
-int orc_ozaki_model_version(void) { return 3; }
+int orc_ozaki_model_version(void) { return 4; }

@@ -3,9 +3,12 @@ product is bit-identical to the product in the form and slice count the
 autotuner picks (vcpcu_autotune_pick), for single products and for a batch
 that mixes both forms; over inner dimensions {2048, 8192}, exponent spreads
 {0, 8, 32} and radius ratios {0, 2^-40, 2^-20} the AUTO enclosures are never
-wider than the plain form's (the tuner falls back to the plain form where no
-slice count qualifies: a 2^64 exponent spread at k = 2048, radii of 2^-20),
-and the picks are the ones the host models give for the same probe."""
+wider than the plain form's (the tuner takes the fast radius products where
+they qualify, the exact ones at spread 8 with radii 2^-40 and k = 2048,
+where the fast ones leave less margin than its rule asks, and falls back to
+the plain form where no slice count qualifies: a 2^64 exponent spread at
+k = 2048, radii of 2^-20), and the picks are the ones the host models give
+for the same probe."""
 import numpy as np
 import pytest
 
@@ -68,12 +71,13 @@ def test_auto_batch_mixes_forms(cuda_lib):
 # (k, phi, radius ratio) -> slice count the probe picks (0: plain form); the
 # host models of both forms give these picks for the probe's rows 96..159 and
 # columns 0, 4, .., 252 of these seeded 256 x 256 products.
-AUTO_PICKS = {(2048, 0, 0.0): 8, (2048, 0, 2.0 ** -40): 8, (2048, 0, 2.0 ** -20): 0,
-              (2048, 8, 0.0): 8, (2048, 8, 2.0 ** -40): 8, (2048, 8, 2.0 ** -20): 0,
+F8 = 8 | pidcuda.SLICES_FAST_RADIUS
+AUTO_PICKS = {(2048, 0, 0.0): F8, (2048, 0, 2.0 ** -40): F8, (2048, 0, 2.0 ** -20): 0,
+              (2048, 8, 0.0): F8, (2048, 8, 2.0 ** -40): 8, (2048, 8, 2.0 ** -20): 0,
               (2048, 32, 0.0): 0, (2048, 32, 2.0 ** -40): 0, (2048, 32, 2.0 ** -20): 0,
-              (8192, 0, 0.0): 8, (8192, 0, 2.0 ** -40): 8, (8192, 0, 2.0 ** -20): 0,
-              (8192, 8, 0.0): 8, (8192, 8, 2.0 ** -40): 8, (8192, 8, 2.0 ** -20): 0,
-              (8192, 32, 0.0): 8, (8192, 32, 2.0 ** -40): 0, (8192, 32, 2.0 ** -20): 0}
+              (8192, 0, 0.0): F8, (8192, 0, 2.0 ** -40): F8, (8192, 0, 2.0 ** -20): 0,
+              (8192, 8, 0.0): F8, (8192, 8, 2.0 ** -40): F8, (8192, 8, 2.0 ** -20): 0,
+              (8192, 32, 0.0): F8, (8192, 32, 2.0 ** -40): 0, (8192, 32, 2.0 ** -20): 0}
 
 
 @pytest.mark.parametrize("case", sorted(AUTO_PICKS), ids=lambda c: f"k{c[0]}-phi{c[1]}-r{c[2]:.0e}")
@@ -104,4 +108,4 @@ def test_auto_pick_same_from_host_and_device_pointers(cuda_lib):
     B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
     h = pidcuda.autotune_pick(A, B, m, n, k)
     d = pidcuda.autotune_pick(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda(), m, n, k)
-    assert h == d == (pidcuda.FORM_OZAKI, 8)
+    assert h == d == (pidcuda.FORM_OZAKI, F8)

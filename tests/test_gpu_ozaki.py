@@ -10,6 +10,10 @@
   1024-element chunks, and extreme digit patterns (chunk sums of +-2^24);
 * zero containment failures against the exact interval hull (long
   accumulator) on every checked entry;
+* with SLICES_FAST_RADIUS the CRT form's radius products leave out the pair
+  of the two low digits and the reassembly adds its Cauchy-Schwarz bound:
+  bit-identical to the model and enclosing where every low digit is 127
+  (the bound is tight);
 * enclosure no wider than the plain FP64 form at the benchmark distribution;
 * non-finite inputs give NaN results and VCPCU_ERR_NONFINITE.
 """
@@ -42,15 +46,17 @@ CASES = [(1, 1, 1, 8), (5, 7, 3, 8), (128, 256, 64, 8), (129, 257, 65, 6), (200,
 
 
 @pytest.mark.parametrize("case", CASES)
-@pytest.mark.parametrize("crt", [True, False], ids=["crt", "slices"])
+@pytest.mark.parametrize("crt", [True, False, "fast"], ids=["crt", "slices", "crt-fast-radius"])
 def test_ozaki_bitexact_model_and_encloses(cuda_lib, oracle, case, crt):
     m, n, k, s = case
     rng = np.random.default_rng(m * 7 + n * 3 + k + s)
     A = W.interval_ephi(rng, m, k, 4, 2.0 ** -40)
     B = W.interval_ephi(rng, k, n, 4, 2.0 ** -40)
     form = pidcuda.FORM_OZAKI if crt else pidcuda.FORM_OZAKI_SLICES
+    if crt == "fast":  # the low x low radius pair left out and bounded
+        s |= pidcuda.SLICES_FAST_RADIUS
     C = pidcuda.mulmm(A, B, m, n, k, form=form, slices=s)
-    ref, st = oracle.ozaki_igemm(m, n, k, A, B, s, 2, crt=crt)
+    ref, st = oracle.ozaki_igemm(m, n, k, A, B, s, 2, crt=bool(crt))
     assert st == 0
     assert np.array_equal(bits(C), bits(ref)), "GPU differs from the host model"
     check_contains(oracle, m, n, k, A, B, C)
@@ -101,6 +107,18 @@ def test_ozaki_zero_rows_and_columns(cuda_lib, oracle):
     C = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=8)
     ref, _ = oracle.ozaki_igemm(m, n, k, A, B, 8, 2)
     assert np.array_equal(bits(C), bits(ref))
+    check_contains(oracle, m, n, k, A, B, C)
+
+
+@pytest.mark.parametrize("fast", [pidcuda.SLICES_FAST_RADIUS, 0], ids=["bound", "exact"])
+@pytest.mark.parametrize("side", [0, 1])
+def test_ozaki_low_pair_bound(cuda_lib, oracle, side, fast):
+    from test_ozaki_model import low127_operands
+    m, n, k = (24, 20, 3000) if side == 0 else (20, 24, 2100)
+    A, B = low127_operands(side, m, n, k)
+    C = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI, slices=8 | fast)
+    ref, st = oracle.ozaki_igemm(m, n, k, A, B, 8 | fast, 2)
+    assert st == 0 and np.array_equal(bits(C), bits(ref))
     check_contains(oracle, m, n, k, A, B, C)
 
 

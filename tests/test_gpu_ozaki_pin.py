@@ -127,10 +127,13 @@ def test_long_inner_dimension_bitexact_model(cuda_lib, oracle, m, n, k):
 # plain form there.  Elsewhere the digits of the radius factors (16 bits
 # relative to the row / column maximum) or the 2^-56 operand truncation at
 # a 2^64 exponent spread can exceed the plain form's own rounding by a few
-# percent; those cases are bounded by the factor 2.
+# percent; those cases are bounded by the factor 2.  NOT_WIDER_FAST: the
+# same with the fast radius products (the bound of their left-out low x low
+# digit pair adds up to 3 % at the 2^64 spread).
 NOT_WIDER = {(2048, 0, 0.0), (2048, 0, 2.0 ** -40), (2048, 8, 0.0), (2048, 8, 2.0 ** -40),
              (8192, 0, 0.0), (8192, 0, 2.0 ** -40), (8192, 8, 0.0), (8192, 8, 2.0 ** -40),
              (8192, 32, 0.0), (8192, 32, 2.0 ** -40)}
+NOT_WIDER_FAST = NOT_WIDER - {(8192, 32, 2.0 ** -40)}
 
 
 @pytest.mark.parametrize("k", [2048, 8192])
@@ -150,3 +153,10 @@ def test_width_against_plain(cuda_lib, k, phi, rr):
     assert np.max(ratio) <= 2.0, float(np.max(ratio))
     if (k, phi, rr) in NOT_WIDER:
         assert np.all(wo <= wp), float(np.max(ratio))
+    Cf = pidcuda.mulmm(A, B, m, n, k, form=pidcuda.FORM_OZAKI,
+                       slices=8 | pidcuda.SLICES_FAST_RADIUS)
+    wf = Cf[1::2] - Cf[0::2]
+    assert np.max(wf / wp) <= 2.0, float(np.max(wf / wp))
+    assert np.all(wf >= wo)  # the bound of the left-out pair only adds
+    if (k, phi, rr) in NOT_WIDER_FAST:
+        assert np.all(wf <= wp), float(np.max(wf / wp))

@@ -2,7 +2,8 @@
 //
 // VCPCU_FORM_AUTO runs the form with the smaller predicted time:
 //   plain  t = 8 m n k / fp64_rate + t_launch
-//   Ozaki  t = (L + 8) 2 Mp Np Kp / tc_rate            (slice GEMMs; L moduli)
+//   Ozaki  t = (L + 6) 2 Mp Np Kp / tc_rate            (slice GEMMs; L moduli,
+//                                                       2 x 3 radius digit pairs)
 //            + 16 (m k + k n) / prep_bw + 12 t_launch    (operand preparation)
 // with the constants measured on this device by vcpcu_autotune (timing one
 // plain and two Ozaki products), kept for the process and optionally stored
@@ -11,8 +12,11 @@
 //
 // When the tensor-core form is the faster one, autotune_pick also chooses
 // its slice count from the operands: the smallest s in {6, 7, 8, 9}
-// (w = 42, 49, 56, 62 bit midpoints) whose enclosures are no wider than the
-// plain form's, else the plain form itself.  The choice is made per key
+// (w = 42, 49, 56, 62 bit midpoints) with the fast radius products
+// (VCPCU_SLICES_FAST_RADIUS: two bf16 GEMMs fewer) whose enclosures are no
+// wider than the plain form's, then s = 8, 9 with the exact radius products
+// (for radius factors whose magnitudes spread over many binades), else the
+// plain form itself.  The choice is made per key
 // (ceil log2 k, exponent spread of the rows of A plus the columns of B in
 // steps of 4, radius-to-midpoint exponent in steps of 4), on a probe: a
 // block of up to 64 rows of A and up to 64 evenly spaced columns of B,
@@ -181,7 +185,7 @@ int autotune_choose(int m, int n, int k, bool batched) {
                Kp = std::ceil((k > 0 ? k : 1) / 64.0) * 64.0;
   OzPlan plan;
   oz_make_plan(m, n, k, 8, 2, &plan, 1);
-  const double gemms = plan.pb.L + 8.0;
+  const double gemms = plan.pb.L + 2.0 * plan.rad.npairs;
   const double to = gemms * 2.0 * Mp * Np * Kp / md.tc_rate +
                     16.0 * ((double)m * k + (double)k * n) / md.prep_bw + 12.0 * tl;
   return to < tp ? VCPCU_FORM_OZAKI : VCPCU_FORM_PLAIN;
@@ -194,14 +198,19 @@ int autotune_pick(int m, int n, int k, const double* A, long lda, const double* 
   if (*form == VCPCU_FORM_PLAIN || m <= 0 || n <= 0 || k <= 0) return VCPCU_OK;
   const int Sr = m < 64 ? m : 64, Sc = n < 64 ? n : 64;
   const int i0 = (m - Sr) / 2, cstride = n / Sc;
+  // candidates in order of cost: s = 6, 7, 8, 9 with the fast radius
+  // products, then 8 and 9 with the exact ones
+  constexpr int NCAND = 6;
+  const int cand[NCAND] = {6 | OZ_FAST_RADIUS, 7 | OZ_FAST_RADIUS, 8 | OZ_FAST_RADIUS,
+                           9 | OZ_FAST_RADIUS, 8, 9};
   const size_t na = 2 * (size_t)Sr * k, nb = 2 * (size_t)k * Sc, nc = 2 * (size_t)Sr * Sc;
   Scratch buf;
-  int st = buf.alloc(sizeof(double) * (na + nb + 5 * nc) + 64, s);
+  int st = buf.alloc(sizeof(double) * (na + nb + (NCAND + 1) * nc) + 64, s);
   if (st) return st;
   double* As = (double*)buf.ptr;
   double* Bs = As + na;
-  double* Cs = Bs + nb;  // plain, then s = 6, 7, 8, 9
-  int* stats = (int*)(Cs + 5 * nc);
+  double* Cs = Bs + nb;  // plain, then the candidates
+  int* stats = (int*)(Cs + (NCAND + 1) * nc);
   VCPCU_CUDA_TRY(cudaMemcpy2DAsync(As, Sr * 16, A + 2 * (size_t)i0, lda * 16, Sr * 16, k,
                                    cudaMemcpyDefault, s));
   for (int c = 0; c < Sc; ++c)  // column c * cstride of B (contiguous)
@@ -230,17 +239,16 @@ int autotune_pick(int m, int n, int k, const double* A, long lda, const double* 
   }
   // probe: the plain form and every candidate on the sampled block
   if ((st = igemm_any(Sr, Sc, k, As, Sr, Bs, k, Cs, Sr, VCPCU_FORM_PLAIN, 0, s))) return st;
-  const int cand[4] = {6, 7, 8, 9};
-  for (int c = 0; c < 4; ++c)
+  for (int c = 0; c < NCAND; ++c)
     if ((st = ozaki_igemm(Sr, Sc, k, As, Sr, Bs, k, Cs + (c + 1) * nc, Sr, VCPCU_FORM_OZAKI,
                           cand[c], s)))
       return st;
-  std::vector<double> hc(5 * nc);
-  VCPCU_CUDA_TRY(cudaMemcpyAsync(hc.data(), Cs, sizeof(double) * 5 * nc, cudaMemcpyDeviceToHost,
-                                 s));
+  std::vector<double> hc((NCAND + 1) * nc);
+  VCPCU_CUDA_TRY(cudaMemcpyAsync(hc.data(), Cs, sizeof(double) * (NCAND + 1) * nc,
+                                 cudaMemcpyDeviceToHost, s));
   VCPCU_CUDA_TRY(cudaStreamSynchronize(s));
   int choice = 0;
-  for (int c = 0; c < 4 && !choice; ++c) {
+  for (int c = 0; c < NCAND && !choice; ++c) {
     std::vector<double> r;
     r.reserve(nc / 2);
     const double* P = hc.data();
@@ -300,12 +308,12 @@ extern "C" int vcpcu_autotune(void* stream, double* constants) {
   const double t3 = time_call(n3, n3, n3, VCPCU_FORM_OZAKI, A, B, C, s, 3);
   Model m;
   m.fp64_rate = 8.0 * n1 * (double)n1 * n1 / tp;
-  // Ozaki: t = a * work + b, work = (L + 8) 2 n^3 (K multiple of the tiles here)
+  // Ozaki: t = a * work + b, work = (L + 6) 2 n^3 (K multiple of the tiles here)
   OzPlan p2, p3;
   oz_make_plan(n2, n2, n2, 8, 2, &p2, 1);
   oz_make_plan(n3, n3, n3, 8, 2, &p3, 1);
-  const double w2 = (p2.pb.L + 8.0) * 2.0 * n2 * (double)n2 * n2;
-  const double w3 = (p3.pb.L + 8.0) * 2.0 * n3 * (double)n3 * n3;
+  const double w2 = (p2.pb.L + 2.0 * p2.rad.npairs) * 2.0 * n2 * (double)n2 * n2;
+  const double w3 = (p3.pb.L + 2.0 * p3.rad.npairs) * 2.0 * n3 * (double)n3 * n3;
   double a = (t3 - t2) / (w3 - w2);
   if (!(a > 0)) a = t3 / w3;
   double b = t2 - a * w2;

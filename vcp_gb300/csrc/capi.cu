@@ -127,9 +127,11 @@ int igemm_check(int m, int n, int k, const double* A, int lda, const double* B, 
     set_error("igemm: unknown form %d", form);
     return VCPCU_ERR_INVALID_ARG;
   }
-  if ((form == VCPCU_FORM_OZAKI || form == VCPCU_FORM_OZAKI_SLICES) && slices != 0 &&
-      (slices < 2 || slices > OZ_MAX_SLICES)) {
-    set_error("igemm: slices must be 0 or in [2, %d], got %d", OZ_MAX_SLICES, slices);
+  const int sc = oz_slice_count(slices);
+  if ((form == VCPCU_FORM_OZAKI || form == VCPCU_FORM_OZAKI_SLICES) && sc != 0 &&
+      (sc < 2 || sc > OZ_MAX_SLICES)) {
+    set_error("igemm: slices must be 0 or in [2, %d] (optionally + VCPCU_SLICES_FAST_RADIUS), "
+              "got %d", OZ_MAX_SLICES, slices);
     return VCPCU_ERR_INVALID_ARG;
   }
   if (m <= 0 || n <= 0) return VCPCU_OK;
@@ -186,8 +188,10 @@ int form_check(int form, int slices) {
     set_error("unknown form %d", form);
     return VCPCU_ERR_INVALID_ARG;
   }
-  if (form != VCPCU_FORM_PLAIN && slices != 0 && (slices < 2 || slices > OZ_MAX_SLICES)) {
-    set_error("slices must be 0 or in [2, %d], got %d", OZ_MAX_SLICES, slices);
+  const int sc = oz_slice_count(slices);
+  if (form != VCPCU_FORM_PLAIN && sc != 0 && (sc < 2 || sc > OZ_MAX_SLICES)) {
+    set_error("slices must be 0 or in [2, %d] (optionally + VCPCU_SLICES_FAST_RADIUS), got %d",
+              OZ_MAX_SLICES, slices);
     return VCPCU_ERR_INVALID_ARG;
   }
   return VCPCU_OK;

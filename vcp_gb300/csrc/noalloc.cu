@@ -69,8 +69,10 @@ extern "C" int vcpcu_igemm_noalloc_dev(int m, int n, int k, const double* A, int
                                        const double* B, int ldb, double* C, int ldc,
                                        int slices, void* stream) {
   clear_error();
-  if (slices != 0 && (slices < 2 || slices > OZ_MAX_SLICES)) {
-    set_error("igemm_noalloc: slices must be 0 or in [2, %d], got %d", OZ_MAX_SLICES, slices);
+  const int sc = oz_slice_count(slices);
+  if (sc != 0 && (sc < 2 || sc > OZ_MAX_SLICES)) {
+    set_error("igemm_noalloc: slices must be 0 or in [2, %d] (optionally + "
+              "VCPCU_SLICES_FAST_RADIUS), got %d", OZ_MAX_SLICES, slices);
     return VCPCU_ERR_INVALID_ARG;
   }
   if (m <= 0 || n <= 0) return VCPCU_OK;
@@ -89,7 +91,7 @@ extern "C" int vcpcu_igemm_noalloc_dev(int m, int n, int k, const double* A, int
     return VCPCU_ERR_INVALID_ARG;
   }
   OzPlan plan;
-  oz_make_plan(m, n, k, slices > 0 ? slices : 8, 2, &plan, /*crt=*/1);
+  oz_make_plan(m, n, k, slices, 2, &plan, /*crt=*/1);
   const size_t need = oz_workspace_bytes(plan.pb);
   if (need > (size_t)VCPCU_NOALLOC_SCRATCH_BYTES) {
     set_error("igemm_noalloc: %d x %d x %d with %d slices needs %zu bytes of scratch, more than "

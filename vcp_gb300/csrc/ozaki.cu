@@ -50,11 +50,15 @@ void build_pairs(int sa, int sb, bool triangular, OzPairList* pl) {
   pl->ngroups = g;
 }
 
-// The radius products' pairs: all sr x sr digit pairs in one group (t
-// ascending, p ascending), each pair weighted by 2^(8 (t_ref - t)) in the
-// epilogue's fp32 upward sum; gt of the group is the largest t.
-void radius_pairs(int sr, OzPairList* pl) {
-  build_pairs(sr, sr, false, pl);
+// The radius products' pairs in one group (t ascending, p ascending), each
+// pair weighted by 2^(8 (t_ref - t)) in the epilogue's fp32 upward sum; gt
+// of the group is the largest t.  low_out (CRT form with OZ_FAST_RADIUS,
+// sr = 2): the pairs with t <= 3 -- the pair of the two low digits is left
+// out and bounded in the reassembly (sum_k lo_A lo_B <= sqrt(sum lo_A^2)
+// sqrt(sum lo_B^2), weight 2^-8 against t_ref = 3): three tensor-core
+// products per radius product instead of four.  Else all sr x sr pairs.
+void radius_pairs(int sr, bool low_out, OzPairList* pl) {
+  build_pairs(sr, sr, low_out, pl);
   pl->gt[0] = pl->gt[pl->ngroups - 1];
   pl->gstart[1] = (int16_t)pl->npairs;
   pl->ngroups = 1;
@@ -238,8 +242,13 @@ int crt_setup(int K, int w, OzPlan* plan) {
   return 0;
 }
 
+static_assert(OZ_FAST_RADIUS == VCPCU_SLICES_FAST_RADIUS, "slices flag of the C ABI");
+
 int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan, int crt) {
   memset(plan, 0, sizeof(*plan));
+  const bool fast_rad = (s & OZ_FAST_RADIUS) != 0;
+  s = oz_slice_count(s);
+  if (s <= 0) s = 8;
   OzProblem& pb = plan->pb;
   pb.M = M;
   pb.N = N;
@@ -250,7 +259,8 @@ int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan, int crt) {
   pb.s = s;
   pb.sr = sr;
   build_pairs(s, s, true, &plan->mid);
-  radius_pairs(sr, &plan->rad);
+  plan->rad_lowb = crt != 0 && fast_rad;
+  radius_pairs(sr, plan->rad_lowb != 0, &plan->rad);
   pb.mplanes = s;
   if (crt) {
     pb.crt = 1;
@@ -286,6 +296,7 @@ OzRadConst oz_rad_const(const OzPlan& plan) {
   rc.run2 = !(plan.point_mask & 1);
   rc.t_ref = plan.t_ref_rad;
   rc.R = plan.R_rad;
+  rc.lowb = plan.rad_lowb;
   return rc;
 }
 
@@ -312,8 +323,8 @@ size_t oz_workspace_bytes(const OzProblem& pb) {
   b += al256(sizeof(int) * 4);
   b += 2 * al256(sizeof(double) * (size_t)pb.M * (pb.K > 0 ? pb.K : 1));
   b += 2 * al256(sizeof(double) * (size_t)pb.Np * pb.Kp);
-  if (pb.crt) b += al256(sizeof(unsigned long long) * 2 * pb.Np);
-  b += al256(sizeof(unsigned long long) * 2 * pb.Mp);
+  if (pb.crt) b += al256(sizeof(unsigned long long) * 4 * pb.Np);
+  b += al256(sizeof(unsigned long long) * 4 * pb.Mp);
   if (pb.crt) b += al256((size_t)pb.L * pb.Np * pb.Mp);
   return b;
 }
@@ -366,10 +377,10 @@ int oz_carve_workspace(const OzProblem& pb, void* base, OzWorkspace* ws) {
   ws->bsum = nullptr;
   if (pb.crt) {
     ws->bsum = (unsigned long long*)p;
-    p += al256(sizeof(unsigned long long) * 2 * pb.Np);
+    p += al256(sizeof(unsigned long long) * 4 * pb.Np);
   }
   ws->asum = (unsigned long long*)p;
-  p += al256(sizeof(unsigned long long) * 2 * pb.Mp);
+  p += al256(sizeof(unsigned long long) * 4 * pb.Mp);
   ws->res = pb.crt ? (uint8_t*)p : nullptr;
   return VCPCU_OK;
 }
@@ -586,9 +597,10 @@ int ozaki_igemm_host_pipelined(int m, int n, int k, const double* A, const doubl
     v.rowmax = ws.rowmax + 3 * (size_t)i0;
     v.E3 = ws.E3 + 3 * (size_t)i0;
     v.delta = ws.delta + i0;
-    v.asum = ws.asum + 2 * (size_t)i0;
+    v.asum = ws.asum + 4 * (size_t)i0;
     v.F2 = ws.F2 + 2 * (size_t)j0;
     v.beta = ws.beta + j0;
+    v.bsum = ws.bsum + 4 * (size_t)j0;
     const bool odd = (nblk++ & 1) != 0;
     cudaStream_t c = odd ? c1 : c0;
     if (odd) {

@@ -7,6 +7,11 @@
 namespace vcpcu {
 
 constexpr int OZ_MAX_SLICES = 12;
+// Flag in a `slices` argument: radius products without their low x low
+// digit pair, which the reassembly bounds (VCPCU_SLICES_FAST_RADIUS).
+constexpr int OZ_FAST_RADIUS = 0x100;
+// The slice count of a `slices` argument without the flag (0: default).
+inline int oz_slice_count(int slices) { return slices & ~OZ_FAST_RADIUS; }
 constexpr int OZ_MAX_RSLICES = 4;
 constexpr int OZ_MAX_PAIRS = 80;
 constexpr int OZ_MAX_GROUPS = 32;
@@ -32,11 +37,13 @@ struct OzWorkspace {
   unsigned long long* delta;          // [Mp] sum of |midpoint digits| per row
   int* F2;                            // [Np][2] exponents Fm, Fr
   double* beta;                       // [Np] sum_k |mB(k,j)| rounded up
-  unsigned long long* asum;           // [Mp][2] CRT form: sum_k |A'(i,k)| as (bits >= 32, bits < 32)
+  unsigned long long* asum;           // [Mp][4] CRT form: sum_k |A'(i,k)| as (bits >= 32, bits < 32);
+                                      // sum_k lo^2 of the low radius digits of P, of rA
   uint8_t* res;                       // [L][Np][Mp] CRT form: residues of A'B' mod m_l
   double *midA, *radA;                // [K][M] midpoints / radii of A (column-major)
   double *midB, *radB;                // [Np][Kp] midpoints / radii of B (k contiguous)
-  unsigned long long* bsum;           // [Np][2] CRT form: sum_k |B'(k,j)| as (bits >= 32, bits < 32)
+  unsigned long long* bsum;           // [Np][4] CRT form: sum_k |B'(k,j)| as (bits >= 32, bits < 32);
+                                      // sum_k lo^2 of the low radius digits of rB, of |mB|
   double* T;                          // [N][Mp] upper bound of the radius product (slice form)
   long long* W;                       // [Np][Mp] int64 fold buffer (slice form)
   int32_t* P;                         // [2 slots][Np][Mp] fp32 folds (bits) of the two radius products
@@ -119,6 +126,9 @@ struct OzPlan {
   // Folds of one radius product: one fp32 upper bound per (product, tile),
   // the epilogue's weighted upward sum of all its digit pairs (rad_slots = 1).
   int rad_slots;
+  // 1: the radius products leave out the pair of the two low digits (CRT
+  // form with OZ_FAST_RADIUS); the reassembly adds its bound.
+  int rad_lowb;
 };
 
 // The radius bound T(i, j) from the folds of the two radius products (the
@@ -127,6 +137,8 @@ struct OzRadConst {
   int nslot;                    // folds per product (slots [0, n) and [n, 2n))
   int run1, run2;               // which products ran (zero-radius operands skip)
   int t_ref, R;
+  int lowb;                     // 1: the pair of the two low digits was left out of
+                                // both products; T adds its Cauchy-Schwarz bound
 };
 OzRadConst oz_rad_const(const OzPlan& plan);
 // Slice form: T from the folds into ws.T (the CRT form's reassembly
@@ -134,6 +146,8 @@ OzRadConst oz_rad_const(const OzPlan& plan);
 int oz_radius_T(const OzPlan& plan, const OzWorkspace& ws, cudaStream_t st);
 
 // crt != 0 selects the CRT form of the midpoint with w = 7 * s integer bits.
+// s may carry OZ_FAST_RADIUS (CRT form: the radius products leave out
+// their low x low digit pair) and is then 0 for the default 8.
 int oz_make_plan(int M, int N, int K, int s, int sr, OzPlan* plan, int crt = 0);
 int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long ldc,
                     cudaStream_t st);
@@ -252,8 +266,8 @@ struct OzGBucket {
   double* beta;            // [Ntot]
   double *midB, *radB;     // [Ntot][Kp] midrad of the stacked B columns
   double *midA, *radA;     // [Kp][Mtot] midrad of the stacked A rows (column-major)
-  unsigned long long* bsum;  // [Ntot][2] sum_k |B'| as (bits >= 32, bits < 32)
-  unsigned long long* asum;  // [Mtot][2]
+  unsigned long long* bsum;  // [Ntot][4] as OzWorkspace::bsum
+  unsigned long long* asum;  // [Mtot][4] as OzWorkspace::asum
   uint8_t* res;
   int32_t* P;
   int* flag;               // [nprob][4]: non-finite input, wait timeout

@@ -197,13 +197,23 @@ __device__ __forceinline__ void rad_folds(const int32_t* __restrict__ P, size_t 
   S2[3] = v2.w;
 }
 
-// RU((S + R) 2^ex), 0 for a zero row or column.  S + R >= the exact W + R >=
-// 0 (the digits of both radius factors are upward, so every product of
-// their reconstructions is non-negative) and is 0 or an integer >= 1: a
-// normal float, whose double is built on the integer pipe.
-__device__ __forceinline__ double rad_term(float S, bool zero, int ex, int R) {
+// RU(sqrt(RU(Q))) scale for a sum Q of squared low radius digits (0 for
+// Q = 0; scale a power of two, so the product is exact).
+__device__ __forceinline__ float lowpair_root(unsigned long long Q, float scale) {
+  return Q ? __fmul_rn(__fsqrt_ru(__ull2float_ru(Q)), scale) : 0.0f;
+}
+
+// RU(RU(S + R) + b) 2^ex, 0 for a zero row or column.  S + R >= the exact
+// W + R of the pairs that ran; b >= the left-out low x low pair (in the units
+// of W: sum_k lo_A lo_B 2^-8 <= sqrt(sum lo_A^2) sqrt(sum lo_B^2) 2^-8,
+// Cauchy-Schwarz), 0 when every pair ran.  The sum is >= 0 (the digits of
+// both radius factors are upward, so every product of their reconstructions
+// is non-negative) and is 0 or at least 2^-16: a normal float, whose double
+// is built on the integer pipe.
+__device__ __forceinline__ double rad_term(float S, bool zero, int ex, int R, float b) {
   if (zero) return 0.0;
-  const float s = R ? __fadd_ru(S, (float)R) : S;
+  float s = R ? __fadd_ru(S, (float)R) : S;
+  s = __fadd_ru(s, b);
   if (!(s > 0.0f)) return 0.0;
   const unsigned u = __float_as_uint(s);
   const double d = __longlong_as_double((long long)(((unsigned long long)((u >> 23) + 896) << 52) |
@@ -211,15 +221,16 @@ __device__ __forceinline__ double rad_term(float S, bool zero, int ex, int R) {
   return scale_pow2(d, ex, true);
 }
 
-// T = RU(RU((|mA| + rA) rB) + RU(rA |mB|)) at (i, j), the products that ran.
+// T = RU(RU((|mA| + rA) rB) + RU(rA |mB|)) at (i, j), the products that ran;
+// l1, l2 the bounds of their left-out pairs.
 __device__ __forceinline__ double rad_T(float S1, float S2, int Ep, int Er, int Fm, int Fr,
-                                        const OzRadConst& rc) {
+                                        const OzRadConst& rc, float l1, float l2) {
   const double b1 = rc.run1 ? rad_term(S1, Ep == OZ_ZERO_EXP || Fr == OZ_ZERO_EXP,
-                                       Ep + Fr - 8 * rc.t_ref, rc.R)
+                                       Ep + Fr - 8 * rc.t_ref, rc.R, l1)
                             : 0.0;
   if (!rc.run2) return b1;
   const double b2 =
-      rad_term(S2, Er == OZ_ZERO_EXP || Fm == OZ_ZERO_EXP, Er + Fm - 8 * rc.t_ref, rc.R);
+      rad_term(S2, Er == OZ_ZERO_EXP || Fm == OZ_ZERO_EXP, Er + Fm - 8 * rc.t_ref, rc.R, l2);
   return rc.run1 ? __dadd_ru(b1, b2) : b2;
 }
 
@@ -241,17 +252,19 @@ oz_radius_T_kernel(int M, int N, int Mp, size_t plane, const int32_t* __restrict
     for (int u = 0; u < 4; ++u) {
       const int i = i0 + u;
       if (i >= M) break;
-      T[e0 + u] = rad_T(W1[u], W2[u], E3[3 * i + 1], E3[3 * i + 2], Fm, Fr, rc);
+      T[e0 + u] = rad_T(W1[u], W2[u], E3[3 * i + 1], E3[3 * i + 2], Fm, Fr, rc, 0.0f, 0.0f);
     }
   }
 }
 
-// Per-row data of 4 consecutive rows: the exponents and sA = RU(sum_k
-// |A'(i,k)|) (asum_hi 2^32 + asum_lo, exact below 2^96), computed once per
+// Per-row data of 4 consecutive rows: the exponents, sA = RU(sum_k
+// |A'(i,k)|) (asum_hi 2^32 + asum_lo, exact below 2^96) and the 2^-8-scaled
+// roots of the low radius digits' squares of P and rA, computed once per
 // thread and reused for every column it assembles.
 struct QuadRows {
   int E[4], Ep[4], Er[4];
   double sA[4];
+  float qp[4], qr[4];
 };
 
 __device__ __forceinline__ void quad_rows(int i0, int M, const int* __restrict__ E3,
@@ -262,11 +275,14 @@ __device__ __forceinline__ void quad_rows(int i0, int M, const int* __restrict__
     const int i = i0 + u;
     r.E[u] = r.Ep[u] = r.Er[u] = OZ_ZERO_EXP;
     r.sA[u] = 0.0;
+    r.qp[u] = r.qr[u] = 0.0f;
     if (i >= M) continue;
     r.E[u] = E3[3 * i];
     r.Ep[u] = E3[3 * i + 1];
     r.Er[u] = E3[3 * i + 2];
-    const unsigned long long ah = asum[2 * i + 0], al = asum[2 * i + 1];
+    r.qp[u] = lowpair_root(asum[4 * i + 2], 0x1p-8f);
+    r.qr[u] = lowpair_root(asum[4 * i + 3], 0x1p-8f);
+    const unsigned long long ah = asum[4 * i + 0], al = asum[4 * i + 1];
     const unsigned __int128 sx = ((unsigned __int128)ah << 32) + al;
     if (sx) {
       double sAdn;
@@ -287,12 +303,14 @@ __device__ __forceinline__ void quad_rows(int i0, int M, const int* __restrict__
 // time, the radius folds 16 bytes, C written as 4 consecutive pairs.  Only
 // the final error sum and the two outward roundings use the FP64 pipe on the
 // common path.  res and P point at row / column 0 of this product; plane =
-// Np Mp of its layout; Fj, Frj the column's exponents, bj its beta.
+// Np Mp of its layout; Fj, Frj the column's exponents, bj its beta, qj its
+// sums of squared low radius digits (of rB and |mB|).
 __device__ __forceinline__ void assemble_quad_col(
     const QuadRows& rw, int i0, int j, int M, int Mp, int L, int w,
     const uint8_t* __restrict__ res, size_t plane, int Fj, int Frj, double bj,
-    const int32_t* __restrict__ P, double* __restrict__ C, long ldc, bool nonfinite,
-    const uint32_t (&Q)[16][4], const uint32_t (&Mm)[4], float invMf, const OzRadConst& rc) {
+    const unsigned long long* __restrict__ qj, const int32_t* __restrict__ P,
+    double* __restrict__ C, long ldc, bool nonfinite, const uint32_t (&Q)[16][4],
+    const uint32_t (&Mm)[4], float invMf, const OzRadConst& rc) {
   const size_t e0 = (size_t)j * Mp + i0;
   uint32_t pk[16];
 #pragma unroll
@@ -300,6 +318,8 @@ __device__ __forceinline__ void assemble_quad_col(
     pk[l] = l < L ? *reinterpret_cast<const uint32_t*>(res + (size_t)l * plane + e0) : 0u;
   float W1[4], W2[4];
   rad_folds(P, plane, e0, rc, W1, W2);
+  const float qb1 = rc.lowb ? lowpair_root(qj[0], 1.0f) : 0.0f;
+  const float qb2 = rc.lowb ? lowpair_root(qj[1], 1.0f) : 0.0f;
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
     const int i = i0 + u;
@@ -316,7 +336,8 @@ __device__ __forceinline__ void assemble_quad_col(
       const double t2 = scale_pow2(rw.sA[u], Ei + Fj - 2 * w - 1, true);
       tr = __dadd_ru(t1, t2);
     }
-    const double Tu = rad_T(W1[u], W2[u], rw.Ep[u], rw.Er[u], Fj, Frj, rc);
+    const double Tu = rad_T(W1[u], W2[u], rw.Ep[u], rw.Er[u], Fj, Frj, rc,
+                            __fmul_ru(rw.qp[u], qb1), __fmul_ru(rw.qr[u], qb2));
     const double err = __dadd_ru(tr, Tu);
     double clo = __dsub_rd(lo, err), cup = __dadd_ru(up, err);
     if (nonfinite) clo = cup = __longlong_as_double(0x7ff8000000000000LL);
@@ -333,6 +354,7 @@ __global__ void __launch_bounds__(256, 3)
 oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __restrict__ res,
                        size_t plane, const int* __restrict__ E3, const int* __restrict__ F2,
                        const unsigned long long* __restrict__ asum,
+                       const unsigned long long* __restrict__ bsum,
                        const double* __restrict__ beta, const int32_t* __restrict__ P,
                        double* __restrict__ C, long ldc, const int* __restrict__ flag,
                        const __grid_constant__ CrtConst cc, const __grid_constant__ OzRadConst rc) {
@@ -344,7 +366,7 @@ oz_crt_assemble_kernel(int M, int N, int Mp, int L, int w, const uint8_t* __rest
   quad_rows(4 * q, M, E3, asum, rw);
   for (int j = blockIdx.y; j < N; j += gridDim.y)
     assemble_quad_col(rw, 4 * q, j, M, Mp, L, w, res, plane, F2[2 * j], F2[2 * j + 1], beta[j],
-                      P, C, ldc, nonfinite, cc.Q, cc.M, cc.invMf, rc);
+                      bsum + 4 * (size_t)j + 2, P, C, ldc, nonfinite, cc.Q, cc.M, cc.invMf, rc);
 }
 
 // Grouped reassembly.  The problems of a bucket share one CRT plan (the
@@ -374,7 +396,8 @@ oz_crt_assemble_g(const __grid_constant__ OzGBucket b, const __grid_constant__ C
     const bool nonfinite = f0 != 0 || b.flag[1] != 0;
     const int qd = (int)(u % Mq), cg = (int)(u / Mq);
     const int* E3 = b.E3 + 3 * (size_t)q.rowoff;
-    const unsigned long long* asum = b.asum + 2 * (size_t)q.rowoff;
+    const unsigned long long* asum = b.asum + 4 * (size_t)q.rowoff;
+    const unsigned long long* bsum = b.bsum + 4 * (size_t)q.coloff;
     const int* F2 = b.F2 + 2 * (size_t)q.coloff;
     const double* beta = b.beta + q.coloff;
     const uint8_t* res = b.res + q.res_off;
@@ -384,7 +407,8 @@ oz_crt_assemble_g(const __grid_constant__ OzGBucket b, const __grid_constant__ C
     quad_rows(4 * qd, m, E3, asum, rw);
     for (int j = cg; j < n; j += NG)
       assemble_quad_col(rw, 4 * qd, j, m, q.Mp, q.L, q.w, res, plane, F2[2 * j], F2[2 * j + 1],
-                        beta[j], P, q.C, q.ldc, nonfinite, cc.Q, cc.M, cc.invMf, rc);
+                        beta[j], bsum + 4 * (size_t)j + 2, P, q.C, q.ldc, nonfinite, cc.Q, cc.M,
+                        cc.invMf, rc);
   }
   if (threadIdx.x == 0 && (f0 | f1)) atomicOr(status, (f0 ? 1 : 0) | (f1 ? 2 : 0));
   if (b.t_last) {
@@ -428,7 +452,7 @@ int oz_crt_assemble(const OzPlan& plan, const OzWorkspace& ws, double* C, long l
   dim3 grid((Mq + 127) / 128, gy < 65535 ? gy : 65535);
   oz_crt_assemble_kernel<<<grid, 128, 0, st>>>(
       pb.M, pb.N, pb.Mp, pb.L, pb.w, ws.res, (size_t)pb.Np * pb.Mp, ws.E3, ws.F2, ws.asum,
-      ws.beta, ws.P, C, ldc, ws.flag, cc, oz_rad_const(plan));
+      ws.bsum, ws.beta, ws.P, C, ldc, ws.flag, cc, oz_rad_const(plan));
   VCPCU_LAUNCH_CHECK("oz_crt_assemble_kernel");
   return VCPCU_OK;
 }

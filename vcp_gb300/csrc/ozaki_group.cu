@@ -65,12 +65,13 @@ constexpr double OZ_GROUP_CHUNK_NS = 400000.0;
 
 // Estimated device time of one problem of a bucket (ns), from the rates the
 // grouped kernels reach on GB300: about 9 ns per k-block (64) of one work
-// item of the slice GEMM (L residue and 8 radius groups per tile), 25 ps per
+// item of the slice GEMM (L residue GEMMs and 2 x 3 radius digit pairs per
+// tile), 25 ps per
 // padded operand entry of the preparation, 27 ps per output entry of the
 // reassembly.  Used only to cut buckets into chunks of similar length.
 double group_cost_ns(const BatchProblemView& q, const OzPlan& pl) {
   const double tiles = (double)(pl.pb.Mp / OZ_BM) * (pl.pb.Np / OZ_BN);
-  return 9.0 * (pl.pb.L + 8) * tiles * (pl.pb.Kp / OZ_BK) +
+  return 9.0 * (pl.pb.L + 2 * pl.rad.npairs) * tiles * (pl.pb.Kp / OZ_BK) +
          0.025 * ((double)pl.pb.Mp + pl.pb.Np) * pl.pb.Kp + 0.027 * (double)q.m * q.n;
 }
 }  // namespace
@@ -79,15 +80,16 @@ int oz_group_plan(int count, const BatchProblemView* problems, const char* selec
                   int persistent, cudaStream_t s, OzGroupPlan** out) {
   *out = nullptr;
   const int nslices = slices > 0 ? slices : 8;
-  // bucket the selected problems by (Kp, L, w): the problems of a bucket
-  // share one CRT plan (moduli, basis, digit pairs, folds)
-  std::map<std::tuple<int, int, int>, std::vector<int>> byKey;
+  // bucket the selected problems by (Kp, L, w, radius pairs): the problems
+  // of a bucket share one CRT plan (moduli, basis, digit pairs, folds)
+  std::map<std::tuple<int, int, int, int>, std::vector<int>> byKey;
   std::vector<OzPlan> plans(count);
   for (int i = 0; i < count; ++i) {
     const BatchProblemView& q = problems[i];
     if ((select && !select[i]) || q.m <= 0 || q.n <= 0 || q.k <= 0) continue;
     oz_make_plan(q.m, q.n, q.k, nslices, 2, &plans[i], 1);
-    byKey[std::make_tuple(plans[i].pb.Kp, plans[i].pb.L, plans[i].pb.w)].push_back(i);
+    byKey[std::make_tuple(plans[i].pb.Kp, plans[i].pb.L, plans[i].pb.w, plans[i].rad.npairs)]
+        .push_back(i);
   }
   // A bucket runs its kernels one after another, so a problem's latency is
   // its bucket's length: each is cut into chunks of about OZ_GROUP_CHUNK_NS
@@ -261,7 +263,7 @@ int oz_group_plan(int count, const BatchProblemView* problems, const char* selec
       return off;
     };
     b.offRowmax = take(sizeof(unsigned long long) * 3 * Mtot);
-    b.offAsum = take(sizeof(unsigned long long) * 2 * Mtot);
+    b.offAsum = take(sizeof(unsigned long long) * 4 * Mtot);
     b.offFlag = take(sizeof(int) * 4 * (size_t)n);
     b.zero_bytes = w;
     b.offE3 = take(sizeof(int) * 3 * Mtot);
@@ -269,7 +271,7 @@ int oz_group_plan(int count, const BatchProblemView* problems, const char* selec
     b.offBeta = take(sizeof(double) * Ntot);
     b.offMidB = take(sizeof(double) * (size_t)Ntot * Kp);
     b.offRadB = take(sizeof(double) * (size_t)Ntot * Kp);
-    b.offBsum = take(sizeof(unsigned long long) * 2 * Ntot);
+    b.offBsum = take(sizeof(unsigned long long) * 4 * Ntot);
     b.offMidA = take(sizeof(double) * (size_t)Mtot * Kp);
     b.offRadA = take(sizeof(double) * (size_t)Mtot * Kp);
     b.offA = take(sizeof(uint16_t) * (size_t)(Lmax + 4) * Mtot * Kp);

@@ -13,6 +13,10 @@
 //                         rB  -> sr digits, upward, exponent Fr_j
 //                         S = |mB| -> sr digits, upward, exponent Fm_j
 //                         beta_j = sum_k |mB(k,j)| rounded upward
+// CRT form: the residues of the w-bit integers A', B' replace the midpoint
+// digits, and the sums of the squared low radius digits (P and rA per row,
+// rB and |mB| per column) bound the low x low radius pair left out of the
+// slice GEMM.
 // Digit planes are K-major bf16: plane[p][row][k], row < Mp (or Np), k < Kp;
 // the padding is zero.
 #include "common.cuh"
@@ -464,7 +468,8 @@ struct TileStore {
 };
 
 // Left factor, CRT form: residues of A' (L planes) + radius digits, and
-// sum_k |A'(i,k)| split as (|A'| >> 32, |A'| & 0xffffffff) sums.
+// sum_k |A'(i,k)| split as (|A'| >> 32, |A'| & 0xffffffff) sums; the sums
+// of the squared low digits of P and rA in asum[4 i + 2], asum[4 i + 3].
 // Block: 32 rows x 64 k; lane = row, warp q takes k0 + 8q .. k0 + 8q + 7, so
 // the loads of mA / rA are coalesced across the warp; each lane's 8 bf16
 // (16 bytes) per plane go out through shared memory (TileStore).
@@ -514,6 +519,7 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
   const bool pad = k0 >= K || by * 32 >= M;
   long long a[8];
   unsigned long long shi = 0, slo = 0;
+  uint32_t qp = 0, qr = 0;  // sums of the squared low radius digits (< 2^18 per lane)
   {
     // radius digit planes first, so that the doubles die before the residues
     uint32_t hp[SR][4] = {}, hr[SR][4] = {};
@@ -536,6 +542,8 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
         digits_of<SR>(p, Ep, 1, u ? d1 : d0);
         digits_of<SR>(r, Er, 1, u ? e1 : e0);
       }
+      qp += (uint32_t)(d0[SR - 1] * d0[SR - 1] + d1[SR - 1] * d1[SR - 1]);
+      qr += (uint32_t)(e0[SR - 1] * e0[SR - 1] + e1[SR - 1] * e1[SR - 1]);
 #pragma unroll
       for (int q = 0; q < SR; ++q) {
         hp[q][t / 2] = bf16_bits(d0[q]) | (bf16_bits(d1[q]) << 16);
@@ -559,14 +567,22 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
     limbs12<NL>(ua, a[t] < 0, hl[t]);
   }
   __shared__ unsigned long long red[2][32];
-  if (threadIdx.x < 32) red[0][lane] = red[1][lane] = 0;
+  __shared__ uint32_t redq[2][32];
+  if (threadIdx.x < 32) {
+    red[0][lane] = red[1][lane] = 0;
+    redq[0][lane] = redq[1][lane] = 0u;
+  }
   __syncthreads();
   atomicAdd(&red[0][lane], shi);
   atomicAdd(&red[1][lane], slo);
+  if (qp) atomicAdd(&redq[0][lane], qp);
+  if (qr) atomicAdd(&redq[1][lane], qr);
   __syncthreads();
   if (threadIdx.x < 32 && i < M) {
-    atomicAdd(&asum[2 * i + 0], red[0][lane]);
-    atomicAdd(&asum[2 * i + 1], red[1][lane]);
+    atomicAdd(&asum[4 * i + 0], red[0][lane]);
+    atomicAdd(&asum[4 * i + 1], red[1][lane]);
+    if (redq[0][lane]) atomicAdd(&asum[4 * i + 2], (unsigned long long)redq[0][lane]);
+    if (redq[1][lane]) atomicAdd(&asum[4 * i + 3], (unsigned long long)redq[1][lane]);
   }
 #pragma unroll
   for (int l = 0; l < OZ_MAX_MODULI_128; ++l) {
@@ -679,7 +695,7 @@ __global__ void __launch_bounds__(256, 3) oz_split_left_crt_g(const __grid_const
                              b.E3 + 3 * (size_t)q.rowoff, b.planesA,
                              b.planesA + (size_t)b.Lmax * pstride,
                              b.planesA + (size_t)(b.Lmax + 2) * pstride,
-                             b.asum + 2 * (size_t)q.rowoff, b.rowmax + 3 * (size_t)q.rowoff);
+                             b.asum + 4 * (size_t)q.rowoff, b.rowmax + 3 * (size_t)q.rowoff);
 }
 
 // Warp reductions of 64-bit maxima and sums.
@@ -749,8 +765,8 @@ __global__ void __launch_bounds__(256) oz_colmax_right_g(const __grid_constant__
   if (lane == 0) {
     b.F2[2 * jst + 0] = j < q.n ? oz_exponent(__longlong_as_double((long long)am)) : OZ_ZERO_EXP;
     b.F2[2 * jst + 1] = j < q.n ? oz_exponent(__longlong_as_double((long long)ar)) : OZ_ZERO_EXP;
-    b.bsum[2 * jst + 0] = 0;
-    b.bsum[2 * jst + 1] = 0;
+    b.bsum[4 * jst + 0] = b.bsum[4 * jst + 1] = 0;
+    b.bsum[4 * jst + 2] = b.bsum[4 * jst + 3] = 0;
   }
 }
 
@@ -774,6 +790,7 @@ __global__ void __launch_bounds__(256) oz_split_right2_g(const __grid_constant__
   uint16_t* planes_s = b.planesB + (size_t)(b.Lmax + 2) * pstride;
   constexpr int HW = KPL / 2;  // 32-bit words per lane and plane
   unsigned long long shi = 0, slo = 0;
+  uint32_t qr = 0, qs = 0;  // sums of the squared low digits of rB, |mB|
   if (k0 < Kp) {
     const size_t off = (size_t)jst * Kp + k0;
     if (j >= q.n || k0 >= K) {  // padding: zeros, nothing to compute
@@ -809,6 +826,8 @@ __global__ void __launch_bounds__(256) oz_split_right2_g(const __grid_constant__
           digits_of<2>(r, Fr, 1, u ? d1 : d0);
           digits_of<2>(oz_abs(m), Fm, 1, u ? e1 : e0);
         }
+        qr += (uint32_t)(d0[1] * d0[1] + d1[1] * d1[1]);
+        qs += (uint32_t)(e0[1] * e0[1] + e1[1] * e1[1]);
 #pragma unroll
         for (int qq = 0; qq < 2; ++qq) {
           hr[qq][t / 2] = bf16_bits(d0[qq]) | (bf16_bits(d1[qq]) << 16);
@@ -833,9 +852,15 @@ __global__ void __launch_bounds__(256) oz_split_right2_g(const __grid_constant__
   }
   shi = warp_sum_u64(shi);
   slo = warp_sum_u64(slo);
-  if (lane == 0 && (shi | slo)) {
-    atomicAdd(&b.bsum[2 * jst + 0], shi);
-    atomicAdd(&b.bsum[2 * jst + 1], slo);
+  qr = __reduce_add_sync(0xffffffffu, qr);
+  qs = __reduce_add_sync(0xffffffffu, qs);
+  if (lane == 0) {
+    if (shi | slo) {
+      atomicAdd(&b.bsum[4 * jst + 0], shi);
+      atomicAdd(&b.bsum[4 * jst + 1], slo);
+    }
+    if (qr) atomicAdd(&b.bsum[4 * jst + 2], (unsigned long long)qr);
+    if (qs) atomicAdd(&b.bsum[4 * jst + 3], (unsigned long long)qs);
   }
 }
 
@@ -847,8 +872,8 @@ __global__ void oz_beta_right_g(const __grid_constant__ OzGBucket b) {
   const int j = jst - q.coloff, Fm = b.F2[2 * jst];
   double bj = 0.0;
   if (j < q.n && Fm != OZ_ZERO_EXP) {
-    const double v = __fma_ru((double)b.bsum[2 * jst], 0x1p32,
-                              (double)(b.bsum[2 * jst + 1] + (unsigned long long)(q.k + 1) / 2));
+    const double v = __fma_ru((double)b.bsum[4 * jst], 0x1p32,
+                              (double)(b.bsum[4 * jst + 1] + (unsigned long long)(q.k + 1) / 2));
     bj = dev_scale_dir(v, Fm - q.w, true);
   }
   b.beta[jst] = bj;
@@ -969,8 +994,8 @@ oz_colmax_right(int K, int N, int Kp, int cols, int colbase, const double* __res
     const int jst = colbase + j;
     F2[2 * jst + 0] = j < N ? oz_exponent(__longlong_as_double((long long)am)) : OZ_ZERO_EXP;
     F2[2 * jst + 1] = j < N ? oz_exponent(__longlong_as_double((long long)ar)) : OZ_ZERO_EXP;
-    bsum[2 * jst + 0] = 0;
-    bsum[2 * jst + 1] = 0;
+    bsum[4 * jst + 0] = bsum[4 * jst + 1] = 0;
+    bsum[4 * jst + 2] = bsum[4 * jst + 3] = 0;
   }
 }
 
@@ -996,6 +1021,7 @@ oz_split_right_crt2(int K, int N, int Kp, int cols, int colbase, size_t pstride,
   const double* mcol = mB + (size_t)j * Kp;
   const double* rcol = rB + (size_t)j * Kp;
   unsigned long long shi = 0, slo = 0;
+  uint32_t qr = 0, qs = 0;  // sums of the squared low digits of rB, |mB|
   if (k0 < Kp) {
     const size_t off = (size_t)jst * Kp + k0;
     float hl[8][NL];
@@ -1019,6 +1045,8 @@ oz_split_right_crt2(int K, int N, int Kp, int cols, int colbase, size_t pstride,
         digits_of<SR>(r, Fr, 1, u ? d1 : d0);
         digits_of<SR>(oz_abs(m), Fm, 1, u ? e1 : e0);
       }
+      qr += (uint32_t)(d0[SR - 1] * d0[SR - 1] + d1[SR - 1] * d1[SR - 1]);
+      qs += (uint32_t)(e0[SR - 1] * e0[SR - 1] + e1[SR - 1] * e1[SR - 1]);
 #pragma unroll
       for (int q = 0; q < SR; ++q) {
         hr[q][t / 2] = bf16_bits(d0[q]) | (bf16_bits(d1[q]) << 16);
@@ -1044,9 +1072,15 @@ oz_split_right_crt2(int K, int N, int Kp, int cols, int colbase, size_t pstride,
   }
   shi = warp_sum_u64(shi);
   slo = warp_sum_u64(slo);
-  if (lane == 0 && (shi | slo)) {
-    atomicAdd(&bsum[2 * jst + 0], shi);
-    atomicAdd(&bsum[2 * jst + 1], slo);
+  qr = __reduce_add_sync(0xffffffffu, qr);
+  qs = __reduce_add_sync(0xffffffffu, qs);
+  if (lane == 0) {
+    if (shi | slo) {
+      atomicAdd(&bsum[4 * jst + 0], shi);
+      atomicAdd(&bsum[4 * jst + 1], slo);
+    }
+    if (qr) atomicAdd(&bsum[4 * jst + 2], (unsigned long long)qr);
+    if (qs) atomicAdd(&bsum[4 * jst + 3], (unsigned long long)qs);
   }
 }
 
@@ -1060,8 +1094,8 @@ __global__ void oz_beta_right(int K, int N, int cols, int colbase, int w,
   const int jst = colbase + j, Fm = F2[2 * jst];
   double bj = 0.0;
   if (j < N && Fm != OZ_ZERO_EXP) {
-    const double v = __fma_ru((double)bsum[2 * jst], 0x1p32,
-                              (double)(bsum[2 * jst + 1] + (unsigned long long)(K + 1) / 2));
+    const double v = __fma_ru((double)bsum[4 * jst], 0x1p32,
+                              (double)(bsum[4 * jst + 1] + (unsigned long long)(K + 1) / 2));
     bj = dev_scale_dir(v, Fm - w, true);
   }
   beta[jst] = bj;
@@ -1072,7 +1106,7 @@ int oz_prepare_left_begin(const OzProblem& pb, OzWorkspace& ws, cudaStream_t st)
   VCPCU_CUDA_TRY(cudaMemsetAsync(ws.delta, 0, sizeof(unsigned long long) * (size_t)pb.Mp, st));
   VCPCU_CUDA_TRY(cudaMemsetAsync(ws.flag, 0, 4 * sizeof(int), st));  // every status word
   if (pb.crt)
-    VCPCU_CUDA_TRY(cudaMemsetAsync(ws.asum, 0, sizeof(unsigned long long) * 2 * (size_t)pb.Mp, st));
+    VCPCU_CUDA_TRY(cudaMemsetAsync(ws.asum, 0, sizeof(unsigned long long) * 4 * (size_t)pb.Mp, st));
   return VCPCU_OK;
 }
 
@@ -1105,7 +1139,7 @@ int split_left_rows(const OzProblem& pb, int i0, int rows, OzWorkspace& ws, cuda
   const double* mA = ws.midA + i0;
   const double* rA = ws.radA + i0;
   int* E3 = ws.E3 + 3 * (size_t)i0;
-  unsigned long long* asum = ws.asum + 2 * (size_t)i0;
+  unsigned long long* asum = ws.asum + 4 * (size_t)i0;
   // |A'| <= 2^(w-1): four 14-bit limbs up to w = 56, five 12-bit limbs up to
   // w = 61, six up to 73
   if (pb.w <= 56)

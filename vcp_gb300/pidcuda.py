@@ -23,6 +23,9 @@ FORM_PLAIN = 0
 FORM_OZAKI = 1
 FORM_AUTO = 2
 FORM_OZAKI_SLICES = 3
+# added to `slices` of FORM_OZAKI: radius products without their low x low
+# digit pair, bounded instead (VCPCU_SLICES_FAST_RADIUS)
+SLICES_FAST_RADIUS = 0x100
 
 
 def to_kv(lo: np.ndarray, up: np.ndarray) -> np.ndarray:
@@ -230,7 +233,8 @@ def autotune_choice(m: int, n: int, k: int, batched: bool = False) -> int:
 def autotune_pick(A, B, m: int, n: int, k: int, stream=None) -> tuple[int, int]:
     """(form, slices) that FORM_AUTO uses for [A] [B] (kv buffers: numpy
     host arrays or float64 CUDA tensors): the tensor-core slice count whose
-    enclosures are no wider than the plain form's on a probe, or FORM_PLAIN."""
+    enclosures are no wider than the plain form's on a probe (possibly with
+    SLICES_FAST_RADIUS added), or FORM_PLAIN."""
     import ctypes
     f, s = ctypes.c_int(0), ctypes.c_int(0)
     if isinstance(A, np.ndarray):
