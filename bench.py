@@ -530,8 +530,8 @@ def measure_fp64_peak(dev):
 # n = 8192 product at 8 slices with the fast radius products (2 x 3 radius
 # digit pairs and 16 residue GEMMs in one launch), from a one-pass ncu
 # capture of dram__bytes_read.sum and dram__bytes_write.sum on a GB300
-# (21.98 + 2.05 GB).
-GEMM_TRAFFIC_N8192 = 24.04e9
+# (21.30 + 2.06 GB).
+GEMM_TRAFFIC_N8192 = 23.36e9
 
 
 def ozaki_roofline(phases, tc_flops, steps, pk, pk_kind, n=8192, fast8=True):
