@@ -74,7 +74,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=8192)
+    # --size is the spelling to use under torchrun, whose own parser reads
+    # "--n" as an ambiguous abbreviation of its options
+    ap.add_argument("--n", "--size", dest="n", type=int, default=8192)
     ap.add_argument("--form", default="auto", choices=["auto", "plain", "ozaki"])
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--plain-steps", type=int, default=2)
