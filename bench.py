@@ -71,7 +71,7 @@ WORKLOAD = "interval GEMM n=8192, mid E(phi=4), rad 2^-40|mid|"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     # --size is the spelling to use under torchrun, whose own parser reads

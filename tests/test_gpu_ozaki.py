@@ -62,10 +62,12 @@ def test_ozaki_bitexact_model_and_encloses(cuda_lib, oracle, case, crt):
     check_contains(oracle, m, n, k, A, B, C)
 
 
-def test_ozaki_extreme_digits(cuda_lib, oracle):
+@pytest.mark.parametrize("k", [3000, 8192])
+def test_ozaki_extreme_digits(cuda_lib, oracle, k):
     """All midpoints equal in magnitude: every top digit is +-128 and every
-    1024-chunk of digit products sums to +-2^24, the exactness limit."""
-    m, n, k = 130, 260, 3000
+    1024-chunk of digit products sums to +-2^24, the exactness limit -- at
+    k = 8192 (the bench's inner dimension) eight full chunks per entry."""
+    m, n = 130, 260
     A = np.empty(2 * m * k); B = np.empty(2 * k * n)
     A[0::2] = A[1::2] = 1.0
     B[0::2] = B[1::2] = 1.0
