@@ -411,11 +411,11 @@ int vcpcu_ddgemm(int m, int n, int k, const double* A, const double* B,
 
 /* The Ozaki-form interval product (same kernels and same results as
  * vcpcu_igemm_dev with form VCPCU_FORM_OZAKI and the same `slices`) for
- * callers that must not allocate device memory: code running inside a
- * stream capture that forbids memory nodes, a real-time loop that must not
- * reach cudaMalloc (it can synchronise the device), a process whose device
- * memory belongs to another allocator, or an FFI caller that promises no
- * allocation after start-up.  No counterpart in the reference (the
+ * callers that must not allocate device memory: a real-time loop that must
+ * not reach cudaMalloc (it can synchronise the device), a process whose
+ * device memory belongs to another allocator (whose budget an allocation
+ * here would overrun), or an FFI caller that promises no allocation after
+ * start-up.  No counterpart in the reference (the
  * reference is CPU code and allocates with std::vector).
  *
  * Scratch is one static 32 MiB (VCPCU_NOALLOC_SCRATCH_BYTES) device array

@@ -1,8 +1,8 @@
 """GPU test of vcpcu_igemm_noalloc_dev, the interval product for callers that
-cannot allocate device memory (stream captures that forbid memory nodes,
-real-time loops that must not reach cudaMalloc, processes whose device
-memory belongs to another allocator, FFI callers that promise no
-allocation after start-up).
+cannot allocate device memory (real-time loops that must not reach
+cudaMalloc, which can synchronise the device; processes whose device memory
+belongs to another allocator; FFI callers that promise no allocation after
+start-up).
 
 It is called through the C ABI and compared with vcpcu_igemm_dev (Ozaki
 form, same slice count): the two run the same kernels, so the results must
@@ -89,3 +89,67 @@ def test_noalloc_reports_nonfinite_input_like_the_allocating_entry_point(cuda_li
     torch.cuda.synchronize()
     _lib.call("vcpcu_status", s)
     assert not torch.isnan(dC).any().item()
+
+
+# CUmemPool_attribute value of the driver API: the high-water mark of the
+# pool's memory in use since its last reset
+_CU_MEMPOOL_ATTR_USED_MEM_HIGH = 8
+
+
+class _DefaultPool:
+    """The current device's default stream-ordered pool (where
+    cudaMallocAsync takes memory), read through the driver API."""
+
+    def __init__(self):
+        import torch
+        self.cu = ctypes.CDLL("libcuda.so.1")
+        for fn in ("cuDeviceGet", "cuDeviceGetDefaultMemPool", "cuMemPoolSetAttribute",
+                   "cuMemPoolGetAttribute"):
+            getattr(self.cu, fn).restype = ctypes.c_int
+        dev = ctypes.c_int(-1)
+        assert self.cu.cuDeviceGet(ctypes.byref(dev), torch.cuda.current_device()) == 0
+        self.pool = ctypes.c_void_p()
+        assert self.cu.cuDeviceGetDefaultMemPool(ctypes.byref(self.pool), dev) == 0
+
+    def reset_high(self):
+        zero = ctypes.c_uint64(0)
+        assert self.cu.cuMemPoolSetAttribute(self.pool, _CU_MEMPOOL_ATTR_USED_MEM_HIGH,
+                                             ctypes.byref(zero)) == 0
+
+    def high(self) -> int:
+        v = ctypes.c_uint64(0)
+        assert self.cu.cuMemPoolGetAttribute(self.pool, _CU_MEMPOOL_ATTR_USED_MEM_HIGH,
+                                             ctypes.byref(v)) == 0
+        return v.value
+
+
+def test_noalloc_takes_no_memory_from_the_stream_ordered_pool(cuda_lib):
+    """The allocating entry point takes its scratch from the device's
+    stream-ordered pool; the no-allocation one must not: the pool's
+    high-water mark of memory in use stays where it was across a call, while
+    the same product through vcpcu_igemm_dev raises it."""
+    import torch
+    from vcp_gb300 import _lib, pidcuda
+    rng = np.random.default_rng(4)
+    m, n, k = 200, 180, 700
+    A = torch.from_numpy(W.interval_ephi(rng, m, k, 4, 2.0 ** -40)).cuda()
+    B = torch.from_numpy(W.interval_ephi(rng, k, n, 4, 2.0 ** -40)).cuda()
+    C = torch.empty(2 * m * n, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+
+    def noalloc():
+        _lib.call("vcpcu_igemm_noalloc_dev", m, n, k, A.data_ptr(), m, B.data_ptr(), k,
+                  C.data_ptr(), m, 8, s)
+        torch.cuda.synchronize()
+        _lib.call("vcpcu_status", s)
+
+    noalloc()  # the first call on the device looks up the scratch address
+    pool = _DefaultPool()
+    pool.reset_high()
+    base = pool.high()
+    noalloc()
+    noalloc()
+    assert pool.high() == base, "the no-allocation entry point took pool memory"
+    pidcuda.mulmm_dev(m, n, k, A, m, B, k, C, m, pidcuda.FORM_OZAKI, 8)
+    torch.cuda.synchronize()
+    assert pool.high() > base, "the pool check does not see the allocating entry point"

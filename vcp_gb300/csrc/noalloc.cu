@@ -2,12 +2,11 @@
 // allocate device memory.
 //
 // Who needs it: code that runs where cudaMalloc / cudaMallocAsync are not
-// allowed or not safe -- a host thread inside a CUDA stream capture of a
-// framework that forbids memory nodes, a real-time loop that must not hit
-// the allocator (cudaMalloc can synchronise the device), a process whose
-// device memory is already owned by another allocator (a framework's
-// caching pool), or an FFI caller whose contract is "no allocation after
-// initialisation".  This entry point runs the same kernels as
+// allowed or not safe -- a real-time loop that must not hit the allocator
+// (cudaMalloc can synchronise the device and its latency is unbounded), a
+// process whose device memory is already owned by another allocator (a
+// framework's caching pool, which would see its budget overrun), or an FFI
+// caller whose contract is "no allocation after initialisation".  This entry point runs the same kernels as
 // vcpcu_igemm_dev with form VCPCU_FORM_OZAKI, but takes its scratch from one
 // file-scope static device array instead of the stream-ordered allocator.
 //

@@ -391,27 +391,63 @@ __device__ __forceinline__ void limbs12(unsigned __int128 a, bool neg, float (&h
   }
 }
 
-// round to the nearest integer, |v| < 2^22
-__device__ __forceinline__ float rint_small(float v) {
-  return __fsub_rn(__fadd_rn(v, 12582912.0f), 12582912.0f);
-}
-
-// Residue r of the integer given by its signed limbs, |r| <= 128 (see
-// above); all on the FP32 pipe.
-template <int NL>
-__device__ __forceinline__ float res_sym(const float (&h)[NL], int l) {
-  const float m = c_modf[l], inv = c_invf[l];
-  float x = h[0];
-#pragma unroll
-  for (int t = 1; t < NL; ++t)
-    x = __fmaf_rn(h[t], NL == 4 ? c_limbf14[l][t] : (NL == 8 ? c_limbf13[l][t] : c_limbf[l][t]), x);
-  return __fmaf_rn(-rint_small(__fmul_rn(x, inv)), m, x);
-}
-
 // bf16 patterns of two small integers (exact: at most 8 significant bits) in
 // one word, the first in the low half.
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   return __byte_perm(__float_as_uint(a), __float_as_uint(b), 0x7632);
+}
+
+// Paired FP32 arithmetic (sm_100 and later): two floats in one 64-bit
+// register pair, the first in the low half; each instruction rounds each
+// half to nearest exactly as the scalar instruction does, so a pair gives
+// the bits of two scalar evaluations in half the issue slots.
+__device__ __forceinline__ unsigned long long f32x2(float lo, float hi) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ unsigned long long fma_x2(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ unsigned long long mul_x2(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ unsigned long long add_x2(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ unsigned long long sub_x2(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// The residues r, |r| <= 128 (see above), of two integers given by their
+// signed limbs h0, h1, modulo modulus l, as one word of two bf16 patterns
+// (h0's in the low half), all on the FP32 pipe and evaluated pairwise:
+// x = h_0 + sum_t h_t c_t by an FMA chain, q = rint(RN(x RN(1/m))) by the
+// add and subtract of 1.5 2^23 (round to nearest for |v| < 2^22), and
+// r = RN(q (-m) + x), the exact value fma(-q, m, x) would round.
+template <int NL>
+__device__ __forceinline__ uint32_t res_pair(const float (&h0)[NL], const float (&h1)[NL],
+                                             int l) {
+  const float m = c_modf[l], inv = c_invf[l];
+  const unsigned long long magic = f32x2(12582912.0f, 12582912.0f);
+  unsigned long long x = f32x2(h0[0], h1[0]);
+#pragma unroll
+  for (int t = 1; t < NL; ++t) {
+    const float c = NL == 4 ? c_limbf14[l][t] : (NL == 8 ? c_limbf13[l][t] : c_limbf[l][t]);
+    x = fma_x2(f32x2(h0[t], h1[t]), f32x2(c, c), x);
+  }
+  const unsigned long long q = sub_x2(add_x2(mul_x2(x, f32x2(inv, inv)), magic), magic);
+  const unsigned long long r = fma_x2(q, f32x2(-m, -m), x);
+  return __byte_perm((uint32_t)r, (uint32_t)(r >> 32), 0x7632);
 }
 
 // x * 2^e rounded up (up) or down, in steps that stay in the double range.
@@ -591,7 +627,7 @@ __device__ __forceinline__ void split_left_crt_body(int bx, int by, int M, int K
     if (!pad) {
 #pragma unroll
       for (int t = 0; t < 8; t += 2)
-        h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
+        h[t / 2] = res_pair<NL>(hl[t], hl[t + 1], l);
     }
     ts.put(make_uint4(h[0], h[1], h[2], h[3]), planes_m + l * pstride + tile0, Kp);
   }
@@ -845,7 +881,7 @@ __global__ void __launch_bounds__(256) oz_split_right2_g(const __grid_constant__
         uint32_t h[HW];
 #pragma unroll
         for (int t = 0; t < KPL; t += 2)
-          h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
+          h[t / 2] = res_pair<NL>(hl[t], hl[t + 1], l);
         store_bf16s<KPL>(planes_m + l * pstride + off, h);
       }
     }
@@ -1066,7 +1102,7 @@ oz_split_right_crt2(int K, int N, int Kp, int cols, int colbase, size_t pstride,
       uint32_t h[4];
 #pragma unroll
       for (int t = 0; t < 8; t += 2)
-        h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
+        h[t / 2] = res_pair<NL>(hl[t], hl[t + 1], l);
       *reinterpret_cast<uint4*>(planes_m + l * pstride + off) = make_uint4(h[0], h[1], h[2], h[3]);
     }
   }
@@ -1326,7 +1362,7 @@ dd_split_left(int M, int K, int Mp, int Kp, const double* __restrict__ A, long l
     uint32_t h[4];
 #pragma unroll
     for (int t = 0; t < 8; t += 2)
-      h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
+      h[t / 2] = res_pair<NL>(hl[t], hl[t + 1], l);
     ts.put(make_uint4(h[0], h[1], h[2], h[3]), planes + l * pstride + tile0, Kp);
   }
 }
@@ -1395,7 +1431,7 @@ dd_split_right(int K, int N, int Kp, int Np, const double* __restrict__ B, long 
     uint32_t h[4];
 #pragma unroll
     for (int t = 0; t < 8; t += 2)
-      h[t / 2] = pack_bf16x2(res_sym<NL>(hl[t], l), res_sym<NL>(hl[t + 1], l));
+      h[t / 2] = res_pair<NL>(hl[t], hl[t + 1], l);
     *reinterpret_cast<uint4*>(planes + l * pstride + off) = make_uint4(h[0], h[1], h[2], h[3]);
   }
 }
