@@ -461,7 +461,12 @@ def run_ours(args, ws, rank, local):
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = cpu_count()
-        rows_s = args.cpu_rows or 128
+        rows_s = args.cpu_rows
+        if not rows_s:
+            # about 10 s of CPU work: a 128-row probe panel, then a panel of
+            # whole 128-row blocks scaled to it
+            _, dt0 = cpu_baseline(A, B, n, 128, threads)
+            rows_s = int(min(n, max(128.0, 128.0 * 10.0 / max(dt0, 1e-3))) // 128 * 128)
         v, dt = cpu_baseline(A, B, n, rows_s, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{rows_s} x {n} x {n} row panel ({dt:.1f} s), oracle restatement of "
