@@ -83,3 +83,11 @@ def test_reference_arm_under_torchrun_prints_one_line_from_rank0():
     assert rec["impl"] == "reference" and rec["n_gpus"] == 2 and rec["steps"] == 1
     assert rec["value"] > 0 and rec["e2e"]["value"] == rec["value"]
     assert rec["cpu_baseline"]["kind"] == "port"
+    # the keys of the one-line contract both arms print
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config"):
+        assert key in rec, key
+    assert rec["higher_is_better"] is True and rec["scaling"] == "weak"
+    assert rec["e2e"]["h2d_bytes_per_step"] == 0 and rec["e2e"]["d2h_bytes_per_step"] == 0
+    assert rec["config"]["workload"] and rec["config"]["n"] == 128
+    assert rec["cpu_baseline"]["cores"] >= 1 and rec["cpu_baseline"]["value"] == rec["value"]
