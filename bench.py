@@ -350,11 +350,13 @@ def run_ours(args, ws, rank, local):
         e1 = torch.cuda.Event(enable_timing=True)
         l0 = _lib.launch_count()
         gc.disable()  # no collector pause while the steps are enqueued
-        e0.record(stream)
-        for _ in range(steps):
-            one(f)
-        e1.record(stream)
-        gc.enable()
+        try:
+            e0.record(stream)
+            for _ in range(steps):
+                one(f)
+            e1.record(stream)
+        finally:
+            gc.enable()
         stream.synchronize()
         l1 = _lib.launch_count()
         torch.cuda.synchronize()
@@ -397,13 +399,15 @@ def run_ours(args, ws, rank, local):
     barrier(ws)
     with ClockSampler(local) as clk_e2e:
         gc.disable()  # no collector pause inside the timed calls (as timeit does)
-        t0 = time.perf_counter()
-        e2e_marks = [t0]
-        for _ in range(e2e_steps):
-            _lib.call("vcpcu_igemm", n, n, n, pa, pb, pc, form, slices)
-            e2e_marks.append(time.perf_counter())  # the call returns synchronised
-        t_e2e = (time.perf_counter() - t0) / e2e_steps
-        gc.enable()
+        try:
+            t0 = time.perf_counter()
+            e2e_marks = [t0]
+            for _ in range(e2e_steps):
+                _lib.call("vcpcu_igemm", n, n, n, pa, pb, pc, form, slices)
+                e2e_marks.append(time.perf_counter())  # the call returns synchronised
+            t_e2e = (time.perf_counter() - t0) / e2e_steps
+        finally:
+            gc.enable()
     e2e_step_ms = [1e3 * (b - a) for a, b in zip(e2e_marks, e2e_marks[1:])]
     t_e2e = max_over_ranks(t_e2e, ws, dev)
     e2e_val = ws * 2.0 * n ** 3 / t_e2e / 1e12
