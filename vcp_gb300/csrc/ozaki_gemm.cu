@@ -172,17 +172,11 @@ __device__ __forceinline__ ItemInfo item_info(const OzGemmArgs& a, int item, int
 // Residue of a one-chunk CRT group on the FP32 pipe (no float-to-int
 // conversion, which GB300 issues on its narrow XU pipe, and no integer
 // reduction).  The chunk value x is an exact integer with |x| <= 2^24, so
-// |RN(x RN(1/m)) - x/m| <= (2^24/m) 2^-23 (1 + 2^-25) and q = rint of it is
-// within 1/2 + 2.0000002/m of x/m: r = x - q m (one FMA, exact) is an
-// integer with |r| <= m/2 + 2, and adding m to a negative r gives [0, m)
-// (m >= 107).
-__device__ __forceinline__ float rint_f(float x) {  // |x| < 2^22
-  return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
-}
-__device__ __forceinline__ float fold_residue(float x, float m, float inv) {
-  const float r = __fmaf_rn(-rint_f(__fmul_rn(x, inv)), m, x);
-  return r < 0.0f ? r + m : r;
-}
+// |RN(x RN(1/m)) - x/m| <= (2^24/m) 2^-23 (1 + 2^-25) and q = rint of it
+// (the add and subtract of 1.5 2^23) is within 1/2 + 2.0000002/m of x/m:
+// r = RN(q (-m) + x) (one FMA, exact) is an integer with |r| <= m/2 + 2,
+// and adding m to a negative r gives [0, m) (m >= 107).  The epilogue
+// evaluates it for two columns per paired FP32 instruction.
 
 __device__ __forceinline__ long long shift_t(int c, int sh) {
   const long long v = (long long)c;
@@ -440,11 +434,25 @@ oz_slice_gemm_kernel(const __grid_constant__ OzGemmArgs args) {
             ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c8 * 64, r);
             ptx::tmem_ld_32x32(tmem + lane_addr + buf * OZ_BN + half * 128 + c8 * 64 + 32, r + 32);
             ptx::tmem_ld_wait();
-            // residue bytes: rr < 256 is the low byte of the bits of rr + 2^23
+            // residue bytes: the residue rr < 256 is the low byte of the bits
+            // of rr + 2^23.  Two columns per paired FP32 instruction: q and
+            // r = RN(q (-m) + x), then 2^23 + r and 2^23 + m + r (both exact
+            // integers below 2^24), the second kept where r < 0 (a float
+            // compare, so that r = -0 keeps the first)
+            const unsigned long long inv2 = f32x2(invf, invf), negm2 = f32x2(-mf, -mf),
+                                     rnd2 = f32x2(12582912.0f, 12582912.0f),
+                                     off2 = f32x2(8388608.0f, 8388608.0f),
+                                     offm2 = f32x2(8388608.0f + mf, 8388608.0f + mf);
 #pragma unroll
-            for (int e = 0; e < 64; ++e)
-              r[e] = __float_as_uint(
-                  __fadd_rn(fold_residue(__uint_as_float(r[e]), mf, invf), 8388608.0f));
+            for (int e = 0; e < 64; e += 2) {
+              const unsigned long long x = f32x2(__uint_as_float(r[e]), __uint_as_float(r[e + 1]));
+              const unsigned long long q = sub_x2(add_x2(mul_x2(x, inv2), rnd2), rnd2);
+              const unsigned long long rr = fma_x2(q, negm2, x);
+              const unsigned long long a = add_x2(rr, off2), b = add_x2(rr, offm2);
+              r[e] = __uint_as_float((uint32_t)rr) < 0.0f ? (uint32_t)b : (uint32_t)a;
+              r[e + 1] = __uint_as_float((uint32_t)(rr >> 32)) < 0.0f ? (uint32_t)(b >> 32)
+                                                                      : (uint32_t)(a >> 32);
+            }
             const int nc = ncol - c8 * 64;
             if (nc >= 64) {  // the common case: no per-column test
 #pragma unroll

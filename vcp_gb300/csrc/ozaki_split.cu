@@ -397,37 +397,6 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   return __byte_perm(__float_as_uint(a), __float_as_uint(b), 0x7632);
 }
 
-// Paired FP32 arithmetic (sm_100 and later): two floats in one 64-bit
-// register pair, the first in the low half; each instruction rounds each
-// half to nearest exactly as the scalar instruction does, so a pair gives
-// the bits of two scalar evaluations in half the issue slots.
-__device__ __forceinline__ unsigned long long f32x2(float lo, float hi) {
-  unsigned long long r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ unsigned long long fma_x2(unsigned long long a, unsigned long long b,
-                                                     unsigned long long c) {
-  unsigned long long d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-__device__ __forceinline__ unsigned long long mul_x2(unsigned long long a, unsigned long long b) {
-  unsigned long long d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ unsigned long long add_x2(unsigned long long a, unsigned long long b) {
-  unsigned long long d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ unsigned long long sub_x2(unsigned long long a, unsigned long long b) {
-  unsigned long long d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-
 // The residues r, |r| <= 128 (see above), of two integers given by their
 // signed limbs h0, h1, modulo modulus l, as one word of two bf16 patterns
 // (h0's in the low half), all on the FP32 pipe and evaluated pairwise:
